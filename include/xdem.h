@@ -1,0 +1,325 @@
+/*
+ * xdem.h -- C ABI of libxdem, the GB300 (sm_103a) DEM contact-step library.
+ *
+ * libxdem replaces the CUDA library of the xdynamics reference (the launchers
+ * in source/mphysics_cuda_def.cu declared by include/mphysics_cuda_dec.cuh).
+ * Every entry point below names the reference function it replaces.  The
+ * arguments keep the reference's meaning and order; three things are added:
+ *   - an explicit CUDA stream (`stream`, a cudaStream_t; 0 = legacy default
+ *     stream, which is what the reference uses);
+ *   - an int status return (XD_OK or an XD_ERR_* code) instead of `void` +
+ *     exit() (the reference's checkCudaErrors), with the first failure also
+ *     kept for xd_last_error();
+ *   - plain C types only: device pointers, sizes and the POD structs below,
+ *     whose byte layouts equal the reference's device structs.
+ *
+ * All pointer arguments of the compute calls are DEVICE pointers owned by the
+ * caller, in the reference's layouts: pos and triangle spheres are double4
+ * (x, y, z, r) rows; vel, acc, omega, alpha, force and moment are packed
+ * double3 rows (24-byte stride); mass and inertia are double.
+ *
+ * Calls on the same stream are ordered like the reference's default-stream
+ * launches.  The stateless calls share one library workspace (for the radix
+ * sort) and the parameter block set by xd_set_symbolic_parameter; like the
+ * reference they are meant for one host thread and one stream at a time.
+ * Independent scenes run concurrently through xd_scene_* handles, which own
+ * their parameters and workspace.
+ */
+#ifndef XDEM_H
+#define XDEM_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XDEM_VERSION "0.1.0"
+
+#ifdef __cplusplus
+#define XD_ALIGN16 alignas(16)
+#else
+#define XD_ALIGN16 _Alignas(16)
+#endif
+
+/* status codes */
+enum {
+    XD_OK = 0,
+    XD_ERR_INVALID = 1,      /* bad argument (null pointer, size, layout) */
+    XD_ERR_CUDA = 2,         /* a CUDA runtime call or launch failed */
+    XD_ERR_NOMEM = 3,        /* device allocation failed */
+    XD_ERR_CAPACITY = 4,     /* a fixed-capacity buffer would overflow */
+    XD_ERR_TIMEOUT = 5,      /* a bounded device-side wait ran out */
+    XD_ERR_STATE = 6         /* call out of order (e.g. no parameters set) */
+};
+
+/* device_parameters (mphysics_cuda_dec.cuh:17-30), 112 bytes */
+typedef struct xd_device_parameters {
+    bool rollingCondition;
+    unsigned int np;
+    unsigned int nsphere;
+    unsigned int ncell;
+    unsigned int grid_size[3];
+    double dt;
+    double half2dt;
+    double cell_size;
+    double cohesion;
+    double gravity[3];
+    double world_origin[3];
+} xd_device_parameters;
+
+/* device_contact_property (mphysics_cuda_dec.cuh:78-88), 88 bytes */
+typedef struct xd_contact_property {
+    double Ei, Ej, pri, prj, Gi, Gj, rest, fric, rfric, coh, sratio;
+} xd_contact_property;
+
+/* device_plane_info (mphysics_cuda_dec.cuh:43-55), 232 bytes */
+typedef struct xd_plane_info {
+    double l1, l2;
+    double u1[3], u2[3], uw[3], xw[3], pa[3], pb[3], w2[3], w3[3], w4[3];
+} xd_plane_info;
+
+/* device_polygon_info (mphysics_cuda_dec.cuh:32-41), 152 bytes */
+typedef struct xd_polygon_info {
+    int id;
+    double P[3], Q[3], R[3], V[3], W[3], N[3];
+} xd_polygon_info;
+
+/* device_polygon_mass_info (mphysics_cuda_dec.cuh:57-65), 160 bytes; ep is a
+ * CUDA double4 and therefore 16-byte aligned. */
+typedef struct xd_polygon_mass_info {
+    double origin[3];
+    XD_ALIGN16 double ep[4];
+    double vel[3], omega[3], force[3], moment[3];
+} xd_polygon_mass_info;
+
+/* ------------------------------------------------------------ library */
+
+const char* xd_version(void);
+const char* xd_status_string(int status);
+/* First failure since the last xd_clear_error(), with a message. */
+int xd_last_error(char* msg, size_t msg_len);
+void xd_clear_error(void);
+/* sizeof of each ABI struct, for binding-side layout checks. */
+size_t xd_sizeof(const char* struct_name);
+/* Free the shared workspace of the stateless calls. */
+int xd_release_workspace(void);
+
+/* setSymbolicParameter (mphysics_cuda_dec.cuh:110; mphysics_cuda_def.cu:13-16).
+ * Copies the host struct; later calls read it at launch time. */
+int xd_set_symbolic_parameter(const xd_device_parameters* h_params);
+
+/* ------------------------------------------------------------ integrator */
+
+/* vv_update_position (mphysics_cuda_dec.cuh:112; def.cu:33-41;
+ * kernel mphysics_cuda_impl.cuh:85-96): pos.xyz += dt*vel + half2dt*acc. */
+int xd_vv_update_position(double* pos, const double* vel, const double* acc, unsigned np,
+                          void* stream);
+
+/* vv_update_velocity (mphysics_cuda_dec.cuh:113; def.cu:43-56;
+ * kernel impl:98-134): a' = F/m, alpha' = M/I, v += dt/2 (a + a'),
+ * w += dt/2 (alpha + alpha'); then force = m*gravity, moment = 0. */
+int xd_vv_update_velocity(double* vel, double* acc, double* omega, double* alpha, double* force,
+                          double* moment, const double* mass, const double* inertia, unsigned np,
+                          void* stream);
+
+/* Fused step boundary: vv_update_velocity of step t followed by
+ * vv_update_position of step t+1 in one pass (same arithmetic, one read of
+ * the state instead of two).  No reference counterpart as a single call; it
+ * equals the reference's consecutive vv_update_velocity / vv_update_position
+ * (dem_simulation.cpp:467 then :454 of the next step). */
+int xd_vv_update_velocity_position(double* pos, double* vel, double* acc, double* omega,
+                                   double* alpha, double* force, double* moment,
+                                   const double* mass, const double* inertia, unsigned np,
+                                   void* stream);
+
+/* ------------------------------------------------------------ cell grid */
+
+/* cu_calculateHashAndIndex (mphysics_cuda_dec.cuh:115; def.cu:58-66;
+ * kernel impl:137-151). */
+int xd_calculate_hash_and_index(unsigned* hash, unsigned* index, const double* pos, unsigned np,
+                                void* stream);
+
+/* cu_calculateHashAndIndexForPolygonSphere (mphysics_cuda_dec.cuh:116-118;
+ * def.cu:68-77; kernel impl:153-164): entries sid .. sid+nsphere-1. */
+int xd_calculate_hash_and_index_polysphere(unsigned* hash, unsigned* index, unsigned sid,
+                                           unsigned nsphere, const double* sphere,
+                                           void* stream);
+
+/* cu_reorderDataAndFindCellStart (mphysics_cuda_dec.cuh:119; def.cu:80-108;
+ * kernel impl:166-212): stable sort of (hash, index) by hash in place,
+ * cstart = 0xffffffff / cend = 0 for every cell without entries, cstart/cend
+ * = [first, one past last) sorted position of each occupied cell, and
+ * sorted_index = index after the sort.  n = np + nsphere entries. */
+int xd_reorder_and_find_cell_start(unsigned* hash, unsigned* index, unsigned* cstart,
+                                   unsigned* cend, unsigned* sorted_index, unsigned n,
+                                   unsigned ncell, void* stream);
+
+/* Stable LSD radix sort of 32-bit (key, value) pairs by the low key_bits of
+ * the key (the sort inside cu_reorderDataAndFindCellStart, def.cu:92-94,
+ * where the reference calls thrust::sort_by_key).  In place. */
+int xd_radix_sort_pairs(unsigned* keys, unsigned* values, unsigned n, unsigned key_bits,
+                        void* stream);
+
+/* ------------------------------------------------------------ contacts */
+
+/* cu_calculate_p2p (mphysics_cuda_dec.cuh:121-126; def.cu:110-136;
+ * kernel impl:403-485), tcm = 1 (the DHS model the application runs;
+ * contact_particles_particles.cpp:135).  cp is a device pointer. */
+int xd_calculate_p2p(int tcm, const double* pos, const double* vel, const double* omega,
+                     double* force, double* moment, const double* mass,
+                     const unsigned* sorted_index, const unsigned* cstart, const unsigned* cend,
+                     const xd_contact_property* cp, unsigned np, void* stream);
+
+/* cu_plane_contact_force (mphysics_cuda_dec.cuh:129-133; def.cu:138-156;
+ * kernel impl:572-621).  plane and cp are device pointers. */
+int xd_plane_contact_force(int tcm, const xd_plane_info* plane, const double* pos,
+                           const double* vel, const double* omega, double* force, double* moment,
+                           const double* mass, unsigned np, const xd_contact_property* cp,
+                           void* stream);
+
+/* cu_cube_contact_force (mphysics_cuda_dec.cuh:135-139; def.cu:158-179):
+ * the six planes of a cube (device array of 6), applied in order. */
+int xd_cube_contact_force(int tcm, const xd_plane_info* planes6, const double* pos,
+                          const double* vel, const double* omega, double* force, double* moment,
+                          const double* mass, unsigned np, const xd_contact_property* cp,
+                          void* stream);
+
+/* Several planes in one pass, applied in array order with the same
+ * per-plane accumulation as nplanes consecutive cu_plane_contact_force calls
+ * (contactManager.cpp:167-174 iterates plane contacts in name order).
+ * planes and cps are device arrays of nplanes entries. */
+int xd_planes_contact_force(int tcm, const xd_plane_info* planes, const xd_contact_property* cps,
+                            unsigned nplanes, const double* pos, const double* vel,
+                            const double* omega, double* force, double* moment,
+                            const double* mass, unsigned np, void* stream);
+
+/* cu_particle_polygonObject_collision (mphysics_cuda_dec.cuh:142-147;
+ * def.cu:203-221; kernel impl:923-1021).  Grid entries k >= np are
+ * triangles k - np.  The reaction on each polygon body is added to
+ * dpmi[body].force / .moment by a deterministic reduction (the reference
+ * adds it with unsynchronised +=, impl:1010-1011). */
+int xd_particle_polygon_collision(int tcm, const xd_polygon_info* dpi, const double* dsph,
+                                  xd_polygon_mass_info* dpmi, const double* pos,
+                                  const double* vel, const double* omega, double* force,
+                                  double* moment, const double* mass, const unsigned* sidx,
+                                  const unsigned* cstart, const unsigned* cend,
+                                  const xd_contact_property* cp, unsigned np, unsigned nbodies,
+                                  void* stream);
+
+/* cu_updatePolygonObjectData (mphysics_cuda_dec.cuh:296-298; def.cu:469-475;
+ * kernel impl:1911-1956): move body-frame triangle vertices vList (9 doubles
+ * per triangle) by the body's origin and Euler parameters, write P, Q, R and
+ * the circumcentre into sphere.xyz. */
+int xd_update_polygon_object_data(const xd_polygon_mass_info* dpmi, const double* vList,
+                                  double* sphere, xd_polygon_info* dpi, unsigned ntriangle,
+                                  void* stream);
+
+/* reductionD3 (mphysics_cuda_dec.cuh:157; def.cu:223-242): sum of n double3
+ * rows, returned to the host in out[3] (deterministic order). */
+int xd_reduction_d3(const double* in, unsigned n, double out[3], void* stream);
+
+/* Contact pair list: for every particle i (ascending) the partners k with
+ * (r_i + r_k) - |x_k - x_i| > 0 found by the 27-cell search, in search order,
+ * written as (i, k) pairs.  counts[np] receives the per-particle counts;
+ * pairs must hold `cap` pairs.  *total gets the total pair count (may exceed
+ * cap, in which case XD_ERR_CAPACITY is returned).  Diagnostic call. */
+int xd_pair_list(const double* pos, const unsigned* sorted_index, const unsigned* cstart,
+                 const unsigned* cend, unsigned np, unsigned* counts, unsigned* pairs,
+                 unsigned long long cap, unsigned long long* total, void* stream);
+
+/* ------------------------------------------------------------ scenes
+ *
+ * A scene owns one DEM system on the device: its state arrays, grid work
+ * arrays, walls, triangle mesh and workspace, and advances whole steps in the
+ * reference's order (dem_simulation::oneStepAnalysis,
+ * dem_simulation.cpp:447-469; contactManager::deviceCollision,
+ * contactManager.cpp:156-185):
+ *   VV position -> hash (+ triangle spheres) -> sort / cell ranges ->
+ *   particle-particle -> planes in array order -> triangles -> VV velocity.
+ * Scenes hold no global state, so independent scenes may run on different
+ * streams at the same time.
+ */
+typedef struct xd_scene xd_scene;
+
+enum {
+    XD_MODE_FP64 = 0   /* the reference's FP64 arithmetic and loop order */
+};
+
+typedef struct xd_scene_desc {
+    xd_device_parameters params;             /* grid, dt, gravity, rolling; params.np = np */
+    unsigned np;                             /* particles */
+    int mode;                                /* XD_MODE_* */
+    xd_contact_property cp_pp;               /* particle-particle property */
+    unsigned nplanes;
+    const xd_plane_info* planes;             /* host array, contact-name order */
+    const xd_contact_property* cp_planes;    /* host array, one per plane */
+    unsigned ntri;                           /* triangles of all polygon bodies */
+    unsigned nbodies;                        /* polygon bodies */
+    const xd_polygon_info* poly;             /* host array [ntri] */
+    const double* sphere;                    /* host array [ntri][4] */
+    const double* vlist;                     /* host array [ntri][9] body-frame vertices */
+    const xd_polygon_mass_info* pmi;         /* host array [nbodies] */
+    const xd_contact_property* cp_poly;      /* host array [nbodies] */
+} xd_scene_desc;
+
+/* Allocates the scene's device memory.  No reference counterpart: the
+ * reference allocates these arrays in dem_simulation::allocationMemory
+ * (dem_simulation.cpp:174-199) and contact::cudaMemoryAlloc (contact.cpp:107-116). */
+int xd_scene_create(const xd_scene_desc* desc, xd_scene** out);
+int xd_scene_destroy(xd_scene* scene);
+
+/* Host <-> device state copies (reference layouts; any argument may be NULL
+ * to skip that array).  Synchronous with respect to `stream`. */
+int xd_scene_upload(xd_scene* scene, const double* pos, const double* vel, const double* acc,
+                    const double* omega, const double* alpha, const double* force,
+                    const double* moment, const double* mass, const double* inertia,
+                    void* stream);
+int xd_scene_download(xd_scene* scene, double* pos, double* vel, double* acc, double* omega,
+                      double* alpha, double* force, double* moment, void* stream);
+
+/* Device pointers of the scene's state, in the reference layouts (for
+ * zero-copy access); any output may be NULL. */
+int xd_scene_device_state(xd_scene* scene, double** pos, double** vel, double** acc,
+                          double** omega, double** alpha, double** force, double** moment,
+                          double** mass, double** inertia);
+/* Device pointers of the grid arrays after the last step's sort. */
+int xd_scene_device_grid(xd_scene* scene, unsigned** hash, unsigned** index, unsigned** sorted,
+                         unsigned** cstart, unsigned** cend);
+
+/* Host copies of the grid arrays after the last step's sort (any may be NULL):
+ * hash/index/sorted hold np + ntri entries, cstart/cend ncell. */
+int xd_scene_download_grid(xd_scene* scene, unsigned* hash, unsigned* index, unsigned* sorted,
+                           unsigned* cstart, unsigned* cend, void* stream);
+
+/* Replace the polygon bodies' motion (origin, Euler parameters, velocity,
+ * angular velocity) from a host array [nbodies]; the triangles are moved by
+ * cu_updatePolygonObjectData semantics before the next step's hashing.
+ * Reaction force/moment fields of the uploaded records are kept. */
+int xd_scene_set_bodies(xd_scene* scene, const xd_polygon_mass_info* pmi, void* stream);
+int xd_scene_get_bodies(xd_scene* scene, xd_polygon_mass_info* pmi, void* stream);
+
+/* Advance nsteps whole steps on `stream`.  Returns after enqueueing; a
+ * device-side error word is checked (with a synchronisation) only when
+ * `check` is non-zero. */
+int xd_scene_step(xd_scene* scene, unsigned nsteps, int check, void* stream);
+
+/* Per-phase timing with CUDA events recorded on the step's stream.  Phases:
+ * 0 VV update, 1 hash, 2 sort + cell ranges, 3 particle-particle,
+ * 4 planes, 5 triangles.  xd_scene_phase_times synchronises the events and
+ * returns the summed milliseconds and launch counts since timing was last
+ * enabled. */
+#define XD_SCENE_PHASES 6
+int xd_scene_set_timing(xd_scene* scene, int enable);
+int xd_scene_phase_times(xd_scene* scene, double* ms, unsigned long long* launches);
+
+/* Number of kernel launches one xd_scene_step of nsteps issues. */
+unsigned long long xd_scene_launches(xd_scene* scene, unsigned nsteps);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

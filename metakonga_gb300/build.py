@@ -1,0 +1,92 @@
+"""In-tree build of libxdem (sm_103a) and the reference-API shim libraries.
+
+    python -m metakonga_gb300.build          # or __graft_entry__.build()
+
+Outputs (git-ignored, rebuilt on every machine):
+    metakonga_gb300/libxdem.so            the CUDA library + C ABI (include/xdem.h)
+    metakonga_gb300/libxdem_mphysics.so   C++ shim with the exact functions of the
+                                          reference's include/mphysics_cuda_dec.cuh
+Objects go to metakonga_gb300/_build/.  Translation units are compiled in
+parallel with one -gencode (compute_103a/sm_103a).
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+INCLUDE = os.path.join(ROOT, "include")
+LIBXDEM = os.path.join(PKG, "libxdem.so")
+LIBSHIM = os.path.join(PKG, "libxdem_mphysics.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                      "-I", INCLUDE, "-I", CSRC, "--expt-relaxed-constexpr"]
+
+# FP64 translation units whose results must match the reference's arithmetic
+# are compiled without multiply-add contraction.
+NO_FMAD = {"xd_grid.cu", "xd_integrate.cu", "xd_contact64.cu"}
+
+CUDA_SOURCES = ["xd_capi.cu", "xd_sort.cu", "xd_grid.cu", "xd_integrate.cu", "xd_contact64.cu",
+                "xd_scene.cu"]
+
+
+def nvcc() -> str:
+    for c in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libxdem")
+
+
+def _compile(src: str) -> str:
+    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+    srcp = os.path.join(CSRC, src)
+    deps = [srcp] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
+    deps.append(os.path.join(INCLUDE, "xdem.h"))
+    if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
+        return obj
+    flags = list(NVCC_COMMON)
+    if src in NO_FMAD:
+        flags.append("--fmad=false")
+    cmd = [nvcc(), "-c", srcp, "-o", obj] + flags
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
+    return obj
+
+
+def _newer(out: str, inputs) -> bool:
+    return os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(i) for i in inputs)
+
+
+def build(verbose: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(_compile, CUDA_SOURCES))
+    if not _newer(LIBXDEM, objs):
+        cmd = [nvcc(), "-shared", "-o", LIBXDEM] + objs + ARCH + ["-Xcompiler", "-fPIC", "-lcudart_static", "-lrt", "-ldl", "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link of libxdem.so failed:\n{r.stdout}\n{r.stderr}")
+    shim_src = os.path.join(CSRC, "shim_mphysics.cpp")
+    shim_deps = [shim_src, LIBXDEM, os.path.join(INCLUDE, "mphysics_cuda_dec.cuh")]
+    if os.path.exists(shim_src) and not _newer(LIBSHIM, shim_deps):
+        cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", LIBSHIM, shim_src,
+               "-I", INCLUDE, "-I", cuda_inc, "-L", PKG, "-lxdem", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"build of libxdem_mphysics.so failed:\n{r.stdout}\n{r.stderr}")
+    if verbose:
+        print("built", LIBXDEM, file=sys.stderr)
+    return LIBXDEM
+
+
+if __name__ == "__main__":
+    build(verbose=True)

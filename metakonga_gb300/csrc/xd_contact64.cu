@@ -1,0 +1,734 @@
+// FP64 contact forces with the reference's semantics (the "plain" form):
+// particle-particle (calculate_p2p_kernel<1>, mphysics_cuda_impl.cuh:403-485),
+// particle-plane (plane_contact_force_kernel<1>, impl:572-621), particle-
+// triangle (particle_polygonObject_collision_kernel<1>, impl:923-1021), the
+// mesh update (impl:1911-1956), reductionD3 (def.cu:223-242) and a pair-list
+// diagnostic.
+//
+// Compiled with --fmad=false.  Differences from the reference's arithmetic,
+// all inside the stated FP64 tolerance:
+//   * pow(cdist, 1.5) is evaluated as cdist * sqrt(cdist) (both within a few
+//     ulp of the exact value; the FP64 pow is far more expensive on GB300);
+//   * the pair-independent parts of getConstant (Eeq, beta = pi / ln e,
+//     1 + beta^2, (4/3) Eeq) are computed once per thread from the contact
+//     property instead of once per pair -- same expressions, same bits.
+// Reference behaviour that is kept on purpose:
+//   * Ft and M live across the pairs of one particle and are only assigned
+//     when |e| != 0 (impl:390-400), so a pair with zero tangential slip adds
+//     the previous pair's Ft and M again;
+//   * planes and triangles are evaluated with ir = 0 in DHSModel, so they
+//     apply no moment to the particle (impl:613-615, 1000-1002);
+//   * corner contacts of a plane use u = (x - corner)/|x - corner|
+//     (impl:506-529) and the third edge test can never pass (impl:549).
+#include <cuda_runtime.h>
+
+#include "xd_grid.cuh"
+#include "xd_internal.cuh"
+
+namespace xd {
+
+struct Fc {
+    double kn, vn, ks, vs, mu;
+};
+
+struct PairConst {
+    double c43Eeq, one_b2, sratio, fric, coh, Ei, Ej, pri, prj;
+};
+
+__device__ __forceinline__ PairConst load_pair_const(const xd_contact_property* cp)
+{
+    PairConst c;
+    double Ei = __ldg(&cp->Ei), Ej = __ldg(&cp->Ej), pri = __ldg(&cp->pri), prj = __ldg(&cp->prj);
+    double Eeq = (Ei * Ej) / (Ei * (1 - prj * prj) + Ej * (1 - pri * pri));
+    double beta = (M_PI / log(__ldg(&cp->rest)));
+    c.c43Eeq = (4.0 / 3.0) * Eeq;
+    c.one_b2 = 1.0 + beta * beta;
+    c.sratio = __ldg(&cp->sratio);
+    c.fric = __ldg(&cp->fric);
+    c.coh = __ldg(&cp->coh);
+    c.Ei = Ei;
+    c.Ej = Ej;
+    c.pri = pri;
+    c.prj = prj;
+    return c;
+}
+
+// getConstant, TCM = 1 (impl:214-256)
+__device__ __forceinline__ Fc get_constant(const PairConst& pc, double ir, double jr, double im,
+                                           double jm)
+{
+    Fc c;
+    double Meq = jm != 0.0 ? (im * jm) / (im + jm) : im;
+    double Req = jr != 0.0 ? (ir * jr) / (ir + jr) : ir;
+    c.kn = pc.c43Eeq * sqrt(Req);
+    c.vn = sqrt((4.0 * Meq * c.kn) / pc.one_b2);
+    c.ks = c.kn * pc.sratio;
+    c.vs = c.vn * pc.sratio;
+    c.mu = pc.fric;
+    return c;
+}
+
+// cohesionForce (impl:259-279)
+__device__ __forceinline__ double cohesion_force(double ri, double rj, double Ei, double Ej,
+                                                 double pri, double prj, double coh, double Fn)
+{
+    double cf = 0.0;
+    if (coh != 0.0) {
+        double req = (ri * rj / (ri + rj));
+        double Eeq = ((1.0 - pri * pri) / Ei) + ((1.0 - prj * prj) / Ej);
+        double rcp = (3.0 * req * (-Fn)) / (4.0 * (1.0 / Eeq));
+        double rc = pow(rcp, 1.0 / 3.0);
+        double Ac = M_PI * rc * rc;
+        cf = coh * Ac;
+    }
+    return cf;
+}
+
+// DHSModel (impl:379-401); Ft and M are in/out (kept across pairs).
+__device__ __forceinline__ void dhs(const Fc& c, double ir, double jr, double Ei, double Ej,
+                                    double pri, double prj, double coh, double cdist, d3 dv,
+                                    d3 unit, double dt, d3& Ft, d3& Fn, d3& M)
+{
+    double fsn = -c.kn * (cdist * sqrt(cdist));
+    double fdn = c.vn * dot(dv, unit);
+    double fca = cohesion_force(ir, jr, Ei, Ej, pri, prj, coh, fsn);
+    Fn = (fsn + fca + fdn) * unit;
+    d3 e = dv - dot(dv, unit) * unit;
+    double mag_e = length(e);
+    if (mag_e != 0.0) {
+        d3 sh = e / mag_e;
+        double ds = mag_e * dt;
+        Ft = fmin(c.ks * ds + c.vs * (dot(dv, sh)), c.mu * length(Fn)) * sh;
+        M = cross(ir * unit, Ft);
+    }
+}
+
+// ------------------------------------------------------- particle-particle
+
+__global__ void __launch_bounds__(128) k_p2p(Params P, const double* __restrict__ pos,
+                                             const double* __restrict__ vel,
+                                             const double* __restrict__ omega,
+                                             double* __restrict__ force, double* __restrict__ moment,
+                                             const double* __restrict__ mass,
+                                             const unsigned* __restrict__ sorted,
+                                             const unsigned* __restrict__ cstart,
+                                             const unsigned* __restrict__ cend,
+                                             const xd_contact_property* __restrict__ cp, unsigned np)
+{
+    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= np) return;
+    const PairConst pc = load_pair_const(cp);
+    d4 ip = ld4(pos, id);
+    d3 ipos = xyz(ip);
+    d3 ivel = ld3(vel, id);
+    d3 iomega = ld3(omega, id);
+    int3 gp = grid_pos(P, ip.x, ip.y, ip.z);
+    double ir = ip.w;
+    double im = __ldg(mass + id);
+    d3 Ft = mk(0, 0, 0), Fn = mk(0, 0, 0), M = mk(0, 0, 0);
+    d3 sumF = mk(0, 0, 0), sumM = mk(0, 0, 0);
+    for (int z = -1; z <= 1; z++) {
+        for (int y = -1; y <= 1; y++) {
+            for (int x = -1; x <= 1; x++) {
+                unsigned h = grid_hash(P, gp.x + x, gp.y + y, gp.z + z);
+                unsigned st = __ldg(cstart + h);
+                if (st == 0xffffffffu) continue;
+                unsigned en = __ldg(cend + h);
+                for (unsigned j = st; j < en; j++) {
+                    unsigned k = __ldg(sorted + j);
+                    if (id == k || k >= np) continue;
+                    d4 jp = ld4(pos, k);
+                    double jr = jp.w;
+                    d3 rp = mk(jp.x - ipos.x, jp.y - ipos.y, jp.z - ipos.z);
+                    double dist = length(rp);
+                    double cdist = (ir + jr) - dist;
+                    if (cdist > 0) {
+                        d3 jvel = ld3(vel, k);
+                        d3 jomega = ld3(omega, k);
+                        double jm = __ldg(mass + k);
+                        d3 unit = rp / dist;
+                        d3 rv = P.rolling ? (jvel + cross(jomega, -jr * unit)) - (ivel + cross(iomega, ir * unit))
+                                          : (jvel - ivel);
+                        Fc c = get_constant(pc, ir, jr, im, jm);
+                        dhs(c, ir, jr, pc.Ei, pc.Ej, pc.pri, pc.prj, pc.coh, cdist, rv, unit, P.dt,
+                            Ft, Fn, M);
+                        sumF += Fn + Ft;
+                        sumM += M;
+                    }
+                }
+            }
+        }
+    }
+    double* f = force + 3 * (size_t)id;
+    double* m = moment + 3 * (size_t)id;
+    f[0] += sumF.x; f[1] += sumF.y; f[2] += sumF.z;
+    m[0] += sumM.x; m[1] += sumM.y; m[2] += sumM.z;
+}
+
+// ------------------------------------------------------------------ planes
+
+struct PlaneD {
+    double l1, l2;
+    d3 u1, u2, uw, xw, w2, w3, w4;
+};
+
+__device__ __forceinline__ PlaneD load_plane(const xd_plane_info* p)
+{
+    PlaneD q;
+    q.l1 = __ldg(&p->l1);
+    q.l2 = __ldg(&p->l2);
+    q.u1 = mk(__ldg(p->u1), __ldg(p->u1 + 1), __ldg(p->u1 + 2));
+    q.u2 = mk(__ldg(p->u2), __ldg(p->u2 + 1), __ldg(p->u2 + 2));
+    q.uw = mk(__ldg(p->uw), __ldg(p->uw + 1), __ldg(p->uw + 2));
+    q.xw = mk(__ldg(p->xw), __ldg(p->xw + 1), __ldg(p->xw + 2));
+    q.w2 = mk(__ldg(p->w2), __ldg(p->w2 + 1), __ldg(p->w2 + 2));
+    q.w3 = mk(__ldg(p->w3), __ldg(p->w3 + 1), __ldg(p->w3 + 2));
+    q.w4 = mk(__ldg(p->w4), __ldg(p->w4 + 1), __ldg(p->w4 + 2));
+    return q;
+}
+
+__device__ __forceinline__ int sgn(double L) { return L < 0 ? -1 : 1; }
+
+// particle_plane_contact_detection (impl:487-570); pow(x, 2.0) is x * x
+// (IEEE: the correctly rounded square).
+__device__ double plane_detection(const PlaneD& pe, d3 xp, d3 wp, d3& u, double r)
+{
+    double a_l1 = (wp.x - pe.l1) * (wp.x - pe.l1);
+    double b_l2 = (wp.y - pe.l2) * (wp.y - pe.l2);
+    double sqa = wp.x * wp.x;
+    double sqb = wp.y * wp.y;
+    double sqc = wp.z * wp.z;
+    double sqr = r * r;
+    if (fabs(wp.z) < r && (wp.x > 0 && wp.x < pe.l1) && (wp.y > 0 && wp.y < pe.l2)) {
+        d3 dp = xp - pe.xw;
+        d3 uu = pe.uw / length(pe.uw);
+        int pp = -sgn(dot(dp, pe.uw));
+        u = (double)pp * uu;
+        return r - fabs(dot(dp, u));
+    }
+    if (wp.x < 0 && wp.y < 0 && (sqa + sqb + sqc) < sqr) {
+        d3 X = xp - pe.xw; double h = length(X); u = X / h; return r - h;
+    } else if (wp.x > pe.l1 && wp.y < 0 && (a_l1 + sqb + sqc) < sqr) {
+        d3 X = xp - pe.w2; double h = length(X); u = X / h; return r - h;
+    } else if (wp.x > pe.l1 && wp.y > pe.l2 && (a_l1 + b_l2 + sqc) < sqr) {
+        d3 X = xp - pe.w3; double h = length(X); u = X / h; return r - h;
+    } else if (wp.x < 0 && wp.y > pe.l2 && (sqa + b_l2 + sqc) < sqr) {
+        d3 X = xp - pe.w4; double h = length(X); u = X / h; return r - h;
+    }
+    d3 X, wj;
+    if ((wp.x > 0 && wp.x < pe.l1) && wp.y < 0 && (sqb + sqc) < sqr) {
+        X = xp - pe.xw; wj = pe.w2 - pe.xw;
+    } else if ((wp.x > 0 && wp.x < pe.l1) && wp.y > pe.l2 && (b_l2 + sqc) < sqr) {
+        X = xp - pe.w4; wj = pe.w3 - pe.w4;
+    } else if ((wp.x > 0 && wp.y < pe.l2) && wp.x < 0 && (sqr + sqc) < sqr) {
+        X = xp - pe.xw; wj = pe.w4 - pe.xw;
+    } else if ((wp.x > 0 && wp.y < pe.l2) && wp.x > pe.l1 && (a_l1 + sqc) < sqr) {
+        X = xp - pe.w2; wj = pe.w3 - pe.w2;
+    } else {
+        return -1.0;
+    }
+    d3 us = wj / length(wj);
+    d3 hs = X - (dot(X, us)) * us;
+    double h = length(hs);
+    u = (-hs) / h;
+    return r - h;
+}
+
+// Planes applied in order; each adds Fn + Ft to the running force exactly
+// like one plane_contact_force_kernel launch per plane.  cp_stride = 0
+// shares one property (cube), 1 gives one per plane.
+__global__ void __launch_bounds__(128) k_planes(Params P, const xd_plane_info* __restrict__ planes,
+                                                const xd_contact_property* __restrict__ cps,
+                                                unsigned cp_stride, unsigned nplanes,
+                                                const double* __restrict__ pos,
+                                                const double* __restrict__ vel,
+                                                const double* __restrict__ omega,
+                                                double* __restrict__ force,
+                                                double* __restrict__ moment,
+                                                const double* __restrict__ mass, unsigned np)
+{
+    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= np) return;
+    double m = __ldg(mass + id);
+    d4 ip = ld4(pos, id);
+    d3 ipos3 = xyz(ip);
+    double r = ip.w;
+    d3 ivel = ld3(vel, id);
+    d3 iomega = ld3(omega, id);
+    d3 f = ld3rw(force, id);
+    d3 mo = ld3rw(moment, id);
+    for (unsigned w = 0; w < nplanes; ++w) {
+        PlaneD pe = load_plane(planes + w);
+        d3 Fn = mk(0, 0, 0), Ft = mk(0, 0, 0), M = mk(0, 0, 0);
+        d3 dp = ipos3 - pe.xw;
+        d3 unit = mk(0, 0, 0);
+        d3 wp = mk(dot(dp, pe.u1), dot(dp, pe.u2), dot(dp, pe.uw));
+        double cdist = plane_detection(pe, ipos3, wp, unit, r);
+        if (cdist > 0) {
+            const xd_contact_property* cp = cps + (size_t)w * cp_stride;
+            PairConst pc = load_pair_const(cp);
+            d3 dv = P.rolling ? -(ivel + cross(iomega, r * unit)) : -ivel;
+            Fc c = get_constant(pc, r, 0.0, m, 0.0);
+            dhs(c, 0, 0, 0, 0, 0, 0, pc.coh, cdist, dv, unit, P.dt, Ft, Fn, M);
+        }
+        f += Fn + Ft;
+        mo += M;
+    }
+    st3(force, id, f);
+    st3(moment, id, mo);
+}
+
+// ---------------------------------------------------------------- polygons
+
+// closestPtPointTriangle (impl:837-899)
+__device__ d3 closest_pt_triangle(d3 a, d3 b, d3 c, d3 p)
+{
+    d3 ab = b - a, ac = c - a, ap = p - a;
+    double d1 = dot(ab, ap), d2 = dot(ac, ap);
+    if (d1 <= 0.0 && d2 <= 0.0) return a;
+    d3 bp = p - b;
+    double d3_ = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3_ >= 0.0 && d4 <= d3_) return b;
+    double vc = d1 * d4 - d3_ * d2;
+    if (vc <= 0.0 && d1 >= 0.0 && d3_ <= 0.0) {
+        double v = d1 / (d1 - d3_);
+        return a + v * ab;
+    }
+    d3 cp = p - c;
+    double d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d6 >= 0.0 && d5 <= d6) return c;
+    double vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
+        double w = d2 / (d2 - d6);
+        return a + w * ac;
+    }
+    double va = d3_ * d6 - d5 * d4;
+    if (va <= 0.0 && (d4 - d3_) >= 0.0 && (d5 - d6) >= 0.0) {
+        double w = (d4 - d3_) / ((d4 - d3_) + (d5 - d6));
+        return b + w * (c - b);
+    }
+    double denom = 1.0 / (va + vb + vc);
+    double v = vb * denom;
+    double w = vc * denom;
+    return (a + v * ab) + w * ac;
+}
+
+__device__ __forceinline__ d3 ldp(const double* a) { return mk(__ldg(a), __ldg(a + 1), __ldg(a + 2)); }
+
+// Reaction on the polygon bodies: NB > 0 keeps per-thread sums for NB
+// bodies and reduces them per block in a fixed order (block partials are
+// summed by k_polygon_reaction_final); NB == 0 adds with atomics (used when
+// the caller does not say how many bodies there are).
+template <int NB>
+__global__ void __launch_bounds__(128) k_polygon(Params P, const xd_polygon_info* __restrict__ dpi,
+                                                 xd_polygon_mass_info* __restrict__ dpmi,
+                                                 const double* __restrict__ pos,
+                                                 const double* __restrict__ vel,
+                                                 const double* __restrict__ omega,
+                                                 double* __restrict__ force,
+                                                 double* __restrict__ moment,
+                                                 const double* __restrict__ mass,
+                                                 const unsigned* __restrict__ sorted,
+                                                 const unsigned* __restrict__ cstart,
+                                                 const unsigned* __restrict__ cend,
+                                                 const xd_contact_property* __restrict__ cp,
+                                                 double* __restrict__ partials)
+{
+    constexpr int NBR = NB > 0 ? NB : 1;
+    double react[NBR][6];
+#pragma unroll
+    for (int b = 0; b < NBR; ++b)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) react[b][q] = 0.0;
+
+    const unsigned cnp = P.np;
+    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id < cnp) {
+        double im = __ldg(mass + id);
+        d4 ip = ld4(pos, id);
+        d3 ipos = xyz(ip);
+        d3 ivel = ld3(vel, id);
+        d3 iomega = ld3(omega, id);
+        int3 gp = grid_pos(P, ip.x, ip.y, ip.z);
+        double ir = ip.w;
+        d3 M = mk(0, 0, 0), Fn = mk(0, 0, 0), Ft = mk(0, 0, 0);
+        d3 sum_force = mk(0, 0, 0), sum_moment = mk(0, 0, 0);
+        for (int z = -1; z <= 1; z++)
+            for (int y = -1; y <= 1; y++)
+                for (int x = -1; x <= 1; x++) {
+                    unsigned h = grid_hash(P, gp.x + x, gp.y + y, gp.z + z);
+                    unsigned st = __ldg(cstart + h);
+                    if (st == 0xffffffffu) continue;
+                    unsigned en = __ldg(cend + h);
+                    for (unsigned j = st; j < en; j++) {
+                        unsigned k = __ldg(sorted + j);
+                        if (k < cnp) continue;
+                        k -= cnp;
+                        const xd_polygon_info* tri = dpi + k;
+                        unsigned pidx = (unsigned)__ldg(&tri->id);
+                        const xd_polygon_mass_info* pmi = dpmi + pidx;
+                        d3 Pv = ldp(tri->P), Qv = ldp(tri->Q), Rv = ldp(tri->R);
+                        d3 cpt = closest_pt_triangle(Pv, Qv, Rv, ipos);
+                        d3 po2cp = cpt - ldv(pmi->origin);
+                        d3 distVec = ipos - cpt;
+                        double dist = length(distVec);
+                        double cdist = ir - dist;
+                        Fn = mk(0, 0, 0);
+                        if (cdist > 0) {
+                            d3 qp = Qv - Pv, rp = Rv - Pv;
+                            d3 unit = -cross(qp, rp);
+                            unit = unit / length(unit);
+                            d3 pvel = ldv(pmi->vel), pom = ldv(pmi->omega);
+                            d3 dv = P.rolling ? (pvel + cross(pom, po2cp)) - (ivel + cross(iomega, ir * unit))
+                                              : (pvel - ivel);
+                            PairConst pc = load_pair_const(cp + pidx);
+                            Fc c = get_constant(pc, ir, 0, im, 0);
+                            dhs(c, 0, 0, 0, 0, 0, 0, 0, cdist, dv, unit, P.dt, Ft, Fn, M);
+                            sum_force += Fn + Ft;
+                            sum_moment += M;
+                            d3 rf = -(Fn + Ft);
+                            d3 rm = -cross(po2cp, Fn + Ft);
+                            if (NB == 0) {
+                                atomicAdd(dpmi[pidx].force + 0, rf.x);
+                                atomicAdd(dpmi[pidx].force + 1, rf.y);
+                                atomicAdd(dpmi[pidx].force + 2, rf.z);
+                                atomicAdd(dpmi[pidx].moment + 0, rm.x);
+                                atomicAdd(dpmi[pidx].moment + 1, rm.y);
+                                atomicAdd(dpmi[pidx].moment + 2, rm.z);
+                            } else if (pidx >= (unsigned)NBR) {
+                                // body id beyond the declared count: no slot, add directly
+                                atomicAdd(dpmi[pidx].force + 0, rf.x);
+                                atomicAdd(dpmi[pidx].force + 1, rf.y);
+                                atomicAdd(dpmi[pidx].force + 2, rf.z);
+                                atomicAdd(dpmi[pidx].moment + 0, rm.x);
+                                atomicAdd(dpmi[pidx].moment + 1, rm.y);
+                                atomicAdd(dpmi[pidx].moment + 2, rm.z);
+                            } else {
+#pragma unroll
+                                for (int b = 0; b < NBR; ++b)
+                                    if ((unsigned)b == pidx) {
+                                        react[b][0] += rf.x; react[b][1] += rf.y; react[b][2] += rf.z;
+                                        react[b][3] += rm.x; react[b][4] += rm.y; react[b][5] += rm.z;
+                                    }
+                            }
+                        }
+                    }
+                }
+        double* f = force + 3 * (size_t)id;
+        double* m = moment + 3 * (size_t)id;
+        f[0] += sum_force.x; f[1] += sum_force.y; f[2] += sum_force.z;
+        m[0] += sum_moment.x; m[1] += sum_moment.y; m[2] += sum_moment.z;
+    }
+    if (NB > 0) {
+        // fixed-order block tree reduction of the per-thread reactions
+        __shared__ double red[128];
+        for (int b = 0; b < NBR; ++b)
+            for (int q = 0; q < 6; ++q) {
+                red[threadIdx.x] = react[b][q];
+                __syncthreads();
+                for (int o = 64; o > 0; o >>= 1) {
+                    if (threadIdx.x < (unsigned)o) red[threadIdx.x] += red[threadIdx.x + o];
+                    __syncthreads();
+                }
+                if (threadIdx.x == 0) partials[((size_t)blockIdx.x * NBR + b) * 6 + q] = red[0];
+                __syncthreads();
+            }
+    }
+}
+
+// Sums the block partials of each body in block order and adds the total to
+// dpmi[b].force / .moment.
+__global__ void k_polygon_reaction_final(const double* __restrict__ partials, unsigned nblocks,
+                                         unsigned nbodies, unsigned nbr,
+                                         xd_polygon_mass_info* __restrict__ dpmi)
+{
+    unsigned t = threadIdx.x;   // one thread per (body, component)
+    if (t >= nbodies * 6) return;
+    unsigned b = t / 6, q = t % 6;
+    double s = 0.0;
+    for (unsigned blk = 0; blk < nblocks; ++blk) s += partials[((size_t)blk * nbr + b) * 6 + q];
+    if (q < 3) dpmi[b].force[q] += s;
+    else dpmi[b].moment[q - 3] += s;
+}
+
+// ----------------------------------------------------------- mesh update
+
+// toGlobal(double3&, double4&) (impl:1898-1909)
+__device__ __forceinline__ d3 to_global(d3 v, double ex, double ey, double ez, double ew)
+{
+    d3 r0 = mk(2.0 * (ex * ex + ey * ey - 0.5), 2.0 * (ey * ez - ex * ew), 2.0 * (ey * ew + ex * ez));
+    d3 r1 = mk(2.0 * (ey * ez + ex * ew), 2.0 * (ex * ex + ez * ez - 0.5), 2.0 * (ez * ew - ex * ey));
+    d3 r2 = mk(2.0 * (ey * ew - ex * ez), 2.0 * (ez * ew + ex * ey), 2.0 * (ex * ex + ew * ew - 0.5));
+    return mk(r0.x * v.x + r0.y * v.y + r0.z * v.z, r1.x * v.x + r1.y * v.y + r1.z * v.z,
+              r2.x * v.x + r2.y * v.y + r2.z * v.z);
+}
+
+// updatePolygonObjectData_kernel (impl:1911-1956); t = 0 where the
+// reference leaves it uninitialised (all three determinants <= 1e-13).
+__global__ void __launch_bounds__(256) k_update_polygon(const xd_polygon_mass_info* __restrict__ dpmi,
+                                                        const double* __restrict__ vlist,
+                                                        double* __restrict__ sphere,
+                                                        xd_polygon_info* __restrict__ dpi,
+                                                        unsigned ntri)
+{
+    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= ntri) return;
+    size_t s = (size_t)id * 9;
+    int mid = dpi[id].id;
+    d3 o = ldp(dpmi[mid].origin);
+    const double* ep = dpmi[mid].ep;
+    double ex = __ldg(ep), ey = __ldg(ep + 1), ez = __ldg(ep + 2), ew = __ldg(ep + 3);
+    d3 Pv = o + to_global(ldp(vlist + s + 0), ex, ey, ez, ew);
+    d3 Qv = o + to_global(ldp(vlist + s + 3), ex, ey, ez, ew);
+    d3 Rv = o + to_global(ldp(vlist + s + 6), ex, ey, ez, ew);
+    d3 V = Qv - Pv, W = Rv - Pv;
+    d3 N = cross(V, W);
+    N = N / length(N);
+    d3 M1 = 0.5 * (Qv + Pv);
+    d3 M2 = 0.5 * (Rv + Pv);
+    d3 D1 = cross(N, V), D2 = cross(N, W);
+    double t = 0.0;
+    if (fabs(D1.x * D2.y - D1.y * D2.x) > 1E-13)
+        t = (D2.x * (M1.y - M2.y)) / (D1.x * D2.y - D1.y * D2.x) - (D2.y * (M1.x - M2.x)) / (D1.x * D2.y - D1.y * D2.x);
+    else if (fabs(D1.x * D2.z - D1.z * D2.x) > 1E-13)
+        t = (D2.x * (M1.z - M2.z)) / (D1.x * D2.z - D1.z * D2.x) - (D2.z * (M1.x - M2.x)) / (D1.x * D2.z - D1.z * D2.x);
+    else if (fabs(D1.y * D2.z - D1.z * D2.y) > 1E-13)
+        t = (D2.y * (M1.z - M2.z)) / (D1.y * D2.z - D1.z * D2.y) - (D2.z * (M1.y - M2.y)) / (D1.y * D2.z - D1.z * D2.y);
+    d3 ctri = M1 + t * D1;
+    double* sp = sphere + 4 * (size_t)id;
+    sp[0] = ctri.x;
+    sp[1] = ctri.y;
+    sp[2] = ctri.z;
+    st3(dpi[id].P, 0, Pv);
+    st3(dpi[id].Q, 0, Qv);
+    st3(dpi[id].R, 0, Rv);
+}
+
+// ----------------------------------------------------------- reductionD3
+
+constexpr int kRedThreads = 256;
+constexpr int kRedBlocksMax = 1024;
+
+__global__ void __launch_bounds__(kRedThreads) k_reduce_d3_partial(const double* __restrict__ in,
+                                                                   unsigned n,
+                                                                   double* __restrict__ partial)
+{
+    __shared__ double red[3][kRedThreads];
+    double s[3] = { 0.0, 0.0, 0.0 };
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        s[0] += in[3 * i];
+        s[1] += in[3 * i + 1];
+        s[2] += in[3 * i + 2];
+    }
+    for (int q = 0; q < 3; ++q) red[q][threadIdx.x] = s[q];
+    __syncthreads();
+    for (int o = kRedThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < (unsigned)o)
+            for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 3; ++q) partial[3 * blockIdx.x + q] = red[q][0];
+}
+
+__global__ void k_reduce_d3_final(const double* __restrict__ partial, unsigned nb, double* __restrict__ out)
+{
+    if (threadIdx.x >= 3) return;
+    double s = 0.0;
+    for (unsigned b = 0; b < nb; ++b) s += partial[3 * b + threadIdx.x];
+    out[threadIdx.x] = s;
+}
+
+// ------------------------------------------------------------- pair list
+
+__device__ __forceinline__ unsigned pair_scan(const Params& P, const double* pos,
+                                              const unsigned* sorted, const unsigned* cstart,
+                                              const unsigned* cend, unsigned np, unsigned id,
+                                              unsigned* out, unsigned cap_left)
+{
+    d4 ip = ld4(pos, id);
+    int3 gp = grid_pos(P, ip.x, ip.y, ip.z);
+    unsigned cnt = 0;
+    for (int z = -1; z <= 1; z++)
+        for (int y = -1; y <= 1; y++)
+            for (int x = -1; x <= 1; x++) {
+                unsigned h = grid_hash(P, gp.x + x, gp.y + y, gp.z + z);
+                unsigned st = __ldg(cstart + h);
+                if (st == 0xffffffffu) continue;
+                unsigned en = __ldg(cend + h);
+                for (unsigned j = st; j < en; j++) {
+                    unsigned k = __ldg(sorted + j);
+                    if (id == k || k >= np) continue;
+                    d4 jp = ld4(pos, k);
+                    d3 rp = mk(jp.x - ip.x, jp.y - ip.y, jp.z - ip.z);
+                    double cdist = (ip.w + jp.w) - length(rp);
+                    if (cdist > 0) {
+                        if (out && cnt < cap_left) {
+                            out[2 * cnt] = id;
+                            out[2 * cnt + 1] = k;
+                        }
+                        cnt++;
+                    }
+                }
+            }
+    return cnt;
+}
+
+__global__ void k_pair_count(Params P, const double* __restrict__ pos, const unsigned* __restrict__ sorted,
+                             const unsigned* __restrict__ cstart, const unsigned* __restrict__ cend,
+                             unsigned np, unsigned* __restrict__ counts)
+{
+    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= np) return;
+    counts[id] = pair_scan(P, pos, sorted, cstart, cend, np, id, nullptr, 0);
+}
+
+__global__ void k_pair_fill(Params P, const double* __restrict__ pos, const unsigned* __restrict__ sorted,
+                            const unsigned* __restrict__ cstart, const unsigned* __restrict__ cend,
+                            unsigned np, const unsigned long long* __restrict__ offsets,
+                            unsigned* __restrict__ pairs, unsigned long long cap)
+{
+    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= np) return;
+    unsigned long long o = offsets[id];
+    if (o >= cap) return;
+    unsigned long long left = cap - o;
+    pair_scan(P, pos, sorted, cstart, cend, np, id, pairs + 2 * o,
+              left > 0xffffffffull ? 0xffffffffu : (unsigned)left);
+}
+
+__global__ void k_pair_offsets(const unsigned* __restrict__ counts, unsigned np,
+                               unsigned long long* __restrict__ offsets)
+{
+    // single thread: exclusive prefix in 64-bit (diagnostic path)
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned long long run = 0;
+    for (unsigned i = 0; i < np; ++i) {
+        offsets[i] = run;
+        run += counts[i];
+    }
+    offsets[np] = run;
+}
+
+// ------------------------------------------------------------- launchers
+
+int launch_p2p(const Params& P, const double* pos, const double* vel, const double* omega,
+               double* force, double* moment, const double* mass, const unsigned* sorted,
+               const unsigned* cstart, const unsigned* cend, const xd_contact_property* cp,
+               unsigned np, cudaStream_t s)
+{
+    if (np == 0) return XD_OK;
+    k_p2p<<<div_up(np, 128), 128, 0, s>>>(P, pos, vel, omega, force, moment, mass, sorted, cstart,
+                                          cend, cp, np);
+    return launch_status("calculate_p2p");
+}
+
+int launch_planes(const Params& P, const xd_plane_info* planes, const xd_contact_property* cps,
+                  unsigned cp_stride, unsigned nplanes, const double* pos, const double* vel,
+                  const double* omega, double* force, double* moment, const double* mass,
+                  unsigned np, cudaStream_t s)
+{
+    if (np == 0 || nplanes == 0) return XD_OK;
+    k_planes<<<div_up(np, 128), 128, 0, s>>>(P, planes, cps, cp_stride, nplanes, pos, vel, omega,
+                                             force, moment, mass, np);
+    return launch_status("plane_contact_force");
+}
+
+static unsigned nbr_for(unsigned nbodies)
+{
+    if (nbodies == 0 || nbodies > 8) return 0;
+    if (nbodies == 1) return 1;
+    if (nbodies == 2) return 2;
+    if (nbodies <= 4) return 4;
+    return 8;
+}
+
+size_t polygon_scratch_bytes(unsigned np, unsigned nbodies)
+{
+    unsigned nbr = nbr_for(nbodies);
+    if (nbr == 0) return 0;
+    return sizeof(double) * 6 * (size_t)nbr * div_up(np ? np : 1u, 128);
+}
+
+int launch_polygon(const Params& P, const xd_polygon_info* dpi, xd_polygon_mass_info* dpmi,
+                   const double* pos, const double* vel, const double* omega, double* force,
+                   double* moment, const double* mass, const unsigned* sidx,
+                   const unsigned* cstart, const unsigned* cend, const xd_contact_property* cp,
+                   unsigned nbodies, void* scratch, cudaStream_t s)
+{
+    unsigned np = P.np;
+    if (np == 0) return XD_OK;
+    unsigned nb = div_up(np, 128);
+    unsigned nbr = nbr_for(nbodies);
+    double* part = static_cast<double*>(scratch);
+#define XD_POLY(NBV)                                                                              \
+    k_polygon<NBV><<<nb, 128, 0, s>>>(P, dpi, dpmi, pos, vel, omega, force, moment, mass, sidx,   \
+                                      cstart, cend, cp, part)
+    switch (nbr) {
+    case 0: XD_POLY(0); break;
+    case 1: XD_POLY(1); break;
+    case 2: XD_POLY(2); break;
+    case 4: XD_POLY(4); break;
+    default: XD_POLY(8); break;
+    }
+#undef XD_POLY
+    int st = launch_status("particle_polygon_collision");
+    if (st != XD_OK || nbr == 0) return st;
+    k_polygon_reaction_final<<<1, 64, 0, s>>>(part, nb, nbodies, nbr, dpmi);
+    return launch_status("particle_polygon_collision (reaction)");
+}
+
+int launch_update_polygon(const xd_polygon_mass_info* dpmi, const double* vlist, double* sphere,
+                          xd_polygon_info* dpi, unsigned ntri, cudaStream_t s)
+{
+    if (ntri == 0) return XD_OK;
+    k_update_polygon<<<div_up(ntri, 256), 256, 0, s>>>(dpmi, vlist, sphere, dpi, ntri);
+    return launch_status("update_polygon_object_data");
+}
+
+size_t reduction_scratch_bytes(unsigned n)
+{
+    (void)n;
+    return sizeof(double) * 3 * (kRedBlocksMax + 1);
+}
+
+int reduction_d3(const double* in, unsigned n, double out[3], void* scratch, cudaStream_t s)
+{
+    double* part = static_cast<double*>(scratch);
+    unsigned nb = div_up(n ? n : 1u, kRedThreads);
+    if (nb > (unsigned)kRedBlocksMax) nb = kRedBlocksMax;
+    k_reduce_d3_partial<<<nb, kRedThreads, 0, s>>>(in, n, part);
+    k_reduce_d3_final<<<1, 32, 0, s>>>(part, nb, part + 3 * kRedBlocksMax);
+    int st = launch_status("reductionD3");
+    if (st != XD_OK) return st;
+    cudaError_t e = cudaMemcpyAsync(out, part + 3 * kRedBlocksMax, 3 * sizeof(double),
+                                    cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return cuda_status(e, "reductionD3 read-back");
+}
+
+size_t pair_list_scratch_bytes(unsigned np) { return sizeof(unsigned long long) * ((size_t)np + 1); }
+
+int pair_list(const Params& P, const double* pos, const unsigned* sorted, const unsigned* cstart,
+              const unsigned* cend, unsigned np, unsigned* counts, unsigned* pairs,
+              unsigned long long cap, unsigned long long* total, void* scratch, cudaStream_t s)
+{
+    *total = 0;
+    if (np == 0) return XD_OK;
+    unsigned long long* off = static_cast<unsigned long long*>(scratch);
+    k_pair_count<<<div_up(np, 128), 128, 0, s>>>(P, pos, sorted, cstart, cend, np, counts);
+    k_pair_offsets<<<1, 1, 0, s>>>(counts, np, off);
+    k_pair_fill<<<div_up(np, 128), 128, 0, s>>>(P, pos, sorted, cstart, cend, np, off, pairs, cap);
+    int st = launch_status("pair_list");
+    if (st != XD_OK) return st;
+    cudaError_t e = cudaMemcpyAsync(total, off + np, sizeof(unsigned long long),
+                                    cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    st = cuda_status(e, "pair_list read-back");
+    if (st != XD_OK) return st;
+    if (*total > cap) return set_error(XD_ERR_CAPACITY, "pair_list: %llu pairs > cap %llu", *total, cap);
+    return XD_OK;
+}
+
+}  // namespace xd

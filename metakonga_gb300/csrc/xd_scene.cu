@@ -1,0 +1,446 @@
+// Scenes: device-resident DEM systems stepped in the reference's order
+// (dem_simulation::oneStepAnalysis, dem_simulation.cpp:447-469).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "xd_grid.cuh"
+#include "xd_internal.cuh"
+
+using namespace xd;
+
+struct xd_scene {
+    xd_scene_desc desc;
+    Params P;
+    unsigned np = 0, ntri = 0, nbodies = 0, nplanes = 0, ncell = 0;
+    // state (reference layouts)
+    double *pos = nullptr, *vel = nullptr, *acc = nullptr, *omega = nullptr, *alpha = nullptr;
+    double *force = nullptr, *moment = nullptr, *mass = nullptr, *inertia = nullptr;
+    // grid
+    unsigned *hash = nullptr, *index = nullptr, *sorted = nullptr, *cstart = nullptr, *cend = nullptr;
+    // walls / mesh
+    xd_plane_info* planes = nullptr;
+    xd_contact_property* cp_planes = nullptr;
+    xd_contact_property* cp_pp = nullptr;
+    xd_polygon_info* poly = nullptr;
+    double* sphere = nullptr;
+    double* vlist = nullptr;
+    xd_polygon_mass_info* pmi = nullptr;
+    xd_contact_property* cp_poly = nullptr;
+    // workspace
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    void* poly_scratch = nullptr;
+    bool bodies_dirty = false;
+    std::vector<void*> allocs;
+    // phase timing
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> spans;
+    double phase_ms[XD_SCENE_PHASES] = {};
+    unsigned long long phase_n[XD_SCENE_PHASES] = {};
+};
+
+namespace {
+
+template <typename T>
+int dalloc(xd_scene* s, T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) return XD_OK;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, sizeof(T) * count);
+    if (e != cudaSuccess) return cuda_status(e, "scene allocation");
+    s->allocs.push_back(q);
+    *p = static_cast<T*>(q);
+    return XD_OK;
+}
+
+int h2d(void* dst, const void* src, size_t bytes, cudaStream_t st)
+{
+    if (!src || !dst || bytes == 0) return XD_OK;
+    return cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st), "scene upload");
+}
+
+int d2h(void* dst, const void* src, size_t bytes, cudaStream_t st)
+{
+    if (!src || !dst || bytes == 0) return XD_OK;
+    return cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st), "scene download");
+}
+
+void free_scene(xd_scene* s)
+{
+    for (void* p : s->allocs) cudaFree(p);
+    s->allocs.clear();
+    for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
+    s->ev_pool.clear();
+}
+
+cudaEvent_t next_event(xd_scene* s)
+{
+    if (s->ev_used == s->ev_pool.size()) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        s->ev_pool.push_back(e);
+    }
+    return s->ev_pool[s->ev_used++];
+}
+
+// Records a [begin, end) event pair around one phase when timing is on.
+struct PhaseSpan {
+    xd_scene* s;
+    int phase;
+    cudaStream_t q;
+    cudaEvent_t b = nullptr;
+    PhaseSpan(xd_scene* s_, int ph, cudaStream_t q_) : s(s_), phase(ph), q(q_)
+    {
+        if (s->timing && (b = next_event(s))) cudaEventRecord(b, q);
+    }
+    ~PhaseSpan()
+    {
+        if (!b) return;
+        cudaEvent_t e = next_event(s);
+        if (!e) return;
+        cudaEventRecord(e, q);
+        s->spans.push_back({ phase, { b, e } });
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int xd_scene_create(const xd_scene_desc* d, xd_scene** out)
+{
+    if (!d || !out) return set_error(XD_ERR_INVALID, "scene_create: null argument");
+    *out = nullptr;
+    if (d->mode != XD_MODE_FP64) return set_error(XD_ERR_INVALID, "scene_create: unknown mode %d", d->mode);
+    const xd_device_parameters& h = d->params;
+    unsigned gx = h.grid_size[0], gy = h.grid_size[1], gz = h.grid_size[2];
+    if (!gx || !gy || !gz || (gx & (gx - 1)) || (gy & (gy - 1)) || (gz & (gz - 1)))
+        return set_error(XD_ERR_INVALID, "scene_create: grid sizes must be powers of two");
+    if ((unsigned long long)gx * gy * gz != h.ncell)
+        return set_error(XD_ERR_INVALID, "scene_create: ncell must equal the grid size product");
+    if (h.cell_size <= 0.0) return set_error(XD_ERR_INVALID, "scene_create: cell_size must be > 0");
+    if (d->nplanes && (!d->planes || !d->cp_planes))
+        return set_error(XD_ERR_INVALID, "scene_create: planes given without arrays");
+    if (d->ntri && (!d->poly || !d->sphere || !d->vlist || !d->pmi || !d->cp_poly || !d->nbodies))
+        return set_error(XD_ERR_INVALID, "scene_create: triangles given without mesh arrays");
+
+    xd_scene* s = new (std::nothrow) xd_scene();
+    if (!s) return set_error(XD_ERR_NOMEM, "scene_create: host allocation");
+    s->desc = *d;
+    s->desc.planes = nullptr;
+    s->desc.cp_planes = nullptr;
+    s->desc.poly = nullptr;
+    s->desc.sphere = nullptr;
+    s->desc.vlist = nullptr;
+    s->desc.pmi = nullptr;
+    s->desc.cp_poly = nullptr;
+    s->np = d->np;
+    s->ntri = d->ntri;
+    s->nbodies = d->ntri ? d->nbodies : 0;
+    s->nplanes = d->nplanes;
+    s->ncell = h.ncell;
+    xd_device_parameters hp = h;
+    hp.np = d->np;
+    s->P = to_params(hp);
+
+    const size_t n = (size_t)s->np, ng = (size_t)s->np + s->ntri;
+    int st = XD_OK;
+    auto A = [&](int r) { if (st == XD_OK) st = r; };
+    A(dalloc(s, &s->pos, 4 * n));
+    A(dalloc(s, &s->vel, 3 * n));
+    A(dalloc(s, &s->acc, 3 * n));
+    A(dalloc(s, &s->omega, 3 * n));
+    A(dalloc(s, &s->alpha, 3 * n));
+    A(dalloc(s, &s->force, 3 * n));
+    A(dalloc(s, &s->moment, 3 * n));
+    A(dalloc(s, &s->mass, n));
+    A(dalloc(s, &s->inertia, n));
+    A(dalloc(s, &s->hash, ng));
+    A(dalloc(s, &s->index, ng));
+    A(dalloc(s, &s->sorted, ng));
+    A(dalloc(s, &s->cstart, s->ncell));
+    A(dalloc(s, &s->cend, s->ncell));
+    A(dalloc(s, &s->cp_pp, 1));
+    A(dalloc(s, &s->planes, s->nplanes));
+    A(dalloc(s, &s->cp_planes, s->nplanes));
+    A(dalloc(s, &s->poly, s->ntri));
+    A(dalloc(s, &s->sphere, 4 * (size_t)s->ntri));
+    A(dalloc(s, &s->vlist, 9 * (size_t)s->ntri));
+    A(dalloc(s, &s->pmi, s->nbodies));
+    A(dalloc(s, &s->cp_poly, s->nbodies));
+    s->scratch_bytes = reorder_scratch_bytes((unsigned)ng);
+    char* scr = nullptr;
+    A(dalloc(s, &scr, s->scratch_bytes));
+    s->scratch = scr;
+    size_t pb = polygon_scratch_bytes(s->np, s->nbodies);
+    char* pscr = nullptr;
+    if (s->ntri) A(dalloc(s, &pscr, pb ? pb : 256));
+    s->poly_scratch = pscr;
+    if (st != XD_OK) {
+        free_scene(s);
+        delete s;
+        return st;
+    }
+    cudaStream_t q = 0;
+    A(h2d(s->cp_pp, &d->cp_pp, sizeof(xd_contact_property), q));
+    A(h2d(s->planes, d->planes, sizeof(xd_plane_info) * s->nplanes, q));
+    A(h2d(s->cp_planes, d->cp_planes, sizeof(xd_contact_property) * s->nplanes, q));
+    A(h2d(s->poly, d->poly, sizeof(xd_polygon_info) * s->ntri, q));
+    A(h2d(s->sphere, d->sphere, sizeof(double) * 4 * s->ntri, q));
+    A(h2d(s->vlist, d->vlist, sizeof(double) * 9 * s->ntri, q));
+    A(h2d(s->pmi, d->pmi, sizeof(xd_polygon_mass_info) * s->nbodies, q));
+    A(h2d(s->cp_poly, d->cp_poly, sizeof(xd_contact_property) * s->nbodies, q));
+    if (st == XD_OK) A(cuda_status(cudaStreamSynchronize(q), "scene_create upload"));
+    if (st != XD_OK) {
+        free_scene(s);
+        delete s;
+        return st;
+    }
+    *out = s;
+    return XD_OK;
+}
+
+int xd_scene_destroy(xd_scene* s)
+{
+    if (!s) return XD_OK;
+    cudaError_t e = cudaDeviceSynchronize();
+    free_scene(s);
+    delete s;
+    return cuda_status(e, "scene_destroy");
+}
+
+int xd_scene_upload(xd_scene* s, const double* pos, const double* vel, const double* acc,
+                    const double* omega, const double* alpha, const double* force,
+                    const double* moment, const double* mass, const double* inertia, void* stream)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_upload: null scene");
+    cudaStream_t q = static_cast<cudaStream_t>(stream);
+    size_t n = s->np;
+    int st = XD_OK;
+    auto A = [&](int r) { if (st == XD_OK) st = r; };
+    A(h2d(s->pos, pos, sizeof(double) * 4 * n, q));
+    A(h2d(s->vel, vel, sizeof(double) * 3 * n, q));
+    A(h2d(s->acc, acc, sizeof(double) * 3 * n, q));
+    A(h2d(s->omega, omega, sizeof(double) * 3 * n, q));
+    A(h2d(s->alpha, alpha, sizeof(double) * 3 * n, q));
+    A(h2d(s->force, force, sizeof(double) * 3 * n, q));
+    A(h2d(s->moment, moment, sizeof(double) * 3 * n, q));
+    A(h2d(s->mass, mass, sizeof(double) * n, q));
+    A(h2d(s->inertia, inertia, sizeof(double) * n, q));
+    if (st == XD_OK) A(cuda_status(cudaStreamSynchronize(q), "scene_upload"));
+    return st;
+}
+
+int xd_scene_download(xd_scene* s, double* pos, double* vel, double* acc, double* omega,
+                      double* alpha, double* force, double* moment, void* stream)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_download: null scene");
+    cudaStream_t q = static_cast<cudaStream_t>(stream);
+    size_t n = s->np;
+    int st = XD_OK;
+    auto A = [&](int r) { if (st == XD_OK) st = r; };
+    A(d2h(pos, s->pos, sizeof(double) * 4 * n, q));
+    A(d2h(vel, s->vel, sizeof(double) * 3 * n, q));
+    A(d2h(acc, s->acc, sizeof(double) * 3 * n, q));
+    A(d2h(omega, s->omega, sizeof(double) * 3 * n, q));
+    A(d2h(alpha, s->alpha, sizeof(double) * 3 * n, q));
+    A(d2h(force, s->force, sizeof(double) * 3 * n, q));
+    A(d2h(moment, s->moment, sizeof(double) * 3 * n, q));
+    if (st == XD_OK) A(cuda_status(cudaStreamSynchronize(q), "scene_download"));
+    return st;
+}
+
+int xd_scene_device_state(xd_scene* s, double** pos, double** vel, double** acc, double** omega,
+                          double** alpha, double** force, double** moment, double** mass,
+                          double** inertia)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_device_state: null scene");
+    if (pos) *pos = s->pos;
+    if (vel) *vel = s->vel;
+    if (acc) *acc = s->acc;
+    if (omega) *omega = s->omega;
+    if (alpha) *alpha = s->alpha;
+    if (force) *force = s->force;
+    if (moment) *moment = s->moment;
+    if (mass) *mass = s->mass;
+    if (inertia) *inertia = s->inertia;
+    return XD_OK;
+}
+
+int xd_scene_device_grid(xd_scene* s, unsigned** hash, unsigned** index, unsigned** sorted,
+                         unsigned** cstart, unsigned** cend)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_device_grid: null scene");
+    if (hash) *hash = s->hash;
+    if (index) *index = s->index;
+    if (sorted) *sorted = s->sorted;
+    if (cstart) *cstart = s->cstart;
+    if (cend) *cend = s->cend;
+    return XD_OK;
+}
+
+int xd_scene_download_grid(xd_scene* s, unsigned* hash, unsigned* index, unsigned* sorted,
+                           unsigned* cstart, unsigned* cend, void* stream)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_download_grid: null scene");
+    cudaStream_t q = static_cast<cudaStream_t>(stream);
+    size_t ng = (size_t)s->np + s->ntri;
+    int st = XD_OK;
+    auto A = [&](int r) { if (st == XD_OK) st = r; };
+    A(d2h(hash, s->hash, sizeof(unsigned) * ng, q));
+    A(d2h(index, s->index, sizeof(unsigned) * ng, q));
+    A(d2h(sorted, s->sorted, sizeof(unsigned) * ng, q));
+    A(d2h(cstart, s->cstart, sizeof(unsigned) * s->ncell, q));
+    A(d2h(cend, s->cend, sizeof(unsigned) * s->ncell, q));
+    if (st == XD_OK) A(cuda_status(cudaStreamSynchronize(q), "scene_download_grid"));
+    return st;
+}
+
+int xd_scene_set_bodies(xd_scene* s, const xd_polygon_mass_info* pmi, void* stream)
+{
+    if (!s || !pmi) return set_error(XD_ERR_INVALID, "scene_set_bodies: null argument");
+    if (!s->nbodies) return set_error(XD_ERR_STATE, "scene_set_bodies: scene has no polygon bodies");
+    cudaStream_t q = static_cast<cudaStream_t>(stream);
+    int st = h2d(s->pmi, pmi, sizeof(xd_polygon_mass_info) * s->nbodies, q);
+    if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "scene_set_bodies");
+    s->bodies_dirty = true;
+    return st;
+}
+
+int xd_scene_get_bodies(xd_scene* s, xd_polygon_mass_info* pmi, void* stream)
+{
+    if (!s || !pmi) return set_error(XD_ERR_INVALID, "scene_get_bodies: null argument");
+    cudaStream_t q = static_cast<cudaStream_t>(stream);
+    int st = d2h(pmi, s->pmi, sizeof(xd_polygon_mass_info) * s->nbodies, q);
+    if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "scene_get_bodies");
+    return st;
+}
+
+int xd_scene_set_timing(xd_scene* s, int enable)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_set_timing: null scene");
+    cudaError_t e = cudaDeviceSynchronize();
+    s->timing = enable != 0;
+    s->spans.clear();
+    s->ev_used = 0;
+    for (int i = 0; i < XD_SCENE_PHASES; ++i) {
+        s->phase_ms[i] = 0.0;
+        s->phase_n[i] = 0;
+    }
+    return cuda_status(e, "scene_set_timing");
+}
+
+int xd_scene_phase_times(xd_scene* s, double* ms, unsigned long long* launches)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_phase_times: null scene");
+    for (auto& sp : s->spans) {
+        cudaError_t e = cudaEventSynchronize(sp.second.second);
+        if (e != cudaSuccess) return cuda_status(e, "scene_phase_times");
+        float t = 0.f;
+        e = cudaEventElapsedTime(&t, sp.second.first, sp.second.second);
+        if (e != cudaSuccess) return cuda_status(e, "scene_phase_times");
+        s->phase_ms[sp.first] += t;
+        s->phase_n[sp.first] += 1;
+    }
+    s->spans.clear();
+    s->ev_used = 0;
+    for (int i = 0; i < XD_SCENE_PHASES; ++i) {
+        if (ms) ms[i] = s->phase_ms[i];
+        if (launches) launches[i] = s->phase_n[i];
+    }
+    return XD_OK;
+}
+
+unsigned long long xd_scene_launches(xd_scene* s, unsigned nsteps)
+{
+    if (!s || nsteps == 0) return 0;
+    unsigned ng = s->np + s->ntri;
+    unsigned passes = (key_bits_for(s->ncell) + 7) / 8;
+    unsigned long long per = 0;
+    per += 1 + (s->ntri ? 1 : 0);                 // hash (+ triangle spheres)
+    per += ng > 1 ? 5ull * passes : 0;            // radix sort
+    per += 2;                                     // fill + cell bounds
+    per += 1;                                     // particle-particle
+    per += s->nplanes ? 1 : 0;                    // planes
+    per += s->ntri ? 2 : 0;                       // triangles + reaction
+    per += 1;                                     // VV velocity(+position)
+    unsigned long long total = per * nsteps;
+    if (s->bodies_dirty && s->ntri) total += 1;   // mesh update
+    total += 1;                                   // first VV position
+    return total;
+}
+
+int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_step: null scene");
+    if (nsteps == 0) return XD_OK;
+    cudaStream_t q = static_cast<cudaStream_t>(stream);
+    const Params& P = s->P;
+    const unsigned np = s->np, ng = s->np + s->ntri;
+    int st = XD_OK;
+    if (s->bodies_dirty && s->ntri) {
+        st = launch_update_polygon(s->pmi, s->vlist, s->sphere, s->poly, s->ntri, q);
+        if (st != XD_OK) return st;
+        s->bodies_dirty = false;
+    }
+    // VV position of the first step (later ones are fused into the velocity pass)
+    {
+        PhaseSpan ps(s, 0, q);
+        st = launch_vv_position(P, s->pos, s->vel, s->acc, np, q);
+    }
+    if (st != XD_OK) return st;
+    for (unsigned t = 0; t < nsteps; ++t) {
+        {
+            PhaseSpan ps(s, 1, q);
+            st = launch_hash(P, s->hash, s->index, s->pos, np, 0, q);
+            if (st == XD_OK && s->ntri) st = launch_hash(P, s->hash, s->index, s->sphere, s->ntri, np, q);
+        }
+        if (st == XD_OK) {
+            PhaseSpan ps(s, 2, q);
+            st = reorder_and_find_cell_start(s->hash, s->index, s->cstart, s->cend, s->sorted, ng,
+                                             s->ncell, s->scratch, q, false);
+        }
+        if (st == XD_OK) {
+            PhaseSpan ps(s, 3, q);
+            st = launch_p2p(P, s->pos, s->vel, s->omega, s->force, s->moment, s->mass, s->sorted,
+                            s->cstart, s->cend, s->cp_pp, np, q);
+        }
+        if (st == XD_OK && s->nplanes) {
+            PhaseSpan ps(s, 4, q);
+            st = launch_planes(P, s->planes, s->cp_planes, 1, s->nplanes, s->pos, s->vel, s->omega,
+                               s->force, s->moment, s->mass, np, q);
+        }
+        if (st == XD_OK && s->ntri) {
+            PhaseSpan ps(s, 5, q);
+            st = launch_polygon(P, s->poly, s->pmi, s->pos, s->vel, s->omega, s->force, s->moment,
+                                s->mass, s->sorted, s->cstart, s->cend, s->cp_poly, s->nbodies,
+                                s->poly_scratch, q);
+        }
+        if (st == XD_OK) {
+            PhaseSpan ps(s, 0, q);
+            if (t + 1 < nsteps)
+                st = launch_vv_velocity_position(P, s->pos, s->vel, s->acc, s->omega, s->alpha,
+                                                 s->force, s->moment, s->mass, s->inertia, np, q);
+            else
+                st = launch_vv_velocity(P, s->vel, s->acc, s->omega, s->alpha, s->force, s->moment,
+                                        s->mass, s->inertia, np, q);
+        }
+        if (st != XD_OK) return st;
+    }
+    if (check) {
+        unsigned herr = 0;
+        cudaError_t e = cudaMemcpyAsync(&herr, s->scratch, sizeof(unsigned), cudaMemcpyDeviceToHost, q);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(q);
+        if (e != cudaSuccess) return cuda_status(e, "scene_step check");
+        if (herr) return set_error(XD_ERR_INVALID, "scene_step: a hash value was >= ncell");
+    }
+    return XD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,141 @@
+"""Device-resident scenes (libxdem's xd_scene_* API).
+
+``DeviceScene`` uploads a metakonga_gb300.scenes.Scene once and advances whole
+steps on the GPU in the reference's order (dem_simulation::oneStepAnalysis,
+dem_simulation.cpp:447-469), without per-step host work.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import call
+
+MODE_FP64 = 0
+
+
+class _Desc(C.Structure):
+    _fields_ = [
+        ("params", C.c_byte * 112), ("np", C.c_uint), ("mode", C.c_int),
+        ("cp_pp", C.c_byte * 88), ("nplanes", C.c_uint),
+        ("planes", C.c_void_p), ("cp_planes", C.c_void_p),
+        ("ntri", C.c_uint), ("nbodies", C.c_uint),
+        ("poly", C.c_void_p), ("sphere", C.c_void_p), ("vlist", C.c_void_p),
+        ("pmi", C.c_void_p), ("cp_poly", C.c_void_p),
+    ]
+
+
+assert C.sizeof(_Desc) == 280 and _Desc.planes.offset == 216 and _Desc.poly.offset == 240
+
+
+def _addr(a):
+    return None if a is None or a.size == 0 else a.ctypes.data
+
+
+class DeviceScene:
+    def __init__(self, scene, mode: int = MODE_FP64):
+        if _lib.lib().xd_sizeof(b"xd_scene_desc") != C.sizeof(_Desc):
+            raise RuntimeError("xd_scene_desc layout mismatch between binding and library")
+        self.scene = scene
+        self.np = scene.np_
+        self.ntri = scene.ntri
+        d = _Desc()
+        p = scene.params.copy()
+        p["np"] = scene.np_
+        C.memmove(d.params, p.ctypes.data, 112)
+        d.np = scene.np_
+        d.mode = mode
+        C.memmove(d.cp_pp, scene.cp_pp.ctypes.data, 88)
+        self._keep = []
+        planes = np.ascontiguousarray(scene.planes)
+        cpl = np.ascontiguousarray(scene.cp_planes)
+        self._keep += [planes, cpl]
+        d.nplanes = planes.shape[0]
+        d.planes, d.cp_planes = _addr(planes), _addr(cpl)
+        if scene.ntri:
+            arrs = [np.ascontiguousarray(a) for a in (scene.poly, scene.sphere, scene.vlist,
+                                                      scene.pmi, scene.cp_poly)]
+            self._keep += arrs
+            d.ntri = scene.ntri
+            d.nbodies = scene.pmi.shape[0]
+            d.poly, d.sphere, d.vlist, d.pmi, d.cp_poly = (a.ctypes.data for a in arrs)
+        h = C.c_void_p()
+        call("xd_scene_create", C.addressof(d), C.addressof(h))
+        self.handle = h
+        self.upload(scene)
+
+    def upload(self, sc, stream: int = 0):
+        arrs = [np.ascontiguousarray(getattr(sc, f)) for f in
+                ("pos", "vel", "acc", "omega", "alpha", "force", "moment", "mass", "inertia")]
+        call("xd_scene_upload", self.handle, *[a.ctypes.data for a in arrs], stream)
+
+    def download(self, stream: int = 0) -> dict:
+        n = self.np
+        out = {"pos": np.empty((n, 4)), "vel": np.empty((n, 3)), "acc": np.empty((n, 3)),
+               "omega": np.empty((n, 3)), "alpha": np.empty((n, 3)), "force": np.empty((n, 3)),
+               "moment": np.empty((n, 3))}
+        call("xd_scene_download", self.handle, *[out[k].ctypes.data for k in
+                                                 ("pos", "vel", "acc", "omega", "alpha", "force",
+                                                  "moment")], stream)
+        return out
+
+    def device_state(self) -> dict:
+        ptrs = [C.c_void_p() for _ in range(9)]
+        call("xd_scene_device_state", self.handle, *[C.addressof(p) for p in ptrs])
+        names = ("pos", "vel", "acc", "omega", "alpha", "force", "moment", "mass", "inertia")
+        return {k: p.value for k, p in zip(names, ptrs)}
+
+    def device_grid(self) -> dict:
+        ptrs = [C.c_void_p() for _ in range(5)]
+        call("xd_scene_device_grid", self.handle, *[C.addressof(p) for p in ptrs])
+        return {k: p.value for k, p in zip(("hash", "index", "sorted", "cstart", "cend"), ptrs)}
+
+    def download_grid(self, stream: int = 0) -> dict:
+        ng = self.np + self.ntri
+        nc = int(self.scene.params["ncell"])
+        out = {"hash": np.empty(ng, np.uint32), "index": np.empty(ng, np.uint32),
+               "sorted": np.empty(ng, np.uint32), "cstart": np.empty(nc, np.uint32),
+               "cend": np.empty(nc, np.uint32)}
+        call("xd_scene_download_grid", self.handle, *[out[k].ctypes.data for k in
+                                                      ("hash", "index", "sorted", "cstart", "cend")],
+             stream)
+        return out
+
+    def set_bodies(self, pmi: np.ndarray, stream: int = 0):
+        a = np.ascontiguousarray(pmi)
+        call("xd_scene_set_bodies", self.handle, a.ctypes.data, stream)
+
+    def get_bodies(self, stream: int = 0) -> np.ndarray:
+        out = np.zeros_like(self.scene.pmi)
+        call("xd_scene_get_bodies", self.handle, out.ctypes.data, stream)
+        return out
+
+    def step(self, nsteps: int = 1, check: bool = False, stream: int = 0):
+        call("xd_scene_step", self.handle, nsteps, 1 if check else 0, stream)
+
+    PHASES = ("vv", "hash", "sort_cells", "p2p", "planes", "triangles")
+
+    def set_timing(self, enable: bool = True):
+        call("xd_scene_set_timing", self.handle, 1 if enable else 0)
+
+    def phase_times(self) -> dict:
+        ms = np.zeros(len(self.PHASES))
+        n = np.zeros(len(self.PHASES), np.uint64)
+        call("xd_scene_phase_times", self.handle, ms.ctypes.data, n.ctypes.data)
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.PHASES)}
+
+    def launches(self, nsteps: int) -> int:
+        return int(_lib.lib().xd_scene_launches(self.handle, nsteps))
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            call("xd_scene_destroy", self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

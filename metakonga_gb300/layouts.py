@@ -1,0 +1,106 @@
+"""Byte layouts of the structs that cross the reference's DEM boundary.
+
+Each numpy dtype has the exact size and field offsets of the matching C struct
+in the reference's include/mphysics_cuda_dec.cuh, so one buffer can be handed
+to the CUDA library (libxdem), to a caller that was written against the
+reference headers, and to the test oracle.
+
+* ``PARAMS``            device_parameters       (mphysics_cuda_dec.cuh:17-30), 112 B
+* ``CONTACT_PROPERTY``  device_contact_property (mphysics_cuda_dec.cuh:78-88), 88 B
+* ``PLANE``             device_plane_info       (mphysics_cuda_dec.cuh:43-55), 232 B
+* ``POLYGON``           device_polygon_info     (mphysics_cuda_dec.cuh:32-41), 152 B
+* ``POLYGON_MASS``      device_polygon_mass_info(mphysics_cuda_dec.cuh:57-65), 160 B
+  (``ep`` is a CUDA double4, aligned to 16 bytes)
+"""
+import numpy as np
+
+V3 = ("<f8", (3,))
+
+PARAMS = np.dtype({
+    "names": ["rolling", "np", "nsphere", "ncell", "grid", "dt", "half2dt", "cell_size",
+              "cohesion", "gravity", "world_origin"],
+    "formats": ["u1", "<u4", "<u4", "<u4", ("<u4", (3,)), "<f8", "<f8", "<f8", "<f8", V3, V3],
+    "offsets": [0, 4, 8, 12, 16, 32, 40, 48, 56, 64, 88],
+    "itemsize": 112,
+})
+
+CONTACT_PROPERTY = np.dtype({
+    "names": ["Ei", "Ej", "pri", "prj", "Gi", "Gj", "rest", "fric", "rfric", "coh", "sratio"],
+    "formats": ["<f8"] * 11,
+    "offsets": [8 * i for i in range(11)],
+    "itemsize": 88,
+})
+
+PLANE = np.dtype({
+    "names": ["l1", "l2", "u1", "u2", "uw", "xw", "pa", "pb", "w2", "w3", "w4"],
+    "formats": ["<f8", "<f8"] + [V3] * 9,
+    "offsets": [0, 8] + [16 + 24 * i for i in range(9)],
+    "itemsize": 232,
+})
+
+POLYGON = np.dtype({
+    "names": ["id", "P", "Q", "R", "V", "W", "N"],
+    "formats": ["<i4"] + [V3] * 6,
+    "offsets": [0] + [8 + 24 * i for i in range(6)],
+    "itemsize": 152,
+})
+
+POLYGON_MASS = np.dtype({
+    "names": ["origin", "ep", "vel", "omega", "force", "moment"],
+    "formats": [V3, ("<f8", (4,)), V3, V3, V3, V3],
+    "offsets": [0, 32, 64, 88, 112, 136],
+    "itemsize": 160,
+})
+
+assert PARAMS.itemsize == 112 and CONTACT_PROPERTY.itemsize == 88
+assert PLANE.itemsize == 232 and POLYGON.itemsize == 152 and POLYGON_MASS.itemsize == 160
+
+
+def make_params(*, np_, ncell, grid, dt, cell_size, world_origin, gravity, rolling=True,
+                nsphere=0, cohesion=0.0):
+    """Fill a ``device_parameters`` record the way dem_simulation::initialize
+    does (dem_simulation.cpp:289-307): half2dt = 0.5*dt*dt."""
+    p = np.zeros((), dtype=PARAMS)
+    p["rolling"] = 1 if rolling else 0
+    p["np"] = np_
+    p["nsphere"] = nsphere
+    p["ncell"] = ncell
+    p["grid"] = grid
+    p["dt"] = dt
+    p["half2dt"] = 0.5 * dt * dt
+    p["cell_size"] = cell_size
+    p["cohesion"] = cohesion
+    p["gravity"] = gravity
+    p["world_origin"] = world_origin
+    return p
+
+
+def make_contact_property(*, E_i, E_j, nu_i, nu_j, G_i=0.0, G_j=0.0, rest, fric, sratio,
+                          coh=0.0):
+    """``device_contact_property`` as contact::cudaMemoryAlloc builds it
+    (contact.cpp:107-116): rolling friction is always 0 there."""
+    c = np.zeros((), dtype=CONTACT_PROPERTY)
+    c["Ei"], c["Ej"], c["pri"], c["prj"] = E_i, E_j, nu_i, nu_j
+    c["Gi"], c["Gj"], c["rest"], c["fric"] = G_i, G_j, rest, fric
+    c["rfric"], c["coh"], c["sratio"] = 0.0, coh, sratio
+    return c
+
+
+def define_plane(xw, pa, pc, pb):
+    """Four-point plane (xcar plane.cpp:47-76): w2 = pa, w3 = pc, w4 = pb;
+    l1 = |pa - xw|, l2 = |pb - xw|, u1, u2 the unit edges, uw = u1 x u2."""
+    xw, pa, pc, pb = (np.asarray(v, dtype=np.float64) for v in (xw, pa, pc, pb))
+    rec = np.zeros((), dtype=PLANE)
+    a = pa - xw
+    b = pb - xw
+    l1 = float(np.sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]))
+    l2 = float(np.sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]))
+    u1 = a / l1
+    u2 = b / l2
+    uw = np.array([u1[1] * u2[2] - u1[2] * u2[1], u1[2] * u2[0] - u1[0] * u2[2],
+                   u1[0] * u2[1] - u1[1] * u2[0]])
+    rec["l1"], rec["l2"] = l1, l2
+    rec["u1"], rec["u2"], rec["uw"], rec["xw"] = u1, u2, uw, xw
+    rec["pa"], rec["pb"] = a, b
+    rec["w2"], rec["w3"], rec["w4"] = pa, pc, pb
+    return rec

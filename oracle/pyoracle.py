@@ -1,0 +1,290 @@
+"""ctypes access to the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+``Oracle``      the C restatement, oracle/libxd_oracle.so (built by
+                ``make -C oracle``; __graft_entry__.build() does this).
+``RefKernels``  the reference's own kernels compiled as host code,
+                oracle/_ref/libxdref.so (``make -C oracle ref``); only
+                available where the reference tree is present.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module; the product (metakonga_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_ORACLE = os.path.join(HERE, "libxd_oracle.so")
+LIB_REF = os.path.join(HERE, "_ref", "libxdref.so")
+
+_vp = C.c_void_p
+_u = C.c_uint
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert isinstance(a, np.ndarray) and a.flags["C_CONTIGUOUS"], "need a C-contiguous array"
+    return a.ctypes.data_as(_vp)
+
+
+def build_oracle(quiet: bool = True) -> str:
+    subprocess.run(["make", "-C", HERE, "libxd_oracle.so"], check=True,
+                   stdout=subprocess.DEVNULL if quiet else None)
+    return LIB_ORACLE
+
+
+class _Scene(C.Structure):
+    _fields_ = [
+        ("prm", C.c_byte * 112), ("np", _u),
+        ("pos", _vp), ("vel", _vp), ("acc", _vp), ("omega", _vp), ("alpha", _vp),
+        ("force", _vp), ("moment", _vp), ("mass", _vp), ("inertia", _vp),
+        ("hash", _vp), ("index", _vp), ("sorted", _vp), ("cstart", _vp), ("cend", _vp),
+        ("cp_pp", _vp), ("nplanes", _u), ("planes", _vp), ("cp_planes", _vp),
+        ("ntri", _u), ("poly", _vp), ("sphere", _vp), ("pmi", _vp), ("cp_poly", _vp),
+    ]
+
+
+class Oracle:
+    """The C restatement of the reference's FP64 GPU path (xdo_*) and CPU path (xdo_cpu_*)."""
+
+    def __init__(self, path: str = LIB_ORACLE):
+        if not os.path.exists(path):
+            build_oracle()
+        self.lib = C.CDLL(path)
+        L = self.lib
+        for name in ("xdo_calculate_hash_and_index", "xdo_calculate_hash_and_index_polysphere",
+                     "xdo_reorder_and_find_cell_start", "xdo_vv_update_position",
+                     "xdo_vv_update_velocity", "xdo_calculate_p2p", "xdo_plane_contact_force",
+                     "xdo_cube_contact_force", "xdo_particle_polygon_collision",
+                     "xdo_update_polygon_object_data", "xdo_step", "xdo_run_steps",
+                     "xdo_cpu_step", "xdo_cpu_run_steps"):
+            getattr(L, name).restype = None
+        L.xdo_pair_list.restype = C.c_ulonglong
+        L.xdo_pair_list.argtypes = [_vp, _vp, _vp, _vp, _vp, _u, _vp, C.c_ulonglong]
+        L.xdo_grid_hash.restype = _u
+        for s in ("params", "plane", "polygon", "polygon_mass", "contact_property"):
+            getattr(L, "xdo_sizeof_" + s).restype = _u
+
+    def sizes(self):
+        L = self.lib
+        return {s: getattr(L, "xdo_sizeof_" + s)() for s in
+                ("params", "plane", "polygon", "polygon_mass", "contact_property")}
+
+    # ---- grid ----
+    def hash_and_index(self, prm, pos, hash_, index):
+        self.lib.xdo_calculate_hash_and_index(_p(prm), _p(hash_), _p(index), _p(pos), _u(pos.shape[0]))
+
+    def hash_and_index_polysphere(self, prm, hash_, index, sid, sphere):
+        self.lib.xdo_calculate_hash_and_index_polysphere(_p(prm), _p(hash_), _p(index), _u(sid),
+                                                         _u(sphere.shape[0]), _p(sphere))
+
+    def reorder(self, hash_, index, cstart, cend, sorted_, n, ncell):
+        self.lib.xdo_reorder_and_find_cell_start(_p(hash_), _p(index), _p(cstart), _p(cend),
+                                                 _p(sorted_), _u(n), _u(ncell))
+
+    def detection(self, prm, pos, sphere=None):
+        """Hash + sort + cell ranges (neighborhood_cell::detection GPU branch)."""
+        npt = pos.shape[0]
+        nt = 0 if sphere is None else sphere.shape[0]
+        n = npt + nt
+        ncell = int(prm["ncell"])
+        h = np.zeros(n, np.uint32)
+        ix = np.zeros(n, np.uint32)
+        self.hash_and_index(prm, pos, h, ix)
+        if nt:
+            self.hash_and_index_polysphere(prm, h, ix, npt, sphere)
+        cs = np.zeros(ncell, np.uint32)
+        ce = np.zeros(ncell, np.uint32)
+        so = np.zeros(n, np.uint32)
+        self.reorder(h, ix, cs, ce, so, n, ncell)
+        return h, ix, cs, ce, so
+
+    # ---- integrator ----
+    def vv_position(self, prm, pos, vel, acc):
+        self.lib.xdo_vv_update_position(_p(prm), _p(pos), _p(vel), _p(acc), _u(pos.shape[0]))
+
+    def vv_velocity(self, prm, vel, acc, omega, alpha, force, moment, mass, inertia):
+        self.lib.xdo_vv_update_velocity(_p(prm), _p(vel), _p(acc), _p(omega), _p(alpha), _p(force),
+                                        _p(moment), _p(mass), _p(inertia), _u(mass.shape[0]))
+
+    # ---- contacts ----
+    def p2p(self, prm, pos, vel, omega, force, moment, mass, sorted_, cstart, cend, cp):
+        self.lib.xdo_calculate_p2p(_p(prm), _p(pos), _p(vel), _p(omega), _p(force), _p(moment),
+                                   _p(mass), _p(sorted_), _p(cstart), _p(cend), _p(cp),
+                                   _u(pos.shape[0]))
+
+    def plane(self, prm, plane, pos, vel, omega, force, moment, mass, cp):
+        self.lib.xdo_plane_contact_force(_p(prm), _p(plane), _p(pos), _p(vel), _p(omega), _p(force),
+                                         _p(moment), _p(mass), _u(pos.shape[0]), _p(cp))
+
+    def cube(self, prm, planes6, pos, vel, omega, force, moment, mass, cp):
+        self.lib.xdo_cube_contact_force(_p(prm), _p(planes6), _p(pos), _p(vel), _p(omega),
+                                        _p(force), _p(moment), _p(mass), _u(pos.shape[0]), _p(cp))
+
+    def polygon(self, prm, poly, sphere, pmi, pos, vel, omega, force, moment, mass, sorted_,
+                cstart, cend, cp):
+        self.lib.xdo_particle_polygon_collision(_p(prm), _p(poly), _p(sphere), _p(pmi), _p(pos),
+                                                _p(vel), _p(omega), _p(force), _p(moment),
+                                                _p(mass), _p(sorted_), _p(cstart), _p(cend),
+                                                _p(cp), _u(pos.shape[0]))
+
+    def update_polygon(self, pmi, vlist, sphere, poly):
+        self.lib.xdo_update_polygon_object_data(_p(pmi), _p(vlist), _p(sphere), _p(poly),
+                                                _u(poly.shape[0]))
+
+    def pair_list(self, prm, pos, sorted_, cstart, cend, cap=None):
+        npt = pos.shape[0]
+        if cap is None:
+            cap = 64 * npt + 16
+        out = np.zeros((cap, 2), np.uint32)
+        n = self.lib.xdo_pair_list(_p(prm), _p(pos), _p(sorted_), _p(cstart), _p(cend), _u(npt),
+                                   _p(out), C.c_ulonglong(cap))
+        assert n <= cap, "pair list overflow"
+        return out[:n]
+
+    # ---- whole steps ----
+    def _scene_struct(self, sc, work):
+        s = _Scene()
+        C.memmove(s.prm, sc.params.ctypes.data, 112)
+        s.np = sc.np_
+        for f in ("pos", "vel", "acc", "omega", "alpha", "force", "moment", "mass", "inertia"):
+            setattr(s, f, getattr(sc, f).ctypes.data)
+        for f in ("hash", "index", "sorted", "cstart", "cend"):
+            setattr(s, f, work[f].ctypes.data)
+        s.cp_pp = sc.cp_pp.ctypes.data
+        s.nplanes = sc.planes.shape[0]
+        s.planes = sc.planes.ctypes.data if sc.planes.shape[0] else None
+        s.cp_planes = sc.cp_planes.ctypes.data if sc.planes.shape[0] else None
+        s.ntri = sc.ntri
+        if sc.ntri:
+            s.poly, s.sphere = sc.poly.ctypes.data, sc.sphere.ctypes.data
+            s.pmi, s.cp_poly = sc.pmi.ctypes.data, sc.cp_poly.ctypes.data
+        return s
+
+    @staticmethod
+    def _work(sc):
+        n = sc.np_ + sc.ntri
+        return {"hash": np.zeros(n, np.uint32), "index": np.zeros(n, np.uint32),
+                "sorted": np.zeros(n, np.uint32), "cstart": np.zeros(sc.ncell, np.uint32),
+                "cend": np.zeros(sc.ncell, np.uint32)}
+
+    def run(self, sc, nsteps: int, cpu_path: bool = False):
+        """Advance ``sc`` (in place) by nsteps whole steps; returns the grid work arrays."""
+        for a in ("pos", "vel", "acc", "omega", "alpha", "force", "moment", "mass", "inertia"):
+            assert getattr(sc, a).flags["C_CONTIGUOUS"]
+        work = self._work(sc)
+        s = self._scene_struct(sc, work)
+        fn = self.lib.xdo_cpu_run_steps if cpu_path else self.lib.xdo_run_steps
+        fn(C.byref(s), _u(nsteps))
+        return work
+
+
+class RefKernels:
+    """The reference's own kernels, compiled as host code (oracle/_ref)."""
+
+    def __init__(self, path: str = LIB_REF):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = C.CDLL(path)
+        for s in ("params", "plane", "polygon", "polygon_mass", "contact_property"):
+            getattr(self.lib, "xdref_sizeof_" + s).restype = _u
+
+    @staticmethod
+    def available(path: str = LIB_REF) -> bool:
+        return os.path.exists(path)
+
+    def sizes(self):
+        return {s: getattr(self.lib, "xdref_sizeof_" + s)() for s in
+                ("params", "plane", "polygon", "polygon_mass", "contact_property")}
+
+    def set_params(self, prm):
+        self.lib.xdref_set_params(_p(prm))
+
+    def hash_and_index(self, prm, pos, hash_, index):
+        self.set_params(prm)
+        self.lib.xdref_calculate_hash_and_index(_p(hash_), _p(index), _p(pos), _u(pos.shape[0]))
+
+    def hash_and_index_polysphere(self, prm, hash_, index, sid, sphere):
+        self.set_params(prm)
+        self.lib.xdref_calculate_hash_and_index_polysphere(_p(hash_), _p(index), _u(sid),
+                                                           _u(sphere.shape[0]), _p(sphere))
+
+    def reorder(self, hash_, index, cstart, cend, sorted_, n, ncell):
+        self.lib.xdref_reorder_and_find_cell_start(_p(hash_), _p(index), _p(cstart), _p(cend),
+                                                   _p(sorted_), _u(n), _u(ncell))
+
+    def detection(self, prm, pos, sphere=None):
+        npt = pos.shape[0]
+        nt = 0 if sphere is None else sphere.shape[0]
+        n = npt + nt
+        ncell = int(prm["ncell"])
+        h = np.zeros(n, np.uint32)
+        ix = np.zeros(n, np.uint32)
+        self.hash_and_index(prm, pos, h, ix)
+        if nt:
+            self.hash_and_index_polysphere(prm, h, ix, npt, sphere)
+        cs = np.zeros(ncell, np.uint32)
+        ce = np.zeros(ncell, np.uint32)
+        so = np.zeros(n, np.uint32)
+        self.reorder(h, ix, cs, ce, so, n, ncell)
+        return h, ix, cs, ce, so
+
+    def vv_position(self, prm, pos, vel, acc):
+        self.set_params(prm)
+        self.lib.xdref_vv_update_position(_p(pos), _p(vel), _p(acc), _u(pos.shape[0]))
+
+    def vv_velocity(self, prm, vel, acc, omega, alpha, force, moment, mass, inertia):
+        self.set_params(prm)
+        self.lib.xdref_vv_update_velocity(_p(vel), _p(acc), _p(omega), _p(alpha), _p(force),
+                                          _p(moment), _p(mass), _p(inertia), _u(mass.shape[0]))
+
+    def p2p(self, prm, pos, vel, omega, force, moment, mass, sorted_, cstart, cend, cp):
+        self.set_params(prm)
+        self.lib.xdref_calculate_p2p(C.c_int(1), _p(pos), _p(vel), _p(omega), _p(force),
+                                     _p(moment), _p(mass), _p(sorted_), _p(cstart), _p(cend),
+                                     _p(cp), _u(pos.shape[0]))
+
+    def plane(self, prm, plane, pos, vel, omega, force, moment, mass, cp):
+        self.set_params(prm)
+        self.lib.xdref_plane_contact_force(C.c_int(1), _p(plane), _p(pos), _p(vel), _p(omega),
+                                           _p(force), _p(moment), _p(mass), _u(pos.shape[0]),
+                                           _p(cp))
+
+    def cube(self, prm, planes6, pos, vel, omega, force, moment, mass, cp):
+        self.set_params(prm)
+        self.lib.xdref_cube_contact_force(C.c_int(1), _p(planes6), _p(pos), _p(vel), _p(omega),
+                                          _p(force), _p(moment), _p(mass), _u(pos.shape[0]),
+                                          _p(cp))
+
+    def polygon(self, prm, poly, sphere, pmi, pos, vel, omega, force, moment, mass, sorted_,
+                cstart, cend, cp):
+        self.set_params(prm)
+        self.lib.xdref_particle_polygon_collision(C.c_int(1), _p(poly), _p(sphere), _p(pmi),
+                                                  _p(pos), _p(vel), _p(omega), _p(force),
+                                                  _p(moment), _p(mass), _p(sorted_), _p(cstart),
+                                                  _p(cend), _p(cp), _u(pos.shape[0]))
+
+    def update_polygon(self, pmi, vlist, sphere, poly):
+        self.lib.xdref_update_polygon_object_data(_p(pmi), _p(vlist), _p(sphere), _p(poly),
+                                                  _u(poly.shape[0]))
+
+    def step(self, sc):
+        """One whole step in the reference's order, on the reference's kernels."""
+        prm = sc.params
+        self.vv_position(prm, sc.pos, sc.vel, sc.acc)
+        h, ix, cs, ce, so = self.detection(prm, sc.pos, sc.sphere if sc.ntri else None)
+        self.p2p(prm, sc.pos, sc.vel, sc.omega, sc.force, sc.moment, sc.mass, so, cs, ce, sc.cp_pp)
+        for i in range(sc.planes.shape[0]):
+            self.plane(prm, sc.planes[i:i + 1], sc.pos, sc.vel, sc.omega, sc.force, sc.moment,
+                       sc.mass, sc.cp_planes[i:i + 1])
+        if sc.ntri:
+            self.polygon(prm, sc.poly, sc.sphere, sc.pmi, sc.pos, sc.vel, sc.omega, sc.force,
+                         sc.moment, sc.mass, so, cs, ce, sc.cp_poly)
+        self.vv_velocity(prm, sc.vel, sc.acc, sc.omega, sc.alpha, sc.force, sc.moment, sc.mass,
+                         sc.inertia)
+        return h, ix, cs, ce, so

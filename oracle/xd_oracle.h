@@ -1,0 +1,164 @@
+/*
+ * xd_oracle: CPU restatement of the xdynamics DEM contact step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker for the CUDA library in
+ * metakonga_gb300/csrc: only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg load it.  The product never links or calls it.
+ *
+ * Two semantics are restated:
+ *   xdo_*      the reference's live FP64 GPU path (include/mphysics_cuda_impl.cuh,
+ *              source/mphysics_cuda_def.cu), evaluated in IEEE double with no
+ *              FMA contraction (build with -ffp-contract=off).  This is the
+ *              parity oracle.
+ *   xdo_cpu_*  the reference's CPU path (source/velocity_verlet.cpp,
+ *              source/neighborhood_cell.cpp, source/contactManager.cpp,
+ *              source/collision/contact*.cpp), single threaded like the
+ *              reference; used as the timed CPU baseline.
+ *
+ * Pinning: the xdo_* functions are checked bit for bit against the reference's
+ * own kernels compiled as host code (oracle/ref_driver.cpp -> oracle/_ref) and
+ * against the golden fixtures generated from them (tests/golden).
+ *
+ * All arrays use the reference's boundary layouts: pos = double4 (x,y,z,r),
+ * vel/acc/omega/alpha/force/moment = packed double3, mass/inertia = double.
+ * The structs below have the byte layout of the reference's device structs
+ * (include/mphysics_cuda_dec.cuh:17-88) so the same buffers feed the oracle,
+ * the reference build and the CUDA library.
+ */
+#ifndef XD_ORACLE_H
+#define XD_ORACLE_H
+
+#include <stdbool.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* include/mphysics_cuda_dec.cuh:17-30 (device_parameters), 112 bytes */
+typedef struct xdo_params {
+    bool rolling;
+    unsigned np;
+    unsigned nsphere;
+    unsigned ncell;
+    unsigned grid[3];
+    double dt;
+    double half2dt;
+    double cell_size;
+    double cohesion;
+    double gravity[3];
+    double world_origin[3];
+} xdo_params;
+
+/* include/mphysics_cuda_dec.cuh:78-88 (device_contact_property), 88 bytes */
+typedef struct xdo_contact_property {
+    double Ei, Ej, pri, prj, Gi, Gj, rest, fric, rfric, coh, sratio;
+} xdo_contact_property;
+
+/* include/mphysics_cuda_dec.cuh:43-55 (device_plane_info), 232 bytes */
+typedef struct xdo_plane {
+    double l1, l2;
+    double u1[3], u2[3], uw[3], xw[3], pa[3], pb[3], w2[3], w3[3], w4[3];
+} xdo_plane;
+
+/* include/mphysics_cuda_dec.cuh:32-41 (device_polygon_info), 152 bytes */
+typedef struct xdo_polygon {
+    int id;
+    double P[3], Q[3], R[3], V[3], W[3], N[3];
+} xdo_polygon;
+
+/* include/mphysics_cuda_dec.cuh:57-65 (device_polygon_mass_info), 160 bytes;
+ * ep is a CUDA double4 (16-byte aligned). */
+typedef struct xdo_polygon_mass {
+    double origin[3];
+    _Alignas(16) double ep[4];
+    double vel[3], omega[3], force[3], moment[3];
+} xdo_polygon_mass;
+
+unsigned xdo_sizeof_params(void);
+unsigned xdo_sizeof_plane(void);
+unsigned xdo_sizeof_polygon(void);
+unsigned xdo_sizeof_polygon_mass(void);
+unsigned xdo_sizeof_contact_property(void);
+
+/* ---- cell grid (impl:65-83, 137-212; def.cu:58-108) ---- */
+void xdo_grid_pos(const xdo_params* prm, const double p[3], int out[3]);
+unsigned xdo_grid_hash(const xdo_params* prm, const int c[3]);
+void xdo_calculate_hash_and_index(const xdo_params* prm, unsigned* hash, unsigned* index,
+                                  const double* pos, unsigned np);
+void xdo_calculate_hash_and_index_polysphere(const xdo_params* prm, unsigned* hash,
+                                             unsigned* index, unsigned sid, unsigned nsphere,
+                                             const double* sphere);
+void xdo_reorder_and_find_cell_start(unsigned* hash, unsigned* index, unsigned* cstart,
+                                     unsigned* cend, unsigned* sorted_index, unsigned n,
+                                     unsigned ncell);
+
+/* ---- integrator (impl:85-134) ---- */
+void xdo_vv_update_position(const xdo_params* prm, double* pos, const double* vel,
+                            const double* acc, unsigned np);
+void xdo_vv_update_velocity(const xdo_params* prm, double* vel, double* acc, double* omega,
+                            double* alpha, double* force, double* moment, const double* mass,
+                            const double* inertia, unsigned np);
+
+/* ---- contact forces (impl:214-621, 837-1021) ---- */
+void xdo_calculate_p2p(const xdo_params* prm, const double* pos, const double* vel,
+                       const double* omega, double* force, double* moment, const double* mass,
+                       const unsigned* sorted_index, const unsigned* cstart,
+                       const unsigned* cend, const xdo_contact_property* cp, unsigned np);
+void xdo_plane_contact_force(const xdo_params* prm, const xdo_plane* plane, const double* pos,
+                             const double* vel, const double* omega, double* force,
+                             double* moment, const double* mass, unsigned np,
+                             const xdo_contact_property* cp);
+void xdo_cube_contact_force(const xdo_params* prm, const xdo_plane* planes6, const double* pos,
+                            const double* vel, const double* omega, double* force,
+                            double* moment, const double* mass, unsigned np,
+                            const xdo_contact_property* cp);
+void xdo_particle_polygon_collision(const xdo_params* prm, const xdo_polygon* dpi,
+                                    const double* sphere, xdo_polygon_mass* dpmi,
+                                    const double* pos, const double* vel, const double* omega,
+                                    double* force, double* moment, const double* mass,
+                                    const unsigned* sorted_index, const unsigned* cstart,
+                                    const unsigned* cend, const xdo_contact_property* cp,
+                                    unsigned np);
+void xdo_update_polygon_object_data(const xdo_polygon_mass* dpmi, const double* vlist,
+                                    double* sphere, xdo_polygon* dpi, unsigned ntri);
+
+/* Contact pair list of one step: for every particle i (ascending) every
+ * partner k found by the 27-cell search with cdist > 0, in search order.
+ * Writes up to cap pairs as (i, k); returns the total number of pairs. */
+unsigned long long xdo_pair_list(const xdo_params* prm, const double* pos,
+                                 const unsigned* sorted_index, const unsigned* cstart,
+                                 const unsigned* cend, unsigned np, unsigned* pairs,
+                                 unsigned long long cap);
+
+/* ---- one whole step in the reference's order (dem_simulation.cpp:447-469,
+ *      contactManager.cpp:156-185) ---- */
+typedef struct xdo_scene {
+    xdo_params prm;
+    unsigned np;
+    double *pos, *vel, *acc, *omega, *alpha, *force, *moment, *mass, *inertia;
+    /* grid work arrays: n = np + ntri entries, ncell cells */
+    unsigned *hash, *index, *sorted, *cstart, *cend;
+    const xdo_contact_property* cp_pp;
+    unsigned nplanes;
+    const xdo_plane* planes;             /* in contact-name order */
+    const xdo_contact_property* cp_planes; /* one per plane */
+    unsigned ntri;
+    xdo_polygon* poly;
+    double* sphere;
+    xdo_polygon_mass* pmi;
+    const xdo_contact_property* cp_poly; /* one per polygon object */
+} xdo_scene;
+
+void xdo_step(xdo_scene* s);
+void xdo_run_steps(xdo_scene* s, unsigned nsteps);
+
+/* ---- the reference CPU path (timed baseline) ---- */
+void xdo_cpu_step(xdo_scene* s);
+void xdo_cpu_run_steps(xdo_scene* s, unsigned nsteps);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,59 @@
+"""Seeded test cases shared by the CPU and GPU tests (small enough for the oracle)."""
+import numpy as np
+
+from metakonga_gb300 import scenes
+from metakonga_gb300.layouts import CONTACT_PROPERTY
+
+
+def packed_scene(n_side=12, radius=0.0057, seed=3, vel_sigma=0.05, omega_sigma=5.0):
+    """A lattice of pitch 11 mm with r = 5.7 mm: every neighbour pair overlaps
+    by up to ~0.4 mm; random velocities and spins so that all force terms are
+    exercised.  Walls are the settle box's five planes, placed so that the
+    outer spheres touch them."""
+    sc = scenes.settle_box(seed=seed, n_side=n_side)
+    rng = np.random.Generator(np.random.MT19937(seed + 100))
+    sc.pos[:, 3] = radius
+    sc.vel[:] = rng.normal(0.0, vel_sigma, sc.vel.shape)
+    sc.omega[:] = rng.normal(0.0, omega_sigma, sc.omega.shape)
+    m, inertia = scenes.mass_inertia(sc.pos[:, 3])
+    sc.mass[:] = m
+    sc.inertia[:] = inertia
+    sc.force[:] = m[:, None] * np.array(scenes.GRAVITY)
+    sc.params["cell_size"] = 2.0 * radius
+    # box walls hugging the lattice so that outer particles overlap them
+    ext = (n_side - 1) * 0.011 / 2.0
+    centre = sc.pos[:, :3].mean(axis=0)
+    lo = centre - ext - radius * 0.9
+    hi = centre + ext + radius * 0.9
+    planes, names = scenes.box_walls(lo, hi, lid=True)
+    sc.planes, sc.plane_names = planes, names
+    sc.cp_planes = np.array([sc.cp_pp] * len(names), dtype=CONTACT_PROPERTY)
+    return sc
+
+
+def random_positions(n, lo, hi, rmin, rmax, seed):
+    rng = np.random.Generator(np.random.MT19937(seed))
+    pos = np.empty((n, 4))
+    pos[:, :3] = rng.uniform(lo, hi, size=(n, 3))
+    pos[:, 3] = rng.uniform(rmin, rmax, size=n)
+    return pos
+
+
+def small_drum(n=600, seed=5):
+    """A drum of radius 0.1 m with a coarse mesh; particles dropped next to the
+    wall so that many touch triangles (faces, edges and vertices)."""
+    sc = scenes.drum(n=n, seed=seed, radius=0.1, length=0.08, n_theta=48, n_z=4, n_ring=6,
+                     rmin=0.004, rmax=0.006, fill_height=0.03)
+    rng = np.random.Generator(np.random.MT19937(seed + 7))
+    # push particles outwards so that they overlap the cylinder wall
+    xz = sc.pos[:, [0, 2]]
+    r = np.linalg.norm(xz, axis=1)
+    target = 0.1 - sc.pos[:, 3] * rng.uniform(0.6, 1.05, size=n)
+    outer = r > 0.05
+    scale = np.where(outer, target / np.maximum(r, 1e-9), 1.0)
+    sc.pos[:, 0] *= scale
+    sc.pos[:, 2] *= scale
+    sc.vel[:] = rng.normal(0.0, 0.05, sc.vel.shape)
+    sc.omega[:] = rng.normal(0.0, 5.0, sc.omega.shape)
+    sc.pmi["vel"] = (0.01, -0.02, 0.005)
+    return sc
