@@ -199,7 +199,11 @@ def polydisperse_box(n: int = 1_000_000, seed: int = 7, rmin: float = 0.002, rma
     hi = np.array([bx / 2, by / 2, bz])
     pts = np.empty((0, 3))
     rad = np.empty((0,))
+    rounds = 0
     while pts.shape[0] < n:
+        rounds += 1
+        if rounds > 200:
+            raise ValueError("polydisperse_box: too dense for rejection sampling")
         m = int((n - pts.shape[0]) * 1.15) + 64
         r_new = rng.uniform(rmin, rmax, size=m)
         p_new = rng.uniform(0.0, 1.0, size=(m, 3)) * (hi - lo - 2 * r_new[:, None]) + lo + r_new[:, None]
@@ -327,7 +331,11 @@ def drum(n: int = 4000, seed: int = 11, rmin: float = 0.003, rmax: float = 0.005
     pts = np.empty((0, 3))
     rad = np.empty((0,))
     fh = fill_height if fill_height is not None else inner
+    rounds = 0
     while pts.shape[0] < n:
+        rounds += 1
+        if rounds > 200:
+            raise ValueError("drum: too dense for rejection sampling; raise fill_height")
         m = int((n - pts.shape[0]) * 1.3) + 64
         r_new = rng.uniform(rmin, rmax, size=m)
         x = rng.uniform(-inner, inner, size=m)

@@ -43,7 +43,7 @@ def small_drum(n=600, seed=5):
     """A drum of radius 0.1 m with a coarse mesh; particles dropped next to the
     wall so that many touch triangles (faces, edges and vertices)."""
     sc = scenes.drum(n=n, seed=seed, radius=0.1, length=0.08, n_theta=48, n_z=4, n_ring=6,
-                     rmin=0.004, rmax=0.006, fill_height=0.03)
+                     rmin=0.004, rmax=0.006, fill_height=0.08)
     rng = np.random.Generator(np.random.MT19937(seed + 7))
     # push particles outwards so that they overlap the cylinder wall
     xz = sc.pos[:, [0, 2]]
