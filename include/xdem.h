@@ -157,6 +157,25 @@ int xd_reorder_and_find_cell_start(unsigned* hash, unsigned* index, unsigned* cs
                                    unsigned* cend, unsigned* sorted_index, unsigned n,
                                    unsigned ncell, void* stream);
 
+/* Allocation-free variant of xd_reorder_and_find_cell_start; no counterpart
+ * in the reference.  For callers that may not allocate device memory while
+ * they run (an application that hands out all device memory from its own
+ * pool at start-up, or a process held to a fixed memory budget): the sort
+ * scratch comes from a fixed device array inside the library instead of
+ * cudaMalloc, and the call allocates nothing.  Limits and rules:
+ *   - at most XD_NOALLOC_MAX_ENTRIES entries (n); larger n -> XD_ERR_CAPACITY;
+ *   - the array (about 8.3 MB) stays on every device that loads the library
+ *     until the process exits;
+ *   - all calls share the array: calls that overlap on the GPU (other
+ *     streams or host threads) race, so serialise them;
+ *   - a device's first call looks up the array's device address, so make it
+ *     before any stream capture on that device.
+ * Same arguments, results and status codes as xd_reorder_and_find_cell_start. */
+#define XD_NOALLOC_MAX_ENTRIES (1u << 20)
+int xd_reorder_and_find_cell_start_noalloc(unsigned* hash, unsigned* index, unsigned* cstart,
+                                           unsigned* cend, unsigned* sorted_index, unsigned n,
+                                           unsigned ncell, void* stream);
+
 /* Stable LSD radix sort of 32-bit (key, value) pairs by the low key_bits of
  * the key (the sort inside cu_reorderDataAndFindCellStart, def.cu:92-94,
  * where the reference calls thrust::sort_by_key).  In place. */

@@ -45,6 +45,7 @@ _SIGS = {
     "xd_calculate_hash_and_index": [vp, vp, vp, u32, vp],
     "xd_calculate_hash_and_index_polysphere": [vp, vp, u32, u32, vp, vp],
     "xd_reorder_and_find_cell_start": [vp] * 5 + [u32, u32, vp],
+    "xd_reorder_and_find_cell_start_noalloc": [vp] * 5 + [u32, u32, vp],
     "xd_radix_sort_pairs": [vp, vp, u32, u32, vp],
     "xd_calculate_p2p": [i32] + [vp] * 10 + [u32, vp],
     "xd_plane_contact_force": [i32] + [vp] * 7 + [u32, vp, vp],
