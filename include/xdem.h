@@ -264,7 +264,10 @@ int xd_pair_list(const double* pos, const unsigned* sorted_index, const unsigned
 typedef struct xd_scene xd_scene;
 
 enum {
-    XD_MODE_FP64 = 0   /* the reference's FP64 arithmetic and loop order */
+    XD_MODE_FP64 = 0,  /* the reference's FP64 arithmetic and loop order */
+    XD_MODE_MIXED = 1  /* FP64 state and integration, exact integer contact
+                          decisions, FP32 contact forces; the scene's own grid
+                          (cell 2 r_max, sized to the initial bounding box) */
 };
 
 typedef struct xd_scene_desc {
@@ -327,12 +330,28 @@ int xd_scene_step(xd_scene* scene, unsigned nsteps, int check, void* stream);
 
 /* Per-phase timing with CUDA events recorded on the step's stream.  Phases:
  * 0 VV update, 1 hash, 2 sort + cell ranges, 3 particle-particle,
- * 4 planes, 5 triangles.  xd_scene_phase_times synchronises the events and
- * returns the summed milliseconds and launch counts since timing was last
- * enabled. */
-#define XD_SCENE_PHASES 6
+ * 4 planes, 5 triangles, 6 reorder (mixed mode).  xd_scene_phase_times
+ * synchronises the events and returns the summed milliseconds and launch
+ * counts since timing was last enabled. */
+#define XD_SCENE_PHASES 7
 int xd_scene_set_timing(xd_scene* scene, int enable);
 int xd_scene_phase_times(xd_scene* scene, double* ms, unsigned long long* launches);
+
+/* Contact forces and moments (without gravity) of the current state, in the
+ * original particle order, written to host arrays [np][3]: the
+ * particle-particle and wall terms that the next step would add.  Diagnostic
+ * call (synchronous); the state is not advanced. */
+int xd_scene_eval_contacts(xd_scene* scene, double* force, double* moment, void* stream);
+
+/* Contact partners of the current state (mixed mode): for every particle i
+ * (original order) counts[i] partners written to partners[i * cap + k] as
+ * original indices, in search order.  Diagnostic call (synchronous). */
+int xd_scene_pair_list(xd_scene* scene, unsigned cap, unsigned* counts, unsigned* partners,
+                       void* stream);
+
+/* Mixed-mode counters of the last contact pass: [0] particles near a wall,
+ * [1] pairs decided by the FP64 guard-band test. */
+int xd_scene_counters(xd_scene* scene, unsigned long long out[4], void* stream);
 
 /* Number of kernel launches one xd_scene_step of nsteps issues. */
 unsigned long long xd_scene_launches(xd_scene* scene, unsigned nsteps);

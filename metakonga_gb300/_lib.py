@@ -67,6 +67,9 @@ _SIGS = {
     "xd_scene_step": [vp, u32, i32, vp],
     "xd_scene_launches": [vp, u32],
     "xd_scene_set_timing": [vp, i32],
+    "xd_scene_eval_contacts": [vp, vp, vp, vp],
+    "xd_scene_pair_list": [vp, u32, vp, vp, vp],
+    "xd_scene_counters": [vp, vp, vp],
     "xd_scene_phase_times": [vp, vp, vp],
 }
 _RESTYPES = {"xd_version": C.c_char_p, "xd_status_string": C.c_char_p, "xd_clear_error": None,

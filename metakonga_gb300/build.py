@@ -34,7 +34,7 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 NO_FMAD = {"xd_grid.cu", "xd_integrate.cu", "xd_contact64.cu"}
 
 CUDA_SOURCES = ["xd_capi.cu", "xd_sort.cu", "xd_grid.cu", "xd_integrate.cu", "xd_contact64.cu",
-                "xd_scene.cu", "xd_noalloc.cu"]
+                "xd_scene.cu", "xd_noalloc.cu", "xd_mixed.cu"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,34 @@
+// Internal interface of the mixed-precision scene path (xd_mixed.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "xd_internal.cuh"
+
+namespace xd {
+
+// Phase hooks for event timing: begin/end of phase p on stream q.
+struct Phases {
+    void* ctx = nullptr;
+    void (*fn)(void*, int, bool, cudaStream_t) = nullptr;
+    void begin(int p, cudaStream_t q) const { if (fn) fn(ctx, p, true, q); }
+    void end(int p, cudaStream_t q) const { if (fn) fn(ctx, p, false, q); }
+};
+
+struct MixedScene;
+
+int mixed_create(const xd_scene_desc& d, MixedScene** out);
+void mixed_destroy(MixedScene* s);
+int mixed_upload(MixedScene* s, const double* pos, const double* vel, const double* acc,
+                 const double* omega, const double* alpha, const double* mass,
+                 const double* inertia, cudaStream_t q);
+int mixed_download(MixedScene* s, double* pos, double* vel, double* acc, double* omega,
+                   double* alpha, double* force, double* moment, cudaStream_t q);
+int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph);
+unsigned long long mixed_launches(MixedScene* s, unsigned nsteps);
+int mixed_eval_contacts(MixedScene* s, double* force, double* moment, cudaStream_t q);
+int mixed_pair_list(MixedScene* s, unsigned cap_per_particle, unsigned* counts, unsigned* partners,
+                    cudaStream_t q);
+int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q);
+
+}  // namespace xd

@@ -1,0 +1,187 @@
+// FP64 contact physics shared by the plain (reference-arithmetic) kernels
+// and the FP64 wall pass of the mixed form: getConstant (TCM = 1),
+// cohesionForce, DHSModel, the finite-plane region test and the
+// closest point on a triangle, each restating the cited reference lines.
+#pragma once
+
+#include "xd_internal.cuh"
+
+namespace xd {
+
+struct Fc {
+    double kn, vn, ks, vs, mu;
+};
+
+struct PairConst {
+    double c43Eeq, one_b2, sratio, fric, coh, Ei, Ej, pri, prj;
+};
+
+__device__ __forceinline__ PairConst load_pair_const(const xd_contact_property* cp)
+{
+    PairConst c;
+    double Ei = __ldg(&cp->Ei), Ej = __ldg(&cp->Ej), pri = __ldg(&cp->pri), prj = __ldg(&cp->prj);
+    double Eeq = (Ei * Ej) / (Ei * (1 - prj * prj) + Ej * (1 - pri * pri));
+    double beta = (M_PI / log(__ldg(&cp->rest)));
+    c.c43Eeq = (4.0 / 3.0) * Eeq;
+    c.one_b2 = 1.0 + beta * beta;
+    c.sratio = __ldg(&cp->sratio);
+    c.fric = __ldg(&cp->fric);
+    c.coh = __ldg(&cp->coh);
+    c.Ei = Ei;
+    c.Ej = Ej;
+    c.pri = pri;
+    c.prj = prj;
+    return c;
+}
+
+// getConstant, TCM = 1 (impl:214-256)
+__device__ __forceinline__ Fc get_constant(const PairConst& pc, double ir, double jr, double im,
+                                           double jm)
+{
+    Fc c;
+    double Meq = jm != 0.0 ? (im * jm) / (im + jm) : im;
+    double Req = jr != 0.0 ? (ir * jr) / (ir + jr) : ir;
+    c.kn = pc.c43Eeq * sqrt(Req);
+    c.vn = sqrt((4.0 * Meq * c.kn) / pc.one_b2);
+    c.ks = c.kn * pc.sratio;
+    c.vs = c.vn * pc.sratio;
+    c.mu = pc.fric;
+    return c;
+}
+
+// cohesionForce (impl:259-279)
+__device__ __forceinline__ double cohesion_force(double ri, double rj, double Ei, double Ej,
+                                                 double pri, double prj, double coh, double Fn)
+{
+    double cf = 0.0;
+    if (coh != 0.0) {
+        double req = (ri * rj / (ri + rj));
+        double Eeq = ((1.0 - pri * pri) / Ei) + ((1.0 - prj * prj) / Ej);
+        double rcp = (3.0 * req * (-Fn)) / (4.0 * (1.0 / Eeq));
+        double rc = pow(rcp, 1.0 / 3.0);
+        double Ac = M_PI * rc * rc;
+        cf = coh * Ac;
+    }
+    return cf;
+}
+
+// DHSModel (impl:379-401); Ft and M are in/out (kept across pairs).
+__device__ __forceinline__ void dhs(const Fc& c, double ir, double jr, double Ei, double Ej,
+                                    double pri, double prj, double coh, double cdist, d3 dv,
+                                    d3 unit, double dt, d3& Ft, d3& Fn, d3& M)
+{
+    double fsn = -c.kn * (cdist * sqrt(cdist));
+    double fdn = c.vn * dot(dv, unit);
+    double fca = cohesion_force(ir, jr, Ei, Ej, pri, prj, coh, fsn);
+    Fn = (fsn + fca + fdn) * unit;
+    d3 e = dv - dot(dv, unit) * unit;
+    double mag_e = length(e);
+    if (mag_e != 0.0) {
+        d3 sh = e / mag_e;
+        double ds = mag_e * dt;
+        Ft = fmin(c.ks * ds + c.vs * (dot(dv, sh)), c.mu * length(Fn)) * sh;
+        M = cross(ir * unit, Ft);
+    }
+}
+
+struct PlaneD {
+    double l1, l2;
+    d3 u1, u2, uw, xw, w2, w3, w4;
+};
+
+__device__ __forceinline__ PlaneD load_plane(const xd_plane_info* p)
+{
+    PlaneD q;
+    q.l1 = __ldg(&p->l1);
+    q.l2 = __ldg(&p->l2);
+    q.u1 = mk(__ldg(p->u1), __ldg(p->u1 + 1), __ldg(p->u1 + 2));
+    q.u2 = mk(__ldg(p->u2), __ldg(p->u2 + 1), __ldg(p->u2 + 2));
+    q.uw = mk(__ldg(p->uw), __ldg(p->uw + 1), __ldg(p->uw + 2));
+    q.xw = mk(__ldg(p->xw), __ldg(p->xw + 1), __ldg(p->xw + 2));
+    q.w2 = mk(__ldg(p->w2), __ldg(p->w2 + 1), __ldg(p->w2 + 2));
+    q.w3 = mk(__ldg(p->w3), __ldg(p->w3 + 1), __ldg(p->w3 + 2));
+    q.w4 = mk(__ldg(p->w4), __ldg(p->w4 + 1), __ldg(p->w4 + 2));
+    return q;
+}
+
+__device__ __forceinline__ int sgn(double L) { return L < 0 ? -1 : 1; }
+
+// particle_plane_contact_detection (impl:487-570); pow(x, 2.0) is x * x
+// (IEEE: the correctly rounded square).
+__device__ __forceinline__ double plane_detection(const PlaneD& pe, d3 xp, d3 wp, d3& u, double r)
+{
+    double a_l1 = (wp.x - pe.l1) * (wp.x - pe.l1);
+    double b_l2 = (wp.y - pe.l2) * (wp.y - pe.l2);
+    double sqa = wp.x * wp.x;
+    double sqb = wp.y * wp.y;
+    double sqc = wp.z * wp.z;
+    double sqr = r * r;
+    if (fabs(wp.z) < r && (wp.x > 0 && wp.x < pe.l1) && (wp.y > 0 && wp.y < pe.l2)) {
+        d3 dp = xp - pe.xw;
+        d3 uu = pe.uw / length(pe.uw);
+        int pp = -sgn(dot(dp, pe.uw));
+        u = (double)pp * uu;
+        return r - fabs(dot(dp, u));
+    }
+    if (wp.x < 0 && wp.y < 0 && (sqa + sqb + sqc) < sqr) {
+        d3 X = xp - pe.xw; double h = length(X); u = X / h; return r - h;
+    } else if (wp.x > pe.l1 && wp.y < 0 && (a_l1 + sqb + sqc) < sqr) {
+        d3 X = xp - pe.w2; double h = length(X); u = X / h; return r - h;
+    } else if (wp.x > pe.l1 && wp.y > pe.l2 && (a_l1 + b_l2 + sqc) < sqr) {
+        d3 X = xp - pe.w3; double h = length(X); u = X / h; return r - h;
+    } else if (wp.x < 0 && wp.y > pe.l2 && (sqa + b_l2 + sqc) < sqr) {
+        d3 X = xp - pe.w4; double h = length(X); u = X / h; return r - h;
+    }
+    d3 X, wj;
+    if ((wp.x > 0 && wp.x < pe.l1) && wp.y < 0 && (sqb + sqc) < sqr) {
+        X = xp - pe.xw; wj = pe.w2 - pe.xw;
+    } else if ((wp.x > 0 && wp.x < pe.l1) && wp.y > pe.l2 && (b_l2 + sqc) < sqr) {
+        X = xp - pe.w4; wj = pe.w3 - pe.w4;
+    } else if ((wp.x > 0 && wp.y < pe.l2) && wp.x < 0 && (sqr + sqc) < sqr) {
+        X = xp - pe.xw; wj = pe.w4 - pe.xw;
+    } else if ((wp.x > 0 && wp.y < pe.l2) && wp.x > pe.l1 && (a_l1 + sqc) < sqr) {
+        X = xp - pe.w2; wj = pe.w3 - pe.w2;
+    } else {
+        return -1.0;
+    }
+    d3 us = wj / length(wj);
+    d3 hs = X - (dot(X, us)) * us;
+    double h = length(hs);
+    u = (-hs) / h;
+    return r - h;
+}
+
+// closestPtPointTriangle (impl:837-899)
+__device__ __forceinline__ d3 closest_pt_triangle(d3 a, d3 b, d3 c, d3 p)
+{
+    d3 ab = b - a, ac = c - a, ap = p - a;
+    double d1 = dot(ab, ap), d2 = dot(ac, ap);
+    if (d1 <= 0.0 && d2 <= 0.0) return a;
+    d3 bp = p - b;
+    double d3_ = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3_ >= 0.0 && d4 <= d3_) return b;
+    double vc = d1 * d4 - d3_ * d2;
+    if (vc <= 0.0 && d1 >= 0.0 && d3_ <= 0.0) {
+        double v = d1 / (d1 - d3_);
+        return a + v * ab;
+    }
+    d3 cp = p - c;
+    double d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d6 >= 0.0 && d5 <= d6) return c;
+    double vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
+        double w = d2 / (d2 - d6);
+        return a + w * ac;
+    }
+    double va = d3_ * d6 - d5 * d4;
+    if (va <= 0.0 && (d4 - d3_) >= 0.0 && (d5 - d6) >= 0.0) {
+        double w = (d4 - d3_) / ((d4 - d3_) + (d5 - d6));
+        return b + w * (c - b);
+    }
+    double denom = 1.0 / (va + vb + vc);
+    double v = vb * denom;
+    double w = vc * denom;
+    return (a + v * ab) + w * ac;
+}
+
+}  // namespace xd

@@ -8,6 +8,7 @@
 
 #include "xd_grid.cuh"
 #include "xd_internal.cuh"
+#include "xd_mixed.cuh"
 
 using namespace xd;
 
@@ -42,6 +43,8 @@ struct xd_scene {
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> spans;
     double phase_ms[XD_SCENE_PHASES] = {};
     unsigned long long phase_n[XD_SCENE_PHASES] = {};
+    cudaEvent_t pending[XD_SCENE_PHASES] = {};
+    MixedScene* mixed = nullptr;
 };
 
 namespace {
@@ -73,6 +76,8 @@ int d2h(void* dst, const void* src, size_t bytes, cudaStream_t st)
 
 void free_scene(xd_scene* s)
 {
+    if (s->mixed) mixed_destroy(s->mixed);
+    s->mixed = nullptr;
     for (void* p : s->allocs) cudaFree(p);
     s->allocs.clear();
     for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
@@ -87,6 +92,30 @@ cudaEvent_t next_event(xd_scene* s)
         s->ev_pool.push_back(e);
     }
     return s->ev_pool[s->ev_used++];
+}
+
+// Phase hook for the mixed path.
+void phase_hook(void* ctx, int phase, bool begin, cudaStream_t q)
+{
+    xd_scene* s = static_cast<xd_scene*>(ctx);
+    if (!s->timing || phase < 0 || phase >= XD_SCENE_PHASES) return;
+    cudaEvent_t e = next_event(s);
+    if (!e) return;
+    cudaEventRecord(e, q);
+    if (begin) {
+        s->pending[phase] = e;
+    } else if (s->pending[phase]) {
+        s->spans.push_back({ phase, { s->pending[phase], e } });
+        s->pending[phase] = nullptr;
+    }
+}
+
+Phases phases_of(xd_scene* s)
+{
+    Phases p;
+    p.ctx = s;
+    p.fn = phase_hook;
+    return p;
 }
 
 // Records a [begin, end) event pair around one phase when timing is on.
@@ -117,7 +146,22 @@ int xd_scene_create(const xd_scene_desc* d, xd_scene** out)
 {
     if (!d || !out) return set_error(XD_ERR_INVALID, "scene_create: null argument");
     *out = nullptr;
-    if (d->mode != XD_MODE_FP64) return set_error(XD_ERR_INVALID, "scene_create: unknown mode %d", d->mode);
+    if (d->mode != XD_MODE_FP64 && d->mode != XD_MODE_MIXED)
+        return set_error(XD_ERR_INVALID, "scene_create: unknown mode %d", d->mode);
+    if (d->mode == XD_MODE_MIXED) {
+        xd_scene* s = new (std::nothrow) xd_scene();
+        if (!s) return set_error(XD_ERR_NOMEM, "scene_create: host allocation");
+        s->desc = *d;
+        s->np = d->np;
+        s->nplanes = d->nplanes;
+        int st = mixed_create(*d, &s->mixed);
+        if (st != XD_OK) {
+            delete s;
+            return st;
+        }
+        *out = s;
+        return XD_OK;
+    }
     const xd_device_parameters& h = d->params;
     unsigned gx = h.grid_size[0], gy = h.grid_size[1], gz = h.grid_size[2];
     if (!gx || !gy || !gz || (gx & (gx - 1)) || (gy & (gy - 1)) || (gz & (gz - 1)))
@@ -221,6 +265,7 @@ int xd_scene_upload(xd_scene* s, const double* pos, const double* vel, const dou
 {
     if (!s) return set_error(XD_ERR_INVALID, "scene_upload: null scene");
     cudaStream_t q = static_cast<cudaStream_t>(stream);
+    if (s->mixed) return mixed_upload(s->mixed, pos, vel, acc, omega, alpha, mass, inertia, q);
     size_t n = s->np;
     int st = XD_OK;
     auto A = [&](int r) { if (st == XD_OK) st = r; };
@@ -242,6 +287,7 @@ int xd_scene_download(xd_scene* s, double* pos, double* vel, double* acc, double
 {
     if (!s) return set_error(XD_ERR_INVALID, "scene_download: null scene");
     cudaStream_t q = static_cast<cudaStream_t>(stream);
+    if (s->mixed) return mixed_download(s->mixed, pos, vel, acc, omega, alpha, force, moment, q);
     size_t n = s->np;
     int st = XD_OK;
     auto A = [&](int r) { if (st == XD_OK) st = r; };
@@ -261,6 +307,7 @@ int xd_scene_device_state(xd_scene* s, double** pos, double** vel, double** acc,
                           double** inertia)
 {
     if (!s) return set_error(XD_ERR_INVALID, "scene_device_state: null scene");
+    if (s->mixed) return set_error(XD_ERR_STATE, "scene_device_state: not available in mixed mode (state is kept in cell order)");
     if (pos) *pos = s->pos;
     if (vel) *vel = s->vel;
     if (acc) *acc = s->acc;
@@ -277,6 +324,7 @@ int xd_scene_device_grid(xd_scene* s, unsigned** hash, unsigned** index, unsigne
                          unsigned** cstart, unsigned** cend)
 {
     if (!s) return set_error(XD_ERR_INVALID, "scene_device_grid: null scene");
+    if (s->mixed) return set_error(XD_ERR_STATE, "scene_device_grid: not available in mixed mode (state is kept in cell order)");
     if (hash) *hash = s->hash;
     if (index) *index = s->index;
     if (sorted) *sorted = s->sorted;
@@ -289,6 +337,7 @@ int xd_scene_download_grid(xd_scene* s, unsigned* hash, unsigned* index, unsigne
                            unsigned* cstart, unsigned* cend, void* stream)
 {
     if (!s) return set_error(XD_ERR_INVALID, "scene_download_grid: null scene");
+    if (s->mixed) return set_error(XD_ERR_STATE, "scene_download_grid: not available in mixed mode (state is kept in cell order)");
     cudaStream_t q = static_cast<cudaStream_t>(stream);
     size_t ng = (size_t)s->np + s->ntri;
     int st = XD_OK;
@@ -322,6 +371,68 @@ int xd_scene_get_bodies(xd_scene* s, xd_polygon_mass_info* pmi, void* stream)
     return st;
 }
 
+int xd_scene_eval_contacts(xd_scene* s, double* force, double* moment, void* stream)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_eval_contacts: null scene");
+    cudaStream_t q = static_cast<cudaStream_t>(stream);
+    if (s->mixed) return mixed_eval_contacts(s->mixed, force, moment, q);
+    // FP64 mode: contacts added onto zeroed force/moment copies
+    const size_t n = s->np, ng = (size_t)s->np + s->ntri;
+    double *f0 = nullptr, *m0 = nullptr;
+    int st = cuda_status(cudaMalloc(&f0, sizeof(double) * 6 * (n ? n : 1)), "scene_eval_contacts");
+    if (st != XD_OK) return st;
+    m0 = f0 + 3 * n;
+    auto A = [&](int r) { if (st == XD_OK) st = r; };
+    A(cuda_status(cudaMemsetAsync(f0, 0, sizeof(double) * 6 * n, q), "scene_eval_contacts"));
+    const Params& P = s->P;
+    A(launch_hash(P, s->hash, s->index, s->pos, s->np, 0, q));
+    if (s->ntri) A(launch_hash(P, s->hash, s->index, s->sphere, s->ntri, s->np, q));
+    if (st == XD_OK)
+        A(reorder_and_find_cell_start(s->hash, s->index, s->cstart, s->cend, s->sorted, (unsigned)ng,
+                                      s->ncell, s->scratch, q, false));
+    if (st == XD_OK)
+        A(launch_p2p(P, s->pos, s->vel, s->omega, f0, m0, s->mass, s->sorted, s->cstart, s->cend,
+                     s->cp_pp, s->np, q));
+    if (st == XD_OK && s->nplanes)
+        A(launch_planes(P, s->planes, s->cp_planes, 1, s->nplanes, s->pos, s->vel, s->omega, f0, m0,
+                        s->mass, s->np, q));
+    if (st == XD_OK && s->ntri) {
+        // the reaction on the bodies is not part of this diagnostic: work on a copy
+        xd_polygon_mass_info* tmp = nullptr;
+        A(cuda_status(cudaMalloc(&tmp, sizeof(xd_polygon_mass_info) * s->nbodies), "scene_eval_contacts"));
+        if (st == XD_OK) {
+            A(cuda_status(cudaMemcpyAsync(tmp, s->pmi, sizeof(xd_polygon_mass_info) * s->nbodies,
+                                          cudaMemcpyDeviceToDevice, q), "scene_eval_contacts"));
+            A(launch_polygon(P, s->poly, tmp, s->pos, s->vel, s->omega, f0, m0, s->mass, s->sorted,
+                             s->cstart, s->cend, s->cp_poly, s->nbodies, s->poly_scratch, q));
+            cudaStreamSynchronize(q);
+            cudaFree(tmp);
+        }
+    }
+    if (st == XD_OK && force) A(d2h(force, f0, sizeof(double) * 3 * n, q));
+    if (st == XD_OK && moment) A(d2h(moment, m0, sizeof(double) * 3 * n, q));
+    if (st == XD_OK) A(cuda_status(cudaStreamSynchronize(q), "scene_eval_contacts"));
+    cudaFree(f0);
+    return st;
+}
+
+int xd_scene_pair_list(xd_scene* s, unsigned cap, unsigned* counts, unsigned* partners, void* stream)
+{
+    if (!s || !counts || !partners) return set_error(XD_ERR_INVALID, "scene_pair_list: null argument");
+    if (!s->mixed) return set_error(XD_ERR_STATE, "scene_pair_list: mixed mode only (use xd_pair_list)");
+    return mixed_pair_list(s->mixed, cap, counts, partners, static_cast<cudaStream_t>(stream));
+}
+
+int xd_scene_counters(xd_scene* s, unsigned long long out[4], void* stream)
+{
+    if (!s || !out) return set_error(XD_ERR_INVALID, "scene_counters: null argument");
+    if (!s->mixed) {
+        for (int i = 0; i < 4; ++i) out[i] = 0;
+        return XD_OK;
+    }
+    return mixed_counters(s->mixed, out, static_cast<cudaStream_t>(stream));
+}
+
 int xd_scene_set_timing(xd_scene* s, int enable)
 {
     if (!s) return set_error(XD_ERR_INVALID, "scene_set_timing: null scene");
@@ -332,6 +443,7 @@ int xd_scene_set_timing(xd_scene* s, int enable)
     for (int i = 0; i < XD_SCENE_PHASES; ++i) {
         s->phase_ms[i] = 0.0;
         s->phase_n[i] = 0;
+        s->pending[i] = nullptr;
     }
     return cuda_status(e, "scene_set_timing");
 }
@@ -360,6 +472,7 @@ int xd_scene_phase_times(xd_scene* s, double* ms, unsigned long long* launches)
 unsigned long long xd_scene_launches(xd_scene* s, unsigned nsteps)
 {
     if (!s || nsteps == 0) return 0;
+    if (s->mixed) return mixed_launches(s->mixed, nsteps);
     unsigned ng = s->np + s->ntri;
     unsigned passes = (key_bits_for(s->ncell) + 7) / 8;
     unsigned long long per = 0;
@@ -381,6 +494,11 @@ int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
     if (!s) return set_error(XD_ERR_INVALID, "scene_step: null scene");
     if (nsteps == 0) return XD_OK;
     cudaStream_t q = static_cast<cudaStream_t>(stream);
+    if (s->mixed) {
+        int r = mixed_step(s->mixed, nsteps, q, phases_of(s));
+        if (r == XD_OK && check) r = cuda_status(cudaStreamSynchronize(q), "scene_step");
+        return r;
+    }
     const Params& P = s->P;
     const unsigned np = s->np, ng = s->np + s->ntri;
     int st = XD_OK;

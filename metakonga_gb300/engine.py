@@ -14,6 +14,7 @@ from . import _lib
 from ._lib import call
 
 MODE_FP64 = 0
+MODE_MIXED = 1
 
 
 class _Desc(C.Structure):
@@ -115,7 +116,7 @@ class DeviceScene:
     def step(self, nsteps: int = 1, check: bool = False, stream: int = 0):
         call("xd_scene_step", self.handle, nsteps, 1 if check else 0, stream)
 
-    PHASES = ("vv", "hash", "sort_cells", "p2p", "planes", "triangles")
+    PHASES = ("vv", "hash", "sort_cells", "p2p", "planes", "triangles", "reorder")
 
     def set_timing(self, enable: bool = True):
         call("xd_scene_set_timing", self.handle, 1 if enable else 0)
@@ -125,6 +126,29 @@ class DeviceScene:
         n = np.zeros(len(self.PHASES), np.uint64)
         call("xd_scene_phase_times", self.handle, ms.ctypes.data, n.ctypes.data)
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.PHASES)}
+
+    def eval_contacts(self, stream: int = 0):
+        """Contact force/moment (no gravity) of the current state, original order."""
+        f = np.empty((self.np, 3))
+        m = np.empty((self.np, 3))
+        call("xd_scene_eval_contacts", self.handle, f.ctypes.data, m.ctypes.data, stream)
+        return f, m
+
+    def pair_list(self, cap: int = 32, stream: int = 0):
+        """(i, k) contact pairs of the current state (mixed mode), original ids."""
+        counts = np.zeros(self.np, np.uint32)
+        partners = np.zeros((self.np, cap), np.uint32)
+        call("xd_scene_pair_list", self.handle, cap, counts.ctypes.data, partners.ctypes.data, stream)
+        assert counts.max(initial=0) <= cap, "pair capacity exceeded"
+        i = np.repeat(np.arange(self.np, dtype=np.uint32), counts)
+        k = np.concatenate([partners[a, :c] for a, c in enumerate(counts)]) if counts.sum() else \
+            np.zeros(0, np.uint32)
+        return np.stack([i, k], axis=1)
+
+    def counters(self, stream: int = 0):
+        out = np.zeros(4, np.uint64)
+        call("xd_scene_counters", self.handle, out.ctypes.data, stream)
+        return {"near_wall": int(out[0]), "fp64_decisions": int(out[1])}
 
     def launches(self, nsteps: int) -> int:
         return int(_lib.lib().xd_scene_launches(self.handle, nsteps))

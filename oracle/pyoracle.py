@@ -62,7 +62,7 @@ class Oracle:
                      "xdo_vv_update_velocity", "xdo_calculate_p2p", "xdo_plane_contact_force",
                      "xdo_cube_contact_force", "xdo_particle_polygon_collision",
                      "xdo_update_polygon_object_data", "xdo_step", "xdo_run_steps",
-                     "xdo_cpu_step", "xdo_cpu_run_steps"):
+                     "xdo_cpu_step", "xdo_cpu_run_steps", "xdo_contact_magnitudes"):
             getattr(L, name).restype = None
         L.xdo_pair_list.restype = C.c_ulonglong
         L.xdo_pair_list.argtypes = [_vp, _vp, _vp, _vp, _vp, _u, _vp, C.c_ulonglong]
@@ -136,6 +136,16 @@ class Oracle:
     def update_polygon(self, pmi, vlist, sphere, poly):
         self.lib.xdo_update_polygon_object_data(_p(pmi), _p(vlist), _p(sphere), _p(poly),
                                                 _u(poly.shape[0]))
+
+    def contact_magnitudes(self, prm, pos, vel, omega, mass, sorted_, cstart, cend, cp, planes,
+                           cp_planes):
+        mag = np.zeros(pos.shape[0])
+        npl = planes.shape[0]
+        self.lib.xdo_contact_magnitudes(_p(prm), _p(pos), _p(vel), _p(omega), _p(mass), _p(sorted_),
+                                        _p(cstart), _p(cend), _p(cp), _u(pos.shape[0]),
+                                        _p(planes) if npl else None,
+                                        _p(cp_planes) if npl else None, _u(npl), _p(mag))
+        return mag
 
     def pair_list(self, prm, pos, sorted_, cstart, cend, cap=None):
         npt = pos.shape[0]

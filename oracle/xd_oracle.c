@@ -52,6 +52,8 @@ unsigned xdo_sizeof_polygon(void) { return (unsigned)sizeof(xdo_polygon); }
 unsigned xdo_sizeof_polygon_mass(void) { return (unsigned)sizeof(xdo_polygon_mass); }
 unsigned xdo_sizeof_contact_property(void) { return (unsigned)sizeof(xdo_contact_property); }
 
+static double plane_detection(const xdo_plane* pe, v3 xp, v3 wp, v3* u, double r);
+
 /* ------------------------------------------------------------------ grid */
 
 /* calcGridPos (impl:74-83): floor((p - wo) / cs), double -> int. */
@@ -301,6 +303,64 @@ void xdo_calculate_p2p(const xdo_params* prm, const double* pos, const double* v
                 }
         acc3(force + 3 * (size_t)id, sumF);
         acc3(moment + 3 * (size_t)id, sumM);
+    }
+}
+
+void xdo_contact_magnitudes(const xdo_params* prm, const double* pos, const double* vel,
+                            const double* omega, const double* mass, const unsigned* sorted_index,
+                            const unsigned* cstart, const unsigned* cend,
+                            const xdo_contact_property* cp, unsigned np, const xdo_plane* planes,
+                            const xdo_contact_property* cp_planes, unsigned nplanes, double* mag)
+{
+    for (unsigned id = 0; id < np; ++id) {
+        const double* ip4 = pos + 4 * (size_t)id;
+        v3 ipos = ld3(ip4), ivel = ld3(vel + 3 * (size_t)id), iomega = ld3(omega + 3 * (size_t)id);
+        int gp[3];
+        xdo_grid_pos(prm, ip4, gp);
+        double ir = ip4[3], im = mass[id];
+        v3 Ft = mk(0, 0, 0), Fn = mk(0, 0, 0), M = mk(0, 0, 0);
+        double sum = 0.0;
+        for (int z = -1; z <= 1; z++)
+            for (int y = -1; y <= 1; y++)
+                for (int x = -1; x <= 1; x++) {
+                    int nb[3] = { gp[0] + x, gp[1] + y, gp[2] + z };
+                    unsigned h = xdo_grid_hash(prm, nb);
+                    unsigned st = cstart[h];
+                    if (st == 0xffffffffu) continue;
+                    for (unsigned j = st; j < cend[h]; j++) {
+                        unsigned k = sorted_index[j];
+                        if (id == k || k >= np) continue;
+                        const double* jp4 = pos + 4 * (size_t)k;
+                        v3 rp = mk(jp4[0] - ipos.x, jp4[1] - ipos.y, jp4[2] - ipos.z);
+                        double dist = len(rp), jr = jp4[3];
+                        double cdist = (ir + jr) - dist;
+                        if (cdist > 0) {
+                            v3 unit = dvd(rp, dist);
+                            v3 jvel = ld3(vel + 3 * (size_t)k), jomega = ld3(omega + 3 * (size_t)k);
+                            v3 rv = prm->rolling
+                                ? sub(add(jvel, cross(jomega, scl(-jr, unit))), add(ivel, cross(iomega, scl(ir, unit))))
+                                : sub(jvel, ivel);
+                            fconst c = get_constant(ir, jr, im, mass[k], cp);
+                            dhs_model(&c, ir, jr, cp->Ei, cp->Ej, cp->pri, cp->prj, cp->coh, cdist, rv,
+                                      unit, prm->dt, &Ft, &Fn, &M);
+                            sum += len(add(Fn, Ft));
+                        }
+                    }
+                }
+        for (unsigned w = 0; w < nplanes; ++w) {
+            const xdo_plane* pl = planes + w;
+            v3 dp = sub(ipos, ld3(pl->xw));
+            v3 wp = mk(dot(dp, ld3(pl->u1)), dot(dp, ld3(pl->u2)), dot(dp, ld3(pl->uw)));
+            v3 u = mk(0, 0, 0), pFn = mk(0, 0, 0), pFt = mk(0, 0, 0), pM = mk(0, 0, 0);
+            double cdist = plane_detection(pl, ipos, wp, &u, ir);
+            if (cdist > 0) {
+                v3 dv = prm->rolling ? neg(add(ivel, cross(iomega, scl(ir, u)))) : neg(ivel);
+                fconst c = get_constant(ir, 0.0, im, 0.0, cp_planes + w);
+                dhs_model(&c, 0, 0, 0, 0, 0, 0, cp_planes[w].coh, cdist, dv, u, prm->dt, &pFt, &pFn, &pM);
+                sum += len(add(pFn, pFt));
+            }
+        }
+        mag[id] += sum;
     }
 }
 

@@ -123,6 +123,15 @@ void xdo_particle_polygon_collision(const xdo_params* prm, const xdo_polygon* dp
 void xdo_update_polygon_object_data(const xdo_polygon_mass* dpmi, const double* vlist,
                                     double* sphere, xdo_polygon* dpi, unsigned ntri);
 
+/* Per-particle sum of contact force magnitudes, sum_c |Fn + Ft|, over the
+ * particle-particle contacts (mag_pp) and the plane contacts (mag_planes),
+ * added into mag[np]: the normaliser of the per-step force error. */
+void xdo_contact_magnitudes(const xdo_params* prm, const double* pos, const double* vel,
+                            const double* omega, const double* mass, const unsigned* sorted_index,
+                            const unsigned* cstart, const unsigned* cend,
+                            const xdo_contact_property* cp, unsigned np, const xdo_plane* planes,
+                            const xdo_contact_property* cp_planes, unsigned nplanes, double* mag);
+
 /* Contact pair list of one step: for every particle i (ascending) every
  * partner k found by the 27-cell search with cdist > 0, in search order.
  * Writes up to cap pairs as (i, k); returns the total number of pairs. */
