@@ -40,7 +40,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s"
 WORKLOAD = "polydisperse_box_settle"
-B_CONTACT = 140          # algorithmic bytes per particle of the contact kernel (FP64 form)
+B_CONTACT = {"fp64": 140, "mixed": 116}   # algorithmic bytes per particle, contact kernel
 
 
 def _args():
@@ -52,6 +52,9 @@ def _args():
     ap.add_argument("--n", type=int, default=1_000_000, help="spheres (default: the 1M scene)")
     ap.add_argument("--cpu-steps", type=int, default=0, help="CPU-baseline sample steps (0: auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"],
+                    help="scene form for the headline value (the other is reported beside it)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the FP64 side measurement")
     return ap.parse_args()
 
 
@@ -71,9 +74,10 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _traffic_from_profiles():
+def _traffic_from_profiles(mode):
     """Per-launch DRAM bytes of the contact kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "p2p_fp64_polydisperse_box.md")
+    name = "p2p_fp64_polydisperse_box.md" if mode == "fp64" else "contact_mixed_polydisperse_box.md"
+    p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -226,11 +230,42 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
-def run_ours(a):
-    import numpy as np
+def _time_scene(sc, mode, steps, warmup, stream, barrier, world, with_clock, local):
+    """Device-timed steps of one scene form; returns (ms, phases, launches, clocks, scene)."""
     import torch
 
     from metakonga_gb300 import engine
+    ds = engine.DeviceScene(sc, mode=engine.MODE_MIXED if mode == "mixed" else engine.MODE_FP64)
+    sh = stream.cuda_stream
+    ds.step(warmup, check=True, stream=sh)
+    barrier()
+    ds.set_timing(True)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(local) if with_clock else None
+    if clk:
+        clk.__enter__()
+    barrier()
+    ev0.record(stream)
+    ds.step(steps, check=False, stream=sh)
+    ev1.record(stream)
+    barrier()
+    if clk:
+        clk.__exit__(None, None, None)
+    ms = ev0.elapsed_time(ev1)
+    phases = ds.phase_times()
+    ds.set_timing(False)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, phases, ds.launches(steps), (clk.summary() if clk else None), ds
+
+
+def run_ours(a):
+    import numpy as np
+    import torch
 
     world, rank, local = _dist()
     torch.cuda.set_device(local)
@@ -238,7 +273,7 @@ def run_ours(a):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     sc = _scene(a.n)
-    ds = engine.DeviceScene(sc)
+    n = a.n
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
 
@@ -249,40 +284,23 @@ def run_ours(a):
             dist.barrier()
 
     with torch.cuda.stream(stream):
-        ds.step(a.warmup, check=True, stream=sh)
-    barrier()
-    ds.set_timing(True)
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        barrier()
-        ev0.record(stream)
-        ds.step(a.steps, check=False, stream=sh)
-        ev1.record(stream)
-        barrier()
-    ms = ev0.elapsed_time(ev1)
-    phases = ds.phase_times()
-    ds.set_timing(False)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * a.n * a.steps / (ms / 1e3)
+        ms, phases, launches, clocks, ds = _time_scene(sc, a.mode, a.steps, a.warmup, stream,
+                                                       barrier, world, True, local)
+    value = world * n * a.steps / (ms / 1e3)
 
     # e2e: through the C ABI with pinned host buffers, state round trip every step
-    n = a.n
     host = {k: torch.from_numpy(np.ascontiguousarray(getattr(sc, k))).pin_memory() for k in
             ("pos", "vel", "acc", "omega", "alpha", "force", "moment", "mass", "inertia")}
     outs = {k: torch.empty_like(host[k]).pin_memory() for k in ("pos", "vel", "acc", "omega", "alpha")}
     from metakonga_gb300._lib import call
-    up = [host[k].data_ptr() for k in ("pos", "vel", "acc", "omega", "alpha", "force", "moment")]
-    h2d = sum(host[k].numel() * 8 for k in ("pos", "vel", "acc", "omega", "alpha", "force", "moment"))
+    up_keys = ("pos", "vel", "acc", "omega", "alpha", "force", "moment", "mass", "inertia")
+    up = [host[k].data_ptr() for k in up_keys]
+    h2d = sum(host[k].numel() * 8 for k in up_keys)
     d2h = sum(outs[k].numel() * 8 for k in outs)
     e2e_steps = max(3, min(a.steps, 10))
 
     def e2e_step():
-        call("xd_scene_upload", ds.handle, *up, None, None, sh)
+        call("xd_scene_upload", ds.handle, *up, sh)
         call("xd_scene_step", ds.handle, 1, 0, sh)
         call("xd_scene_download", ds.handle, outs["pos"].data_ptr(), outs["vel"].data_ptr(),
              outs["acc"].data_ptr(), outs["omega"].data_ptr(), outs["alpha"].data_ptr(), None,
@@ -296,18 +314,30 @@ def run_ours(a):
     barrier()
     e2e_s = time.perf_counter() - t0
     e2e_value = world * n * e2e_steps / e2e_s
-
-    launches = ds.launches(a.steps)
-    p2p_ms, p2p_n = phases["p2p"]
-    peak, peak_kind = _peaks()
-    achieved = (n * B_CONTACT) / (p2p_ms / p2p_n / 1e3) / 1e9 if p2p_n else None
-    roof = {"bound": "hbm", "kernel": "k_p2p (FP64 particle-particle)", "achieved": achieved,
-            "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-            "peak_kind": peak_kind, "traffic": _traffic_from_profiles(),
-            "bytes_per_particle": B_CONTACT,
-            "avg_launch_ms": p2p_ms / p2p_n if p2p_n else None}
-    phase_ms = {k: round(v[0] / max(v[1], 1), 4) for k, v in phases.items()}
     ds.close()
+
+    c_ms, c_n = phases["p2p"]
+    peak, peak_kind = _peaks()
+    bpp = B_CONTACT[a.mode]
+    achieved = (n * bpp) / (c_ms / c_n / 1e3) / 1e9 if c_n else None
+    kname = "k_mx_contact (mixed particle-particle)" if a.mode == "mixed" else "k_p2p (FP64 particle-particle)"
+    roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
+            "traffic": _traffic_from_profiles(a.mode), "bytes_per_particle": bpp,
+            "avg_launch_ms": c_ms / c_n if c_n else None}
+    phase_ms = {k: round(v[0] / max(v[1], 1), 4) for k, v in phases.items() if v[1]}
+
+    plain = None
+    if not a.no_plain:
+        other = "fp64" if a.mode == "mixed" else "mixed"
+        psteps = max(3, min(a.steps, 10))
+        with torch.cuda.stream(stream):
+            pms, pph, _, _, pds = _time_scene(sc, other, psteps, 1, stream, barrier, world, False,
+                                              local)
+        pds.close()
+        plain = {"mode": other, "value": world * n * psteps / (pms / 1e3), "steps": psteps,
+                 "ms_per_step": pms / psteps,
+                 "phase_ms_per_launch": {k: round(v[0] / max(v[1], 1), 4) for k, v in pph.items() if v[1]}}
 
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
@@ -325,18 +355,20 @@ def run_ours(a):
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if a.mode == "fp64" else "f64+f32",
         "data": "synthetic (seeded MT19937 rejection-sampled spheres)",
-        "config": {"workload": WORKLOAD, "particles": n, "dt": 5e-6, "mode": "fp64",
-                   "grid": "128^3 wrapped, cell 8 mm", "l2": "state > L2 (no flush)",
-                   "parallelism": f"replicas x{world}"},
+        "config": {"workload": WORKLOAD, "particles": n, "dt": 5e-6, "mode": a.mode,
+                   "grid": ("128^3 wrapped, cell 8 mm" if a.mode == "fp64" else
+                            "scene grid sized to the box, cell 2 r_max"),
+                   "l2": "state > L2 (no flush)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": roof,
         "phase_ms_per_launch": phase_ms,
+        "other_form": plain,
         "cpu_baseline": cpu,
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
 
