@@ -104,6 +104,10 @@ int xd_last_error(char* msg, size_t msg_len);
 void xd_clear_error(void);
 /* sizeof of each ABI struct, for binding-side layout checks. */
 size_t xd_sizeof(const char* struct_name);
+/* Record XD_ERR_INVALID ("<what>: not provided") for a declared entry point
+ * that this build does not implement (used by the reference-API shim);
+ * returns XD_ERR_INVALID. */
+int xd_report_unsupported(const char* what);
 /* Free the shared workspace of the stateless calls. */
 int xd_release_workspace(void);
 

@@ -38,6 +38,7 @@ _SIGS = {
     "xd_clear_error": [],
     "xd_sizeof": [C.c_char_p],
     "xd_release_workspace": [],
+    "xd_report_unsupported": [C.c_char_p],
     "xd_set_symbolic_parameter": [vp],
     "xd_vv_update_position": [vp, vp, vp, u32, vp],
     "xd_vv_update_velocity": [vp] * 8 + [u32, vp],

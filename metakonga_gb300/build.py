@@ -75,11 +75,14 @@ def build(verbose: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link of libxdem.so failed:\n{r.stdout}\n{r.stderr}")
     shim_src = os.path.join(CSRC, "shim_mphysics.cpp")
-    shim_deps = [shim_src, LIBXDEM, os.path.join(INCLUDE, "mphysics_cuda_dec.cuh")]
+    shim_deps = [shim_src, LIBXDEM, os.path.join(INCLUDE, "mphysics_cuda_dec.cuh"),
+                 os.path.join(INCLUDE, "xdem_host.h")]
     if os.path.exists(shim_src) and not _newer(LIBSHIM, shim_deps):
-        cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
+        cuda_root = os.path.dirname(os.path.dirname(nvcc()))
         cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", LIBSHIM, shim_src,
-               "-I", INCLUDE, "-I", cuda_inc, "-L", PKG, "-lxdem", "-Wl,-rpath,$ORIGIN"]
+               "-I", INCLUDE, "-I", os.path.join(cuda_root, "include"), "-L", PKG, "-lxdem",
+               "-L", os.path.join(cuda_root, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN",
+               "-Wl,-rpath," + os.path.join(cuda_root, "lib64")]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"build of libxdem_mphysics.so failed:\n{r.stdout}\n{r.stderr}")

@@ -162,6 +162,11 @@ size_t xd_sizeof(const char* n)
 
 int xd_release_workspace(void) { return release_workspace(); }
 
+int xd_report_unsupported(const char* what)
+{
+    return set_error(XD_ERR_INVALID, "%s: not provided", what ? what : "entry point");
+}
+
 int xd_set_symbolic_parameter(const xd_device_parameters* h)
 {
     XD_REQUIRE(h, "set_symbolic_parameter: null parameters");
