@@ -231,7 +231,10 @@ def run_reference(a):
 
 
 def _time_scene(sc, mode, steps, warmup, stream, barrier, world, with_clock, local):
-    """Device-timed steps of one scene form; returns (ms, phases, launches, clocks, scene)."""
+    """Device-timed steps of one scene form; returns (ms, phases, launches, clocks, scene).
+
+    The timed run has phase timing off (so the mixed form replays its CUDA
+    graphs); a second run of the same length records per-phase CUDA events."""
     import torch
 
     from metakonga_gb300 import engine
@@ -239,7 +242,6 @@ def _time_scene(sc, mode, steps, warmup, stream, barrier, world, with_clock, loc
     sh = stream.cuda_stream
     ds.step(warmup, check=True, stream=sh)
     barrier()
-    ds.set_timing(True)
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     clk = ClockSampler(local) if with_clock else None
@@ -253,8 +255,11 @@ def _time_scene(sc, mode, steps, warmup, stream, barrier, world, with_clock, loc
     if clk:
         clk.__exit__(None, None, None)
     ms = ev0.elapsed_time(ev1)
+    ds.set_timing(True)
+    ds.step(steps, check=False, stream=sh)
     phases = ds.phase_times()
     ds.set_timing(False)
+    barrier()
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([ms], device="cuda")

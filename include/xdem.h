@@ -168,7 +168,7 @@ int xd_reorder_and_find_cell_start(unsigned* hash, unsigned* index, unsigned* cs
  * scratch comes from a fixed device array inside the library instead of
  * cudaMalloc, and the call allocates nothing.  Limits and rules:
  *   - at most XD_NOALLOC_MAX_ENTRIES entries (n); larger n -> XD_ERR_CAPACITY;
- *   - the array (about 8.3 MB) stays on every device that loads the library
+ *   - the array (about 9.4 MB) stays on every device that loads the library
  *     until the process exits;
  *   - all calls share the array: calls that overlap on the GPU (other
  *     streams or host threads) race, so serialise them;
@@ -353,8 +353,11 @@ int xd_scene_eval_contacts(xd_scene* scene, double* force, double* moment, void*
 int xd_scene_pair_list(xd_scene* scene, unsigned cap, unsigned* counts, unsigned* partners,
                        void* stream);
 
-/* Mixed-mode counters of the last contact pass: [0] particles near a wall,
- * [1] pairs decided by the FP64 guard-band test. */
+/* Mixed-mode counters: [0] particles near a wall in the last contact pass,
+ * [1] pairs decided by the FP64 guard-band test (cumulative), [2] normal
+ * forces formed in FP64 because the elastic and damping terms nearly cancel
+ * (cumulative), [3] slips formed in FP64 because the rotation term cancels
+ * most of the tangential velocity (cumulative). */
 int xd_scene_counters(xd_scene* scene, unsigned long long out[4], void* stream);
 
 /* Number of kernel launches one xd_scene_step of nsteps issues. */

@@ -129,7 +129,8 @@ void* workspace(size_t bytes, int* status);
 
 inline unsigned div_up(unsigned a, unsigned b) { return (a + b - 1) / b; }
 
-// radix sort (xd_sort.cu)
+// radix sort (xd_sort.cu): keys per tile (8 warps x 4 rounds x 32 lanes)
+constexpr unsigned kSortTile = 1024;
 size_t radix_sort_scratch_bytes(unsigned n);
 int radix_sort_pairs(unsigned* keys, unsigned* vals, unsigned n, unsigned key_bits, void* scratch,
                      cudaStream_t s, unsigned** out_keys, unsigned** out_vals);

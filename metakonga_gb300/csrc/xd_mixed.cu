@@ -55,11 +55,13 @@ struct MixParams {
     unsigned n;
     double wo[3];
     double inv_cs;
+    float inv_csf;
     double dt, half2dt;
     double g[3];
     float dtf;
     float tol;          // prefilter tolerance (m)
     float c43Eeq, one_b2, sratio, fric;
+    double c43Eeq_d, one_b2_d;   // the same constants in FP64 (normal-force recheck)
     long long guard_q;  // guard band in fixed-point units
     int nplanes;
     float pxw[kMaxPlanes][3];   // plane corner relative to the grid origin (FP32)
@@ -81,6 +83,7 @@ struct MixedScene {
     longlong2* qa = nullptr;
     longlong2* qb = nullptr;
     float4* vf = nullptr;
+    float4* vlo = nullptr;   // low parts of the double-float velocity
     float4* wf = nullptr;
     float4* Fc = nullptr;
     float4* Mc = nullptr;
@@ -89,13 +92,14 @@ struct MixedScene {
     unsigned *cstart = nullptr, *cend = nullptr;
     bool cells_clean = false;      // cstart/cend hold only prev_keys' cells
     void* sort_scratch = nullptr;
-    unsigned* sorted_keys = nullptr;   // valid after a sort (points into keys or scratch)
-    unsigned* perm = nullptr;
+    // near-sorted resort buffers
+    unsigned *mv_bcount = nullptr, *mv_prefix = nullptr, *mv_key = nullptr, *mv_slot = nullptr;
+    unsigned *mv_skey = nullptr, *mv_sslot = nullptr, *mv_sorted = nullptr, *mv_perm = nullptr;
     // walls
     xd_plane_info* planes = nullptr;
     xd_contact_property* cps = nullptr;
     unsigned* wall_list = nullptr;
-    unsigned* counters = nullptr;   // [0] wall count, [1] FP64 decisions, [2] error flags
+    unsigned* counters = nullptr;   // [0] wall count, [1] FP64 decisions, [2] FP64 normal forces, [4] movers
     // pair recording
     unsigned* rec_count = nullptr;
     unsigned* rec_pairs = nullptr;
@@ -103,6 +107,8 @@ struct MixedScene {
     double* xfer = nullptr;
     bool state_valid_forces = false;   // Fc/Mc hold the forces of the current state
     bool ready = false;                // grid and buffers set up (first upload)
+    cudaGraphExec_t graph[2] = { nullptr, nullptr };   // two middle steps, per buffer parity
+    bool use_graphs = true;
     unsigned rec_cap_alloc = 0;
     xd_scene_desc desc;
     std::vector<xd_plane_info> host_planes;
@@ -125,11 +131,15 @@ int alloc(MixedScene* s, T** p, size_t count)
     return XD_OK;
 }
 
+// Cell of a position.  The offset from the grid origin is formed in FP64 and
+// scaled in FP32: the FP32 rounding (< 3e-7 m over a 4 m box) is far inside
+// the 0.1 % margin by which the cell exceeds the largest contact distance, so
+// every touching pair still lies in neighbouring cells.
 __device__ __forceinline__ unsigned cell_key(const MixParams& P, double x, double y, double z)
 {
-    int cx = (int)floor((x - P.wo[0]) * P.inv_cs) + 1;
-    int cy = (int)floor((y - P.wo[1]) * P.inv_cs) + 1;
-    int cz = (int)floor((z - P.wo[2]) * P.inv_cs) + 1;
+    int cx = (int)floorf((float)(x - P.wo[0]) * P.inv_csf) + 1;
+    int cy = (int)floorf((float)(y - P.wo[1]) * P.inv_csf) + 1;
+    int cz = (int)floorf((float)(z - P.wo[2]) * P.inv_csf) + 1;
     cx = min(max(cx, 1), P.gx - 2);
     cy = min(max(cy, 1), P.gy - 2);
     cz = min(max(cz, 1), P.gz - 2);
@@ -150,12 +160,12 @@ __global__ void __launch_bounds__(256) k_mx_integrate(MixParams P, Master M,
     double ax = M.f[FAX][i], ay = M.f[FAY][i], az = M.f[FAZ][i];
     double vx = M.f[FVX][i], vy = M.f[FVY][i], vz = M.f[FVZ][i];
     if (MODE != 0) {
-        const double m = M.f[FM][i], im = M.f[FIM][i], iI = M.f[FII][i];
+        const double im = M.f[FIM][i], iI = M.f[FII][i];
         const float4 f = Fc[i], t = Mc[i];
-        // force = m g + contacts (vv_update_velocity_kernel, impl:117-133)
-        double nax = im * (m * P.g[0] + (double)f.x);
-        double nay = im * (m * P.g[1] + (double)f.y);
-        double naz = im * (m * P.g[2] + (double)f.z);
+        // a' = (m g + F_contact) / m = g + F_contact / m (vv_update_velocity_kernel, impl:117-133)
+        double nax = fma(im, (double)f.x, P.g[0]);
+        double nay = fma(im, (double)f.y, P.g[1]);
+        double naz = fma(im, (double)f.z, P.g[2]);
         double nbx = iI * (double)t.x, nby = iI * (double)t.y, nbz = iI * (double)t.z;
         const double h = 0.5 * P.dt;
         vx += h * (ax + nax);
@@ -195,6 +205,7 @@ __global__ void __launch_bounds__(256) k_mx_reorder(MixParams P, Master S, Maste
                                                     longlong2* __restrict__ qa,
                                                     longlong2* __restrict__ qb,
                                                     float4* __restrict__ vf,
+                                                    float4* __restrict__ vlo,
                                                     float4* __restrict__ wf)
 {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -211,7 +222,10 @@ __global__ void __launch_bounds__(256) k_mx_reorder(MixParams P, Master S, Maste
     pf[i] = make_float4((float)rx, (float)ry, (float)rz, (float)v[FR]);
     qa[i] = make_longlong2(__double2ll_rn(rx * kQ), __double2ll_rn(ry * kQ));
     qb[i] = make_longlong2(__double2ll_rn(rz * kQ), __double2ll_rn(v[FR] * kQ));
-    vf[i] = make_float4((float)v[FVX], (float)v[FVY], (float)v[FVZ], (float)v[FM]);
+    const float hx = (float)v[FVX], hy = (float)v[FVY], hz = (float)v[FVZ];
+    vf[i] = make_float4(hx, hy, hz, (float)v[FM]);
+    vlo[i] = make_float4((float)(v[FVX] - (double)hx), (float)(v[FVY] - (double)hy),
+                         (float)(v[FVZ] - (double)hz), 0.f);
     wf[i] = make_float4((float)v[FWX], (float)v[FWY], (float)v[FWZ], 0.f);
 }
 
@@ -265,12 +279,192 @@ __device__ __forceinline__ f3 fcross(f3 a, f3 b)
     return fk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 
+// Error-free transformations (Knuth's TwoSum, FMA-based TwoProd).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = __fadd_rn(a, b);
+    const float z = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z));
+}
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e)
+{
+    p = __fmul_rn(a, b);
+    e = __fmaf_rn(a, b, -p);
+}
+
+// vj - vi of two double-float velocities (hi + lo) as an unevaluated pair
+// s + t that keeps the low bits of nearly equal velocities.
+__device__ __forceinline__ void df_diff(float ah, float bh, float dlo, float& s, float& t)
+{
+    float e;
+    two_sum(ah, -bh, s, e);
+    t = __fadd_rn(e, dlo);
+}
+
+// Normal speed (dv . dq) / |dq| in double-float: dv = s + t per component,
+// dq the exact integer separation (|dq| < 2^31), D2 = |dq|^2 exact, d0 its
+// FP32 square root.  The dot product of a fast tangential velocity with the
+// contact normal cancels; here it is carried with ~2^-44 relative error and
+// rounded once.
+__device__ __forceinline__ float normal_speed(const float s[3], const float t[3], const int dq[3],
+                                              float d0, long long D2)
+{
+    float hi = 0.f, lo = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float qh = __int2float_rn(dq[k]);
+        const float ql = __int2float_rn(dq[k] - __float2int_rn(qh));
+        float p, pe, ns, e1;
+        two_prod(s[k], qh, p, pe);
+        two_sum(hi, p, ns, e1);
+        hi = ns;
+        lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(e1, pe), __fmaf_rn(s[k], ql, __fmul_rn(t[k], qh))));
+    }
+    float nv, nl;
+    two_sum(hi, lo, nv, nl);
+    // |dq| = d0 + c with c = (D2 - d0^2) / (2 d0)
+    float p, pe;
+    two_prod(d0, d0, p, pe);
+    const float D2h = __ll2float_rn(D2);
+    const float D2l = __ll2float_rn(D2 - __float2ll_rn(D2h));
+    const float c = __fdiv_rn(__fadd_rn(__fsub_rn(__fsub_rn(D2h, p), pe), D2l), __fmul_rn(2.f, d0));
+    // (nv + nl) / (d0 + c)
+    const float q0 = __fdiv_rn(nv, d0);
+    float qp, qpe;
+    two_prod(q0, d0, qp, qpe);
+    const float rem = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(nv, qp), qpe), nl), __fmul_rn(q0, c));
+    return __fadd_rn(q0, __fdiv_rn(rem, d0));
+}
+
+// Per-particle contact state carried across the pairs of one particle (the
+// reference keeps Ft and M in the kernel across pairs, impl:426-428).
+struct PairAcc {
+    f3 Ft, Mm, sumF, sumM;
+};
+
+// The force of one contact (i, j) with overlap `delta` (FP32), or, when
+// `guard` is set, with the overlap from the reference's FP64 test.
+// getConstant TCM = 1 (impl:238-246) and DHSModel (impl:379-401) in FP32, the
+// relative velocity formed from double-float velocities, and the two
+// cancellation cases (normal force near zero, rolling slip) formed in FP64.
+__device__ __forceinline__ void contact_force(const MixParams& P, const Master& M, unsigned i,
+                                              unsigned j, float delta, bool guard,
+                                              const longlong2& qai, const longlong2& qbi,
+                                              const float4& vi4, const float4& vil, const f3& wi,
+                                              float ir, float im, const float4* __restrict__ pf,
+                                              const longlong2* __restrict__ qa,
+                                              const longlong2* __restrict__ qb,
+                                              const float4* __restrict__ vf,
+                                              const float4* __restrict__ vlo,
+                                              const float4* __restrict__ wf,
+                                              unsigned* __restrict__ counters, PairAcc& A)
+{
+    const float dt = P.dtf;
+    const longlong2 qaj = __ldg(qa + j), qbj = __ldg(qb + j);
+    const long long ddx = qaj.x - qai.x, ddy = qaj.y - qai.y, ddz = qbj.x - qbi.x;
+    const long long D2 = ddx * ddx + ddy * ddy + ddz * ddz;
+    const float dn = sqrtf((float)D2);
+    const float inv = 1.0f / dn;
+    const f3 u = fk((float)ddx * inv, (float)ddy * inv, (float)ddz * inv);
+    const float4 vj4 = __ldg(vf + j), wj4 = __ldg(wf + j), vjl = __ldg(vlo + j);
+    const f3 wj = fk(wj4.x, wj4.y, wj4.z);
+    const float jr = __ldg(pf + j).w, jm = vj4.w;
+    // vj - vi formed exactly from the double-float velocities
+    float dvs[3], dvt[3];
+    df_diff(vj4.x, vi4.x, __fsub_rn(vjl.x, vil.x), dvs[0], dvt[0]);
+    df_diff(vj4.y, vi4.y, __fsub_rn(vjl.y, vil.y), dvs[1], dvt[1]);
+    df_diff(vj4.z, vi4.z, __fsub_rn(vjl.z, vil.z), dvs[2], dvt[2]);
+    const f3 dv = fk(dvs[0] + dvt[0], dvs[1] + dvt[1], dvs[2] + dvt[2]);
+    // rv = vj + wj x (-rj u) - (vi + wi x (ri u))   (impl:455)
+    const f3 wterm = fcross(wj, (-jr) * u) - fcross(wi, ir * u);
+    const f3 rv = dv + wterm;
+    // rv . u = dv . u (the rotation term is perpendicular to u), in double-float
+    const int dqi[3] = { (int)ddx, (int)ddy, (int)ddz };
+    const float rvu = normal_speed(dvs, dvt, dqi, dn, D2);
+    f3 ev = rv - rvu * u;
+    float ee = fdot(ev, ev);
+    if (ee < 0.0025f * fdot(wterm, wterm)) {
+        // rolling: the rotation term cancels most of the slip; form the slip in
+        // FP64 from the FP64 state (FP32 rounding of the terms would dominate)
+        atomicAdd(counters + 3, 1u);
+        const double dd = sqrt((double)D2);
+        const double ux = (double)ddx / dd, uy = (double)ddy / dd, uz = (double)ddz / dd;
+        const double ri = __ldg(M.f[FR] + i), rj = __ldg(M.f[FR] + j);
+        const double wix = __ldg(M.f[FWX] + i), wiy = __ldg(M.f[FWY] + i), wiz = __ldg(M.f[FWZ] + i);
+        const double wjx = __ldg(M.f[FWX] + j), wjy = __ldg(M.f[FWY] + j), wjz = __ldg(M.f[FWZ] + j);
+        const double dvx = __ldg(M.f[FVX] + j) - __ldg(M.f[FVX] + i);
+        const double dvy = __ldg(M.f[FVY] + j) - __ldg(M.f[FVY] + i);
+        const double dvz = __ldg(M.f[FVZ] + j) - __ldg(M.f[FVZ] + i);
+        const double rx = dvx - rj * (wjy * uz - wjz * uy) - ri * (wiy * uz - wiz * uy);
+        const double ry = dvy - rj * (wjz * ux - wjx * uz) - ri * (wiz * ux - wix * uz);
+        const double rz = dvz - rj * (wjx * uy - wjy * ux) - ri * (wix * uy - wiy * ux);
+        const double ru = rx * ux + ry * uy + rz * uz;
+        ev = fk((float)(rx - ru * ux), (float)(ry - ru * uy), (float)(rz - ru * uz));
+        ee = fdot(ev, ev);
+    }
+    // getConstant, TCM = 1 (impl:238-246)
+    const float Meq = (im * jm) / (im + jm);
+    const float Req = (ir * jr) / (ir + jr);
+    const float kn = P.c43Eeq * sqrtf(Req);
+    const float vn = sqrtf((4.0f * Meq * kn) / P.one_b2);
+    const float ks = kn * P.sratio, vs = vn * P.sratio;
+    // DHSModel (impl:379-401)
+    const float fsn = -kn * (delta * sqrtf(delta));
+    const float fdn = vn * rvu;
+    float fn = fsn + fdn;
+    if (fabsf(fn) < 0.03f * fmaxf(fabsf(fsn), fabsf(fdn))) {
+        // The elastic and damping terms nearly cancel (the normal force of an
+        // unloading contact crossing zero): FP32 rounding of each term would
+        // dominate the small sum, so it is formed in FP64 from the FP64 state,
+        // with the overlap and normal taken from the FP64 positions.
+        atomicAdd(counters + 2, 1u);
+        const double px = __ldg(M.f[FX] + j) - __ldg(M.f[FX] + i);
+        const double py = __ldg(M.f[FY] + j) - __ldg(M.f[FY] + i);
+        const double pz = __ldg(M.f[FZ] + j) - __ldg(M.f[FZ] + i);
+        const double dd = sqrt(px * px + py * py + pz * pz);
+        const double ux = px / dd, uy = py / dd, uz = pz / dd;
+        const double dl = fp64_cdist(M, i, j);
+        const double ri = __ldg(M.f[FR] + i), rj = __ldg(M.f[FR] + j);
+        const double mi = __ldg(M.f[FM] + i), mj = __ldg(M.f[FM] + j);
+        const double vix = __ldg(M.f[FVX] + i), viy = __ldg(M.f[FVY] + i), viz = __ldg(M.f[FVZ] + i);
+        const double vjx = __ldg(M.f[FVX] + j), vjy = __ldg(M.f[FVY] + j), vjz = __ldg(M.f[FVZ] + j);
+        const double wix = __ldg(M.f[FWX] + i), wiy = __ldg(M.f[FWY] + i), wiz = __ldg(M.f[FWZ] + i);
+        const double wjx = __ldg(M.f[FWX] + j), wjy = __ldg(M.f[FWY] + j), wjz = __ldg(M.f[FWZ] + j);
+        const double rvx = (vjx - rj * (wjy * uz - wjz * uy)) - (vix + ri * (wiy * uz - wiz * uy));
+        const double rvy = (vjy - rj * (wjz * ux - wjx * uz)) - (viy + ri * (wiz * ux - wix * uz));
+        const double rvz = (vjz - rj * (wjx * uy - wjy * ux)) - (viz + ri * (wix * uy - wiy * ux));
+        const double Meqd = (mi * mj) / (mi + mj), Reqd = (ri * rj) / (ri + rj);
+        const double knd = P.c43Eeq_d * sqrt(Reqd);
+        const double vnd = sqrt((4.0 * Meqd * knd) / P.one_b2_d);
+        fn = (float)(-knd * (dl * sqrt(dl)) + vnd * (rvx * ux + rvy * uy + rvz * uz));
+    }
+    (void)guard;
+    const f3 Fn = fn * u;
+    const float mag_e = sqrtf(ee);
+    if (mag_e != 0.f) {
+        const f3 sh = (1.0f / mag_e) * ev;
+        // dv . sh = |e| exactly (sh is the unit slip direction)
+        A.Ft = fminf(ks * (mag_e * dt) + vs * mag_e, P.fric * fabsf(fn)) * sh;
+        A.Mm = fcross(ir * u, A.Ft);
+    }
+    A.sumF = A.sumF + (Fn + A.Ft);
+    A.sumM = A.sumM + A.Mm;
+}
+
+constexpr int kMaxStaged = 20;   // contacts staged per thread in shared memory
+
+// Particle-particle contacts in two phases: (1) the candidate loop -- FP32
+// prefilter, exact integer test, FP64 guard band -- stages each contact's
+// partner and overlap in shared memory; (2) the force loop runs over the
+// staged contacts in the same order.  A particle with more contacts than the
+// stage holds finishes the rest by re-scanning its candidates (same order).
 template <bool RECORD>
 __global__ void __launch_bounds__(256) k_mx_contact(MixParams P, Master M,
                                                     const float4* __restrict__ pf,
                                                     const longlong2* __restrict__ qa,
                                                     const longlong2* __restrict__ qb,
                                                     const float4* __restrict__ vf,
+                                                    const float4* __restrict__ vlo,
                                                     const float4* __restrict__ wf,
                                                     const unsigned* __restrict__ keys,
                                                     const unsigned* __restrict__ cstart,
@@ -281,21 +475,20 @@ __global__ void __launch_bounds__(256) k_mx_contact(MixParams P, Master M,
                                                     unsigned* __restrict__ rec_count,
                                                     unsigned* __restrict__ rec_pairs, unsigned rec_cap)
 {
-    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ unsigned st_j[kMaxStaged][256];
+    __shared__ float st_d[kMaxStaged][256];
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
+    const unsigned tx = threadIdx.x;
     const float4 pi = __ldg(pf + i);
     const longlong2 qai = __ldg(qa + i), qbi = __ldg(qb + i);
-    const float4 vi4 = __ldg(vf + i), wi4 = __ldg(wf + i);
-    const f3 vi = fk(vi4.x, vi4.y, vi4.z), wi = fk(wi4.x, wi4.y, wi4.z);
-    const float ir = pi.w, im = vi4.w;
+    const float ir = pi.w;
     const unsigned key = __ldg(keys + i);
     const int cx = (int)(key % (unsigned)P.gx);
     const int cy = (int)((key / (unsigned)P.gx) % (unsigned)P.gy);
     const int cz = (int)(key / ((unsigned)P.gx * (unsigned)P.gy));
-    f3 Ft = fk(0.f, 0.f, 0.f), Fn = fk(0.f, 0.f, 0.f), Mm = fk(0.f, 0.f, 0.f);
-    f3 sumF = fk(0.f, 0.f, 0.f), sumM = fk(0.f, 0.f, 0.f);
-    unsigned nrec = 0;
-    const float dt = P.dtf;
+    unsigned ncont = 0;
+    // ---- phase 1: candidates
     for (int dz = -1; dz <= 1; ++dz) {
         for (int dy = -1; dy <= 1; ++dy) {
             const unsigned c0 = ((unsigned)(cz + dz) * (unsigned)P.gy + (unsigned)(cy + dy)) * (unsigned)P.gx +
@@ -317,54 +510,81 @@ __global__ void __launch_bounds__(256) k_mx_contact(MixParams P, Master M,
                 const long long band = 2 * Rq * P.guard_q;
                 float delta;
                 if (N > band) {
-                    const float d = sqrtf((float)D2);
-                    delta = ((float)N / ((float)Rq + d)) * kU;
+                    delta = ((float)N / ((float)Rq + sqrtf((float)D2))) * kU;
                 } else if (N < -band) {
                     continue;
                 } else {
                     atomicAdd(counters + 1, 1u);
                     const double cd = fp64_cdist(M, i, j);
                     if (!(cd > 0)) continue;
-                    delta = (float)cd;
+                    delta = -(float)cd;     // negative: decided by the FP64 test
                 }
-                if (RECORD) {
-                    if (nrec < rec_cap) rec_pairs[(size_t)i * rec_cap + nrec] = j;
-                    ++nrec;
+                if (RECORD && ncont < rec_cap) rec_pairs[(size_t)i * rec_cap + ncont] = j;
+                if (ncont < (unsigned)kMaxStaged) {
+                    st_j[ncont][tx] = j;
+                    st_d[ncont][tx] = delta;
                 }
-                const float dn = sqrtf((float)D2);
-                const float inv = 1.0f / dn;
-                const f3 u = fk((float)ddx * inv, (float)ddy * inv, (float)ddz * inv);
-                const float4 vj4 = __ldg(vf + j), wj4 = __ldg(wf + j);
-                const f3 vj = fk(vj4.x, vj4.y, vj4.z), wj = fk(wj4.x, wj4.y, wj4.z);
-                const float jr = pj.w, jm = vj4.w;
-                // rv = vj + wj x (-rj u) - (vi + wi x (ri u))   (impl:455)
-                const f3 rv = (vj + fcross(wj, (-jr) * u)) - (vi + fcross(wi, ir * u));
-                // getConstant, TCM = 1 (impl:238-246)
-                const float Meq = (im * jm) / (im + jm);
-                const float Req = (ir * jr) / (ir + jr);
-                const float kn = P.c43Eeq * sqrtf(Req);
-                const float vn = sqrtf((4.0f * Meq * kn) / P.one_b2);
-                const float ks = kn * P.sratio, vs = vn * P.sratio;
-                // DHSModel (impl:379-401)
-                const float fsn = -kn * (delta * sqrtf(delta));
-                const float rvu = fdot(rv, u);
-                Fn = (fsn + vn * rvu) * u;
-                const f3 ev = rv - rvu * u;
-                const float mag_e = sqrtf(fdot(ev, ev));
-                if (mag_e != 0.f) {
-                    const f3 sh = (1.0f / mag_e) * ev;
-                    const float lenFn = sqrtf(fdot(Fn, Fn));
-                    Ft = fminf(ks * (mag_e * dt) + vs * fdot(rv, sh), P.fric * lenFn) * sh;
-                    Mm = fcross(ir * u, Ft);
-                }
-                sumF = sumF + (Fn + Ft);
-                sumM = sumM + Mm;
+                ++ncont;
             }
         }
     }
-    Fc[i] = make_float4(sumF.x, sumF.y, sumF.z, 0.f);
-    Mc[i] = make_float4(sumM.x, sumM.y, sumM.z, 0.f);
-    if (RECORD) rec_count[i] = nrec;
+    if (RECORD) rec_count[i] = ncont;
+    // ---- phase 2: forces of the staged contacts, in search order
+    PairAcc A;
+    A.Ft = fk(0.f, 0.f, 0.f);
+    A.Mm = fk(0.f, 0.f, 0.f);
+    A.sumF = fk(0.f, 0.f, 0.f);
+    A.sumM = fk(0.f, 0.f, 0.f);
+    if (ncont) {
+        const float4 vi4 = __ldg(vf + i), vil = __ldg(vlo + i), wi4 = __ldg(wf + i);
+        const f3 wi = fk(wi4.x, wi4.y, wi4.z);
+        const float im = vi4.w;
+        const unsigned nst = min(ncont, (unsigned)kMaxStaged);
+        for (unsigned c = 0; c < nst; ++c) {
+            const float d = st_d[c][tx];
+            contact_force(P, M, i, st_j[c][tx], fabsf(d), d < 0.f, qai, qbi, vi4, vil, wi, ir, im, pf,
+                          qa, qb, vf, vlo, wf, counters, A);
+        }
+        if (ncont > (unsigned)kMaxStaged) {
+            // ---- phase 3 (rare): contacts beyond the stage, by re-scanning
+            unsigned k = 0;
+            for (int dz = -1; dz <= 1; ++dz)
+                for (int dy = -1; dy <= 1; ++dy) {
+                    const unsigned c0 = ((unsigned)(cz + dz) * (unsigned)P.gy + (unsigned)(cy + dy)) *
+                                            (unsigned)P.gx + (unsigned)(cx - 1);
+                    const unsigned s = min(min(__ldg(cstart + c0), __ldg(cstart + c0 + 1)), __ldg(cstart + c0 + 2));
+                    const unsigned e = max(max(__ldg(cend + c0), __ldg(cend + c0 + 1)), __ldg(cend + c0 + 2));
+                    for (unsigned j = s; j < e; ++j) {
+                        if (j == i) continue;
+                        const float4 pj = __ldg(pf + j);
+                        const float dxf = pj.x - pi.x, dyf = pj.y - pi.y, dzf = pj.z - pi.z;
+                        const float Rt = ir + pj.w + P.tol;
+                        if (dxf * dxf + dyf * dyf + dzf * dzf >= Rt * Rt) continue;
+                        const longlong2 qaj = __ldg(qa + j), qbj = __ldg(qb + j);
+                        const long long ddx = qaj.x - qai.x, ddy = qaj.y - qai.y, ddz = qbj.x - qbi.x;
+                        const long long Rq = qbi.y + qbj.y;
+                        const long long D2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                        const long long N = Rq * Rq - D2;
+                        const long long band = 2 * Rq * P.guard_q;
+                        float delta;
+                        if (N > band) {
+                            delta = ((float)N / ((float)Rq + sqrtf((float)D2))) * kU;
+                        } else if (N < -band) {
+                            continue;
+                        } else {
+                            const double cd = fp64_cdist(M, i, j);
+                            if (!(cd > 0)) continue;
+                            delta = (float)cd;
+                        }
+                        if (k++ < (unsigned)kMaxStaged) continue;
+                        contact_force(P, M, i, j, delta, false, qai, qbi, vi4, vil, wi, ir, im, pf, qa,
+                                      qb, vf, vlo, wf, counters, A);
+                    }
+                }
+        }
+    }
+    Fc[i] = make_float4(A.sumF.x, A.sumF.y, A.sumF.z, 0.f);
+    Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
     // walls: FP32 distance to each plane's supporting plane; near ones go to the FP64 pass
     bool near = false;
     for (int w = 0; w < P.nplanes; ++w) {
@@ -506,6 +726,199 @@ __global__ void __launch_bounds__(256) k_mx_keys(MixParams P, Master M, unsigned
     vals[i] = i;
 }
 
+// ---- near-sorted resort ("movers") -----------------------------------------
+// The state is in the previous step's cell order, so prev[] (that order's
+// keys) is ascending and most particles keep their key.  Sorting (key, slot)
+// stably then only needs the movers (key != prev) ranked among themselves;
+// every other slot keeps its relative order:
+//   position(stayer i) = (i - movers before i) + movers with (key, slot) < (prev[i], i)
+//   position(mover m)  = stayers with (prev, slot) < (key_m, slot_m) + rank of m among movers
+// which is exactly the stable sort's output.
+constexpr int kMvBlock = 1024;     // slots per block in the flag/compact pass (256 threads x 4)
+
+__global__ void __launch_bounds__(256) k_mv_count(const unsigned* __restrict__ keys,
+                                                  const unsigned* __restrict__ prev, unsigned n,
+                                                  unsigned* __restrict__ bcount)
+{
+    __shared__ unsigned wsum[8];
+    const unsigned base = blockIdx.x * kMvBlock;
+    unsigned c = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        unsigned i = base + k * 256 + threadIdx.x;
+        if (i < n && keys[i] != prev[i]) ++c;
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = 0;
+        for (int w = 0; w < 8; ++w) t += wsum[w];
+        bcount[blockIdx.x] = t;
+    }
+}
+
+// exclusive scan of the per-block counts (one block); total movers -> *total
+__global__ void __launch_bounds__(1024) k_mv_scan(unsigned* __restrict__ bcount, unsigned nb,
+                                                  unsigned* __restrict__ total)
+{
+    __shared__ unsigned wsum[32];
+    __shared__ unsigned carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (unsigned b0 = 0; b0 < nb; b0 += 1024) {
+        unsigned i = b0 + threadIdx.x;
+        unsigned v = i < nb ? bcount[i] : 0u;
+        unsigned x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (unsigned)o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned w = wsum[lane], t = w;
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= (unsigned)o) t += y;
+            }
+            wsum[lane] = t - w;
+        }
+        __syncthreads();
+        unsigned excl = x - v + wsum[warp] + carry;
+        if (i < nb) bcount[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+// movers compacted in slot order; mprefix[i] = movers in slots [0, i)
+__global__ void __launch_bounds__(256) k_mv_compact(const unsigned* __restrict__ keys,
+                                                    const unsigned* __restrict__ prev, unsigned n,
+                                                    const unsigned* __restrict__ boff,
+                                                    unsigned* __restrict__ mprefix,
+                                                    unsigned* __restrict__ mkey,
+                                                    unsigned* __restrict__ mslot)
+{
+    __shared__ unsigned wsum[32];
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned run = boff[blockIdx.x];
+    const unsigned base = blockIdx.x * kMvBlock;
+    for (int k = 0; k < 4; ++k) {
+        unsigned i = base + k * 256 + threadIdx.x;
+        bool mv = i < n && keys[i] != prev[i];
+        unsigned bal = __ballot_sync(0xffffffffu, mv);
+        if (lane == 0) wsum[warp] = __popc(bal);
+        __syncthreads();
+        unsigned before = 0, all = 0;
+        for (int w = 0; w < 8; ++w) {
+            unsigned c = wsum[w];
+            if (w < (int)warp) before += c;
+            all += c;
+        }
+        unsigned pos = run + before + __popc(bal & ((1u << lane) - 1u));
+        if (i < n) mprefix[i] = pos;
+        if (mv) {
+            mkey[pos] = keys[i];
+            mslot[pos] = i;
+        }
+        if (i == n - 1) mprefix[n] = pos + (mv ? 1u : 0u);
+        run += all;
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ bool pair_less(unsigned ka, unsigned sa, unsigned kb, unsigned sb)
+{
+    return ka < kb || (ka == kb && sa < sb);
+}
+
+// first index in a[0, n) with a[idx] >= v
+__device__ __forceinline__ unsigned lower_bound_u(const unsigned* __restrict__ a, unsigned n, unsigned v)
+{
+    unsigned lo = 0, hi = n;
+    while (lo < hi) {
+        unsigned mid = (lo + hi) >> 1;
+        if (__ldg(a + mid) < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Ranks each mover among all movers (shared-memory tiles of the mover set,
+// O(M^2) compares: M is a few thousand per step; any M stays correct) and
+// places it.  Also writes the sorted mover list for the stayers' searches.
+constexpr int kRankTile = 2048;
+__global__ void __launch_bounds__(256) k_mv_rank(const unsigned* __restrict__ total,
+                                                 const unsigned* __restrict__ mkey,
+                                                 const unsigned* __restrict__ mslot,
+                                                 const unsigned* __restrict__ prev,
+                                                 const unsigned* __restrict__ mprefix, unsigned n,
+                                                 unsigned* __restrict__ smkey,
+                                                 unsigned* __restrict__ smslot,
+                                                 unsigned* __restrict__ skeys,
+                                                 unsigned* __restrict__ perm)
+{
+    __shared__ unsigned tk[kRankTile], ts[kRankTile];
+    const unsigned M = *total;
+    const unsigned stride = gridDim.x * blockDim.x;
+    for (unsigned base = blockIdx.x * blockDim.x; base < M; base += stride) {
+        const unsigned m = base + threadIdx.x;
+        const bool act = m < M;
+        const unsigned key = act ? mkey[m] : 0u, slot = act ? mslot[m] : 0u;
+        unsigned rank = 0;
+        for (unsigned t0 = 0; t0 < M; t0 += kRankTile) {
+            const unsigned cnt = min((unsigned)kRankTile, M - t0);
+            __syncthreads();
+            for (unsigned k = threadIdx.x; k < cnt; k += blockDim.x) {
+                tk[k] = mkey[t0 + k];
+                ts[k] = mslot[t0 + k];
+            }
+            __syncthreads();
+            if (act)
+                for (unsigned k = 0; k < cnt; ++k) rank += pair_less(tk[k], ts[k], key, slot) ? 1u : 0u;
+        }
+        if (act) {
+            smkey[rank] = key;
+            smslot[rank] = slot;
+            const unsigned L = lower_bound_u(prev, n, key);
+            const unsigned U = lower_bound_u(prev, n, key + 1u);
+            const unsigned cend = max(L, min(U, slot));
+            const unsigned pos = (cend - mprefix[cend]) + rank;
+            skeys[pos] = key;
+            perm[pos] = slot;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_mv_place(const unsigned* __restrict__ keys,
+                                                  const unsigned* __restrict__ prev, unsigned n,
+                                                  const unsigned* __restrict__ mprefix,
+                                                  const unsigned* __restrict__ total,
+                                                  const unsigned* __restrict__ smkey,
+                                                  const unsigned* __restrict__ smslot,
+                                                  unsigned* __restrict__ skeys,
+                                                  unsigned* __restrict__ perm)
+{
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned k = prev[i];
+    if (keys[i] != k) return;   // a mover: placed by k_mv_rank
+    const unsigned M = *total;
+    unsigned lo = 0, hi = M;    // movers with (key, slot) < (k, i)
+    while (lo < hi) {
+        unsigned mid = (lo + hi) >> 1;
+        if (pair_less(__ldg(smkey + mid), __ldg(smslot + mid), k, i)) lo = mid + 1;
+        else hi = mid;
+    }
+    const unsigned pos = (i - mprefix[i]) + lo;
+    skeys[pos] = k;
+    perm[pos] = i;
+}
+
 inline unsigned blocks(unsigned n, unsigned t) { return div_up(n ? n : 1u, t); }
 
 }  // namespace
@@ -563,6 +976,7 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
         P.g[a] = d.params.gravity[a];
     }
     P.inv_cs = 1.0 / s->cs;
+    P.inv_csf = (float)P.inv_cs;
     P.dt = d.params.dt;
     P.half2dt = d.params.half2dt;
     P.dtf = (float)d.params.dt;
@@ -571,8 +985,10 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     const xd_contact_property& cp = d.cp_pp;
     double Eeq = (cp.Ei * cp.Ej) / (cp.Ei * (1 - cp.prj * cp.prj) + cp.Ej * (1 - cp.pri * cp.pri));
     double beta = M_PI / log(cp.rest);
-    P.c43Eeq = (float)((4.0 / 3.0) * Eeq);
-    P.one_b2 = (float)(1.0 + beta * beta);
+    P.c43Eeq_d = (4.0 / 3.0) * Eeq;
+    P.one_b2_d = 1.0 + beta * beta;
+    P.c43Eeq = (float)P.c43Eeq_d;
+    P.one_b2 = (float)P.one_b2_d;
     P.sratio = (float)cp.sratio;
     P.fric = (float)cp.fric;
     P.guard_q = (long long)ceil(kGuard * kQ);
@@ -597,6 +1013,7 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     A(alloc(s, &s->qa, n));
     A(alloc(s, &s->qb, n));
     A(alloc(s, &s->vf, n));
+    A(alloc(s, &s->vlo, n));
     A(alloc(s, &s->wf, n));
     A(alloc(s, &s->Fc, n));
     A(alloc(s, &s->Mc, n));
@@ -611,7 +1028,15 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     A(alloc(s, &s->planes, s->nplanes));
     A(alloc(s, &s->cps, s->nplanes));
     A(alloc(s, &s->wall_list, n));
-    A(alloc(s, &s->counters, 4));
+    A(alloc(s, &s->mv_bcount, div_up((unsigned)(n ? n : 1), 1024u)));
+    A(alloc(s, &s->mv_prefix, n + 1));
+    A(alloc(s, &s->mv_key, n));
+    A(alloc(s, &s->mv_slot, n));
+    A(alloc(s, &s->mv_skey, n));
+    A(alloc(s, &s->mv_sslot, n));
+    A(alloc(s, &s->mv_sorted, n));
+    A(alloc(s, &s->mv_perm, n));
+    A(alloc(s, &s->counters, 8));
     if (st == XD_OK && s->nplanes) {
         A(cuda_status(cudaMemcpy(s->planes, d.planes, sizeof(xd_plane_info) * s->nplanes, cudaMemcpyHostToDevice), "mixed planes"));
         A(cuda_status(cudaMemcpy(s->cps, d.cp_planes, sizeof(xd_contact_property) * s->nplanes, cudaMemcpyHostToDevice), "mixed planes"));
@@ -648,6 +1073,8 @@ void mixed_destroy(MixedScene* s)
 {
     if (!s) return;
     cudaDeviceSynchronize();
+    for (int k = 0; k < 2; ++k)
+        if (s->graph[k]) cudaGraphExecDestroy(s->graph[k]);
     for (void* p : s->allocs) cudaFree(p);
     delete s;
 }
@@ -688,6 +1115,7 @@ int mixed_upload(MixedScene* s, const double* pos, const double* vel, const doub
     cp(dI, inertia, n);
     if (st != XD_OK) return st;
     s->cur = 0;
+    s->cells_clean = false;   // the state is in upload order again: next resort is a full sort
     k_mx_load<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[0], dpos, dvel, dacc, dom, dal, dm, dI);
     st = launch_status("mixed upload");
     if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "mixed upload");
@@ -731,11 +1159,27 @@ static int grid_and_contacts(MixedScene* s, cudaStream_t q, const Phases& ph, bo
     int st;
     unsigned *sk = nullptr, *sv = nullptr;
     ph.begin(2, q);
-    st = radix_sort_pairs(s->keys, s->vals, n, key_bits_for(s->ncell), s->sort_scratch, q, &sk, &sv);
-    if (st == XD_OK) {
-        if (!s->cells_clean) {
-            st = launch_fill_cells(s->cstart, s->cend, s->ncell, q);
-        } else {
+    if (!s->cells_clean) {
+        // no previous order to exploit: full stable radix sort
+        st = radix_sort_pairs(s->keys, s->vals, n, key_bits_for(s->ncell), s->sort_scratch, q, &sk, &sv);
+        if (st == XD_OK) st = launch_fill_cells(s->cstart, s->cend, s->ncell, q);
+        if (st == XD_OK)
+            st = cuda_status(cudaMemsetAsync(s->counters + 4, 0, sizeof(unsigned), q), "mixed movers");
+    } else {
+        const unsigned nb = div_up(n, 1024u);
+        unsigned* total = s->counters + 4;
+        k_mv_count<<<nb, 256, 0, q>>>(s->keys, s->prev_keys, n, s->mv_bcount);
+        k_mv_scan<<<1, 1024, 0, q>>>(s->mv_bcount, nb, total);
+        k_mv_compact<<<nb, 256, 0, q>>>(s->keys, s->prev_keys, n, s->mv_bcount, s->mv_prefix,
+                                        s->mv_key, s->mv_slot);
+        k_mv_rank<<<152 * 2, 256, 0, q>>>(total, s->mv_key, s->mv_slot, s->prev_keys, s->mv_prefix,
+                                          n, s->mv_skey, s->mv_sslot, s->mv_sorted, s->mv_perm);
+        k_mv_place<<<blocks(n, 256), 256, 0, q>>>(s->keys, s->prev_keys, n, s->mv_prefix, total,
+                                                  s->mv_skey, s->mv_sslot, s->mv_sorted, s->mv_perm);
+        st = launch_status("mixed near-sorted resort");
+        sk = s->mv_sorted;
+        sv = s->mv_perm;
+        if (st == XD_OK) {
             k_mx_clear<<<blocks(n, 256), 256, 0, q>>>(s->prev_keys, n, s->cstart, s->cend);
             st = launch_status("mixed clear cells");
         }
@@ -750,7 +1194,7 @@ static int grid_and_contacts(MixedScene* s, cudaStream_t q, const Phases& ph, bo
     ph.begin(6, q);
     const int nxt = 1 - s->cur;
     k_mx_reorder<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->m[nxt], sv, s->pf, s->qa, s->qb,
-                                                s->vf, s->wf);
+                                                s->vf, s->vlo, s->wf);
     st = launch_status("mixed reorder");
     s->cur = nxt;
     ph.end(6, q);
@@ -761,12 +1205,12 @@ static int grid_and_contacts(MixedScene* s, cudaStream_t q, const Phases& ph, bo
     // prev_keys now holds the sorted keys: the contact kernel reads cell coordinates from it
     if (record)
         k_mx_contact<true><<<blocks(n, 256), 256, 0, q>>>(
-            s->P, s->m[s->cur], s->pf, s->qa, s->qb, s->vf, s->wf, s->prev_keys, s->cstart, s->cend,
-            s->Fc, s->Mc, s->wall_list, s->counters, s->rec_count, s->rec_pairs, rec_cap);
+            s->P, s->m[s->cur], s->pf, s->qa, s->qb, s->vf, s->vlo, s->wf, s->prev_keys, s->cstart,
+            s->cend, s->Fc, s->Mc, s->wall_list, s->counters, s->rec_count, s->rec_pairs, rec_cap);
     else
         k_mx_contact<false><<<blocks(n, 256), 256, 0, q>>>(
-            s->P, s->m[s->cur], s->pf, s->qa, s->qb, s->vf, s->wf, s->prev_keys, s->cstart, s->cend,
-            s->Fc, s->Mc, s->wall_list, s->counters, nullptr, nullptr, 0);
+            s->P, s->m[s->cur], s->pf, s->qa, s->qb, s->vf, s->vlo, s->wf, s->prev_keys, s->cstart,
+            s->cend, s->Fc, s->Mc, s->wall_list, s->counters, nullptr, nullptr, 0);
     st = launch_status("mixed contact");
     ph.end(3, q);
     if (st != XD_OK || !s->nplanes) return st;
@@ -777,27 +1221,86 @@ static int grid_and_contacts(MixedScene* s, cudaStream_t q, const Phases& ph, bo
     return st;
 }
 
+// One middle step: grid, contacts and walls, then the fused velocity/position update.
+static int middle_step(MixedScene* s, cudaStream_t q, const Phases& ph, bool last)
+{
+    const unsigned n = s->n;
+    int st = grid_and_contacts(s, q, ph, false, 0);
+    if (st != XD_OK) return st;
+    ph.begin(0, q);
+    if (!last)
+        k_mx_integrate<1><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc, s->keys, s->vals);
+    else
+        k_mx_integrate<2><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc, s->keys, s->vals);
+    st = launch_status("mixed integrate");
+    ph.end(0, q);
+    return st;
+}
+
+// Captures two middle steps into a graph for the current buffer parity (the
+// pair of steps leaves the parity unchanged).  Needs cells_clean.
+static int capture_pair(MixedScene* s, cudaStream_t q)
+{
+    const int parity = s->cur;
+    cudaStream_t cs = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_status(e, "mixed graph stream");
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    int st = cuda_status(e, "mixed graph capture");
+    Phases none;
+    if (st == XD_OK) st = middle_step(s, cs, none, false);
+    if (st == XD_OK) st = middle_step(s, cs, none, false);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(cs, &g);
+    if (st == XD_OK) st = cuda_status(e, "mixed graph capture");
+    s->cur = parity;   // capture only recorded the launches
+    if (st == XD_OK) st = cuda_status(cudaGraphInstantiate(&s->graph[parity], g, 0), "mixed graph instantiate");
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    (void)q;
+    return st;
+}
+
 int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
 {
     if (nsteps == 0 || s->n == 0) return XD_OK;
     if (!s->ready) return set_error(XD_ERR_STATE, "mixed mode: no state uploaded");
     const unsigned n = s->n;
+    const bool graphs = s->use_graphs && ph.fn == nullptr;
     int st;
+    if (s->cells_clean && s->n > 1) {
+        // The near-sorted resort ranks the movers in O(M^2); after a burst of
+        // movers in the previous call, start this one with a full radix sort.
+        unsigned prev_movers = 0;
+        st = cuda_status(cudaMemcpyAsync(&prev_movers, s->counters + 4, sizeof(unsigned),
+                                         cudaMemcpyDeviceToHost, q), "mixed mover count");
+        if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "mixed mover count");
+        if (st != XD_OK) return st;
+        if (prev_movers > s->n / 16 || prev_movers > 65536u) s->cells_clean = false;
+    }
     ph.begin(0, q);
     k_mx_integrate<0><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc, s->keys, s->vals);
     st = launch_status("mixed integrate");
     ph.end(0, q);
     if (st != XD_OK) return st;
-    for (unsigned t = 0; t < nsteps; ++t) {
-        st = grid_and_contacts(s, q, ph, false, 0);
+    unsigned t = 0;
+    if (!s->cells_clean) {
+        st = middle_step(s, q, ph, nsteps == 1);
         if (st != XD_OK) return st;
-        ph.begin(0, q);
-        if (t + 1 < nsteps)
-            k_mx_integrate<1><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc, s->keys, s->vals);
-        else
-            k_mx_integrate<2><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc, s->keys, s->vals);
-        st = launch_status("mixed integrate");
-        ph.end(0, q);
+        t = 1;
+    }
+    // pairs of middle steps as one graph launch; the last step runs directly
+    while (graphs && nsteps - t >= 3) {
+        if (!s->graph[s->cur]) {
+            st = capture_pair(s, q);
+            if (st != XD_OK) return st;
+        }
+        st = cuda_status(cudaGraphLaunch(s->graph[s->cur], q), "mixed graph launch");
+        if (st != XD_OK) return st;
+        t += 2;   // two reorders: the buffer parity is unchanged
+    }
+    for (; t < nsteps; ++t) {
+        st = middle_step(s, q, ph, t + 1 == nsteps);
         if (st != XD_OK) return st;
     }
     s->state_valid_forces = false;
@@ -807,10 +1310,12 @@ int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
 unsigned long long mixed_launches(MixedScene* s, unsigned nsteps)
 {
     if (!s || nsteps == 0 || s->n == 0) return 0;
-    unsigned passes = (key_bits_for(s->ncell) + 7) / 8;
-    unsigned long long per = (s->n > 1 ? 5ull * passes : 0) + 1 /*clear or fill*/ + 1 /*bounds*/ +
-                             1 /*reorder*/ + 1 /*contact*/ + (s->nplanes ? 1 : 0) + 1 /*integrate*/;
-    return 1 + per * nsteps;
+    const unsigned passes = (key_bits_for(s->ncell) + 7) / 8;
+    // per step: 5 resort kernels + clear + bounds + reorder + contact (+ walls) + integrate
+    const unsigned long long per = 5 + 1 + 1 + 1 + 1 + (s->nplanes ? 1 : 0) + 1;
+    unsigned long long total = 1 + per * nsteps;   // + the first position update
+    if (!s->cells_clean && s->n > 1) total += 5ull * passes - 5;   // first step: full radix sort
+    return total;
 }
 
 int mixed_eval_contacts(MixedScene* s, double* force, double* moment, cudaStream_t q)

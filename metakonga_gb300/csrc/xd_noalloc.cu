@@ -11,7 +11,7 @@
 // allocation at all.
 //
 // * The array holds the scratch for up to XD_NOALLOC_MAX_ENTRIES entries
-//   (about 8.3 MB); it lives in every device that loads the library until the
+//   (about 9.4 MB); it lives in every device that loads the library until the
 //   process exits.  Larger sorts are rejected with XD_ERR_CAPACITY.
 // * Every call shares the array, which keeps the previous call's contents.
 //   The only word that must start at zero (the out-of-range-hash flag) is
@@ -36,7 +36,7 @@ namespace {
 // counts (256 x tiles) + scan chunk sums, each rounded up to 256 bytes.
 constexpr size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 constexpr size_t kMax = XD_NOALLOC_MAX_ENTRIES;
-constexpr size_t kTiles = (kMax + 4095) / 4096;
+constexpr size_t kTiles = (kMax + xd::kSortTile - 1) / xd::kSortTile;
 constexpr size_t kHist = 256 * kTiles;
 constexpr size_t kChunks = (kHist + 4095) / 4096;
 constexpr size_t kScratchBytes = 256 + al256(4 * kMax) + al256(4 * kMax) + al256(4 * kHist) +

@@ -10,7 +10,7 @@
 //                    first output slot;
 //   3. k_scatter     stable in-tile ranking with __match_any_sync and a
 //                    coalesced read of the tile, then the scatter.
-// A tile is 4096 keys: 8 warps x 16 rounds x 32 lanes, visited in index
+// A tile is 1024 keys: 8 warps x 4 rounds x 32 lanes, visited in index
 // order, so equal digits keep their input order and the sort is stable.
 #include <cuda_runtime.h>
 
@@ -23,8 +23,9 @@ constexpr int kBits = 8;
 constexpr int kRadix = 1 << kBits;
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
-constexpr int kRounds = 16;
-constexpr int kTile = kThreads * kRounds;   // 4096
+constexpr int kRounds = 4;
+constexpr int kTile = kThreads * kRounds;   // 1024
+static_assert(kTile == (int)kSortTile, "tile size shared with the fixed-scratch entry point");
 constexpr int kScanThreads = 1024;
 constexpr int kScanChunk = 4096;            // elements per scan block
 
