@@ -1,27 +1,46 @@
-// Mixed-precision scene step: FP64 state and integration, exact integer
-// contact decisions, FP32 contact forces.
+// Mixed-precision scene step: exact integer contact decisions, FP32 contact
+// forces, FP64 positions, double-float velocities.
 //
-// Per step (same order as dem_simulation::oneStepAnalysis,
-// dem_simulation.cpp:447-469):
-//   k_mx_integrate  FP64 velocity-Verlet: velocity of step t (from the FP32
-//                   contact force + m g) fused with the position of step t+1,
-//                   and the particle's cell key in the scene's own grid;
-//   radix sort      keys -> permutation (the state is kept in cell order, so
-//                   the permutation is close to the identity);
-//   k_mx_bounds     cell ranges (only the previous step's cells are cleared);
-//   k_mx_reorder    gathers the FP64 state into the new order and builds the
-//                   contact view: an FP32 float4 (x, y, z, r) for a cheap
-//                   prefilter and int64 fixed-point coordinates (2^-36 m);
-//   k_mx_contact    particle-particle forces: FP32 prefilter, then the exact
-//                   integer test N = (ri + rj)^2 - |qj - qi|^2 > 0 (no
-//                   cancellation), overlap delta = N / (R + |d|) with ~1e-7
-//                   relative precision, FP32 Hertz-Mindlin (DHSModel); pairs
-//                   within 2e-10 m of touching are decided by the reference's
-//                   FP64 expression instead, so pair lists equal the FP64
-//                   path's; particles near a wall are appended to a list;
-//   k_mx_walls      the listed particles' plane contacts in FP64.
+// GB300 issues about 1.6 FP64 operations per clock per SM against about 117
+// FP32 FMAs, so FP64 arithmetic in a per-particle kernel costs ~70 FP32
+// operations.  The state is laid out so that the bulk kernels do almost none:
+//   positions, radii        FP64 (the FP64 guard-band decisions and the
+//                           downloaded state are the uploaded bits)
+//   velocities, ang. vel.   double-float hi + lo (two FP32, ~48-bit
+//                           significand), updated with FP32 arithmetic
+//   accelerations           FP32: the contact part a - g, and alpha
+//   m, 1/m, 1/I             FP32 (the FP64 mass, by particle id, serves the
+//                           FP64 rechecks, the walls and the download)
+// The only FP64 operations per particle and step are the position update
+// (two adds per axis) and the fixed-point conversion (one FMA per axis).
+//
+// Per step (dem_simulation::oneStepAnalysis order, dem_simulation.cpp:447-469):
+//   k_mx_keys     the cell key of the next position, from an FP32 estimate
+//                 (the cell exceeds the contact range by a margin larger than
+//                 the estimate's error, so touching pairs stay in neighbour
+//                 cells);
+//   resort        near-sorted: only particles that changed cell are ranked
+//                 among the others (a full radix sort after an upload or a
+//                 burst of movers);
+//   k_lb_fill     lb[c] = first sorted slot whose key is >= c, for every cell,
+//                 so a row of three cells is the slot range [lb[c0], lb[c0+3]);
+//   k_mx_gather   moves the state into the new order and applies the
+//                 velocity-Verlet update on the way (velocity of step t from
+//                 the contact force, position of step t + 1), then writes the
+//                 contact view: FP32 (x, y, z, r) and int64 fixed point
+//                 (2^-36 m);
+//   k_mx_search   candidates: FP32 prefilter, then the exact integer test
+//                 N = (ri + rj)^2 - |qj - qi|^2 > 0 (no cancellation); pairs
+//                 within 2e-10 m of touching are decided by the reference's
+//                 FP64 expression, so pair lists equal the FP64 path's.  Each
+//                 particle's contacts go to a list in search order; particles
+//                 near a wall go to the wall list with a plane mask;
+//   k_mx_force    FP32 Hertz-Mindlin (DHSModel) over each particle's list in
+//                 the reference's pair order (a pair without slip reuses the
+//                 previous pair's tangential force, impl:426-428);
+//   k_mx_walls    the listed particles' plane contacts in FP64.
 // The grid is the scene's own (not the reference's wrapped 128^3): cell size
-// 2 r_max (+0.1 %), padded by one cell on every side, keys clamped inside.
+// 2 r_max plus a margin, padded by one cell on every side, keys clamped inside.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -39,30 +58,54 @@ namespace xd {
 namespace {
 
 constexpr int kMaxPlanes = 16;
-constexpr int kFields = 20;   // x y z r vx vy vz wx wy wz ax ay az bx by bz m I 1/m 1/I
-enum { FX, FY, FZ, FR, FVX, FVY, FVZ, FWX, FWY, FWZ, FAX, FAY, FAZ, FBX, FBY, FBZ, FM, FI, FIM, FII };
-constexpr double kQ = 68719476736.0;          // 2^36 fixed-point units per metre
-constexpr float kU = 1.4551915228366852e-11f; // 2^-36 m
-constexpr double kGuard = 2e-10;              // metres: FP64 decision inside this band
+constexpr double kQ = 68719476736.0;           // 2^36 fixed-point units per metre
+constexpr float kU = 1.4551915228366852e-11f;  // 2^-36 m
+constexpr double kGuard = 2e-10;               // metres: FP64 decision inside this band
+constexpr double kMagic = 6755399441055744.0;  // 1.5 * 2^52
+constexpr unsigned kListCap = 24;              // contacts per particle kept in the list
+constexpr unsigned kGuardBit = 0x80000000u;    // list entry decided by the FP64 test
+
+// Counter words (one memset clears [0, kPerStepCounters) every step).
+enum {
+    CN_WALLS = 0,      // wall-list length
+    CN_FORCE = 1,      // force-list length
+    CN_GAPS = 2,       // long gaps of the cell lower-bound array
+    kPerStepCounters = 3,
+    CN_DECISIONS = 3,  // FP64 contact decisions (cumulative)
+    CN_NORMALS = 4,    // FP64 normal-force rechecks (cumulative)
+    CN_SLIPS = 5,      // FP64 slip rechecks (cumulative)
+    CN_MOVERS = 6,     // particles that changed cell in the last resort
+    kCounters = 8
+};
 
 struct Master {
-    double* f[kFields];
-    unsigned* id;
+    double *x, *y, *z, *r;   // FP64 positions and radii
+    float4* vh;              // velocity hi; .w = m
+    float4* vl;              // velocity lo; .w = 1/m
+    float4* wh;              // angular velocity hi; .w = 1/I
+    float4* wl;              // angular velocity lo; .w = particle id (bits)
+    float4* ab;              // contact acceleration a - g; .w = alpha.x
+    float2* b2;              // alpha.y, alpha.z
 };
 
 struct MixParams {
     int gx, gy, gz;
     unsigned n;
-    double wo[3];
-    double inv_cs;
-    float inv_csf;
-    double dt, half2dt;
+    unsigned gxy;        // gx * gy: key offset of one cell in z
+    double wo[3];        // grid origin, a multiple of 2^-36 m
+    double qoff[3];      // 1.5 * 2^52 - wo * 2^36 (fixed-point offsets)
     double g[3];
-    float dtf;
-    float tol;          // prefilter tolerance (m)
+    double dt;
+    float inv_csf;
+    float dtf, hf, half2dtf;
+    float gf[3];
+    float2 dt_df;        // dt as double-float
+    float2 G1[3];        // dt * g, double-float (gravity's velocity increment)
+    float2 G2[3];        // dt^2 / 2 * g, double-float
+    float tol;           // prefilter tolerance (m)
     float c43Eeq, one_b2, sratio, fric;
-    double c43Eeq_d, one_b2_d;   // the same constants in FP64 (normal-force recheck)
-    long long guard_q;  // guard band in fixed-point units
+    double c43Eeq_d, one_b2_d;   // the same constants in FP64 (rechecks)
+    long long guard_q;   // guard band in fixed-point units
     int nplanes;
     float pxw[kMaxPlanes][3];   // plane corner relative to the grid origin (FP32)
     float pun[kMaxPlanes][3];   // unit normal (FP32)
@@ -78,19 +121,23 @@ struct MixedScene {
     MixParams P;
     Master m[2];
     int cur = 0;
-    // view (sorted order)
+    double* mass0 = nullptr;   // FP64 mass by particle id (rechecks, walls, download)
+    // contact view (sorted order)
     float4* pf = nullptr;
     longlong2* qa = nullptr;
     longlong2* qb = nullptr;
-    float4* vf = nullptr;
-    float4* vlo = nullptr;   // low parts of the double-float velocity
-    float4* wf = nullptr;
     float4* Fc = nullptr;
     float4* Mc = nullptr;
+    // contact lists
+    unsigned* ccount = nullptr;   // contacts per particle
+    unsigned* clist = nullptr;    // [kListCap][n]: partner slot | kGuardBit
+    unsigned* flist = nullptr;    // particles with contacts
     // grid
     unsigned *keys = nullptr, *vals = nullptr, *prev_keys = nullptr;
-    unsigned *cstart = nullptr, *cend = nullptr;
-    bool cells_clean = false;      // cstart/cend hold only prev_keys' cells
+    unsigned* lb = nullptr;       // ncell + 1 entries
+    uint4* gaps = nullptr;
+    unsigned gap_cap = 0;
+    bool cells_clean = false;     // prev_keys holds the current order's sorted keys
     void* sort_scratch = nullptr;
     // near-sorted resort buffers
     unsigned *mv_bcount = nullptr, *mv_prefix = nullptr, *mv_key = nullptr, *mv_slot = nullptr;
@@ -98,14 +145,13 @@ struct MixedScene {
     // walls
     xd_plane_info* planes = nullptr;
     xd_contact_property* cps = nullptr;
-    unsigned* wall_list = nullptr;
-    unsigned* counters = nullptr;   // [0] wall count, [1] FP64 decisions, [2] FP64 normal forces, [4] movers
+    uint2* wall_list = nullptr;   // (slot, plane mask)
+    unsigned* counters = nullptr;
     // pair recording
     unsigned* rec_count = nullptr;
     unsigned* rec_pairs = nullptr;
     // host-order transfer buffers
     double* xfer = nullptr;
-    bool state_valid_forces = false;   // Fc/Mc hold the forces of the current state
     bool ready = false;                // grid and buffers set up (first upload)
     cudaGraphExec_t graph[2] = { nullptr, nullptr };   // two middle steps, per buffer parity
     bool use_graphs = true;
@@ -131,140 +177,9 @@ int alloc(MixedScene* s, T** p, size_t count)
     return XD_OK;
 }
 
-// Cell of a position.  The offset from the grid origin is formed in FP64 and
-// scaled in FP32: the FP32 rounding (< 3e-7 m over a 4 m box) is far inside
-// the 0.1 % margin by which the cell exceeds the largest contact distance, so
-// every touching pair still lies in neighbouring cells.
-__device__ __forceinline__ unsigned cell_key(const MixParams& P, double x, double y, double z)
-{
-    int cx = (int)floorf((float)(x - P.wo[0]) * P.inv_csf) + 1;
-    int cy = (int)floorf((float)(y - P.wo[1]) * P.inv_csf) + 1;
-    int cz = (int)floorf((float)(z - P.wo[2]) * P.inv_csf) + 1;
-    cx = min(max(cx, 1), P.gx - 2);
-    cy = min(max(cy, 1), P.gy - 2);
-    cz = min(max(cz, 1), P.gz - 2);
-    return ((unsigned)cz * (unsigned)P.gy + (unsigned)cy) * (unsigned)P.gx + (unsigned)cx;
-}
+inline unsigned blocks(unsigned n, unsigned t) { return div_up(n ? n : 1u, t); }
 
-// MODE 0: position only (first step of a call); 1: velocity of step t fused
-// with the position of step t+1; 2: velocity only (last step of a call).
-template <int MODE>
-__global__ void __launch_bounds__(256) k_mx_integrate(MixParams P, Master M,
-                                                      const float4* __restrict__ Fc,
-                                                      const float4* __restrict__ Mc,
-                                                      unsigned* __restrict__ keys,
-                                                      unsigned* __restrict__ vals)
-{
-    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    double ax = M.f[FAX][i], ay = M.f[FAY][i], az = M.f[FAZ][i];
-    double vx = M.f[FVX][i], vy = M.f[FVY][i], vz = M.f[FVZ][i];
-    if (MODE != 0) {
-        const double im = M.f[FIM][i], iI = M.f[FII][i];
-        const float4 f = Fc[i], t = Mc[i];
-        // a' = (m g + F_contact) / m = g + F_contact / m (vv_update_velocity_kernel, impl:117-133)
-        double nax = fma(im, (double)f.x, P.g[0]);
-        double nay = fma(im, (double)f.y, P.g[1]);
-        double naz = fma(im, (double)f.z, P.g[2]);
-        double nbx = iI * (double)t.x, nby = iI * (double)t.y, nbz = iI * (double)t.z;
-        const double h = 0.5 * P.dt;
-        vx += h * (ax + nax);
-        vy += h * (ay + nay);
-        vz += h * (az + naz);
-        M.f[FWX][i] += h * (M.f[FBX][i] + nbx);
-        M.f[FWY][i] += h * (M.f[FBY][i] + nby);
-        M.f[FWZ][i] += h * (M.f[FBZ][i] + nbz);
-        M.f[FVX][i] = vx;
-        M.f[FVY][i] = vy;
-        M.f[FVZ][i] = vz;
-        M.f[FAX][i] = ax = nax;
-        M.f[FAY][i] = ay = nay;
-        M.f[FAZ][i] = az = naz;
-        M.f[FBX][i] = nbx;
-        M.f[FBY][i] = nby;
-        M.f[FBZ][i] = nbz;
-    }
-    double x = M.f[FX][i], y = M.f[FY][i], z = M.f[FZ][i];
-    if (MODE != 2) {
-        // vv_update_position_kernel (impl:85-96)
-        x += P.dt * vx + P.half2dt * ax;
-        y += P.dt * vy + P.half2dt * ay;
-        z += P.dt * vz + P.half2dt * az;
-        M.f[FX][i] = x;
-        M.f[FY][i] = y;
-        M.f[FZ][i] = z;
-    }
-    keys[i] = cell_key(P, x, y, z);
-    vals[i] = i;
-}
-
-// Gathers the state into the sorted order and builds the contact view.
-__global__ void __launch_bounds__(256) k_mx_reorder(MixParams P, Master S, Master D,
-                                                    const unsigned* __restrict__ perm,
-                                                    float4* __restrict__ pf,
-                                                    longlong2* __restrict__ qa,
-                                                    longlong2* __restrict__ qb,
-                                                    float4* __restrict__ vf,
-                                                    float4* __restrict__ vlo,
-                                                    float4* __restrict__ wf)
-{
-    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    unsigned o = perm[i];
-    double v[kFields];
-#pragma unroll
-    for (int k = 0; k < kFields; ++k) {
-        v[k] = __ldg(S.f[k] + o);
-        D.f[k][i] = v[k];
-    }
-    D.id[i] = __ldg(S.id + o);
-    double rx = v[FX] - P.wo[0], ry = v[FY] - P.wo[1], rz = v[FZ] - P.wo[2];
-    pf[i] = make_float4((float)rx, (float)ry, (float)rz, (float)v[FR]);
-    qa[i] = make_longlong2(__double2ll_rn(rx * kQ), __double2ll_rn(ry * kQ));
-    qb[i] = make_longlong2(__double2ll_rn(rz * kQ), __double2ll_rn(v[FR] * kQ));
-    const float hx = (float)v[FVX], hy = (float)v[FVY], hz = (float)v[FVZ];
-    vf[i] = make_float4(hx, hy, hz, (float)v[FM]);
-    vlo[i] = make_float4((float)(v[FVX] - (double)hx), (float)(v[FVY] - (double)hy),
-                         (float)(v[FVZ] - (double)hz), 0.f);
-    wf[i] = make_float4((float)v[FWX], (float)v[FWY], (float)v[FWZ], 0.f);
-}
-
-__global__ void __launch_bounds__(256) k_mx_clear(const unsigned* __restrict__ prev, unsigned n,
-                                                  unsigned* __restrict__ cstart,
-                                                  unsigned* __restrict__ cend)
-{
-    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    unsigned k = prev[i];
-    if (i == 0 || prev[i - 1] != k) {
-        cstart[k] = 0xffffffffu;
-        cend[k] = 0u;
-    }
-}
-
-__global__ void __launch_bounds__(256) k_mx_bounds(const unsigned* __restrict__ sk, unsigned n,
-                                                   unsigned* __restrict__ cstart,
-                                                   unsigned* __restrict__ cend,
-                                                   unsigned* __restrict__ prev)
-{
-    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    unsigned k = sk[i];
-    prev[i] = k;
-    if (i == 0 || sk[i - 1] != k) cstart[k] = i;
-    if (i == n - 1 || sk[i + 1] != k) cend[k] = i + 1;
-}
-
-// Reference FP64 contact decision (calculate_p2p_kernel, impl:449-452),
-// evaluated without multiply-add contraction like the oracle.
-__device__ __forceinline__ double fp64_cdist(const Master& M, unsigned i, unsigned j)
-{
-    double dx = __dsub_rn(__ldg(M.f[FX] + j), __ldg(M.f[FX] + i));
-    double dy = __dsub_rn(__ldg(M.f[FY] + j), __ldg(M.f[FY] + i));
-    double dz = __dsub_rn(__ldg(M.f[FZ] + j), __ldg(M.f[FZ] + i));
-    double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-    return __dsub_rn(__dadd_rn(__ldg(M.f[FR] + i), __ldg(M.f[FR] + j)), __dsqrt_rn(d2));
-}
+// ---- FP32 helpers ----------------------------------------------------------
 
 struct f3 {
     float x, y, z;
@@ -290,6 +205,52 @@ __device__ __forceinline__ void two_prod(float a, float b, float& p, float& e)
 {
     p = __fmul_rn(a, b);
     e = __fmaf_rn(a, b, -p);
+}
+// s + e = a + b exactly for |a| >= |b| (Dekker's FastTwoSum)
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e)
+{
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+// Double-float numbers hi + lo (|lo| <= ulp(hi) / 2): Dekker/Knuth pair
+// arithmetic, ~2^-48 relative rounding per operation.
+struct dfl {
+    float hi, lo;
+};
+__device__ __forceinline__ dfl df_add(dfl a, dfl b)
+{
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    dfl r;
+    fast_two_sum(s, e, r.hi, r.lo);
+    return r;
+}
+__device__ __forceinline__ dfl df_add_f(dfl a, float b)
+{
+    float s, e;
+    two_sum(a.hi, b, s, e);
+    e = __fadd_rn(e, a.lo);
+    dfl r;
+    fast_two_sum(s, e, r.hi, r.lo);
+    return r;
+}
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b)
+{
+    float p, e;
+    two_prod(a.hi, b.hi, p, e);
+    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+    dfl r;
+    fast_two_sum(p, e, r.hi, r.lo);
+    return r;
+}
+__device__ __forceinline__ dfl df_of(float2 v) { return dfl{ v.x, v.y }; }
+__device__ __forceinline__ double df_to_d(float hi, float lo) { return (double)hi + (double)lo; }
+__host__ inline float2 df_split(double v)
+{
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
 }
 
 // vj - vi of two double-float velocities (hi + lo) as an unevaluated pair
@@ -336,47 +297,414 @@ __device__ __forceinline__ float normal_speed(const float s[3], const float t[3]
     return __fadd_rn(q0, __fdiv_rn(rem, d0));
 }
 
+// ---- fixed point and the contact view --------------------------------------
+
+// round((x - wo) * 2^36), ties to even, in one FMA: x * 2^36 + (1.5 * 2^52 -
+// wo * 2^36) lies in [2^52, 2^53), where FP64 numbers are spaced 1 apart, so
+// the rounded sum's low bits are the integer.  Needs |x - wo| < 2^15 m.
+__device__ __forceinline__ long long fixed_q(double x, double off)
+{
+    return __double_as_longlong(__fma_rn(x, kQ, off)) - __double_as_longlong(kMagic);
+}
+
+// FP32 value of a fixed-point coordinate (|q| < 2^51), from two exact 32-bit
+// conversions (the 64-bit integer conversions run on the FP64 pipe).
+__device__ __forceinline__ float q_to_f(long long q)
+{
+    return __fmaf_rn(__int2float_rn((int)(q >> 20)), 0x1p-16f,
+                     __fmul_rn(__int2float_rn((int)(q & 0xfffff)), 0x1p-36f));
+}
+
+__device__ __forceinline__ void write_view(const MixParams& P, unsigned i, double x, double y,
+                                           double z, double r, float4* __restrict__ pf,
+                                           longlong2* __restrict__ qa, longlong2* __restrict__ qb)
+{
+    const long long qx = fixed_q(x, P.qoff[0]), qy = fixed_q(y, P.qoff[1]), qz = fixed_q(z, P.qoff[2]);
+    const long long qr = fixed_q(r, kMagic);
+    qa[i] = make_longlong2(qx, qy);
+    qb[i] = make_longlong2(qz, qr);
+    pf[i] = make_float4(q_to_f(qx), q_to_f(qy), q_to_f(qz), (float)r);
+}
+
+// Cell key of a position relative to the grid origin (FP32).  Interior cells
+// only: keys are clamped to [1, g - 2] on every axis.
+__device__ __forceinline__ unsigned cell_key(const MixParams& P, float x, float y, float z)
+{
+    int cx = (int)floorf(x * P.inv_csf) + 1;
+    int cy = (int)floorf(y * P.inv_csf) + 1;
+    int cz = (int)floorf(z * P.inv_csf) + 1;
+    cx = min(max(cx, 1), P.gx - 2);
+    cy = min(max(cy, 1), P.gy - 2);
+    cz = min(max(cz, 1), P.gz - 2);
+    return ((unsigned)cz * (unsigned)P.gy + (unsigned)cy) * (unsigned)P.gx + (unsigned)cx;
+}
+
+// ---- integration -----------------------------------------------------------
+//
+// Velocity Verlet as the reference splits it (vv_update_position_kernel
+// impl:85-96, vv_update_velocity_kernel impl:117-133), with a = g + F / m:
+//   MODE 0  position of step t + 1 from (v, a) of step t (first step of a call)
+//   MODE 1  velocity of step t from the step's contact force, then the
+//           position of step t + 1
+//   MODE 2  velocity only (last step of a call)
+//   MODE 3  no update (contacts of the current state)
+
+// k_mx_keys: the key of the next position, estimated in FP32 from the view.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_mx_keys(MixParams P, Master M, const float4* __restrict__ pf,
+                                                 const float4* __restrict__ Fc,
+                                                 unsigned* __restrict__ keys,
+                                                 unsigned* __restrict__ vals)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const float4 p = pf[i];
+    float x = p.x, y = p.y, z = p.z;
+    if (MODE == 0 || MODE == 1) {
+        const float4 v = M.vh[i], a = M.ab[i];
+        float vx = v.x, vy = v.y, vz = v.z, ax = a.x, ay = a.y, az = a.z;
+        if (MODE == 1) {
+            const float4 f = Fc[i];
+            const float im = M.vl[i].w;
+            const float nx = f.x * im, ny = f.y * im, nz = f.z * im;
+            vx += P.hf * (2.f * P.gf[0] + ax + nx);
+            vy += P.hf * (2.f * P.gf[1] + ay + ny);
+            vz += P.hf * (2.f * P.gf[2] + az + nz);
+            ax = nx;
+            ay = ny;
+            az = nz;
+        }
+        x += P.dtf * vx + P.half2dtf * (P.gf[0] + ax);
+        y += P.dtf * vy + P.half2dtf * (P.gf[1] + ay);
+        z += P.dtf * vz + P.half2dtf * (P.gf[2] + az);
+    }
+    keys[i] = cell_key(P, x, y, z);
+    vals[i] = i;
+}
+
+// Velocity update of one particle (MODE 1 and 2): v += dt g + h (a_c + a_c'),
+// w += h (alpha + alpha'), with a_c' = F / m and alpha' = M / I.
+__device__ __forceinline__ void kick(const MixParams& P, float4& vh, float4& vl, float4& wh,
+                                     float4& wl, float4& ab, float2& b2, const float4& f,
+                                     const float4& t)
+{
+    const float im = vl.w, iI = wh.w;
+    const float ax = f.x * im, ay = f.y * im, az = f.z * im;
+    const float bx = t.x * iI, by = t.y * iI, bz = t.z * iI;
+    dfl v;
+    v = df_add_f(df_add(dfl{ vh.x, vl.x }, df_of(P.G1[0])), P.hf * (ab.x + ax));
+    vh.x = v.hi; vl.x = v.lo;
+    v = df_add_f(df_add(dfl{ vh.y, vl.y }, df_of(P.G1[1])), P.hf * (ab.y + ay));
+    vh.y = v.hi; vl.y = v.lo;
+    v = df_add_f(df_add(dfl{ vh.z, vl.z }, df_of(P.G1[2])), P.hf * (ab.z + az));
+    vh.z = v.hi; vl.z = v.lo;
+    v = df_add_f(dfl{ wh.x, wl.x }, P.hf * (ab.w + bx));
+    wh.x = v.hi; wl.x = v.lo;
+    v = df_add_f(dfl{ wh.y, wl.y }, P.hf * (b2.x + by));
+    wh.y = v.hi; wl.y = v.lo;
+    v = df_add_f(dfl{ wh.z, wl.z }, P.hf * (b2.y + bz));
+    wh.z = v.hi; wl.z = v.lo;
+    ab = make_float4(ax, ay, az, bx);
+    b2 = make_float2(by, bz);
+}
+
+// x += dt v + dt^2/2 (g + a_c): the increment in double-float, added in FP64.
+__device__ __forceinline__ double drift(const MixParams& P, double x, float vhi, float vlo, int k,
+                                        float ac)
+{
+    dfl inc = df_mul(df_of(P.dt_df), dfl{ vhi, vlo });
+    inc = df_add(inc, df_of(P.G2[k]));
+    inc = df_add_f(inc, P.half2dtf * ac);
+    return __dadd_rn(x, __dadd_rn((double)inc.hi, (double)inc.lo));
+}
+
+// Gathers the state into the new order (perm: new slot -> old slot), applies
+// the update of MODE on the way and writes the contact view.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_mx_gather(MixParams P, Master S, Master D,
+                                                   const unsigned* __restrict__ perm,
+                                                   const float4* __restrict__ Fc,
+                                                   const float4* __restrict__ Mc,
+                                                   float4* __restrict__ pf,
+                                                   longlong2* __restrict__ qa,
+                                                   longlong2* __restrict__ qb)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const unsigned o = __ldg(perm + i);
+    double x = __ldg(S.x + o), y = __ldg(S.y + o), z = __ldg(S.z + o);
+    const double r = __ldg(S.r + o);
+    float4 vh = __ldg(S.vh + o), vl = __ldg(S.vl + o), wh = __ldg(S.wh + o), wl = __ldg(S.wl + o);
+    float4 ab = __ldg(S.ab + o);
+    float2 b2 = __ldg(S.b2 + o);
+    if (MODE == 1) kick(P, vh, vl, wh, wl, ab, b2, __ldg(Fc + o), __ldg(Mc + o));
+    if (MODE == 0 || MODE == 1) {
+        x = drift(P, x, vh.x, vl.x, 0, ab.x);
+        y = drift(P, y, vh.y, vl.y, 1, ab.y);
+        z = drift(P, z, vh.z, vl.z, 2, ab.z);
+    }
+    D.x[i] = x;
+    D.y[i] = y;
+    D.z[i] = z;
+    D.r[i] = r;
+    D.vh[i] = vh;
+    D.vl[i] = vl;
+    D.wh[i] = wh;
+    D.wl[i] = wl;
+    D.ab[i] = ab;
+    D.b2[i] = b2;
+    write_view(P, i, x, y, z, r, pf, qa, qb);
+}
+
+// MODE 2: velocity only, in place (the last step of a call).
+__global__ void __launch_bounds__(256) k_mx_finish(MixParams P, Master M, const float4* __restrict__ Fc,
+                                                   const float4* __restrict__ Mc)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    float4 vh = M.vh[i], vl = M.vl[i], wh = M.wh[i], wl = M.wl[i], ab = M.ab[i];
+    float2 b2 = M.b2[i];
+    kick(P, vh, vl, wh, wl, ab, b2, Fc[i], Mc[i]);
+    M.vh[i] = vh;
+    M.vl[i] = vl;
+    M.wh[i] = wh;
+    M.wl[i] = wl;
+    M.ab[i] = ab;
+    M.b2[i] = b2;
+}
+
+// ---- cell lower bounds -----------------------------------------------------
+//
+// lb[c] for c in (sk[t-1], sk[t]] is t (lb[0..sk[0]] = 0, lb(sk[n-1]..ncell] = n).
+// Each slot fills the gap of empty cells before its own: short gaps by the
+// thread, medium ones by its warp, long ones by every block (k_lb_long).
+constexpr unsigned kGapThread = 16, kGapWarp = 4096;
+
+__global__ void __launch_bounds__(256) k_lb_fill(const unsigned* __restrict__ sk, unsigned n,
+                                                 unsigned ncell, unsigned* __restrict__ lb,
+                                                 unsigned* __restrict__ prev,
+                                                 uint4* __restrict__ gaps,
+                                                 unsigned* __restrict__ counters)
+{
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;   // slots 0 .. n
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned lo = 1, hi = 0;
+    if (t <= n) {
+        const unsigned kc = t < n ? sk[t] : ncell;
+        if (t < n) prev[t] = kc;
+        lo = t == 0 ? 0u : sk[t - 1] + 1u;
+        hi = kc;
+    }
+    const unsigned len = hi >= lo ? hi - lo + 1u : 0u;
+    if (len && len <= kGapThread)
+        for (unsigned c = lo; c <= hi; ++c) lb[c] = t;
+    unsigned pend = __ballot_sync(0xffffffffu, len > kGapThread && len <= kGapWarp);
+    while (pend) {
+        const int src = __ffs(pend) - 1;
+        const unsigned glo = __shfl_sync(0xffffffffu, lo, src);
+        const unsigned ghi = __shfl_sync(0xffffffffu, hi, src);
+        const unsigned gv = __shfl_sync(0xffffffffu, t, src);
+        for (unsigned c = glo + lane; c <= ghi; c += 32) lb[c] = gv;
+        pend &= pend - 1u;
+    }
+    if (len > kGapWarp) gaps[atomicAdd(counters + CN_GAPS, 1u)] = make_uint4(lo, hi, t, 0u);
+}
+
+__global__ void __launch_bounds__(256) k_lb_long(const uint4* __restrict__ gaps,
+                                                 const unsigned* __restrict__ counters,
+                                                 unsigned* __restrict__ lb)
+{
+    const unsigned m = counters[CN_GAPS];
+    const unsigned stride = gridDim.x * blockDim.x;
+    for (unsigned g = 0; g < m; ++g) {
+        const uint4 G = gaps[g];
+        for (unsigned c = G.x + blockIdx.x * blockDim.x + threadIdx.x; c <= G.y; c += stride) lb[c] = G.z;
+    }
+}
+
+// ---- contacts --------------------------------------------------------------
+
+// Reference FP64 contact decision (calculate_p2p_kernel, impl:449-452),
+// evaluated without multiply-add contraction like the oracle.
+__device__ __forceinline__ double fp64_cdist(const Master& M, unsigned i, unsigned j)
+{
+    double dx = __dsub_rn(__ldg(M.x + j), __ldg(M.x + i));
+    double dy = __dsub_rn(__ldg(M.y + j), __ldg(M.y + i));
+    double dz = __dsub_rn(__ldg(M.z + j), __ldg(M.z + i));
+    double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    return __dsub_rn(__dadd_rn(__ldg(M.r + i), __ldg(M.r + j)), __dsqrt_rn(d2));
+}
+
+// Visits the contacts of slot i in the reference's order (neighbour rows z
+// then y, each row's slots ascending): fn(j, guard) for every touching j.
+// Candidates pass an FP32 prefilter, then the exact integer test; pairs in
+// the guard band are decided by fp64_cdist.
+template <bool COUNT, typename Fn>
+__device__ __forceinline__ void for_each_contact(const MixParams& P, const Master& M, unsigned i,
+                                                 const float4& pi, const longlong2& qai,
+                                                 const longlong2& qbi, unsigned key,
+                                                 const float4* __restrict__ pf,
+                                                 const longlong2* __restrict__ qa,
+                                                 const longlong2* __restrict__ qb,
+                                                 const unsigned* __restrict__ lb,
+                                                 unsigned* __restrict__ counters, Fn fn)
+{
+    // row (dz, dy) starts at cell key - 1 + dy gx + dz gx gy; the next row's
+    // bounds are loaded while this row's candidates are visited
+    unsigned c0 = key - 1u - (unsigned)P.gx - P.gxy;
+    unsigned s = __ldg(lb + c0), e = __ldg(lb + c0 + 3);
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+        const unsigned c1 = (r % 3 == 2) ? c0 - 2u * (unsigned)P.gx + P.gxy : c0 + (unsigned)P.gx;
+        unsigned sn = 0, en = 0;
+        if (r < 8) {
+            sn = __ldg(lb + c1);
+            en = __ldg(lb + c1 + 3);
+        }
+        for (unsigned j = s; j < e; ++j) {
+            if (j == i) continue;
+            const float4 pj = __ldg(pf + j);
+            const float dxf = pj.x - pi.x, dyf = pj.y - pi.y, dzf = pj.z - pi.z;
+            const float Rt = pi.w + pj.w + P.tol;
+            if (dxf * dxf + dyf * dyf + dzf * dzf >= Rt * Rt) continue;
+            const longlong2 qaj = __ldg(qa + j), qbj = __ldg(qb + j);
+            const long long ddx = qaj.x - qai.x, ddy = qaj.y - qai.y, ddz = qbj.x - qbi.x;
+            const long long Rq = qbi.y + qbj.y;
+            const long long N = Rq * Rq - (ddx * ddx + ddy * ddy + ddz * ddz);
+            const long long band = 2 * Rq * P.guard_q;
+            bool guard = false;
+            if (N <= band) {
+                if (N < -band) continue;
+                if (COUNT) atomicAdd(counters + CN_DECISIONS, 1u);
+                if (!(fp64_cdist(M, i, j) > 0)) continue;
+                guard = true;
+            }
+            fn(j, guard);
+        }
+        s = sn;
+        e = en;
+        c0 = c1;
+    }
+}
+
+// Appends v to list (counter *cnt) for the lanes where take is set, one
+// atomic per warp.  Every lane of the warp calls it.
+template <typename T>
+__device__ __forceinline__ void warp_append(bool take, const T& v, T* __restrict__ list,
+                                            unsigned* __restrict__ cnt)
+{
+    const unsigned bal = __ballot_sync(0xffffffffu, take);
+    if (!bal) return;
+    const unsigned lane = threadIdx.x & 31u;
+    const int leader = __ffs(bal) - 1;
+    unsigned base = 0;
+    if ((int)lane == leader) base = atomicAdd(cnt, (unsigned)__popc(bal));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (take) list[base + __popc(bal & ((1u << lane) - 1u))] = v;
+}
+
+// Candidate search of every particle: the contact list, the force list (the
+// particles with contacts; the others get zero contact force here), and the
+// wall list with each particle's mask of nearby planes.
+template <bool RECORD>
+__global__ void __launch_bounds__(256) k_mx_search(MixParams P, Master M, const float4* __restrict__ pf,
+                                                   const longlong2* __restrict__ qa,
+                                                   const longlong2* __restrict__ qb,
+                                                   const unsigned* __restrict__ keys,
+                                                   const unsigned* __restrict__ lb,
+                                                   unsigned* __restrict__ ccount,
+                                                   unsigned* __restrict__ clist,
+                                                   unsigned* __restrict__ flist,
+                                                   float4* __restrict__ Fc, float4* __restrict__ Mc,
+                                                   uint2* __restrict__ wall_list,
+                                                   unsigned* __restrict__ counters,
+                                                   unsigned* __restrict__ rec_count,
+                                                   unsigned* __restrict__ rec_pairs, unsigned rec_cap)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < P.n;
+    unsigned nc = 0, wmask = 0;
+    if (live) {
+        const float4 pi = __ldg(pf + i);
+        const longlong2 qai = __ldg(qa + i), qbi = __ldg(qb + i);
+        const unsigned n = P.n;
+        for_each_contact<true>(P, M, i, pi, qai, qbi, __ldg(keys + i), pf, qa, qb, lb, counters,
+                               [&](unsigned j, bool guard) {
+                                   if (nc < kListCap) clist[(size_t)nc * n + i] = j | (guard ? kGuardBit : 0u);
+                                   if (RECORD && nc < rec_cap) rec_pairs[(size_t)i * rec_cap + nc] = j;
+                                   ++nc;
+                               });
+        ccount[i] = nc;
+        if (RECORD) rec_count[i] = nc;
+        if (!nc) {
+            Fc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            Mc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        // walls: FP32 distance to each plane's supporting plane
+        for (int w = 0; w < P.nplanes; ++w) {
+            const float hz = (pi.x - P.pxw[w][0]) * P.pun[w][0] + (pi.y - P.pxw[w][1]) * P.pun[w][1] +
+                             (pi.z - P.pxw[w][2]) * P.pun[w][2];
+            if (fabsf(hz) < pi.w + P.wall_tol) wmask |= 1u << w;
+        }
+    }
+    warp_append(live && nc > 0, i, flist, counters + CN_FORCE);
+    warp_append(wmask != 0u, make_uint2(i, wmask), wall_list, counters + CN_WALLS);
+}
+
 // Per-particle contact state carried across the pairs of one particle (the
 // reference keeps Ft and M in the kernel across pairs, impl:426-428).
 struct PairAcc {
     f3 Ft, Mm, sumF, sumM;
 };
 
-// The force of one contact (i, j) with overlap `delta` (FP32), or, when
-// `guard` is set, with the overlap from the reference's FP64 test.
-// getConstant TCM = 1 (impl:238-246) and DHSModel (impl:379-401) in FP32, the
-// relative velocity formed from double-float velocities, and the two
+// Own data of particle i for its force loop.
+struct Own {
+    unsigned i;
+    longlong2 qa, qb;
+    float4 vh, vl;
+    f3 w;
+    float r, m;
+};
+
+// The force of one contact (i, j).  getConstant TCM = 1 (impl:238-246) and
+// DHSModel (impl:379-401) in FP32: the overlap from the exact integer
+// separation (or the reference's FP64 expression for guard-band pairs), the
+// relative velocity from the double-float velocities, and the two
 // cancellation cases (normal force near zero, rolling slip) formed in FP64.
-__device__ __forceinline__ void contact_force(const MixParams& P, const Master& M, unsigned i,
-                                              unsigned j, float delta, bool guard,
-                                              const longlong2& qai, const longlong2& qbi,
-                                              const float4& vi4, const float4& vil, const f3& wi,
-                                              float ir, float im, const float4* __restrict__ pf,
+__device__ __forceinline__ void contact_force(const MixParams& P, const Master& M, const Own& I,
+                                              unsigned j, bool guard, const double* __restrict__ mass0,
+                                              const float4* __restrict__ pf,
                                               const longlong2* __restrict__ qa,
                                               const longlong2* __restrict__ qb,
-                                              const float4* __restrict__ vf,
-                                              const float4* __restrict__ vlo,
-                                              const float4* __restrict__ wf,
                                               unsigned* __restrict__ counters, PairAcc& A)
 {
+    const unsigned i = I.i;
     const float dt = P.dtf;
     const longlong2 qaj = __ldg(qa + j), qbj = __ldg(qb + j);
-    const long long ddx = qaj.x - qai.x, ddy = qaj.y - qai.y, ddz = qbj.x - qbi.x;
+    const long long ddx = qaj.x - I.qa.x, ddy = qaj.y - I.qa.y, ddz = qbj.x - I.qb.x;
     const long long D2 = ddx * ddx + ddy * ddy + ddz * ddz;
     const float dn = sqrtf((float)D2);
+    float delta;
+    if (guard) {
+        delta = (float)fp64_cdist(M, i, j);
+    } else {
+        const long long Rq = I.qb.y + qbj.y;
+        delta = ((float)(Rq * Rq - D2) / ((float)Rq + dn)) * kU;
+    }
     const float inv = 1.0f / dn;
     const f3 u = fk((float)ddx * inv, (float)ddy * inv, (float)ddz * inv);
-    const float4 vj4 = __ldg(vf + j), wj4 = __ldg(wf + j), vjl = __ldg(vlo + j);
+    const float4 vj4 = __ldg(M.vh + j), vjl = __ldg(M.vl + j), wj4 = __ldg(M.wh + j);
     const f3 wj = fk(wj4.x, wj4.y, wj4.z);
     const float jr = __ldg(pf + j).w, jm = vj4.w;
+    const float ir = I.r, im = I.m;
     // vj - vi formed exactly from the double-float velocities
     float dvs[3], dvt[3];
-    df_diff(vj4.x, vi4.x, __fsub_rn(vjl.x, vil.x), dvs[0], dvt[0]);
-    df_diff(vj4.y, vi4.y, __fsub_rn(vjl.y, vil.y), dvs[1], dvt[1]);
-    df_diff(vj4.z, vi4.z, __fsub_rn(vjl.z, vil.z), dvs[2], dvt[2]);
+    df_diff(vj4.x, I.vh.x, __fsub_rn(vjl.x, I.vl.x), dvs[0], dvt[0]);
+    df_diff(vj4.y, I.vh.y, __fsub_rn(vjl.y, I.vl.y), dvs[1], dvt[1]);
+    df_diff(vj4.z, I.vh.z, __fsub_rn(vjl.z, I.vl.z), dvs[2], dvt[2]);
     const f3 dv = fk(dvs[0] + dvt[0], dvs[1] + dvt[1], dvs[2] + dvt[2]);
     // rv = vj + wj x (-rj u) - (vi + wi x (ri u))   (impl:455)
-    const f3 wterm = fcross(wj, (-jr) * u) - fcross(wi, ir * u);
+    const f3 wterm = fcross(wj, (-jr) * u) - fcross(I.w, ir * u);
     const f3 rv = dv + wterm;
     // rv . u = dv . u (the rotation term is perpendicular to u), in double-float
     const int dqi[3] = { (int)ddx, (int)ddy, (int)ddz };
@@ -385,16 +713,17 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     float ee = fdot(ev, ev);
     if (ee < 0.0025f * fdot(wterm, wterm)) {
         // rolling: the rotation term cancels most of the slip; form the slip in
-        // FP64 from the FP64 state (FP32 rounding of the terms would dominate)
-        atomicAdd(counters + 3, 1u);
+        // FP64 (FP32 rounding of the terms would dominate)
+        atomicAdd(counters + CN_SLIPS, 1u);
         const double dd = sqrt((double)D2);
         const double ux = (double)ddx / dd, uy = (double)ddy / dd, uz = (double)ddz / dd;
-        const double ri = __ldg(M.f[FR] + i), rj = __ldg(M.f[FR] + j);
-        const double wix = __ldg(M.f[FWX] + i), wiy = __ldg(M.f[FWY] + i), wiz = __ldg(M.f[FWZ] + i);
-        const double wjx = __ldg(M.f[FWX] + j), wjy = __ldg(M.f[FWY] + j), wjz = __ldg(M.f[FWZ] + j);
-        const double dvx = __ldg(M.f[FVX] + j) - __ldg(M.f[FVX] + i);
-        const double dvy = __ldg(M.f[FVY] + j) - __ldg(M.f[FVY] + i);
-        const double dvz = __ldg(M.f[FVZ] + j) - __ldg(M.f[FVZ] + i);
+        const double ri = __ldg(M.r + i), rj = __ldg(M.r + j);
+        const float4 wil = __ldg(M.wl + i), wjl = __ldg(M.wl + j);
+        const double wix = df_to_d(I.w.x, wil.x), wiy = df_to_d(I.w.y, wil.y), wiz = df_to_d(I.w.z, wil.z);
+        const double wjx = df_to_d(wj.x, wjl.x), wjy = df_to_d(wj.y, wjl.y), wjz = df_to_d(wj.z, wjl.z);
+        const double dvx = (double)dvs[0] + (double)dvt[0];
+        const double dvy = (double)dvs[1] + (double)dvt[1];
+        const double dvz = (double)dvs[2] + (double)dvt[2];
         const double rx = dvx - rj * (wjy * uz - wjz * uy) - ri * (wiy * uz - wiz * uy);
         const double ry = dvy - rj * (wjz * ux - wjx * uz) - ri * (wiz * ux - wix * uz);
         const double rz = dvz - rj * (wjx * uy - wjy * ux) - ri * (wix * uy - wiy * ux);
@@ -415,30 +744,31 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     if (fabsf(fn) < 0.03f * fmaxf(fabsf(fsn), fabsf(fdn))) {
         // The elastic and damping terms nearly cancel (the normal force of an
         // unloading contact crossing zero): FP32 rounding of each term would
-        // dominate the small sum, so it is formed in FP64 from the FP64 state,
-        // with the overlap and normal taken from the FP64 positions.
-        atomicAdd(counters + 2, 1u);
-        const double px = __ldg(M.f[FX] + j) - __ldg(M.f[FX] + i);
-        const double py = __ldg(M.f[FY] + j) - __ldg(M.f[FY] + i);
-        const double pz = __ldg(M.f[FZ] + j) - __ldg(M.f[FZ] + i);
+        // dominate the small sum, so it is formed in FP64, with the overlap
+        // and normal from the FP64 positions.
+        atomicAdd(counters + CN_NORMALS, 1u);
+        const double px = __ldg(M.x + j) - __ldg(M.x + i);
+        const double py = __ldg(M.y + j) - __ldg(M.y + i);
+        const double pz = __ldg(M.z + j) - __ldg(M.z + i);
         const double dd = sqrt(px * px + py * py + pz * pz);
         const double ux = px / dd, uy = py / dd, uz = pz / dd;
         const double dl = fp64_cdist(M, i, j);
-        const double ri = __ldg(M.f[FR] + i), rj = __ldg(M.f[FR] + j);
-        const double mi = __ldg(M.f[FM] + i), mj = __ldg(M.f[FM] + j);
-        const double vix = __ldg(M.f[FVX] + i), viy = __ldg(M.f[FVY] + i), viz = __ldg(M.f[FVZ] + i);
-        const double vjx = __ldg(M.f[FVX] + j), vjy = __ldg(M.f[FVY] + j), vjz = __ldg(M.f[FVZ] + j);
-        const double wix = __ldg(M.f[FWX] + i), wiy = __ldg(M.f[FWY] + i), wiz = __ldg(M.f[FWZ] + i);
-        const double wjx = __ldg(M.f[FWX] + j), wjy = __ldg(M.f[FWY] + j), wjz = __ldg(M.f[FWZ] + j);
-        const double rvx = (vjx - rj * (wjy * uz - wjz * uy)) - (vix + ri * (wiy * uz - wiz * uy));
-        const double rvy = (vjy - rj * (wjz * ux - wjx * uz)) - (viy + ri * (wiz * ux - wix * uz));
-        const double rvz = (vjz - rj * (wjx * uy - wjy * ux)) - (viz + ri * (wix * uy - wiy * ux));
+        const double ri = __ldg(M.r + i), rj = __ldg(M.r + j);
+        const float4 wil = __ldg(M.wl + i), wjl = __ldg(M.wl + j);
+        const double mi = __ldg(mass0 + __float_as_uint(wil.w)), mj = __ldg(mass0 + __float_as_uint(wjl.w));
+        const double wix = df_to_d(I.w.x, wil.x), wiy = df_to_d(I.w.y, wil.y), wiz = df_to_d(I.w.z, wil.z);
+        const double wjx = df_to_d(wj.x, wjl.x), wjy = df_to_d(wj.y, wjl.y), wjz = df_to_d(wj.z, wjl.z);
+        const double dvx = (double)dvs[0] + (double)dvt[0];
+        const double dvy = (double)dvs[1] + (double)dvt[1];
+        const double dvz = (double)dvs[2] + (double)dvt[2];
+        const double rvx = dvx - rj * (wjy * uz - wjz * uy) - ri * (wiy * uz - wiz * uy);
+        const double rvy = dvy - rj * (wjz * ux - wjx * uz) - ri * (wiz * ux - wix * uz);
+        const double rvz = dvz - rj * (wjx * uy - wjy * ux) - ri * (wix * uy - wiy * ux);
         const double Meqd = (mi * mj) / (mi + mj), Reqd = (ri * rj) / (ri + rj);
         const double knd = P.c43Eeq_d * sqrt(Reqd);
         const double vnd = sqrt((4.0 * Meqd * knd) / P.one_b2_d);
         fn = (float)(-knd * (dl * sqrt(dl)) + vnd * (rvx * ux + rvy * uy + rvz * uz));
     }
-    (void)guard;
     const f3 Fn = fn * u;
     const float mag_e = sqrtf(ee);
     if (mag_e != 0.f) {
@@ -451,178 +781,82 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     A.sumM = A.sumM + A.Mm;
 }
 
-constexpr int kMaxStaged = 20;   // contacts staged per thread in shared memory
-
-// Particle-particle contacts in two phases: (1) the candidate loop -- FP32
-// prefilter, exact integer test, FP64 guard band -- stages each contact's
-// partner and overlap in shared memory; (2) the force loop runs over the
-// staged contacts in the same order.  A particle with more contacts than the
-// stage holds finishes the rest by re-scanning its candidates (same order).
-template <bool RECORD>
-__global__ void __launch_bounds__(256) k_mx_contact(MixParams P, Master M,
-                                                    const float4* __restrict__ pf,
-                                                    const longlong2* __restrict__ qa,
-                                                    const longlong2* __restrict__ qb,
-                                                    const float4* __restrict__ vf,
-                                                    const float4* __restrict__ vlo,
-                                                    const float4* __restrict__ wf,
-                                                    const unsigned* __restrict__ keys,
-                                                    const unsigned* __restrict__ cstart,
-                                                    const unsigned* __restrict__ cend,
-                                                    float4* __restrict__ Fc, float4* __restrict__ Mc,
-                                                    unsigned* __restrict__ wall_list,
-                                                    unsigned* __restrict__ counters,
-                                                    unsigned* __restrict__ rec_count,
-                                                    unsigned* __restrict__ rec_pairs, unsigned rec_cap)
+// Forces of the particles with contacts, over each one's list in search
+// order; a particle with more than kListCap contacts finds the rest by
+// searching again (same order).
+__global__ void __launch_bounds__(256) k_mx_force(MixParams P, Master M, const float4* __restrict__ pf,
+                                                  const longlong2* __restrict__ qa,
+                                                  const longlong2* __restrict__ qb,
+                                                  const unsigned* __restrict__ keys,
+                                                  const unsigned* __restrict__ lb,
+                                                  const unsigned* __restrict__ ccount,
+                                                  const unsigned* __restrict__ clist,
+                                                  const unsigned* __restrict__ flist,
+                                                  const double* __restrict__ mass0,
+                                                  float4* __restrict__ Fc, float4* __restrict__ Mc,
+                                                  unsigned* __restrict__ counters)
 {
-    __shared__ unsigned st_j[kMaxStaged][256];
-    __shared__ float st_d[kMaxStaged][256];
-    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    const unsigned tx = threadIdx.x;
-    const float4 pi = __ldg(pf + i);
-    const longlong2 qai = __ldg(qa + i), qbi = __ldg(qb + i);
-    const float ir = pi.w;
-    const unsigned key = __ldg(keys + i);
-    const int cx = (int)(key % (unsigned)P.gx);
-    const int cy = (int)((key / (unsigned)P.gx) % (unsigned)P.gy);
-    const int cz = (int)(key / ((unsigned)P.gx * (unsigned)P.gy));
-    unsigned ncont = 0;
-    // ---- phase 1: candidates
-    for (int dz = -1; dz <= 1; ++dz) {
-        for (int dy = -1; dy <= 1; ++dy) {
-            const unsigned c0 = ((unsigned)(cz + dz) * (unsigned)P.gy + (unsigned)(cy + dy)) * (unsigned)P.gx +
-                                (unsigned)(cx - 1);
-            const unsigned s = min(min(__ldg(cstart + c0), __ldg(cstart + c0 + 1)), __ldg(cstart + c0 + 2));
-            const unsigned e = max(max(__ldg(cend + c0), __ldg(cend + c0 + 1)), __ldg(cend + c0 + 2));
-            for (unsigned j = s; j < e; ++j) {
-                if (j == i) continue;
-                const float4 pj = __ldg(pf + j);
-                const float dxf = pj.x - pi.x, dyf = pj.y - pi.y, dzf = pj.z - pi.z;
-                const float Rt = ir + pj.w + P.tol;
-                if (dxf * dxf + dyf * dyf + dzf * dzf >= Rt * Rt) continue;
-                // exact integer test on the fixed-point coordinates
-                const longlong2 qaj = __ldg(qa + j), qbj = __ldg(qb + j);
-                const long long ddx = qaj.x - qai.x, ddy = qaj.y - qai.y, ddz = qbj.x - qbi.x;
-                const long long Rq = qbi.y + qbj.y;
-                const long long D2 = ddx * ddx + ddy * ddy + ddz * ddz;
-                const long long N = Rq * Rq - D2;
-                const long long band = 2 * Rq * P.guard_q;
-                float delta;
-                if (N > band) {
-                    delta = ((float)N / ((float)Rq + sqrtf((float)D2))) * kU;
-                } else if (N < -band) {
-                    continue;
-                } else {
-                    atomicAdd(counters + 1, 1u);
-                    const double cd = fp64_cdist(M, i, j);
-                    if (!(cd > 0)) continue;
-                    delta = -(float)cd;     // negative: decided by the FP64 test
-                }
-                if (RECORD && ncont < rec_cap) rec_pairs[(size_t)i * rec_cap + ncont] = j;
-                if (ncont < (unsigned)kMaxStaged) {
-                    st_j[ncont][tx] = j;
-                    st_d[ncont][tx] = delta;
-                }
-                ++ncont;
-            }
+    const unsigned total = counters[CN_FORCE];
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        Own I;
+        I.i = __ldg(flist + t);
+        const unsigned i = I.i;
+        const unsigned nc = __ldg(ccount + i);
+        I.qa = __ldg(qa + i);
+        I.qb = __ldg(qb + i);
+        I.vh = __ldg(M.vh + i);
+        I.vl = __ldg(M.vl + i);
+        const float4 w4 = __ldg(M.wh + i);
+        I.w = fk(w4.x, w4.y, w4.z);
+        I.r = __ldg(pf + i).w;
+        I.m = I.vh.w;
+        PairAcc A;
+        A.Ft = fk(0.f, 0.f, 0.f);
+        A.Mm = fk(0.f, 0.f, 0.f);
+        A.sumF = fk(0.f, 0.f, 0.f);
+        A.sumM = fk(0.f, 0.f, 0.f);
+        const unsigned nl = min(nc, kListCap);
+        for (unsigned k = 0; k < nl; ++k) {
+            const unsigned e = __ldg(clist + (size_t)k * P.n + i);
+            contact_force(P, M, I, e & ~kGuardBit, (e & kGuardBit) != 0u, mass0, pf, qa, qb, counters, A);
         }
-    }
-    if (RECORD) rec_count[i] = ncont;
-    // ---- phase 2: forces of the staged contacts, in search order
-    PairAcc A;
-    A.Ft = fk(0.f, 0.f, 0.f);
-    A.Mm = fk(0.f, 0.f, 0.f);
-    A.sumF = fk(0.f, 0.f, 0.f);
-    A.sumM = fk(0.f, 0.f, 0.f);
-    if (ncont) {
-        const float4 vi4 = __ldg(vf + i), vil = __ldg(vlo + i), wi4 = __ldg(wf + i);
-        const f3 wi = fk(wi4.x, wi4.y, wi4.z);
-        const float im = vi4.w;
-        const unsigned nst = min(ncont, (unsigned)kMaxStaged);
-        for (unsigned c = 0; c < nst; ++c) {
-            const float d = st_d[c][tx];
-            contact_force(P, M, i, st_j[c][tx], fabsf(d), d < 0.f, qai, qbi, vi4, vil, wi, ir, im, pf,
-                          qa, qb, vf, vlo, wf, counters, A);
-        }
-        if (ncont > (unsigned)kMaxStaged) {
-            // ---- phase 3 (rare): contacts beyond the stage, by re-scanning
+        if (nc > kListCap) {
             unsigned k = 0;
-            for (int dz = -1; dz <= 1; ++dz)
-                for (int dy = -1; dy <= 1; ++dy) {
-                    const unsigned c0 = ((unsigned)(cz + dz) * (unsigned)P.gy + (unsigned)(cy + dy)) *
-                                            (unsigned)P.gx + (unsigned)(cx - 1);
-                    const unsigned s = min(min(__ldg(cstart + c0), __ldg(cstart + c0 + 1)), __ldg(cstart + c0 + 2));
-                    const unsigned e = max(max(__ldg(cend + c0), __ldg(cend + c0 + 1)), __ldg(cend + c0 + 2));
-                    for (unsigned j = s; j < e; ++j) {
-                        if (j == i) continue;
-                        const float4 pj = __ldg(pf + j);
-                        const float dxf = pj.x - pi.x, dyf = pj.y - pi.y, dzf = pj.z - pi.z;
-                        const float Rt = ir + pj.w + P.tol;
-                        if (dxf * dxf + dyf * dyf + dzf * dzf >= Rt * Rt) continue;
-                        const longlong2 qaj = __ldg(qa + j), qbj = __ldg(qb + j);
-                        const long long ddx = qaj.x - qai.x, ddy = qaj.y - qai.y, ddz = qbj.x - qbi.x;
-                        const long long Rq = qbi.y + qbj.y;
-                        const long long D2 = ddx * ddx + ddy * ddy + ddz * ddz;
-                        const long long N = Rq * Rq - D2;
-                        const long long band = 2 * Rq * P.guard_q;
-                        float delta;
-                        if (N > band) {
-                            delta = ((float)N / ((float)Rq + sqrtf((float)D2))) * kU;
-                        } else if (N < -band) {
-                            continue;
-                        } else {
-                            const double cd = fp64_cdist(M, i, j);
-                            if (!(cd > 0)) continue;
-                            delta = (float)cd;
-                        }
-                        if (k++ < (unsigned)kMaxStaged) continue;
-                        contact_force(P, M, i, j, delta, false, qai, qbi, vi4, vil, wi, ir, im, pf, qa,
-                                      qb, vf, vlo, wf, counters, A);
-                    }
-                }
+            for_each_contact<false>(P, M, i, __ldg(pf + i), I.qa, I.qb, __ldg(keys + i), pf, qa, qb, lb,
+                                    counters, [&](unsigned j, bool guard) {
+                                        if (k++ >= kListCap)
+                                            contact_force(P, M, I, j, guard, mass0, pf, qa, qb, counters, A);
+                                    });
         }
-    }
-    Fc[i] = make_float4(A.sumF.x, A.sumF.y, A.sumF.z, 0.f);
-    Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
-    // walls: FP32 distance to each plane's supporting plane; near ones go to the FP64 pass
-    bool near = false;
-    for (int w = 0; w < P.nplanes; ++w) {
-        const float hz = (pi.x - P.pxw[w][0]) * P.pun[w][0] + (pi.y - P.pxw[w][1]) * P.pun[w][1] +
-                         (pi.z - P.pxw[w][2]) * P.pun[w][2];
-        near |= fabsf(hz) < ir + P.wall_tol;
-    }
-    const unsigned act = __activemask();
-    const unsigned ballot = __ballot_sync(act, near);
-    if (ballot) {
-        const unsigned lane = threadIdx.x & 31u;
-        const int leader = __ffs(ballot) - 1;
-        unsigned base = 0;
-        if ((int)lane == leader) base = atomicAdd(counters, (unsigned)__popc(ballot));
-        base = __shfl_sync(act, base, leader);
-        if (near) wall_list[base + __popc(ballot & ((1u << lane) - 1u))] = i;
+        Fc[i] = make_float4(A.sumF.x, A.sumF.y, A.sumF.z, 0.f);
+        Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
     }
 }
 
-// plane_contact_force_kernel<1> (impl:572-621) for the listed particles, all
-// planes in order, in FP64; adds to the FP32 contact force.
+// plane_contact_force_kernel<1> (impl:572-621) for the listed particles, the
+// planes of each one's mask in order (the others are out of reach and add
+// exactly zero), in FP64; adds to the FP32 contact force.
 __global__ void __launch_bounds__(128) k_mx_walls(MixParams P, Master M,
                                                   const xd_plane_info* __restrict__ planes,
                                                   const xd_contact_property* __restrict__ cps,
-                                                  const unsigned* __restrict__ wall_list,
+                                                  const uint2* __restrict__ wall_list,
                                                   const unsigned* __restrict__ counters,
+                                                  const double* __restrict__ mass0,
                                                   float4* __restrict__ Fc)
 {
-    const unsigned count = counters[0];
+    const unsigned count = counters[CN_WALLS];
     for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
-        const unsigned i = wall_list[k];
-        const double m = M.f[FM][i];
-        const d3 ip = mk(M.f[FX][i], M.f[FY][i], M.f[FZ][i]);
-        const double r = M.f[FR][i];
-        const d3 iv = mk(M.f[FVX][i], M.f[FVY][i], M.f[FVZ][i]);
-        const d3 iw = mk(M.f[FWX][i], M.f[FWY][i], M.f[FWZ][i]);
+        const uint2 wl = wall_list[k];
+        const unsigned i = wl.x;
+        const float4 vh = M.vh[i], vl = M.vl[i], wh = M.wh[i], wlo = M.wl[i];
+        const double m = mass0[__float_as_uint(wlo.w)];
+        const d3 ip = mk(M.x[i], M.y[i], M.z[i]);
+        const double r = M.r[i];
+        const d3 iv = mk(df_to_d(vh.x, vl.x), df_to_d(vh.y, vl.y), df_to_d(vh.z, vl.z));
+        const d3 iw = mk(df_to_d(wh.x, wlo.x), df_to_d(wh.y, wlo.y), df_to_d(wh.z, wlo.z));
         d3 f = mk(0, 0, 0);
-        for (int w = 0; w < P.nplanes; ++w) {
+        for (unsigned mask = wl.y; mask; mask &= mask - 1u) {
+            const int w = __ffs(mask) - 1;
             PlaneD pe = load_plane(planes + w);
             d3 Fn = mk(0, 0, 0), Ft = mk(0, 0, 0), Mo = mk(0, 0, 0);
             d3 dp = ip - pe.xw;
@@ -645,70 +879,87 @@ __global__ void __launch_bounds__(128) k_mx_walls(MixParams P, Master M,
     }
 }
 
-// host-order state <-> master (reference layouts)
+// ---- host-order state <-> master (reference layouts) -----------------------
+
 __global__ void __launch_bounds__(256) k_mx_load(MixParams P, Master M, const double* __restrict__ pos,
                                                  const double* __restrict__ vel,
                                                  const double* __restrict__ acc,
                                                  const double* __restrict__ omega,
                                                  const double* __restrict__ alpha,
                                                  const double* __restrict__ mass,
-                                                 const double* __restrict__ inertia)
+                                                 const double* __restrict__ inertia,
+                                                 double* __restrict__ mass0, float4* __restrict__ pf,
+                                                 longlong2* __restrict__ qa, longlong2* __restrict__ qb)
 {
-    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    M.f[FX][i] = pos[4 * (size_t)i + 0];
-    M.f[FY][i] = pos[4 * (size_t)i + 1];
-    M.f[FZ][i] = pos[4 * (size_t)i + 2];
-    M.f[FR][i] = pos[4 * (size_t)i + 3];
+    const size_t i3 = 3 * (size_t)i;
+    const double x = pos[4 * (size_t)i + 0], y = pos[4 * (size_t)i + 1], z = pos[4 * (size_t)i + 2];
+    const double r = pos[4 * (size_t)i + 3];
+    M.x[i] = x;
+    M.y[i] = y;
+    M.z[i] = z;
+    M.r[i] = r;
+    const double m = mass[i], I = inertia[i];
+    mass0[i] = m;
+    float h[3], l[3], wh[3], wl[3];
     for (int a = 0; a < 3; ++a) {
-        M.f[FVX + a][i] = vel[3 * (size_t)i + a];
-        M.f[FWX + a][i] = omega[3 * (size_t)i + a];
-        M.f[FAX + a][i] = acc[3 * (size_t)i + a];
-        M.f[FBX + a][i] = alpha[3 * (size_t)i + a];
+        const double v = vel[i3 + a], w = omega[i3 + a];
+        h[a] = __double2float_rn(v);
+        l[a] = __double2float_rn(v - (double)h[a]);
+        wh[a] = __double2float_rn(w);
+        wl[a] = __double2float_rn(w - (double)wh[a]);
     }
-    double m = mass[i], I = inertia[i];
-    M.f[FM][i] = m;
-    M.f[FI][i] = I;
-    M.f[FIM][i] = 1.0 / m;
-    M.f[FII][i] = 1.0 / I;
-    M.id[i] = i;
+    M.vh[i] = make_float4(h[0], h[1], h[2], (float)m);
+    M.vl[i] = make_float4(l[0], l[1], l[2], (float)(1.0 / m));
+    M.wh[i] = make_float4(wh[0], wh[1], wh[2], (float)(1.0 / I));
+    M.wl[i] = make_float4(wl[0], wl[1], wl[2], __uint_as_float(i));
+    M.ab[i] = make_float4((float)(acc[i3 + 0] - P.g[0]), (float)(acc[i3 + 1] - P.g[1]),
+                          (float)(acc[i3 + 2] - P.g[2]), (float)alpha[i3 + 0]);
+    M.b2[i] = make_float2((float)alpha[i3 + 1], (float)alpha[i3 + 2]);
+    write_view(P, i, x, y, z, r, pf, qa, qb);
 }
 
-__global__ void __launch_bounds__(256) k_mx_store(MixParams P, Master M, double* __restrict__ pos,
-                                                  double* __restrict__ vel, double* __restrict__ acc,
-                                                  double* __restrict__ omega,
+__global__ void __launch_bounds__(256) k_mx_store(MixParams P, Master M, const double* __restrict__ mass0,
+                                                  double* __restrict__ pos, double* __restrict__ vel,
+                                                  double* __restrict__ acc, double* __restrict__ omega,
                                                   double* __restrict__ alpha,
                                                   double* __restrict__ force,
                                                   double* __restrict__ moment)
 {
-    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    size_t o = M.id[i];
-    pos[4 * o + 0] = M.f[FX][i];
-    pos[4 * o + 1] = M.f[FY][i];
-    pos[4 * o + 2] = M.f[FZ][i];
-    pos[4 * o + 3] = M.f[FR][i];
-    double m = M.f[FM][i];
+    const float4 vh = M.vh[i], vl = M.vl[i], wh = M.wh[i], wl = M.wl[i], ab = M.ab[i];
+    const float2 b2 = M.b2[i];
+    const size_t o = __float_as_uint(wl.w);
+    pos[4 * o + 0] = M.x[i];
+    pos[4 * o + 1] = M.y[i];
+    pos[4 * o + 2] = M.z[i];
+    pos[4 * o + 3] = M.r[i];
+    const double m = mass0[o];
+    const float vh3[3] = { vh.x, vh.y, vh.z }, vl3[3] = { vl.x, vl.y, vl.z };
+    const float wh3[3] = { wh.x, wh.y, wh.z }, wl3[3] = { wl.x, wl.y, wl.z };
+    const float a3[3] = { ab.x, ab.y, ab.z }, b3[3] = { ab.w, b2.x, b2.y };
     for (int a = 0; a < 3; ++a) {
-        vel[3 * o + a] = M.f[FVX + a][i];
-        omega[3 * o + a] = M.f[FWX + a][i];
-        acc[3 * o + a] = M.f[FAX + a][i];
-        alpha[3 * o + a] = M.f[FBX + a][i];
+        vel[3 * o + a] = df_to_d(vh3[a], vl3[a]);
+        omega[3 * o + a] = df_to_d(wh3[a], wl3[a]);
+        acc[3 * o + a] = P.g[a] + (double)a3[a];
+        alpha[3 * o + a] = b3[a];
         force[3 * o + a] = m * P.g[a];
         moment[3 * o + a] = 0.0;
     }
 }
 
-__global__ void __launch_bounds__(256) k_mx_store_forces(MixParams P, const unsigned* __restrict__ id,
+__global__ void __launch_bounds__(256) k_mx_store_forces(MixParams P, Master M,
                                                          const float4* __restrict__ Fc,
                                                          const float4* __restrict__ Mc,
                                                          double* __restrict__ force,
                                                          double* __restrict__ moment)
 {
-    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    size_t o = id[i];
-    float4 f = Fc[i], t = Mc[i];
+    const size_t o = __float_as_uint(M.wl[i].w);
+    const float4 f = Fc[i], t = Mc[i];
     force[3 * o + 0] = f.x;
     force[3 * o + 1] = f.y;
     force[3 * o + 2] = f.z;
@@ -717,13 +968,11 @@ __global__ void __launch_bounds__(256) k_mx_store_forces(MixParams P, const unsi
     moment[3 * o + 2] = t.z;
 }
 
-__global__ void __launch_bounds__(256) k_mx_keys(MixParams P, Master M, unsigned* __restrict__ keys,
-                                                 unsigned* __restrict__ vals)
+__global__ void __launch_bounds__(256) k_mx_ids(MixParams P, Master M, unsigned* __restrict__ ids)
 {
-    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    keys[i] = cell_key(P, M.f[FX][i], M.f[FY][i], M.f[FZ][i]);
-    vals[i] = i;
+    ids[i] = __float_as_uint(M.wl[i].w);
 }
 
 // ---- near-sorted resort ("movers") -----------------------------------------
@@ -919,8 +1168,6 @@ __global__ void __launch_bounds__(256) k_mv_place(const unsigned* __restrict__ k
     perm[pos] = i;
 }
 
-inline unsigned blocks(unsigned n, unsigned t) { return div_up(n ? n : 1u, t); }
-
 }  // namespace
 
 // ------------------------------------------------------------------ host
@@ -929,6 +1176,7 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
 {
     s->n = d.np;
     s->nplanes = d.nplanes;
+    if (d.np >= 0x7fffffffu) return set_error(XD_ERR_CAPACITY, "mixed mode: too many particles");
     // grid from the bounding box of particles and walls
     double lo[3] = { 1e300, 1e300, 1e300 }, hi[3] = { -1e300, -1e300, -1e300 };
     double rmax = 0.0;
@@ -953,35 +1201,51 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
         rmax = 0.5;
     }
     if (!(rmax > 0.0)) return set_error(XD_ERR_INVALID, "mixed mode: particle radii must be > 0");
-    s->cs = 2.0 * rmax * 1.001;
+    double extent = 0.0;
+    for (int a = 0; a < 3; ++a) extent = fmax(extent, hi[a] - lo[a] + 8.0 * rmax);
+    if (!(extent < 16384.0))
+        return set_error(XD_ERR_INVALID, "mixed mode: scene extent %g m exceeds 16384 m", extent);
+    // The cell exceeds the contact range 2 r_max by 0.1 % plus the error of the
+    // FP32 position estimates that place particles in cells (a few ulp of the
+    // extent), so touching pairs always land in neighbouring cells.
+    s->cs = 2.0 * rmax * 1.001 + extent * 0x1p-19;
     double margin = 2.0 * s->cs;
     int g[3];
     unsigned long long ncell = 1;
     for (int a = 0; a < 3; ++a) {
         lo[a] -= margin;
         hi[a] += margin;
+        // origin on the 2^-20 m grid: a multiple of 2^-36 m as well
+        lo[a] = std::floor(lo[a] * 1048576.0) / 1048576.0;
         g[a] = (int)ceil((hi[a] - lo[a]) / s->cs) + 2;
         ncell *= (unsigned long long)g[a];
     }
-    if (ncell > 0x7fffffffull)
+    if (ncell > 0x7ffffff0ull)
         return set_error(XD_ERR_CAPACITY, "mixed mode: grid of %llu cells is too large", ncell);
     s->gx = g[0]; s->gy = g[1]; s->gz = g[2];
     s->ncell = (unsigned)ncell;
     MixParams& P = s->P;
     memset(&P, 0, sizeof(P));
     P.gx = g[0]; P.gy = g[1]; P.gz = g[2];
+    P.gxy = (unsigned)(g[0] * g[1]);
     P.n = d.np;
+    const double dt = d.params.dt, half2dt = d.params.half2dt;
     for (int a = 0; a < 3; ++a) {
         P.wo[a] = lo[a];
+        P.qoff[a] = kMagic - lo[a] * kQ;
         P.g[a] = d.params.gravity[a];
+        P.gf[a] = (float)P.g[a];
+        P.G1[a] = df_split(dt * P.g[a]);
+        P.G2[a] = df_split(half2dt * P.g[a]);
     }
-    P.inv_cs = 1.0 / s->cs;
-    P.inv_csf = (float)P.inv_cs;
-    P.dt = d.params.dt;
-    P.half2dt = d.params.half2dt;
-    P.dtf = (float)d.params.dt;
-    P.tol = 4e-6f;
-    P.wall_tol = 1e-5f;
+    P.dt = dt;
+    P.inv_csf = (float)(1.0 / s->cs);
+    P.dtf = (float)dt;
+    P.hf = (float)(0.5 * dt);
+    P.half2dtf = (float)half2dt;
+    P.dt_df = df_split(dt);
+    P.tol = (float)(4e-6 + extent * 0x1p-20);
+    P.wall_tol = (float)(1e-5 + extent * 0x1p-20);
     const xd_contact_property& cp = d.cp_pp;
     double Eeq = (cp.Ei * cp.Ej) / (cp.Ei * (1 - cp.prj * cp.prj) + cp.Ej * (1 - cp.pri * cp.pri));
     double beta = M_PI / log(cp.rest);
@@ -1006,22 +1270,33 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     int st = XD_OK;
     auto A = [&](int r) { if (st == XD_OK) st = r; };
     for (int b = 0; b < 2; ++b) {
-        for (int k = 0; k < kFields; ++k) A(alloc(s, &s->m[b].f[k], n));
-        A(alloc(s, &s->m[b].id, n));
+        Master& M = s->m[b];
+        A(alloc(s, &M.x, n));
+        A(alloc(s, &M.y, n));
+        A(alloc(s, &M.z, n));
+        A(alloc(s, &M.r, n));
+        A(alloc(s, &M.vh, n));
+        A(alloc(s, &M.vl, n));
+        A(alloc(s, &M.wh, n));
+        A(alloc(s, &M.wl, n));
+        A(alloc(s, &M.ab, n));
+        A(alloc(s, &M.b2, n));
     }
+    A(alloc(s, &s->mass0, n));
     A(alloc(s, &s->pf, n));
     A(alloc(s, &s->qa, n));
     A(alloc(s, &s->qb, n));
-    A(alloc(s, &s->vf, n));
-    A(alloc(s, &s->vlo, n));
-    A(alloc(s, &s->wf, n));
     A(alloc(s, &s->Fc, n));
     A(alloc(s, &s->Mc, n));
+    A(alloc(s, &s->ccount, n));
+    A(alloc(s, &s->clist, n * kListCap));
+    A(alloc(s, &s->flist, n));
     A(alloc(s, &s->keys, n));
     A(alloc(s, &s->vals, n));
     A(alloc(s, &s->prev_keys, n));
-    A(alloc(s, &s->cstart, s->ncell));
-    A(alloc(s, &s->cend, s->ncell));
+    A(alloc(s, &s->lb, (size_t)s->ncell + 1));
+    s->gap_cap = s->ncell / kGapWarp + 2;
+    A(alloc(s, &s->gaps, s->gap_cap));
     char* scr = nullptr;
     A(alloc(s, &scr, radix_sort_scratch_bytes((unsigned)n)));
     s->sort_scratch = scr;
@@ -1036,7 +1311,8 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     A(alloc(s, &s->mv_sslot, n));
     A(alloc(s, &s->mv_sorted, n));
     A(alloc(s, &s->mv_perm, n));
-    A(alloc(s, &s->counters, 8));
+    A(alloc(s, &s->counters, kCounters));
+    if (st == XD_OK) A(cuda_status(cudaMemset(s->counters, 0, sizeof(unsigned) * kCounters), "mixed counters"));
     if (st == XD_OK && s->nplanes) {
         A(cuda_status(cudaMemcpy(s->planes, d.planes, sizeof(xd_plane_info) * s->nplanes, cudaMemcpyHostToDevice), "mixed planes"));
         A(cuda_status(cudaMemcpy(s->cps, d.cp_planes, sizeof(xd_contact_property) * s->nplanes, cudaMemcpyHostToDevice), "mixed planes"));
@@ -1116,10 +1392,10 @@ int mixed_upload(MixedScene* s, const double* pos, const double* vel, const doub
     if (st != XD_OK) return st;
     s->cur = 0;
     s->cells_clean = false;   // the state is in upload order again: next resort is a full sort
-    k_mx_load<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[0], dpos, dvel, dacc, dom, dal, dm, dI);
+    k_mx_load<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[0], dpos, dvel, dacc, dom, dal, dm, dI,
+                                                s->mass0, s->pf, s->qa, s->qb);
     st = launch_status("mixed upload");
     if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "mixed upload");
-    s->state_valid_forces = false;
     return st;
 }
 
@@ -1134,7 +1410,8 @@ int mixed_download(MixedScene* s, double* pos, double* vel, double* acc, double*
     double *dpos = b, *dvel = b + 4 * n, *dacc = dvel + 3 * n, *dom = dacc + 3 * n,
            *dal = dom + 3 * n, *df = dal + 3 * n, *dmo = df + 3 * n;
     // xfer holds 4n + 18n + 2n doubles: pos, vel, acc, omega, alpha, force, moment fit in 22n
-    k_mx_store<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur], dpos, dvel, dacc, dom, dal, df, dmo);
+    k_mx_store<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->mass0, dpos, dvel, dacc, dom,
+                                                 dal, df, dmo);
     st = launch_status("mixed download");
     auto cp = [&](double* h, const double* d, size_t cnt) {
         if (st == XD_OK && h)
@@ -1151,23 +1428,26 @@ int mixed_download(MixedScene* s, double* pos, double* vel, double* acc, double*
     return st;
 }
 
-// grid + reorder + contacts for the current positions (keys already in s->keys)
+// Sort, cell bounds, gather (with the update of MODE) and contacts, for the
+// keys already in s->keys.
+template <int MODE>
 static int grid_and_contacts(MixedScene* s, cudaStream_t q, const Phases& ph, bool record,
                              unsigned rec_cap)
 {
     const unsigned n = s->n;
-    int st;
+    int st = cuda_status(cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * kPerStepCounters, q),
+                         "mixed counters");
+    if (st != XD_OK) return st;
     unsigned *sk = nullptr, *sv = nullptr;
     ph.begin(2, q);
     if (!s->cells_clean) {
         // no previous order to exploit: full stable radix sort
         st = radix_sort_pairs(s->keys, s->vals, n, key_bits_for(s->ncell), s->sort_scratch, q, &sk, &sv);
-        if (st == XD_OK) st = launch_fill_cells(s->cstart, s->cend, s->ncell, q);
         if (st == XD_OK)
-            st = cuda_status(cudaMemsetAsync(s->counters + 4, 0, sizeof(unsigned), q), "mixed movers");
+            st = cuda_status(cudaMemsetAsync(s->counters + CN_MOVERS, 0, sizeof(unsigned), q), "mixed movers");
     } else {
         const unsigned nb = div_up(n, 1024u);
-        unsigned* total = s->counters + 4;
+        unsigned* total = s->counters + CN_MOVERS;
         k_mv_count<<<nb, 256, 0, q>>>(s->keys, s->prev_keys, n, s->mv_bcount);
         k_mv_scan<<<1, 1024, 0, q>>>(s->mv_bcount, nb, total);
         k_mv_compact<<<nb, 256, 0, q>>>(s->keys, s->prev_keys, n, s->mv_bcount, s->mv_prefix,
@@ -1179,13 +1459,11 @@ static int grid_and_contacts(MixedScene* s, cudaStream_t q, const Phases& ph, bo
         st = launch_status("mixed near-sorted resort");
         sk = s->mv_sorted;
         sv = s->mv_perm;
-        if (st == XD_OK) {
-            k_mx_clear<<<blocks(n, 256), 256, 0, q>>>(s->prev_keys, n, s->cstart, s->cend);
-            st = launch_status("mixed clear cells");
-        }
     }
     if (st == XD_OK) {
-        k_mx_bounds<<<blocks(n, 256), 256, 0, q>>>(sk, n, s->cstart, s->cend, s->prev_keys);
+        k_lb_fill<<<blocks(n + 1, 256), 256, 0, q>>>(sk, n, s->ncell, s->lb, s->prev_keys, s->gaps,
+                                                     s->counters);
+        k_lb_long<<<152 * 4, 256, 0, q>>>(s->gaps, s->counters, s->lb);
         st = launch_status("mixed cell bounds");
         s->cells_clean = true;
     }
@@ -1193,48 +1471,59 @@ static int grid_and_contacts(MixedScene* s, cudaStream_t q, const Phases& ph, bo
     if (st != XD_OK) return st;
     ph.begin(6, q);
     const int nxt = 1 - s->cur;
-    k_mx_reorder<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->m[nxt], sv, s->pf, s->qa, s->qb,
-                                                s->vf, s->vlo, s->wf);
-    st = launch_status("mixed reorder");
+    k_mx_gather<MODE><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->m[nxt], sv, s->Fc, s->Mc,
+                                                     s->pf, s->qa, s->qb);
+    st = launch_status("mixed gather");
     s->cur = nxt;
     ph.end(6, q);
     if (st != XD_OK) return st;
     ph.begin(3, q);
-    st = cuda_status(cudaMemsetAsync(s->counters, 0, sizeof(unsigned), q), "mixed counters");
-    if (st != XD_OK) return st;
-    // prev_keys now holds the sorted keys: the contact kernel reads cell coordinates from it
+    // prev_keys holds the sorted keys: the search reads each particle's cell from it
+    const Master& M = s->m[s->cur];
     if (record)
-        k_mx_contact<true><<<blocks(n, 256), 256, 0, q>>>(
-            s->P, s->m[s->cur], s->pf, s->qa, s->qb, s->vf, s->vlo, s->wf, s->prev_keys, s->cstart,
-            s->cend, s->Fc, s->Mc, s->wall_list, s->counters, s->rec_count, s->rec_pairs, rec_cap);
+        k_mx_search<true><<<blocks(n, 256), 256, 0, q>>>(
+            s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->ccount, s->clist, s->flist, s->Fc,
+            s->Mc, s->wall_list, s->counters, s->rec_count, s->rec_pairs, rec_cap);
     else
-        k_mx_contact<false><<<blocks(n, 256), 256, 0, q>>>(
-            s->P, s->m[s->cur], s->pf, s->qa, s->qb, s->vf, s->vlo, s->wf, s->prev_keys, s->cstart,
-            s->cend, s->Fc, s->Mc, s->wall_list, s->counters, nullptr, nullptr, 0);
+        k_mx_search<false><<<blocks(n, 256), 256, 0, q>>>(
+            s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->ccount, s->clist, s->flist, s->Fc,
+            s->Mc, s->wall_list, s->counters, nullptr, nullptr, 0);
+    k_mx_force<<<min(blocks(n, 256), 152u * 8u), 256, 0, q>>>(s->P, M, s->pf, s->qa, s->qb,
+                                                              s->prev_keys, s->lb, s->ccount, s->clist,
+                                                              s->flist, s->mass0, s->Fc, s->Mc,
+                                                              s->counters);
     st = launch_status("mixed contact");
     ph.end(3, q);
     if (st != XD_OK || !s->nplanes) return st;
     ph.begin(4, q);
-    k_mx_walls<<<152 * 4, 128, 0, q>>>(s->P, s->m[s->cur], s->planes, s->cps, s->wall_list, s->counters, s->Fc);
+    k_mx_walls<<<152 * 4, 128, 0, q>>>(s->P, M, s->planes, s->cps, s->wall_list, s->counters, s->mass0,
+                                       s->Fc);
     st = launch_status("mixed walls");
     ph.end(4, q);
     return st;
 }
 
-// One middle step: grid, contacts and walls, then the fused velocity/position update.
-static int middle_step(MixedScene* s, cudaStream_t q, const Phases& ph, bool last)
+// The keys of the next position (MODE 1) or the last velocity update (last).
+static int after_contacts(MixedScene* s, cudaStream_t q, const Phases& ph, bool last)
 {
     const unsigned n = s->n;
-    int st = grid_and_contacts(s, q, ph, false, 0);
-    if (st != XD_OK) return st;
     ph.begin(0, q);
     if (!last)
-        k_mx_integrate<1><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc, s->keys, s->vals);
+        k_mx_keys<1><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->pf, s->Fc, s->keys, s->vals);
     else
-        k_mx_integrate<2><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc, s->keys, s->vals);
-    st = launch_status("mixed integrate");
+        k_mx_finish<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc);
+    int st = launch_status(last ? "mixed finish" : "mixed keys");
     ph.end(0, q);
     return st;
+}
+
+// One middle step: velocity of step t and position of step t + 1 (in the
+// gather), contacts, then the next step's keys.
+static int middle_step(MixedScene* s, cudaStream_t q, const Phases& ph, bool last)
+{
+    int st = grid_and_contacts<1>(s, q, ph, false, 0);
+    if (st != XD_OK) return st;
+    return after_contacts(s, q, ph, last);
 }
 
 // Captures two middle steps into a graph for the current buffer parity (the
@@ -1272,23 +1561,21 @@ int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
         // The near-sorted resort ranks the movers in O(M^2); after a burst of
         // movers in the previous call, start this one with a full radix sort.
         unsigned prev_movers = 0;
-        st = cuda_status(cudaMemcpyAsync(&prev_movers, s->counters + 4, sizeof(unsigned),
+        st = cuda_status(cudaMemcpyAsync(&prev_movers, s->counters + CN_MOVERS, sizeof(unsigned),
                                          cudaMemcpyDeviceToHost, q), "mixed mover count");
         if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "mixed mover count");
         if (st != XD_OK) return st;
         if (prev_movers > s->n / 16 || prev_movers > 65536u) s->cells_clean = false;
     }
+    // step 1: position update (in the gather) from the state's (v, a)
     ph.begin(0, q);
-    k_mx_integrate<0><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc, s->keys, s->vals);
-    st = launch_status("mixed integrate");
+    k_mx_keys<0><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->pf, s->Fc, s->keys, s->vals);
+    st = launch_status("mixed keys");
     ph.end(0, q);
+    if (st == XD_OK) st = grid_and_contacts<0>(s, q, ph, false, 0);
+    if (st == XD_OK) st = after_contacts(s, q, ph, nsteps == 1);
     if (st != XD_OK) return st;
-    unsigned t = 0;
-    if (!s->cells_clean) {
-        st = middle_step(s, q, ph, nsteps == 1);
-        if (st != XD_OK) return st;
-        t = 1;
-    }
+    unsigned t = 1;
     // pairs of middle steps as one graph launch; the last step runs directly
     while (graphs && nsteps - t >= 3) {
         if (!s->graph[s->cur]) {
@@ -1297,13 +1584,12 @@ int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
         }
         st = cuda_status(cudaGraphLaunch(s->graph[s->cur], q), "mixed graph launch");
         if (st != XD_OK) return st;
-        t += 2;   // two reorders: the buffer parity is unchanged
+        t += 2;   // two gathers: the buffer parity is unchanged
     }
     for (; t < nsteps; ++t) {
         st = middle_step(s, q, ph, t + 1 == nsteps);
         if (st != XD_OK) return st;
     }
-    s->state_valid_forces = false;
     return XD_OK;
 }
 
@@ -1311,26 +1597,34 @@ unsigned long long mixed_launches(MixedScene* s, unsigned nsteps)
 {
     if (!s || nsteps == 0 || s->n == 0) return 0;
     const unsigned passes = (key_bits_for(s->ncell) + 7) / 8;
-    // per step: 5 resort kernels + clear + bounds + reorder + contact (+ walls) + integrate
-    const unsigned long long per = 5 + 1 + 1 + 1 + 1 + (s->nplanes ? 1 : 0) + 1;
-    unsigned long long total = 1 + per * nsteps;   // + the first position update
+    // per step: 5 resort kernels + 2 cell-bound kernels + gather + search + force
+    // (+ walls) + the next keys or the last velocity update
+    const unsigned long long per = 5 + 2 + 1 + 2 + (s->nplanes ? 1 : 0) + 1;
+    unsigned long long total = 1 + per * nsteps;   // + the first keys
     if (!s->cells_clean && s->n > 1) total += 5ull * passes - 5;   // first step: full radix sort
     return total;
+}
+
+// Contacts of the current state: keys of the current positions, sort and
+// gather without an update.
+static int current_contacts(MixedScene* s, cudaStream_t q, bool record, unsigned rec_cap)
+{
+    Phases none;
+    k_mx_keys<3><<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->pf, s->Fc, s->keys, s->vals);
+    int st = launch_status("mixed keys");
+    if (st == XD_OK) st = grid_and_contacts<3>(s, q, none, record, rec_cap);
+    return st;
 }
 
 int mixed_eval_contacts(MixedScene* s, double* force, double* moment, cudaStream_t q)
 {
     if (!s->ready) return set_error(XD_ERR_STATE, "mixed mode: no state uploaded");
     int st = ensure_xfer(s);
-    if (st != XD_OK) return st;
-    Phases none;
-    k_mx_keys<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->keys, s->vals);
-    st = launch_status("mixed keys");
-    if (st == XD_OK) st = grid_and_contacts(s, q, none, false, 0);
+    if (st == XD_OK) st = current_contacts(s, q, false, 0);
     if (st != XD_OK) return st;
     size_t n = s->n;
     double *df = s->xfer, *dm = s->xfer + 3 * n;
-    k_mx_store_forces<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur].id, s->Fc, s->Mc, df, dm);
+    k_mx_store_forces<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc, df, dm);
     st = launch_status("mixed store forces");
     if (st == XD_OK && force)
         st = cuda_status(cudaMemcpyAsync(force, df, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, q), "eval");
@@ -1351,16 +1645,14 @@ int mixed_pair_list(MixedScene* s, unsigned cap_per_particle, unsigned* counts, 
         st = alloc(s, &s->rec_pairs, (size_t)s->n * cap_per_particle);
         s->rec_cap_alloc = cap_per_particle;
     }
-    if (st != XD_OK) return st;
-    Phases none;
-    k_mx_keys<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->keys, s->vals);
-    st = launch_status("mixed keys");
-    if (st == XD_OK) st = grid_and_contacts(s, q, none, true, cap_per_particle);
+    if (st == XD_OK) st = current_contacts(s, q, true, cap_per_particle);
     if (st != XD_OK) return st;
     // counts/partners are reported in original particle ids
     size_t n = s->n;
+    k_mx_ids<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->vals);
+    st = launch_status("pairs");
     std::vector<unsigned> ids(n), cnt(n), part((size_t)n * cap_per_particle);
-    st = cuda_status(cudaMemcpyAsync(ids.data(), s->m[s->cur].id, 4 * n, cudaMemcpyDeviceToHost, q), "pairs");
+    if (st == XD_OK) st = cuda_status(cudaMemcpyAsync(ids.data(), s->vals, 4 * n, cudaMemcpyDeviceToHost, q), "pairs");
     if (st == XD_OK) st = cuda_status(cudaMemcpyAsync(cnt.data(), s->rec_count, 4 * n, cudaMemcpyDeviceToHost, q), "pairs");
     if (st == XD_OK)
         st = cuda_status(cudaMemcpyAsync(part.data(), s->rec_pairs, 4 * n * cap_per_particle, cudaMemcpyDeviceToHost, q), "pairs");
@@ -1377,10 +1669,13 @@ int mixed_pair_list(MixedScene* s, unsigned cap_per_particle, unsigned* counts, 
 
 int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q)
 {
-    unsigned c[4] = {};
+    unsigned c[kCounters] = {};
     int st = cuda_status(cudaMemcpyAsync(c, s->counters, sizeof(c), cudaMemcpyDeviceToHost, q), "counters");
     if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "counters");
-    for (int i = 0; i < 4; ++i) out[i] = c[i];
+    out[0] = c[CN_WALLS];
+    out[1] = c[CN_DECISIONS];
+    out[2] = c[CN_NORMALS];
+    out[3] = c[CN_SLIPS];
     return st;
 }
 

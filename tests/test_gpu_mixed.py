@@ -188,3 +188,46 @@ def test_mixed_fast_movers_keep_pairs_exact(cuda, oracle):
     ds.close()
     assert _pairset(pairs) == _pairset(pairs_ref)
     assert _norm_err(f, f_ref, mag, sc.mass) <= FORCE_TOL
+
+
+def test_mixed_crowded_contacts_beyond_list(cuda, oracle):
+    """Large spheres each touched by 40 small ones: more contacts than the
+    per-particle contact list holds, so the rest come from a second search in
+    the same order; pairs and forces still match the oracle."""
+    rng = np.random.Generator(np.random.MT19937(23))
+    R, r, nshell = 0.004, 0.001, 40
+    k = np.arange(nshell) + 0.5
+    phi = np.arccos(1.0 - 2.0 * k / nshell)
+    th = np.pi * (1.0 + 5.0 ** 0.5) * k
+    shell = np.stack([np.cos(th) * np.sin(phi), np.sin(th) * np.sin(phi), np.cos(phi)], axis=1)
+    rows = []
+    for b in range(6):
+        c = np.array([0.03 * b, 0.1, 0.1])
+        rows.append([*c, R])
+        for d in shell:
+            rows.append([*(c + d * (R + r - rng.uniform(1e-6, 3e-5))), r])
+    pos = np.array(rows)
+    n = pos.shape[0]
+    sc = scenes.settle_box(n_side=2)
+    sc.pos = pos
+    for key, val in scenes._state(pos).items():
+        setattr(sc, key, val)
+    sc.vel[:] = rng.normal(0, 0.1, sc.vel.shape)
+    sc.omega[:] = rng.normal(0, 10, sc.omega.shape)
+    sc.params = make_params(np_=n, ncell=128 ** 3, grid=(128, 128, 128), dt=1e-5, cell_size=0.0081,
+                            world_origin=(-1.0, -1.0, -1.0), gravity=(0, 0, -9.81))
+    sc.planes = sc.planes[:0]
+    sc.cp_planes = sc.cp_planes[:0]
+    sc.plane_names = []
+    ds = engine.DeviceScene(sc, mode=engine.MODE_MIXED)
+    pairs = ds.pair_list(cap=64)
+    f, m = ds.eval_contacts()
+    st = ds.download()
+    ds.close()
+    pairs_ref, f_ref, m_ref, mag = _oracle_view(oracle, sc, st)
+    big = np.flatnonzero(pos[:, 3] == R)
+    assert all((np.asarray(pairs_ref)[:, 0] == b).sum() == nshell for b in big)
+    assert _pairset(pairs) == _pairset(pairs_ref)
+    rr = sc.pos[:, 3:4]
+    assert _norm_err(f, f_ref, mag, sc.mass) <= FORCE_TOL
+    assert _norm_err(m / rr, m_ref / rr, mag, sc.mass) <= FORCE_TOL
