@@ -360,8 +360,19 @@ int xd_scene_pair_list(xd_scene* scene, unsigned cap, unsigned* counts, unsigned
  * most of the tangential velocity (cumulative). */
 int xd_scene_counters(xd_scene* scene, unsigned long long out[4], void* stream);
 
-/* Number of kernel launches one xd_scene_step of nsteps issues. */
+/* Number of kernel launches one xd_scene_step of nsteps issues, not counting
+ * the cell re-binnings the mixed mode decides on the device (see
+ * xd_scene_rebuilds); the FP64 mode's count is exact. */
 unsigned long long xd_scene_launches(xd_scene* scene, unsigned nsteps);
+
+/* Mixed mode: cell re-binnings so far (*count, cumulative) and the kernel
+ * launches each one issues (*launches_each).  A mixed scene keeps every
+ * particle in its assigned cell while it stays within half a skin of it and
+ * re-bins all cells in the step where one leaves; the FP64 mode re-bins every
+ * step as the reference does and reports 0 here.  No counterpart in the
+ * reference. */
+int xd_scene_rebuilds(xd_scene* scene, unsigned long long* count, unsigned long long* launches_each,
+                      void* stream);
 
 #ifdef __cplusplus
 }

@@ -71,6 +71,7 @@ _SIGS = {
     "xd_scene_eval_contacts": [vp, vp, vp, vp],
     "xd_scene_pair_list": [vp, u32, vp, vp, vp],
     "xd_scene_counters": [vp, vp, vp],
+    "xd_scene_rebuilds": [vp, vp, vp, vp],
     "xd_scene_phase_times": [vp, vp, vp],
 }
 _RESTYPES = {"xd_version": C.c_char_p, "xd_status_string": C.c_char_p, "xd_clear_error": None,

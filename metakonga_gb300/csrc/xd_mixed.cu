@@ -15,20 +15,21 @@
 // (two adds per axis) and the fixed-point conversion (one FMA per axis).
 //
 // Per step (dem_simulation::oneStepAnalysis order, dem_simulation.cpp:447-469):
-//   k_mx_keys     the cell key of the next position, from an FP32 estimate
-//                 (the cell exceeds the contact range by a margin larger than
-//                 the estimate's error, so touching pairs stay in neighbour
-//                 cells);
-//   resort        near-sorted: only particles that changed cell are ranked
-//                 among the others (a full radix sort after an upload or a
-//                 burst of movers);
-//   k_lb_fill     lb[c] = first sorted slot whose key is >= c, for every cell,
-//                 so a row of three cells is the slot range [lb[c0], lb[c0+3]);
-//   k_mx_gather   moves the state into the new order and applies the
-//                 velocity-Verlet update on the way (velocity of step t from
-//                 the contact force, position of step t + 1), then writes the
-//                 contact view: FP32 (x, y, z, r) and int64 fixed point
-//                 (2^-36 m);
+//   k_mx_keys     the cell key of the next position, estimated in FP32, and
+//                 the skin test: every particle keeps its assigned cell (and
+//                 its slot in the cell order) while it stays inside that cell
+//                 widened by half the skin; cells are 2 r_max + skin wide, so
+//                 touching pairs still lie in neighbouring assigned cells;
+//   re-binning    only when a particle left its widened cell (a CUDA graph
+//                 conditional node, or the host between direct launches):
+//                 stable radix sort of the keys, then k_lb_fill:
+//                 lb[c] = first slot whose key is >= c, for every cell, so a
+//                 row of three cells is the slot range [lb[c0], lb[c0 + 3]);
+//   k_mx_gather   applies the velocity-Verlet update (velocity of step t from
+//                 the contact force, position of step t + 1) while moving the
+//                 state into the new cell order after a re-binning (in order
+//                 otherwise), then writes the contact view: FP32 (x, y, z, r)
+//                 and int64 fixed point (2^-36 m);
 //   k_mx_search   candidates: FP32 prefilter, then the exact integer test
 //                 N = (ri + rj)^2 - |qj - qi|^2 > 0 (no cancellation); pairs
 //                 within 2e-10 m of touching are decided by the reference's
@@ -36,11 +37,11 @@
 //                 particle's contacts go to a list in search order; particles
 //                 near a wall go to the wall list with a plane mask;
 //   k_mx_force    FP32 Hertz-Mindlin (DHSModel) over each particle's list in
-//                 the reference's pair order (a pair without slip reuses the
-//                 previous pair's tangential force, impl:426-428);
+//                 search order (a pair without slip reuses the previous pair's
+//                 tangential force, impl:426-428);
 //   k_mx_walls    the listed particles' plane contacts in FP64.
-// The grid is the scene's own (not the reference's wrapped 128^3): cell size
-// 2 r_max plus a margin, padded by one cell on every side, keys clamped inside.
+// The grid is the scene's own (not the reference's wrapped 128^3): padded by
+// one cell on every side, keys clamped inside.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -70,12 +71,14 @@ enum {
     CN_WALLS = 0,      // wall-list length
     CN_FORCE = 1,      // force-list length
     CN_GAPS = 2,       // long gaps of the cell lower-bound array
-    kPerStepCounters = 3,
-    CN_DECISIONS = 3,  // FP64 contact decisions (cumulative)
-    CN_NORMALS = 4,    // FP64 normal-force rechecks (cumulative)
-    CN_SLIPS = 5,      // FP64 slip rechecks (cumulative)
-    CN_MOVERS = 6,     // particles that changed cell in the last resort
-    kCounters = 8
+    CN_REBUILD = 3,    // nonzero: this step re-bins the cells
+    CN_DONE = 4,       // blocks of k_mx_keys finished (last-block hand-off)
+    kPerStepCounters = 5,
+    CN_DECISIONS = 5,  // FP64 contact decisions (cumulative)
+    CN_NORMALS = 6,    // FP64 normal-force rechecks (cumulative)
+    CN_SLIPS = 7,      // FP64 slip rechecks (cumulative)
+    CN_REBUILDS = 8,   // re-binnings (cumulative)
+    kCounters = 12
 };
 
 struct Master {
@@ -96,7 +99,8 @@ struct MixParams {
     double qoff[3];      // 1.5 * 2^52 - wo * 2^36 (fixed-point offsets)
     double g[3];
     double dt;
-    float inv_csf;
+    float csf, inv_csf;
+    float half_skin;     // a particle keeps its cell while within half the skin of it
     float dtf, hf, half2dtf;
     float gf[3];
     float2 dt_df;        // dt as double-float
@@ -137,11 +141,10 @@ struct MixedScene {
     unsigned* lb = nullptr;       // ncell + 1 entries
     uint4* gaps = nullptr;
     unsigned gap_cap = 0;
-    bool cells_clean = false;     // prev_keys holds the current order's sorted keys
+    bool cells_clean = false;     // prev_keys holds the current order's assigned keys
     void* sort_scratch = nullptr;
-    // near-sorted resort buffers
-    unsigned *mv_bcount = nullptr, *mv_prefix = nullptr, *mv_key = nullptr, *mv_slot = nullptr;
-    unsigned *mv_skey = nullptr, *mv_sslot = nullptr, *mv_sorted = nullptr, *mv_perm = nullptr;
+    unsigned* perm = nullptr;     // re-binning: new slot -> old slot (the sort's value output)
+    unsigned* sorted_keys = nullptr;
     // walls
     xd_plane_info* planes = nullptr;
     xd_contact_property* cps = nullptr;
@@ -154,6 +157,7 @@ struct MixedScene {
     double* xfer = nullptr;
     bool ready = false;                // grid and buffers set up (first upload)
     cudaGraphExec_t graph[2] = { nullptr, nullptr };   // two middle steps, per buffer parity
+    unsigned passes = 0;          // radix passes of one re-binning
     bool use_graphs = true;
     unsigned rec_cap_alloc = 0;
     xd_scene_desc desc;
@@ -349,37 +353,70 @@ __device__ __forceinline__ unsigned cell_key(const MixParams& P, float x, float 
 //   MODE 2  velocity only (last step of a call)
 //   MODE 3  no update (contacts of the current state)
 
-// k_mx_keys: the key of the next position, estimated in FP32 from the view.
+// Is p (FP32, relative to the grid origin) outside assigned cell c (key
+// coordinate; cell c spans [(c - 1) cs, c cs)) widened by half the skin?
+// Clamped boundary cells are open outward.
+__device__ __forceinline__ bool outside_cell(const MixParams& P, float p, unsigned c, int g)
+{
+    const float lo = (float)((int)c - 1) * P.csf;
+    return ((int)c > 1 && p < lo - P.half_skin) || ((int)c < g - 2 && p > lo + P.csf + P.half_skin);
+}
+
+// k_mx_keys: the key of the next position, estimated in FP32 from the view,
+// and the skin test against the assigned cell (prev).  Any particle outside
+// its widened cell sets CN_REBUILD; the last block to finish passes the flag
+// to the graph's conditional node (use_cond), the one caller it allows.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_mx_keys(MixParams P, Master M, const float4* __restrict__ pf,
                                                  const float4* __restrict__ Fc,
+                                                 const unsigned* __restrict__ prev,
                                                  unsigned* __restrict__ keys,
-                                                 unsigned* __restrict__ vals)
+                                                 unsigned* __restrict__ vals,
+                                                 unsigned* __restrict__ counters,
+                                                 cudaGraphConditionalHandle cond, int use_cond)
 {
+    __shared__ bool last;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    const float4 p = pf[i];
-    float x = p.x, y = p.y, z = p.z;
-    if (MODE == 0 || MODE == 1) {
-        const float4 v = M.vh[i], a = M.ab[i];
-        float vx = v.x, vy = v.y, vz = v.z, ax = a.x, ay = a.y, az = a.z;
-        if (MODE == 1) {
-            const float4 f = Fc[i];
-            const float im = M.vl[i].w;
-            const float nx = f.x * im, ny = f.y * im, nz = f.z * im;
-            vx += P.hf * (2.f * P.gf[0] + ax + nx);
-            vy += P.hf * (2.f * P.gf[1] + ay + ny);
-            vz += P.hf * (2.f * P.gf[2] + az + nz);
-            ax = nx;
-            ay = ny;
-            az = nz;
+    bool out = false;
+    if (i < P.n) {
+        const float4 p = pf[i];
+        float x = p.x, y = p.y, z = p.z;
+        if (MODE == 0 || MODE == 1) {
+            const float4 v = M.vh[i], a = M.ab[i];
+            float vx = v.x, vy = v.y, vz = v.z, ax = a.x, ay = a.y, az = a.z;
+            if (MODE == 1) {
+                const float4 f = Fc[i];
+                const float im = M.vl[i].w;
+                const float nx = f.x * im, ny = f.y * im, nz = f.z * im;
+                vx += P.hf * (2.f * P.gf[0] + ax + nx);
+                vy += P.hf * (2.f * P.gf[1] + ay + ny);
+                vz += P.hf * (2.f * P.gf[2] + az + nz);
+                ax = nx;
+                ay = ny;
+                az = nz;
+            }
+            x += P.dtf * vx + P.half2dtf * (P.gf[0] + ax);
+            y += P.dtf * vy + P.half2dtf * (P.gf[1] + ay);
+            z += P.dtf * vz + P.half2dtf * (P.gf[2] + az);
         }
-        x += P.dtf * vx + P.half2dtf * (P.gf[0] + ax);
-        y += P.dtf * vy + P.half2dtf * (P.gf[1] + ay);
-        z += P.dtf * vz + P.half2dtf * (P.gf[2] + az);
+        keys[i] = cell_key(P, x, y, z);
+        vals[i] = i;
+        const unsigned a = __ldg(prev + i);
+        const unsigned cz = a / P.gxy, rem = a - cz * P.gxy;
+        const unsigned cy = rem / (unsigned)P.gx, cx = rem - cy * (unsigned)P.gx;
+        out = outside_cell(P, x, cx, P.gx) || outside_cell(P, y, cy, P.gy) || outside_cell(P, z, cz, P.gz);
     }
-    keys[i] = cell_key(P, x, y, z);
-    vals[i] = i;
+    if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31u) == 0) atomicOr(counters + CN_REBUILD, 1u);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(counters + CN_DONE, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        const unsigned f = atomicOr(counters + CN_REBUILD, 0u);
+        if (use_cond) cudaGraphSetConditional(cond, f ? 1u : 0u);
+        counters[CN_DONE] = 0;
+    }
 }
 
 // Velocity update of one particle (MODE 1 and 2): v += dt g + h (a_c + a_c'),
@@ -418,11 +455,13 @@ __device__ __forceinline__ double drift(const MixParams& P, double x, float vhi,
     return __dadd_rn(x, __dadd_rn((double)inc.hi, (double)inc.lo));
 }
 
-// Gathers the state into the new order (perm: new slot -> old slot), applies
-// the update of MODE on the way and writes the contact view.
+// Applies the update of MODE and writes the contact view; after a re-binning
+// (counters[CN_REBUILD] set) it also moves the state into the new order
+// (perm: new slot -> old slot).
 template <int MODE>
 __global__ void __launch_bounds__(256) k_mx_gather(MixParams P, Master S, Master D,
                                                    const unsigned* __restrict__ perm,
+                                                   const unsigned* __restrict__ counters,
                                                    const float4* __restrict__ Fc,
                                                    const float4* __restrict__ Mc,
                                                    float4* __restrict__ pf,
@@ -431,7 +470,7 @@ __global__ void __launch_bounds__(256) k_mx_gather(MixParams P, Master S, Master
 {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
-    const unsigned o = __ldg(perm + i);
+    const unsigned o = counters[CN_REBUILD] ? __ldg(perm + i) : i;
     double x = __ldg(S.x + o), y = __ldg(S.y + o), z = __ldg(S.z + o);
     const double r = __ldg(S.r + o);
     float4 vh = __ldg(S.vh + o), vl = __ldg(S.vl + o), wh = __ldg(S.wh + o), wl = __ldg(S.wl + o);
@@ -488,6 +527,7 @@ __global__ void __launch_bounds__(256) k_lb_fill(const unsigned* __restrict__ sk
 {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;   // slots 0 .. n
     const unsigned lane = threadIdx.x & 31u;
+    if (t == 0) atomicAdd(counters + CN_REBUILDS, 1u);
     unsigned lo = 1, hi = 0;
     if (t <= n) {
         const unsigned kc = t < n ? sk[t] : ncell;
@@ -975,199 +1015,6 @@ __global__ void __launch_bounds__(256) k_mx_ids(MixParams P, Master M, unsigned*
     ids[i] = __float_as_uint(M.wl[i].w);
 }
 
-// ---- near-sorted resort ("movers") -----------------------------------------
-// The state is in the previous step's cell order, so prev[] (that order's
-// keys) is ascending and most particles keep their key.  Sorting (key, slot)
-// stably then only needs the movers (key != prev) ranked among themselves;
-// every other slot keeps its relative order:
-//   position(stayer i) = (i - movers before i) + movers with (key, slot) < (prev[i], i)
-//   position(mover m)  = stayers with (prev, slot) < (key_m, slot_m) + rank of m among movers
-// which is exactly the stable sort's output.
-constexpr int kMvBlock = 1024;     // slots per block in the flag/compact pass (256 threads x 4)
-
-__global__ void __launch_bounds__(256) k_mv_count(const unsigned* __restrict__ keys,
-                                                  const unsigned* __restrict__ prev, unsigned n,
-                                                  unsigned* __restrict__ bcount)
-{
-    __shared__ unsigned wsum[8];
-    const unsigned base = blockIdx.x * kMvBlock;
-    unsigned c = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        unsigned i = base + k * 256 + threadIdx.x;
-        if (i < n && keys[i] != prev[i]) ++c;
-    }
-    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
-    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned t = 0;
-        for (int w = 0; w < 8; ++w) t += wsum[w];
-        bcount[blockIdx.x] = t;
-    }
-}
-
-// exclusive scan of the per-block counts (one block); total movers -> *total
-__global__ void __launch_bounds__(1024) k_mv_scan(unsigned* __restrict__ bcount, unsigned nb,
-                                                  unsigned* __restrict__ total)
-{
-    __shared__ unsigned wsum[32];
-    __shared__ unsigned carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (unsigned b0 = 0; b0 < nb; b0 += 1024) {
-        unsigned i = b0 + threadIdx.x;
-        unsigned v = i < nb ? bcount[i] : 0u;
-        unsigned x = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= (unsigned)o) x += y;
-        }
-        if (lane == 31) wsum[warp] = x;
-        __syncthreads();
-        if (warp == 0) {
-            unsigned w = wsum[lane], t = w;
-            for (int o = 1; o < 32; o <<= 1) {
-                unsigned y = __shfl_up_sync(0xffffffffu, t, o);
-                if (lane >= (unsigned)o) t += y;
-            }
-            wsum[lane] = t - w;
-        }
-        __syncthreads();
-        unsigned excl = x - v + wsum[warp] + carry;
-        if (i < nb) bcount[i] = excl;
-        __syncthreads();
-        if (threadIdx.x == 1023) carry = excl + v;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *total = carry;
-}
-
-// movers compacted in slot order; mprefix[i] = movers in slots [0, i)
-__global__ void __launch_bounds__(256) k_mv_compact(const unsigned* __restrict__ keys,
-                                                    const unsigned* __restrict__ prev, unsigned n,
-                                                    const unsigned* __restrict__ boff,
-                                                    unsigned* __restrict__ mprefix,
-                                                    unsigned* __restrict__ mkey,
-                                                    unsigned* __restrict__ mslot)
-{
-    __shared__ unsigned wsum[32];
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned run = boff[blockIdx.x];
-    const unsigned base = blockIdx.x * kMvBlock;
-    for (int k = 0; k < 4; ++k) {
-        unsigned i = base + k * 256 + threadIdx.x;
-        bool mv = i < n && keys[i] != prev[i];
-        unsigned bal = __ballot_sync(0xffffffffu, mv);
-        if (lane == 0) wsum[warp] = __popc(bal);
-        __syncthreads();
-        unsigned before = 0, all = 0;
-        for (int w = 0; w < 8; ++w) {
-            unsigned c = wsum[w];
-            if (w < (int)warp) before += c;
-            all += c;
-        }
-        unsigned pos = run + before + __popc(bal & ((1u << lane) - 1u));
-        if (i < n) mprefix[i] = pos;
-        if (mv) {
-            mkey[pos] = keys[i];
-            mslot[pos] = i;
-        }
-        if (i == n - 1) mprefix[n] = pos + (mv ? 1u : 0u);
-        run += all;
-        __syncthreads();
-    }
-}
-
-__device__ __forceinline__ bool pair_less(unsigned ka, unsigned sa, unsigned kb, unsigned sb)
-{
-    return ka < kb || (ka == kb && sa < sb);
-}
-
-// first index in a[0, n) with a[idx] >= v
-__device__ __forceinline__ unsigned lower_bound_u(const unsigned* __restrict__ a, unsigned n, unsigned v)
-{
-    unsigned lo = 0, hi = n;
-    while (lo < hi) {
-        unsigned mid = (lo + hi) >> 1;
-        if (__ldg(a + mid) < v) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
-// Ranks each mover among all movers (shared-memory tiles of the mover set,
-// O(M^2) compares: M is a few thousand per step; any M stays correct) and
-// places it.  Also writes the sorted mover list for the stayers' searches.
-constexpr int kRankTile = 2048;
-__global__ void __launch_bounds__(256) k_mv_rank(const unsigned* __restrict__ total,
-                                                 const unsigned* __restrict__ mkey,
-                                                 const unsigned* __restrict__ mslot,
-                                                 const unsigned* __restrict__ prev,
-                                                 const unsigned* __restrict__ mprefix, unsigned n,
-                                                 unsigned* __restrict__ smkey,
-                                                 unsigned* __restrict__ smslot,
-                                                 unsigned* __restrict__ skeys,
-                                                 unsigned* __restrict__ perm)
-{
-    __shared__ unsigned tk[kRankTile], ts[kRankTile];
-    const unsigned M = *total;
-    const unsigned stride = gridDim.x * blockDim.x;
-    for (unsigned base = blockIdx.x * blockDim.x; base < M; base += stride) {
-        const unsigned m = base + threadIdx.x;
-        const bool act = m < M;
-        const unsigned key = act ? mkey[m] : 0u, slot = act ? mslot[m] : 0u;
-        unsigned rank = 0;
-        for (unsigned t0 = 0; t0 < M; t0 += kRankTile) {
-            const unsigned cnt = min((unsigned)kRankTile, M - t0);
-            __syncthreads();
-            for (unsigned k = threadIdx.x; k < cnt; k += blockDim.x) {
-                tk[k] = mkey[t0 + k];
-                ts[k] = mslot[t0 + k];
-            }
-            __syncthreads();
-            if (act)
-                for (unsigned k = 0; k < cnt; ++k) rank += pair_less(tk[k], ts[k], key, slot) ? 1u : 0u;
-        }
-        if (act) {
-            smkey[rank] = key;
-            smslot[rank] = slot;
-            const unsigned L = lower_bound_u(prev, n, key);
-            const unsigned U = lower_bound_u(prev, n, key + 1u);
-            const unsigned cend = max(L, min(U, slot));
-            const unsigned pos = (cend - mprefix[cend]) + rank;
-            skeys[pos] = key;
-            perm[pos] = slot;
-        }
-    }
-}
-
-__global__ void __launch_bounds__(256) k_mv_place(const unsigned* __restrict__ keys,
-                                                  const unsigned* __restrict__ prev, unsigned n,
-                                                  const unsigned* __restrict__ mprefix,
-                                                  const unsigned* __restrict__ total,
-                                                  const unsigned* __restrict__ smkey,
-                                                  const unsigned* __restrict__ smslot,
-                                                  unsigned* __restrict__ skeys,
-                                                  unsigned* __restrict__ perm)
-{
-    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const unsigned k = prev[i];
-    if (keys[i] != k) return;   // a mover: placed by k_mv_rank
-    const unsigned M = *total;
-    unsigned lo = 0, hi = M;    // movers with (key, slot) < (k, i)
-    while (lo < hi) {
-        unsigned mid = (lo + hi) >> 1;
-        if (pair_less(__ldg(smkey + mid), __ldg(smslot + mid), k, i)) lo = mid + 1;
-        else hi = mid;
-    }
-    const unsigned pos = (i - mprefix[i]) + lo;
-    skeys[pos] = k;
-    perm[pos] = i;
-}
-
 }  // namespace
 
 // ------------------------------------------------------------------ host
@@ -1205,10 +1052,12 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     for (int a = 0; a < 3; ++a) extent = fmax(extent, hi[a] - lo[a] + 8.0 * rmax);
     if (!(extent < 16384.0))
         return set_error(XD_ERR_INVALID, "mixed mode: scene extent %g m exceeds 16384 m", extent);
-    // The cell exceeds the contact range 2 r_max by 0.1 % plus the error of the
-    // FP32 position estimates that place particles in cells (a few ulp of the
-    // extent), so touching pairs always land in neighbouring cells.
-    s->cs = 2.0 * rmax * 1.001 + extent * 0x1p-19;
+    // The cell is the contact range 2 r_max plus the skin, plus 0.1 % and the
+    // error of the FP32 position estimates that place particles (a few ulp of
+    // the extent): two touching particles, each within half the skin of its
+    // assigned cell, always have neighbouring assigned cells.
+    const double skin = 0.1 * rmax;
+    s->cs = 2.0 * rmax * 1.001 + skin + extent * 0x1p-19;
     double margin = 2.0 * s->cs;
     int g[3];
     unsigned long long ncell = 1;
@@ -1239,7 +1088,9 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
         P.G2[a] = df_split(half2dt * P.g[a]);
     }
     P.dt = dt;
+    P.csf = (float)s->cs;
     P.inv_csf = (float)(1.0 / s->cs);
+    P.half_skin = (float)(0.5 * skin);
     P.dtf = (float)dt;
     P.hf = (float)(0.5 * dt);
     P.half2dtf = (float)half2dt;
@@ -1303,15 +1154,8 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     A(alloc(s, &s->planes, s->nplanes));
     A(alloc(s, &s->cps, s->nplanes));
     A(alloc(s, &s->wall_list, n));
-    A(alloc(s, &s->mv_bcount, div_up((unsigned)(n ? n : 1), 1024u)));
-    A(alloc(s, &s->mv_prefix, n + 1));
-    A(alloc(s, &s->mv_key, n));
-    A(alloc(s, &s->mv_slot, n));
-    A(alloc(s, &s->mv_skey, n));
-    A(alloc(s, &s->mv_sslot, n));
-    A(alloc(s, &s->mv_sorted, n));
-    A(alloc(s, &s->mv_perm, n));
     A(alloc(s, &s->counters, kCounters));
+    s->passes = (key_bits_for(s->ncell) + 7) / 8;
     if (st == XD_OK) A(cuda_status(cudaMemset(s->counters, 0, sizeof(unsigned) * kCounters), "mixed counters"));
     if (st == XD_OK && s->nplanes) {
         A(cuda_status(cudaMemcpy(s->planes, d.planes, sizeof(xd_plane_info) * s->nplanes, cudaMemcpyHostToDevice), "mixed planes"));
@@ -1428,57 +1272,102 @@ int mixed_download(MixedScene* s, double* pos, double* vel, double* acc, double*
     return st;
 }
 
-// Sort, cell bounds, gather (with the update of MODE) and contacts, for the
-// keys already in s->keys.
+// Re-binning: stable radix sort of the keys, then the cell lower bounds.
+static int rebuild(MixedScene* s, cudaStream_t q)
+{
+    const unsigned n = s->n;
+    unsigned *sk = nullptr, *sv = nullptr;
+    int st = radix_sort_pairs(s->keys, s->vals, n, key_bits_for(s->ncell), s->sort_scratch, q, &sk, &sv);
+    if (st != XD_OK) return st;
+    // the output buffers depend only on the pass count: fixed for the scene
+    s->perm = sv;
+    s->sorted_keys = sk;
+    k_lb_fill<<<blocks(n + 1, 256), 256, 0, q>>>(sk, n, s->ncell, s->lb, s->prev_keys, s->gaps, s->counters);
+    k_lb_long<<<152 * 4, 256, 0, q>>>(s->gaps, s->counters, s->lb);
+    return launch_status("mixed re-binning");
+}
+
+// Inside a stream capture: a conditional node that runs the re-binning when
+// the handle is set (by k_mx_keys), with the capture continuing after it.
+static int capture_conditional_rebuild(MixedScene* s, cudaStream_t q, cudaGraphConditionalHandle h)
+{
+    cudaStreamCaptureStatus cst;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    int st = cuda_status(cudaStreamGetCaptureInfo(q, &cst, nullptr, &g, &deps, nullptr, &nd), "mixed capture info");
+    if (st != XD_OK) return st;
+    cudaGraphNodeParams np = { cudaGraphNodeTypeConditional };
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    st = cuda_status(cudaGraphAddNode(&node, g, deps, nullptr, nd, &np), "mixed conditional node");
+    if (st != XD_OK) return st;
+    cudaStream_t bs = nullptr;
+    st = cuda_status(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking), "mixed conditional stream");
+    if (st != XD_OK) return st;
+    st = cuda_status(cudaStreamBeginCaptureToGraph(bs, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                   cudaStreamCaptureModeThreadLocal), "mixed conditional capture");
+    if (st == XD_OK) {
+        int r = rebuild(s, bs);
+        cudaGraph_t body = nullptr;
+        st = cuda_status(cudaStreamEndCapture(bs, &body), "mixed conditional capture");
+        if (r != XD_OK) st = r;
+    }
+    cudaStreamDestroy(bs);
+    if (st != XD_OK) return st;
+    return cuda_status(cudaStreamUpdateCaptureDependencies(q, &node, nullptr, 1, cudaStreamSetCaptureDependencies),
+                       "mixed capture dependencies");
+}
+
+// One step: keys and the skin test, re-binning when needed, the gather with
+// the update of MODE, contacts and walls.  cond: the conditional handle when
+// capturing into a graph (nullptr for direct launches).
 template <int MODE>
-static int grid_and_contacts(MixedScene* s, cudaStream_t q, const Phases& ph, bool record,
-                             unsigned rec_cap)
+static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool record, unsigned rec_cap,
+                     const cudaGraphConditionalHandle* cond)
 {
     const unsigned n = s->n;
     int st = cuda_status(cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * kPerStepCounters, q),
                          "mixed counters");
     if (st != XD_OK) return st;
-    unsigned *sk = nullptr, *sv = nullptr;
+    Master& Mcur = s->m[s->cur];
+    ph.begin(0, q);
+    k_mx_keys<MODE><<<blocks(n, 256), 256, 0, q>>>(s->P, Mcur, s->pf, s->Fc, s->prev_keys, s->keys, s->vals,
+                                                   s->counters, cond ? *cond : 0, cond ? 1 : 0);
+    st = launch_status("mixed keys");
+    ph.end(0, q);
+    if (st != XD_OK) return st;
     ph.begin(2, q);
-    if (!s->cells_clean) {
-        // no previous order to exploit: full stable radix sort
-        st = radix_sort_pairs(s->keys, s->vals, n, key_bits_for(s->ncell), s->sort_scratch, q, &sk, &sv);
-        if (st == XD_OK)
-            st = cuda_status(cudaMemsetAsync(s->counters + CN_MOVERS, 0, sizeof(unsigned), q), "mixed movers");
+    if (cond) {
+        st = capture_conditional_rebuild(s, q, *cond);
     } else {
-        const unsigned nb = div_up(n, 1024u);
-        unsigned* total = s->counters + CN_MOVERS;
-        k_mv_count<<<nb, 256, 0, q>>>(s->keys, s->prev_keys, n, s->mv_bcount);
-        k_mv_scan<<<1, 1024, 0, q>>>(s->mv_bcount, nb, total);
-        k_mv_compact<<<nb, 256, 0, q>>>(s->keys, s->prev_keys, n, s->mv_bcount, s->mv_prefix,
-                                        s->mv_key, s->mv_slot);
-        k_mv_rank<<<152 * 2, 256, 0, q>>>(total, s->mv_key, s->mv_slot, s->prev_keys, s->mv_prefix,
-                                          n, s->mv_skey, s->mv_sslot, s->mv_sorted, s->mv_perm);
-        k_mv_place<<<blocks(n, 256), 256, 0, q>>>(s->keys, s->prev_keys, n, s->mv_prefix, total,
-                                                  s->mv_skey, s->mv_sslot, s->mv_sorted, s->mv_perm);
-        st = launch_status("mixed near-sorted resort");
-        sk = s->mv_sorted;
-        sv = s->mv_perm;
-    }
-    if (st == XD_OK) {
-        k_lb_fill<<<blocks(n + 1, 256), 256, 0, q>>>(sk, n, s->ncell, s->lb, s->prev_keys, s->gaps,
-                                                     s->counters);
-        k_lb_long<<<152 * 4, 256, 0, q>>>(s->gaps, s->counters, s->lb);
-        st = launch_status("mixed cell bounds");
-        s->cells_clean = true;
+        bool need = !s->cells_clean;
+        if (need) {
+            st = cuda_status(cudaMemsetAsync(s->counters + CN_REBUILD, 1, 1, q), "mixed re-binning flag");
+        } else {
+            unsigned flag = 0;
+            st = cuda_status(cudaMemcpyAsync(&flag, s->counters + CN_REBUILD, sizeof(unsigned),
+                                             cudaMemcpyDeviceToHost, q), "mixed re-binning flag");
+            if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "mixed re-binning flag");
+            need = flag != 0;
+        }
+        if (st == XD_OK && need) st = rebuild(s, q);
     }
     ph.end(2, q);
     if (st != XD_OK) return st;
+    s->cells_clean = true;
     ph.begin(6, q);
     const int nxt = 1 - s->cur;
-    k_mx_gather<MODE><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->m[nxt], sv, s->Fc, s->Mc,
-                                                     s->pf, s->qa, s->qb);
+    k_mx_gather<MODE><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->m[nxt], s->perm, s->counters,
+                                                     s->Fc, s->Mc, s->pf, s->qa, s->qb);
     st = launch_status("mixed gather");
     s->cur = nxt;
     ph.end(6, q);
     if (st != XD_OK) return st;
     ph.begin(3, q);
-    // prev_keys holds the sorted keys: the search reads each particle's cell from it
+    // prev_keys holds the assigned keys: the search reads each particle's cell from it
     const Master& M = s->m[s->cur];
     if (record)
         k_mx_search<true><<<blocks(n, 256), 256, 0, q>>>(
@@ -1503,32 +1392,9 @@ static int grid_and_contacts(MixedScene* s, cudaStream_t q, const Phases& ph, bo
     return st;
 }
 
-// The keys of the next position (MODE 1) or the last velocity update (last).
-static int after_contacts(MixedScene* s, cudaStream_t q, const Phases& ph, bool last)
-{
-    const unsigned n = s->n;
-    ph.begin(0, q);
-    if (!last)
-        k_mx_keys<1><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->pf, s->Fc, s->keys, s->vals);
-    else
-        k_mx_finish<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc);
-    int st = launch_status(last ? "mixed finish" : "mixed keys");
-    ph.end(0, q);
-    return st;
-}
-
-// One middle step: velocity of step t and position of step t + 1 (in the
-// gather), contacts, then the next step's keys.
-static int middle_step(MixedScene* s, cudaStream_t q, const Phases& ph, bool last)
-{
-    int st = grid_and_contacts<1>(s, q, ph, false, 0);
-    if (st != XD_OK) return st;
-    return after_contacts(s, q, ph, last);
-}
-
 // Captures two middle steps into a graph for the current buffer parity (the
 // pair of steps leaves the parity unchanged).  Needs cells_clean.
-static int capture_pair(MixedScene* s, cudaStream_t q)
+static int capture_pair(MixedScene* s)
 {
     const int parity = s->cur;
     cudaStream_t cs = nullptr;
@@ -1536,9 +1402,18 @@ static int capture_pair(MixedScene* s, cudaStream_t q)
     if (e != cudaSuccess) return cuda_status(e, "mixed graph stream");
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     int st = cuda_status(e, "mixed graph capture");
+    cudaGraph_t cg = nullptr;
+    cudaGraphConditionalHandle h[2] = { 0, 0 };
+    if (st == XD_OK) {
+        cudaStreamCaptureStatus cst;
+        st = cuda_status(cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg), "mixed capture info");
+    }
+    for (int k = 0; k < 2 && st == XD_OK; ++k)
+        st = cuda_status(cudaGraphConditionalHandleCreate(&h[k], cg, 0, cudaGraphCondAssignDefault),
+                         "mixed conditional handle");
     Phases none;
-    if (st == XD_OK) st = middle_step(s, cs, none, false);
-    if (st == XD_OK) st = middle_step(s, cs, none, false);
+    if (st == XD_OK) st = step_once<1>(s, cs, none, false, 0, &h[0]);
+    if (st == XD_OK) st = step_once<1>(s, cs, none, false, 0, &h[1]);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(cs, &g);
     if (st == XD_OK) st = cuda_status(e, "mixed graph capture");
@@ -1546,7 +1421,6 @@ static int capture_pair(MixedScene* s, cudaStream_t q)
     if (st == XD_OK) st = cuda_status(cudaGraphInstantiate(&s->graph[parity], g, 0), "mixed graph instantiate");
     if (g) cudaGraphDestroy(g);
     cudaStreamDestroy(cs);
-    (void)q;
     return st;
 }
 
@@ -1554,66 +1428,64 @@ int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
 {
     if (nsteps == 0 || s->n == 0) return XD_OK;
     if (!s->ready) return set_error(XD_ERR_STATE, "mixed mode: no state uploaded");
-    const unsigned n = s->n;
     const bool graphs = s->use_graphs && ph.fn == nullptr;
-    int st;
-    if (s->cells_clean && s->n > 1) {
-        // The near-sorted resort ranks the movers in O(M^2); after a burst of
-        // movers in the previous call, start this one with a full radix sort.
-        unsigned prev_movers = 0;
-        st = cuda_status(cudaMemcpyAsync(&prev_movers, s->counters + CN_MOVERS, sizeof(unsigned),
-                                         cudaMemcpyDeviceToHost, q), "mixed mover count");
-        if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "mixed mover count");
-        if (st != XD_OK) return st;
-        if (prev_movers > s->n / 16 || prev_movers > 65536u) s->cells_clean = false;
-    }
-    // step 1: position update (in the gather) from the state's (v, a)
-    ph.begin(0, q);
-    k_mx_keys<0><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->pf, s->Fc, s->keys, s->vals);
-    st = launch_status("mixed keys");
-    ph.end(0, q);
-    if (st == XD_OK) st = grid_and_contacts<0>(s, q, ph, false, 0);
-    if (st == XD_OK) st = after_contacts(s, q, ph, nsteps == 1);
+    // step 1: the position update (in the gather) from the state's (v, a)
+    int st = step_once<0>(s, q, ph, false, 0, nullptr);
     if (st != XD_OK) return st;
     unsigned t = 1;
-    // pairs of middle steps as one graph launch; the last step runs directly
-    while (graphs && nsteps - t >= 3) {
+    // pairs of middle steps as one graph launch
+    while (graphs && nsteps - t >= 2) {
         if (!s->graph[s->cur]) {
-            st = capture_pair(s, q);
+            st = capture_pair(s);
             if (st != XD_OK) return st;
         }
         st = cuda_status(cudaGraphLaunch(s->graph[s->cur], q), "mixed graph launch");
         if (st != XD_OK) return st;
         t += 2;   // two gathers: the buffer parity is unchanged
     }
-    for (; t < nsteps; ++t) {
-        st = middle_step(s, q, ph, t + 1 == nsteps);
-        if (st != XD_OK) return st;
-    }
-    return XD_OK;
+    for (; t < nsteps && st == XD_OK; ++t) st = step_once<1>(s, q, ph, false, 0, nullptr);
+    if (st != XD_OK) return st;
+    // the last velocity update
+    ph.begin(0, q);
+    k_mx_finish<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc);
+    st = launch_status("mixed finish");
+    ph.end(0, q);
+    return st;
 }
 
 unsigned long long mixed_launches(MixedScene* s, unsigned nsteps)
 {
     if (!s || nsteps == 0 || s->n == 0) return 0;
-    const unsigned passes = (key_bits_for(s->ncell) + 7) / 8;
-    // per step: 5 resort kernels + 2 cell-bound kernels + gather + search + force
-    // (+ walls) + the next keys or the last velocity update
-    const unsigned long long per = 5 + 2 + 1 + 2 + (s->nplanes ? 1 : 0) + 1;
-    unsigned long long total = 1 + per * nsteps;   // + the first keys
-    if (!s->cells_clean && s->n > 1) total += 5ull * passes - 5;   // first step: full radix sort
+    // per step: keys + gather + search + force (+ walls); + the last velocity
+    // update; a step that re-bins adds mixed_rebuild_launches()
+    const unsigned long long per = 4 + (s->nplanes ? 1 : 0);
+    unsigned long long total = per * nsteps + 1;
+    if (!s->cells_clean) total += mixed_rebuild_launches(s);   // the first step re-bins
     return total;
 }
 
-// Contacts of the current state: keys of the current positions, sort and
-// gather without an update.
+unsigned long long mixed_rebuild_launches(MixedScene* s)
+{
+    if (!s || s->n <= 1) return s && s->n ? 2 : 0;
+    return 5ull * s->passes + 2;
+}
+
+int mixed_rebuilds(MixedScene* s, unsigned long long* out, cudaStream_t q)
+{
+    unsigned c = 0;
+    int st = cuda_status(cudaMemcpyAsync(&c, s->counters + CN_REBUILDS, sizeof(unsigned), cudaMemcpyDeviceToHost, q),
+                         "rebuilds");
+    if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "rebuilds");
+    *out = c;
+    return st;
+}
+
+// Contacts of the current state: keys of the current positions, re-binning
+// if needed, and the gather without an update.
 static int current_contacts(MixedScene* s, cudaStream_t q, bool record, unsigned rec_cap)
 {
     Phases none;
-    k_mx_keys<3><<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->pf, s->Fc, s->keys, s->vals);
-    int st = launch_status("mixed keys");
-    if (st == XD_OK) st = grid_and_contacts<3>(s, q, none, record, rec_cap);
-    return st;
+    return step_once<3>(s, q, none, record, rec_cap, nullptr);
 }
 
 int mixed_eval_contacts(MixedScene* s, double* force, double* moment, cudaStream_t q)

@@ -26,6 +26,8 @@ int mixed_download(MixedScene* s, double* pos, double* vel, double* acc, double*
                    double* alpha, double* force, double* moment, cudaStream_t q);
 int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph);
 unsigned long long mixed_launches(MixedScene* s, unsigned nsteps);
+unsigned long long mixed_rebuild_launches(MixedScene* s);
+int mixed_rebuilds(MixedScene* s, unsigned long long* out, cudaStream_t q);
 int mixed_eval_contacts(MixedScene* s, double* force, double* moment, cudaStream_t q);
 int mixed_pair_list(MixedScene* s, unsigned cap_per_particle, unsigned* counts, unsigned* partners,
                     cudaStream_t q);

@@ -433,6 +433,19 @@ int xd_scene_counters(xd_scene* s, unsigned long long out[4], void* stream)
     return mixed_counters(s->mixed, out, static_cast<cudaStream_t>(stream));
 }
 
+int xd_scene_rebuilds(xd_scene* s, unsigned long long* count, unsigned long long* launches_each,
+                      void* stream)
+{
+    if (!s || !count || !launches_each) return set_error(XD_ERR_INVALID, "scene_rebuilds: null argument");
+    if (!s->mixed) {
+        *count = 0;
+        *launches_each = 0;
+        return XD_OK;
+    }
+    *launches_each = mixed_rebuild_launches(s->mixed);
+    return mixed_rebuilds(s->mixed, count, static_cast<cudaStream_t>(stream));
+}
+
 int xd_scene_set_timing(xd_scene* s, int enable)
 {
     if (!s) return set_error(XD_ERR_INVALID, "scene_set_timing: null scene");

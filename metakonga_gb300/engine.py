@@ -151,6 +151,13 @@ class DeviceScene:
         return {"near_wall": int(out[0]), "fp64_decisions": int(out[1]),
                 "fp64_normal_forces": int(out[2]), "fp64_slips": int(out[3])}
 
+    def rebuilds(self, stream: int = 0):
+        """(re-binnings so far, kernel launches per re-binning) of a mixed scene."""
+        cnt = np.zeros(1, np.uint64)
+        each = np.zeros(1, np.uint64)
+        call("xd_scene_rebuilds", self.handle, cnt.ctypes.data, each.ctypes.data, stream)
+        return int(cnt[0]), int(each[0])
+
     def launches(self, nsteps: int) -> int:
         return int(_lib.lib().xd_scene_launches(self.handle, nsteps))
 
