@@ -319,15 +319,30 @@ __device__ __forceinline__ float q_to_f(long long q)
                      __fmul_rn(__int2float_rn((int)(q & 0xfffff)), 0x1p-36f));
 }
 
-__device__ __forceinline__ void write_view(const MixParams& P, unsigned i, double x, double y,
-                                           double z, double r, float4* __restrict__ pf,
-                                           longlong2* __restrict__ qa, longlong2* __restrict__ qb)
+__device__ __forceinline__ float4 write_view(const MixParams& P, unsigned i, double x, double y,
+                                             double z, double r, float4* __restrict__ pf,
+                                             longlong2* __restrict__ qa, longlong2* __restrict__ qb)
 {
     const long long qx = fixed_q(x, P.qoff[0]), qy = fixed_q(y, P.qoff[1]), qz = fixed_q(z, P.qoff[2]);
     const long long qr = fixed_q(r, kMagic);
     qa[i] = make_longlong2(qx, qy);
     qb[i] = make_longlong2(qz, qr);
-    pf[i] = make_float4(q_to_f(qx), q_to_f(qy), q_to_f(qz), (float)r);
+    const float4 v = make_float4(q_to_f(qx), q_to_f(qy), q_to_f(qz), (float)r);
+    pf[i] = v;
+    return v;
+}
+
+// Planes within reach of a particle: FP32 distance to each plane's supporting
+// plane against r plus a tolerance (the finite plane is never nearer).
+__device__ __forceinline__ unsigned near_planes(const MixParams& P, const float4& p)
+{
+    unsigned mask = 0;
+    for (int w = 0; w < P.nplanes; ++w) {
+        const float hz = (p.x - P.pxw[w][0]) * P.pun[w][0] + (p.y - P.pxw[w][1]) * P.pun[w][1] +
+                         (p.z - P.pxw[w][2]) * P.pun[w][2];
+        if (fabsf(hz) < p.w + P.wall_tol) mask |= 1u << w;
+    }
+    return mask;
 }
 
 // Cell key of a position relative to the grid origin (FP32).  Interior cells
@@ -341,6 +356,22 @@ __device__ __forceinline__ unsigned cell_key(const MixParams& P, float x, float 
     cy = min(max(cy, 1), P.gy - 2);
     cz = min(max(cz, 1), P.gz - 2);
     return ((unsigned)cz * (unsigned)P.gy + (unsigned)cy) * (unsigned)P.gx + (unsigned)cx;
+}
+
+// Appends v to list (counter *cnt) for the lanes where take is set, one
+// atomic per warp.  Every lane of the warp calls it.
+template <typename T>
+__device__ __forceinline__ void warp_append(bool take, const T& v, T* __restrict__ list,
+                                            unsigned* __restrict__ cnt)
+{
+    const unsigned bal = __ballot_sync(0xffffffffu, take);
+    if (!bal) return;
+    const unsigned lane = threadIdx.x & 31u;
+    const int leader = __ffs(bal) - 1;
+    unsigned base = 0;
+    if ((int)lane == leader) base = atomicAdd(cnt, (unsigned)__popc(bal));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (take) list[base + __popc(bal & ((1u << lane) - 1u))] = v;
 }
 
 // ---- integration -----------------------------------------------------------
@@ -455,44 +486,49 @@ __device__ __forceinline__ double drift(const MixParams& P, double x, float vhi,
     return __dadd_rn(x, __dadd_rn((double)inc.hi, (double)inc.lo));
 }
 
-// Applies the update of MODE and writes the contact view; after a re-binning
-// (counters[CN_REBUILD] set) it also moves the state into the new order
-// (perm: new slot -> old slot).
+// Applies the update of MODE and writes the contact view and the wall list;
+// after a re-binning (counters[CN_REBUILD] set) it also moves the state into
+// the new order (perm: new slot -> old slot).
 template <int MODE>
 __global__ void __launch_bounds__(256) k_mx_gather(MixParams P, Master S, Master D,
                                                    const unsigned* __restrict__ perm,
-                                                   const unsigned* __restrict__ counters,
+                                                   unsigned* __restrict__ counters,
                                                    const float4* __restrict__ Fc,
                                                    const float4* __restrict__ Mc,
                                                    float4* __restrict__ pf,
                                                    longlong2* __restrict__ qa,
-                                                   longlong2* __restrict__ qb)
+                                                   longlong2* __restrict__ qb,
+                                                   uint2* __restrict__ wall_list)
 {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
-    const unsigned o = counters[CN_REBUILD] ? __ldg(perm + i) : i;
-    double x = __ldg(S.x + o), y = __ldg(S.y + o), z = __ldg(S.z + o);
-    const double r = __ldg(S.r + o);
-    float4 vh = __ldg(S.vh + o), vl = __ldg(S.vl + o), wh = __ldg(S.wh + o), wl = __ldg(S.wl + o);
-    float4 ab = __ldg(S.ab + o);
-    float2 b2 = __ldg(S.b2 + o);
-    if (MODE == 1) kick(P, vh, vl, wh, wl, ab, b2, __ldg(Fc + o), __ldg(Mc + o));
-    if (MODE == 0 || MODE == 1) {
-        x = drift(P, x, vh.x, vl.x, 0, ab.x);
-        y = drift(P, y, vh.y, vl.y, 1, ab.y);
-        z = drift(P, z, vh.z, vl.z, 2, ab.z);
+    unsigned wmask = 0;
+    if (i < P.n) {
+        const unsigned o = counters[CN_REBUILD] ? __ldg(perm + i) : i;
+        double x = __ldg(S.x + o), y = __ldg(S.y + o), z = __ldg(S.z + o);
+        const double r = __ldg(S.r + o);
+        float4 vh = __ldg(S.vh + o), vl = __ldg(S.vl + o), wh = __ldg(S.wh + o), wl = __ldg(S.wl + o);
+        float4 ab = __ldg(S.ab + o);
+        float2 b2 = __ldg(S.b2 + o);
+        if (MODE == 1) kick(P, vh, vl, wh, wl, ab, b2, __ldg(Fc + o), __ldg(Mc + o));
+        if (MODE == 0 || MODE == 1) {
+            x = drift(P, x, vh.x, vl.x, 0, ab.x);
+            y = drift(P, y, vh.y, vl.y, 1, ab.y);
+            z = drift(P, z, vh.z, vl.z, 2, ab.z);
+        }
+        D.x[i] = x;
+        D.y[i] = y;
+        D.z[i] = z;
+        D.r[i] = r;
+        D.vh[i] = vh;
+        D.vl[i] = vl;
+        D.wh[i] = wh;
+        D.wl[i] = wl;
+        D.ab[i] = ab;
+        D.b2[i] = b2;
+        wmask = near_planes(P, write_view(P, i, x, y, z, r, pf, qa, qb));
     }
-    D.x[i] = x;
-    D.y[i] = y;
-    D.z[i] = z;
-    D.r[i] = r;
-    D.vh[i] = vh;
-    D.vl[i] = vl;
-    D.wh[i] = wh;
-    D.wl[i] = wl;
-    D.ab[i] = ab;
-    D.b2[i] = b2;
-    write_view(P, i, x, y, z, r, pf, qa, qb);
+    // the wall pass takes the particles near a plane, with their plane masks
+    warp_append(wmask != 0u, make_uint2(i, wmask), wall_list, counters + CN_WALLS);
 }
 
 // MODE 2: velocity only, in place (the last step of a call).
@@ -575,6 +611,30 @@ __device__ __forceinline__ double fp64_cdist(const Master& M, unsigned i, unsign
     return __dsub_rn(__dadd_rn(__ldg(M.r + i), __ldg(M.r + j)), __dsqrt_rn(d2));
 }
 
+// The candidate test of pair (i, j): FP32 prefilter, exact integer test,
+// FP64 guard band.  Returns 0 (no contact), 1 (contact) or 2 (contact decided
+// by the FP64 test).
+template <bool COUNT>
+__device__ __forceinline__ int touch(const MixParams& P, const Master& M, unsigned i, unsigned j,
+                                     const float4& pi, const longlong2& qai, const longlong2& qbi,
+                                     const float4* __restrict__ pf, const longlong2* __restrict__ qa,
+                                     const longlong2* __restrict__ qb, unsigned* __restrict__ counters)
+{
+    const float4 pj = __ldg(pf + j);
+    const float dxf = pj.x - pi.x, dyf = pj.y - pi.y, dzf = pj.z - pi.z;
+    const float Rt = pi.w + pj.w + P.tol;
+    if (dxf * dxf + dyf * dyf + dzf * dzf >= Rt * Rt) return 0;
+    const longlong2 qaj = __ldg(qa + j), qbj = __ldg(qb + j);
+    const long long ddx = qaj.x - qai.x, ddy = qaj.y - qai.y, ddz = qbj.x - qbi.x;
+    const long long Rq = qbi.y + qbj.y;
+    const long long N = Rq * Rq - (ddx * ddx + ddy * ddy + ddz * ddz);
+    const long long band = 2 * Rq * P.guard_q;
+    if (N > band) return 1;
+    if (N < -band) return 0;
+    if (COUNT) atomicAdd(counters + CN_DECISIONS, 1u);
+    return fp64_cdist(M, i, j) > 0 ? 2 : 0;
+}
+
 // Visits the contacts of slot i in the reference's order (neighbour rows z
 // then y, each row's slots ascending): fn(j, guard) for every touching j.
 // Candidates pass an FP32 prefilter, then the exact integer test; pairs in
@@ -603,23 +663,8 @@ __device__ __forceinline__ void for_each_contact(const MixParams& P, const Maste
         }
         for (unsigned j = s; j < e; ++j) {
             if (j == i) continue;
-            const float4 pj = __ldg(pf + j);
-            const float dxf = pj.x - pi.x, dyf = pj.y - pi.y, dzf = pj.z - pi.z;
-            const float Rt = pi.w + pj.w + P.tol;
-            if (dxf * dxf + dyf * dyf + dzf * dzf >= Rt * Rt) continue;
-            const longlong2 qaj = __ldg(qa + j), qbj = __ldg(qb + j);
-            const long long ddx = qaj.x - qai.x, ddy = qaj.y - qai.y, ddz = qbj.x - qbi.x;
-            const long long Rq = qbi.y + qbj.y;
-            const long long N = Rq * Rq - (ddx * ddx + ddy * ddy + ddz * ddz);
-            const long long band = 2 * Rq * P.guard_q;
-            bool guard = false;
-            if (N <= band) {
-                if (N < -band) continue;
-                if (COUNT) atomicAdd(counters + CN_DECISIONS, 1u);
-                if (!(fp64_cdist(M, i, j) > 0)) continue;
-                guard = true;
-            }
-            fn(j, guard);
+            const int t = touch<COUNT>(P, M, i, j, pi, qai, qbi, pf, qa, qb, counters);
+            if (t) fn(j, t == 2);
         }
         s = sn;
         e = en;
@@ -627,25 +672,15 @@ __device__ __forceinline__ void for_each_contact(const MixParams& P, const Maste
     }
 }
 
-// Appends v to list (counter *cnt) for the lanes where take is set, one
-// atomic per warp.  Every lane of the warp calls it.
-template <typename T>
-__device__ __forceinline__ void warp_append(bool take, const T& v, T* __restrict__ list,
-                                            unsigned* __restrict__ cnt)
-{
-    const unsigned bal = __ballot_sync(0xffffffffu, take);
-    if (!bal) return;
-    const unsigned lane = threadIdx.x & 31u;
-    const int leader = __ffs(bal) - 1;
-    unsigned base = 0;
-    if ((int)lane == leader) base = atomicAdd(cnt, (unsigned)__popc(bal));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (take) list[base + __popc(bal & ((1u << lane) - 1u))] = v;
-}
+constexpr unsigned kIncomplete = 0x80000000u;   // ccount flag: the list is not complete
 
-// Candidate search of every particle: the contact list, the force list (the
-// particles with contacts; the others get zero contact force here), and the
-// wall list with each particle's mask of nearby planes.
+// Candidate search, one thread per particle: the nine neighbour rows' slot
+// ranges are staged in shared memory and visited as one flattened loop (rows
+// z then y, slots ascending: the reference's order), so a warp runs as many
+// iterations as its busiest lane has candidates.  Writes the contact list
+// (kListCap entries; more marks it incomplete and the force pass searches
+// again), zero contact force for the particles without contacts, and the
+// force list (the particles with contacts).
 template <bool RECORD>
 __global__ void __launch_bounds__(256) k_mx_search(MixParams P, Master M, const float4* __restrict__ pf,
                                                    const longlong2* __restrict__ qa,
@@ -656,39 +691,52 @@ __global__ void __launch_bounds__(256) k_mx_search(MixParams P, Master M, const 
                                                    unsigned* __restrict__ clist,
                                                    unsigned* __restrict__ flist,
                                                    float4* __restrict__ Fc, float4* __restrict__ Mc,
-                                                   uint2* __restrict__ wall_list,
                                                    unsigned* __restrict__ counters,
                                                    unsigned* __restrict__ rec_count,
                                                    unsigned* __restrict__ rec_pairs, unsigned rec_cap)
 {
-    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ uint2 rows[9][256];
+    const unsigned tid = threadIdx.x;
+    const unsigned i = blockIdx.x * blockDim.x + tid;
     const bool live = i < P.n;
-    unsigned nc = 0, wmask = 0;
+    unsigned nc = 0;
     if (live) {
         const float4 pi = __ldg(pf + i);
         const longlong2 qai = __ldg(qa + i), qbi = __ldg(qb + i);
+        const unsigned key = __ldg(keys + i);
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+            const unsigned c = key - 1u + (unsigned)(r % 3 - 1) * (unsigned)P.gx + (unsigned)(r / 3 - 1) * P.gxy;
+            rows[r][tid] = make_uint2(__ldg(lb + c), __ldg(lb + c + 3));
+        }
         const unsigned n = P.n;
-        for_each_contact<true>(P, M, i, pi, qai, qbi, __ldg(keys + i), pf, qa, qb, lb, counters,
-                               [&](unsigned j, bool guard) {
-                                   if (nc < kListCap) clist[(size_t)nc * n + i] = j | (guard ? kGuardBit : 0u);
-                                   if (RECORD && nc < rec_cap) rec_pairs[(size_t)i * rec_cap + nc] = j;
-                                   ++nc;
-                               });
-        ccount[i] = nc;
+        unsigned r = 0;
+        uint2 b = rows[0][tid];
+        unsigned j = b.x;
+        for (;;) {
+            while (j >= b.y && ++r < 9) {
+                b = rows[r][tid];
+                j = b.x;
+            }
+            if (r >= 9) break;
+            if (j != i) {
+                const int t = touch<true>(P, M, i, j, pi, qai, qbi, pf, qa, qb, counters);
+                if (t) {
+                    if (nc < kListCap) clist[(size_t)nc * n + i] = j | (t == 2 ? kGuardBit : 0u);
+                    if (RECORD && nc < rec_cap) rec_pairs[(size_t)i * rec_cap + nc] = j;
+                    ++nc;
+                }
+            }
+            ++j;
+        }
+        ccount[i] = nc | (nc > kListCap ? kIncomplete : 0u);
         if (RECORD) rec_count[i] = nc;
         if (!nc) {
             Fc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
             Mc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        // walls: FP32 distance to each plane's supporting plane
-        for (int w = 0; w < P.nplanes; ++w) {
-            const float hz = (pi.x - P.pxw[w][0]) * P.pun[w][0] + (pi.y - P.pxw[w][1]) * P.pun[w][1] +
-                             (pi.z - P.pxw[w][2]) * P.pun[w][2];
-            if (fabsf(hz) < pi.w + P.wall_tol) wmask |= 1u << w;
-        }
     }
     warp_append(live && nc > 0, i, flist, counters + CN_FORCE);
-    warp_append(wmask != 0u, make_uint2(i, wmask), wall_list, counters + CN_WALLS);
 }
 
 // Per-particle contact state carried across the pairs of one particle (the
@@ -822,8 +870,7 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
 }
 
 // Forces of the particles with contacts, over each one's list in search
-// order; a particle with more than kListCap contacts finds the rest by
-// searching again (same order).
+// order; a particle whose list is incomplete is searched again (same order).
 __global__ void __launch_bounds__(256) k_mx_force(MixParams P, Master M, const float4* __restrict__ pf,
                                                   const longlong2* __restrict__ qa,
                                                   const longlong2* __restrict__ qb,
@@ -841,7 +888,7 @@ __global__ void __launch_bounds__(256) k_mx_force(MixParams P, Master M, const f
         Own I;
         I.i = __ldg(flist + t);
         const unsigned i = I.i;
-        const unsigned nc = __ldg(ccount + i);
+        const unsigned cc = __ldg(ccount + i);
         I.qa = __ldg(qa + i);
         I.qb = __ldg(qb + i);
         I.vh = __ldg(M.vh + i);
@@ -855,17 +902,15 @@ __global__ void __launch_bounds__(256) k_mx_force(MixParams P, Master M, const f
         A.Mm = fk(0.f, 0.f, 0.f);
         A.sumF = fk(0.f, 0.f, 0.f);
         A.sumM = fk(0.f, 0.f, 0.f);
-        const unsigned nl = min(nc, kListCap);
-        for (unsigned k = 0; k < nl; ++k) {
-            const unsigned e = __ldg(clist + (size_t)k * P.n + i);
-            contact_force(P, M, I, e & ~kGuardBit, (e & kGuardBit) != 0u, mass0, pf, qa, qb, counters, A);
-        }
-        if (nc > kListCap) {
-            unsigned k = 0;
+        if (!(cc & kIncomplete)) {
+            for (unsigned k = 0; k < cc; ++k) {
+                const unsigned e = __ldg(clist + (size_t)k * P.n + i);
+                contact_force(P, M, I, e & ~kGuardBit, (e & kGuardBit) != 0u, mass0, pf, qa, qb, counters, A);
+            }
+        } else {
             for_each_contact<false>(P, M, i, __ldg(pf + i), I.qa, I.qb, __ldg(keys + i), pf, qa, qb, lb,
                                     counters, [&](unsigned j, bool guard) {
-                                        if (k++ >= kListCap)
-                                            contact_force(P, M, I, j, guard, mass0, pf, qa, qb, counters, A);
+                                        contact_force(P, M, I, j, guard, mass0, pf, qa, qb, counters, A);
                                     });
         }
         Fc[i] = make_float4(A.sumF.x, A.sumF.y, A.sumF.z, 0.f);
@@ -1361,7 +1406,7 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
     ph.begin(6, q);
     const int nxt = 1 - s->cur;
     k_mx_gather<MODE><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->m[nxt], s->perm, s->counters,
-                                                     s->Fc, s->Mc, s->pf, s->qa, s->qb);
+                                                     s->Fc, s->Mc, s->pf, s->qa, s->qb, s->wall_list);
     st = launch_status("mixed gather");
     s->cur = nxt;
     ph.end(6, q);
@@ -1372,11 +1417,11 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
     if (record)
         k_mx_search<true><<<blocks(n, 256), 256, 0, q>>>(
             s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->ccount, s->clist, s->flist, s->Fc,
-            s->Mc, s->wall_list, s->counters, s->rec_count, s->rec_pairs, rec_cap);
+            s->Mc, s->counters, s->rec_count, s->rec_pairs, rec_cap);
     else
         k_mx_search<false><<<blocks(n, 256), 256, 0, q>>>(
             s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->ccount, s->clist, s->flist, s->Fc,
-            s->Mc, s->wall_list, s->counters, nullptr, nullptr, 0);
+            s->Mc, s->counters, nullptr, nullptr, 0);
     k_mx_force<<<min(blocks(n, 256), 152u * 8u), 256, 0, q>>>(s->P, M, s->pf, s->qa, s->qb,
                                                               s->prev_keys, s->lb, s->ccount, s->clist,
                                                               s->flist, s->mass0, s->Fc, s->Mc,
