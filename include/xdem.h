@@ -353,7 +353,8 @@ int xd_scene_eval_contacts(xd_scene* scene, double* force, double* moment, void*
 int xd_scene_pair_list(xd_scene* scene, unsigned cap, unsigned* counts, unsigned* partners,
                        void* stream);
 
-/* Mixed-mode counters: [0] particles near a wall in the last contact pass,
+/* Mixed-mode counters: [0] particles the contact pass visits (those with a
+ * Verlet neighbour or a plane within reach at the last list build),
  * [1] pairs decided by the FP64 guard-band test (cumulative), [2] normal
  * forces formed in FP64 because the elastic and damping terms nearly cancel
  * (cumulative), [3] slips formed in FP64 because the rotation term cancels

@@ -9,37 +9,37 @@
 //   velocities, ang. vel.   double-float hi + lo (two FP32, ~48-bit
 //                           significand), updated with FP32 arithmetic
 //   accelerations           FP32: the contact part a - g, and alpha
-//   m, 1/m, 1/I             FP32 (the FP64 mass, by particle id, serves the
+//   1/m, 1/I                FP32 (the FP64 mass, by particle id, serves the
 //                           FP64 rechecks, the walls and the download)
 // The only FP64 operations per particle and step are the position update
 // (two adds per axis) and the fixed-point conversion (one FMA per axis).
 //
 // Per step (dem_simulation::oneStepAnalysis order, dem_simulation.cpp:447-469):
-//   k_mx_keys     the cell key of the next position, estimated in FP32, and
-//                 the skin test: every particle keeps its assigned cell (and
-//                 its slot in the cell order) while it stays inside that cell
-//                 widened by half the skin; cells are 2 r_max + skin wide, so
-//                 touching pairs still lie in neighbouring assigned cells;
-//   re-binning    only when a particle left its widened cell (a CUDA graph
-//                 conditional node, or the host between direct launches):
-//                 stable radix sort of the keys, then k_lb_fill:
-//                 lb[c] = first slot whose key is >= c, for every cell, so a
-//                 row of three cells is the slot range [lb[c0], lb[c0 + 3]);
-//   k_mx_gather   applies the velocity-Verlet update (velocity of step t from
-//                 the contact force, position of step t + 1) while moving the
-//                 state into the new cell order after a re-binning (in order
-//                 otherwise), then writes the contact view: FP32 (x, y, z, r)
-//                 and int64 fixed point (2^-36 m);
-//   k_mx_search   candidates: FP32 prefilter, then the exact integer test
-//                 N = (ri + rj)^2 - |qj - qi|^2 > 0 (no cancellation); pairs
-//                 within 2e-10 m of touching are decided by the reference's
-//                 FP64 expression, so pair lists equal the FP64 path's.  Each
-//                 particle's contacts go to a list in search order; particles
-//                 near a wall go to the wall list with a plane mask;
-//   k_mx_force    FP32 Hertz-Mindlin (DHSModel) over each particle's list in
-//                 search order (a pair without slip reuses the previous pair's
-//                 tangential force, impl:426-428);
-//   k_mx_walls    the listed particles' plane contacts in FP64.
+//   k_mx_advance  the velocity-Verlet update in place (velocity of step t from
+//                 the contact force, position of step t + 1), the contact view
+//                 -- FP32 (x, y, z, r) and int64 fixed point (2^-36 m) -- and
+//                 the skin test: cells are 2 r_max + skin wide and every
+//                 particle's Verlet list holds the slots within ri + rj + skin
+//                 of it at the list build, so both stay valid while no
+//                 particle has moved half the skin since;
+//   re-binning    only when one has (a CUDA graph conditional node, or the
+//                 host between direct launches): cell keys, stable radix sort,
+//                 the state permuted into the new cell order, k_lb_fill
+//                 (lb[c] = first slot whose key is >= c, for every cell, so a
+//                 row of three cells is the slot range [lb[c0], lb[c0 + 3])),
+//                 then k_mx_build: the Verlet lists from the neighbour cells in
+//                 the reference's order (rows z then y, slots ascending), the
+//                 planes in reach, and the heavy list of the particles with
+//                 either;
+//   k_mx_contact  for the heavy list only (the others keep zero contact
+//                 force): particle pairs over the Verlet list -- FP32
+//                 prefilter, then the exact integer test
+//                 N = (ri + rj)^2 - |qj - qi|^2 > 0 (no cancellation), pairs
+//                 within 2e-10 m of touching decided by the reference's FP64
+//                 expression so pair lists equal the FP64 path's, FP32
+//                 Hertz-Mindlin (DHSModel) in search order (a pair without slip
+//                 reuses the previous pair's tangential force, impl:426-428) --
+//                 then the planes in reach in FP64.
 // The grid is the scene's own (not the reference's wrapped 128^3): padded by
 // one cell on every side, keys clamped inside.
 #include <cuda_runtime.h>
@@ -63,28 +63,26 @@ constexpr double kQ = 68719476736.0;           // 2^36 fixed-point units per met
 constexpr float kU = 1.4551915228366852e-11f;  // 2^-36 m
 constexpr double kGuard = 2e-10;               // metres: FP64 decision inside this band
 constexpr double kMagic = 6755399441055744.0;  // 1.5 * 2^52
-constexpr unsigned kListCap = 24;              // contacts per particle kept in the list
+constexpr unsigned kVerletCap = 48;            // neighbours per particle kept in the Verlet list
 constexpr unsigned kGuardBit = 0x80000000u;    // list entry decided by the FP64 test
 
-// Counter words (one memset clears [0, kPerStepCounters) every step).
+// Counter words.
 enum {
-    CN_WALLS = 0,      // wall-list length
-    CN_FORCE = 1,      // force-list length
-    CN_GAPS = 2,       // long gaps of the cell lower-bound array
-    CN_REBUILD = 3,    // nonzero: this step re-bins the cells
-    CN_DONE = 4,       // blocks of k_mx_keys finished (last-block hand-off)
-    kPerStepCounters = 5,
-    CN_DECISIONS = 5,  // FP64 contact decisions (cumulative)
-    CN_NORMALS = 6,    // FP64 normal-force rechecks (cumulative)
-    CN_SLIPS = 7,      // FP64 slip rechecks (cumulative)
-    CN_REBUILDS = 8,   // re-binnings (cumulative)
-    kCounters = 12
+    CN_REBUILD = 0,    // nonzero: this step re-bins (set by k_mx_advance, cleared by k_mx_contact)
+    CN_DONE = 1,       // blocks of k_mx_advance finished (last-block hand-off; reset by the last)
+    CN_GAPS = 2,       // long gaps of the cell lower-bound array (re-binning)
+    CN_HEAVY = 3,      // particles with Verlet neighbours or planes in reach (since the last build)
+    CN_DECISIONS = 4,  // FP64 contact decisions (cumulative)
+    CN_NORMALS = 5,    // FP64 normal-force rechecks (cumulative)
+    CN_SLIPS = 6,      // FP64 slip rechecks (cumulative)
+    CN_REBUILDS = 7,   // re-binnings (cumulative)
+    kCounters = 8
 };
 
 struct Master {
     double *x, *y, *z, *r;   // FP64 positions and radii
-    float4* vh;              // velocity hi; .w = m
-    float4* vl;              // velocity lo; .w = 1/m
+    float4* vh;              // velocity hi; .w = 1/m
+    float4* vl;              // velocity lo; .w unused
     float4* wh;              // angular velocity hi; .w = 1/I
     float4* wl;              // angular velocity lo; .w = particle id (bits)
     float4* ab;              // contact acceleration a - g; .w = alpha.x
@@ -101,6 +99,10 @@ struct MixParams {
     double dt;
     float csf, inv_csf;
     float half_skin;     // a particle keeps its cell while within half the skin of it
+    float rmaxf;         // largest radius
+    float vcut;          // Verlet list: pairs within ri + rj + vcut are listed
+    float disp2;         // squared displacement that forces re-binning
+    float inv_gx, inv_gxy;   // 1 / gx, 1 / (gx gy) for the key decode
     float dtf, hf, half2dtf;
     float gf[3];
     float2 dt_df;        // dt as double-float
@@ -123,7 +125,7 @@ struct MixedScene {
     int gx = 0, gy = 0, gz = 0;
     double cs = 0.0;
     MixParams P;
-    Master m[2];
+    Master m[2];                  // m[0] the state in cell order; m[1] scratch for re-binning
     int cur = 0;
     double* mass0 = nullptr;   // FP64 mass by particle id (rechecks, walls, download)
     // contact view (sorted order)
@@ -132,10 +134,12 @@ struct MixedScene {
     longlong2* qb = nullptr;
     float4* Fc = nullptr;
     float4* Mc = nullptr;
-    // contact lists
-    unsigned* ccount = nullptr;   // contacts per particle
-    unsigned* clist = nullptr;    // [kListCap][n]: partner slot | kGuardBit
-    unsigned* flist = nullptr;    // particles with contacts
+    // Verlet lists (slots of the current cell order, rebuilt with the cells)
+    unsigned* hlist = nullptr;    // particles with neighbours or planes in reach
+    unsigned short* wmask = nullptr;   // planes in reach of each particle
+    unsigned* vcount = nullptr;   // Verlet neighbours per particle (| kIncomplete: overflow)
+    unsigned* vlist = nullptr;    // [kVerletCap][n]: neighbour slots in search order
+    float4* pref = nullptr;       // FP32 positions at the last list build
     // grid
     unsigned *keys = nullptr, *vals = nullptr, *prev_keys = nullptr;
     unsigned* lb = nullptr;       // ncell + 1 entries
@@ -148,7 +152,6 @@ struct MixedScene {
     // walls
     xd_plane_info* planes = nullptr;
     xd_contact_property* cps = nullptr;
-    uint2* wall_list = nullptr;   // (slot, plane mask)
     unsigned* counters = nullptr;
     // pair recording
     unsigned* rec_count = nullptr;
@@ -333,14 +336,14 @@ __device__ __forceinline__ float4 write_view(const MixParams& P, unsigned i, dou
 }
 
 // Planes within reach of a particle: FP32 distance to each plane's supporting
-// plane against r plus a tolerance (the finite plane is never nearer).
-__device__ __forceinline__ unsigned near_planes(const MixParams& P, const float4& p)
+// plane against r + pad (the finite plane is never nearer).
+__device__ __forceinline__ unsigned near_planes(const MixParams& P, const float4& p, float pad)
 {
     unsigned mask = 0;
     for (int w = 0; w < P.nplanes; ++w) {
         const float hz = (p.x - P.pxw[w][0]) * P.pun[w][0] + (p.y - P.pxw[w][1]) * P.pun[w][1] +
                          (p.z - P.pxw[w][2]) * P.pun[w][2];
-        if (fabsf(hz) < p.w + P.wall_tol) mask |= 1u << w;
+        if (fabsf(hz) < p.w + pad) mask |= 1u << w;
     }
     return mask;
 }
@@ -384,70 +387,19 @@ __device__ __forceinline__ void warp_append(bool take, const T& v, T* __restrict
 //   MODE 2  velocity only (last step of a call)
 //   MODE 3  no update (contacts of the current state)
 
-// Is p (FP32, relative to the grid origin) outside assigned cell c (key
-// coordinate; cell c spans [(c - 1) cs, c cs)) widened by half the skin?
-// Clamped boundary cells are open outward.
-__device__ __forceinline__ bool outside_cell(const MixParams& P, float p, unsigned c, int g)
+// Cell coordinates of a key: FP32 reciprocal estimates, each off by at most
+// one (the quotient is below 2^16), then corrected.
+__device__ __forceinline__ void decode_key(const MixParams& P, unsigned key, unsigned& cx, unsigned& cy,
+                                           unsigned& cz)
 {
-    const float lo = (float)((int)c - 1) * P.csf;
-    return ((int)c > 1 && p < lo - P.half_skin) || ((int)c < g - 2 && p > lo + P.csf + P.half_skin);
-}
-
-// k_mx_keys: the key of the next position, estimated in FP32 from the view,
-// and the skin test against the assigned cell (prev).  Any particle outside
-// its widened cell sets CN_REBUILD; the last block to finish passes the flag
-// to the graph's conditional node (use_cond), the one caller it allows.
-template <int MODE>
-__global__ void __launch_bounds__(256) k_mx_keys(MixParams P, Master M, const float4* __restrict__ pf,
-                                                 const float4* __restrict__ Fc,
-                                                 const unsigned* __restrict__ prev,
-                                                 unsigned* __restrict__ keys,
-                                                 unsigned* __restrict__ vals,
-                                                 unsigned* __restrict__ counters,
-                                                 cudaGraphConditionalHandle cond, int use_cond)
-{
-    __shared__ bool last;
-    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool out = false;
-    if (i < P.n) {
-        const float4 p = pf[i];
-        float x = p.x, y = p.y, z = p.z;
-        if (MODE == 0 || MODE == 1) {
-            const float4 v = M.vh[i], a = M.ab[i];
-            float vx = v.x, vy = v.y, vz = v.z, ax = a.x, ay = a.y, az = a.z;
-            if (MODE == 1) {
-                const float4 f = Fc[i];
-                const float im = M.vl[i].w;
-                const float nx = f.x * im, ny = f.y * im, nz = f.z * im;
-                vx += P.hf * (2.f * P.gf[0] + ax + nx);
-                vy += P.hf * (2.f * P.gf[1] + ay + ny);
-                vz += P.hf * (2.f * P.gf[2] + az + nz);
-                ax = nx;
-                ay = ny;
-                az = nz;
-            }
-            x += P.dtf * vx + P.half2dtf * (P.gf[0] + ax);
-            y += P.dtf * vy + P.half2dtf * (P.gf[1] + ay);
-            z += P.dtf * vz + P.half2dtf * (P.gf[2] + az);
-        }
-        keys[i] = cell_key(P, x, y, z);
-        vals[i] = i;
-        const unsigned a = __ldg(prev + i);
-        const unsigned cz = a / P.gxy, rem = a - cz * P.gxy;
-        const unsigned cy = rem / (unsigned)P.gx, cx = rem - cy * (unsigned)P.gx;
-        out = outside_cell(P, x, cx, P.gx) || outside_cell(P, y, cy, P.gy) || outside_cell(P, z, cz, P.gz);
-    }
-    if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31u) == 0) atomicOr(counters + CN_REBUILD, 1u);
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(counters + CN_DONE, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        const unsigned f = atomicOr(counters + CN_REBUILD, 0u);
-        if (use_cond) cudaGraphSetConditional(cond, f ? 1u : 0u);
-        counters[CN_DONE] = 0;
-    }
+    cz = (unsigned)((float)key * P.inv_gxy);
+    if (cz * P.gxy > key) --cz;
+    else if ((cz + 1u) * P.gxy <= key) ++cz;
+    const unsigned rem = key - cz * P.gxy;
+    cy = (unsigned)((float)rem * P.inv_gx);
+    if (cy * (unsigned)P.gx > rem) --cy;
+    else if ((cy + 1u) * (unsigned)P.gx <= rem) ++cy;
+    cx = rem - cy * (unsigned)P.gx;
 }
 
 // Velocity update of one particle (MODE 1 and 2): v += dt g + h (a_c + a_c'),
@@ -456,7 +408,7 @@ __device__ __forceinline__ void kick(const MixParams& P, float4& vh, float4& vl,
                                      float4& wl, float4& ab, float2& b2, const float4& f,
                                      const float4& t)
 {
-    const float im = vl.w, iI = wh.w;
+    const float im = vh.w, iI = wh.w;
     const float ax = f.x * im, ay = f.y * im, az = f.z * im;
     const float bx = t.x * iI, by = t.y * iI, bz = t.z * iI;
     dfl v;
@@ -486,49 +438,114 @@ __device__ __forceinline__ double drift(const MixParams& P, double x, float vhi,
     return __dadd_rn(x, __dadd_rn((double)inc.hi, (double)inc.lo));
 }
 
-// Applies the update of MODE and writes the contact view and the wall list;
-// after a re-binning (counters[CN_REBUILD] set) it also moves the state into
-// the new order (perm: new slot -> old slot).
+// k_mx_advance: one step of the state in place (MODE as above), the contact
+// view, then the skin test on the new position: every particle must stay
+// within half the skin of its position at the last list build (pref); one
+// that does not sets CN_REBUILD.  The last block to finish passes the flag to
+// the graph's conditional node (use_cond), one caller as the conditional
+// requires.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_mx_gather(MixParams P, Master S, Master D,
-                                                   const unsigned* __restrict__ perm,
-                                                   unsigned* __restrict__ counters,
-                                                   const float4* __restrict__ Fc,
-                                                   const float4* __restrict__ Mc,
-                                                   float4* __restrict__ pf,
-                                                   longlong2* __restrict__ qa,
-                                                   longlong2* __restrict__ qb,
-                                                   uint2* __restrict__ wall_list)
+__global__ void __launch_bounds__(256) k_mx_advance(MixParams P, Master M, const float4* __restrict__ Fc,
+                                                    const float4* __restrict__ Mc,
+                                                    const float4* __restrict__ pref,
+                                                    float4* __restrict__ pf, longlong2* __restrict__ qa,
+                                                    longlong2* __restrict__ qb,
+                                                    unsigned* __restrict__ counters,
+                                                    cudaGraphConditionalHandle cond, int use_cond)
 {
+    __shared__ bool last;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned wmask = 0;
+    bool out = false;
     if (i < P.n) {
-        const unsigned o = counters[CN_REBUILD] ? __ldg(perm + i) : i;
-        double x = __ldg(S.x + o), y = __ldg(S.y + o), z = __ldg(S.z + o);
-        const double r = __ldg(S.r + o);
-        float4 vh = __ldg(S.vh + o), vl = __ldg(S.vl + o), wh = __ldg(S.wh + o), wl = __ldg(S.wl + o);
-        float4 ab = __ldg(S.ab + o);
-        float2 b2 = __ldg(S.b2 + o);
-        if (MODE == 1) kick(P, vh, vl, wh, wl, ab, b2, __ldg(Fc + o), __ldg(Mc + o));
+        double x = M.x[i], y = M.y[i], z = M.z[i];
+        const double r = M.r[i];
         if (MODE == 0 || MODE == 1) {
+            float4 vh = M.vh[i], vl = M.vl[i], ab = M.ab[i];
+            if (MODE == 1) {
+                float4 wh = M.wh[i], wl = M.wl[i];
+                float2 b2 = M.b2[i];
+                kick(P, vh, vl, wh, wl, ab, b2, Fc[i], Mc[i]);
+                M.vh[i] = vh;
+                M.vl[i] = vl;
+                M.wh[i] = wh;
+                M.wl[i] = wl;
+                M.ab[i] = ab;
+                M.b2[i] = b2;
+            }
             x = drift(P, x, vh.x, vl.x, 0, ab.x);
             y = drift(P, y, vh.y, vl.y, 1, ab.y);
             z = drift(P, z, vh.z, vl.z, 2, ab.z);
+            M.x[i] = x;
+            M.y[i] = y;
+            M.z[i] = z;
         }
-        D.x[i] = x;
-        D.y[i] = y;
-        D.z[i] = z;
-        D.r[i] = r;
-        D.vh[i] = vh;
-        D.vl[i] = vl;
-        D.wh[i] = wh;
-        D.wl[i] = wl;
-        D.ab[i] = ab;
-        D.b2[i] = b2;
-        wmask = near_planes(P, write_view(P, i, x, y, z, r, pf, qa, qb));
+        const float4 v = write_view(P, i, x, y, z, r, pf, qa, qb);
+        const float4 r0 = pref[i];
+        const float dx = v.x - r0.x, dy = v.y - r0.y, dz = v.z - r0.z;
+        out = !(dx * dx + dy * dy + dz * dz < P.disp2);
     }
-    // the wall pass takes the particles near a plane, with their plane masks
-    warp_append(wmask != 0u, make_uint2(i, wmask), wall_list, counters + CN_WALLS);
+    if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31u) == 0) atomicOr(counters + CN_REBUILD, 1u);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(counters + CN_DONE, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        const unsigned f = atomicOr(counters + CN_REBUILD, 0u) ? 1u : 0u;
+        if (use_cond) cudaGraphSetConditional(cond, f);
+        counters[CN_DONE] = 0;
+    }
+}
+
+// Re-binning, 1: the cell key of every slot's current position.
+__global__ void __launch_bounds__(256) k_mx_keys(MixParams P, const float4* __restrict__ pf,
+                                                 unsigned* __restrict__ keys, unsigned* __restrict__ vals)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const float4 p = pf[i];
+    keys[i] = cell_key(P, p.x, p.y, p.z);
+    vals[i] = i;
+}
+
+// Re-binning, 2: the state in the new order (perm: new slot -> old slot) into D.
+__global__ void __launch_bounds__(256) k_mx_permute(MixParams P, Master S, Master D,
+                                                    const unsigned* __restrict__ perm)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const unsigned o = __ldg(perm + i);
+    D.x[i] = __ldg(S.x + o);
+    D.y[i] = __ldg(S.y + o);
+    D.z[i] = __ldg(S.z + o);
+    D.r[i] = __ldg(S.r + o);
+    D.vh[i] = __ldg(S.vh + o);
+    D.vl[i] = __ldg(S.vl + o);
+    D.wh[i] = __ldg(S.wh + o);
+    D.wl[i] = __ldg(S.wl + o);
+    D.ab[i] = __ldg(S.ab + o);
+    D.b2[i] = __ldg(S.b2 + o);
+}
+
+// Re-binning, 3: back into the state arrays, with the contact view.
+__global__ void __launch_bounds__(256) k_mx_copyback(MixParams P, Master S, Master D,
+                                                     float4* __restrict__ pf, longlong2* __restrict__ qa,
+                                                     longlong2* __restrict__ qb)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const double x = S.x[i], y = S.y[i], z = S.z[i], r = S.r[i];
+    D.x[i] = x;
+    D.y[i] = y;
+    D.z[i] = z;
+    D.r[i] = r;
+    D.vh[i] = S.vh[i];
+    D.vl[i] = S.vl[i];
+    D.wh[i] = S.wh[i];
+    D.wl[i] = S.wl[i];
+    D.ab[i] = S.ab[i];
+    D.b2[i] = S.b2[i];
+    write_view(P, i, x, y, z, r, pf, qa, qb);
 }
 
 // MODE 2: velocity only, in place (the last step of a call).
@@ -611,19 +628,16 @@ __device__ __forceinline__ double fp64_cdist(const Master& M, unsigned i, unsign
     return __dsub_rn(__dadd_rn(__ldg(M.r + i), __ldg(M.r + j)), __dsqrt_rn(d2));
 }
 
-// The candidate test of pair (i, j): FP32 prefilter, exact integer test,
-// FP64 guard band.  Returns 0 (no contact), 1 (contact) or 2 (contact decided
-// by the FP64 test).
+// The exact test of a candidate pair that passed the FP32 prefilter: the
+// integer separation against the radii, and the FP64 guard band.  Returns 0
+// (no contact), 1 (contact) or 2 (contact decided by the FP64 test).
 template <bool COUNT>
-__device__ __forceinline__ int touch(const MixParams& P, const Master& M, unsigned i, unsigned j,
-                                     const float4& pi, const longlong2& qai, const longlong2& qbi,
-                                     const float4* __restrict__ pf, const longlong2* __restrict__ qa,
-                                     const longlong2* __restrict__ qb, unsigned* __restrict__ counters)
+__device__ __forceinline__ int exact_touch(const MixParams& P, const Master& M, unsigned i, unsigned j,
+                                           const longlong2& qai, const longlong2& qbi,
+                                           const longlong2* __restrict__ qa,
+                                           const longlong2* __restrict__ qb,
+                                           unsigned* __restrict__ counters)
 {
-    const float4 pj = __ldg(pf + j);
-    const float dxf = pj.x - pi.x, dyf = pj.y - pi.y, dzf = pj.z - pi.z;
-    const float Rt = pi.w + pj.w + P.tol;
-    if (dxf * dxf + dyf * dyf + dzf * dzf >= Rt * Rt) return 0;
     const longlong2 qaj = __ldg(qa + j), qbj = __ldg(qb + j);
     const long long ddx = qaj.x - qai.x, ddy = qaj.y - qai.y, ddz = qbj.x - qbi.x;
     const long long Rq = qbi.y + qbj.y;
@@ -633,6 +647,20 @@ __device__ __forceinline__ int touch(const MixParams& P, const Master& M, unsign
     if (N < -band) return 0;
     if (COUNT) atomicAdd(counters + CN_DECISIONS, 1u);
     return fp64_cdist(M, i, j) > 0 ? 2 : 0;
+}
+
+// The candidate test of pair (i, j): FP32 prefilter, then the exact test.
+template <bool COUNT>
+__device__ __forceinline__ int touch(const MixParams& P, const Master& M, unsigned i, unsigned j,
+                                     const float4& pi, const longlong2& qai, const longlong2& qbi,
+                                     const float4* __restrict__ pf, const longlong2* __restrict__ qa,
+                                     const longlong2* __restrict__ qb, unsigned* __restrict__ counters)
+{
+    const float4 pj = __ldg(pf + j);
+    const float dxf = pj.x - pi.x, dyf = pj.y - pi.y, dzf = pj.z - pi.z;
+    const float Rt = pi.w + P.tol + pj.w;
+    if (fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf)) >= Rt * Rt) return 0;
+    return exact_touch<COUNT>(P, M, i, j, qai, qbi, qa, qb, counters);
 }
 
 // Visits the contacts of slot i in the reference's order (neighbour rows z
@@ -672,71 +700,89 @@ __device__ __forceinline__ void for_each_contact(const MixParams& P, const Maste
     }
 }
 
-constexpr unsigned kIncomplete = 0x80000000u;   // ccount flag: the list is not complete
+constexpr unsigned kIncomplete = 0x80000000u;   // vcount flag: the list is not complete
 
-// Candidate search, one thread per particle: the nine neighbour rows' slot
-// ranges are staged in shared memory and visited as one flattened loop (rows
-// z then y, slots ascending: the reference's order), so a warp runs as many
-// iterations as its busiest lane has candidates.  Writes the contact list
-// (kListCap entries; more marks it incomplete and the force pass searches
-// again), zero contact force for the particles without contacts, and the
-// force list (the particles with contacts).
-template <bool RECORD>
-__global__ void __launch_bounds__(256) k_mx_search(MixParams P, Master M, const float4* __restrict__ pf,
-                                                   const longlong2* __restrict__ qa,
-                                                   const longlong2* __restrict__ qb,
-                                                   const unsigned* __restrict__ keys,
-                                                   const unsigned* __restrict__ lb,
-                                                   unsigned* __restrict__ ccount,
-                                                   unsigned* __restrict__ clist,
-                                                   unsigned* __restrict__ flist,
-                                                   float4* __restrict__ Fc, float4* __restrict__ Mc,
-                                                   unsigned* __restrict__ counters,
-                                                   unsigned* __restrict__ rec_count,
-                                                   unsigned* __restrict__ rec_pairs, unsigned rec_cap)
+// Verlet list build (steps that re-bin the cells), one thread per particle:
+// the nine neighbour rows' slot ranges, trimmed to the cells within reach,
+// are staged in shared memory and visited as one flattened loop (rows z then
+// y, slots ascending: the reference's order); every j with
+// |pj - pi| < ri + rj + vcut (FP32) is listed.  More than kVerletCap marks the
+// list incomplete (the contact pass then searches the cells).  Also records
+// the build positions for the skin test, each particle's planes in reach
+// (within r + skin), zero contact force, and the list of the particles with
+// neighbours or planes in reach -- the only ones the contact pass visits until
+// the next build.
+__global__ void __launch_bounds__(256) k_mx_build(MixParams P, const float4* __restrict__ pf,
+                                                  const unsigned* __restrict__ keys,
+                                                  const unsigned* __restrict__ lb,
+                                                  unsigned* __restrict__ vcount,
+                                                  unsigned* __restrict__ vlist,
+                                                  float4* __restrict__ pref,
+                                                  unsigned short* __restrict__ wmask,
+                                                  unsigned* __restrict__ hlist,
+                                                  float4* __restrict__ Fc, float4* __restrict__ Mc,
+                                                  unsigned* __restrict__ counters)
 {
     __shared__ uint2 rows[9][256];
     const unsigned tid = threadIdx.x;
     const unsigned i = blockIdx.x * blockDim.x + tid;
-    const bool live = i < P.n;
-    unsigned nc = 0;
-    if (live) {
+    bool heavy = false;
+    if (i < P.n) {
         const float4 pi = __ldg(pf + i);
-        const longlong2 qai = __ldg(qa + i), qbi = __ldg(qb + i);
+        pref[i] = pi;
+        Fc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        Mc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        const unsigned wm = near_planes(P, pi, P.wall_tol + P.vcut);
+        wmask[i] = (unsigned short)wm;
         const unsigned key = __ldg(keys + i);
+        // Neighbour cells out of reach are skipped: particles assigned to the
+        // cell below on an axis lie at most half a skin above its top face, so
+        // none of them is within ri + r_max + vcut of i when i is farther than
+        // that above it; likewise above.
+        unsigned cx, cy, cz;
+        decode_key(P, key, cx, cy, cz);
+        const float reach = pi.w + P.rmaxf + P.vcut + P.half_skin;
+        const float bx = (float)((int)cx - 1) * P.csf, by = (float)((int)cy - 1) * P.csf,
+                    bz = (float)((int)cz - 1) * P.csf;
+        const bool lox = pi.x - bx < reach, hix = bx + P.csf - pi.x < reach;
+        const bool loy = pi.y - by < reach, hiy = by + P.csf - pi.y < reach;
+        const bool loz = pi.z - bz < reach, hiz = bz + P.csf - pi.z < reach;
+        const unsigned x0 = key - (lox ? 1u : 0u), x1 = key + (hix ? 2u : 1u);
+        unsigned left = 0;   // candidates over all rows
 #pragma unroll
         for (int r = 0; r < 9; ++r) {
-            const unsigned c = key - 1u + (unsigned)(r % 3 - 1) * (unsigned)P.gx + (unsigned)(r / 3 - 1) * P.gxy;
-            rows[r][tid] = make_uint2(__ldg(lb + c), __ldg(lb + c + 3));
+            const int dy = r % 3 - 1, dz = r / 3 - 1;
+            const bool use = (dy < 0 ? loy : dy > 0 ? hiy : true) && (dz < 0 ? loz : dz > 0 ? hiz : true);
+            const unsigned off = (unsigned)dy * (unsigned)P.gx + (unsigned)dz * P.gxy;
+            // cell indices wrap in 32-bit unsigned arithmetic before indexing
+            const unsigned c0 = x0 + off, c1 = x1 + off;
+            const uint2 b = use ? make_uint2(__ldg(lb + c0), __ldg(lb + c1)) : make_uint2(0u, 0u);
+            rows[r][tid] = b;
+            left += b.y - b.x;
         }
         const unsigned n = P.n;
-        unsigned r = 0;
+        const float rt0 = pi.w + P.vcut;
+        unsigned nv = 0, r = 0;
         uint2 b = rows[0][tid];
         unsigned j = b.x;
-        for (;;) {
-            while (j >= b.y && ++r < 9) {
-                b = rows[r][tid];
+        for (; left; --left, ++j) {
+            if (j == b.y) {   // next non-empty row (one exists while candidates are left)
+                do {
+                    b = rows[++r][tid];
+                } while (b.x == b.y);
                 j = b.x;
             }
-            if (r >= 9) break;
-            if (j != i) {
-                const int t = touch<true>(P, M, i, j, pi, qai, qbi, pf, qa, qb, counters);
-                if (t) {
-                    if (nc < kListCap) clist[(size_t)nc * n + i] = j | (t == 2 ? kGuardBit : 0u);
-                    if (RECORD && nc < rec_cap) rec_pairs[(size_t)i * rec_cap + nc] = j;
-                    ++nc;
-                }
-            }
-            ++j;
+            const float4 pj = __ldg(pf + j);
+            const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+            const float Rt = rt0 + pj.w;
+            if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) >= Rt * Rt || j == i) continue;
+            if (nv < kVerletCap) vlist[(size_t)nv * n + i] = j;
+            ++nv;
         }
-        ccount[i] = nc | (nc > kListCap ? kIncomplete : 0u);
-        if (RECORD) rec_count[i] = nc;
-        if (!nc) {
-            Fc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-            Mc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
+        vcount[i] = nv > kVerletCap ? (kVerletCap | kIncomplete) : nv;
+        heavy = nv > 0 || wm != 0u;
     }
-    warp_append(live && nc > 0, i, flist, counters + CN_FORCE);
+    warp_append(heavy, i, hlist, counters + CN_HEAVY);
 }
 
 // Per-particle contact state carried across the pairs of one particle (the
@@ -751,7 +797,7 @@ struct Own {
     longlong2 qa, qb;
     float4 vh, vl;
     f3 w;
-    float r, m;
+    float r, im;   // radius, 1/m
 };
 
 // The force of one contact (i, j).  getConstant TCM = 1 (impl:238-246) and
@@ -783,8 +829,8 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     const f3 u = fk((float)ddx * inv, (float)ddy * inv, (float)ddz * inv);
     const float4 vj4 = __ldg(M.vh + j), vjl = __ldg(M.vl + j), wj4 = __ldg(M.wh + j);
     const f3 wj = fk(wj4.x, wj4.y, wj4.z);
-    const float jr = __ldg(pf + j).w, jm = vj4.w;
-    const float ir = I.r, im = I.m;
+    const float jr = __ldg(pf + j).w, jim = vj4.w;
+    const float ir = I.r;
     // vj - vi formed exactly from the double-float velocities
     float dvs[3], dvt[3];
     df_diff(vj4.x, I.vh.x, __fsub_rn(vjl.x, I.vl.x), dvs[0], dvt[0]);
@@ -820,7 +866,7 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
         ee = fdot(ev, ev);
     }
     // getConstant, TCM = 1 (impl:238-246)
-    const float Meq = (im * jm) / (im + jm);
+    const float Meq = 1.0f / (I.im + jim);   // m_i m_j / (m_i + m_j)
     const float Req = (ir * jr) / (ir + jr);
     const float kn = P.c43Eeq * sqrtf(Req);
     const float vn = sqrtf((4.0f * Meq * kn) / P.one_b2);
@@ -869,98 +915,101 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     A.sumM = A.sumM + A.Mm;
 }
 
-// Forces of the particles with contacts, over each one's list in search
-// order; a particle whose list is incomplete is searched again (same order).
-__global__ void __launch_bounds__(256) k_mx_force(MixParams P, Master M, const float4* __restrict__ pf,
-                                                  const longlong2* __restrict__ qa,
-                                                  const longlong2* __restrict__ qb,
-                                                  const unsigned* __restrict__ keys,
-                                                  const unsigned* __restrict__ lb,
-                                                  const unsigned* __restrict__ ccount,
-                                                  const unsigned* __restrict__ clist,
-                                                  const unsigned* __restrict__ flist,
-                                                  const double* __restrict__ mass0,
-                                                  float4* __restrict__ Fc, float4* __restrict__ Mc,
-                                                  unsigned* __restrict__ counters)
+// Contact forces of the particles on the heavy list (the others keep the
+// zero force of the last build): the particle pairs of the Verlet list (or,
+// for an incomplete list, of the neighbour cells) in search order -- FP32
+// prefilter, exact integer test, FP64 guard band, FP32 Hertz-Mindlin -- then
+// plane_contact_force_kernel<1> (impl:572-621) for the planes in reach, in
+// FP64, in plane order (the others are out of reach and add exactly zero).
+// Block 0 clears CN_REBUILD for the next step's skin test.
+template <bool RECORD>
+__global__ void __launch_bounds__(256) k_mx_contact(MixParams P, Master M, const float4* __restrict__ pf,
+                                                    const longlong2* __restrict__ qa,
+                                                    const longlong2* __restrict__ qb,
+                                                    const unsigned* __restrict__ keys,
+                                                    const unsigned* __restrict__ lb,
+                                                    const unsigned* __restrict__ vcount,
+                                                    const unsigned* __restrict__ vlist,
+                                                    const unsigned* __restrict__ hlist,
+                                                    const unsigned short* __restrict__ wmask,
+                                                    const xd_plane_info* __restrict__ planes,
+                                                    const xd_contact_property* __restrict__ cps,
+                                                    const double* __restrict__ mass0,
+                                                    float4* __restrict__ Fc, float4* __restrict__ Mc,
+                                                    unsigned* __restrict__ counters,
+                                                    unsigned* __restrict__ rec_count,
+                                                    unsigned* __restrict__ rec_pairs, unsigned rec_cap)
 {
-    const unsigned total = counters[CN_FORCE];
+    if (blockIdx.x == 0 && threadIdx.x == 0) counters[CN_REBUILD] = 0;
+    const unsigned total = counters[CN_HEAVY];
+    const unsigned n = P.n;
     for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
         Own I;
-        I.i = __ldg(flist + t);
+        I.i = __ldg(hlist + t);
         const unsigned i = I.i;
-        const unsigned cc = __ldg(ccount + i);
+        const float4 pi = __ldg(pf + i);
         I.qa = __ldg(qa + i);
         I.qb = __ldg(qb + i);
         I.vh = __ldg(M.vh + i);
         I.vl = __ldg(M.vl + i);
         const float4 w4 = __ldg(M.wh + i);
         I.w = fk(w4.x, w4.y, w4.z);
-        I.r = __ldg(pf + i).w;
-        I.m = I.vh.w;
+        I.r = pi.w;
+        I.im = I.vh.w;
         PairAcc A;
         A.Ft = fk(0.f, 0.f, 0.f);
         A.Mm = fk(0.f, 0.f, 0.f);
         A.sumF = fk(0.f, 0.f, 0.f);
         A.sumM = fk(0.f, 0.f, 0.f);
-        if (!(cc & kIncomplete)) {
-            for (unsigned k = 0; k < cc; ++k) {
-                const unsigned e = __ldg(clist + (size_t)k * P.n + i);
-                contact_force(P, M, I, e & ~kGuardBit, (e & kGuardBit) != 0u, mass0, pf, qa, qb, counters, A);
+        unsigned nc = 0;
+        auto add = [&](unsigned j, bool guard) {
+            contact_force(P, M, I, j, guard, mass0, pf, qa, qb, counters, A);
+            if (RECORD && nc < rec_cap) rec_pairs[(size_t)i * rec_cap + nc] = j;
+            ++nc;
+        };
+        const unsigned vc = __ldg(vcount + i);
+        if (!(vc & kIncomplete)) {
+            for (unsigned k = 0; k < vc; ++k) {
+                const unsigned j = __ldg(vlist + (size_t)k * n + i);
+                const int c = touch<true>(P, M, i, j, pi, I.qa, I.qb, pf, qa, qb, counters);
+                if (c) add(j, c == 2);
             }
         } else {
-            for_each_contact<false>(P, M, i, __ldg(pf + i), I.qa, I.qb, __ldg(keys + i), pf, qa, qb, lb,
-                                    counters, [&](unsigned j, bool guard) {
-                                        contact_force(P, M, I, j, guard, mass0, pf, qa, qb, counters, A);
-                                    });
+            for_each_contact<true>(P, M, i, pi, I.qa, I.qb, __ldg(keys + i), pf, qa, qb, lb, counters, add);
         }
-        Fc[i] = make_float4(A.sumF.x, A.sumF.y, A.sumF.z, 0.f);
-        Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
-    }
-}
-
-// plane_contact_force_kernel<1> (impl:572-621) for the listed particles, the
-// planes of each one's mask in order (the others are out of reach and add
-// exactly zero), in FP64; adds to the FP32 contact force.
-__global__ void __launch_bounds__(128) k_mx_walls(MixParams P, Master M,
-                                                  const xd_plane_info* __restrict__ planes,
-                                                  const xd_contact_property* __restrict__ cps,
-                                                  const uint2* __restrict__ wall_list,
-                                                  const unsigned* __restrict__ counters,
-                                                  const double* __restrict__ mass0,
-                                                  float4* __restrict__ Fc)
-{
-    const unsigned count = counters[CN_WALLS];
-    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
-        const uint2 wl = wall_list[k];
-        const unsigned i = wl.x;
-        const float4 vh = M.vh[i], vl = M.vl[i], wh = M.wh[i], wlo = M.wl[i];
-        const double m = mass0[__float_as_uint(wlo.w)];
-        const d3 ip = mk(M.x[i], M.y[i], M.z[i]);
-        const double r = M.r[i];
-        const d3 iv = mk(df_to_d(vh.x, vl.x), df_to_d(vh.y, vl.y), df_to_d(vh.z, vl.z));
-        const d3 iw = mk(df_to_d(wh.x, wlo.x), df_to_d(wh.y, wlo.y), df_to_d(wh.z, wlo.z));
-        d3 f = mk(0, 0, 0);
-        for (unsigned mask = wl.y; mask; mask &= mask - 1u) {
-            const int w = __ffs(mask) - 1;
-            PlaneD pe = load_plane(planes + w);
-            d3 Fn = mk(0, 0, 0), Ft = mk(0, 0, 0), Mo = mk(0, 0, 0);
-            d3 dp = ip - pe.xw;
-            d3 unit = mk(0, 0, 0);
-            d3 wp = mk(dot(dp, pe.u1), dot(dp, pe.u2), dot(dp, pe.uw));
-            double cdist = plane_detection(pe, ip, wp, unit, r);
-            if (cdist > 0) {
-                PairConst pc = load_pair_const(cps + w);
-                d3 dv = -(iv + cross(iw, r * unit));
-                xd::Fc c = get_constant(pc, r, 0.0, m, 0.0);
-                dhs(c, 0, 0, 0, 0, 0, 0, pc.coh, cdist, dv, unit, P.dt, Ft, Fn, Mo);
+        float4 F = make_float4(A.sumF.x, A.sumF.y, A.sumF.z, 0.f);
+        const unsigned wm = __ldg(wmask + i);
+        if (wm) {
+            const float4 wl = __ldg(M.wl + i), wh = w4;
+            const double m = __ldg(mass0 + __float_as_uint(wl.w));
+            const d3 ip = mk(__ldg(M.x + i), __ldg(M.y + i), __ldg(M.z + i));
+            const double r = __ldg(M.r + i);
+            const d3 iv = mk(df_to_d(I.vh.x, I.vl.x), df_to_d(I.vh.y, I.vl.y), df_to_d(I.vh.z, I.vl.z));
+            const d3 iw = mk(df_to_d(wh.x, wl.x), df_to_d(wh.y, wl.y), df_to_d(wh.z, wl.z));
+            d3 f = mk(0, 0, 0);
+            for (unsigned mask = wm; mask; mask &= mask - 1u) {
+                const int w = __ffs(mask) - 1;
+                PlaneD pe = load_plane(planes + w);
+                d3 Fn = mk(0, 0, 0), Ft = mk(0, 0, 0), Mo = mk(0, 0, 0);
+                d3 dp = ip - pe.xw;
+                d3 unit = mk(0, 0, 0);
+                d3 wp = mk(dot(dp, pe.u1), dot(dp, pe.u2), dot(dp, pe.uw));
+                double cdist = plane_detection(pe, ip, wp, unit, r);
+                if (cdist > 0) {
+                    PairConst pc = load_pair_const(cps + w);
+                    d3 dv = -(iv + cross(iw, r * unit));
+                    xd::Fc c = get_constant(pc, r, 0.0, m, 0.0);
+                    dhs(c, 0, 0, 0, 0, 0, 0, pc.coh, cdist, dv, unit, P.dt, Ft, Fn, Mo);
+                }
+                f += Fn + Ft;
             }
-            f += Fn + Ft;
+            F.x += (float)f.x;
+            F.y += (float)f.y;
+            F.z += (float)f.z;
         }
-        float4 o = Fc[i];
-        o.x += (float)f.x;
-        o.y += (float)f.y;
-        o.z += (float)f.z;
-        Fc[i] = o;
+        Fc[i] = F;
+        Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
+        if (RECORD) rec_count[i] = nc;
     }
 }
 
@@ -995,8 +1044,8 @@ __global__ void __launch_bounds__(256) k_mx_load(MixParams P, Master M, const do
         wh[a] = __double2float_rn(w);
         wl[a] = __double2float_rn(w - (double)wh[a]);
     }
-    M.vh[i] = make_float4(h[0], h[1], h[2], (float)m);
-    M.vl[i] = make_float4(l[0], l[1], l[2], (float)(1.0 / m));
+    M.vh[i] = make_float4(h[0], h[1], h[2], (float)(1.0 / m));
+    M.vl[i] = make_float4(l[0], l[1], l[2], 0.f);
     M.wh[i] = make_float4(wh[0], wh[1], wh[2], (float)(1.0 / I));
     M.wl[i] = make_float4(wl[0], wl[1], wl[2], __uint_as_float(i));
     M.ab[i] = make_float4((float)(acc[i3 + 0] - P.g[0]), (float)(acc[i3 + 1] - P.g[1]),
@@ -1136,11 +1185,19 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     P.csf = (float)s->cs;
     P.inv_csf = (float)(1.0 / s->cs);
     P.half_skin = (float)(0.5 * skin);
+    P.rmaxf = (float)rmax;
+    P.inv_gx = 1.0f / (float)g[0];
+    P.inv_gxy = 1.0f / (float)((double)g[0] * g[1]);
     P.dtf = (float)dt;
     P.hf = (float)(0.5 * dt);
     P.half2dtf = (float)half2dt;
     P.dt_df = df_split(dt);
     P.tol = (float)(4e-6 + extent * 0x1p-20);
+    // The Verlet list holds the pairs within ri + rj + skin + tol at its build;
+    // re-binning (and a new list) comes before any particle has moved half the
+    // skin less the FP32 position error, so no unlisted pair can touch.
+    P.vcut = (float)skin + P.tol;
+    P.disp2 = (float)((0.5 * skin - P.tol) * (0.5 * skin - P.tol));
     P.wall_tol = (float)(1e-5 + extent * 0x1p-20);
     const xd_contact_property& cp = d.cp_pp;
     double Eeq = (cp.Ei * cp.Ej) / (cp.Ei * (1 - cp.prj * cp.prj) + cp.Ej * (1 - cp.pri * cp.pri));
@@ -1184,9 +1241,11 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     A(alloc(s, &s->qb, n));
     A(alloc(s, &s->Fc, n));
     A(alloc(s, &s->Mc, n));
-    A(alloc(s, &s->ccount, n));
-    A(alloc(s, &s->clist, n * kListCap));
-    A(alloc(s, &s->flist, n));
+    A(alloc(s, &s->hlist, n));
+    A(alloc(s, &s->wmask, n));
+    A(alloc(s, &s->vcount, n));
+    A(alloc(s, &s->vlist, n * kVerletCap));
+    A(alloc(s, &s->pref, n));
     A(alloc(s, &s->keys, n));
     A(alloc(s, &s->vals, n));
     A(alloc(s, &s->prev_keys, n));
@@ -1198,7 +1257,6 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     s->sort_scratch = scr;
     A(alloc(s, &s->planes, s->nplanes));
     A(alloc(s, &s->cps, s->nplanes));
-    A(alloc(s, &s->wall_list, n));
     A(alloc(s, &s->counters, kCounters));
     s->passes = (key_bits_for(s->ncell) + 7) / 8;
     if (st == XD_OK) A(cuda_status(cudaMemset(s->counters, 0, sizeof(unsigned) * kCounters), "mixed counters"));
@@ -1280,7 +1338,9 @@ int mixed_upload(MixedScene* s, const double* pos, const double* vel, const doub
     cp(dI, inertia, n);
     if (st != XD_OK) return st;
     s->cur = 0;
-    s->cells_clean = false;   // the state is in upload order again: next resort is a full sort
+    s->cells_clean = false;   // the state is in upload order again: the next step re-bins
+    st = cuda_status(cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * CN_DECISIONS, q), "mixed upload");
+    if (st != XD_OK) return st;
     k_mx_load<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[0], dpos, dvel, dacc, dom, dal, dm, dI,
                                                 s->mass0, s->pf, s->qa, s->qb);
     st = launch_status("mixed upload");
@@ -1317,24 +1377,33 @@ int mixed_download(MixedScene* s, double* pos, double* vel, double* acc, double*
     return st;
 }
 
-// Re-binning: stable radix sort of the keys, then the cell lower bounds.
+// Re-binning: cell keys of the current positions, stable radix sort, the
+// state permuted into the new order, the cell lower bounds, then the Verlet
+// lists, plane masks and heavy list.
 static int rebuild(MixedScene* s, cudaStream_t q)
 {
     const unsigned n = s->n;
-    unsigned *sk = nullptr, *sv = nullptr;
-    int st = radix_sort_pairs(s->keys, s->vals, n, key_bits_for(s->ncell), s->sort_scratch, q, &sk, &sv);
+    int st = cuda_status(cudaMemsetAsync(s->counters + CN_GAPS, 0, 2 * sizeof(unsigned), q), "mixed re-binning");
     if (st != XD_OK) return st;
-    // the output buffers depend only on the pass count: fixed for the scene
-    s->perm = sv;
-    s->sorted_keys = sk;
+    k_mx_keys<<<blocks(n, 256), 256, 0, q>>>(s->P, s->pf, s->keys, s->vals);
+    st = launch_status("mixed keys");
+    if (st != XD_OK) return st;
+    unsigned *sk = nullptr, *sv = nullptr;
+    st = radix_sort_pairs(s->keys, s->vals, n, key_bits_for(s->ncell), s->sort_scratch, q, &sk, &sv);
+    if (st != XD_OK) return st;
+    k_mx_permute<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[0], s->m[1], sv);
+    k_mx_copyback<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[1], s->m[0], s->pf, s->qa, s->qb);
     k_lb_fill<<<blocks(n + 1, 256), 256, 0, q>>>(sk, n, s->ncell, s->lb, s->prev_keys, s->gaps, s->counters);
     k_lb_long<<<152 * 4, 256, 0, q>>>(s->gaps, s->counters, s->lb);
+    k_mx_build<<<blocks(n, 256), 256, 0, q>>>(s->P, s->pf, s->prev_keys, s->lb, s->vcount, s->vlist, s->pref,
+                                              s->wmask, s->hlist, s->Fc, s->Mc, s->counters);
     return launch_status("mixed re-binning");
 }
 
-// Inside a stream capture: a conditional node that runs the re-binning when
-// the handle is set (by k_mx_keys), with the capture continuing after it.
-static int capture_conditional_rebuild(MixedScene* s, cudaStream_t q, cudaGraphConditionalHandle h)
+// Inside a stream capture: a conditional node that runs body(s, stream) when
+// the handle is set (by k_mx_keys); the capture continues after it.
+template <typename Body>
+static int capture_conditional(MixedScene* s, cudaStream_t q, cudaGraphConditionalHandle h, Body body)
 {
     cudaStreamCaptureStatus cst;
     cudaGraph_t g = nullptr;
@@ -1355,9 +1424,9 @@ static int capture_conditional_rebuild(MixedScene* s, cudaStream_t q, cudaGraphC
     st = cuda_status(cudaStreamBeginCaptureToGraph(bs, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                                    cudaStreamCaptureModeThreadLocal), "mixed conditional capture");
     if (st == XD_OK) {
-        int r = rebuild(s, bs);
-        cudaGraph_t body = nullptr;
-        st = cuda_status(cudaStreamEndCapture(bs, &body), "mixed conditional capture");
+        int r = body(s, bs);
+        cudaGraph_t body_graph = nullptr;
+        st = cuda_status(cudaStreamEndCapture(bs, &body_graph), "mixed conditional capture");
         if (r != XD_OK) st = r;
     }
     cudaStreamDestroy(bs);
@@ -1366,32 +1435,28 @@ static int capture_conditional_rebuild(MixedScene* s, cudaStream_t q, cudaGraphC
                        "mixed capture dependencies");
 }
 
-// One step: keys and the skin test, re-binning when needed, the gather with
-// the update of MODE, contacts and walls.  cond: the conditional handle when
-// capturing into a graph (nullptr for direct launches).
+// One step: the state advanced in place with the skin test, re-binning when
+// a particle has left its skin (or the cells are not set up), then the
+// contact forces.  cond: the conditional handle when capturing into a graph
+// (nullptr for direct launches, where the host reads the flag).
 template <int MODE>
 static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool record, unsigned rec_cap,
                      const cudaGraphConditionalHandle* cond)
 {
     const unsigned n = s->n;
-    int st = cuda_status(cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * kPerStepCounters, q),
-                         "mixed counters");
-    if (st != XD_OK) return st;
-    Master& Mcur = s->m[s->cur];
+    const Master& M = s->m[0];
     ph.begin(0, q);
-    k_mx_keys<MODE><<<blocks(n, 256), 256, 0, q>>>(s->P, Mcur, s->pf, s->Fc, s->prev_keys, s->keys, s->vals,
-                                                   s->counters, cond ? *cond : 0, cond ? 1 : 0);
-    st = launch_status("mixed keys");
+    k_mx_advance<MODE><<<blocks(n, 256), 256, 0, q>>>(s->P, M, s->Fc, s->Mc, s->pref, s->pf, s->qa, s->qb,
+                                                      s->counters, cond ? *cond : 0, cond ? 1 : 0);
+    int st = launch_status("mixed advance");
     ph.end(0, q);
     if (st != XD_OK) return st;
     ph.begin(2, q);
     if (cond) {
-        st = capture_conditional_rebuild(s, q, *cond);
+        st = capture_conditional(s, q, *cond, rebuild);
     } else {
         bool need = !s->cells_clean;
-        if (need) {
-            st = cuda_status(cudaMemsetAsync(s->counters + CN_REBUILD, 1, 1, q), "mixed re-binning flag");
-        } else {
+        if (!need) {
             unsigned flag = 0;
             st = cuda_status(cudaMemcpyAsync(&flag, s->counters + CN_REBUILD, sizeof(unsigned),
                                              cudaMemcpyDeviceToHost, q), "mixed re-binning flag");
@@ -1403,45 +1468,28 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
     ph.end(2, q);
     if (st != XD_OK) return st;
     s->cells_clean = true;
-    ph.begin(6, q);
-    const int nxt = 1 - s->cur;
-    k_mx_gather<MODE><<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->m[nxt], s->perm, s->counters,
-                                                     s->Fc, s->Mc, s->pf, s->qa, s->qb, s->wall_list);
-    st = launch_status("mixed gather");
-    s->cur = nxt;
-    ph.end(6, q);
-    if (st != XD_OK) return st;
     ph.begin(3, q);
-    // prev_keys holds the assigned keys: the search reads each particle's cell from it
-    const Master& M = s->m[s->cur];
-    if (record)
-        k_mx_search<true><<<blocks(n, 256), 256, 0, q>>>(
-            s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->ccount, s->clist, s->flist, s->Fc,
-            s->Mc, s->counters, s->rec_count, s->rec_pairs, rec_cap);
-    else
-        k_mx_search<false><<<blocks(n, 256), 256, 0, q>>>(
-            s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->ccount, s->clist, s->flist, s->Fc,
-            s->Mc, s->counters, nullptr, nullptr, 0);
-    k_mx_force<<<min(blocks(n, 256), 152u * 8u), 256, 0, q>>>(s->P, M, s->pf, s->qa, s->qb,
-                                                              s->prev_keys, s->lb, s->ccount, s->clist,
-                                                              s->flist, s->mass0, s->Fc, s->Mc,
-                                                              s->counters);
+    const unsigned grid = min(blocks(n, 256), 152u * 8u);
+    if (record) {
+        st = cuda_status(cudaMemsetAsync(s->rec_count, 0, sizeof(unsigned) * n, q), "mixed pair count");
+        if (st != XD_OK) return st;
+        k_mx_contact<true><<<grid, 256, 0, q>>>(s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->vcount,
+                                                s->vlist, s->hlist, s->wmask, s->planes, s->cps, s->mass0,
+                                                s->Fc, s->Mc, s->counters, s->rec_count, s->rec_pairs, rec_cap);
+    } else {
+        k_mx_contact<false><<<grid, 256, 0, q>>>(s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->vcount,
+                                                 s->vlist, s->hlist, s->wmask, s->planes, s->cps, s->mass0,
+                                                 s->Fc, s->Mc, s->counters, nullptr, nullptr, 0);
+    }
     st = launch_status("mixed contact");
     ph.end(3, q);
-    if (st != XD_OK || !s->nplanes) return st;
-    ph.begin(4, q);
-    k_mx_walls<<<152 * 4, 128, 0, q>>>(s->P, M, s->planes, s->cps, s->wall_list, s->counters, s->mass0,
-                                       s->Fc);
-    st = launch_status("mixed walls");
-    ph.end(4, q);
     return st;
 }
 
-// Captures two middle steps into a graph for the current buffer parity (the
-// pair of steps leaves the parity unchanged).  Needs cells_clean.
+// Captures two middle steps into one graph, each with its conditional
+// re-binning node.  Needs cells_clean.
 static int capture_pair(MixedScene* s)
 {
-    const int parity = s->cur;
     cudaStream_t cs = nullptr;
     cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_status(e, "mixed graph stream");
@@ -1462,8 +1510,7 @@ static int capture_pair(MixedScene* s)
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(cs, &g);
     if (st == XD_OK) st = cuda_status(e, "mixed graph capture");
-    s->cur = parity;   // capture only recorded the launches
-    if (st == XD_OK) st = cuda_status(cudaGraphInstantiate(&s->graph[parity], g, 0), "mixed graph instantiate");
+    if (st == XD_OK) st = cuda_status(cudaGraphInstantiate(&s->graph[0], g, 0), "mixed graph instantiate");
     if (g) cudaGraphDestroy(g);
     cudaStreamDestroy(cs);
     return st;
@@ -1474,25 +1521,25 @@ int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
     if (nsteps == 0 || s->n == 0) return XD_OK;
     if (!s->ready) return set_error(XD_ERR_STATE, "mixed mode: no state uploaded");
     const bool graphs = s->use_graphs && ph.fn == nullptr;
-    // step 1: the position update (in the gather) from the state's (v, a)
+    // step 1: the position update from the state's (v, a)
     int st = step_once<0>(s, q, ph, false, 0, nullptr);
     if (st != XD_OK) return st;
     unsigned t = 1;
     // pairs of middle steps as one graph launch
     while (graphs && nsteps - t >= 2) {
-        if (!s->graph[s->cur]) {
+        if (!s->graph[0]) {
             st = capture_pair(s);
             if (st != XD_OK) return st;
         }
-        st = cuda_status(cudaGraphLaunch(s->graph[s->cur], q), "mixed graph launch");
+        st = cuda_status(cudaGraphLaunch(s->graph[0], q), "mixed graph launch");
         if (st != XD_OK) return st;
-        t += 2;   // two gathers: the buffer parity is unchanged
+        t += 2;
     }
     for (; t < nsteps && st == XD_OK; ++t) st = step_once<1>(s, q, ph, false, 0, nullptr);
     if (st != XD_OK) return st;
     // the last velocity update
     ph.begin(0, q);
-    k_mx_finish<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc);
+    k_mx_finish<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[0], s->Fc, s->Mc);
     st = launch_status("mixed finish");
     ph.end(0, q);
     return st;
@@ -1501,9 +1548,9 @@ int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
 unsigned long long mixed_launches(MixedScene* s, unsigned nsteps)
 {
     if (!s || nsteps == 0 || s->n == 0) return 0;
-    // per step: keys + gather + search + force (+ walls); + the last velocity
-    // update; a step that re-bins adds mixed_rebuild_launches()
-    const unsigned long long per = 4 + (s->nplanes ? 1 : 0);
+    // per step: advance + contact; + the last velocity update; a step that
+    // re-bins adds mixed_rebuild_launches()
+    const unsigned long long per = 2;
     unsigned long long total = per * nsteps + 1;
     if (!s->cells_clean) total += mixed_rebuild_launches(s);   // the first step re-bins
     return total;
@@ -1511,8 +1558,9 @@ unsigned long long mixed_launches(MixedScene* s, unsigned nsteps)
 
 unsigned long long mixed_rebuild_launches(MixedScene* s)
 {
-    if (!s || s->n <= 1) return s && s->n ? 2 : 0;
-    return 5ull * s->passes + 2;
+    if (!s || s->n == 0) return 0;
+    // keys, sort, permute, copy back, cell bounds (2), list build
+    return (s->n > 1 ? 5ull * s->passes : 0ull) + 6;
 }
 
 int mixed_rebuilds(MixedScene* s, unsigned long long* out, cudaStream_t q)
@@ -1589,7 +1637,7 @@ int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q)
     unsigned c[kCounters] = {};
     int st = cuda_status(cudaMemcpyAsync(c, s->counters, sizeof(c), cudaMemcpyDeviceToHost, q), "counters");
     if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "counters");
-    out[0] = c[CN_WALLS];
+    out[0] = c[CN_HEAVY];
     out[1] = c[CN_DECISIONS];
     out[2] = c[CN_NORMALS];
     out[3] = c[CN_SLIPS];

@@ -148,7 +148,7 @@ class DeviceScene:
     def counters(self, stream: int = 0):
         out = np.zeros(4, np.uint64)
         call("xd_scene_counters", self.handle, out.ctypes.data, stream)
-        return {"near_wall": int(out[0]), "fp64_decisions": int(out[1]),
+        return {"contact_list": int(out[0]), "fp64_decisions": int(out[1]),
                 "fp64_normal_forces": int(out[2]), "fp64_slips": int(out[3])}
 
     def rebuilds(self, stream: int = 0):
