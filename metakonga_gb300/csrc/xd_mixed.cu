@@ -115,6 +115,8 @@ struct MixParams {
     int nplanes;
     float pxw[kMaxPlanes][3];   // plane corner relative to the grid origin (FP32)
     float pun[kMaxPlanes][3];   // unit normal (FP32)
+    double pl_c43Eeq[kMaxPlanes], pl_one_b2[kMaxPlanes];   // getConstant's pair constants per plane
+    double pl_sratio[kMaxPlanes], pl_fric[kMaxPlanes];
     float wall_tol;
 };
 
@@ -484,8 +486,12 @@ __global__ void __launch_bounds__(256) k_mx_advance(MixParams P, Master M, const
         const float dx = v.x - r0.x, dy = v.y - r0.y, dz = v.z - r0.z;
         out = !(dx * dx + dy * dy + dz * dz < P.disp2);
     }
-    if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31u) == 0) atomicOr(counters + CN_REBUILD, 1u);
-    __threadfence();
+    // only the flag must be visible to the last block: the lanes that set it
+    // fence; the state and view writes need no ordering here
+    if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31u) == 0) {
+        atomicOr(counters + CN_REBUILD, 1u);
+        __threadfence();
+    }
     __syncthreads();
     if (threadIdx.x == 0) last = atomicAdd(counters + CN_DONE, 1u) == gridDim.x - 1;
     __syncthreads();
@@ -922,8 +928,11 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
 // plane_contact_force_kernel<1> (impl:572-621) for the planes in reach, in
 // FP64, in plane order (the others are out of reach and add exactly zero).
 // Block 0 clears CN_REBUILD for the next step's skin test.
+constexpr unsigned kContactThreads = 64;
+constexpr unsigned kContactBlocks = 152 * 8;
+
 template <bool RECORD>
-__global__ void __launch_bounds__(256) k_mx_contact(MixParams P, Master M, const float4* __restrict__ pf,
+__global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Master M, const float4* __restrict__ pf,
                                                     const longlong2* __restrict__ qa,
                                                     const longlong2* __restrict__ qb,
                                                     const unsigned* __restrict__ keys,
@@ -943,19 +952,19 @@ __global__ void __launch_bounds__(256) k_mx_contact(MixParams P, Master M, const
     if (blockIdx.x == 0 && threadIdx.x == 0) counters[CN_REBUILD] = 0;
     const unsigned total = counters[CN_HEAVY];
     const unsigned n = P.n;
-    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-        Own I;
-        I.i = __ldg(hlist + t);
-        const unsigned i = I.i;
+    // runs of 32 consecutive list entries (neighbouring slots) go to the warps
+    // of all blocks in turn: every SM gets an equal share however short the list
+    const unsigned warps = gridDim.x * (blockDim.x / 32u);
+    const unsigned gw = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u;
+    for (unsigned t = gw * 32u + (threadIdx.x & 31u); t < total; t += warps * 32u) {
+        const unsigned i = __ldg(hlist + t);
         const float4 pi = __ldg(pf + i);
-        I.qa = __ldg(qa + i);
-        I.qb = __ldg(qb + i);
-        I.vh = __ldg(M.vh + i);
-        I.vl = __ldg(M.vl + i);
-        const float4 w4 = __ldg(M.wh + i);
-        I.w = fk(w4.x, w4.y, w4.z);
+        // the particle's own data is loaded when first needed: most listed
+        // particles have neighbours within the skin but no contact
+        Own I;
+        I.i = i;
         I.r = pi.w;
-        I.im = I.vh.w;
+        bool have_q = false, have_v = false;
         PairAcc A;
         A.Ft = fk(0.f, 0.f, 0.f);
         A.Mm = fk(0.f, 0.f, 0.f);
@@ -963,28 +972,57 @@ __global__ void __launch_bounds__(256) k_mx_contact(MixParams P, Master M, const
         A.sumM = fk(0.f, 0.f, 0.f);
         unsigned nc = 0;
         auto add = [&](unsigned j, bool guard) {
+            if (!have_v) {
+                I.vh = __ldg(M.vh + i);
+                I.vl = __ldg(M.vl + i);
+                const float4 w4 = __ldg(M.wh + i);
+                I.w = fk(w4.x, w4.y, w4.z);
+                I.im = I.vh.w;
+                have_v = true;
+            }
             contact_force(P, M, I, j, guard, mass0, pf, qa, qb, counters, A);
             if (RECORD && nc < rec_cap) rec_pairs[(size_t)i * rec_cap + nc] = j;
             ++nc;
         };
         const unsigned vc = __ldg(vcount + i);
         if (!(vc & kIncomplete)) {
+            const float rt0 = pi.w + P.tol;
             for (unsigned k = 0; k < vc; ++k) {
                 const unsigned j = __ldg(vlist + (size_t)k * n + i);
-                const int c = touch<true>(P, M, i, j, pi, I.qa, I.qb, pf, qa, qb, counters);
+                const float4 pj = __ldg(pf + j);
+                const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                const float Rt = rt0 + pj.w;
+                if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) >= Rt * Rt) continue;
+                if (!have_q) {
+                    I.qa = __ldg(qa + i);
+                    I.qb = __ldg(qb + i);
+                    have_q = true;
+                }
+                const int c = exact_touch<true>(P, M, i, j, I.qa, I.qb, qa, qb, counters);
                 if (c) add(j, c == 2);
             }
         } else {
+            I.qa = __ldg(qa + i);
+            I.qb = __ldg(qb + i);
             for_each_contact<true>(P, M, i, pi, I.qa, I.qb, __ldg(keys + i), pf, qa, qb, lb, counters, add);
         }
         float4 F = make_float4(A.sumF.x, A.sumF.y, A.sumF.z, 0.f);
-        const unsigned wm = __ldg(wmask + i);
+        // planes in reach: an FP32 distance to the supporting plane first (the
+        // finite plane is never nearer), the reference's FP64 test after it
+        unsigned wm = __ldg(wmask + i);
+        for (unsigned mask = wm; mask; mask &= mask - 1u) {
+            const int w = __ffs(mask) - 1;
+            const float hz = (pi.x - P.pxw[w][0]) * P.pun[w][0] + (pi.y - P.pxw[w][1]) * P.pun[w][1] +
+                             (pi.z - P.pxw[w][2]) * P.pun[w][2];
+            if (!(fabsf(hz) < pi.w + P.tol)) wm &= ~(1u << w);
+        }
         if (wm) {
-            const float4 wl = __ldg(M.wl + i), wh = w4;
+            const float4 vh = __ldg(M.vh + i), vl = __ldg(M.vl + i);
+            const float4 wl = __ldg(M.wl + i), wh = __ldg(M.wh + i);
             const double m = __ldg(mass0 + __float_as_uint(wl.w));
             const d3 ip = mk(__ldg(M.x + i), __ldg(M.y + i), __ldg(M.z + i));
             const double r = __ldg(M.r + i);
-            const d3 iv = mk(df_to_d(I.vh.x, I.vl.x), df_to_d(I.vh.y, I.vl.y), df_to_d(I.vh.z, I.vl.z));
+            const d3 iv = mk(df_to_d(vh.x, vl.x), df_to_d(vh.y, vl.y), df_to_d(vh.z, vl.z));
             const d3 iw = mk(df_to_d(wh.x, wl.x), df_to_d(wh.y, wl.y), df_to_d(wh.z, wl.z));
             d3 f = mk(0, 0, 0);
             for (unsigned mask = wm; mask; mask &= mask - 1u) {
@@ -996,10 +1034,15 @@ __global__ void __launch_bounds__(256) k_mx_contact(MixParams P, Master M, const
                 d3 wp = mk(dot(dp, pe.u1), dot(dp, pe.u2), dot(dp, pe.uw));
                 double cdist = plane_detection(pe, ip, wp, unit, r);
                 if (cdist > 0) {
-                    PairConst pc = load_pair_const(cps + w);
                     d3 dv = -(iv + cross(iw, r * unit));
-                    xd::Fc c = get_constant(pc, r, 0.0, m, 0.0);
-                    dhs(c, 0, 0, 0, 0, 0, 0, pc.coh, cdist, dv, unit, P.dt, Ft, Fn, Mo);
+                    // getConstant with the plane's hoisted material terms (Meq = m, Req = r)
+                    xd::Fc c;
+                    c.kn = P.pl_c43Eeq[w] * sqrt(r);
+                    c.vn = sqrt((4.0 * m * c.kn) / P.pl_one_b2[w]);
+                    c.ks = c.kn * P.pl_sratio[w];
+                    c.vs = c.vn * P.pl_sratio[w];
+                    c.mu = P.pl_fric[w];
+                    dhs(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit, P.dt, Ft, Fn, Mo);
                 }
                 f += Fn + Ft;
             }
@@ -1211,6 +1254,16 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     P.guard_q = (long long)ceil(kGuard * kQ);
     P.nplanes = (int)d.nplanes;
     for (unsigned w = 0; w < d.nplanes; ++w) {
+        // getConstant's material terms (impl:214-256), hoisted out of the kernel
+        const xd_contact_property& c = d.cp_planes[w];
+        const double eq = (c.Ei * c.Ej) / (c.Ei * (1 - c.prj * c.prj) + c.Ej * (1 - c.pri * c.pri));
+        const double bt = M_PI / log(c.rest);
+        P.pl_c43Eeq[w] = (4.0 / 3.0) * eq;
+        P.pl_one_b2[w] = 1.0 + bt * bt;
+        P.pl_sratio[w] = c.sratio;
+        P.pl_fric[w] = c.fric;
+    }
+    for (unsigned w = 0; w < d.nplanes; ++w) {
         const xd_plane_info& p = d.planes[w];
         double un = sqrt(p.uw[0] * p.uw[0] + p.uw[1] * p.uw[1] + p.uw[2] * p.uw[2]);
         for (int a = 0; a < 3; ++a) {
@@ -1276,6 +1329,9 @@ int mixed_create(const xd_scene_desc& d, MixedScene** out)
     if (d.cp_pp.coh != 0.0) return set_error(XD_ERR_INVALID, "mixed mode: cohesion is not supported");
     if (d.nplanes && (!d.planes || !d.cp_planes))
         return set_error(XD_ERR_INVALID, "mixed mode: planes given without arrays");
+    for (unsigned w = 0; w < d.nplanes; ++w)
+        if (d.cp_planes[w].coh != 0.0)
+            return set_error(XD_ERR_INVALID, "mixed mode: cohesion is not supported (plane %u)", w);
     MixedScene* s = new (std::nothrow) MixedScene();
     if (!s) return set_error(XD_ERR_NOMEM, "mixed scene: host allocation");
     s->desc = d;
@@ -1469,15 +1525,15 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
     if (st != XD_OK) return st;
     s->cells_clean = true;
     ph.begin(3, q);
-    const unsigned grid = min(blocks(n, 256), 152u * 8u);
+    const unsigned grid = kContactBlocks;
     if (record) {
         st = cuda_status(cudaMemsetAsync(s->rec_count, 0, sizeof(unsigned) * n, q), "mixed pair count");
         if (st != XD_OK) return st;
-        k_mx_contact<true><<<grid, 256, 0, q>>>(s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->vcount,
+        k_mx_contact<true><<<grid, kContactThreads, 0, q>>>(s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->vcount,
                                                 s->vlist, s->hlist, s->wmask, s->planes, s->cps, s->mass0,
                                                 s->Fc, s->Mc, s->counters, s->rec_count, s->rec_pairs, rec_cap);
     } else {
-        k_mx_contact<false><<<grid, 256, 0, q>>>(s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->vcount,
+        k_mx_contact<false><<<grid, kContactThreads, 0, q>>>(s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->vcount,
                                                  s->vlist, s->hlist, s->wmask, s->planes, s->cps, s->mass0,
                                                  s->Fc, s->Mc, s->counters, nullptr, nullptr, 0);
     }
