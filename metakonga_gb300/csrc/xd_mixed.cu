@@ -44,6 +44,7 @@
 // one cell on every side, keys clamped inside.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -64,6 +65,8 @@ constexpr float kU = 1.4551915228366852e-11f;  // 2^-36 m
 constexpr double kGuard = 2e-10;               // metres: FP64 decision inside this band
 constexpr double kMagic = 6755399441055744.0;  // 1.5 * 2^52
 constexpr unsigned kVerletCap = 48;            // neighbours per particle kept in the Verlet list
+constexpr unsigned kTriCap = 16;               // triangles per particle kept in its list
+constexpr int kMaxBodies = 8;                  // polygon bodies of a mixed scene
 constexpr unsigned kGuardBit = 0x80000000u;    // list entry decided by the FP64 test
 
 // Counter words.
@@ -118,6 +121,11 @@ struct MixParams {
     double pl_c43Eeq[kMaxPlanes], pl_one_b2[kMaxPlanes];   // getConstant's pair constants per plane
     double pl_sratio[kMaxPlanes], pl_fric[kMaxPlanes];
     float wall_tol;
+    int rolling;         // rollingCondition: rotation terms in the relative velocity
+    unsigned ntri, nbodies;
+    float tri_reach;     // a triangle is registered in every cell within this of its box
+    double pb_c43Eeq[kMaxBodies], pb_one_b2[kMaxBodies];   // getConstant's terms per polygon body
+    double pb_sratio[kMaxBodies], pb_fric[kMaxBodies];
 };
 
 }  // namespace
@@ -142,6 +150,29 @@ struct MixedScene {
     unsigned* vcount = nullptr;   // Verlet neighbours per particle (| kIncomplete: overflow)
     unsigned* vlist = nullptr;    // [kVerletCap][n]: neighbour slots in search order
     float4* pref = nullptr;       // FP32 positions at the last list build
+    // triangle meshes (FP64, world frame) and their polygon bodies
+    unsigned ntri = 0, nbodies = 0;
+    xd_polygon_info* poly = nullptr;
+    double* sphere = nullptr;     // circumcentres (written by the mesh update)
+    double* vlist_body = nullptr; // body-frame vertices [ntri][9]
+    xd_polygon_mass_info* pmi = nullptr;
+    float* tri_ref = nullptr;     // vertices at the last build, FP32 relative to the grid origin
+    unsigned* tcells = nullptr;   // cells per triangle, then their exclusive scan [ntri + 1]
+    unsigned* tpk = nullptr;      // (cell, triangle) pairs [tpair_cap]: keys, triangles
+    unsigned* tpt = nullptr;
+    unsigned tpair_cap = 0;
+    void* tsort_scratch = nullptr;
+    unsigned* tpk_sorted = nullptr;   // the sort's outputs (fixed for the scene)
+    unsigned* tpt_sorted = nullptr;
+    unsigned* tcount = nullptr;   // triangles in reach per particle (| kIncomplete: overflow)
+    unsigned* tlist = nullptr;    // [kTriCap][n]: triangle ids in id order
+    double* rxn = nullptr;        // reaction on the bodies per particle [nbodies][6][n]
+    double* rxn_part = nullptr;   // block partials of its fixed-order sum
+    bool bodies_dirty = false;
+    std::vector<xd_polygon_info> host_poly;
+    std::vector<double> host_sphere, host_vlist;
+    std::vector<xd_polygon_mass_info> host_pmi;
+    std::vector<xd_contact_property> host_cppoly;
     // grid
     unsigned *keys = nullptr, *vals = nullptr, *prev_keys = nullptr;
     unsigned* lb = nullptr;       // ncell + 1 entries
@@ -708,6 +739,184 @@ __device__ __forceinline__ void for_each_contact(const MixParams& P, const Maste
 
 constexpr unsigned kIncomplete = 0x80000000u;   // vcount flag: the list is not complete
 
+// ---- triangle meshes ---------------------------------------------------------
+//
+// At a re-binning every triangle is registered in each cell that its
+// bounding box, widened by the reach of the largest particle, overlaps;
+// each particle then lists the triangles of its cell whose closest point is
+// within r + skin (FP64), in triangle-id order.  Meshes move only between
+// calls (xd_scene_set_bodies); the mesh update then compares the vertices
+// with those of the last build and raises CN_REBUILD past half the skin.
+
+// The interior cells a triangle's widened bounding box covers, and its
+// vertices in FP32 relative to the grid origin.
+__device__ __forceinline__ void tri_box(const MixParams& P, const xd_polygon_info* __restrict__ t,
+                                        int lo[3], int hi[3], float v[9])
+{
+    const double* V[3] = { t->P, t->Q, t->R };
+    const int g[3] = { P.gx, P.gy, P.gz };
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float mn = 3.0e38f, mx = -3.0e38f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float c = (float)(__ldg(V[k] + a) - P.wo[a]);
+            v[3 * k + a] = c;
+            mn = fminf(mn, c);
+            mx = fmaxf(mx, c);
+        }
+        lo[a] = min(max((int)floorf((mn - P.tri_reach) * P.inv_csf) + 1, 1), g[a] - 2);
+        hi[a] = min(max((int)floorf((mx + P.tri_reach) * P.inv_csf) + 1, 1), g[a] - 2);
+    }
+}
+
+// Cells per triangle (tcells[ntri] = 0 for the scan) and the build vertices.
+__global__ void __launch_bounds__(256) k_tri_count(MixParams P, const xd_polygon_info* __restrict__ poly,
+                                                   unsigned* __restrict__ tcells,
+                                                   float* __restrict__ tri_ref)
+{
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > P.ntri) return;
+    if (t == P.ntri) {
+        tcells[t] = 0;
+        return;
+    }
+    int lo[3], hi[3];
+    float v[9];
+    tri_box(P, poly + t, lo, hi, v);
+    for (int k = 0; k < 9; ++k) tri_ref[9 * (size_t)t + k] = v[k];
+    tcells[t] = (unsigned)((hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1));
+}
+
+// In-place exclusive scan of m values, one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_scan1(unsigned* __restrict__ a, unsigned m)
+{
+    __shared__ unsigned wsum[32];
+    __shared__ unsigned carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (unsigned b0 = 0; b0 < m; b0 += 1024) {
+        const unsigned i = b0 + threadIdx.x;
+        const unsigned v = i < m ? a[i] : 0u;
+        unsigned x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (unsigned)o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            const unsigned w = wsum[lane];
+            unsigned t = w;
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= (unsigned)o) t += y;
+            }
+            wsum[lane] = t - w;
+        }
+        __syncthreads();
+        const unsigned excl = x - v + wsum[warp] + carry;
+        if (i < m) a[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = excl + v;
+        __syncthreads();
+    }
+}
+
+// The (cell key, triangle) pairs, cells in key order per triangle.
+__global__ void __launch_bounds__(256) k_tri_fill(MixParams P, const xd_polygon_info* __restrict__ poly,
+                                                  const unsigned* __restrict__ toff, unsigned cap,
+                                                  unsigned* __restrict__ tpk, unsigned* __restrict__ tpt)
+{
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.ntri) return;
+    int lo[3], hi[3];
+    float v[9];
+    tri_box(P, poly + t, lo, hi, v);
+    unsigned k = toff[t];
+    for (int z = lo[2]; z <= hi[2]; ++z)
+        for (int y = lo[1]; y <= hi[1]; ++y)
+            for (int x = lo[0]; x <= hi[0]; ++x, ++k)
+                if (k < cap) {
+                    tpk[k] = ((unsigned)z * (unsigned)P.gy + (unsigned)y) * (unsigned)P.gx + (unsigned)x;
+                    tpt[k] = t;
+                }
+}
+
+// Unused pair slots sort to the end (key = ncell, past every cell).
+__global__ void __launch_bounds__(256) k_tri_pad(const unsigned* __restrict__ toff, unsigned ntri,
+                                                 unsigned cap, unsigned ncell, unsigned* __restrict__ tpk,
+                                                 unsigned* __restrict__ tpt)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap || i < toff[ntri]) return;
+    tpk[i] = ncell;
+    tpt[i] = 0;
+}
+
+// First index in a[0, m) with a[idx] >= v.
+__device__ __forceinline__ unsigned lower_bound_u(const unsigned* __restrict__ a, unsigned m, unsigned v)
+{
+    unsigned lo = 0, hi = m;
+    while (lo < hi) {
+        const unsigned mid = (lo + hi) >> 1;
+        if (__ldg(a + mid) < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ d3 tri_vertex(const double* v) { return mk(__ldg(v), __ldg(v + 1), __ldg(v + 2)); }
+
+// Per particle: the triangles of its cell within r + skin (FP64 closest point).
+__global__ void __launch_bounds__(256) k_tri_build(MixParams P, Master M, const unsigned* __restrict__ keys,
+                                                   const unsigned* __restrict__ tpk,
+                                                   const unsigned* __restrict__ tpt, unsigned cap,
+                                                   const xd_polygon_info* __restrict__ poly,
+                                                   unsigned* __restrict__ tcount, unsigned* __restrict__ tlist)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const unsigned key = __ldg(keys + i);
+    const unsigned b = lower_bound_u(tpk, cap, key), e = lower_bound_u(tpk, cap, key + 1u);
+    const d3 ip = mk(M.x[i], M.y[i], M.z[i]);
+    const double lim = M.r[i] + (double)(P.vcut);
+    const unsigned n = P.n;
+    unsigned c = 0;
+    for (unsigned k = b; k < e; ++k) {
+        const unsigned t = __ldg(tpt + k);
+        const xd_polygon_info* tri = poly + t;
+        const d3 cp = closest_pt_triangle(tri_vertex(tri->P), tri_vertex(tri->Q), tri_vertex(tri->R), ip);
+        if (length(ip - cp) < lim) {
+            if (c < kTriCap) tlist[(size_t)c * n + i] = t;
+            ++c;
+        }
+    }
+    tcount[i] = c > kTriCap ? (kTriCap | kIncomplete) : c;
+}
+
+// After a mesh update: has any vertex moved half the skin since the build?
+__global__ void __launch_bounds__(256) k_tri_moved(MixParams P, const xd_polygon_info* __restrict__ poly,
+                                                   const float* __restrict__ tri_ref,
+                                                   unsigned* __restrict__ counters)
+{
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    bool out = false;
+    if (t < P.ntri) {
+        const double* V[3] = { poly[t].P, poly[t].Q, poly[t].R };
+        for (int k = 0; k < 3; ++k) {
+            float d2 = 0.f;
+            for (int a = 0; a < 3; ++a) {
+                const float d = (float)(V[k][a] - P.wo[a]) - tri_ref[9 * (size_t)t + 3 * k + a];
+                d2 += d * d;
+            }
+            out |= !(d2 < P.disp2);
+        }
+    }
+    if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31u) == 0) atomicOr(counters + CN_REBUILD, 1u);
+}
+
 // Verlet list build (steps that re-bin the cells), one thread per particle:
 // the nine neighbour rows' slot ranges, trimmed to the cells within reach,
 // are staged in shared memory and visited as one flattened loop (rows z then
@@ -725,6 +934,8 @@ __global__ void __launch_bounds__(256) k_mx_build(MixParams P, const float4* __r
                                                   unsigned* __restrict__ vlist,
                                                   float4* __restrict__ pref,
                                                   unsigned short* __restrict__ wmask,
+                                                  const unsigned* __restrict__ tcount,
+                                                  double* __restrict__ rxn,
                                                   unsigned* __restrict__ hlist,
                                                   float4* __restrict__ Fc, float4* __restrict__ Mc,
                                                   unsigned* __restrict__ counters)
@@ -738,6 +949,7 @@ __global__ void __launch_bounds__(256) k_mx_build(MixParams P, const float4* __r
         pref[i] = pi;
         Fc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         Mc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (unsigned q = 0; q < 6 * P.nbodies; ++q) rxn[(size_t)q * P.n + i] = 0.0;
         const unsigned wm = near_planes(P, pi, P.wall_tol + P.vcut);
         wmask[i] = (unsigned short)wm;
         const unsigned key = __ldg(keys + i);
@@ -786,7 +998,7 @@ __global__ void __launch_bounds__(256) k_mx_build(MixParams P, const float4* __r
             ++nv;
         }
         vcount[i] = nv > kVerletCap ? (kVerletCap | kIncomplete) : nv;
-        heavy = nv > 0 || wm != 0u;
+        heavy = nv > 0 || wm != 0u || (P.ntri && __ldg(tcount + i) != 0u);
     }
     warp_append(heavy, i, hlist, counters + CN_HEAVY);
 }
@@ -843,8 +1055,8 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     df_diff(vj4.y, I.vh.y, __fsub_rn(vjl.y, I.vl.y), dvs[1], dvt[1]);
     df_diff(vj4.z, I.vh.z, __fsub_rn(vjl.z, I.vl.z), dvs[2], dvt[2]);
     const f3 dv = fk(dvs[0] + dvt[0], dvs[1] + dvt[1], dvs[2] + dvt[2]);
-    // rv = vj + wj x (-rj u) - (vi + wi x (ri u))   (impl:455)
-    const f3 wterm = fcross(wj, (-jr) * u) - fcross(I.w, ir * u);
+    // rv = vj + wj x (-rj u) - (vi + wi x (ri u)), or vj - vi without rolling (impl:455)
+    const f3 wterm = P.rolling ? fcross(wj, (-jr) * u) - fcross(I.w, ir * u) : fk(0.f, 0.f, 0.f);
     const f3 rv = dv + wterm;
     // rv . u = dv . u (the rotation term is perpendicular to u), in double-float
     const int dqi[3] = { (int)ddx, (int)ddy, (int)ddz };
@@ -944,6 +1156,13 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
                                                     const xd_plane_info* __restrict__ planes,
                                                     const xd_contact_property* __restrict__ cps,
                                                     const double* __restrict__ mass0,
+                                                    const xd_polygon_info* __restrict__ poly,
+                                                    const xd_polygon_mass_info* __restrict__ pmi,
+                                                    const unsigned* __restrict__ tcount,
+                                                    const unsigned* __restrict__ tlist,
+                                                    const unsigned* __restrict__ tpk,
+                                                    const unsigned* __restrict__ tpt, unsigned tcap,
+                                                    double* __restrict__ rxn,
                                                     float4* __restrict__ Fc, float4* __restrict__ Mc,
                                                     unsigned* __restrict__ counters,
                                                     unsigned* __restrict__ rec_count,
@@ -1034,7 +1253,7 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
                 d3 wp = mk(dot(dp, pe.u1), dot(dp, pe.u2), dot(dp, pe.uw));
                 double cdist = plane_detection(pe, ip, wp, unit, r);
                 if (cdist > 0) {
-                    d3 dv = -(iv + cross(iw, r * unit));
+                    d3 dv = P.rolling ? -(iv + cross(iw, r * unit)) : -iv;
                     // getConstant with the plane's hoisted material terms (Meq = m, Req = r)
                     xd::Fc c;
                     c.kn = P.pl_c43Eeq[w] * sqrt(r);
@@ -1050,10 +1269,105 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
             F.y += (float)f.y;
             F.z += (float)f.z;
         }
+        // triangles in reach: particle_polygonObject_collision_kernel<1>
+        // (impl:923-1021) in FP64, the normal from the face winding, the wall
+        // velocity of the body at the contact point, no particle moment (ir = 0
+        // as the reference calls DHSModel); Ft persists across triangles.  The
+        // reaction on each body goes to this particle's own slots of rxn and is
+        // summed over particles in a fixed order afterwards.
+        const unsigned tc = P.ntri ? __ldg(tcount + i) : 0u;
+        if (tc) {
+            for (unsigned q = 0; q < 6 * P.nbodies; ++q) rxn[(size_t)q * n + i] = 0.0;
+            const float4 vh = __ldg(M.vh + i), vl = __ldg(M.vl + i);
+            const float4 wl = __ldg(M.wl + i), wh = __ldg(M.wh + i);
+            const double m = __ldg(mass0 + __float_as_uint(wl.w));
+            const d3 ip = mk(__ldg(M.x + i), __ldg(M.y + i), __ldg(M.z + i));
+            const double r = __ldg(M.r + i);
+            const d3 iv = mk(df_to_d(vh.x, vl.x), df_to_d(vh.y, vl.y), df_to_d(vh.z, vl.z));
+            const d3 iw = mk(df_to_d(wh.x, wl.x), df_to_d(wh.y, wl.y), df_to_d(wh.z, wl.z));
+            d3 f = mk(0, 0, 0), Ft = mk(0, 0, 0), Mo = mk(0, 0, 0);
+            const bool listed = !(tc & kIncomplete);
+            unsigned kb = 0, ke = tc;
+            if (!listed) {
+                const unsigned key = __ldg(keys + i);
+                kb = lower_bound_u(tpk, tcap, key);
+                ke = lower_bound_u(tpk, tcap, key + 1u);
+            }
+            for (unsigned k = kb; k < ke; ++k) {
+                const unsigned t = listed ? __ldg(tlist + (size_t)k * n + i) : __ldg(tpt + k);
+                const xd_polygon_info* tri = poly + t;
+                const unsigned b = (unsigned)__ldg(&tri->id);
+                const d3 Pv = tri_vertex(tri->P), Qv = tri_vertex(tri->Q), Rv = tri_vertex(tri->R);
+                const d3 cpt = closest_pt_triangle(Pv, Qv, Rv, ip);
+                const double cdist = r - length(ip - cpt);
+                if (!(cdist > 0)) continue;
+                const d3 po2cp = cpt - tri_vertex(pmi[b].origin);
+                d3 unit = -cross(Qv - Pv, Rv - Pv);
+                unit = unit / length(unit);
+                const d3 pvel = tri_vertex(pmi[b].vel), pom = tri_vertex(pmi[b].omega);
+                const d3 dv = P.rolling ? (pvel + cross(pom, po2cp)) - (iv + cross(iw, r * unit)) : (pvel - iv);
+                xd::Fc c;
+                c.kn = P.pb_c43Eeq[b] * sqrt(r);
+                c.vn = sqrt((4.0 * m * c.kn) / P.pb_one_b2[b]);
+                c.ks = c.kn * P.pb_sratio[b];
+                c.vs = c.vn * P.pb_sratio[b];
+                c.mu = P.pb_fric[b];
+                d3 Fn = mk(0, 0, 0);
+                dhs(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit, P.dt, Ft, Fn, Mo);
+                const d3 fc = Fn + Ft;
+                f += fc;
+                const d3 rm = -cross(po2cp, fc);
+                double* rb = rxn + (size_t)b * 6 * n + i;
+                rb[0] -= fc.x;
+                rb[n] -= fc.y;
+                rb[2 * (size_t)n] -= fc.z;
+                rb[3 * (size_t)n] += rm.x;
+                rb[4 * (size_t)n] += rm.y;
+                rb[5 * (size_t)n] += rm.z;
+            }
+            F.x += (float)f.x;
+            F.y += (float)f.y;
+            F.z += (float)f.z;
+        }
         Fc[i] = F;
         Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
         if (RECORD) rec_count[i] = nc;
     }
+}
+
+// Body reactions: rxn[(b * 6 + q) * n + i] summed over i in a fixed order
+// (kRxnBlocks fixed chunks, each a fixed tree), then added to the bodies.
+constexpr unsigned kRxnBlocks = 152;
+__global__ void __launch_bounds__(256) k_rxn_partial(const double* __restrict__ rxn, unsigned n,
+                                                     unsigned nq, double* __restrict__ part)
+{
+    __shared__ double sh[256];
+    const unsigned chunk = (n + gridDim.x - 1) / gridDim.x;
+    const unsigned b0 = blockIdx.x * chunk, b1 = min(n, b0 + chunk);
+    for (unsigned q = 0; q < nq; ++q) {
+        double s = 0.0;
+        for (unsigned i = b0 + threadIdx.x; i < b1; i += blockDim.x) s += rxn[(size_t)q * n + i];
+        sh[threadIdx.x] = s;
+        __syncthreads();
+        for (unsigned o = 128; o > 0; o >>= 1) {
+            if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) part[(size_t)q * gridDim.x + blockIdx.x] = sh[0];
+        __syncthreads();
+    }
+}
+
+__global__ void k_rxn_final(const double* __restrict__ part, unsigned nblocks, unsigned nbodies,
+                            xd_polygon_mass_info* __restrict__ pmi)
+{
+    const unsigned q = threadIdx.x;   // one thread per (body, component)
+    if (q >= 6 * nbodies) return;
+    double s = 0.0;
+    for (unsigned k = 0; k < nblocks; ++k) s += part[(size_t)q * nblocks + k];
+    const unsigned b = q / 6, c = q % 6;
+    if (c < 3) pmi[b].force[c] += s;
+    else pmi[b].moment[c - 3] += s;
 }
 
 // ---- host-order state <-> master (reference layouts) -----------------------
@@ -1180,6 +1494,23 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
                 hi[a] = fmax(hi[a], q[a]);
             }
     }
+    // triangle meshes (as placed now; a body that later moves beyond the grid
+    // has its triangles clamped into the boundary cells)
+    double tri_edge = 0.0;
+    for (unsigned t = 0; t < d.ntri; ++t) {
+        const xd_polygon_info& tr = d.poly[t];
+        const double* V[3] = { tr.P, tr.Q, tr.R };
+        for (int k = 0; k < 3; ++k) {
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = fmin(lo[a], V[k][a]);
+                hi[a] = fmax(hi[a], V[k][a]);
+            }
+            const double* W = V[(k + 1) % 3];
+            const double e = sqrt((V[k][0] - W[0]) * (V[k][0] - W[0]) + (V[k][1] - W[1]) * (V[k][1] - W[1]) +
+                                  (V[k][2] - W[2]) * (V[k][2] - W[2]));
+            tri_edge = fmax(tri_edge, e);
+        }
+    }
     if (d.np == 0) {
         for (int a = 0; a < 3; ++a) { lo[a] = 0; hi[a] = 1; }
         rmax = 0.5;
@@ -1253,6 +1584,22 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     P.fric = (float)cp.fric;
     P.guard_q = (long long)ceil(kGuard * kQ);
     P.nplanes = (int)d.nplanes;
+    P.rolling = d.params.rollingCondition ? 1 : 0;
+    P.ntri = d.ntri;
+    P.nbodies = d.ntri ? d.nbodies : 0;
+    // a particle within r + skin of a triangle has its centre within this of
+    // the triangle's bounding box
+    P.tri_reach = (float)(rmax + skin) + 2.0f * P.tol;
+    for (unsigned b = 0; b < P.nbodies; ++b) {
+        // getConstant's material terms (impl:214-256) of each body's contact property
+        const xd_contact_property& c = d.cp_poly[b];
+        const double eq = (c.Ei * c.Ej) / (c.Ei * (1 - c.prj * c.prj) + c.Ej * (1 - c.pri * c.pri));
+        const double bt = M_PI / log(c.rest);
+        P.pb_c43Eeq[b] = (4.0 / 3.0) * eq;
+        P.pb_one_b2[b] = 1.0 + bt * bt;
+        P.pb_sratio[b] = c.sratio;
+        P.pb_fric[b] = c.fric;
+    }
     for (unsigned w = 0; w < d.nplanes; ++w) {
         // getConstant's material terms (impl:214-256), hoisted out of the kernel
         const xd_contact_property& c = d.cp_planes[w];
@@ -1317,13 +1664,57 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
         A(cuda_status(cudaMemcpy(s->planes, d.planes, sizeof(xd_plane_info) * s->nplanes, cudaMemcpyHostToDevice), "mixed planes"));
         A(cuda_status(cudaMemcpy(s->cps, d.cp_planes, sizeof(xd_contact_property) * s->nplanes, cudaMemcpyHostToDevice), "mixed planes"));
     }
+    if (st == XD_OK && d.ntri) {
+        s->ntri = d.ntri;
+        s->nbodies = d.nbodies;
+        // (cell, triangle) pairs: a triangle's box, widened by the reach, spans
+        // at most ceil((edge + 2 reach) / cs) + 1 cells per axis in any pose
+        const double span = ceil((tri_edge + 2.0 * (double)P.tri_reach) / s->cs) + 1.0;
+        const double cap = (double)d.ntri * span * span * span;
+        if (cap > (double)(1u << 30))
+            return set_error(XD_ERR_CAPACITY, "mixed mode: %u triangles of up to %g m span %g cells each; "
+                             "the cell-triangle table would exceed 2^30 entries", d.ntri, tri_edge,
+                             span * span * span);
+        s->tpair_cap = (unsigned)cap;
+        A(alloc(s, &s->poly, s->ntri));
+        A(alloc(s, &s->sphere, 4 * (size_t)s->ntri));
+        A(alloc(s, &s->vlist_body, 9 * (size_t)s->ntri));
+        A(alloc(s, &s->pmi, s->nbodies));
+        A(alloc(s, &s->tri_ref, 9 * (size_t)s->ntri));
+        A(alloc(s, &s->tcells, (size_t)s->ntri + 1));
+        A(alloc(s, &s->tpk, s->tpair_cap));
+        A(alloc(s, &s->tpt, s->tpair_cap));
+        char* tscr = nullptr;
+        A(alloc(s, &tscr, radix_sort_scratch_bytes(s->tpair_cap)));
+        s->tsort_scratch = tscr;
+        A(alloc(s, &s->tcount, n));
+        A(alloc(s, &s->tlist, n * kTriCap));
+        A(alloc(s, &s->rxn, (size_t)6 * s->nbodies * n));
+        A(alloc(s, &s->rxn_part, (size_t)6 * s->nbodies * kRxnBlocks));
+        if (st == XD_OK) {
+            A(cuda_status(cudaMemcpy(s->poly, d.poly, sizeof(xd_polygon_info) * s->ntri, cudaMemcpyHostToDevice), "mixed mesh"));
+            A(cuda_status(cudaMemcpy(s->sphere, d.sphere, sizeof(double) * 4 * s->ntri, cudaMemcpyHostToDevice), "mixed mesh"));
+            A(cuda_status(cudaMemcpy(s->vlist_body, d.vlist, sizeof(double) * 9 * s->ntri, cudaMemcpyHostToDevice), "mixed mesh"));
+            A(cuda_status(cudaMemcpy(s->pmi, d.pmi, sizeof(xd_polygon_mass_info) * s->nbodies, cudaMemcpyHostToDevice), "mixed mesh"));
+        }
+    }
     return st;
 }
 
 int mixed_create(const xd_scene_desc& d, MixedScene** out)
 {
     *out = nullptr;
-    if (d.ntri) return set_error(XD_ERR_INVALID, "mixed mode: triangle meshes are not supported yet");
+    if (d.ntri && (!d.poly || !d.sphere || !d.vlist || !d.pmi || !d.cp_poly || !d.nbodies))
+        return set_error(XD_ERR_INVALID, "mixed mode: triangles given without mesh arrays");
+    if (d.ntri && d.nbodies > (unsigned)kMaxBodies)
+        return set_error(XD_ERR_INVALID, "mixed mode: at most %d polygon bodies", kMaxBodies);
+    for (unsigned b = 0; d.ntri && b < d.nbodies; ++b)
+        if (d.cp_poly[b].coh != 0.0)
+            return set_error(XD_ERR_INVALID, "mixed mode: cohesion is not supported (body %u)", b);
+    for (unsigned t = 0; t < d.ntri; ++t)
+        if (d.poly[t].id < 0 || (unsigned)d.poly[t].id >= d.nbodies)
+            return set_error(XD_ERR_INVALID, "mixed mode: triangle %u names body %d of %u", t, d.poly[t].id,
+                             d.nbodies);
     if (d.nplanes > (unsigned)kMaxPlanes)
         return set_error(XD_ERR_INVALID, "mixed mode: at most %d planes", kMaxPlanes);
     if (d.cp_pp.coh != 0.0) return set_error(XD_ERR_INVALID, "mixed mode: cohesion is not supported");
@@ -1339,11 +1730,18 @@ int mixed_create(const xd_scene_desc& d, MixedScene** out)
     s->host_cps.assign(d.cp_planes, d.cp_planes + d.nplanes);
     s->desc.planes = s->host_planes.data();
     s->desc.cp_planes = s->host_cps.data();
-    s->desc.poly = nullptr;
-    s->desc.sphere = nullptr;
-    s->desc.vlist = nullptr;
-    s->desc.pmi = nullptr;
-    s->desc.cp_poly = nullptr;
+    if (d.ntri) {
+        s->host_poly.assign(d.poly, d.poly + d.ntri);
+        s->host_sphere.assign(d.sphere, d.sphere + 4 * (size_t)d.ntri);
+        s->host_vlist.assign(d.vlist, d.vlist + 9 * (size_t)d.ntri);
+        s->host_pmi.assign(d.pmi, d.pmi + d.nbodies);
+        s->host_cppoly.assign(d.cp_poly, d.cp_poly + d.nbodies);
+    }
+    s->desc.poly = s->host_poly.data();
+    s->desc.sphere = s->host_sphere.data();
+    s->desc.vlist = s->host_vlist.data();
+    s->desc.pmi = s->host_pmi.data();
+    s->desc.cp_poly = s->host_cppoly.data();
     *out = s;
     return XD_OK;
 }
@@ -1451,9 +1849,44 @@ static int rebuild(MixedScene* s, cudaStream_t q)
     k_mx_copyback<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[1], s->m[0], s->pf, s->qa, s->qb);
     k_lb_fill<<<blocks(n + 1, 256), 256, 0, q>>>(sk, n, s->ncell, s->lb, s->prev_keys, s->gaps, s->counters);
     k_lb_long<<<152 * 4, 256, 0, q>>>(s->gaps, s->counters, s->lb);
+    st = launch_status("mixed re-binning");
+    if (st == XD_OK && s->ntri) {
+        // triangles: (cell, triangle) pairs sorted by cell, then each particle's list
+        const unsigned T = s->ntri, cap = s->tpair_cap;
+        k_tri_count<<<blocks(T + 1, 256), 256, 0, q>>>(s->P, s->poly, s->tcells, s->tri_ref);
+        k_scan1<<<1, 1024, 0, q>>>(s->tcells, T + 1);
+        k_tri_fill<<<blocks(T, 256), 256, 0, q>>>(s->P, s->poly, s->tcells, cap, s->tpk, s->tpt);
+        k_tri_pad<<<blocks(cap, 256), 256, 0, q>>>(s->tcells, T, cap, s->ncell, s->tpk, s->tpt);
+        st = launch_status("mixed triangle cells");
+        unsigned *tk = nullptr, *tt = nullptr;
+        if (st == XD_OK)
+            st = radix_sort_pairs(s->tpk, s->tpt, cap, key_bits_for(s->ncell + 1), s->tsort_scratch, q, &tk, &tt);
+        if (st != XD_OK) return st;
+        s->tpk_sorted = tk;
+        s->tpt_sorted = tt;
+        k_tri_build<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[0], s->prev_keys, tk, tt, cap, s->poly, s->tcount,
+                                                   s->tlist);
+        st = launch_status("mixed triangle lists");
+    }
+    if (st != XD_OK) return st;
     k_mx_build<<<blocks(n, 256), 256, 0, q>>>(s->P, s->pf, s->prev_keys, s->lb, s->vcount, s->vlist, s->pref,
-                                              s->wmask, s->hlist, s->Fc, s->Mc, s->counters);
+                                              s->wmask, s->tcount, s->rxn, s->hlist, s->Fc, s->Mc,
+                                              s->counters);
     return launch_status("mixed re-binning");
+}
+
+// Moves the triangles to the bodies' current poses (after xd_scene_set_bodies)
+// and raises the re-binning flag if a vertex moved half the skin since the
+// last build.  Runs before a step's advance.
+static int update_mesh(MixedScene* s, cudaStream_t q)
+{
+    if (!s->ntri || !s->bodies_dirty) return XD_OK;
+    int st = launch_update_polygon(s->pmi, s->vlist_body, s->sphere, s->poly, s->ntri, q);
+    if (st != XD_OK) return st;
+    k_tri_moved<<<blocks(s->ntri, 256), 256, 0, q>>>(s->P, s->poly, s->tri_ref, s->counters);
+    st = launch_status("mixed mesh moved");
+    if (st == XD_OK) s->bodies_dirty = false;
+    return st;
 }
 
 // Inside a stream capture: a conditional node that runs body(s, stream) when
@@ -1531,13 +1964,23 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
         if (st != XD_OK) return st;
         k_mx_contact<true><<<grid, kContactThreads, 0, q>>>(s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->vcount,
                                                 s->vlist, s->hlist, s->wmask, s->planes, s->cps, s->mass0,
+                                                s->poly, s->pmi, s->tcount, s->tlist, s->tpk_sorted,
+                                                s->tpt_sorted, s->tpair_cap, s->rxn,
                                                 s->Fc, s->Mc, s->counters, s->rec_count, s->rec_pairs, rec_cap);
     } else {
         k_mx_contact<false><<<grid, kContactThreads, 0, q>>>(s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->vcount,
                                                  s->vlist, s->hlist, s->wmask, s->planes, s->cps, s->mass0,
+                                                 s->poly, s->pmi, s->tcount, s->tlist, s->tpk_sorted,
+                                                 s->tpt_sorted, s->tpair_cap, s->rxn,
                                                  s->Fc, s->Mc, s->counters, nullptr, nullptr, 0);
     }
     st = launch_status("mixed contact");
+    if (st == XD_OK && s->nbodies && MODE != 3) {
+        // this step's reaction on the polygon bodies, summed in a fixed order
+        k_rxn_partial<<<kRxnBlocks, 256, 0, q>>>(s->rxn, n, 6 * s->nbodies, s->rxn_part);
+        k_rxn_final<<<1, 64, 0, q>>>(s->rxn_part, kRxnBlocks, s->nbodies, s->pmi);
+        st = launch_status("mixed body reaction");
+    }
     ph.end(3, q);
     return st;
 }
@@ -1577,8 +2020,10 @@ int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
     if (nsteps == 0 || s->n == 0) return XD_OK;
     if (!s->ready) return set_error(XD_ERR_STATE, "mixed mode: no state uploaded");
     const bool graphs = s->use_graphs && ph.fn == nullptr;
+    int st = update_mesh(s, q);
+    if (st != XD_OK) return st;
     // step 1: the position update from the state's (v, a)
-    int st = step_once<0>(s, q, ph, false, 0, nullptr);
+    st = step_once<0>(s, q, ph, false, 0, nullptr);
     if (st != XD_OK) return st;
     unsigned t = 1;
     // pairs of middle steps as one graph launch
@@ -1606,7 +2051,7 @@ unsigned long long mixed_launches(MixedScene* s, unsigned nsteps)
     if (!s || nsteps == 0 || s->n == 0) return 0;
     // per step: advance + contact; + the last velocity update; a step that
     // re-bins adds mixed_rebuild_launches()
-    const unsigned long long per = 2;
+    const unsigned long long per = 2 + (s->nbodies ? 2 : 0);
     unsigned long long total = per * nsteps + 1;
     if (!s->cells_clean) total += mixed_rebuild_launches(s);   // the first step re-bins
     return total;
@@ -1615,8 +2060,11 @@ unsigned long long mixed_launches(MixedScene* s, unsigned nsteps)
 unsigned long long mixed_rebuild_launches(MixedScene* s)
 {
     if (!s || s->n == 0) return 0;
-    // keys, sort, permute, copy back, cell bounds (2), list build
-    return (s->n > 1 ? 5ull * s->passes : 0ull) + 6;
+    // keys, sort, permute, copy back, cell bounds (2), list build; with
+    // triangles also count, scan, fill, pad, their sort and their lists
+    unsigned long long k = (s->n > 1 ? 5ull * s->passes : 0ull) + 6;
+    if (s->ntri) k += 5 + 5ull * ((key_bits_for(s->ncell + 1) + 7) / 8);
+    return k;
 }
 
 int mixed_rebuilds(MixedScene* s, unsigned long long* out, cudaStream_t q)
@@ -1634,6 +2082,8 @@ int mixed_rebuilds(MixedScene* s, unsigned long long* out, cudaStream_t q)
 static int current_contacts(MixedScene* s, cudaStream_t q, bool record, unsigned rec_cap)
 {
     Phases none;
+    int st = update_mesh(s, q);
+    if (st != XD_OK) return st;
     return step_once<3>(s, q, none, record, rec_cap, nullptr);
 }
 
@@ -1686,6 +2136,35 @@ int mixed_pair_list(MixedScene* s, unsigned cap_per_particle, unsigned* counts, 
         for (unsigned k = 0; k < c; ++k) partners[(size_t)o * cap_per_particle + k] = ids[part[i * cap_per_particle + k]];
     }
     return XD_OK;
+}
+
+int mixed_set_bodies(MixedScene* s, const xd_polygon_mass_info* pmi, cudaStream_t q)
+{
+    if (!s->ntri) return set_error(XD_ERR_STATE, "scene_set_bodies: scene has no polygon bodies");
+    if (!s->ready) {
+        // before the first upload: the set-up takes the bodies from the description
+        s->host_pmi.assign(pmi, pmi + s->nbodies);
+        s->desc.pmi = s->host_pmi.data();
+        return XD_OK;
+    }
+    int st = cuda_status(cudaMemcpyAsync(s->pmi, pmi, sizeof(xd_polygon_mass_info) * s->nbodies,
+                                         cudaMemcpyHostToDevice, q), "scene_set_bodies");
+    if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "scene_set_bodies");
+    s->bodies_dirty = true;
+    return st;
+}
+
+int mixed_get_bodies(MixedScene* s, xd_polygon_mass_info* pmi, cudaStream_t q)
+{
+    if (!s->ntri) return set_error(XD_ERR_STATE, "scene_get_bodies: scene has no polygon bodies");
+    if (!s->ready) {
+        std::copy(s->host_pmi.begin(), s->host_pmi.end(), pmi);
+        return XD_OK;
+    }
+    int st = cuda_status(cudaMemcpyAsync(pmi, s->pmi, sizeof(xd_polygon_mass_info) * s->nbodies,
+                                         cudaMemcpyDeviceToHost, q), "scene_get_bodies");
+    if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "scene_get_bodies");
+    return st;
 }
 
 int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q)

@@ -354,6 +354,7 @@ int xd_scene_download_grid(xd_scene* s, unsigned* hash, unsigned* index, unsigne
 int xd_scene_set_bodies(xd_scene* s, const xd_polygon_mass_info* pmi, void* stream)
 {
     if (!s || !pmi) return set_error(XD_ERR_INVALID, "scene_set_bodies: null argument");
+    if (s->mixed) return mixed_set_bodies(s->mixed, pmi, static_cast<cudaStream_t>(stream));
     if (!s->nbodies) return set_error(XD_ERR_STATE, "scene_set_bodies: scene has no polygon bodies");
     cudaStream_t q = static_cast<cudaStream_t>(stream);
     int st = h2d(s->pmi, pmi, sizeof(xd_polygon_mass_info) * s->nbodies, q);
@@ -365,6 +366,7 @@ int xd_scene_set_bodies(xd_scene* s, const xd_polygon_mass_info* pmi, void* stre
 int xd_scene_get_bodies(xd_scene* s, xd_polygon_mass_info* pmi, void* stream)
 {
     if (!s || !pmi) return set_error(XD_ERR_INVALID, "scene_get_bodies: null argument");
+    if (s->mixed) return mixed_get_bodies(s->mixed, pmi, static_cast<cudaStream_t>(stream));
     cudaStream_t q = static_cast<cudaStream_t>(stream);
     int st = d2h(pmi, s->pmi, sizeof(xd_polygon_mass_info) * s->nbodies, q);
     if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "scene_get_bodies");
