@@ -375,6 +375,21 @@ unsigned long long xd_scene_launches(xd_scene* scene, unsigned nsteps);
 int xd_scene_rebuilds(xd_scene* scene, unsigned long long* count, unsigned long long* launches_each,
                       void* stream);
 
+/* Advance `count` independent scenes (scenes[i] by nsteps[i] steps) side by
+ * side on the current device: the scenes are spread over a pool of 16
+ * library streams that start after the work queued on `stream` and that
+ * `stream` waits for on return, so the batch is ordered on `stream` like one
+ * xd_scene_step.  Each scene's result is bit for bit the one xd_scene_step
+ * gives it alone.  Two scenes of one call must not be the same scene.  With
+ * `check` non-zero the call synchronises `stream`.  No counterpart in the
+ * reference, which runs one model per process. */
+int xd_scene_step_many(xd_scene* const* scenes, const unsigned* nsteps, unsigned count, int check,
+                       void* stream);
+
+/* Device memory the scene holds, in bytes (state, grid, lists, meshes,
+ * workspace).  No counterpart in the reference. */
+int xd_scene_device_bytes(xd_scene* scene, unsigned long long* bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,6 +72,8 @@ _SIGS = {
     "xd_scene_pair_list": [vp, u32, vp, vp, vp],
     "xd_scene_counters": [vp, vp, vp],
     "xd_scene_rebuilds": [vp, vp, vp, vp],
+    "xd_scene_step_many": [vp, vp, u32, i32, vp],
+    "xd_scene_device_bytes": [vp, vp],
     "xd_scene_phase_times": [vp, vp, vp],
 }
 _RESTYPES = {"xd_version": C.c_char_p, "xd_status_string": C.c_char_p, "xd_clear_error": None,

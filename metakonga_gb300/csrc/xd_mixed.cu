@@ -192,7 +192,7 @@ struct MixedScene {
     // host-order transfer buffers
     double* xfer = nullptr;
     bool ready = false;                // grid and buffers set up (first upload)
-    cudaGraphExec_t graph[2] = { nullptr, nullptr };   // two middle steps, per buffer parity
+    cudaGraphExec_t graph[3] = { nullptr, nullptr, nullptr };   // first step, two steps, one step
     unsigned passes = 0;          // radix passes of one re-binning
     bool use_graphs = true;
     unsigned rec_cap_alloc = 0;
@@ -200,6 +200,7 @@ struct MixedScene {
     std::vector<xd_plane_info> host_planes;
     std::vector<xd_contact_property> host_cps;
     std::vector<void*> allocs;
+    unsigned long long bytes = 0;   // device memory held
 };
 
 namespace {
@@ -213,6 +214,7 @@ int alloc(MixedScene* s, T** p, size_t count)
     cudaError_t e = cudaMalloc(&q, sizeof(T) * count);
     if (e != cudaSuccess) return cuda_status(e, "mixed scene allocation");
     s->allocs.push_back(q);
+    s->bytes += sizeof(T) * count;
     *p = static_cast<T*>(q);
     return XD_OK;
 }
@@ -1750,7 +1752,7 @@ void mixed_destroy(MixedScene* s)
 {
     if (!s) return;
     cudaDeviceSynchronize();
-    for (int k = 0; k < 2; ++k)
+    for (int k = 0; k < 3; ++k)
         if (s->graph[k]) cudaGraphExecDestroy(s->graph[k]);
     for (void* p : s->allocs) cudaFree(p);
     delete s;
@@ -1985,9 +1987,12 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
     return st;
 }
 
-// Captures two middle steps into one graph, each with its conditional
-// re-binning node.  Needs cells_clean.
-static int capture_pair(MixedScene* s)
+// Step graphs of a scene: kFirstStep (the first step of a call, MODE 0),
+// kTwoSteps and kOneStep (middle steps, MODE 1); each step has its own
+// conditional re-binning node.
+enum { kFirstStep = 0, kTwoSteps = 1, kOneStep = 2 };
+
+static int capture_steps(MixedScene* s, int kind)
 {
     cudaStream_t cs = nullptr;
     cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
@@ -2000,44 +2005,60 @@ static int capture_pair(MixedScene* s)
         cudaStreamCaptureStatus cst;
         st = cuda_status(cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg), "mixed capture info");
     }
-    for (int k = 0; k < 2 && st == XD_OK; ++k)
+    const int nh = kind == kTwoSteps ? 2 : 1;
+    for (int k = 0; k < nh && st == XD_OK; ++k)
         st = cuda_status(cudaGraphConditionalHandleCreate(&h[k], cg, 0, cudaGraphCondAssignDefault),
                          "mixed conditional handle");
+    const bool clean = s->cells_clean;
     Phases none;
-    if (st == XD_OK) st = step_once<1>(s, cs, none, false, 0, &h[0]);
-    if (st == XD_OK) st = step_once<1>(s, cs, none, false, 0, &h[1]);
+    if (st == XD_OK) {
+        if (kind == kFirstStep) st = step_once<0>(s, cs, none, false, 0, &h[0]);
+        else st = step_once<1>(s, cs, none, false, 0, &h[0]);
+    }
+    if (st == XD_OK && kind == kTwoSteps) st = step_once<1>(s, cs, none, false, 0, &h[1]);
+    s->cells_clean = clean;   // capture only recorded the launches
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(cs, &g);
     if (st == XD_OK) st = cuda_status(e, "mixed graph capture");
-    if (st == XD_OK) st = cuda_status(cudaGraphInstantiate(&s->graph[0], g, 0), "mixed graph instantiate");
+    if (st == XD_OK) st = cuda_status(cudaGraphInstantiate(&s->graph[kind], g, 0), "mixed graph instantiate");
     if (g) cudaGraphDestroy(g);
     cudaStreamDestroy(cs);
     return st;
+}
+
+static int launch_steps(MixedScene* s, int kind, cudaStream_t q)
+{
+    if (!s->graph[kind]) {
+        int st = capture_steps(s, kind);
+        if (st != XD_OK) return st;
+    }
+    return cuda_status(cudaGraphLaunch(s->graph[kind], q), "mixed graph launch");
 }
 
 int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
 {
     if (nsteps == 0 || s->n == 0) return XD_OK;
     if (!s->ready) return set_error(XD_ERR_STATE, "mixed mode: no state uploaded");
-    const bool graphs = s->use_graphs && ph.fn == nullptr;
     int st = update_mesh(s, q);
     if (st != XD_OK) return st;
-    // step 1: the position update from the state's (v, a)
-    st = step_once<0>(s, q, ph, false, 0, nullptr);
-    if (st != XD_OK) return st;
-    unsigned t = 1;
-    // pairs of middle steps as one graph launch
-    while (graphs && nsteps - t >= 2) {
-        if (!s->graph[0]) {
-            st = capture_pair(s);
-            if (st != XD_OK) return st;
-        }
-        st = cuda_status(cudaGraphLaunch(s->graph[0], q), "mixed graph launch");
+    if (s->use_graphs && ph.fn == nullptr) {
+        // Every step in a graph, re-binning decided on the device: the call
+        // never waits for the GPU.  A scene without cells yet (after an
+        // upload) is made to re-bin through the same flag.
+        if (!s->cells_clean)
+            st = cuda_status(cudaMemsetAsync(s->counters + CN_REBUILD, 1, 1, q), "mixed re-binning flag");
+        if (st == XD_OK) st = launch_steps(s, kFirstStep, q);
+        unsigned t = 1;
+        for (; st == XD_OK && nsteps - t >= 2; t += 2) st = launch_steps(s, kTwoSteps, q);
+        if (st == XD_OK && t < nsteps) st = launch_steps(s, kOneStep, q);
         if (st != XD_OK) return st;
-        t += 2;
+        s->cells_clean = true;
+    } else {
+        // direct launches (phase timing): the host reads the re-binning flag
+        st = step_once<0>(s, q, ph, false, 0, nullptr);
+        for (unsigned t = 1; t < nsteps && st == XD_OK; ++t) st = step_once<1>(s, q, ph, false, 0, nullptr);
+        if (st != XD_OK) return st;
     }
-    for (; t < nsteps && st == XD_OK; ++t) st = step_once<1>(s, q, ph, false, 0, nullptr);
-    if (st != XD_OK) return st;
     // the last velocity update
     ph.begin(0, q);
     k_mx_finish<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[0], s->Fc, s->Mc);
@@ -2166,6 +2187,8 @@ int mixed_get_bodies(MixedScene* s, xd_polygon_mass_info* pmi, cudaStream_t q)
     if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "scene_get_bodies");
     return st;
 }
+
+unsigned long long mixed_device_bytes(MixedScene* s) { return s ? s->bytes : 0; }
 
 int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q)
 {

@@ -32,6 +32,7 @@ int mixed_eval_contacts(MixedScene* s, double* force, double* moment, cudaStream
 int mixed_pair_list(MixedScene* s, unsigned cap_per_particle, unsigned* counts, unsigned* partners,
                     cudaStream_t q);
 int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q);
+unsigned long long mixed_device_bytes(MixedScene* s);
 int mixed_set_bodies(MixedScene* s, const xd_polygon_mass_info* pmi, cudaStream_t q);
 int mixed_get_bodies(MixedScene* s, xd_polygon_mass_info* pmi, cudaStream_t q);
 

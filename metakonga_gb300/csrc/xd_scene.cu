@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -36,6 +37,7 @@ struct xd_scene {
     void* poly_scratch = nullptr;
     bool bodies_dirty = false;
     std::vector<void*> allocs;
+    unsigned long long bytes = 0;   // device memory held by the FP64 form
     // phase timing
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -58,6 +60,7 @@ int dalloc(xd_scene* s, T** p, size_t count)
     cudaError_t e = cudaMalloc(&q, sizeof(T) * count);
     if (e != cudaSuccess) return cuda_status(e, "scene allocation");
     s->allocs.push_back(q);
+    s->bytes += sizeof(T) * count;
     *p = static_cast<T*>(q);
     return XD_OK;
 }
@@ -137,6 +140,43 @@ struct PhaseSpan {
         s->spans.push_back({ phase, { b, e } });
     }
 };
+
+// Streams on which xd_scene_step_many runs its scenes side by side: kPoolStreams
+// non-blocking streams per device, made on first use and kept for the
+// process; the calls that use them take the mutex.
+constexpr int kPoolStreams = 16;
+constexpr int kPoolDevices = 64;
+
+struct StreamPool {
+    cudaStream_t s[kPoolStreams] = {};
+    cudaEvent_t done[kPoolStreams] = {};
+    cudaEvent_t start = nullptr;
+    bool ready = false;
+};
+
+std::mutex g_pool_mutex;
+StreamPool g_pools[kPoolDevices];
+
+int pool_of_current_device(StreamPool** out)
+{
+    int dev = 0;
+    int st = cuda_status(cudaGetDevice(&dev), "step_many device");
+    if (st != XD_OK) return st;
+    if (dev < 0 || dev >= kPoolDevices) return set_error(XD_ERR_INVALID, "step_many: device ordinal out of range");
+    StreamPool& p = g_pools[dev];
+    if (!p.ready) {
+        st = cuda_status(cudaEventCreateWithFlags(&p.start, cudaEventDisableTiming), "step_many events");
+        for (int k = 0; k < kPoolStreams && st == XD_OK; ++k) {
+            st = cuda_status(cudaStreamCreateWithFlags(&p.s[k], cudaStreamNonBlocking), "step_many streams");
+            if (st == XD_OK)
+                st = cuda_status(cudaEventCreateWithFlags(&p.done[k], cudaEventDisableTiming), "step_many events");
+        }
+        if (st != XD_OK) return st;
+        p.ready = true;
+    }
+    *out = &p;
+    return XD_OK;
+}
 
 }  // namespace
 
@@ -573,6 +613,41 @@ int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
         if (e != cudaSuccess) return cuda_status(e, "scene_step check");
         if (herr) return set_error(XD_ERR_INVALID, "scene_step: a hash value was >= ncell");
     }
+    return XD_OK;
+}
+
+int xd_scene_step_many(xd_scene* const* scenes, const unsigned* nsteps, unsigned count, int check, void* stream)
+{
+    if (count == 0) return XD_OK;
+    if (!scenes || !nsteps) return set_error(XD_ERR_INVALID, "scene_step_many: null array");
+    for (unsigned i = 0; i < count; ++i)
+        if (!scenes[i]) return set_error(XD_ERR_INVALID, "scene_step_many: null scene");
+    cudaStream_t q = static_cast<cudaStream_t>(stream);
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    StreamPool* p = nullptr;
+    int st = pool_of_current_device(&p);
+    if (st != XD_OK) return st;
+    // the pool streams start after the work already queued on `stream`
+    st = cuda_status(cudaEventRecord(p->start, q), "scene_step_many");
+    const unsigned used = count < (unsigned)kPoolStreams ? count : (unsigned)kPoolStreams;
+    for (unsigned k = 0; k < used && st == XD_OK; ++k)
+        st = cuda_status(cudaStreamWaitEvent(p->s[k], p->start, 0), "scene_step_many");
+    for (unsigned i = 0; i < count && st == XD_OK; ++i)
+        st = xd_scene_step(scenes[i], nsteps[i], 0, p->s[i % kPoolStreams]);
+    // `stream` continues after every scene, also when a launch failed
+    for (unsigned k = 0; k < used; ++k) {
+        int e = cuda_status(cudaEventRecord(p->done[k], p->s[k]), "scene_step_many");
+        if (e == XD_OK) e = cuda_status(cudaStreamWaitEvent(q, p->done[k], 0), "scene_step_many");
+        if (st == XD_OK) st = e;
+    }
+    if (st == XD_OK && check) st = cuda_status(cudaStreamSynchronize(q), "scene_step_many");
+    return st;
+}
+
+int xd_scene_device_bytes(xd_scene* s, unsigned long long* bytes)
+{
+    if (!s || !bytes) return set_error(XD_ERR_INVALID, "scene_device_bytes: null argument");
+    *bytes = s->bytes + (s->mixed ? mixed_device_bytes(s->mixed) : 0ull);
     return XD_OK;
 }
 

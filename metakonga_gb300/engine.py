@@ -161,6 +161,12 @@ class DeviceScene:
     def launches(self, nsteps: int) -> int:
         return int(_lib.lib().xd_scene_launches(self.handle, nsteps))
 
+    def device_bytes(self) -> int:
+        """Device memory the scene holds, in bytes."""
+        out = np.zeros(1, np.uint64)
+        call("xd_scene_device_bytes", self.handle, out.ctypes.data)
+        return int(out[0])
+
     def close(self):
         if getattr(self, "handle", None) is not None and self.handle.value:
             call("xd_scene_destroy", self.handle)
@@ -171,3 +177,22 @@ class DeviceScene:
             self.close()
         except Exception:
             pass
+
+
+def step_many(scenes, nsteps, check: bool = False, stream: int = 0) -> None:
+    """Advance several DeviceScenes side by side (xd_scene_step_many): scene
+    k by nsteps[k] steps (an int applies to all).  Each result equals the one
+    the scene's own step gives alone."""
+    scenes = list(scenes)
+    k = len(scenes)
+    if k == 0:
+        return
+    if isinstance(nsteps, (int, np.integer)):
+        nsteps = [int(nsteps)] * k
+    if len(nsteps) != k:
+        raise ValueError("step_many: one step count per scene")
+    if len({id(s) for s in scenes}) != k:
+        raise ValueError("step_many: a scene appears twice")
+    handles = (C.c_void_p * k)(*[s.handle.value for s in scenes])
+    counts = np.ascontiguousarray(nsteps, dtype=np.uint32)
+    call("xd_scene_step_many", C.cast(handles, C.c_void_p), counts.ctypes.data, k, 1 if check else 0, stream)

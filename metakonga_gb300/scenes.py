@@ -13,6 +13,10 @@ material constants of the benchmark scenes:
                    walls, dt = 5e-6 s.
 * ``drum``         spheres inside a closed, tessellated cylinder that rotates
                    about its axis (particle-triangle contacts).
+* ``hopper``       spheres in a 60-degree conical hopper of 4,096 triangles
+                   above a plane floor, r ~ U[2, 4] mm, orifice of 6-12
+                   particle diameters; ``hopper_batch`` draws the batch of
+                   independent hoppers (log-uniform particle counts).
 
 Every scene carries the state arrays the reference's dem_simulation allocates
 (dem_simulation.cpp:174-199, 232-251): pos (x, y, z, r) as double4, vel, acc,
@@ -380,3 +384,150 @@ def drum(n: int = 4000, seed: int = 11, rmin: float = 0.003, rmax: float = 0.005
 def euler_parameters_about_y(angle: float):
     """Euler parameters (e0, e1, e2, e3) of a rotation by ``angle`` about y."""
     return (math.cos(angle / 2), 0.0, math.sin(angle / 2), 0.0)
+
+
+def cone_mesh(r_bottom: float, r_top: float, z_bottom: float, height: float, n_theta: int = 64,
+              n_z: int = 32) -> np.ndarray:
+    """Open cone frustum about the z axis from radius r_bottom at z_bottom to
+    r_top at z_bottom + height: n_theta x n_z quads, two triangles each
+    (64 x 32 x 2 = 4,096 by default), (T, 3, 3).  Every triangle is wound so
+    that (Q - P) x (R - P) points towards the axis, the side the particles
+    are on."""
+    th = np.linspace(0.0, 2 * np.pi, n_theta + 1)[:-1]
+    ct, st_ = np.cos(th), np.sin(th)
+    tris = np.empty((n_z, n_theta, 2, 3, 3))
+    for j in range(n_z):
+        z0 = z_bottom + height * j / n_z
+        z1 = z_bottom + height * (j + 1) / n_z
+        r0 = r_bottom + (r_top - r_bottom) * j / n_z
+        r1 = r_bottom + (r_top - r_bottom) * (j + 1) / n_z
+        i1 = (np.arange(n_theta) + 1) % n_theta
+        a = np.stack([r0 * ct, r0 * st_, np.full(n_theta, z0)], axis=1)
+        b = np.stack([r0 * ct[i1], r0 * st_[i1], np.full(n_theta, z0)], axis=1)
+        c = np.stack([r1 * ct[i1], r1 * st_[i1], np.full(n_theta, z1)], axis=1)
+        d = np.stack([r1 * ct, r1 * st_, np.full(n_theta, z1)], axis=1)
+        tris[j, :, 0] = np.stack([a, b, c], axis=1)
+        tris[j, :, 1] = np.stack([a, c, d], axis=1)
+    tri = tris.reshape(-1, 3, 3)
+    n = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    inward = -tri.mean(axis=1)
+    inward[:, 2] = 0.0
+    flip = np.einsum("ij,ij->i", n, inward) < 0
+    tri[flip] = tri[flip][:, [0, 2, 1]]
+    return tri
+
+
+def _mesh_arrays(tri: np.ndarray, body: int = 0):
+    """POLYGON records, circumspheres and body-frame vertex list of a mesh."""
+    T = tri.shape[0]
+    cen = circumcentre(tri[:, 0], tri[:, 1], tri[:, 2])
+    trad = np.linalg.norm(cen - tri[:, 0], axis=1)
+    poly = np.zeros(T, dtype=POLYGON)
+    poly["id"] = body
+    poly["P"], poly["Q"], poly["R"] = tri[:, 0], tri[:, 1], tri[:, 2]
+    poly["V"] = tri[:, 1] - tri[:, 0]
+    poly["W"] = tri[:, 2] - tri[:, 0]
+    poly["N"] = np.cross(poly["V"], poly["W"])
+    sphere = np.empty((T, 4))
+    sphere[:, :3] = cen
+    sphere[:, 3] = trad
+    return poly, sphere, tri.reshape(T, 9).copy()
+
+
+def hopper(n: int = 20_000, seed: int = 3, orifice: float = 8.0, fric: float = 0.4,
+           rmin: float = 0.002, rmax: float = 0.004, wall_angle_deg: float = 60.0,
+           n_theta: int = 64, n_z: int = 32, steps: int = 10_000, dt: float = 5.0e-6,
+           packing: float = 0.25) -> Scene:
+    """Hopper discharge: n spheres, r ~ U[rmin, rmax], on a jittered cubic
+    lattice (no overlaps) inside a conical hopper whose wall rises at
+    ``wall_angle_deg`` from the horizontal; the orifice (at z = 0) is
+    ``orifice`` mean particle diameters wide and open, with a plane floor
+    below it.  The cone is a fixed polygon body of n_theta x n_z x 2
+    triangles; its top radius is chosen so that the spheres (the lattice
+    pitch gives the packing fraction, at most ``packing``) fill the lower 60%
+    of its volume.  Particle-particle friction is ``fric``, as is the wall's."""
+    rng = _rng(seed)
+    d_mean = rmin + rmax
+    r_o = 0.5 * orifice * d_mean
+    slope = math.tan(math.radians(wall_angle_deg))
+    mean_vol = math.pi * (rmax ** 4 - rmin ** 4) / (3.0 * (rmax - rmin))
+    # jittered cubic lattice: pitch >= 2 rmax, so that no two spheres overlap
+    pitch = max(2.04 * rmax, (mean_vol / packing) ** (1.0 / 3.0))
+    sin_a = math.sin(math.radians(wall_angle_deg))
+    margin = 0.05 * rmin
+
+    def usable(rt):
+        h = (rt - r_o) * slope
+        return math.pi * h / 3.0 * (r_o * r_o + r_o * rt + rt * rt)
+
+    def radius_holding(vol):
+        lo_r, hi_r = r_o, 1.0
+        while usable(hi_r) < vol:
+            hi_r *= 2.0
+        for _ in range(60):
+            mid = 0.5 * (lo_r + hi_r)
+            if usable(mid) >= vol:
+                hi_r = mid
+            else:
+                lo_r = mid
+        return hi_r
+
+    def sites(r_fill):
+        """Lattice sites of the cone below radius r_fill whose ball of
+        radius pitch / 2 stays off the wall and above the orifice plane."""
+        z_fill = (r_fill - r_o) * slope
+        k = int(math.ceil(r_fill / pitch))
+        g = np.arange(-k, k + 1) * pitch
+        zs = np.arange(0.5 * pitch + margin, z_fill, pitch)
+        X, Y, Z = np.meshgrid(g, g, zs, indexing="ij")
+        p = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+        # the facets lie inside the smooth cone by up to r (1 - cos(pi / n_theta))
+        inner = (r_o + p[:, 2] / slope) * math.cos(math.pi / n_theta)
+        room = (inner - np.hypot(p[:, 0], p[:, 1])) * sin_a
+        return p[room > 0.5 * pitch + margin]
+
+    r_fill = radius_holding(n * pitch ** 3)
+    cand = sites(r_fill)
+    while cand.shape[0] < n:
+        r_fill *= 1.03
+        cand = sites(r_fill)
+    r_top = max(radius_holding(usable(r_fill) / 0.6), r_fill + 2.0 * pitch)
+    height = (r_top - r_o) * slope
+    tri = cone_mesh(r_o, r_top, 0.0, height, n_theta, n_z)
+    poly, sphere, vlist = _mesh_arrays(tri)
+    # the lowest n sites (ties in lattice order), each with a random radius and
+    # a jitter that keeps every pair apart: |shift| <= pitch / 2 - r
+    order = np.argsort(cand[:, 2], kind="stable")[:n]
+    pts = cand[np.sort(order)]
+    rad = rng.uniform(rmin, rmax, size=n)
+    amp = (0.5 * pitch - rad) / math.sqrt(3.0)
+    pts = pts + rng.uniform(-1.0, 1.0, size=(n, 3)) * amp[:, None]
+    pos = np.empty((n, 4), dtype=np.float64)
+    pos[:, :3] = pts
+    pos[:, 3] = rad
+    pmi = np.zeros(1, dtype=POLYGON_MASS)
+    pmi["ep"] = (1.0, 0.0, 0.0, 0.0)
+    cp = _default_property(fric=fric)
+    zf = -max(0.1, 10.0 * d_mean)
+    w = r_top + 0.1
+    floor = define_plane((-w, -w, zf), (w, -w, zf), (w, w, zf), (-w, w, zf))
+    planes = np.array([floor], dtype=PLANE)
+    maxr = max(rmax, float(sphere[:, 3].max()))
+    return Scene(name="hopper", seed=seed, dt=dt, steps=steps,
+                 params=_reference_grid(maxr, n, dt), pos=pos, **_state(pos),
+                 cp_pp=cp, planes=planes, plane_names=["floor"],
+                 cp_planes=np.array([cp], dtype=CONTACT_PROPERTY), poly=poly, sphere=sphere,
+                 vlist=vlist, pmi=pmi, cp_poly=np.array([cp], dtype=CONTACT_PROPERTY))
+
+
+def hopper_batch(count: int = 256, seed: int = 1, n_min: int = 2_000, n_max: int = 200_000):
+    """Parameters of a batch of independent hoppers: particle count
+    log-uniform in [n_min, n_max], orifice U[6, 12] diameters, friction
+    U[0.2, 0.6], one seed each.  Returns a list of keyword dicts for
+    ``hopper``."""
+    rng = _rng(seed)
+    ns = np.exp(rng.uniform(math.log(n_min), math.log(n_max), size=count)).astype(np.int64)
+    orif = rng.uniform(6.0, 12.0, size=count)
+    mu = rng.uniform(0.2, 0.6, size=count)
+    return [dict(n=int(ns[k]), seed=seed * 100_003 + k, orifice=float(orif[k]), fric=float(mu[k]))
+            for k in range(count)]

@@ -1,0 +1,189 @@
+"""Serving many DEM scenes on one GPU: admission by device memory, continuous
+batching of their steps.
+
+A ``Server`` takes requests (a scene and a step count) that arrive over time.
+It admits a request as soon as the device memory the scene will hold fits in
+the budget next to the scenes already resident, then advances every resident
+scene by up to ``chunk`` steps per tick in one ``engine.step_many`` call: the
+scenes' kernels run side by side on the library's stream pool, so requests
+that arrive while others run join the next tick instead of waiting for the
+GPU to drain.  A scene whose steps are done is downloaded and freed, which
+makes room for the next request.  Each result is the one the scene gives when
+stepped alone (the step sequence of a scene does not depend on how its steps
+are split into calls or on what runs beside it).
+
+The reference runs one model per process (xDynamicsSolver); this loop has no
+counterpart there.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+import time
+
+import numpy as np
+
+from . import engine
+
+_MIXED_PER_PARTICLE = 1100     # bytes: two state copies, view, lists, sort, transfer buffer
+_FP64_PER_PARTICLE = 320       # bytes: reference layouts, grid arrays, sort scratch
+_PER_TRIANGLE = 512            # bytes: records, circumspheres, vertex lists, cell ranges
+
+
+def _mixed_cells(sc) -> tuple:
+    """Cells of the mixed form's grid and its cell size (the rule of
+    mixed_setup: bounding box of particles, planes and triangles, 4 r_max
+    padding, cell = 2.002 r_max + skin + extent 2^-19, two margin cells)."""
+    pts = [sc.pos[:, :3]]
+    if sc.planes.shape[0]:
+        for f in ("xw", "w2", "w3", "w4"):
+            pts.append(np.asarray(sc.planes[f]).reshape(-1, 3))
+    if sc.ntri:
+        pts.append(sc.vlist.reshape(-1, 3))
+    p = np.concatenate(pts)
+    lo, hi = p.min(axis=0), p.max(axis=0)
+    rmax = float(sc.pos[:, 3].max()) if sc.np_ else 0.5
+    extent = float((hi - lo + 8.0 * rmax).max())
+    cs = 2.0 * rmax * 1.001 + 0.1 * rmax + extent * 2.0 ** -19
+    g = np.ceil((hi - lo + 4.0 * cs) / cs) + 3
+    return float(np.prod(g)), cs, rmax
+
+
+def estimate_device_bytes(sc, mode: int = engine.MODE_MIXED) -> int:
+    """Upper estimate of the device memory a DeviceScene of `sc` holds once
+    uploaded (what the server books against its budget)."""
+    n, t = sc.np_, sc.ntri
+    nb = 0 if not t else int(sc.pmi.shape[0])
+    if mode == engine.MODE_MIXED:
+        ncell, cs, rmax = _mixed_cells(sc)
+        total = n * _MIXED_PER_PARTICLE + 8.0 * ncell
+        if t:
+            tri = sc.vlist.reshape(-1, 3, 3)
+            edge = float(np.linalg.norm(tri - np.roll(tri, 1, axis=1), axis=2).max())
+            reach = 2.0 * (1.1 * rmax + 1e-4)
+            span = math.ceil((edge + 2.0 * reach) / cs) + 1.0
+            # cell-triangle table (keys, triangles, sort buffers), per-particle
+            # triangle lists and per-body reaction slots
+            total += t * _PER_TRIANGLE + t * span ** 3 * 20.0 + n * (4 + 64 + 48 * nb)
+    else:
+        ncell = float(sc.params["ncell"])
+        total = n * _FP64_PER_PARTICLE + t * (_PER_TRIANGLE + 16) + 8.0 * ncell
+    return int(1.1 * total) + (4 << 20)
+
+
+@dataclasses.dataclass
+class Request:
+    rid: object
+    scene: object
+    steps: int
+    arrival: float                       # seconds after the server's start
+    bytes: int = 0
+    admitted: float = math.nan
+    done: float = math.nan
+    remaining: int = 0
+    handle: object = None
+    result: dict = None
+
+
+class Server:
+    """Continuous-batching DEM server on the current CUDA device.
+
+    budget_bytes: device memory the resident scenes may hold together (a
+    request larger than the budget is admitted alone when nothing else is
+    resident).  chunk: steps per scene per tick; smaller chunks admit new
+    requests sooner, larger ones cost fewer host round trips."""
+
+    def __init__(self, budget_bytes: int, chunk: int = 20, mode: int = engine.MODE_MIXED,
+                 stream: int = 0, keep_results: bool = True, clock=time.perf_counter):
+        if chunk < 1:
+            raise ValueError("chunk must be >= 1")
+        self.budget = int(budget_bytes)
+        self.chunk = int(chunk)
+        self.mode = mode
+        self.stream = stream
+        self.keep_results = keep_results
+        self.clock = clock
+        self.pending: list = []
+        self.finished: list = []
+        self.used = 0
+        self.peak_used = 0
+        self.ticks = 0
+        self.peak_active = 0
+        self.wall = 0.0
+
+    def submit(self, rid, scene, steps: int, arrival: float = 0.0) -> None:
+        if steps < 1:
+            raise ValueError("a request needs at least one step")
+        self.pending.append(Request(rid=rid, scene=scene, steps=int(steps), arrival=float(arrival),
+                                    bytes=estimate_device_bytes(scene, self.mode),
+                                    remaining=int(steps)))
+
+    def _admit(self, now: float, active: list, t0: float) -> None:
+        # first come, first served: a request that does not fit holds back the
+        # ones behind it, so that a large request is not starved
+        while self.pending and self.pending[0].arrival <= now:
+            r = self.pending[0]
+            if active and self.used + r.bytes > self.budget:
+                break
+            self.pending.pop(0)
+            r.handle = engine.DeviceScene(r.scene, mode=self.mode)
+            r.admitted = self.clock() - t0
+            self.used += r.bytes
+            self.peak_used = max(self.peak_used, self.used)
+            active.append(r)
+
+    def run(self) -> list:
+        """Serve every submitted request; returns them in completion order."""
+        self.pending.sort(key=lambda r: r.arrival)
+        active: list = []
+        t0 = self.clock()
+        while self.pending or active:
+            now = self.clock() - t0
+            self._admit(now, active, t0)
+            if not active:
+                time.sleep(max(0.0, self.pending[0].arrival - (self.clock() - t0)))
+                continue
+            self.peak_active = max(self.peak_active, len(active))
+            counts = [min(self.chunk, r.remaining) for r in active]
+            engine.step_many([r.handle for r in active], counts, check=True, stream=self.stream)
+            self.ticks += 1
+            now = self.clock() - t0
+            still = []
+            for r, c in zip(active, counts):
+                r.remaining -= c
+                if r.remaining:
+                    still.append(r)
+                    continue
+                if self.keep_results:
+                    r.result = r.handle.download(self.stream)
+                r.handle.close()
+                r.handle = None
+                r.done = self.clock() - t0
+                self.used -= r.bytes
+                self.finished.append(r)
+            active = still
+        self.wall = self.clock() - t0
+        return self.finished
+
+    def report(self) -> dict:
+        """Completion latency (arrival to result) percentiles in ms, waiting
+        time before admission, and the aggregate particle-steps/s."""
+        if not self.finished:
+            return {"requests": 0}
+        lat = np.array([r.done - r.arrival for r in self.finished]) * 1e3
+        wait = np.array([r.admitted - r.arrival for r in self.finished]) * 1e3
+        work = float(sum(r.scene.np_ * r.steps for r in self.finished))
+        return {"requests": len(self.finished),
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "p50_wait_ms": float(np.percentile(wait, 50)),
+                "p99_wait_ms": float(np.percentile(wait, 99)),
+                "particle_steps": work, "wall_s": self.wall,
+                "particle_steps_per_s": work / self.wall if self.wall > 0 else 0.0,
+                "ticks": self.ticks, "peak_active": self.peak_active,
+                "peak_booked_bytes": self.peak_used}
+
+
+def poisson_arrivals(count: int, rate: float, seed: int = 0) -> np.ndarray:
+    """Arrival times (s) of a Poisson stream of `rate` requests per second."""
+    rng = np.random.Generator(np.random.MT19937(seed))
+    return np.cumsum(rng.exponential(1.0 / rate, size=count))

@@ -57,3 +57,29 @@ def small_drum(n=600, seed=5):
     sc.omega[:] = rng.normal(0.0, 5.0, sc.omega.shape)
     sc.pmi["vel"] = (0.01, -0.02, 0.005)
     return sc
+
+
+def small_hopper(n=1500, seed=5):
+    """A small hopper (4,096 triangles, r_top ~0.1 m) whose outer spheres are
+    pushed into the cone wall: each sphere within two diameters of the wall
+    is moved out radially until its gap to the smooth cone is -r U[0, 0.4]
+    .. +0.05 r, so that faces, edges and vertices of the facets are touched."""
+    sc = scenes.hopper(n=n, seed=seed, orifice=7.0, fric=0.3)
+    rng = np.random.Generator(np.random.MT19937(seed + 11))
+    tri = sc.vlist.reshape(-1, 3, 3)
+    r_o = np.hypot(tri[:, :, 0], tri[:, :, 1]).min()
+    slope = np.tan(np.radians(60.0))
+    sin_a = np.sin(np.radians(60.0))
+    rho = np.hypot(sc.pos[:, 0], sc.pos[:, 1])
+    r_z = r_o + sc.pos[:, 2] / slope
+    room = (r_z - rho) * sin_a
+    r = sc.pos[:, 3]
+    outer = (room < 4.0 * r) & (rho > 1e-6)
+    target = r * rng.uniform(0.6, 1.05, size=sc.np_)
+    new_rho = r_z - target / sin_a
+    scale = np.where(outer, new_rho / np.maximum(rho, 1e-9), 1.0)
+    sc.pos[:, 0] *= scale
+    sc.pos[:, 1] *= scale
+    sc.vel[:] = rng.normal(0.0, 0.05, sc.vel.shape)
+    sc.omega[:] = rng.normal(0.0, 5.0, sc.omega.shape)
+    return sc

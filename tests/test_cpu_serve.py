@@ -1,0 +1,179 @@
+"""Host logic of the serving loop, with the device calls replaced by fakes:
+first-come-first-served admission under the memory budget, continuous
+batching (late arrivals join running scenes), chunked step counts, the
+latency report, and the memory estimate's growth with the scene."""
+import numpy as np
+import pytest
+
+from metakonga_gb300 import engine, scenes, serve
+
+from .cases import packed_scene
+
+
+class _FakeScene:
+    live = 0
+
+    def __init__(self, sc, mode=engine.MODE_MIXED):
+        self.sc = sc
+        self.steps = 0
+        _FakeScene.live += 1
+
+    def download(self, stream=0):
+        return {"steps": self.steps}
+
+    def close(self):
+        _FakeScene.live -= 1
+
+
+class _Clock:
+    """Deterministic clock: each tick of the fake batch advances 1 ms."""
+
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        return self.t
+
+
+@pytest.fixture
+def fake(monkeypatch):
+    clock = _Clock()
+    calls = []
+
+    def step_many(handles, counts, check=False, stream=0):
+        calls.append([(h.sc.name, c) for h, c in zip(handles, counts)])
+        for h, c in zip(handles, counts):
+            h.steps += c
+        clock.t += 1e-3
+
+    monkeypatch.setattr(engine, "DeviceScene", _FakeScene)
+    monkeypatch.setattr(engine, "step_many", step_many)
+    monkeypatch.setattr(serve.time, "sleep", lambda s: setattr(clock, "t", clock.t + max(s, 0.0)))
+    _FakeScene.live = 0
+    return clock, calls
+
+
+def _named(name, n_side=4):
+    sc = packed_scene(n_side=n_side)
+    sc.name = name
+    return sc
+
+
+def test_chunks_and_results(fake):
+    clock, calls = fake
+    srv = serve.Server(budget_bytes=1 << 40, chunk=4, clock=clock)
+    srv.submit("a", _named("a"), 10)
+    srv.submit("b", _named("b"), 3)
+    done = srv.run()
+    assert [r.rid for r in done] == ["b", "a"]
+    assert calls[0] == [("a", 4), ("b", 3)]
+    assert calls[1] == [("a", 4)] and calls[2] == [("a", 2)]
+    assert all(r.result["steps"] == r.steps for r in done)
+    assert _FakeScene.live == 0 and srv.used == 0
+
+
+def test_late_arrival_joins_running_batch(fake):
+    clock, calls = fake
+    srv = serve.Server(budget_bytes=1 << 40, chunk=2, clock=clock)
+    srv.submit("a", _named("a"), 20, arrival=0.0)
+    srv.submit("b", _named("b"), 4, arrival=0.0035)
+    done = srv.run()
+    # b arrives during a's fourth tick and runs beside a from the fifth
+    assert calls[3] == [("a", 2)]
+    assert calls[4] == [("a", 2), ("b", 2)]
+    assert [r.rid for r in done] == ["b", "a"]
+    rep = srv.report()
+    assert rep["peak_active"] == 2
+    b = done[0]
+    assert b.admitted == pytest.approx(0.004)
+    assert b.done - b.arrival == pytest.approx(0.0025)
+
+
+def test_budget_is_first_come_first_served(fake):
+    clock, calls = fake
+    big, small = _named("big", 6), _named("s2", 3)
+    eb, es = serve.estimate_device_bytes(big), serve.estimate_device_bytes(small)
+    srv = serve.Server(budget_bytes=eb + es - 1, chunk=5, clock=clock)
+    srv.submit("s1", _named("s1", 3), 5, arrival=0.0)
+    srv.submit("big", big, 5, arrival=0.0)
+    srv.submit("s2", small, 5, arrival=0.0)
+    done = srv.run()
+    # big does not fit beside s1, and s2 may not overtake it
+    assert calls[0] == [("s1", 5)]
+    assert calls[1] == [("big", 5)]
+    assert calls[2] == [("s2", 5)]
+    assert [r.rid for r in done] == ["s1", "big", "s2"]
+    assert srv.peak_used <= srv.budget
+
+
+def test_oversized_request_runs_alone(fake):
+    clock, calls = fake
+    srv = serve.Server(budget_bytes=1, chunk=5, clock=clock)
+    srv.submit("x", _named("x"), 5)
+    srv.submit("y", _named("y"), 5)
+    done = srv.run()
+    assert [r.rid for r in done] == ["x", "y"]
+    assert all(len(c) == 1 for c in calls)
+
+
+def test_idle_server_waits_for_arrivals(fake):
+    clock, calls = fake
+    srv = serve.Server(budget_bytes=1 << 40, chunk=5, clock=clock)
+    srv.submit("late", _named("late"), 5, arrival=2.0)
+    done = srv.run()
+    assert done[0].admitted >= 2.0
+    assert srv.report()["p50_wait_ms"] < 1.0
+
+
+def test_report_percentiles(fake):
+    clock, _ = fake
+    srv = serve.Server(budget_bytes=1 << 40, chunk=1, clock=clock)
+    for k in range(10):
+        srv.submit(k, _named(str(k)), k + 1)
+    srv.run()
+    rep = srv.report()
+    lat = sorted(r.done - r.arrival for r in srv.finished)
+    assert rep["p50_ms"] == pytest.approx(np.percentile(np.array(lat) * 1e3, 50))
+    assert rep["p99_ms"] >= rep["p50_ms"]
+    assert rep["particle_steps"] == sum(64 * (k + 1) for k in range(10))
+
+
+def test_estimate_grows_with_the_scene():
+    small, large = scenes.hopper(n=2000, seed=1), scenes.hopper(n=20000, seed=1)
+    for mode in (engine.MODE_MIXED, engine.MODE_FP64):
+        a, b = serve.estimate_device_bytes(small, mode), serve.estimate_device_bytes(large, mode)
+        assert 0 < a < b
+
+
+def test_poisson_arrivals():
+    t = serve.poisson_arrivals(20000, rate=50.0, seed=3)
+    assert np.all(np.diff(t) > 0)
+    assert abs(t[-1] / 20000 - 1 / 50.0) < 1e-3
+
+
+def test_hopper_batch_ranges():
+    b = scenes.hopper_batch(count=256, seed=1)
+    ns = np.array([d["n"] for d in b])
+    assert len(b) == 256 and ns.min() >= 2000 and ns.max() <= 200000
+    assert all(6.0 <= d["orifice"] <= 12.0 and 0.2 <= d["fric"] <= 0.6 for d in b)
+
+
+def test_hopper_geometry():
+    sc = scenes.hopper(n=3000, seed=2)
+    tri = sc.vlist.reshape(-1, 3, 3)
+    assert tri.shape[0] == 4096
+    # facet normals point at the axis, and no sphere starts inside the wall
+    nrm = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    cen = tri.mean(axis=1)
+    cen[:, 2] = 0.0
+    assert np.all(np.einsum("ij,ij->i", nrm, -cen) > 0)
+    u = nrm / np.linalg.norm(nrm, axis=1, keepdims=True)
+    d = np.einsum("tj,ij->it", u, sc.pos[:, :3]) - np.einsum("tj,tj->t", u, tri[:, 0])[None, :]
+    # the faceted cone is convex: the smallest signed distance to the facet
+    # planes is the gap to the wall
+    gap = d.min(axis=1) - sc.pos[:, 3]
+    assert gap.min() > 0
+    from scipy.spatial import cKDTree
+    pr = cKDTree(sc.pos[:, :3]).query_pairs(0.008, output_type="ndarray")
+    dist = np.linalg.norm(sc.pos[pr[:, 0], :3] - sc.pos[pr[:, 1], :3], axis=1)
+    assert np.all(dist >= sc.pos[pr[:, 0], 3] + sc.pos[pr[:, 1], 3])

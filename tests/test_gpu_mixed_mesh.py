@@ -1,7 +1,8 @@
 """Triangle meshes in the mixed form against the FP64 oracle.
 
 The drum case presses spheres against a coarse cylinder mesh (face, edge and
-vertex contacts).  Gates: particle pair lists equal the oracle's; per-particle
+vertex contacts); the hopper case presses them against a 4,096-triangle cone
+above a plane floor.  Gates: particle pair lists equal the oracle's; per-particle
 contact force (pairs + triangles) within 2e-5 of max(sum_c |F_c|, m g), the sum
 over every contact of the particle, triangles included; the
 reaction on the polygon body after one step within 1e-9 of its scale (the
@@ -13,7 +14,7 @@ import pytest
 from metakonga_gb300 import engine
 from metakonga_gb300.scenes import euler_parameters_about_y
 
-from .cases import small_drum
+from .cases import small_drum, small_hopper
 from .test_gpu_mixed import FORCE_TOL, _norm_err, _pairset
 
 pytestmark = pytest.mark.gpu
@@ -32,6 +33,8 @@ def _oracle_mesh_view(oracle, sc, st, poly=None, sphere=None):
     f = np.zeros((sc.np_, 3))
     m = np.zeros((sc.np_, 3))
     oracle.p2p(p, pos, vel, om, f, m, sc.mass, so, cs, ce, sc.cp_pp)
+    for i in range(sc.planes.shape[0]):
+        oracle.plane(p, sc.planes[i:i + 1], pos, vel, om, f, m, sc.mass, sc.cp_planes[i:i + 1])
     pmi = sc.pmi.copy()
     pmi["force"] = 0
     pmi["moment"] = 0
@@ -53,6 +56,23 @@ def test_mixed_drum_pairs_and_forces(cuda, oracle):
     pairs_ref, f_ref, m_ref, mag, _ = _oracle_mesh_view(oracle, sc, st)
     # the case must exercise the mesh: compare against forces without triangles
     assert np.abs(f_ref).max() > 0
+    pairs = ds.pair_list(cap=48)
+    f, m = ds.eval_contacts()
+    ds.close()
+    assert _pairset(pairs) == _pairset(pairs_ref)
+    assert _norm_err(f, f_ref, mag, sc.mass) <= FORCE_TOL
+    r = sc.pos[:, 3:4]
+    assert _norm_err(m / r, m_ref / r, mag, sc.mass) <= FORCE_TOL
+
+
+def test_mixed_hopper_pairs_and_forces(cuda, oracle):
+    sc = small_hopper()
+    ds = engine.DeviceScene(sc, mode=engine.MODE_MIXED)
+    ds.step(2)
+    st = ds.download()
+    pairs_ref, f_ref, m_ref, mag, pmi = _oracle_mesh_view(oracle, sc, st)
+    # the case must exercise the cone: the body takes a reaction
+    assert np.abs(pmi["force"]).max() > 0
     pairs = ds.pair_list(cap=48)
     f, m = ds.eval_contacts()
     ds.close()
