@@ -1,33 +1,51 @@
 """Benchmark: particle-steps/s of the DEM contact step on one GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload batched|served|box]
 
-Workload: the polydisperse settle -- 1,000,000 spheres, r ~ U[2, 4] mm,
-rejection-sampled without overlap in a 1 x 1 x 2 m box of five plane walls,
-dt = 5e-6 s, the reference's grid (origin -1, 128^3 cells of 2 x r_max), seeded
-synthetic input.  A step is one whole DEM step (VV position, hash, sort, cell
-ranges, particle-particle, planes, VV velocity).
+Workloads (seeded synthetic input; every scene is generated here):
+  batched  (default) 256 independent hopper-discharge scenes: particle counts
+           log-uniform in [2,000, 200,000] (11.56 M spheres in all), r ~ U[2, 4]
+           mm, a 60-degree cone of 4,096 triangles above a plane floor, orifice
+           U[6, 12] diameters, friction U[0.2, 0.6], dt = 5e-6 s.  A step
+           advances every scene by one time step; the scenes run side by side
+           (xd_scene_step_many) in the mixed form.
+  served   a Poisson stream of settle-box and hopper requests, particle counts
+           log-uniform in [1,000, 500,000], step counts U[1,000, 20,000],
+           admitted under a 150 GB device-memory budget by the continuous-
+           batching server; p50/p99 completion latency and particle-steps/s.
+  box      the 1,000,000-sphere polydisperse settle (r ~ U[2, 4] mm in a
+           1 x 1 x 2 m box of five plane walls, dt = 5e-6 s), one scene.
 
-Our arm (default) prints one JSON line with:
-  value      particle-steps/s with the state resident in HBM (device timed,
-             CUDA events on the launching stream; the state, ~190 MB, is
-             larger than L2, so no flush is needed between steps);
-  e2e        the same metric through the C ABI with host buffers: every step
-             uploads the evolving state from pinned host memory, steps once
-             and downloads pos/vel/omega/acc/alpha;
-  roofline   the particle-particle kernel's algorithmic bytes (140 B/particle)
-             over its live event-timed duration vs the measured HBM peak;
-  cpu_baseline  the reference's CPU path (restated in the oracle, single
-             thread) on a bounded sample of the same scene.
---impl reference runs that CPU path on the host cores instead (one scene
-replica per core) and prints the same metric.
-Under torchrun each rank advances its own replica (scenes shard with no
-exchange); value is the sum over ranks over the max rank time.
+The default (batched) line carries:
+  value        particle-steps/s of the batch, device-timed (CUDA events on
+               the launching stream; the batch's state, ~15 GB, is far larger
+               than L2, so no flush is needed between steps);
+  e2e          the same through the public API with host buffers: each
+               scene's state uploaded from pinned host memory, K steps, the
+               state downloaded (all inside the timed region);
+  plain_fp64   the same scenes run one at a time in the FP64 form (the
+               reference's algorithm and grid), and the ratio to it;
+  fp64_check   per-particle contact-force error of the mixed form against the
+               FP64 form on one scene of the batch after the timed steps;
+  served       the served stream (p50/p99 ms, particle-steps/s, and the same
+               requests' time alone in the FP64 form);
+  roofline     the mixed form's dominant kernel (k_mx_advance) timed per
+               launch on the 1M-sphere box, whose state streams from HBM
+               every step, against the measured HBM peak; batch_hbm gives the
+               batch step's algorithmic bytes over its time;
+  cpu_baseline the reference's CPU path (restated in the oracle, one thread)
+               on one scene of the batch.
+--impl reference runs that CPU path on the host cores instead (one scene per
+core, drawn from the same batch) and prints the same metric.
+Under torchrun each rank advances its own replica of the workload (scenes
+shard with no exchange); value is the sum over ranks over the max rank time.
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -37,9 +55,14 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# scenes of a batch overlap on 32 library streams: give them 32 hardware
+# queues (read when the CUDA context is created)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "particle-steps/s"
 WORKLOAD = "polydisperse_box_settle"
+BATCH_WORKLOAD = "hopper_batch_256"
+SERVED_WORKLOAD = "served_settle_and_hopper_requests"
 B_CONTACT = {"fp64": 140, "mixed": 116}   # algorithmic bytes per particle, contact kernel
 # k_mx_advance (the mixed form's dominant kernel), per particle and middle step:
 # reads x y z r (32), vh vl wh wl ab (80), b2 (8), Fc Mc (32), pref (16) = 168;
@@ -50,7 +73,7 @@ B_ADVANCE = 328
 def _args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000, help="spheres (default: the 1M scene)")
@@ -59,6 +82,12 @@ def _args():
     ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"],
                     help="scene form for the headline value (the other is reported beside it)")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 side measurement")
+    ap.add_argument("--workload", default="batched", choices=["batched", "served", "box"])
+    ap.add_argument("--count", type=int, default=256, help="scenes in the batch")
+    ap.add_argument("--requests", type=int, default=32, help="requests of the served stream")
+    ap.add_argument("--rate", type=float, default=4.0, help="served arrivals per second")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="served device-memory budget")
+    ap.add_argument("--chunk", type=int, default=50, help="served steps per scene per tick")
     return ap.parse_args()
 
 
@@ -173,38 +202,63 @@ def _scene(n):
     return sc
 
 
+def _cpu_scene(spec):
+    """("box", n) -> the n-sphere polydisperse box; ("hopper", count, k) ->
+    scene k of the count-scene hopper batch."""
+    if spec[0] == "box":
+        return _scene(spec[1])
+    from metakonga_gb300 import scenes
+    return scenes.hopper(**scenes.hopper_batch(count=spec[1])[spec[2]])
+
+
 def _cpu_worker(args):
-    """One CPU-path replica (spawned process): builds the scene once, then
+    """One CPU-path replica (spawned process): builds its scene once, then
     times `samples` runs of `steps` steps; returns (particles*steps, [seconds])."""
-    n, steps, samples = args
+    spec, steps, samples = args
     sys.path.insert(0, ROOT)
     from oracle.pyoracle import Oracle
-    sc = _scene(n)
+    sc = _cpu_scene(spec)
     o = Oracle()
     times = []
     for _ in range(samples):
         t0 = time.perf_counter()
         o.run(sc, steps, cpu_path=True)
         times.append(time.perf_counter() - t0)
-    return n * steps, times
+    return sc.np_ * steps, times
 
 
-def cpu_baseline(n, steps, procs=1, samples=1):
-    """Reference CPU path throughput: procs replicas, each timing `samples`
-    runs of `steps` steps; per sample, value = procs * n * steps / slowest."""
+def cpu_baseline(specs, steps, samples=1):
+    """Reference CPU path throughput: one replica per spec (one process each
+    when there are several), each timing `samples` runs of `steps` steps; per
+    sample, value = sum of particle-steps / slowest replica."""
     import multiprocessing as mp
-    if procs == 1:
-        done, times = _cpu_worker((n, steps, samples))
+    if len(specs) == 1:
+        done, times = _cpu_worker((specs[0], steps, samples))
         return [done / t for t in times], times
     ctx = mp.get_context("spawn")
-    with ctx.Pool(procs) as pool:
-        res = pool.map(_cpu_worker, [(n, steps, samples)] * procs)
+    with ctx.Pool(len(specs)) as pool:
+        res = pool.map(_cpu_worker, [(sp, steps, samples) for sp in specs])
     vals, walls = [], []
     for i in range(samples):
         wall = max(r[1][i] for r in res)
         vals.append(sum(r[0] for r in res) / wall)
         walls.append(wall)
     return vals, walls
+
+
+def _batch_cpu_specs(count, cores, limit=50_000, seed=11):
+    """Scenes of the batch for the CPU replicas: a seeded draw (without
+    replacement while it lasts) among the scenes of at most `limit` spheres,
+    so that a sample stays within seconds."""
+    import numpy as np
+
+    from metakonga_gb300 import scenes
+    ns = np.array([d["n"] for d in scenes.hopper_batch(count=count)])
+    pool = np.flatnonzero(ns <= limit)
+    rng = np.random.Generator(np.random.MT19937(seed))
+    pick = rng.permutation(pool)
+    pick = np.resize(pick, cores)
+    return [("hopper", count, int(k)) for k in pick], int(ns[pick].sum())
 
 
 def run_reference(a):
@@ -214,19 +268,29 @@ def run_reference(a):
     cores = os.cpu_count() or 1
     steps = a.cpu_steps or 1
     t0 = time.perf_counter()
-    vals, walls = cpu_baseline(a.n, steps, procs=cores, samples=a.warmup + a.steps)
+    if a.workload == "box":
+        specs = [("box", a.n)] * cores
+        workload, cfg = WORKLOAD, {"particles": a.n, "grid": "128^3 wrapped"}
+        sample = (f"{steps} step(s) of the {a.n}-sphere scene per sample, one single-threaded "
+                  f"replica per core ({cores})")
+        per_sample = a.n * cores
+    else:
+        specs, per_sample = _batch_cpu_specs(a.count, cores)
+        workload = BATCH_WORKLOAD if a.workload == "batched" else SERVED_WORKLOAD
+        cfg = {"scenes": a.count, "grid": "128^3 wrapped, cell 2 x max(r, triangle circumradius)"}
+        sample = (f"{steps} step(s) per sample of {cores} hopper scenes of the {a.count}-scene batch "
+                  f"(a seeded draw among those of <= 50,000 spheres; {per_sample} spheres), one "
+                  f"single-threaded scene per core ({cores})")
+    vals, walls = cpu_baseline(specs, steps, samples=a.warmup + a.steps)
     vals = vals[a.warmup:]
     v = statistics.median(vals)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": a.gpus,
-        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * a.n / v,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * per_sample / v,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded MT19937 rejection-sampled spheres)",
-        "config": {"workload": WORKLOAD, "particles": a.n, "dt": 5e-6, "grid": "128^3 wrapped",
-                   "l2": "state > L2 (no flush)"},
-        "cpu_baseline": {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
-                         "sample": f"{steps} step(s) of the {a.n}-sphere scene per sample, one "
-                                   f"single-threaded replica per core ({cores})"},
+        "data": "synthetic (seeded MT19937 scenes)",
+        "config": dict({"workload": workload, "dt": 5e-6, "l2": "state > L2 (no flush)"}, **cfg),
+        "cpu_baseline": {"value": v, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": time.perf_counter() - t0,
     }
@@ -280,6 +344,35 @@ def _time_scene(sc, mode, steps, warmup, stream, barrier, world, with_clock, loc
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     return ms, phases, launches, (clk.summary() if clk else None), ds, rebuilds
+
+
+def _roofline(mode, n, steps, phases, one):
+    """Roofline object of a scene's dominant kernel from its phase timings
+    (phases: a K-step call's, one: a 1-step call's)."""
+    peak, peak_kind = _peaks()
+    c_ms, c_n = phases["p2p"]
+    contact = {"avg_launch_ms": c_ms / c_n if c_n else None}
+    if mode == "mixed":
+        # dominant kernel: the in-place advance (velocity-Verlet, contact view, skin test)
+        k_ms = (phases["vv"][0] - one["vv"][0]) / max(steps - 1, 1)
+        bpp = B_ADVANCE
+        kname = "k_mx_advance<1> (in-place velocity-Verlet, contact view, skin test)"
+        traffic = _traffic_from_profiles("advance_mixed_polydisperse_box.md")
+        contact.update({"kernel": "k_mx_contact (Verlet-list pairs and planes of the heavy list)",
+                        "traffic": _traffic_from_profiles("contact_mixed_polydisperse_box.md"),
+                        "bytes_per_particle_full_pass": B_CONTACT["mixed"],
+                        "achieved_full_pass_gbs": (n * B_CONTACT["mixed"]) / (c_ms / c_n / 1e3) / 1e9
+                        if c_n else None})
+    else:
+        k_ms = c_ms / c_n if c_n else None
+        bpp = B_CONTACT["fp64"]
+        kname = "k_p2p (FP64 particle-particle)"
+        traffic = _traffic_from_profiles("p2p_fp64_polydisperse_box.md")
+    achieved = (n * bpp) / (k_ms / 1e3) / 1e9 if k_ms else None
+    return {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
+            "traffic": traffic, "bytes_per_particle": bpp, "avg_launch_ms": k_ms,
+            "contact_pass": contact}
 
 
 def run_ours(a):
@@ -336,30 +429,7 @@ def run_ours(a):
     ds.close()
 
     one = phases.pop("_one")
-    peak, peak_kind = _peaks()
-    c_ms, c_n = phases["p2p"]
-    contact = {"avg_launch_ms": c_ms / c_n if c_n else None}
-    if a.mode == "mixed":
-        # dominant kernel: the in-place advance (velocity-Verlet, contact view, skin test)
-        k_ms = (phases["vv"][0] - one["vv"][0]) / max(a.steps - 1, 1)
-        bpp = B_ADVANCE
-        kname = "k_mx_advance<1> (in-place velocity-Verlet, contact view, skin test)"
-        traffic = _traffic_from_profiles("advance_mixed_polydisperse_box.md")
-        contact.update({"kernel": "k_mx_contact (Verlet-list pairs and planes of the heavy list)",
-                        "traffic": _traffic_from_profiles("contact_mixed_polydisperse_box.md"),
-                        "bytes_per_particle_full_pass": B_CONTACT["mixed"],
-                        "achieved_full_pass_gbs": (n * B_CONTACT["mixed"]) / (c_ms / c_n / 1e3) / 1e9
-                        if c_n else None})
-    else:
-        k_ms = c_ms / c_n if c_n else None
-        bpp = B_CONTACT["fp64"]
-        kname = "k_p2p (FP64 particle-particle)"
-        traffic = _traffic_from_profiles("p2p_fp64_polydisperse_box.md")
-    achieved = (n * bpp) / (k_ms / 1e3) / 1e9 if k_ms else None
-    roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
-            "traffic": traffic, "bytes_per_particle": bpp, "avg_launch_ms": k_ms,
-            "contact_pass": contact}
+    roof = _roofline(a.mode, n, a.steps, phases, one)
     phase_ms = {k: round(v[0] / max(v[1], 1), 4) for k, v in phases.items() if v[1]}
 
     plain = None
@@ -378,7 +448,7 @@ def run_ours(a):
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
         csteps = a.cpu_steps or 3
-        vals, times = cpu_baseline(n, csteps, procs=1, samples=1)
+        vals, times = cpu_baseline([("box", n)], csteps, samples=1)
         cpu = {"value": vals[0], "unit": METRIC, "cores": 1, "kind": "port",
                "sample": f"{csteps} steps of the same {n}-sphere scene, reference CPU path "
                          f"(restated, single thread), {times[0]:.1f} s"}
@@ -410,10 +480,318 @@ def run_ours(a):
     print(json.dumps(line), flush=True)
 
 
+def _torch_setup():
+    import torch
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    return world, rank, local, barrier
+
+
+def _max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _fp64_alone(scs, steps, stream):
+    """Each scene alone in the plain FP64 form (one warm-up step, then `steps`
+    device-timed steps): its ms per step."""
+    import torch
+
+    from metakonga_gb300 import engine
+    sh = stream.cuda_stream
+    out = []
+    for sc in scs:
+        d = engine.DeviceScene(sc, mode=engine.MODE_FP64)
+        d.step(1, check=True, stream=sh)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        d.step(steps, check=False, stream=sh)
+        e1.record(stream)
+        e1.synchronize()
+        out.append(e0.elapsed_time(e1) / steps)
+        d.close()
+    return out
+
+
+def _fp64_check(sc, squeeze=0.92, seed=29):
+    """Contact forces of the mixed form against the FP64 form on one state:
+    scene `sc` squeezed towards its centroid by `squeeze` (the lattice pitch
+    falls below the larger diameters, so that neighbouring spheres overlap)
+    with random velocities and spins; per particle
+    |F_mixed - F_fp64| / max(|F_fp64|, m g), and the same for the torque / r."""
+    import numpy as np
+
+    from metakonga_gb300 import engine
+    st = sc.copy()
+    rng = np.random.Generator(np.random.MT19937(seed))
+    c = st.pos[:, :3].mean(axis=0)
+    st.pos[:, :3] = c + (st.pos[:, :3] - c) * squeeze
+    st.vel[:] = rng.normal(0.0, 0.2, st.vel.shape)
+    st.omega[:] = rng.normal(0.0, 20.0, st.omega.shape)
+    out = []
+    for mode in (engine.MODE_MIXED, engine.MODE_FP64):
+        d = engine.DeviceScene(st, mode=mode)
+        out.append(d.eval_contacts())
+        d.close()
+    (f_m, m_m), (f_r, m_r) = out
+    den = np.maximum(np.linalg.norm(f_r, axis=1), st.mass * 9.81)
+    err = np.linalg.norm(f_m - f_r, axis=1) / den
+    r = st.pos[:, 3]
+    merr = np.linalg.norm((m_m - m_r) / r[:, None], axis=1) / den
+    touching = np.linalg.norm(f_r, axis=1) > 0
+    return {"particles": int(st.np_), "touching": int(touching.sum()),
+            "max_force_err": float(err.max()), "p999_force_err": float(np.percentile(err, 99.9)),
+            "max_torque_over_r_err": float(merr.max()),
+            "state": f"scene squeezed by {squeeze} towards its centroid, velocities N(0, 0.2) m/s, "
+                     "spins N(0, 20) rad/s",
+            "normaliser": "max(|F_fp64|, m g) per particle", "tolerance": 2e-5}
+
+
+def _box_roofline(a, stream, barrier, world, local):
+    """The 1M-sphere box in the mixed form: value and the advance kernel's
+    live roofline (its state streams from HBM every step)."""
+    sc = _scene(1_000_000)
+    import torch
+    with torch.cuda.stream(stream):
+        ms, phases, launches, _, ds, rebuilds = _time_scene(sc, "mixed", a.steps, a.warmup, stream,
+                                                            barrier, world, False, local)
+    ds.close()
+    one = phases.pop("_one")
+    roof = _roofline("mixed", sc.np_, a.steps, phases, one)
+    roof["workload"] = ("polydisperse_box_settle, 1,000,000 spheres (one scene: the batch's scenes "
+                        "overlap on 32 streams, so their launches have no separate duration)")
+    return roof, {"value": world * sc.np_ * a.steps / (ms / 1e3), "ms_per_step": ms / a.steps,
+                  "gpu_launches": launches, "cell_rebinnings_in_timed_steps": rebuilds}
+
+
+def _served(a, stream, plain=True):
+    """The served request stream: report of the continuous-batching server,
+    and the same requests' time alone in the FP64 form."""
+    from metakonga_gb300 import scenes, serve
+    t0 = time.perf_counter()
+    reqs = scenes.served_requests(count=a.requests, seed=4)
+    scs = [scenes.make_request_scene(r) for r in reqs]
+    gen_s = time.perf_counter() - t0
+    arrivals = serve.poisson_arrivals(len(reqs), a.rate, seed=5)
+    srv = serve.Server(budget_bytes=int(a.budget_gb * 1e9), chunk=a.chunk, stream=stream.cuda_stream,
+                       keep_results=True)
+    for k, (r, sc) in enumerate(zip(reqs, scs)):
+        srv.submit(k, sc, r["steps"], arrival=float(arrivals[k]))
+    clk = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    with clk:
+        srv.run()
+    rep = srv.report()
+    rep["clocks"] = clk.summary()
+    rep["generation_s"] = gen_s
+    rep["arrival_rate_per_s"] = a.rate
+    rep["budget_bytes"] = int(a.budget_gb * 1e9)
+    rep["chunk_steps"] = a.chunk
+    rep["particles"] = [int(sc.np_) for sc in scs]
+    rep["steps"] = [int(r["steps"]) for r in reqs]
+    rep["kinds"] = [r["kind"] for r in reqs]
+    rep["e2e_note"] = ("latency from arrival to the downloaded result: scene upload, steps and "
+                       "download through the public API (DeviceScene, engine.step_many)")
+    if plain:
+        per = _fp64_alone(scs, 2, stream)
+        alone_s = sum(r["steps"] * ms / 1e3 for r, ms in zip(reqs, per))
+        rep["plain_fp64_alone"] = {
+            "seconds_one_after_another": alone_s,
+            "particle_steps_per_s": rep["particle_steps"] / alone_s,
+            "method": "each request's scene alone in the FP64 form, 2 device-timed steps after one "
+                      "warm-up step, times its step count; summed over requests"}
+        rep["vs_plain_fp64"] = rep["particle_steps_per_s"] / (rep["particle_steps"] / alone_s)
+    del rep["particles"], rep["steps"]
+    return rep
+
+
+def run_batched(a):
+    import numpy as np
+    import torch
+
+    from metakonga_gb300 import engine, scenes
+    from metakonga_gb300._lib import call
+    world, rank, local, barrier = _torch_setup()
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    t0 = time.perf_counter()
+    specs = scenes.hopper_batch(count=a.count)
+    scs = [scenes.hopper(**d) for d in specs]
+    gen_s = time.perf_counter() - t0
+    n_tot = sum(sc.np_ for sc in scs)
+    ds = [engine.DeviceScene(sc, mode=engine.MODE_MIXED) for sc in scs]
+    dev_bytes = sum(d.device_bytes() for d in ds)
+    engine.step_many(ds, a.warmup, check=True, stream=sh)
+    barrier()
+    rb0 = [d.rebuilds(sh) for d in ds]
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(local)
+    barrier()
+    with clk:
+        ev0.record(stream)
+        engine.step_many(ds, a.steps, check=False, stream=sh)
+        ev1.record(stream)
+        barrier()
+    ms = _max_over_ranks(ev0.elapsed_time(ev1), world)
+    value = world * n_tot * a.steps / (ms / 1e3)
+    rb1 = [d.rebuilds(sh) for d in ds]
+    rebuilds = sum(b[0] - r[0] for r, b in zip(rb0, rb1))
+    launches = sum(d.launches(a.steps) for d in ds) + sum((b[0] - r[0]) * b[1] for r, b in zip(rb0, rb1))
+
+    k_med = int(np.argsort([sc.np_ for sc in scs])[len(scs) // 2])
+
+    # e2e: every scene's state uploaded from pinned host memory, K steps, the
+    # state downloaded; the downloaded state is the next upload's input
+    keys = ("pos", "vel", "acc", "omega", "alpha")
+    host = []
+    for d, sc in zip(ds, scs):
+        st = d.download(sh)
+        h = {k: torch.from_numpy(np.ascontiguousarray(st[k])).pin_memory() for k in keys}
+        for k in ("force", "moment", "mass", "inertia"):
+            h[k] = torch.from_numpy(np.ascontiguousarray(getattr(sc, k))).pin_memory()
+        host.append(h)
+    h2d = sum(sum(h[k].numel() * 8 for k in keys + ("mass", "inertia")) for h in host)
+    d2h = sum(sum(h[k].numel() * 8 for k in keys) for h in host)
+
+    def e2e_job():
+        for d, h in zip(ds, host):
+            call("xd_scene_upload", d.handle, *[h[k].data_ptr() for k in
+                                                ("pos", "vel", "acc", "omega", "alpha", "force",
+                                                 "moment", "mass", "inertia")], sh)
+        engine.step_many(ds, a.steps, check=False, stream=sh)
+        for d, h in zip(ds, host):
+            call("xd_scene_download", d.handle, *[h[k].data_ptr() for k in keys], None, None, sh)
+        torch.cuda.current_stream().synchronize()
+        stream.synchronize()
+
+    barrier()
+    t1 = time.perf_counter()
+    e2e_job()
+    barrier()
+    e2e_s = _max_over_ranks(time.perf_counter() - t1, world)
+    e2e_value = world * n_tot * a.steps / e2e_s
+
+    # the batch step's algorithmic bytes: the advance and a full contact pass per sphere
+    batch_bytes = n_tot * (B_ADVANCE + B_CONTACT["mixed"])
+    peak, peak_kind = _peaks()
+    batch_gbs = batch_bytes / (ms / a.steps / 1e3) / 1e9
+    for d in ds:
+        d.close()
+    del host
+    torch.cuda.empty_cache()
+
+    plain = None
+    if not a.no_plain:
+        psteps = 2
+        per = _fp64_alone(scs, psteps, stream)
+        fp64_ms = sum(per)
+        plain = {"value": world * n_tot / (fp64_ms / 1e3), "unit": METRIC,
+                 "ms_per_batch_step": fp64_ms,
+                 "method": "each scene alone in the FP64 form (the reference's algorithm: 128^3 grid "
+                           "of 2 x max(r, triangle circumradius) cells, re-sorted every step), one "
+                           f"warm-up step then {psteps} device-timed steps; ms summed over scenes",
+                 "ratio": value / (world * n_tot / (fp64_ms / 1e3))}
+
+    # FP64 check on the median-size scene, in a state with contacts
+    check = _fp64_check(scs[k_med])
+    check["scene"] = k_med
+    roof, box = _box_roofline(a, stream, barrier, world, local)
+    served = _served(a, stream, plain=not a.no_plain) if rank == 0 else None
+
+    cpu = None
+    if rank == 0 and not a.no_cpu_baseline:
+        k_cpu = k_med
+        csteps = a.cpu_steps or 100
+        vals, times = cpu_baseline([("hopper", a.count, k_cpu)], csteps, samples=1)
+        cpu = {"value": vals[0], "unit": METRIC, "cores": 1, "kind": "port",
+               "sample": f"{csteps} steps of scene {k_cpu} of the batch ({scs[k_cpu].np_} spheres), "
+                         f"reference CPU path (restated, single thread), {times[0]:.1f} s"}
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic (seeded MT19937 scenes: jittered lattices in cones of triangles)",
+        "config": {"workload": BATCH_WORKLOAD, "scenes": len(scs), "particles": n_tot,
+                   "particles_min": min(sc.np_ for sc in scs), "particles_max": max(sc.np_ for sc in scs),
+                   "triangles_per_scene": int(scs[0].ntri), "dt": 5e-6, "mode": "mixed",
+                   "grid": "one grid per scene sized to its cone, cell 2 r_max + skin",
+                   "l2": "batch state > L2 (no flush)", "device_bytes": dev_bytes,
+                   "generation_s": gen_s, "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d / a.steps,
+                "d2h_bytes_per_step": d2h / a.steps, "h2d_bytes_per_job": h2d, "d2h_bytes_per_job": d2h,
+                "job": f"upload all {len(scs)} states from pinned host memory, {a.steps} steps, download"},
+        "gpu_launches": launches,
+        "cell_rebinnings_in_timed_steps": rebuilds,
+        "plain_fp64": plain,
+        "fp64_check": check,
+        "batch_hbm": {"bytes_per_step": batch_bytes, "achieved_gbs": batch_gbs, "peak": peak,
+                      "frac": batch_gbs / peak, "peak_kind": peak_kind,
+                      "bytes_per_particle": B_ADVANCE + B_CONTACT["mixed"]},
+        "roofline": roof,
+        "single_scene_box": box,
+        "served": served,
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_served(a):
+    import torch
+    world, rank, local, barrier = _torch_setup()
+    stream = torch.cuda.Stream()
+    rep = _served(a, stream, plain=not a.no_plain)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": rep["particle_steps_per_s"], "unit": METRIC, "n_gpus": world,
+        "steps": a.requests, "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic (seeded MT19937 request stream)",
+        "config": {"workload": SERVED_WORKLOAD, "requests": a.requests, "rate_per_s": a.rate,
+                   "budget_gb": a.budget_gb, "chunk": a.chunk, "mode": "mixed"},
+        "e2e": {"value": rep["particle_steps_per_s"], "unit": METRIC,
+                "note": "the served value is end to end (upload, steps, download per request)"},
+        "p50_ms": rep["p50_ms"], "p99_ms": rep["p99_ms"], "served": rep,
+        "clocks": rep["clocks"],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = _args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "batched":
+        run_batched(a)
+    elif a.workload == "served":
+        run_served(a)
     else:
         run_ours(a)
 

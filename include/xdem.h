@@ -376,10 +376,12 @@ int xd_scene_rebuilds(xd_scene* scene, unsigned long long* count, unsigned long 
                       void* stream);
 
 /* Advance `count` independent scenes (scenes[i] by nsteps[i] steps) side by
- * side on the current device: the scenes are spread over a pool of 16
+ * side on the current device: the scenes are spread over a pool of 32
  * library streams that start after the work queued on `stream` and that
  * `stream` waits for on return, so the batch is ordered on `stream` like one
- * xd_scene_step.  Each scene's result is bit for bit the one xd_scene_step
+ * xd_scene_step.  The streams overlap on the device up to the
+ * CUDA_DEVICE_MAX_CONNECTIONS hardware queues (set it to 32 before the CUDA
+ * context is created).  Each scene's result is bit for bit the one xd_scene_step
  * gives it alone.  Two scenes of one call must not be the same scene.  With
  * `check` non-zero the call synchronises `stream`.  No counterpart in the
  * reference, which runs one model per process. */

@@ -45,6 +45,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -79,7 +80,8 @@ enum {
     CN_NORMALS = 5,    // FP64 normal-force rechecks (cumulative)
     CN_SLIPS = 6,      // FP64 slip rechecks (cumulative)
     CN_REBUILDS = 7,   // re-binnings (cumulative)
-    kCounters = 8
+    CN_RXN = 8,        // blocks of k_rxn_sum done (the last one finishes the sum)
+    kCounters = 9
 };
 
 struct Master {
@@ -1337,39 +1339,65 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
     }
 }
 
-// Body reactions: rxn[(b * 6 + q) * n + i] summed over i in a fixed order
-// (kRxnBlocks fixed chunks, each a fixed tree), then added to the bodies.
+// Body reactions: rxn[(b * 6 + q) * n + i] summed over i in a fixed order and
+// added to the bodies, in one launch.  Each block sums a fixed chunk of i for
+// every q (per thread a strided run, then a fixed shuffle tree and the warps
+// in order) into part[q * gridDim.x + block]; the last block to finish adds
+// the blocks' partials in block order.  The order depends only on n and the
+// grid, so a scene's reaction is the same in every run.
 constexpr unsigned kRxnBlocks = 152;
-__global__ void __launch_bounds__(256) k_rxn_partial(const double* __restrict__ rxn, unsigned n,
-                                                     unsigned nq, double* __restrict__ part)
+constexpr unsigned kRxnThreads = 256;
+
+static unsigned rxn_grid(unsigned n) { return std::max(1u, std::min(kRxnBlocks, (n + kRxnThreads - 1) / kRxnThreads)); }
+
+__global__ void __launch_bounds__(kRxnThreads) k_rxn_sum(const double* __restrict__ rxn, unsigned n, unsigned nbodies,
+                                                         double* __restrict__ part, unsigned* __restrict__ counters,
+                                                         xd_polygon_mass_info* __restrict__ pmi)
 {
-    __shared__ double sh[256];
+    __shared__ double warp_sum[6][kRxnThreads / 32];
+    __shared__ bool last;
+    const unsigned nq = 6 * nbodies;
     const unsigned chunk = (n + gridDim.x - 1) / gridDim.x;
     const unsigned b0 = blockIdx.x * chunk, b1 = min(n, b0 + chunk);
-    for (unsigned q = 0; q < nq; ++q) {
-        double s = 0.0;
-        for (unsigned i = b0 + threadIdx.x; i < b1; i += blockDim.x) s += rxn[(size_t)q * n + i];
-        sh[threadIdx.x] = s;
-        __syncthreads();
-        for (unsigned o = 128; o > 0; o >>= 1) {
-            if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-            __syncthreads();
+    const unsigned lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    for (unsigned b = 0; b < nbodies; ++b) {
+        // the six components of one body together: six independent loads per
+        // particle and one barrier per body
+        double v[6] = { 0.0, 0.0, 0.0, 0.0, 0.0, 0.0 };
+        const double* rb = rxn + (size_t)b * 6 * n;
+        for (unsigned i = b0 + threadIdx.x; i < b1; i += blockDim.x)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) v[c] += rb[(size_t)c * n + i];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            for (unsigned o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
+            if (lane == 0) warp_sum[c][wid] = v[c];
         }
-        if (threadIdx.x == 0) part[(size_t)q * gridDim.x + blockIdx.x] = sh[0];
+        __syncthreads();
+        if (threadIdx.x < 6) {
+            double t = 0.0;
+            for (unsigned w = 0; w < blockDim.x / 32u; ++w) t += warp_sum[threadIdx.x][w];
+            part[(size_t)(b * 6 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
+            __threadfence();   // visible before this block is counted done
+        }
         __syncthreads();
     }
-}
-
-__global__ void k_rxn_final(const double* __restrict__ part, unsigned nblocks, unsigned nbodies,
-                            xd_polygon_mass_info* __restrict__ pmi)
-{
-    const unsigned q = threadIdx.x;   // one thread per (body, component)
-    if (q >= 6 * nbodies) return;
-    double s = 0.0;
-    for (unsigned k = 0; k < nblocks; ++k) s += part[(size_t)q * nblocks + k];
-    const unsigned b = q / 6, c = q % 6;
-    if (c < 3) pmi[b].force[c] += s;
-    else pmi[b].moment[c - 3] += s;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(counters + CN_RXN, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x < nq) {
+        const unsigned q = threadIdx.x;
+        double t = 0.0;
+        for (unsigned k = 0; k < gridDim.x; ++k) t += __ldcg(part + (size_t)q * gridDim.x + k);
+        const unsigned b = q / 6, c = q % 6;
+        if (c < 3) pmi[b].force[c] += t;
+        else pmi[b].moment[c - 3] += t;
+    }
+    if (threadIdx.x == 0) counters[CN_RXN] = 0;
 }
 
 // ---- host-order state <-> master (reference layouts) -----------------------
@@ -1728,6 +1756,10 @@ int mixed_create(const xd_scene_desc& d, MixedScene** out)
     MixedScene* s = new (std::nothrow) MixedScene();
     if (!s) return set_error(XD_ERR_NOMEM, "mixed scene: host allocation");
     s->desc = d;
+    // XDEM_NO_GRAPHS=1: launch every kernel directly (the host reads the
+    // re-binning flag each step), so that a profiler sees each kernel
+    const char* ng = getenv("XDEM_NO_GRAPHS");
+    s->use_graphs = !(ng && ng[0] && ng[0] != '0');
     s->host_planes.assign(d.planes, d.planes + d.nplanes);
     s->host_cps.assign(d.cp_planes, d.cp_planes + d.nplanes);
     s->desc.planes = s->host_planes.data();
@@ -1960,7 +1992,8 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
     if (st != XD_OK) return st;
     s->cells_clean = true;
     ph.begin(3, q);
-    const unsigned grid = kContactBlocks;
+    // the list holds at most n particles: no more warps than that
+    const unsigned grid = std::max(1u, std::min(kContactBlocks, (n + kContactThreads - 1) / kContactThreads));
     if (record) {
         st = cuda_status(cudaMemsetAsync(s->rec_count, 0, sizeof(unsigned) * n, q), "mixed pair count");
         if (st != XD_OK) return st;
@@ -1979,8 +2012,7 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
     st = launch_status("mixed contact");
     if (st == XD_OK && s->nbodies && MODE != 3) {
         // this step's reaction on the polygon bodies, summed in a fixed order
-        k_rxn_partial<<<kRxnBlocks, 256, 0, q>>>(s->rxn, n, 6 * s->nbodies, s->rxn_part);
-        k_rxn_final<<<1, 64, 0, q>>>(s->rxn_part, kRxnBlocks, s->nbodies, s->pmi);
+        k_rxn_sum<<<rxn_grid(n), kRxnThreads, 0, q>>>(s->rxn, n, s->nbodies, s->rxn_part, s->counters, s->pmi);
         st = launch_status("mixed body reaction");
     }
     ph.end(3, q);
@@ -2072,7 +2104,7 @@ unsigned long long mixed_launches(MixedScene* s, unsigned nsteps)
     if (!s || nsteps == 0 || s->n == 0) return 0;
     // per step: advance + contact; + the last velocity update; a step that
     // re-bins adds mixed_rebuild_launches()
-    const unsigned long long per = 2 + (s->nbodies ? 2 : 0);
+    const unsigned long long per = 2 + (s->nbodies ? 1 : 0);
     unsigned long long total = per * nsteps + 1;
     if (!s->cells_clean) total += mixed_rebuild_launches(s);   // the first step re-bins
     return total;

@@ -113,11 +113,13 @@ void phase_hook(void* ctx, int phase, bool begin, cudaStream_t q)
     }
 }
 
+// No hook while timing is off: the mixed path then runs its steps as CUDA
+// graphs and decides re-binning on the device.
 Phases phases_of(xd_scene* s)
 {
     Phases p;
     p.ctx = s;
-    p.fn = phase_hook;
+    p.fn = s->timing ? phase_hook : nullptr;
     return p;
 }
 
@@ -143,8 +145,10 @@ struct PhaseSpan {
 
 // Streams on which xd_scene_step_many runs its scenes side by side: kPoolStreams
 // non-blocking streams per device, made on first use and kept for the
-// process; the calls that use them take the mutex.
-constexpr int kPoolStreams = 16;
+// process; the calls that use them take the mutex.  The device runs streams
+// truly side by side only up to CUDA_DEVICE_MAX_CONNECTIONS hardware queues
+// (8 unless the variable is set before the context is made; 32 at most).
+constexpr int kPoolStreams = 32;
 constexpr int kPoolDevices = 64;
 
 struct StreamPool {

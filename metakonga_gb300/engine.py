@@ -7,8 +7,14 @@ dem_simulation.cpp:447-469), without per-step host work.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
+
+# xd_scene_step_many overlaps scenes on 32 library streams; the device gives
+# streams their own hardware queues only up to this count (default 8).  It
+# takes effect when set before the process creates its CUDA context.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 from . import _lib
 from ._lib import call

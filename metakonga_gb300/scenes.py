@@ -13,6 +13,8 @@ material constants of the benchmark scenes:
                    walls, dt = 5e-6 s.
 * ``drum``         spheres inside a closed, tessellated cylinder that rotates
                    about its axis (particle-triangle contacts).
+* ``lattice_box``  the polydisperse settle's box and density with the
+                   spheres on a jittered lattice (fast, for request streams).
 * ``hopper``       spheres in a 60-degree conical hopper of 4,096 triangles
                    above a plane floor, r ~ U[2, 4] mm, orifice of 6-12
                    particle diameters; ``hopper_batch`` draws the batch of
@@ -226,6 +228,72 @@ def polydisperse_box(n: int = 1_000_000, seed: int = 7, rmin: float = 0.002, rma
                  params=_reference_grid(rmax, n, dt, grid=grid), pos=pos, **_state(pos),
                  cp_pp=cp, planes=planes, plane_names=names,
                  cp_planes=np.array([cp] * len(names), dtype=CONTACT_PROPERTY))
+
+
+def lattice_box(n: int = 100_000, seed: int = 7, rmin: float = 0.002, rmax: float = 0.004,
+                box=(1.0, 1.0, 2.0), steps: int = 20_000, dt: float = 5.0e-6) -> Scene:
+    """The polydisperse settle's geometry and density (the box's x/y extent
+    scaled by sqrt(n / 1e6) as in ``polydisperse_box``), with the spheres on
+    a jittered cubic lattice instead of rejection-sampled: n random sites of
+    a lattice that fills the box, r ~ U[rmin, rmax], each moved by at most
+    pitch / 2 - r so that none overlap.  Generation is O(n) numpy (for the
+    served request stream, which makes many such scenes)."""
+    rng = _rng(seed)
+    scale = (n / 1_000_000) ** 0.5
+    ext = np.array([box[0] * scale, box[1] * scale, box[2]])
+    lo = np.array([-ext[0] / 2, -ext[1] / 2, 0.0])
+    pitch = (float(np.prod(ext)) / n) ** (1.0 / 3.0)
+    while True:
+        # sites at least pitch / 2 from every wall
+        k = np.floor(ext / pitch).astype(int)
+        if pitch < 2.04 * rmax:
+            raise ValueError("lattice_box: box too small for n spheres")
+        if int(np.prod(k)) >= n:
+            break
+        pitch *= 0.98
+    start = lo + 0.5 * (ext - (k - 1) * pitch)
+    pick = np.sort(rng.choice(int(np.prod(k)), size=n, replace=False))
+    ix, iy, iz = np.unravel_index(pick, tuple(k))
+    pts = start + np.stack([ix, iy, iz], axis=1) * pitch
+    rad = rng.uniform(rmin, rmax, size=n)
+    amp = np.minimum(0.5 * pitch - rad, rmax) / math.sqrt(3.0)
+    pts = pts + rng.uniform(-1.0, 1.0, size=(n, 3)) * amp[:, None]
+    pos = np.empty((n, 4), dtype=np.float64)
+    pos[:, :3] = pts
+    pos[:, 3] = rad
+    planes, names = box_walls(lo, lo + ext)
+    cp = _default_property()
+    return Scene(name="lattice_box", seed=seed, dt=dt, steps=steps,
+                 params=_reference_grid(rmax, n, dt), pos=pos, **_state(pos),
+                 cp_pp=cp, planes=planes, plane_names=names,
+                 cp_planes=np.array([cp] * len(names), dtype=CONTACT_PROPERTY))
+
+
+def served_requests(count: int = 32, seed: int = 4, n_min: int = 1_000, n_max: int = 500_000,
+                    steps_min: int = 1_000, steps_max: int = 20_000):
+    """A request stream's scene parameters: geometry a settle box
+    (``lattice_box``) or a hopper (``hopper``, orifice U[6, 12], friction
+    U[0.2, 0.6]) with equal odds, particle count log-uniform in
+    [n_min, n_max], step count uniform in [steps_min, steps_max].  Returns
+    a list of dicts (kind, kwargs, steps)."""
+    rng = _rng(seed)
+    out = []
+    for k in range(count):
+        n = int(math.exp(rng.uniform(math.log(n_min), math.log(n_max))))
+        steps = int(rng.integers(steps_min, steps_max + 1))
+        if rng.uniform() < 0.5:
+            out.append(dict(kind="box", kwargs=dict(n=n, seed=seed * 7919 + k), steps=steps))
+        else:
+            out.append(dict(kind="hopper", kwargs=dict(n=n, seed=seed * 7919 + k,
+                                                       orifice=float(rng.uniform(6.0, 12.0)),
+                                                       fric=float(rng.uniform(0.2, 0.6))),
+                            steps=steps))
+    return out
+
+
+def make_request_scene(req) -> Scene:
+    """The scene of one ``served_requests`` entry."""
+    return lattice_box(**req["kwargs"]) if req["kind"] == "box" else hopper(**req["kwargs"])
 
 
 def circumcentre(P, Q, R):
