@@ -83,6 +83,8 @@ def _args():
                     help="scene form for the headline value (the other is reported beside it)")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 side measurement")
     ap.add_argument("--workload", default="batched", choices=["batched", "served", "box"])
+    ap.add_argument("--no-served", action="store_true", help="batched: skip the served stream")
+    ap.add_argument("--no-box", action="store_true", help="batched: skip the 1M-box roofline run")
     ap.add_argument("--count", type=int, default=256, help="scenes in the batch")
     ap.add_argument("--requests", type=int, default=32, help="requests of the served stream")
     ap.add_argument("--rate", type=float, default=4.0, help="served arrivals per second")
@@ -711,8 +713,8 @@ def run_batched(a):
     # FP64 check on the median-size scene, in a state with contacts
     check = _fp64_check(scs[k_med])
     check["scene"] = k_med
-    roof, box = _box_roofline(a, stream, barrier, world, local)
-    served = _served(a, stream, plain=not a.no_plain) if rank == 0 else None
+    roof, box = _box_roofline(a, stream, barrier, world, local) if not a.no_box else (None, None)
+    served = _served(a, stream, plain=not a.no_plain) if rank == 0 and not a.no_served else None
 
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
