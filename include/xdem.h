@@ -95,6 +95,40 @@ typedef struct xd_polygon_mass_info {
     double vel[3], omega[3], force[3], moment[3];
 } xd_polygon_mass_info;
 
+/* Single-precision twins of the structs (mphysics_cuda_dec.cuh:165-246). */
+typedef struct xd_device_parameters_f {   /* device_parameters_f, 64 bytes */
+    unsigned int np;
+    unsigned int nsphere;
+    unsigned int ncell;
+    unsigned int grid_size[3];
+    float dt;
+    float half2dt;
+    float cell_size;
+    float cohesion;
+    float gravity[3];
+    float world_origin[3];
+} xd_device_parameters_f;
+
+typedef struct xd_contact_property_f {    /* device_contact_property_f, 44 bytes */
+    float Ei, Ej, pri, prj, Gi, Gj, rest, fric, rfric, coh, sratio;
+} xd_contact_property_f;
+
+typedef struct xd_plane_info_f {          /* device_plane_info_f, 116 bytes */
+    float l1, l2;
+    float u1[3], u2[3], uw[3], xw[3], pa[3], pb[3], w2[3], w3[3], w4[3];
+} xd_plane_info_f;
+
+typedef struct xd_polygon_info_f {        /* device_polygon_info_f, 76 bytes */
+    int id;
+    float P[3], Q[3], R[3], V[3], W[3], N[3];
+} xd_polygon_info_f;
+
+typedef struct xd_polygon_mass_info_f {   /* device_polygon_mass_info_f, 80 bytes; ep a float4 */
+    float origin[3];
+    XD_ALIGN16 float ep[4];
+    float vel[3], omega[3], force[3], moment[3];
+} xd_polygon_mass_info_f;
+
 /* ------------------------------------------------------------ library */
 
 const char* xd_version(void);
@@ -252,6 +286,89 @@ int xd_reduction_d3(const double* in, unsigned n, double out[3], void* stream);
 int xd_pair_list(const double* pos, const unsigned* sorted_index, const unsigned* cstart,
                  const unsigned* cend, unsigned np, unsigned* counts, unsigned* pairs,
                  unsigned long long cap, unsigned long long* total, void* stream);
+
+/* ------------------------------------------------------------ single precision
+ *
+ * The FP32 twins of the live API (mphysics_cuda_dec.cuh:248-300, launchers
+ * mphysics_cuda_def.cu:254-466, kernels mphysics_cuda_impl.cuh:1094-1895):
+ * pos and triangle spheres are float4 rows (16-byte aligned), vel, acc,
+ * omega, alpha, force and moment packed float3 rows (12-byte stride), mass
+ * and inertia float.  The arithmetic follows the reference's float kernels
+ * expression by expression, with their mixed float/double constants.
+ * Reference behaviour kept on purpose:
+ *   - the cell hash wraps with the grid size of the FP64 parameter block
+ *     (calcGridHash, impl:65-72, reads cte.grid_size, which only
+ *     setSymbolicParameter sets): set it with xd_set_symbolic_parameter too,
+ *     or, as when the reference runs in single precision without it, the
+ *     grid size is 0 and the hash is the x cell index alone;
+ *   - particle-particle forces always include the rotation terms (the float
+ *     parameter block has no rolling switch);
+ *   - a triangle contact adds only its normal force to the particle and no
+ *     moment, while the body takes -(Fn + Ft) (impl:1880-1888);
+ *   - planes apply no moment (DHSModel with ir = 0, impl:1553-1561).
+ * The body reaction, summed racily by the reference kernel, is summed here in
+ * a fixed order.  Only tcm = 1 (DHS) is provided, as for FP64. */
+
+/* setSymbolicParameter_f (mphysics_cuda_dec.cuh:248; def.cu:255-258). */
+int xd_set_symbolic_parameter_f(const xd_device_parameters_f* h_params);
+
+/* vv_update_position(float*) (dec.cuh:250; def.cu:260-267; impl:1105-1116). */
+int xd_vv_update_position_f(float* pos, const float* vel, const float* acc, unsigned np, void* stream);
+
+/* vv_update_velocity(float*) (dec.cuh:251; def.cu:269-282; impl:1118-1153). */
+int xd_vv_update_velocity_f(float* vel, float* acc, float* omega, float* alpha, float* force,
+                            float* moment, const float* mass, const float* inertia, unsigned np,
+                            void* stream);
+
+/* cu_calculateHashAndIndex(float*) (dec.cuh:253; def.cu:284-292; impl:1156-1168). */
+int xd_calculate_hash_and_index_f(unsigned* hash, unsigned* index, const float* pos, unsigned np,
+                                  void* stream);
+
+/* cu_calculateHashAndIndexForPolygonSphere(float*) (dec.cuh:254; def.cu:294-302;
+ * impl:1170-1182). */
+int xd_calculate_hash_and_index_polysphere_f(unsigned* hash, unsigned* index, unsigned sid,
+                                             unsigned nsphere, const float* sphere, void* stream);
+
+/* cu_reorderDataAndFindCellStart_f (dec.cuh:255-258; def.cu:305-333;
+ * impl:1184-1227): the same integer work as the FP64 call. */
+int xd_reorder_and_find_cell_start_f(unsigned* hash, unsigned* index, unsigned* cstart,
+                                     unsigned* cend, unsigned* sorted_index, unsigned n,
+                                     unsigned ncell, void* stream);
+
+/* cu_calculate_p2p(float*) (dec.cuh:260-266; def.cu:335-361; impl:1345-1425). */
+int xd_calculate_p2p_f(int tcm, const float* pos, const float* vel, const float* omega,
+                       float* force, float* moment, const float* mass,
+                       const unsigned* sorted_index, const unsigned* cstart, const unsigned* cend,
+                       const xd_contact_property_f* cp, unsigned np, void* stream);
+
+/* cu_plane_contact_force(float*) (dec.cuh:268-272; def.cu:363-381; impl:1427-1564). */
+int xd_plane_contact_force_f(int tcm, const xd_plane_info_f* plane, const float* pos,
+                             const float* vel, const float* omega, float* force, float* moment,
+                             const float* mass, unsigned np, const xd_contact_property_f* cp,
+                             void* stream);
+
+/* cu_cube_contact_force(float*) (dec.cuh:274-279; def.cu:383-404): the six
+ * planes in order, one shared property. */
+int xd_cube_contact_force_f(int tcm, const xd_plane_info_f* planes6, const float* pos,
+                            const float* vel, const float* omega, float* force, float* moment,
+                            const float* mass, unsigned np, const xd_contact_property_f* cp,
+                            void* stream);
+
+/* cu_particle_polygonObject_collision(float*) (dec.cuh:281-286; def.cu:428-446;
+ * impl:1808-1895).  Entries of sidx >= np are triangles (index - np); the
+ * reaction -(Fn + Ft) and its moment are added to dpmi[body]: for nbodies
+ * bodies (at most 8) in a fixed order, or with atomics when nbodies = 0. */
+int xd_particle_polygon_collision_f(int tcm, const xd_polygon_info_f* dpi, const float* dsph,
+                                    xd_polygon_mass_info_f* dpmi, const float* pos,
+                                    const float* vel, const float* omega, float* force,
+                                    float* moment, const float* mass, const unsigned* sidx,
+                                    const unsigned* cstart, const unsigned* cend,
+                                    const xd_contact_property_f* cp, unsigned np,
+                                    unsigned nbodies, void* stream);
+
+/* reductionD3(float3*) (dec.cuh:300; def.cu:448-466): sum of n float3 rows,
+ * returned to the host in out[3] (deterministic order). */
+int xd_reduction_f3(const float* in, unsigned n, float out[3], void* stream);
 
 /* ------------------------------------------------------------ scenes
  *

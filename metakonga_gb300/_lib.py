@@ -53,6 +53,17 @@ _SIGS = {
     "xd_cube_contact_force": [i32] + [vp] * 7 + [u32, vp, vp],
     "xd_planes_contact_force": [i32, vp, vp, u32] + [vp] * 6 + [u32, vp],
     "xd_particle_polygon_collision": [i32] + [vp] * 13 + [u32, u32, vp],
+    "xd_set_symbolic_parameter_f": [vp],
+    "xd_vv_update_position_f": [vp, vp, vp, u32, vp],
+    "xd_vv_update_velocity_f": [vp] * 8 + [u32, vp],
+    "xd_calculate_hash_and_index_f": [vp, vp, vp, u32, vp],
+    "xd_calculate_hash_and_index_polysphere_f": [vp, vp, u32, u32, vp, vp],
+    "xd_reorder_and_find_cell_start_f": [vp] * 5 + [u32, u32, vp],
+    "xd_calculate_p2p_f": [i32] + [vp] * 10 + [u32, vp],
+    "xd_plane_contact_force_f": [i32] + [vp] * 7 + [u32, vp, vp],
+    "xd_cube_contact_force_f": [i32] + [vp] * 7 + [u32, vp, vp],
+    "xd_particle_polygon_collision_f": [i32] + [vp] * 13 + [u32, u32, vp],
+    "xd_reduction_f3": [vp, u32, vp, vp],
     "xd_update_polygon_object_data": [vp] * 4 + [u32, vp],
     "xd_reduction_d3": [vp, u32, vp, vp],
     "xd_pair_list": [vp] * 4 + [u32, vp, vp, u64, vp, vp],

@@ -31,10 +31,10 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 
 # FP64 translation units whose results must match the reference's arithmetic
 # are compiled without multiply-add contraction.
-NO_FMAD = {"xd_grid.cu", "xd_integrate.cu", "xd_contact64.cu"}
+NO_FMAD = {"xd_grid.cu", "xd_integrate.cu", "xd_contact64.cu", "xd_twin32.cu"}
 
 CUDA_SOURCES = ["xd_capi.cu", "xd_sort.cu", "xd_grid.cu", "xd_integrate.cu", "xd_contact64.cu",
-                "xd_scene.cu", "xd_noalloc.cu", "xd_mixed.cu"]
+                "xd_scene.cu", "xd_noalloc.cu", "xd_mixed.cu", "xd_twin32.cu"]
 
 
 def nvcc() -> str:

@@ -135,57 +135,103 @@ void cu_updatePolygonObjectData(device_polygon_mass_info* dpmi, double* vList, d
                                   kDefaultStream);
 }
 
-// ---------------------------------------------------- FP32 (not provided)
+// ---------------------------------------------------------------- FP32 API
 
-void setSymbolicParameter_f(device_parameters_f*) { not_provided("setSymbolicParameter_f"); }
-void vv_update_position(float*, float*, float*, unsigned int) { not_provided("vv_update_position(float)"); }
-void vv_update_velocity(float*, float*, float*, float*, float*, float*, float*, float*, unsigned int)
+static_assert(sizeof(device_parameters_f) == sizeof(xd_device_parameters_f), "device_parameters_f layout");
+static_assert(sizeof(device_plane_info_f) == sizeof(xd_plane_info_f), "device_plane_info_f layout");
+static_assert(sizeof(device_polygon_info_f) == sizeof(xd_polygon_info_f), "device_polygon_info_f layout");
+static_assert(sizeof(device_polygon_mass_info_f) == sizeof(xd_polygon_mass_info_f), "mass info f layout");
+static_assert(sizeof(device_contact_property_f) == sizeof(xd_contact_property_f), "property f layout");
+
+void setSymbolicParameter_f(device_parameters_f* h_paras)
 {
-    not_provided("vv_update_velocity(float)");
+    xd_set_symbolic_parameter_f(reinterpret_cast<const xd_device_parameters_f*>(h_paras));
 }
-void cu_calculateHashAndIndex(unsigned int*, unsigned int*, float*, unsigned int) { not_provided("hash(float)"); }
-void cu_calculateHashAndIndexForPolygonSphere(unsigned int*, unsigned int*, unsigned int, unsigned int, float*)
+
+void vv_update_position(float* pos, float* vel, float* acc, unsigned int np)
 {
-    not_provided("hash polysphere(float)");
+    xd_vv_update_position_f(pos, vel, acc, np, kDefaultStream);
 }
-void cu_reorderDataAndFindCellStart_f(unsigned int*, unsigned int*, unsigned int*, unsigned int*,
-                                      unsigned int*, unsigned int, unsigned int)
+
+void vv_update_velocity(float* vel, float* acc, float* omega, float* alpha, float* force, float* moment,
+                        float* mass, float* iner, unsigned int np)
 {
-    not_provided("cu_reorderDataAndFindCellStart_f");
+    xd_vv_update_velocity_f(vel, acc, omega, alpha, force, moment, mass, iner, np, kDefaultStream);
 }
-void cu_calculate_p2p(const int, float*, float*, float*, float*, float*, float*, unsigned int*,
-                      unsigned int*, unsigned int*, device_contact_property_f*, unsigned int)
+
+void cu_calculateHashAndIndex(unsigned int* hash, unsigned int* index, float* pos, unsigned int np)
 {
-    not_provided("cu_calculate_p2p(float)");
+    xd_calculate_hash_and_index_f(hash, index, pos, np, kDefaultStream);
 }
-void cu_plane_contact_force(const int, device_plane_info_f*, float*, float*, float*, float*, float*,
-                            float*, unsigned int, device_contact_property_f*)
+
+void cu_calculateHashAndIndexForPolygonSphere(unsigned int* hash, unsigned int* index, unsigned int sid,
+                                              unsigned int nsphere, float* sphere)
 {
-    not_provided("cu_plane_contact_force(float)");
+    xd_calculate_hash_and_index_polysphere_f(hash, index, sid, nsphere, sphere, kDefaultStream);
 }
-void cu_cube_contact_force(const int, device_plane_info_f*, float*, float*, float*, float*, float*,
-                           float*, unsigned int, device_contact_property_f*)
+
+void cu_reorderDataAndFindCellStart_f(unsigned int* hash, unsigned int* index, unsigned int* cstart,
+                                      unsigned int* cend, unsigned int* sorted_index, unsigned int np,
+                                      unsigned int ncell)
 {
-    not_provided("cu_cube_contact_force(float)");
+    xd_reorder_and_find_cell_start_f(hash, index, cstart, cend, sorted_index, np, ncell, kDefaultStream);
 }
-void cu_particle_polygonObject_collision(const int, device_polygon_info_f*, float*,
-                                         device_polygon_mass_info_f*, float*, float*, float*,
-                                         float*, float*, float*, unsigned int*, unsigned int*,
-                                         unsigned int*, device_contact_property_f*, unsigned int)
+
+void cu_calculate_p2p(const int tcm, float* pos, float* vel, float* omega, float* force, float* moment,
+                      float* mass, unsigned int* sorted_index, unsigned int* cstart, unsigned int* cend,
+                      device_contact_property_f* cp, unsigned int np)
 {
-    not_provided("cu_particle_polygonObject_collision(float)");
+    xd_calculate_p2p_f(tcm, pos, vel, omega, force, moment, mass, sorted_index, cstart, cend,
+                       reinterpret_cast<const xd_contact_property_f*>(cp), np, kDefaultStream);
 }
+
+void cu_plane_contact_force(const int tcm, device_plane_info_f* plan, float* pos, float* vel, float* omega,
+                            float* force, float* moment, float* mass, unsigned int np,
+                            device_contact_property_f* cp)
+{
+    xd_plane_contact_force_f(tcm, reinterpret_cast<const xd_plane_info_f*>(plan), pos, vel, omega, force,
+                             moment, mass, np, reinterpret_cast<const xd_contact_property_f*>(cp),
+                             kDefaultStream);
+}
+
+void cu_cube_contact_force(const int tcm, device_plane_info_f* plan, float* pos, float* vel, float* omega,
+                           float* force, float* moment, float* mass, unsigned int np,
+                           device_contact_property_f* cp)
+{
+    xd_cube_contact_force_f(tcm, reinterpret_cast<const xd_plane_info_f*>(plan), pos, vel, omega, force,
+                            moment, mass, np, reinterpret_cast<const xd_contact_property_f*>(cp),
+                            kDefaultStream);
+}
+
+void cu_particle_polygonObject_collision(const int tcm, device_polygon_info_f* dpi, float* dsph,
+                                         device_polygon_mass_info_f* dpmi, float* pos, float* vel,
+                                         float* omega, float* force, float* moment, float* mass,
+                                         unsigned int* sidx, unsigned int* cstart, unsigned int* cend,
+                                         device_contact_property_f* cp, unsigned int np)
+{
+    // the body count is not part of the reference signature: reactions are
+    // added with atomics (nbodies = 0)
+    xd_particle_polygon_collision_f(tcm, reinterpret_cast<const xd_polygon_info_f*>(dpi), dsph,
+                                    reinterpret_cast<xd_polygon_mass_info_f*>(dpmi), pos, vel, omega, force,
+                                    moment, mass, sidx, cstart, cend,
+                                    reinterpret_cast<const xd_contact_property_f*>(cp), np, 0, kDefaultStream);
+}
+
 void cu_cylinder_hertzian_contact_force(const int, device_cylinder_info*, float*, float*, float*,
                                         float*, float*, float*, unsigned int,
                                         device_contact_property_f*, float3*, float3*, float3*,
                                         float3&, float3&)
 {
+    // no caller in the reference application, and declared with the FP64
+    // cylinder struct but defined with the float one (def.cu:406-426)
     not_provided("cu_cylinder_hertzian_contact_force(float)");
 }
-float3 reductionD3(float3*, unsigned int)
+
+float3 reductionD3(float3* in, unsigned int np)
 {
-    not_provided("reductionD3(float)");
-    return make_float3(0.f, 0.f, 0.f);
+    float out[3] = { 0.f, 0.f, 0.f };
+    xd_reduction_f3(reinterpret_cast<const float*>(in), np, out, kDefaultStream);
+    return make_float3(out[0], out[1], out[2]);
 }
 
 // ------------------------------------------------------------ host classes

@@ -16,6 +16,12 @@ static_assert(sizeof(xd_plane_info) == 232, "device_plane_info layout");
 static_assert(sizeof(xd_polygon_info) == 152, "device_polygon_info layout");
 static_assert(sizeof(xd_polygon_mass_info) == 160, "device_polygon_mass_info layout");
 static_assert(offsetof(xd_polygon_mass_info, ep) == 32, "device_polygon_mass_info.ep offset");
+static_assert(sizeof(xd_device_parameters_f) == 64, "device_parameters_f layout");
+static_assert(sizeof(xd_contact_property_f) == 44, "device_contact_property_f layout");
+static_assert(sizeof(xd_plane_info_f) == 116, "device_plane_info_f layout");
+static_assert(sizeof(xd_polygon_info_f) == 76, "device_polygon_info_f layout");
+static_assert(sizeof(xd_polygon_mass_info_f) == 80, "device_polygon_mass_info_f layout");
+static_assert(offsetof(xd_polygon_mass_info_f, ep) == 16, "device_polygon_mass_info_f.ep offset");
 
 namespace xd {
 
@@ -156,6 +162,11 @@ size_t xd_sizeof(const char* n)
     if (!strcmp(n, "device_plane_info")) return sizeof(xd_plane_info);
     if (!strcmp(n, "device_polygon_info")) return sizeof(xd_polygon_info);
     if (!strcmp(n, "device_polygon_mass_info")) return sizeof(xd_polygon_mass_info);
+    if (!strcmp(n, "device_parameters_f")) return sizeof(xd_device_parameters_f);
+    if (!strcmp(n, "device_contact_property_f")) return sizeof(xd_contact_property_f);
+    if (!strcmp(n, "device_plane_info_f")) return sizeof(xd_plane_info_f);
+    if (!strcmp(n, "device_polygon_info_f")) return sizeof(xd_polygon_info_f);
+    if (!strcmp(n, "device_polygon_mass_info_f")) return sizeof(xd_polygon_mass_info_f);
     if (!strcmp(n, "xd_scene_desc")) return sizeof(xd_scene_desc);
     return 0;
 }

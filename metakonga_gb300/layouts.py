@@ -11,6 +11,14 @@ reference headers, and to the test oracle.
 * ``POLYGON``           device_polygon_info     (mphysics_cuda_dec.cuh:32-41), 152 B
 * ``POLYGON_MASS``      device_polygon_mass_info(mphysics_cuda_dec.cuh:57-65), 160 B
   (``ep`` is a CUDA double4, aligned to 16 bytes)
+
+and their single-precision twins (mphysics_cuda_dec.cuh:165-263):
+
+* ``PARAMS_F``            device_parameters_f        64 B
+* ``CONTACT_PROPERTY_F``  device_contact_property_f  44 B
+* ``PLANE_F``             device_plane_info_f       116 B
+* ``POLYGON_F``           device_polygon_info_f      76 B
+* ``POLYGON_MASS_F``      device_polygon_mass_info_f 80 B (``ep`` a float4 at offset 16)
 """
 import numpy as np
 
@@ -54,6 +62,53 @@ POLYGON_MASS = np.dtype({
 
 assert PARAMS.itemsize == 112 and CONTACT_PROPERTY.itemsize == 88
 assert PLANE.itemsize == 232 and POLYGON.itemsize == 152 and POLYGON_MASS.itemsize == 160
+
+F3 = ("<f4", (3,))
+
+PARAMS_F = np.dtype({
+    "names": ["np", "nsphere", "ncell", "grid", "dt", "half2dt", "cell_size", "cohesion",
+              "gravity", "world_origin"],
+    "formats": ["<u4", "<u4", "<u4", ("<u4", (3,)), "<f4", "<f4", "<f4", "<f4", F3, F3],
+    "offsets": [0, 4, 8, 12, 24, 28, 32, 36, 40, 52],
+    "itemsize": 64,
+})
+
+CONTACT_PROPERTY_F = np.dtype({
+    "names": list(CONTACT_PROPERTY.names),
+    "formats": ["<f4"] * 11,
+    "offsets": [4 * i for i in range(11)],
+    "itemsize": 44,
+})
+
+PLANE_F = np.dtype({
+    "names": list(PLANE.names),
+    "formats": ["<f4", "<f4"] + [F3] * 9,
+    "offsets": [0, 4] + [8 + 12 * i for i in range(9)],
+    "itemsize": 116,
+})
+
+POLYGON_F = np.dtype({
+    "names": list(POLYGON.names),
+    "formats": ["<i4"] + [F3] * 6,
+    "offsets": [0] + [4 + 12 * i for i in range(6)],
+    "itemsize": 76,
+})
+
+POLYGON_MASS_F = np.dtype({
+    "names": list(POLYGON_MASS.names),
+    "formats": [F3, ("<f4", (4,)), F3, F3, F3, F3],
+    "offsets": [0, 16, 32, 44, 56, 68],
+    "itemsize": 80,
+})
+
+
+def to_single(rec: np.ndarray, dtype: np.dtype) -> np.ndarray:
+    """A double-precision record array converted field by field to its
+    single-precision twin (values rounded to nearest float)."""
+    out = np.zeros(rec.shape, dtype=dtype)
+    for name in dtype.names:
+        out[name] = rec[name]
+    return out
 
 
 def make_params(*, np_, ncell, grid, dt, cell_size, world_origin, gravity, rolling=True,

@@ -283,6 +283,60 @@ class RefKernels:
         self.lib.xdref_update_polygon_object_data(_p(pmi), _p(vlist), _p(sphere), _p(poly),
                                                   _u(poly.shape[0]))
 
+    # ---- the reference's single-precision kernels (its float launchers, def.cu:254-466)
+
+    def set_params_f(self, prm_f, hash_grid=None):
+        """The float parameter block; hash_grid (an FP64 ``PARAMS`` record) sets
+        the FP64 block whose grid size the reference's calcGridHash reads."""
+        self.lib.xdref_set_params_f(_p(prm_f))
+        if hash_grid is not None:
+            self.lib.xdref_set_params(_p(hash_grid))
+
+    def vv_position_f(self, pos, vel, acc):
+        self.lib.xdref_vv_update_position_f(_p(pos), _p(vel), _p(acc), _u(pos.shape[0]))
+
+    def vv_velocity_f(self, vel, acc, omega, alpha, force, moment, mass, inertia):
+        self.lib.xdref_vv_update_velocity_f(_p(vel), _p(acc), _p(omega), _p(alpha), _p(force),
+                                            _p(moment), _p(mass), _p(inertia), _u(mass.shape[0]))
+
+    def detection_f(self, prm_f, pos, sphere=None):
+        npt = pos.shape[0]
+        nt = 0 if sphere is None else sphere.shape[0]
+        n = npt + nt
+        ncell = int(prm_f["ncell"])
+        h = np.zeros(n, np.uint32)
+        ix = np.zeros(n, np.uint32)
+        self.lib.xdref_calculate_hash_and_index_f(_p(h), _p(ix), _p(pos), _u(npt))
+        if nt:
+            self.lib.xdref_calculate_hash_and_index_polysphere_f(_p(h), _p(ix), _u(npt), _u(nt),
+                                                                 _p(sphere))
+        cs = np.zeros(ncell, np.uint32)
+        ce = np.zeros(ncell, np.uint32)
+        so = np.zeros(n, np.uint32)
+        self.lib.xdref_reorder_and_find_cell_start_f(_p(h), _p(ix), _p(cs), _p(ce), _p(so), _u(n),
+                                                     _u(ncell))
+        return h, ix, cs, ce, so
+
+    def p2p_f(self, pos, vel, omega, force, moment, mass, sorted_, cstart, cend, cp):
+        self.lib.xdref_calculate_p2p_f(_p(pos), _p(vel), _p(omega), _p(force), _p(moment),
+                                       _p(mass), _p(sorted_), _p(cstart), _p(cend), _p(cp),
+                                       _u(pos.shape[0]))
+
+    def plane_f(self, plane, pos, vel, omega, force, moment, mass, cp):
+        self.lib.xdref_plane_contact_force_f(_p(plane), _p(pos), _p(vel), _p(omega), _p(force),
+                                             _p(moment), _p(mass), _u(pos.shape[0]), _p(cp))
+
+    def cube_f(self, planes6, pos, vel, omega, force, moment, mass, cp):
+        self.lib.xdref_cube_contact_force_f(_p(planes6), _p(pos), _p(vel), _p(omega), _p(force),
+                                            _p(moment), _p(mass), _u(pos.shape[0]), _p(cp))
+
+    def polygon_f(self, poly, sphere, pmi, pos, vel, omega, force, moment, mass, sorted_, cstart,
+                  cend, cp):
+        self.lib.xdref_particle_polygon_collision_f(_p(poly), _p(sphere), _p(pmi), _p(pos),
+                                                    _p(vel), _p(omega), _p(force), _p(moment),
+                                                    _p(mass), _p(sorted_), _p(cstart), _p(cend),
+                                                    _p(cp), _u(pos.shape[0]))
+
     def step(self, sc):
         """One whole step in the reference's order, on the reference's kernels."""
         prm = sc.params

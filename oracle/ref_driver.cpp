@@ -201,4 +201,72 @@ void xdref_calculate_hash_and_index_f(unsigned* hash, unsigned* index, float* po
     launch(np, 512, [&] { calculateHashAndIndex_kernel(hash, index, (float4*)pos, np); });
 }
 
+/* def.cu:294-302 */
+void xdref_calculate_hash_and_index_polysphere_f(unsigned* hash, unsigned* index, unsigned sid,
+                                                 unsigned nsphere, float* sphere)
+{
+    launch(nsphere, 512, [&] {
+        calculateHashAndIndexForPolygonSphere_kernel(hash, index, sid, nsphere, (float4*)sphere);
+    });
+}
+
+/* def.cu:305-333 */
+void xdref_reorder_and_find_cell_start_f(unsigned* hash, unsigned* index, unsigned* cstart,
+                                         unsigned* cend, unsigned* sorted_index, unsigned np,
+                                         unsigned ncell)
+{
+    stable_sort_by_key(hash, index, np);
+    std::memset(cstart, 0xff, sizeof(unsigned) * ncell);
+    std::memset(cend, 0, sizeof(unsigned) * ncell);
+    launch(np, 512, [&] {
+        reorderDataAndFindCellStart_kernel_f(hash, index, cstart, cend, sorted_index, np);
+    });
+}
+
+/* def.cu:335-361 (tcm = 1) */
+void xdref_calculate_p2p_f(float* pos, float* vel, float* omega, float* force, float* moment,
+                           float* mass, unsigned* sorted_index, unsigned* cstart, unsigned* cend,
+                           device_contact_property_f* cp, unsigned np)
+{
+    launch(np, 512, [&] {
+        calculate_p2p_kernel<1>((float4*)pos, (float3*)vel, (float3*)omega, (float3*)force,
+                                (float3*)moment, mass, sorted_index, cstart, cend, cp, np);
+    });
+}
+
+/* def.cu:363-381 (tcm = 1) */
+void xdref_plane_contact_force_f(device_plane_info_f* plane, float* pos, float* vel, float* omega,
+                                 float* force, float* moment, float* mass, unsigned np,
+                                 device_contact_property_f* cp)
+{
+    launch(np, 512, [&] {
+        plane_contact_force_kernel<1>(plane, (float4*)pos, (float3*)vel, (float3*)omega,
+                                      (float3*)force, (float3*)moment, cp, mass, np);
+    });
+}
+
+/* def.cu:383-404: six launches over the cube's planes */
+void xdref_cube_contact_force_f(device_plane_info_f* planes, float* pos, float* vel, float* omega,
+                                float* force, float* moment, float* mass, unsigned np,
+                                device_contact_property_f* cp)
+{
+    for (int i = 0; i < 6; ++i)
+        xdref_plane_contact_force_f(planes + i, pos, vel, omega, force, moment, mass, np, cp);
+}
+
+/* def.cu:428-446 (tcm = 1); the body reaction's += runs in thread order here */
+void xdref_particle_polygon_collision_f(device_polygon_info_f* dpi, float* dsph,
+                                        device_polygon_mass_info_f* dpmi, float* pos, float* vel,
+                                        float* omega, float* force, float* moment, float* mass,
+                                        unsigned* sorted_index, unsigned* cstart, unsigned* cend,
+                                        device_contact_property_f* cp, unsigned np)
+{
+    launch(np, 512, [&] {
+        particle_polygonObject_collision_kernel<1>(dpi, (float4*)dsph, dpmi, (float4*)pos,
+                                                   (float3*)vel, (float3*)omega, (float3*)force,
+                                                   (float3*)moment, mass, sorted_index, cstart,
+                                                   cend, cp, np);
+    });
+}
+
 }  // extern "C"

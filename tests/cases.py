@@ -83,3 +83,42 @@ def small_hopper(n=1500, seed=5):
     sc.vel[:] = rng.normal(0.0, 0.05, sc.vel.shape)
     sc.omega[:] = rng.normal(0.0, 5.0, sc.omega.shape)
     return sc
+
+
+def to_single(sc):
+    """The single-precision form of a scene, as the reference's float path
+    holds it: float32 state rows, float records (``layouts.*_F``), the float
+    parameter block (dem_simulation.cpp:410-426: dt and the other values cast
+    to float, half2dt = float(0.5 * dt_f * dt_f) evaluated in double) and the
+    FP64 block whose grid size the float cell hash reads."""
+    from metakonga_gb300.layouts import (CONTACT_PROPERTY_F, PARAMS_F, PLANE_F, POLYGON_F,
+                                         POLYGON_MASS_F, to_single as rec_single)
+    p = sc.params
+    pf = np.zeros((), dtype=PARAMS_F)
+    pf["np"] = sc.np_
+    pf["nsphere"] = 0
+    pf["ncell"] = p["ncell"]
+    pf["grid"] = p["grid"]
+    dt_f = np.float32(p["dt"])
+    pf["dt"] = dt_f
+    pf["half2dt"] = np.float32(0.5 * np.float64(dt_f) * np.float64(dt_f))
+    pf["cell_size"] = np.float32(p["cell_size"])
+    pf["cohesion"] = 0.0
+    pf["gravity"] = np.asarray(p["gravity"], np.float32)
+    pf["world_origin"] = np.asarray(p["world_origin"], np.float32)
+    hash_grid = p.copy()
+    hash_grid["np"] = sc.np_
+    out = {"params_f": pf, "hash_grid": hash_grid}
+    for k in ("pos", "vel", "acc", "omega", "alpha", "mass", "inertia"):
+        out[k] = np.ascontiguousarray(getattr(sc, k), dtype=np.float32)
+    out["force"] = (out["mass"][:, None] * pf["gravity"][None, :]).astype(np.float32)
+    out["moment"] = np.zeros_like(out["vel"])
+    out["cp_pp"] = rec_single(sc.cp_pp.reshape(1), CONTACT_PROPERTY_F)
+    out["planes"] = rec_single(sc.planes, PLANE_F)
+    out["cp_planes"] = rec_single(sc.cp_planes, CONTACT_PROPERTY_F)
+    if sc.ntri:
+        out["poly"] = rec_single(sc.poly, POLYGON_F)
+        out["sphere"] = np.ascontiguousarray(sc.sphere, dtype=np.float32)
+        out["pmi"] = rec_single(sc.pmi, POLYGON_MASS_F)
+        out["cp_poly"] = rec_single(sc.cp_poly, CONTACT_PROPERTY_F)
+    return out

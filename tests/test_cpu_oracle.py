@@ -13,7 +13,9 @@ from .cases import packed_scene, random_positions, small_drum
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-GOLDEN = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+GOLDEN = sorted(p for p in glob.glob(os.path.join(HERE, "golden", "*.npz"))
+                if not os.path.basename(p).startswith("f32_"))
+GOLDEN_F32 = sorted(glob.glob(os.path.join(HERE, "golden", "f32_*.npz")))
 STATE = ("pos", "vel", "acc", "omega", "alpha", "force", "moment", "mass", "inertia")
 
 
@@ -61,6 +63,41 @@ def test_oracle_reproduces_golden(oracle, path):
 
 def test_golden_fixtures_present():
     assert len(GOLDEN) >= 2
+    assert len(GOLDEN_F32) == 3
+
+
+def test_fp32_golden_reproduced_by_reference_kernels(tmp_path, monkeypatch):
+    """The single-precision fixtures are what the reference's float kernels
+    give now (regenerated into a temporary folder and compared bit for bit)."""
+    _ref()
+    from tests.golden import make_golden_fp32 as gen
+    monkeypatch.setattr(gen, "HERE", str(tmp_path))
+    gen.main()
+    for path in GOLDEN_F32:
+        a = np.load(path)
+        b = np.load(os.path.join(tmp_path, os.path.basename(path)))
+        assert sorted(a.files) == sorted(b.files)
+        for k in a.files:
+            assert np.array_equal(a[k], b[k]), (path, k)
+
+
+def test_fp32_layouts_match_reference_structs():
+    """The float records have the reference's sizes (mphysics_cuda_dec.cuh:165-246),
+    also as compiled into the reference kernels' host build when present."""
+    from metakonga_gb300 import _lib
+    L = _lib.lib()
+    for name, dt in (("device_parameters_f", layouts.PARAMS_F),
+                     ("device_contact_property_f", layouts.CONTACT_PROPERTY_F),
+                     ("device_plane_info_f", layouts.PLANE_F),
+                     ("device_polygon_info_f", layouts.POLYGON_F),
+                     ("device_polygon_mass_info_f", layouts.POLYGON_MASS_F)):
+        assert L.xd_sizeof(name.encode()) == dt.itemsize, name
+    from oracle.pyoracle import RefKernels
+    if RefKernels.available():
+        import ctypes as C
+        lib = C.CDLL(RefKernels().lib._name)
+        lib.xdref_sizeof_params_f.restype = C.c_uint
+        assert lib.xdref_sizeof_params_f() == layouts.PARAMS_F.itemsize
 
 
 def _ref():
