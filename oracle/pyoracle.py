@@ -46,7 +46,36 @@ class _Scene(C.Structure):
         ("hash", _vp), ("index", _vp), ("sorted", _vp), ("cstart", _vp), ("cend", _vp),
         ("cp_pp", _vp), ("nplanes", _u), ("planes", _vp), ("cp_planes", _vp),
         ("ntri", _u), ("poly", _vp), ("sphere", _vp), ("pmi", _vp), ("cp_poly", _vp),
+        ("hist", _vp),
     ]
+
+
+class _History(C.Structure):
+    _fields_ = [("slots", _u), ("np", _u), ("key", _vp), ("delta", _vp), ("overflow", C.c_ulonglong)]
+
+
+HIST_EMPTY = 0xFFFFFFFF
+HIST_PLANE = 0x80000000
+HIST_TRI = 0xC0000000
+
+
+class History:
+    """Tangential-spring history of a scene (xdo_history): up to `slots`
+    contacts per particle, key[s, i] and delta[s, i, 3]."""
+
+    def __init__(self, np_: int, slots: int = 12):
+        assert 1 <= slots <= 32
+        self.key = np.full((slots, np_), HIST_EMPTY, np.uint32)
+        self.delta = np.zeros((slots, np_, 3))
+        self.c = _History(slots, np_, self.key.ctypes.data, self.delta.ctypes.data, 0)
+
+    @property
+    def overflow(self) -> int:
+        return int(self.c.overflow)
+
+    def contacts(self, i: int) -> dict:
+        """{key: delta} of particle i."""
+        return {int(k): self.delta[s, i].copy() for s, k in enumerate(self.key[:, i]) if k != HIST_EMPTY}
 
 
 class Oracle:
@@ -147,6 +176,17 @@ class Oracle:
                                         _p(cp_planes) if npl else None, _u(npl), _p(mag))
         return mag
 
+    def hist_p2p(self, prm, pos, vel, omega, force, moment, mass, sorted_, cstart, cend, cp,
+                 history):
+        self.lib.xdo_hist_p2p(_p(prm), _p(pos), _p(vel), _p(omega), _p(force), _p(moment),
+                              _p(mass), _p(sorted_), _p(cstart), _p(cend), _p(cp),
+                              _u(pos.shape[0]), C.byref(history.c))
+
+    def hist_planes(self, prm, planes, cps, pos, vel, omega, force, moment, mass, history):
+        self.lib.xdo_hist_planes(_p(prm), _p(planes), _p(cps), _u(planes.shape[0]), _p(pos),
+                                 _p(vel), _p(omega), _p(force), _p(moment), _p(mass),
+                                 _u(pos.shape[0]), C.byref(history.c))
+
     def pair_list(self, prm, pos, sorted_, cstart, cend, cap=None):
         npt = pos.shape[0]
         if cap is None:
@@ -183,12 +223,16 @@ class Oracle:
                 "sorted": np.zeros(n, np.uint32), "cstart": np.zeros(sc.ncell, np.uint32),
                 "cend": np.zeros(sc.ncell, np.uint32)}
 
-    def run(self, sc, nsteps: int, cpu_path: bool = False):
-        """Advance ``sc`` (in place) by nsteps whole steps; returns the grid work arrays."""
+    def run(self, sc, nsteps: int, cpu_path: bool = False, history: "History" = None):
+        """Advance ``sc`` (in place) by nsteps whole steps; returns the grid work
+        arrays.  With ``history`` the contacts keep tangential springs."""
         for a in ("pos", "vel", "acc", "omega", "alpha", "force", "moment", "mass", "inertia"):
             assert getattr(sc, a).flags["C_CONTIGUOUS"]
         work = self._work(sc)
         s = self._scene_struct(sc, work)
+        if history is not None:
+            assert not cpu_path
+            s.hist = C.addressof(history.c)
         fn = self.lib.xdo_cpu_run_steps if cpu_path else self.lib.xdo_run_steps
         fn(C.byref(s), _u(nsteps))
         return work

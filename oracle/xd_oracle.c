@@ -646,6 +646,262 @@ void xdo_update_polygon_object_data(const xdo_polygon_mass* dpmi, const double* 
     }
 }
 
+/* ------------------------------------------------ tangential history */
+
+typedef struct {
+    unsigned keys[XDO_HIST_MAX];
+    unsigned freem, matched;
+} hstate;
+
+static unsigned hist_class(unsigned k) { return k < XDO_HIST_PLANE ? 0u : (k < XDO_HIST_TRI ? 1u : 2u); }
+
+static void hist_begin(const xdo_history* h, unsigned i, hstate* st)
+{
+    st->freem = 0;
+    st->matched = 0;
+    for (unsigned s = 0; s < h->slots; ++s) {
+        st->keys[s] = h->key[(size_t)s * h->np + i];
+        if (st->keys[s] == XDO_HIST_EMPTY) st->freem |= 1u << s;
+    }
+}
+
+/* The entry of `key` (its old d in d[]), else a free entry (d = 0); -1 when
+ * none is free (the contact then has no history this step). */
+static int hist_slot(xdo_history* h, hstate* st, unsigned i, unsigned key, double d[3])
+{
+    d[0] = d[1] = d[2] = 0.0;
+    for (unsigned s = 0; s < h->slots; ++s)
+        if (st->keys[s] == key) {
+            const double* p = h->delta + ((size_t)s * h->np + i) * 3;
+            d[0] = p[0]; d[1] = p[1]; d[2] = p[2];
+            st->matched |= 1u << s;
+            return (int)s;
+        }
+    if (st->freem) {
+        unsigned s = 0;
+        while (!(st->freem & (1u << s))) ++s;
+        st->freem &= ~(1u << s);
+        h->key[(size_t)s * h->np + i] = key;
+        return (int)s;
+    }
+    h->overflow++;
+    return -1;
+}
+
+static void hist_store(xdo_history* h, int s, unsigned i, const double d[3])
+{
+    if (s < 0) return;
+    double* p = h->delta + ((size_t)s * h->np + i) * 3;
+    p[0] = d[0]; p[1] = d[1]; p[2] = d[2];
+}
+
+/* entries of class cls whose contact did not recur this step are freed */
+static void hist_end(xdo_history* h, const hstate* st, unsigned i, unsigned cls)
+{
+    for (unsigned s = 0; s < h->slots; ++s) {
+        unsigned k = st->keys[s];
+        if (k == XDO_HIST_EMPTY || hist_class(k) != cls || (st->matched & (1u << s))) continue;
+        h->key[(size_t)s * h->np + i] = XDO_HIST_EMPTY;
+        double* p = h->delta + ((size_t)s * h->np + i) * 3;
+        p[0] = p[1] = p[2] = 0.0;
+    }
+}
+
+/* DHSModel's normal force (impl:385-388). */
+static v3 normal_force(const fconst* c, double ir, double jr, double Ei, double Ej, double pri,
+                       double prj, double coh, double cdist, v3 dv, v3 unit)
+{
+    double fsn = -c->kn * pow(cdist, 1.5);
+    double fdn = c->vn * dot(dv, unit);
+    double fca = cohesion_force(ir, jr, Ei, Ej, pri, prj, coh, fsn);
+    return scl(fsn + fca + fdn, unit);
+}
+
+/* The tangential spring with history (see xd_oracle.h). */
+static void hist_tangential(const fconst* c, double ir, v3 dv, v3 unit, double dt, v3 Fn,
+                            double d[3], v3* Ft, v3* M)
+{
+    v3 vt = sub(dv, scl(dot(dv, unit), unit));
+    v3 d0 = mk(d[0], d[1], d[2]);
+    double m0 = len(d0);
+    v3 dp = sub(d0, scl(dot(d0, unit), unit));
+    double mp = len(dp);
+    v3 dn = mp > 0.0 ? scl(m0 / mp, dp) : mk(0, 0, 0);
+    dn = add(dn, scl(dt, vt));
+    v3 ft = add(scl(c->ks, dn), scl(c->vs, vt));
+    double fmax = c->mu * len(Fn);
+    double mf = len(ft);
+    if (mf > fmax) {
+        ft = scl(fmax / mf, ft);
+        dn = dvd(sub(ft, scl(c->vs, vt)), c->ks);
+    }
+    d[0] = dn.x; d[1] = dn.y; d[2] = dn.z;
+    *Ft = ft;
+    *M = cross(scl(ir, unit), ft);
+}
+
+void xdo_hist_p2p(const xdo_params* prm, const double* pos, const double* vel,
+                  const double* omega, double* force, double* moment, const double* mass,
+                  const unsigned* sorted_index, const unsigned* cstart, const unsigned* cend,
+                  const xdo_contact_property* cp, unsigned np, xdo_history* h)
+{
+    for (unsigned id = 0; id < np; ++id) {
+        const double* ip4 = pos + 4 * (size_t)id;
+        v3 ipos = ld3(ip4);
+        v3 ivel = ld3(vel + 3 * (size_t)id);
+        v3 iomega = ld3(omega + 3 * (size_t)id);
+        int gp[3];
+        xdo_grid_pos(prm, ip4, gp);
+        double ir = ip4[3];
+        double im = mass[id];
+        hstate st;
+        hist_begin(h, id, &st);
+        v3 sumF = mk(0, 0, 0), sumM = mk(0, 0, 0);
+        for (int z = -1; z <= 1; z++)
+            for (int y = -1; y <= 1; y++)
+                for (int x = -1; x <= 1; x++) {
+                    int nb[3] = { gp[0] + x, gp[1] + y, gp[2] + z };
+                    unsigned hh = xdo_grid_hash(prm, nb);
+                    unsigned s0 = cstart[hh];
+                    if (s0 == 0xffffffffu) continue;
+                    unsigned en = cend[hh];
+                    for (unsigned j = s0; j < en; j++) {
+                        unsigned k = sorted_index[j];
+                        if (id == k || k >= np) continue;
+                        const double* jp4 = pos + 4 * (size_t)k;
+                        double jr = jp4[3];
+                        v3 rp = mk(jp4[0] - ipos.x, jp4[1] - ipos.y, jp4[2] - ipos.z);
+                        double dist = len(rp);
+                        double cdist = (ir + jr) - dist;
+                        if (cdist > 0) {
+                            v3 jvel = ld3(vel + 3 * (size_t)k);
+                            v3 jomega = ld3(omega + 3 * (size_t)k);
+                            v3 unit = dvd(rp, dist);
+                            v3 rv = prm->rolling
+                                ? sub(add(jvel, cross(jomega, scl(-jr, unit))),
+                                      add(ivel, cross(iomega, scl(ir, unit))))
+                                : sub(jvel, ivel);
+                            fconst c = get_constant(ir, jr, im, mass[k], cp);
+                            v3 Fn = normal_force(&c, ir, jr, cp->Ei, cp->Ej, cp->pri, cp->prj, cp->coh,
+                                                 cdist, rv, unit);
+                            double d[3];
+                            int sl = hist_slot(h, &st, id, k, d);
+                            v3 Ft, M;
+                            hist_tangential(&c, ir, rv, unit, prm->dt, Fn, d, &Ft, &M);
+                            hist_store(h, sl, id, d);
+                            sumF = add(sumF, add(Fn, Ft));
+                            sumM = add(sumM, M);
+                        }
+                    }
+                }
+        hist_end(h, &st, id, 0u);
+        acc3(force + 3 * (size_t)id, sumF);
+        acc3(moment + 3 * (size_t)id, sumM);
+    }
+}
+
+void xdo_hist_planes(const xdo_params* prm, const xdo_plane* planes,
+                     const xdo_contact_property* cps, unsigned nplanes, const double* pos,
+                     const double* vel, const double* omega, double* force, double* moment,
+                     const double* mass, unsigned np, xdo_history* h)
+{
+    for (unsigned id = 0; id < np; ++id) {
+        double m = mass[id];
+        const double* p4 = pos + 4 * (size_t)id;
+        v3 ipos3 = ld3(p4);
+        double r = p4[3];
+        v3 ivel = ld3(vel + 3 * (size_t)id);
+        v3 iomega = ld3(omega + 3 * (size_t)id);
+        hstate st;
+        hist_begin(h, id, &st);
+        for (unsigned w = 0; w < nplanes; ++w) {
+            const xdo_plane* pl = planes + w;
+            v3 Fn = mk(0, 0, 0), Ft = mk(0, 0, 0), M = mk(0, 0, 0);
+            v3 dp = sub(ipos3, ld3(pl->xw));
+            v3 unit = mk(0, 0, 0);
+            v3 wp = mk(dot(dp, ld3(pl->u1)), dot(dp, ld3(pl->u2)), dot(dp, ld3(pl->uw)));
+            double cdist = plane_detection(pl, ipos3, wp, &unit, r);
+            if (cdist > 0) {
+                v3 dv = prm->rolling ? neg(add(ivel, cross(iomega, scl(r, unit)))) : neg(ivel);
+                fconst c = get_constant(r, 0.0, m, 0.0, cps + w);
+                Fn = normal_force(&c, 0, 0, 0, 0, 0, 0, cps[w].coh, cdist, dv, unit);
+                double d[3];
+                int sl = hist_slot(h, &st, id, XDO_HIST_PLANE | w, d);
+                hist_tangential(&c, 0.0, dv, unit, prm->dt, Fn, d, &Ft, &M);
+                hist_store(h, sl, id, d);
+            }
+            acc3(force + 3 * (size_t)id, add(Fn, Ft));
+            acc3(moment + 3 * (size_t)id, M);
+        }
+        hist_end(h, &st, id, 1u);
+    }
+}
+
+void xdo_hist_polygon(const xdo_params* prm, const xdo_polygon* dpi, xdo_polygon_mass* dpmi,
+                      const double* pos, const double* vel, const double* omega, double* force,
+                      double* moment, const double* mass, const unsigned* sorted_index,
+                      const unsigned* cstart, const unsigned* cend, const xdo_contact_property* cp,
+                      xdo_history* h)
+{
+    unsigned cnp = prm->np;
+    for (unsigned id = 0; id < cnp; ++id) {
+        const double* p4 = pos + 4 * (size_t)id;
+        double im = mass[id];
+        v3 ipos = ld3(p4);
+        v3 ivel = ld3(vel + 3 * (size_t)id);
+        v3 iomega = ld3(omega + 3 * (size_t)id);
+        int gp[3];
+        xdo_grid_pos(prm, p4, gp);
+        double ir = p4[3];
+        hstate st;
+        hist_begin(h, id, &st);
+        v3 sum_force = mk(0, 0, 0), sum_moment = mk(0, 0, 0);
+        for (int z = -1; z <= 1; z++)
+            for (int y = -1; y <= 1; y++)
+                for (int x = -1; x <= 1; x++) {
+                    int nb[3] = { gp[0] + x, gp[1] + y, gp[2] + z };
+                    unsigned hh = xdo_grid_hash(prm, nb);
+                    unsigned s0 = cstart[hh];
+                    if (s0 == 0xffffffffu) continue;
+                    unsigned en = cend[hh];
+                    for (unsigned j = s0; j < en; j++) {
+                        unsigned k = sorted_index[j];
+                        if (k < cnp) continue;
+                        k -= cnp;
+                        const xdo_polygon* tri = dpi + k;
+                        unsigned pidx = (unsigned)tri->id;
+                        xdo_polygon_mass* pmi = dpmi + pidx;
+                        v3 P = ld3(tri->P), Q = ld3(tri->Q), R = ld3(tri->R);
+                        v3 cpt = closest_pt_triangle(P, Q, R, ipos);
+                        v3 po2cp = sub(cpt, ld3(pmi->origin));
+                        double cdist = ir - len(sub(ipos, cpt));
+                        if (cdist > 0) {
+                            v3 unit = neg(cross(sub(Q, P), sub(R, P)));
+                            unit = dvd(unit, len(unit));
+                            v3 pvel = ld3(pmi->vel), pom = ld3(pmi->omega);
+                            v3 dv = prm->rolling
+                                ? sub(add(pvel, cross(pom, po2cp)), add(ivel, cross(iomega, scl(ir, unit))))
+                                : sub(pvel, ivel);
+                            fconst c = get_constant(ir, 0, im, 0, cp + pidx);
+                            v3 Fn = normal_force(&c, 0, 0, 0, 0, 0, 0, 0, cdist, dv, unit);
+                            double d[3];
+                            int sl = hist_slot(h, &st, id, XDO_HIST_TRI | k, d);
+                            v3 Ft, M;
+                            hist_tangential(&c, 0.0, dv, unit, prm->dt, Fn, d, &Ft, &M);
+                            hist_store(h, sl, id, d);
+                            sum_force = add(sum_force, add(Fn, Ft));
+                            sum_moment = add(sum_moment, M);
+                            acc3(pmi->force, neg(add(Fn, Ft)));
+                            acc3(pmi->moment, neg(cross(po2cp, add(Fn, Ft))));
+                        }
+                    }
+                }
+        hist_end(h, &st, id, 2u);
+        acc3(force + 3 * (size_t)id, sum_force);
+        acc3(moment + 3 * (size_t)id, sum_moment);
+    }
+}
+
 /* ------------------------------------------------------------ whole step */
 
 /* dem_simulation::oneStepAnalysis (dem_simulation.cpp:447-469) with
@@ -662,16 +918,28 @@ void xdo_step(xdo_scene* s)
     if (s->ntri)
         xdo_calculate_hash_and_index_polysphere(prm, s->hash, s->index, np, s->ntri, s->sphere);
     xdo_reorder_and_find_cell_start(s->hash, s->index, s->cstart, s->cend, s->sorted, n, prm->ncell);
-    if (s->cp_pp)
-        xdo_calculate_p2p(prm, s->pos, s->vel, s->omega, s->force, s->moment, s->mass, s->sorted,
-                          s->cstart, s->cend, s->cp_pp, np);
-    for (unsigned i = 0; i < s->nplanes; ++i)
-        xdo_plane_contact_force(prm, s->planes + i, s->pos, s->vel, s->omega, s->force, s->moment,
-                                s->mass, np, s->cp_planes + i);
-    if (s->ntri)
-        xdo_particle_polygon_collision(prm, s->poly, s->sphere, s->pmi, s->pos, s->vel, s->omega,
-                                       s->force, s->moment, s->mass, s->sorted, s->cstart, s->cend,
-                                       s->cp_poly, np);
+    if (s->hist) {
+        if (s->cp_pp)
+            xdo_hist_p2p(prm, s->pos, s->vel, s->omega, s->force, s->moment, s->mass, s->sorted,
+                         s->cstart, s->cend, s->cp_pp, np, s->hist);
+        if (s->nplanes)
+            xdo_hist_planes(prm, s->planes, s->cp_planes, s->nplanes, s->pos, s->vel, s->omega,
+                            s->force, s->moment, s->mass, np, s->hist);
+        if (s->ntri)
+            xdo_hist_polygon(prm, s->poly, s->pmi, s->pos, s->vel, s->omega, s->force, s->moment,
+                             s->mass, s->sorted, s->cstart, s->cend, s->cp_poly, s->hist);
+    } else {
+        if (s->cp_pp)
+            xdo_calculate_p2p(prm, s->pos, s->vel, s->omega, s->force, s->moment, s->mass,
+                              s->sorted, s->cstart, s->cend, s->cp_pp, np);
+        for (unsigned i = 0; i < s->nplanes; ++i)
+            xdo_plane_contact_force(prm, s->planes + i, s->pos, s->vel, s->omega, s->force,
+                                    s->moment, s->mass, np, s->cp_planes + i);
+        if (s->ntri)
+            xdo_particle_polygon_collision(prm, s->poly, s->sphere, s->pmi, s->pos, s->vel,
+                                           s->omega, s->force, s->moment, s->mass, s->sorted,
+                                           s->cstart, s->cend, s->cp_poly, np);
+    }
     xdo_vv_update_velocity(prm, s->vel, s->acc, s->omega, s->alpha, s->force, s->moment, s->mass,
                            s->inertia, np);
 }

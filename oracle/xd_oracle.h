@@ -140,6 +140,43 @@ unsigned long long xdo_pair_list(const xdo_params* prm, const double* pos,
                                  const unsigned* cend, unsigned np, unsigned* pairs,
                                  unsigned long long cap);
 
+/* ---- tangential-spring history: an extension with no counterpart in the
+ *      reference (its DHSModel, impl:379-401, keeps no state between steps).
+ *      Each particle holds up to `slots` contacts keyed by partner: particle
+ *      j -> j, plane w -> XDO_HIST_PLANE | w, triangle t -> XDO_HIST_TRI | t.
+ *      Per contact and step, with vt the tangential relative velocity:
+ *        d <- d - (d.u)u, rescaled to |d| (turned onto the new tangent plane)
+ *        d <- d + vt dt;  Ft = ks d + vs vt
+ *        if |Ft| > mu |Fn|: Ft <- (mu |Fn| / |Ft|) Ft, d <- (Ft - vs vt) / ks
+ *        M = (ir u) x Ft  (ir = 0 for planes and triangles, as in the reference)
+ *      A new contact starts from d = 0, so its first step gives the
+ *      reference's DHS force; a contact that ends frees its entry. ---- */
+#define XDO_HIST_EMPTY 0xffffffffu
+#define XDO_HIST_PLANE 0x80000000u
+#define XDO_HIST_TRI 0xC0000000u
+#define XDO_HIST_MAX 32
+typedef struct xdo_history {
+    unsigned slots;                /* entries per particle, <= XDO_HIST_MAX */
+    unsigned np;
+    unsigned* key;                 /* key[s * np + i] */
+    double* delta;                 /* delta[(s * np + i) * 3 + a] */
+    unsigned long long overflow;   /* contacts that found no free entry (force without history) */
+} xdo_history;
+
+void xdo_hist_p2p(const xdo_params* prm, const double* pos, const double* vel,
+                  const double* omega, double* force, double* moment, const double* mass,
+                  const unsigned* sorted_index, const unsigned* cstart, const unsigned* cend,
+                  const xdo_contact_property* cp, unsigned np, xdo_history* h);
+void xdo_hist_planes(const xdo_params* prm, const xdo_plane* planes,
+                     const xdo_contact_property* cps, unsigned nplanes, const double* pos,
+                     const double* vel, const double* omega, double* force, double* moment,
+                     const double* mass, unsigned np, xdo_history* h);
+void xdo_hist_polygon(const xdo_params* prm, const xdo_polygon* dpi, xdo_polygon_mass* dpmi,
+                      const double* pos, const double* vel, const double* omega, double* force,
+                      double* moment, const double* mass, const unsigned* sorted_index,
+                      const unsigned* cstart, const unsigned* cend, const xdo_contact_property* cp,
+                      xdo_history* h);
+
 /* ---- one whole step in the reference's order (dem_simulation.cpp:447-469,
  *      contactManager.cpp:156-185) ---- */
 typedef struct xdo_scene {
@@ -157,6 +194,7 @@ typedef struct xdo_scene {
     double* sphere;
     xdo_polygon_mass* pmi;
     const xdo_contact_property* cp_poly; /* one per polygon object */
+    xdo_history* hist;                   /* NULL: the reference's DHS, no history */
 } xdo_scene;
 
 void xdo_step(xdo_scene* s);
