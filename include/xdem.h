@@ -492,6 +492,28 @@ unsigned long long xd_scene_launches(xd_scene* scene, unsigned nsteps);
 int xd_scene_rebuilds(xd_scene* scene, unsigned long long* count, unsigned long long* launches_each,
                       void* stream);
 
+/* Tangential-spring history, an extension: the reference's DHSModel
+ * (mphysics_cuda_impl.cuh:379-401) keeps no state between steps.  With
+ * slots > 0 (at most 32) every particle keeps up to `slots` contacts keyed
+ * by partner (particle j -> j, plane w -> 0x80000000 | w, triangle t ->
+ * 0xC0000000 | t) with an FP64 tangential spring d.  Per contact and step,
+ * with u the contact normal and vt the tangential relative velocity:
+ *   d <- d - (d.u)u, rescaled to |d|;  d <- d + vt dt;  Ft = ks d + vs vt;
+ *   if |Ft| > mu |Fn|:  Ft <- mu |Fn| Ft / |Ft|,  d <- (Ft - vs vt) / ks;
+ *   the moment is (ir u) x Ft with ir = 0 for walls, as in the reference.
+ * A new contact starts from d = 0, so its first step has the reference's DHS
+ * force; a contact that ends frees its entry; a contact that finds no free
+ * entry is counted as overflow and computed without history.  The normal
+ * force is the reference's.  slots = 0 restores the reference model.  The
+ * call empties the tables. */
+int xd_scene_set_tangential_history(xd_scene* scene, unsigned slots);
+
+/* The history tables in original particle order: keys[s * np + i] (0xffffffff
+ * empty) and delta[(s * np + i) * 3 + a], and the overflow count.  Any
+ * pointer may be NULL.  Synchronous. */
+int xd_scene_download_history(xd_scene* scene, unsigned* keys, double* delta,
+                              unsigned long long* overflow, void* stream);
+
 /* Advance `count` independent scenes (scenes[i] by nsteps[i] steps) side by
  * side on the current device: the scenes are spread over a pool of 32
  * library streams that start after the work queued on `stream` and that

@@ -30,6 +30,7 @@ namespace xd {
 
 // ------------------------------------------------------- particle-particle
 
+template <bool HIST>
 __global__ void __launch_bounds__(128) k_p2p(Params P, const double* __restrict__ pos,
                                              const double* __restrict__ vel,
                                              const double* __restrict__ omega,
@@ -38,10 +39,13 @@ __global__ void __launch_bounds__(128) k_p2p(Params P, const double* __restrict_
                                              const unsigned* __restrict__ sorted,
                                              const unsigned* __restrict__ cstart,
                                              const unsigned* __restrict__ cend,
-                                             const xd_contact_property* __restrict__ cp, unsigned np)
+                                             const xd_contact_property* __restrict__ cp, unsigned np,
+                                             HistTable ht)
 {
     unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= np) return;
+    HistState hs;
+    if (HIST) hist_begin(ht, id, hs);
     const PairConst pc = load_pair_const(cp);
     d4 ip = ld4(pos, id);
     d3 ipos = xyz(ip);
@@ -75,8 +79,16 @@ __global__ void __launch_bounds__(128) k_p2p(Params P, const double* __restrict_
                         d3 rv = P.rolling ? (jvel + cross(jomega, -jr * unit)) - (ivel + cross(iomega, ir * unit))
                                           : (jvel - ivel);
                         Fc c = get_constant(pc, ir, jr, im, jm);
-                        dhs(c, ir, jr, pc.Ei, pc.Ej, pc.pri, pc.prj, pc.coh, cdist, rv, unit, P.dt,
-                            Ft, Fn, M);
+                        if (HIST) {
+                            Fn = normal_force(c, ir, jr, pc.Ei, pc.Ej, pc.pri, pc.prj, pc.coh, cdist, rv, unit);
+                            d3 d;
+                            int sl = hist_slot(ht, hs, id, k, d);
+                            hist_tangential(c, ir, rv, unit, P.dt, Fn, d, Ft, M);
+                            hist_store(ht, sl, id, d);
+                        } else {
+                            dhs(c, ir, jr, pc.Ei, pc.Ej, pc.pri, pc.prj, pc.coh, cdist, rv, unit, P.dt,
+                                Ft, Fn, M);
+                        }
                         sumF += Fn + Ft;
                         sumM += M;
                     }
@@ -84,6 +96,7 @@ __global__ void __launch_bounds__(128) k_p2p(Params P, const double* __restrict_
             }
         }
     }
+    if (HIST) hist_end(ht, hs, id, 0u);
     double* f = force + 3 * (size_t)id;
     double* m = moment + 3 * (size_t)id;
     f[0] += sumF.x; f[1] += sumF.y; f[2] += sumF.z;
@@ -95,6 +108,7 @@ __global__ void __launch_bounds__(128) k_p2p(Params P, const double* __restrict_
 // Planes applied in order; each adds Fn + Ft to the running force exactly
 // like one plane_contact_force_kernel launch per plane.  cp_stride = 0
 // shares one property (cube), 1 gives one per plane.
+template <bool HIST>
 __global__ void __launch_bounds__(128) k_planes(Params P, const xd_plane_info* __restrict__ planes,
                                                 const xd_contact_property* __restrict__ cps,
                                                 unsigned cp_stride, unsigned nplanes,
@@ -103,10 +117,13 @@ __global__ void __launch_bounds__(128) k_planes(Params P, const xd_plane_info* _
                                                 const double* __restrict__ omega,
                                                 double* __restrict__ force,
                                                 double* __restrict__ moment,
-                                                const double* __restrict__ mass, unsigned np)
+                                                const double* __restrict__ mass, unsigned np,
+                                                HistTable ht)
 {
     unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= np) return;
+    HistState hs;
+    if (HIST) hist_begin(ht, id, hs);
     double m = __ldg(mass + id);
     d4 ip = ld4(pos, id);
     d3 ipos3 = xyz(ip);
@@ -127,11 +144,20 @@ __global__ void __launch_bounds__(128) k_planes(Params P, const xd_plane_info* _
             PairConst pc = load_pair_const(cp);
             d3 dv = P.rolling ? -(ivel + cross(iomega, r * unit)) : -ivel;
             Fc c = get_constant(pc, r, 0.0, m, 0.0);
-            dhs(c, 0, 0, 0, 0, 0, 0, pc.coh, cdist, dv, unit, P.dt, Ft, Fn, M);
+            if (HIST) {
+                Fn = normal_force(c, 0, 0, 0, 0, 0, 0, pc.coh, cdist, dv, unit);
+                d3 d;
+                int sl = hist_slot(ht, hs, id, kHistPlane | w, d);
+                hist_tangential(c, 0.0, dv, unit, P.dt, Fn, d, Ft, M);
+                hist_store(ht, sl, id, d);
+            } else {
+                dhs(c, 0, 0, 0, 0, 0, 0, pc.coh, cdist, dv, unit, P.dt, Ft, Fn, M);
+            }
         }
         f += Fn + Ft;
         mo += M;
     }
+    if (HIST) hist_end(ht, hs, id, 1u);
     st3(force, id, f);
     st3(moment, id, mo);
 }
@@ -144,7 +170,7 @@ __device__ __forceinline__ d3 ldp(const double* a) { return mk(__ldg(a), __ldg(a
 // bodies and reduces them per block in a fixed order (block partials are
 // summed by k_polygon_reaction_final); NB == 0 adds with atomics (used when
 // the caller does not say how many bodies there are).
-template <int NB>
+template <int NB, bool HIST>
 __global__ void __launch_bounds__(128) k_polygon(Params P, const xd_polygon_info* __restrict__ dpi,
                                                  xd_polygon_mass_info* __restrict__ dpmi,
                                                  const double* __restrict__ pos,
@@ -157,7 +183,7 @@ __global__ void __launch_bounds__(128) k_polygon(Params P, const xd_polygon_info
                                                  const unsigned* __restrict__ cstart,
                                                  const unsigned* __restrict__ cend,
                                                  const xd_contact_property* __restrict__ cp,
-                                                 double* __restrict__ partials)
+                                                 double* __restrict__ partials, HistTable ht)
 {
     constexpr int NBR = NB > 0 ? NB : 1;
     double react[NBR][6];
@@ -178,6 +204,8 @@ __global__ void __launch_bounds__(128) k_polygon(Params P, const xd_polygon_info
         double ir = ip.w;
         d3 M = mk(0, 0, 0), Fn = mk(0, 0, 0), Ft = mk(0, 0, 0);
         d3 sum_force = mk(0, 0, 0), sum_moment = mk(0, 0, 0);
+        HistState hs;
+        if (HIST) hist_begin(ht, id, hs);
         for (int z = -1; z <= 1; z++)
             for (int y = -1; y <= 1; y++)
                 for (int x = -1; x <= 1; x++) {
@@ -208,7 +236,15 @@ __global__ void __launch_bounds__(128) k_polygon(Params P, const xd_polygon_info
                                               : (pvel - ivel);
                             PairConst pc = load_pair_const(cp + pidx);
                             Fc c = get_constant(pc, ir, 0, im, 0);
-                            dhs(c, 0, 0, 0, 0, 0, 0, 0, cdist, dv, unit, P.dt, Ft, Fn, M);
+                            if (HIST) {
+                                Fn = normal_force(c, 0, 0, 0, 0, 0, 0, 0, cdist, dv, unit);
+                                d3 d;
+                                int sl = hist_slot(ht, hs, id, kHistTri | k, d);
+                                hist_tangential(c, 0.0, dv, unit, P.dt, Fn, d, Ft, M);
+                                hist_store(ht, sl, id, d);
+                            } else {
+                                dhs(c, 0, 0, 0, 0, 0, 0, 0, cdist, dv, unit, P.dt, Ft, Fn, M);
+                            }
                             sum_force += Fn + Ft;
                             sum_moment += M;
                             d3 rf = -(Fn + Ft);
@@ -239,6 +275,7 @@ __global__ void __launch_bounds__(128) k_polygon(Params P, const xd_polygon_info
                         }
                     }
                 }
+        if (HIST) hist_end(ht, hs, id, 2u);
         double* f = force + 3 * (size_t)id;
         double* m = moment + 3 * (size_t)id;
         f[0] += sum_force.x; f[1] += sum_force.y; f[2] += sum_force.z;
@@ -441,22 +478,30 @@ __global__ void k_pair_offsets(const unsigned* __restrict__ counts, unsigned np,
 int launch_p2p(const Params& P, const double* pos, const double* vel, const double* omega,
                double* force, double* moment, const double* mass, const unsigned* sorted,
                const unsigned* cstart, const unsigned* cend, const xd_contact_property* cp,
-               unsigned np, cudaStream_t s)
+               unsigned np, cudaStream_t s, const HistTable* ht)
 {
     if (np == 0) return XD_OK;
-    k_p2p<<<div_up(np, 128), 128, 0, s>>>(P, pos, vel, omega, force, moment, mass, sorted, cstart,
-                                          cend, cp, np);
+    if (ht)
+        k_p2p<true><<<div_up(np, 128), 128, 0, s>>>(P, pos, vel, omega, force, moment, mass, sorted, cstart,
+                                                    cend, cp, np, *ht);
+    else
+        k_p2p<false><<<div_up(np, 128), 128, 0, s>>>(P, pos, vel, omega, force, moment, mass, sorted, cstart,
+                                                     cend, cp, np, HistTable{});
     return launch_status("calculate_p2p");
 }
 
 int launch_planes(const Params& P, const xd_plane_info* planes, const xd_contact_property* cps,
                   unsigned cp_stride, unsigned nplanes, const double* pos, const double* vel,
                   const double* omega, double* force, double* moment, const double* mass,
-                  unsigned np, cudaStream_t s)
+                  unsigned np, cudaStream_t s, const HistTable* ht)
 {
     if (np == 0 || nplanes == 0) return XD_OK;
-    k_planes<<<div_up(np, 128), 128, 0, s>>>(P, planes, cps, cp_stride, nplanes, pos, vel, omega,
-                                             force, moment, mass, np);
+    if (ht)
+        k_planes<true><<<div_up(np, 128), 128, 0, s>>>(P, planes, cps, cp_stride, nplanes, pos, vel, omega,
+                                                       force, moment, mass, np, *ht);
+    else
+        k_planes<false><<<div_up(np, 128), 128, 0, s>>>(P, planes, cps, cp_stride, nplanes, pos, vel, omega,
+                                                        force, moment, mass, np, HistTable{});
     return launch_status("plane_contact_force");
 }
 
@@ -480,7 +525,7 @@ int launch_polygon(const Params& P, const xd_polygon_info* dpi, xd_polygon_mass_
                    const double* pos, const double* vel, const double* omega, double* force,
                    double* moment, const double* mass, const unsigned* sidx,
                    const unsigned* cstart, const unsigned* cend, const xd_contact_property* cp,
-                   unsigned nbodies, void* scratch, cudaStream_t s)
+                   unsigned nbodies, void* scratch, cudaStream_t s, const HistTable* ht)
 {
     unsigned np = P.np;
     if (np == 0) return XD_OK;
@@ -488,8 +533,14 @@ int launch_polygon(const Params& P, const xd_polygon_info* dpi, xd_polygon_mass_
     unsigned nbr = nbr_for(nbodies);
     double* part = static_cast<double*>(scratch);
 #define XD_POLY(NBV)                                                                              \
-    k_polygon<NBV><<<nb, 128, 0, s>>>(P, dpi, dpmi, pos, vel, omega, force, moment, mass, sidx,   \
-                                      cstart, cend, cp, part)
+    do {                                                                                          \
+        if (ht)                                                                                   \
+            k_polygon<NBV, true><<<nb, 128, 0, s>>>(P, dpi, dpmi, pos, vel, omega, force, moment, \
+                                                    mass, sidx, cstart, cend, cp, part, *ht);     \
+        else                                                                                      \
+            k_polygon<NBV, false><<<nb, 128, 0, s>>>(P, dpi, dpmi, pos, vel, omega, force, moment, \
+                                                     mass, sidx, cstart, cend, cp, part, HistTable{}); \
+    } while (0)
     switch (nbr) {
     case 0: XD_POLY(0); break;
     case 1: XD_POLY(1); break;

@@ -10,6 +10,8 @@ namespace xd {
 // cell grid (xd_grid.cu)
 unsigned key_bits_for(unsigned ncell);
 size_t reorder_scratch_bytes(unsigned n);
+struct HistTable;   // xd_physics64.cuh: tangential-spring history of a scene
+
 int launch_hash(const Params& P, unsigned* hash, unsigned* index, const double* pos, unsigned n,
                 unsigned sid, cudaStream_t s);
 int launch_fill_cells(unsigned* cstart, unsigned* cend, unsigned ncell, cudaStream_t s);
@@ -32,17 +34,17 @@ int launch_vv_velocity_position(const Params& P, double* pos, double* vel, doubl
 int launch_p2p(const Params& P, const double* pos, const double* vel, const double* omega,
                double* force, double* moment, const double* mass, const unsigned* sorted,
                const unsigned* cstart, const unsigned* cend, const xd_contact_property* cp,
-               unsigned np, cudaStream_t s);
+               unsigned np, cudaStream_t s, const HistTable* ht = nullptr);
 int launch_planes(const Params& P, const xd_plane_info* planes, const xd_contact_property* cps,
                   unsigned cp_stride, unsigned nplanes, const double* pos, const double* vel,
                   const double* omega, double* force, double* moment, const double* mass,
-                  unsigned np, cudaStream_t s);
+                  unsigned np, cudaStream_t s, const HistTable* ht = nullptr);
 size_t polygon_scratch_bytes(unsigned np, unsigned nbodies);
 int launch_polygon(const Params& P, const xd_polygon_info* dpi, xd_polygon_mass_info* dpmi,
                    const double* pos, const double* vel, const double* omega, double* force,
                    double* moment, const double* mass, const unsigned* sidx,
                    const unsigned* cstart, const unsigned* cend, const xd_contact_property* cp,
-                   unsigned nbodies, void* scratch, cudaStream_t s);
+                   unsigned nbodies, void* scratch, cudaStream_t s, const HistTable* ht = nullptr);
 int launch_update_polygon(const xd_polygon_mass_info* dpmi, const double* vlist, double* sphere,
                           xd_polygon_info* dpi, unsigned ntri, cudaStream_t s);
 int reduction_d3(const double* in, unsigned n, double out[3], void* scratch, cudaStream_t s);

@@ -2222,6 +2222,20 @@ int mixed_get_bodies(MixedScene* s, xd_polygon_mass_info* pmi, cudaStream_t q)
 
 unsigned long long mixed_device_bytes(MixedScene* s) { return s ? s->bytes : 0; }
 
+int mixed_set_history(MixedScene* s, unsigned slots)
+{
+    (void)s;
+    if (slots == 0) return XD_OK;
+    return set_error(XD_ERR_INVALID, "mixed mode: tangential history not provided yet");
+}
+
+int mixed_download_history(MixedScene* s, unsigned* keys, double* delta, unsigned long long* overflow,
+                           cudaStream_t q)
+{
+    (void)s; (void)keys; (void)delta; (void)overflow; (void)q;
+    return set_error(XD_ERR_STATE, "scene_download_history: history is off");
+}
+
 int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q)
 {
     unsigned c[kCounters] = {};

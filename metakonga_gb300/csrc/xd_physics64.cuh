@@ -84,6 +84,125 @@ __device__ __forceinline__ void dhs(const Fc& c, double ir, double jr, double Ei
     }
 }
 
+// ---------------------------------------------- tangential-spring history
+//
+// An extension with no counterpart in the reference (DHSModel keeps no state
+// between steps).  A particle holds up to `slots` contacts, keyed by partner:
+// particle j -> its original index, plane w -> kHistPlane | w, triangle t ->
+// kHistTri | t; key[s * n + i], delta[(s * n + i) * 3 + a].  Per contact and
+// step, vt the tangential relative velocity:
+//   d <- d - (d.u)u rescaled to |d|; d <- d + vt dt; Ft = ks d + vs vt;
+//   if |Ft| > mu |Fn|: Ft <- mu |Fn| Ft / |Ft|, d <- (Ft - vs vt) / ks;
+//   M = (ir u) x Ft.
+// A new contact starts from d = 0 (its first step is the reference's DHS
+// force); a contact that ends frees its entry; a contact that finds no free
+// entry is counted in *overflow and computed without history.
+constexpr unsigned kHistEmpty = 0xffffffffu;
+constexpr unsigned kHistPlane = 0x80000000u;
+constexpr unsigned kHistTri = 0xC0000000u;
+constexpr unsigned kHistMaxSlots = 32;
+
+struct HistTable {
+    unsigned* key;
+    double* delta;
+    unsigned slots;
+    unsigned n;
+    unsigned long long* overflow;
+};
+
+__device__ __forceinline__ unsigned hist_class(unsigned k) { return k < kHistPlane ? 0u : (k < kHistTri ? 1u : 2u); }
+
+struct HistState {
+    unsigned freem, matched;
+};
+
+__device__ __forceinline__ void hist_begin(const HistTable& h, unsigned i, HistState& st)
+{
+    st.freem = 0;
+    st.matched = 0;
+    for (unsigned s = 0; s < h.slots; ++s)
+        if (h.key[(size_t)s * h.n + i] == kHistEmpty) st.freem |= 1u << s;
+}
+
+// the entry of `key` (its spring in d), else the lowest free entry (d = 0), else -1
+__device__ __forceinline__ int hist_slot(const HistTable& h, HistState& st, unsigned i, unsigned key, d3& d)
+{
+    d = mk(0, 0, 0);
+    for (unsigned s = 0; s < h.slots; ++s) {
+        const size_t e = (size_t)s * h.n + i;
+        if (h.key[e] == key) {
+            const double* p = h.delta + e * 3;
+            d = mk(p[0], p[1], p[2]);
+            st.matched |= 1u << s;
+            return (int)s;
+        }
+    }
+    if (st.freem) {
+        const unsigned s = __ffs(st.freem) - 1;
+        st.freem &= ~(1u << s);
+        st.matched |= 1u << s;
+        h.key[(size_t)s * h.n + i] = key;
+        return (int)s;
+    }
+    atomicAdd(h.overflow, 1ull);
+    return -1;
+}
+
+__device__ __forceinline__ void hist_store(const HistTable& h, int s, unsigned i, d3 d)
+{
+    if (s < 0) return;
+    double* p = h.delta + ((size_t)s * h.n + i) * 3;
+    p[0] = d.x;
+    p[1] = d.y;
+    p[2] = d.z;
+}
+
+// entries of class cls whose contact did not recur are freed
+__device__ __forceinline__ void hist_end(const HistTable& h, const HistState& st, unsigned i, unsigned cls)
+{
+    for (unsigned s = 0; s < h.slots; ++s) {
+        if (st.matched & (1u << s)) continue;
+        const size_t e = (size_t)s * h.n + i;
+        const unsigned k = h.key[e];
+        if (k == kHistEmpty || hist_class(k) != cls) continue;
+        h.key[e] = kHistEmpty;
+        double* p = h.delta + e * 3;
+        p[0] = p[1] = p[2] = 0.0;
+    }
+}
+
+// DHSModel's normal force (impl:385-388)
+__device__ __forceinline__ d3 normal_force(const Fc& c, double ir, double jr, double Ei, double Ej, double pri,
+                                           double prj, double coh, double cdist, d3 dv, d3 unit)
+{
+    double fsn = -c.kn * (cdist * sqrt(cdist));
+    double fdn = c.vn * dot(dv, unit);
+    double fca = cohesion_force(ir, jr, Ei, Ej, pri, prj, coh, fsn);
+    return (fsn + fca + fdn) * unit;
+}
+
+// the tangential spring with history (see above); d in/out
+__device__ __forceinline__ void hist_tangential(const Fc& c, double ir, d3 dv, d3 unit, double dt, d3 Fn, d3& d,
+                                                d3& Ft, d3& M)
+{
+    d3 vt = dv - dot(dv, unit) * unit;
+    double m0 = length(d);
+    d3 dp = d - dot(d, unit) * unit;
+    double mp = length(dp);
+    d3 dn = mp > 0.0 ? (m0 / mp) * dp : mk(0, 0, 0);
+    dn = dn + dt * vt;
+    d3 ft = c.ks * dn + c.vs * vt;
+    double fmax = c.mu * length(Fn);
+    double mf = length(ft);
+    if (mf > fmax) {
+        ft = (fmax / mf) * ft;
+        dn = (ft - c.vs * vt) / c.ks;
+    }
+    d = dn;
+    Ft = ft;
+    M = cross(ir * unit, ft);
+}
+
 struct PlaneD {
     double l1, l2;
     d3 u1, u2, uw, xw, w2, w3, w4;

@@ -10,6 +10,7 @@
 #include "xd_grid.cuh"
 #include "xd_internal.cuh"
 #include "xd_mixed.cuh"
+#include "xd_physics64.cuh"
 
 using namespace xd;
 
@@ -47,6 +48,11 @@ struct xd_scene {
     unsigned long long phase_n[XD_SCENE_PHASES] = {};
     cudaEvent_t pending[XD_SCENE_PHASES] = {};
     MixedScene* mixed = nullptr;
+    // tangential-spring history (FP64 form; the mixed form keeps its own)
+    unsigned hist_slots = 0;
+    unsigned* hist_key = nullptr;
+    double* hist_delta = nullptr;
+    unsigned long long* hist_overflow = nullptr;
 };
 
 namespace {
@@ -77,8 +83,31 @@ int d2h(void* dst, const void* src, size_t bytes, cudaStream_t st)
     return cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st), "scene download");
 }
 
+void free_history(xd_scene* s)
+{
+    if (s->hist_key) cudaFree(s->hist_key);
+    if (s->hist_delta) cudaFree(s->hist_delta);
+    if (s->hist_overflow) cudaFree(s->hist_overflow);
+    s->hist_key = nullptr;
+    s->hist_delta = nullptr;
+    s->hist_overflow = nullptr;
+    s->hist_slots = 0;
+}
+
+HistTable history_of(xd_scene* s)
+{
+    HistTable h;
+    h.key = s->hist_key;
+    h.delta = s->hist_delta;
+    h.slots = s->hist_slots;
+    h.n = s->np;
+    h.overflow = s->hist_overflow;
+    return h;
+}
+
 void free_scene(xd_scene* s)
 {
+    free_history(s);
     if (s->mixed) mixed_destroy(s->mixed);
     s->mixed = nullptr;
     for (void* p : s->allocs) cudaFree(p);
@@ -560,6 +589,8 @@ int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
     }
     const Params& P = s->P;
     const unsigned np = s->np, ng = s->np + s->ntri;
+    const HistTable ht = history_of(s);
+    const HistTable* hp = s->hist_slots ? &ht : nullptr;
     int st = XD_OK;
     if (s->bodies_dirty && s->ntri) {
         st = launch_update_polygon(s->pmi, s->vlist, s->sphere, s->poly, s->ntri, q);
@@ -586,18 +617,18 @@ int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
         if (st == XD_OK) {
             PhaseSpan ps(s, 3, q);
             st = launch_p2p(P, s->pos, s->vel, s->omega, s->force, s->moment, s->mass, s->sorted,
-                            s->cstart, s->cend, s->cp_pp, np, q);
+                            s->cstart, s->cend, s->cp_pp, np, q, hp);
         }
         if (st == XD_OK && s->nplanes) {
             PhaseSpan ps(s, 4, q);
             st = launch_planes(P, s->planes, s->cp_planes, 1, s->nplanes, s->pos, s->vel, s->omega,
-                               s->force, s->moment, s->mass, np, q);
+                               s->force, s->moment, s->mass, np, q, hp);
         }
         if (st == XD_OK && s->ntri) {
             PhaseSpan ps(s, 5, q);
             st = launch_polygon(P, s->poly, s->pmi, s->pos, s->vel, s->omega, s->force, s->moment,
                                 s->mass, s->sorted, s->cstart, s->cend, s->cp_poly, s->nbodies,
-                                s->poly_scratch, q);
+                                s->poly_scratch, q, hp);
         }
         if (st == XD_OK) {
             PhaseSpan ps(s, 0, q);
@@ -618,6 +649,46 @@ int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
         if (herr) return set_error(XD_ERR_INVALID, "scene_step: a hash value was >= ncell");
     }
     return XD_OK;
+}
+
+int xd_scene_set_tangential_history(xd_scene* s, unsigned slots)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_set_tangential_history: null scene");
+    if (slots > kHistMaxSlots)
+        return set_error(XD_ERR_INVALID, "scene_set_tangential_history: at most %u contacts per particle",
+                         kHistMaxSlots);
+    if (s->mixed) return mixed_set_history(s->mixed, slots);
+    free_history(s);
+    if (slots == 0 || s->np == 0) return XD_OK;
+    const size_t e = (size_t)slots * s->np;
+    int st = cuda_status(cudaMalloc(&s->hist_key, sizeof(unsigned) * e), "tangential history");
+    if (st == XD_OK) st = cuda_status(cudaMalloc(&s->hist_delta, sizeof(double) * 3 * e), "tangential history");
+    if (st == XD_OK) st = cuda_status(cudaMalloc(&s->hist_overflow, sizeof(unsigned long long)), "tangential history");
+    if (st == XD_OK) st = cuda_status(cudaMemset(s->hist_key, 0xff, sizeof(unsigned) * e), "tangential history");
+    if (st == XD_OK) st = cuda_status(cudaMemset(s->hist_delta, 0, sizeof(double) * 3 * e), "tangential history");
+    if (st == XD_OK) st = cuda_status(cudaMemset(s->hist_overflow, 0, sizeof(unsigned long long)), "tangential history");
+    if (st != XD_OK) {
+        free_history(s);
+        return st;
+    }
+    s->hist_slots = slots;
+    return XD_OK;
+}
+
+int xd_scene_download_history(xd_scene* s, unsigned* keys, double* delta, unsigned long long* overflow,
+                              void* stream)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_download_history: null scene");
+    cudaStream_t q = static_cast<cudaStream_t>(stream);
+    if (s->mixed) return mixed_download_history(s->mixed, keys, delta, overflow, q);
+    if (!s->hist_slots) return set_error(XD_ERR_STATE, "scene_download_history: history is off");
+    const size_t e = (size_t)s->hist_slots * s->np;
+    int st = XD_OK;
+    if (keys) st = d2h(keys, s->hist_key, sizeof(unsigned) * e, q);
+    if (st == XD_OK && delta) st = d2h(delta, s->hist_delta, sizeof(double) * 3 * e, q);
+    if (st == XD_OK && overflow) st = d2h(overflow, s->hist_overflow, sizeof(unsigned long long), q);
+    if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "scene_download_history");
+    return st;
 }
 
 int xd_scene_step_many(xd_scene* const* scenes, const unsigned* nsteps, unsigned count, int check, void* stream)

@@ -167,6 +167,20 @@ class DeviceScene:
     def launches(self, nsteps: int) -> int:
         return int(_lib.lib().xd_scene_launches(self.handle, nsteps))
 
+    def set_tangential_history(self, slots: int = 12):
+        """Tangential springs kept per contact (xd_scene_set_tangential_history);
+        0 restores the reference's DHS model."""
+        self.hist_slots = int(slots)
+        call("xd_scene_set_tangential_history", self.handle, self.hist_slots)
+
+    def download_history(self, stream: int = 0):
+        """(keys [slots, np], delta [slots, np, 3], overflow) in original order."""
+        k = np.zeros((self.hist_slots, self.np), np.uint32)
+        d = np.zeros((self.hist_slots, self.np, 3))
+        ov = np.zeros(1, np.uint64)
+        call("xd_scene_download_history", self.handle, k.ctypes.data, d.ctypes.data, ov.ctypes.data, stream)
+        return k, d, int(ov[0])
+
     def device_bytes(self) -> int:
         """Device memory the scene holds, in bytes."""
         out = np.zeros(1, np.uint64)
