@@ -195,6 +195,14 @@ struct MixedScene {
     double* xfer = nullptr;
     bool ready = false;                // grid and buffers set up (first upload)
     cudaGraphExec_t graph[3] = { nullptr, nullptr, nullptr };   // first step, two steps, one step
+    // tangential-spring history (an extension): [s * n + slot] tables in the
+    // state's slot order, permuted with the particles at re-binning
+    unsigned hslots = 0;
+    unsigned* hkey = nullptr;
+    double* hdelta = nullptr;
+    unsigned* hkey2 = nullptr;
+    double* hdelta2 = nullptr;
+    unsigned long long* hoverflow = nullptr;
     unsigned passes = 0;          // radix passes of one re-binning
     bool use_graphs = true;
     unsigned rec_cap_alloc = 0;
@@ -1027,12 +1035,17 @@ struct Own {
 // separation (or the reference's FP64 expression for guard-band pairs), the
 // relative velocity from the double-float velocities, and the two
 // cancellation cases (normal force near zero, rolling slip) formed in FP64.
+// HIST: 0 the reference's DHS; 1 tangential springs kept in the table (an
+// extension, formed in FP64 from the FP32 normal, slip and normal force);
+// 2 the same read-only (diagnostic evaluation).
+template <int HIST>
 __device__ __forceinline__ void contact_force(const MixParams& P, const Master& M, const Own& I,
                                               unsigned j, bool guard, const double* __restrict__ mass0,
                                               const float4* __restrict__ pf,
                                               const longlong2* __restrict__ qa,
                                               const longlong2* __restrict__ qb,
-                                              unsigned* __restrict__ counters, PairAcc& A)
+                                              unsigned* __restrict__ counters, PairAcc& A,
+                                              const HistTable& ht, HistState& hs)
 {
     const unsigned i = I.i;
     const float dt = P.dtf;
@@ -1126,12 +1139,33 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
         fn = (float)(-knd * (dl * sqrt(dl)) + vnd * (rvx * ux + rvy * uy + rvz * uz));
     }
     const f3 Fn = fn * u;
-    const float mag_e = sqrtf(ee);
-    if (mag_e != 0.f) {
-        const f3 sh = (1.0f / mag_e) * ev;
-        // dv . sh = |e| exactly (sh is the unit slip direction)
-        A.Ft = fminf(ks * (mag_e * dt) + vs * mag_e, P.fric * fabsf(fn)) * sh;
-        A.Mm = fcross(ir * u, A.Ft);
+    if (HIST) {
+        // the partner's key is its original index
+        const unsigned key = __float_as_uint(__ldg(M.wl + j).w);
+        d3 d;
+        int sl = -1;
+        if (HIST == 1) sl = hist_slot(ht, hs, i, key, d);
+        else hist_peek(ht, i, key, d);
+        xd::Fc c;
+        c.kn = kn;
+        c.vn = vn;
+        c.ks = ks;
+        c.vs = vs;
+        c.mu = P.fric;
+        d3 Ftd, Md;
+        hist_tangential(c, (double)ir, mk(ev.x, ev.y, ev.z), mk(u.x, u.y, u.z), P.dt, mk(Fn.x, Fn.y, Fn.z), d,
+                        Ftd, Md);
+        if (HIST == 1) hist_store(ht, sl, i, d);
+        A.Ft = fk((float)Ftd.x, (float)Ftd.y, (float)Ftd.z);
+        A.Mm = fk((float)Md.x, (float)Md.y, (float)Md.z);
+    } else {
+        const float mag_e = sqrtf(ee);
+        if (mag_e != 0.f) {
+            const f3 sh = (1.0f / mag_e) * ev;
+            // dv . sh = |e| exactly (sh is the unit slip direction)
+            A.Ft = fminf(ks * (mag_e * dt) + vs * mag_e, P.fric * fabsf(fn)) * sh;
+            A.Mm = fcross(ir * u, A.Ft);
+        }
     }
     A.sumF = A.sumF + (Fn + A.Ft);
     A.sumM = A.sumM + A.Mm;
@@ -1147,7 +1181,7 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
 constexpr unsigned kContactThreads = 64;
 constexpr unsigned kContactBlocks = 152 * 8;
 
-template <bool RECORD>
+template <bool RECORD, int HIST>
 __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Master M, const float4* __restrict__ pf,
                                                     const longlong2* __restrict__ qa,
                                                     const longlong2* __restrict__ qb,
@@ -1170,7 +1204,8 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
                                                     float4* __restrict__ Fc, float4* __restrict__ Mc,
                                                     unsigned* __restrict__ counters,
                                                     unsigned* __restrict__ rec_count,
-                                                    unsigned* __restrict__ rec_pairs, unsigned rec_cap)
+                                                    unsigned* __restrict__ rec_pairs, unsigned rec_cap,
+                                                    HistTable ht)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) counters[CN_REBUILD] = 0;
     const unsigned total = counters[CN_HEAVY];
@@ -1194,6 +1229,8 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
         A.sumF = fk(0.f, 0.f, 0.f);
         A.sumM = fk(0.f, 0.f, 0.f);
         unsigned nc = 0;
+        HistState hs;
+        if (HIST == 1) hist_begin(ht, i, hs);
         auto add = [&](unsigned j, bool guard) {
             if (!have_v) {
                 I.vh = __ldg(M.vh + i);
@@ -1203,7 +1240,7 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
                 I.im = I.vh.w;
                 have_v = true;
             }
-            contact_force(P, M, I, j, guard, mass0, pf, qa, qb, counters, A);
+            contact_force<HIST>(P, M, I, j, guard, mass0, pf, qa, qb, counters, A, ht, hs);
             if (RECORD && nc < rec_cap) rec_pairs[(size_t)i * rec_cap + nc] = j;
             ++nc;
         };
@@ -1265,7 +1302,17 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
                     c.ks = c.kn * P.pl_sratio[w];
                     c.vs = c.vn * P.pl_sratio[w];
                     c.mu = P.pl_fric[w];
-                    dhs(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit, P.dt, Ft, Fn, Mo);
+                    if (HIST) {
+                        Fn = normal_force(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit);
+                        d3 d;
+                        int sl = -1;
+                        if (HIST == 1) sl = hist_slot(ht, hs, i, kHistPlane | (unsigned)w, d);
+                        else hist_peek(ht, i, kHistPlane | (unsigned)w, d);
+                        hist_tangential(c, 0.0, dv, unit, P.dt, Fn, d, Ft, Mo);
+                        if (HIST == 1) hist_store(ht, sl, i, d);
+                    } else {
+                        dhs(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit, P.dt, Ft, Fn, Mo);
+                    }
                 }
                 f += Fn + Ft;
             }
@@ -1317,7 +1364,17 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
                 c.vs = c.vn * P.pb_sratio[b];
                 c.mu = P.pb_fric[b];
                 d3 Fn = mk(0, 0, 0);
-                dhs(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit, P.dt, Ft, Fn, Mo);
+                if (HIST) {
+                    Fn = normal_force(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit);
+                    d3 d;
+                    int sl = -1;
+                    if (HIST == 1) sl = hist_slot(ht, hs, i, kHistTri | t, d);
+                    else hist_peek(ht, i, kHistTri | t, d);
+                    hist_tangential(c, 0.0, dv, unit, P.dt, Fn, d, Ft, Mo);
+                    if (HIST == 1) hist_store(ht, sl, i, d);
+                } else {
+                    dhs(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit, P.dt, Ft, Fn, Mo);
+                }
                 const d3 fc = Fn + Ft;
                 f += fc;
                 const d3 rm = -cross(po2cp, fc);
@@ -1333,6 +1390,7 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
             F.y += (float)f.y;
             F.z += (float)f.z;
         }
+        if (HIST == 1) hist_end_all(ht, hs, i);
         Fc[i] = F;
         Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
         if (RECORD) rec_count[i] = nc;
@@ -1796,6 +1854,8 @@ static int ensure_xfer(MixedScene* s)
     return alloc(s, &s->xfer, (size_t)s->n * (4 + 3 * 6 + 2));
 }
 
+static int reset_history(MixedScene* s, cudaStream_t q);
+
 int mixed_upload(MixedScene* s, const double* pos, const double* vel, const double* acc,
                  const double* omega, const double* alpha, const double* mass,
                  const double* inertia, cudaStream_t q)
@@ -1827,6 +1887,8 @@ int mixed_upload(MixedScene* s, const double* pos, const double* vel, const doub
     if (st != XD_OK) return st;
     s->cur = 0;
     s->cells_clean = false;   // the state is in upload order again: the next step re-bins
+    st = reset_history(s, q);   // an uploaded state starts with no springs
+    if (st != XD_OK) return st;
     st = cuda_status(cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * CN_DECISIONS, q), "mixed upload");
     if (st != XD_OK) return st;
     k_mx_load<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[0], dpos, dvel, dacc, dom, dal, dm, dI,
@@ -1868,6 +1930,66 @@ int mixed_download(MixedScene* s, double* pos, double* vel, double* acc, double*
 // Re-binning: cell keys of the current positions, stable radix sort, the
 // state permuted into the new order, the cell lower bounds, then the Verlet
 // lists, plane masks and heavy list.
+static HistTable history_table(MixedScene* s)
+{
+    HistTable h;
+    h.key = s->hkey;
+    h.delta = s->hdelta;
+    h.slots = s->hslots;
+    h.n = s->n;
+    h.overflow = s->hoverflow;
+    return h;
+}
+
+// Re-binning with history: the tables follow their particles (new slot i
+// takes old slot perm[i]); the partner keys are original indices and stay.
+__global__ void __launch_bounds__(256) k_hist_permute(unsigned n, unsigned slots, const unsigned* __restrict__ perm,
+                                                      const unsigned* __restrict__ key, const double* __restrict__ delta,
+                                                      unsigned* __restrict__ key2, double* __restrict__ delta2)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned o = __ldg(perm + i);
+    for (unsigned s = 0; s < slots; ++s) {
+        const size_t a = (size_t)s * n + i, b = (size_t)s * n + o;
+        key2[a] = __ldg(key + b);
+        delta2[3 * a + 0] = __ldg(delta + 3 * b + 0);
+        delta2[3 * a + 1] = __ldg(delta + 3 * b + 1);
+        delta2[3 * a + 2] = __ldg(delta + 3 * b + 2);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_hist_copy(size_t e, const unsigned* __restrict__ key2,
+                                                   const double* __restrict__ delta2, unsigned* __restrict__ key,
+                                                   double* __restrict__ delta)
+{
+    for (size_t a = (size_t)blockIdx.x * blockDim.x + threadIdx.x; a < e; a += (size_t)gridDim.x * blockDim.x) {
+        key[a] = key2[a];
+        delta[3 * a + 0] = delta2[3 * a + 0];
+        delta[3 * a + 1] = delta2[3 * a + 1];
+        delta[3 * a + 2] = delta2[3 * a + 2];
+    }
+}
+
+// The tables in original order (diagnostic download): row id of the output
+// takes slot i, id = the particle's original index.
+__global__ void __launch_bounds__(256) k_hist_gather(unsigned n, unsigned slots, Master M,
+                                                     const unsigned* __restrict__ key,
+                                                     const double* __restrict__ delta, unsigned* __restrict__ okey,
+                                                     double* __restrict__ odelta)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned id = __float_as_uint(M.wl[i].w);
+    for (unsigned s = 0; s < slots; ++s) {
+        const size_t a = (size_t)s * n + i, b = (size_t)s * n + id;
+        okey[b] = key[a];
+        odelta[3 * b + 0] = delta[3 * a + 0];
+        odelta[3 * b + 1] = delta[3 * a + 1];
+        odelta[3 * b + 2] = delta[3 * a + 2];
+    }
+}
+
 static int rebuild(MixedScene* s, cudaStream_t q)
 {
     const unsigned n = s->n;
@@ -1881,6 +2003,16 @@ static int rebuild(MixedScene* s, cudaStream_t q)
     if (st != XD_OK) return st;
     k_mx_permute<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[0], s->m[1], sv);
     k_mx_copyback<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[1], s->m[0], s->pf, s->qa, s->qb);
+    if (s->hslots) {
+        k_hist_permute<<<blocks(n, 256), 256, 0, q>>>(n, s->hslots, sv, s->hkey, s->hdelta, s->hkey2, s->hdelta2);
+        st = launch_status("mixed history re-binning");
+        if (st != XD_OK) return st;
+        const size_t e = (size_t)s->hslots * n;
+        k_hist_copy<<<(unsigned)std::min<size_t>((e + 255) / 256, 152 * 16), 256, 0, q>>>(e, s->hkey2, s->hdelta2,
+                                                                                         s->hkey, s->hdelta);
+        st = launch_status("mixed history re-binning");
+        if (st != XD_OK) return st;
+    }
     k_lb_fill<<<blocks(n + 1, 256), 256, 0, q>>>(sk, n, s->ncell, s->lb, s->prev_keys, s->gaps, s->counters);
     k_lb_long<<<152 * 4, 256, 0, q>>>(s->gaps, s->counters, s->lb);
     st = launch_status("mixed re-binning");
@@ -1994,21 +2126,33 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
     ph.begin(3, q);
     // the list holds at most n particles: no more warps than that
     const unsigned grid = std::max(1u, std::min(kContactBlocks, (n + kContactThreads - 1) / kContactThreads));
+    // tangential springs: updated by a step, read only by the diagnostic evaluation (MODE 3)
+    const HistTable ht = history_table(s);
+    const int hist = s->hslots ? (MODE == 3 ? 2 : 1) : 0;
+    unsigned* rc = nullptr;
+    unsigned* rp = nullptr;
     if (record) {
         st = cuda_status(cudaMemsetAsync(s->rec_count, 0, sizeof(unsigned) * n, q), "mixed pair count");
         if (st != XD_OK) return st;
-        k_mx_contact<true><<<grid, kContactThreads, 0, q>>>(s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->vcount,
-                                                s->vlist, s->hlist, s->wmask, s->planes, s->cps, s->mass0,
-                                                s->poly, s->pmi, s->tcount, s->tlist, s->tpk_sorted,
-                                                s->tpt_sorted, s->tpair_cap, s->rxn,
-                                                s->Fc, s->Mc, s->counters, s->rec_count, s->rec_pairs, rec_cap);
-    } else {
-        k_mx_contact<false><<<grid, kContactThreads, 0, q>>>(s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb, s->vcount,
-                                                 s->vlist, s->hlist, s->wmask, s->planes, s->cps, s->mass0,
-                                                 s->poly, s->pmi, s->tcount, s->tlist, s->tpk_sorted,
-                                                 s->tpt_sorted, s->tpair_cap, s->rxn,
-                                                 s->Fc, s->Mc, s->counters, nullptr, nullptr, 0);
+        rc = s->rec_count;
+        rp = s->rec_pairs;
     }
+#define XD_MX_CONTACT(REC, H)                                                                                   \
+    k_mx_contact<REC, H><<<grid, kContactThreads, 0, q>>>(s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb,     \
+                                                          s->vcount, s->vlist, s->hlist, s->wmask, s->planes,    \
+                                                          s->cps, s->mass0, s->poly, s->pmi, s->tcount, s->tlist, \
+                                                          s->tpk_sorted, s->tpt_sorted, s->tpair_cap, s->rxn,   \
+                                                          s->Fc, s->Mc, s->counters, rc, rp, record ? rec_cap : 0u, ht)
+    if (record) {
+        if (hist == 2) XD_MX_CONTACT(true, 2);
+        else if (hist == 1) XD_MX_CONTACT(true, 1);
+        else XD_MX_CONTACT(true, 0);
+    } else {
+        if (hist == 2) XD_MX_CONTACT(false, 2);
+        else if (hist == 1) XD_MX_CONTACT(false, 1);
+        else XD_MX_CONTACT(false, 0);
+    }
+#undef XD_MX_CONTACT
     st = launch_status("mixed contact");
     if (st == XD_OK && s->nbodies && MODE != 3) {
         // this step's reaction on the polygon bodies, summed in a fixed order
@@ -2222,18 +2366,73 @@ int mixed_get_bodies(MixedScene* s, xd_polygon_mass_info* pmi, cudaStream_t q)
 
 unsigned long long mixed_device_bytes(MixedScene* s) { return s ? s->bytes : 0; }
 
+static int reset_history(MixedScene* s, cudaStream_t q)
+{
+    if (!s->hslots) return XD_OK;
+    const size_t e = (size_t)s->hslots * s->desc.np;
+    int st = cuda_status(cudaMemsetAsync(s->hkey, 0xff, sizeof(unsigned) * e, q), "mixed history");
+    if (st == XD_OK) st = cuda_status(cudaMemsetAsync(s->hdelta, 0, sizeof(double) * 3 * e, q), "mixed history");
+    if (st == XD_OK) st = cuda_status(cudaMemsetAsync(s->hoverflow, 0, sizeof(unsigned long long), q), "mixed history");
+    return st;
+}
+
 int mixed_set_history(MixedScene* s, unsigned slots)
 {
-    (void)s;
-    if (slots == 0) return XD_OK;
-    return set_error(XD_ERR_INVALID, "mixed mode: tangential history not provided yet");
+    if (slots == s->hslots) {
+        int st = reset_history(s, nullptr);
+        if (st == XD_OK) st = cuda_status(cudaDeviceSynchronize(), "mixed history");
+        return st;
+    }
+    // the step graphs hold the table pointers: capture them again
+    for (int k = 0; k < 3; ++k)
+        if (s->graph[k]) {
+            cudaGraphExecDestroy(s->graph[k]);
+            s->graph[k] = nullptr;
+        }
+    s->hslots = 0;
+    const unsigned n = s->desc.np;   // the particle count (set before the first upload too)
+    if (slots == 0 || n == 0) return XD_OK;
+    const size_t e = (size_t)slots * n;
+    int st = XD_OK;
+    auto A = [&](int r) { if (st == XD_OK) st = r; };
+    A(alloc(s, &s->hkey, e));
+    A(alloc(s, &s->hdelta, 3 * e));
+    A(alloc(s, &s->hkey2, e));
+    A(alloc(s, &s->hdelta2, 3 * e));
+    A(alloc(s, &s->hoverflow, 1));
+    if (st != XD_OK) return st;
+    s->hslots = slots;
+    st = reset_history(s, nullptr);
+    if (st == XD_OK) st = cuda_status(cudaDeviceSynchronize(), "mixed history");
+    return st;
 }
 
 int mixed_download_history(MixedScene* s, unsigned* keys, double* delta, unsigned long long* overflow,
                            cudaStream_t q)
 {
-    (void)s; (void)keys; (void)delta; (void)overflow; (void)q;
-    return set_error(XD_ERR_STATE, "scene_download_history: history is off");
+    if (!s->hslots) return set_error(XD_ERR_STATE, "scene_download_history: history is off");
+    if (!s->ready) return set_error(XD_ERR_STATE, "mixed mode: no state uploaded");
+    const size_t e = (size_t)s->hslots * s->n;
+    unsigned* ok = nullptr;
+    double* od = nullptr;
+    int st = cuda_status(cudaMalloc(&ok, sizeof(unsigned) * e), "scene_download_history");
+    if (st == XD_OK) st = cuda_status(cudaMalloc(&od, sizeof(double) * 3 * e), "scene_download_history");
+    if (st == XD_OK) {
+        k_hist_gather<<<blocks(s->n, 256), 256, 0, q>>>(s->n, s->hslots, s->m[0], s->hkey, s->hdelta, ok, od);
+        st = launch_status("scene_download_history");
+    }
+    if (st == XD_OK && keys)
+        st = cuda_status(cudaMemcpyAsync(keys, ok, sizeof(unsigned) * e, cudaMemcpyDeviceToHost, q), "scene_download_history");
+    if (st == XD_OK && delta)
+        st = cuda_status(cudaMemcpyAsync(delta, od, sizeof(double) * 3 * e, cudaMemcpyDeviceToHost, q),
+                         "scene_download_history");
+    if (st == XD_OK && overflow)
+        st = cuda_status(cudaMemcpyAsync(overflow, s->hoverflow, sizeof(unsigned long long), cudaMemcpyDeviceToHost, q),
+                         "scene_download_history");
+    if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "scene_download_history");
+    if (ok) cudaFree(ok);
+    if (od) cudaFree(od);
+    return st;
 }
 
 int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q)

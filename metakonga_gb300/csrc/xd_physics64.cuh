@@ -171,6 +171,34 @@ __device__ __forceinline__ void hist_end(const HistTable& h, const HistState& st
     }
 }
 
+// every entry whose contact did not recur this step is freed (one pass over
+// all contact kinds)
+__device__ __forceinline__ void hist_end_all(const HistTable& h, const HistState& st, unsigned i)
+{
+    for (unsigned s = 0; s < h.slots; ++s) {
+        if (st.matched & (1u << s)) continue;
+        const size_t e = (size_t)s * h.n + i;
+        if (h.key[e] == kHistEmpty) continue;
+        h.key[e] = kHistEmpty;
+        double* p = h.delta + e * 3;
+        p[0] = p[1] = p[2] = 0.0;
+    }
+}
+
+// read-only lookup (diagnostic evaluation): the spring of `key`, or 0
+__device__ __forceinline__ void hist_peek(const HistTable& h, unsigned i, unsigned key, d3& d)
+{
+    d = mk(0, 0, 0);
+    for (unsigned s = 0; s < h.slots; ++s) {
+        const size_t e = (size_t)s * h.n + i;
+        if (h.key[e] == key) {
+            const double* p = h.delta + e * 3;
+            d = mk(p[0], p[1], p[2]);
+            return;
+        }
+    }
+}
+
 // DHSModel's normal force (impl:385-388)
 __device__ __forceinline__ d3 normal_force(const Fc& c, double ir, double jr, double Ei, double Ej, double pri,
                                            double prj, double coh, double cdist, d3 dv, d3 unit)
