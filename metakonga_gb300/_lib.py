@@ -64,6 +64,17 @@ _SIGS = {
     "xd_cube_contact_force_f": [i32] + [vp] * 7 + [u32, vp, vp],
     "xd_particle_polygon_collision_f": [i32] + [vp] * 13 + [u32, u32, vp],
     "xd_reduction_f3": [vp, u32, vp, vp],
+    "xd_legacy_set_symbolic_parameter": [vp],
+    "xd_legacy_vv_update_position": [vp, vp, vp, u32, vp],
+    "xd_legacy_vv_update_velocity": [vp] * 6 + [u32, vp],
+    "xd_legacy_calculate_hash_and_index": [vp, vp, vp, u32, vp],
+    "xd_legacy_reorder_and_find_cell_start": [vp] * 5 + [u32, u32, vp],
+    "xd_legacy_calculate_p2p": [vp] * 10 + [u32, u32, vp],
+    "xd_legacy_cube_hertzian_contact_force": [vp] + [C.c_double] * 5 + [vp] * 6 + [u32, vp],
+    "xd_legacy_shape_hertzian_contact_force": [vp] * 5 + [C.c_double] * 5 + [vp] * 7 + [u32] + [vp] * 5,
+    "xd_legacy_update_polygons_position": [vp, vp, vp, u32, vp, vp],
+    "xd_legacy_update_polygons_information": [vp, vp, vp, u32, vp],
+    "xd_legacy_mergedata": [vp, vp, u32, vp, u32, vp],
     "xd_update_polygon_object_data": [vp] * 4 + [u32, vp],
     "xd_reduction_d3": [vp, u32, vp, vp],
     "xd_pair_list": [vp] * 4 + [u32, vp, vp, u64, vp, vp],

@@ -24,6 +24,7 @@ BUILD = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 LIBXDEM = os.path.join(PKG, "libxdem.so")
 LIBSHIM = os.path.join(PKG, "libxdem_mphysics.so")
+LIBLEGACY = os.path.join(PKG, "libxdem_legacy.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -31,10 +32,10 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 
 # FP64 translation units whose results must match the reference's arithmetic
 # are compiled without multiply-add contraction.
-NO_FMAD = {"xd_grid.cu", "xd_integrate.cu", "xd_contact64.cu", "xd_twin32.cu"}
+NO_FMAD = {"xd_grid.cu", "xd_integrate.cu", "xd_contact64.cu", "xd_twin32.cu", "xd_legacy.cu"}
 
 CUDA_SOURCES = ["xd_capi.cu", "xd_sort.cu", "xd_grid.cu", "xd_integrate.cu", "xd_contact64.cu",
-                "xd_scene.cu", "xd_noalloc.cu", "xd_mixed.cu", "xd_twin32.cu"]
+                "xd_scene.cu", "xd_noalloc.cu", "xd_mixed.cu", "xd_twin32.cu", "xd_legacy.cu"]
 
 
 def nvcc() -> str:
@@ -74,18 +75,19 @@ def build(verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link of libxdem.so failed:\n{r.stdout}\n{r.stderr}")
-    shim_src = os.path.join(CSRC, "shim_mphysics.cpp")
-    shim_deps = [shim_src, LIBXDEM, os.path.join(INCLUDE, "mphysics_cuda_dec.cuh"),
-                 os.path.join(INCLUDE, "xdem_host.h")]
-    if os.path.exists(shim_src) and not _newer(LIBSHIM, shim_deps):
-        cuda_root = os.path.dirname(os.path.dirname(nvcc()))
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", LIBSHIM, shim_src,
-               "-I", INCLUDE, "-I", os.path.join(cuda_root, "include"), "-L", PKG, "-lxdem",
-               "-L", os.path.join(cuda_root, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN",
-               "-Wl,-rpath," + os.path.join(cuda_root, "lib64")]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"build of libxdem_mphysics.so failed:\n{r.stdout}\n{r.stderr}")
+    for out, src, heads in ((LIBSHIM, "shim_mphysics.cpp", ("mphysics_cuda_dec.cuh", "xdem_host.h", "xdem.h")),
+                            (LIBLEGACY, "shim_legacy.cpp", ("cu_dem_dec.cuh", "xdem_legacy.h", "xdem.h"))):
+        shim_src = os.path.join(CSRC, src)
+        shim_deps = [shim_src, LIBXDEM] + [os.path.join(INCLUDE, h) for h in heads]
+        if os.path.exists(shim_src) and not _newer(out, shim_deps):
+            cuda_root = os.path.dirname(os.path.dirname(nvcc()))
+            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", out, shim_src,
+                   "-I", INCLUDE, "-I", os.path.join(cuda_root, "include"), "-L", PKG, "-lxdem",
+                   "-L", os.path.join(cuda_root, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN",
+                   "-Wl,-rpath," + os.path.join(cuda_root, "lib64")]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"build of {os.path.basename(out)} failed:\n{r.stdout}\n{r.stderr}")
     if verbose:
         print("built", LIBXDEM, file=sys.stderr)
     return LIBXDEM

@@ -159,3 +159,30 @@ def define_plane(xw, pa, pc, pb):
     rec["pa"], rec["pb"] = a, b
     rec["w2"], rec["w3"], rec["w4"] = pa, pc, pb
     return rec
+
+
+# ---- the legacy interface (cu_dem_dec.cuh:41-87) ----
+LEGACY_PARAMS = np.dtype({
+    "names": ["np", "nsp", "ncell", "grid", "dt", "half2dt", "cell_size", "gravity", "world_origin",
+              "kn", "vn", "ks", "vs", "mu", "cohesive"],
+    "formats": ["<u4", "<u4", "<u4", ("<u4", (3,)), "<f8", "<f8", "<f8", V3, V3,
+                "<f8", "<f8", "<f8", "<f8", "<f8", "<f8"],
+    "offsets": [0, 4, 8, 12, 24, 32, 40, 48, 72, 96, 104, 112, 120, 128, 136],
+    "itemsize": 144,
+})
+
+LEGACY_PLANE = np.dtype({
+    "names": ["l1", "l2", "u1", "u2", "uw", "xw", "pa", "pb"],
+    "formats": ["<f8", "<f8"] + [V3] * 6,
+    "offsets": [0, 8] + [16 + 24 * i for i in range(6)],
+    "itemsize": 160,
+})
+
+LEGACY_POLYGON = np.dtype({
+    "names": ["P", "Q", "R", "V", "W", "N"],
+    "formats": [V3] * 6,
+    "offsets": [24 * i for i in range(6)],
+    "itemsize": 144,
+})
+
+LEGACY_MASS_INFO = np.dtype({"names": ["pos", "vel"], "formats": [V3, V3], "offsets": [0, 24], "itemsize": 48})

@@ -20,6 +20,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_ORACLE = os.path.join(HERE, "libxd_oracle.so")
 LIB_REF = os.path.join(HERE, "_ref", "libxdref.so")
+LIB_REF_LEGACY = os.path.join(HERE, "_ref", "libxdref_legacy.so")
 
 _vp = C.c_void_p
 _u = C.c_uint
@@ -396,3 +397,71 @@ class RefKernels:
         self.vv_velocity(prm, sc.vel, sc.acc, sc.omega, sc.alpha, sc.force, sc.moment, sc.mass,
                          sc.inertia)
         return h, ix, cs, ce, so
+
+
+class LegacyRefKernels:
+    """The reference's legacy kernels (include/cu_dem_impl.cuh), compiled as
+    host code (oracle/_ref/libxdref_legacy.so).  Arrays in the legacy layouts:
+    pos, vel, acc, omega, alpha double4 rows, force and moment double3."""
+
+    def __init__(self, path: str = LIB_REF_LEGACY):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = C.CDLL(path)
+        for s_ in ("params", "plane", "polygon", "mass_info"):
+            getattr(self.lib, "xdrefl_sizeof_" + s_).restype = _u
+        for f in ("cube_hertzian_contact_force", "shape_hertzian_contact_force"):
+            getattr(self.lib, "xdrefl_" + f).restype = None
+
+    @staticmethod
+    def available(path: str = LIB_REF_LEGACY) -> bool:
+        return os.path.exists(path)
+
+    def sizes(self):
+        return {s_: getattr(self.lib, "xdrefl_sizeof_" + s_)() for s_ in ("params", "plane", "polygon", "mass_info")}
+
+    def set_params(self, prm):
+        self.lib.xdrefl_set_params(_p(prm))
+
+    def vv_position(self, pos, vel, acc, np_):
+        self.lib.xdrefl_vv_update_position(_p(pos), _p(vel), _p(acc), _u(np_))
+
+    def vv_velocity(self, vel, acc, omega, alpha, force, moment, np_):
+        self.lib.xdrefl_vv_update_velocity(_p(vel), _p(acc), _p(omega), _p(alpha), _p(force), _p(moment), _u(np_))
+
+    def mergedata(self, data, pos, np_, vertice, snp):
+        self.lib.xdrefl_mergedata(_p(data), _p(pos), _u(np_), _p(vertice), _u(snp))
+
+    def hash_and_index(self, hash_, index, pos, n):
+        self.lib.xdrefl_calculate_hash_and_index(_p(hash_), _p(index), _p(pos), _u(n))
+
+    def reorder(self, hash_, index, cstart, cend, sorted_, n, nc):
+        self.lib.xdrefl_reorder_and_find_cell_start(_p(hash_), _p(index), _p(cstart), _p(cend), _p(sorted_),
+                                                    _u(n), _u(nc))
+
+    def p2p(self, pos, vel, acc, omega, alpha, force, moment, sorted_, cstart, cend, np_):
+        self.lib.xdrefl_calculate_p2p(_p(pos), _p(vel), _p(acc), _p(omega), _p(alpha), _p(force), _p(moment),
+                                      _p(sorted_), _p(cstart), _p(cend), _u(np_), _u(0))
+
+    def cube(self, planes, kn, vn, ks, vs, mu, line, pos, vel, omega, force, moment, np_):
+        d = C.c_double
+        self.lib.xdrefl_cube_hertzian_contact_force(_p(planes), d(kn), d(vn), d(ks), d(vs), d(mu), _p(line),
+                                                    _p(pos), _p(vel), _p(omega), _p(force), _p(moment),
+                                                    _u(np_))
+
+    def shape(self, minfo, polygons, id_set, poly_start, poly_end, kn, vn, ks, vs, mu, line, pos, vel, omega,
+              force, moment, np_, sorted_, cstart, cend):
+        d = C.c_double
+        out = np.zeros(3)
+        self.lib.xdrefl_shape_hertzian_contact_force(_p(minfo), _p(polygons), _p(id_set), _p(poly_start),
+                                                     _p(poly_end), d(kn), d(vn), d(ks), d(vs), d(mu), _p(line),
+                                                     _p(pos), _p(vel), _p(omega), _p(force), _p(moment),
+                                                     _u(np_), _p(sorted_), _p(cstart), _p(cend), _p(out))
+        return out
+
+    def update_polygons_position(self, mpos, A, local_vertice, pos):
+        self.lib.xdrefl_update_polygons_position(_p(mpos), _p(A), _p(local_vertice), _u(local_vertice.shape[0]),
+                                                 _p(pos))
+
+    def update_polygons_information(self, polygons, indice, pos):
+        self.lib.xdrefl_update_polygons_information(_p(polygons), _p(indice), _p(pos), _u(indice.shape[0]))

@@ -16,7 +16,9 @@
 #include <cmath>
 #include "vector_types.h"
 
-/* ---- group 2: double3, const-reference twins ---- */
+/* ---- group 2: double3, const-reference twins (not for the legacy header,
+ *      cu_dem_impl.cuh, whose own double3 operators take values) ---- */
+#ifndef XD_REFSHIM_LEGACY
 inline double dot(const double3& a, const double3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline double3 operator-(const double3& a, const double3& b) { return make_double3(a.x - b.x, a.y - b.y, a.z - b.z); }
 inline double3 operator-(const double3& a) { return make_double3(-a.x, -a.y, -a.z); }
@@ -24,6 +26,7 @@ inline double3 operator*(double s, const double3& a) { return make_double3(s * a
 inline double3 operator+(const double3& a, const double3& b) { return make_double3(a.x + b.x, a.y + b.y, a.z + b.z); }
 inline double3 operator/(const double3& a, double s) { return make_double3(a.x / s, a.y / s, a.z / s); }
 inline double length(const double3& a) { return std::sqrt(dot(a, a)); }
+#endif
 
 /* ---- group 1: float vectors ---- */
 inline float3 make_float3(const float4& a) { return make_float3(a.x, a.y, a.z); }

@@ -122,3 +122,74 @@ def to_single(sc):
         out["pmi"] = rec_single(sc.pmi, POLYGON_MASS_F)
         out["cp_poly"] = rec_single(sc.cp_poly, CONTACT_PROPERTY_F)
     return out
+
+
+def legacy_constants(r_eq, m_eq, fric=scenes.FRICTION):
+    """The legacy interface's global contact constants (kn, vn, ks, vs, mu)
+    for one equivalent radius and mass, from the DHS definitions."""
+    import math
+    E, nu, e = scenes.E_YOUNG, scenes.POISSON, scenes.RESTITUTION
+    eeq = (E * E) / (E * (1 - nu * nu) + E * (1 - nu * nu))
+    beta = math.pi / math.log(e)
+    kn = (4.0 / 3.0) * eeq * math.sqrt(r_eq)
+    vn = math.sqrt((4.0 * m_eq * kn) / (1.0 + beta * beta))
+    return kn, vn, kn * scenes.STIFFNESS_RATIO, vn * scenes.STIFFNESS_RATIO, fric
+
+
+def to_legacy(sc, nsp=0, cell_size=None):
+    """A scene in the legacy layouts (cu_dem_dec.cuh): double4 pos, vel, acc
+    (mass in .w), omega, alpha (inertia in .w); double3 force and moment;
+    the parameter block with the particle-particle constants of the mean
+    radius."""
+    from metakonga_gb300.layouts import LEGACY_PARAMS
+    n = sc.np_
+    out = {"pos": np.ascontiguousarray(sc.pos, dtype=np.float64)}
+    for k, w in (("vel", None), ("acc", "mass"), ("omega", None), ("alpha", "inertia")):
+        a = np.zeros((n, 4))
+        a[:, :3] = getattr(sc, k)
+        if w:
+            a[:, 3] = getattr(sc, w)
+        out[k] = a
+    out["force"] = np.zeros((n, 3))
+    out["moment"] = np.zeros((n, 3))
+    r = float(sc.pos[:, 3].mean())
+    m = float(sc.mass.mean())
+    kn, vn, ks, vs, mu = legacy_constants(r / 2, m / 2)
+    p = np.zeros((), dtype=LEGACY_PARAMS)
+    p["np"], p["nsp"], p["ncell"] = n, nsp, sc.params["ncell"]
+    p["grid"] = sc.params["grid"]
+    p["dt"] = sc.params["dt"]
+    p["half2dt"] = sc.params["half2dt"]
+    p["cell_size"] = cell_size if cell_size is not None else sc.params["cell_size"]
+    p["gravity"] = sc.params["gravity"]
+    p["world_origin"] = sc.params["world_origin"]
+    p["kn"], p["vn"], p["ks"], p["vs"], p["mu"] = kn, vn, ks, vs, mu
+    p["cohesive"] = 0.0
+    out["params"] = p
+    out["wall"] = legacy_constants(r, m)
+    return out
+
+
+def legacy_planes(planes):
+    """Legacy plane records (no w2..w4) of live PLANE records."""
+    from metakonga_gb300.layouts import LEGACY_PLANE
+    out = np.zeros(planes.shape[0], dtype=LEGACY_PLANE)
+    for k in LEGACY_PLANE.names:
+        out[k] = planes[k]
+    return out
+
+
+def legacy_mesh(tri):
+    """Indexed mesh of triangles (T, 3, 3): vertices (V, 3), indice (T, 3)
+    and the polygons of each vertex as id_set / poly_start / poly_end."""
+    v = tri.reshape(-1, 3)
+    key = np.round(v, 12)
+    verts, inv = np.unique(key, axis=0, return_inverse=True)
+    inv = inv.reshape(-1)
+    indice = inv.reshape(-1, 3).astype(np.uint32)
+    pairs = sorted((int(indice[t, c]), t) for t in range(indice.shape[0]) for c in range(3))
+    id_set = np.array([t for _, t in pairs], np.uint32)
+    counts = np.bincount([vv for vv, _ in pairs], minlength=verts.shape[0])
+    poly_end = np.cumsum(counts).astype(np.uint32)
+    poly_start = (poly_end - counts).astype(np.uint32)
+    return verts.astype(np.float64), indice, id_set, poly_start, poly_end

@@ -14,8 +14,9 @@ from .cases import packed_scene, random_positions, small_drum
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 GOLDEN = sorted(p for p in glob.glob(os.path.join(HERE, "golden", "*.npz"))
-                if not os.path.basename(p).startswith("f32_"))
+                if not os.path.basename(p).startswith(("f32_", "legacy_")))
 GOLDEN_F32 = sorted(glob.glob(os.path.join(HERE, "golden", "f32_*.npz")))
+GOLDEN_LEGACY = sorted(glob.glob(os.path.join(HERE, "golden", "legacy_*.npz")))
 STATE = ("pos", "vel", "acc", "omega", "alpha", "force", "moment", "mass", "inertia")
 
 
@@ -79,6 +80,33 @@ def test_fp32_golden_reproduced_by_reference_kernels(tmp_path, monkeypatch):
         assert sorted(a.files) == sorted(b.files)
         for k in a.files:
             assert np.array_equal(a[k], b[k]), (path, k)
+
+
+def test_legacy_golden_reproduced_by_reference_kernels(tmp_path, monkeypatch):
+    """The legacy-interface fixtures are what the reference's legacy kernels
+    give now (regenerated into a temporary folder and compared bit for bit)."""
+    from oracle.pyoracle import LegacyRefKernels
+    if not LegacyRefKernels.available():
+        pytest.skip("legacy reference kernels not built here (oracle/_ref needs the reference tree)")
+    assert len(GOLDEN_LEGACY) == 2
+    from tests.golden import make_golden_legacy as gen
+    monkeypatch.setattr(gen, "HERE", str(tmp_path))
+    gen.main()
+    for path in GOLDEN_LEGACY:
+        a = np.load(path)
+        b = np.load(os.path.join(tmp_path, os.path.basename(path)))
+        assert sorted(a.files) == sorted(b.files)
+        for k in a.files:
+            assert np.array_equal(a[k], b[k]), (path, k)
+
+
+def test_legacy_layouts_match_reference_structs():
+    from oracle.pyoracle import LegacyRefKernels
+    if not LegacyRefKernels.available():
+        pytest.skip("legacy reference kernels not built here")
+    sz = LegacyRefKernels().sizes()
+    assert sz == {"params": layouts.LEGACY_PARAMS.itemsize, "plane": layouts.LEGACY_PLANE.itemsize,
+                  "polygon": layouts.LEGACY_POLYGON.itemsize, "mass_info": layouts.LEGACY_MASS_INFO.itemsize}
 
 
 def test_fp32_layouts_match_reference_structs():
@@ -216,10 +244,11 @@ def test_drum_mesh_winding_and_count():
 
 
 def test_abi_library_exports_every_declared_symbol():
-    """libxdem loads without a GPU and exports every function include/xdem.h declares."""
+    """libxdem loads without a GPU and exports every function include/xdem.h and
+    include/xdem_legacy.h declare."""
     from metakonga_gb300 import _lib
     lib = _lib.lib()
-    decl = open(os.path.join(ROOT, "include", "xdem.h")).read()
+    decl = "".join(open(os.path.join(ROOT, "include", h)).read() for h in ("xdem.h", "xdem_legacy.h"))
     names = set(re.findall(r"\b(xd_[a-z0-9_]+)\s*\(", decl))
     assert len(names) > 25
     for n in sorted(names):

@@ -1,0 +1,149 @@
+"""The legacy DEM interface (cu_dem_dec.cuh) on the GPU against the
+reference's own legacy kernels (fixtures from tests/golden/make_golden_legacy.py).
+
+Gates: hashes, sorted indices and occupied cells' ranges bit-exact; contact
+forces and moments within 1e-12 of max(|F_ref|, m g) per particle (FP64; the
+device pow and the reference's host pow may differ in the last place);
+positions 1e-13 and velocities 1e-9 relative after the steps; the mesh
+placement within 1e-15 of the mesh's extent; face/edge flags equal; the shape
+call's force sum within 1e-12 of the summed force magnitudes."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from metakonga_gb300._lib import call
+from metakonga_gb300.layouts import LEGACY_PARAMS, LEGACY_POLYGON
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TOL = 1e-12
+
+
+def _dev(a):
+    a = np.ascontiguousarray(a)
+    if a.dtype == np.uint32:
+        a = a.view(np.int32)
+    if a.dtype == np.bool_:
+        a = a.view(np.uint8)
+    return torch.from_numpy(a.copy()).cuda()
+
+
+def _h(t, dtype=None):
+    a = t.cpu().numpy()
+    return a.view(dtype) if dtype is not None else a
+
+
+def _err(f, f_ref, mass, g=9.81):
+    den = np.maximum(np.linalg.norm(f_ref, axis=1), mass * g)
+    return float((np.linalg.norm(f - f_ref, axis=1) / den).max())
+
+
+def _params(d):
+    p = np.frombuffer(d["params"].tobytes(), dtype=LEGACY_PARAMS).copy()
+    call("xd_legacy_set_symbolic_parameter", p.ctypes.data)
+    return p[0]
+
+
+def test_legacy_packed_steps_match_reference(cuda):
+    d = np.load(os.path.join(GOLDEN, "legacy_packed_512_cube.npz"))
+    p = _params(d)
+    n, nc = int(p["np"]), int(p["ncell"])
+    S = {k: _dev(d["in_" + k]) for k in ("pos", "vel", "acc", "omega", "alpha")}
+    S["force"] = torch.zeros((n, 3), dtype=torch.float64, device="cuda")
+    S["moment"] = torch.zeros_like(S["force"])
+    planes = _dev(d["planes"])
+    cend = torch.zeros(nc, dtype=torch.int32, device="cuda")
+    line = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    mass = d["in_acc"][:, 3]
+    kn, vn, ks, vs, mu = (float(x) for x in d["wall"])
+    P = lambda k: S[k].data_ptr()   # noqa: E731
+    for t in range(int(d["steps"])):
+        call("xd_legacy_vv_update_position", P("pos"), P("vel"), P("acc"), n, None)
+        h = torch.zeros(n, dtype=torch.int32, device="cuda")
+        ix = torch.zeros_like(h)
+        call("xd_legacy_calculate_hash_and_index", h.data_ptr(), ix.data_ptr(), P("pos"), n, None)
+        cs = torch.zeros(nc, dtype=torch.int32, device="cuda")
+        so = torch.zeros_like(h)
+        call("xd_legacy_reorder_and_find_cell_start", h.data_ptr(), ix.data_ptr(), cs.data_ptr(), cend.data_ptr(),
+             so.data_ptr(), n, nc, None)
+        S["force"].zero_()
+        S["moment"].zero_()
+        call("xd_legacy_calculate_p2p", P("pos"), P("vel"), P("acc"), P("omega"), P("alpha"), P("force"),
+             P("moment"), so.data_ptr(), cs.data_ptr(), cend.data_ptr(), n, 0, None)
+        torch.cuda.synchronize()
+        assert _err(_h(S["force"]), d[f"s{t}_p2p_force"], mass) <= TOL
+        assert _err(_h(S["moment"]) / 0.0057, d[f"s{t}_p2p_moment"] / 0.0057, mass) <= TOL
+        call("xd_legacy_cube_hertzian_contact_force", planes.data_ptr(), kn, vn, ks, vs, mu, line.data_ptr(),
+             P("pos"), P("vel"), P("omega"), P("force"), P("moment"), n, None)
+        torch.cuda.synchronize()
+        assert _err(_h(S["force"]), d[f"s{t}_force"], mass) <= TOL
+        assert _err(_h(S["moment"]) / 0.0057, d[f"s{t}_moment"] / 0.0057, mass) <= TOL
+        call("xd_legacy_vv_update_velocity", P("vel"), P("acc"), P("omega"), P("alpha"), P("force"),
+             P("moment"), n, None)
+        torch.cuda.synchronize()
+        cs_h, ce_h = _h(cs, np.uint32), _h(cend, np.uint32)
+        occ = np.flatnonzero(cs_h != 0xFFFFFFFF)
+        assert np.array_equal(_h(h, np.uint32), d[f"s{t}_hash"])
+        assert np.array_equal(_h(so, np.uint32), d[f"s{t}_sorted"])
+        assert np.array_equal(occ, d[f"s{t}_cells"])
+        assert np.array_equal(cs_h[occ], d[f"s{t}_cstart"]) and np.array_equal(ce_h[occ], d[f"s{t}_cend"])
+        for k, tol in (("pos", 1e-13), ("vel", 1e-9)):
+            ref = d[f"s{t}_{k}"]
+            assert np.abs(_h(S[k]) - ref).max() <= tol * np.abs(ref).max(), (t, k)
+        assert np.array_equal(_h(S["acc"])[:, 3], d[f"s{t}_acc"][:, 3])
+
+
+def test_legacy_shape_matches_reference(cuda):
+    d = np.load(os.path.join(GOLDEN, "legacy_drum_600_shape.npz"))
+    p = _params(d)
+    n, nc, nv = int(p["np"]), int(p["ncell"]), int(p["nsp"])
+    verts, A, mpos = _dev(d["verts"]), _dev(d["A"]), _dev(d["mpos"])
+    world = torch.zeros((nv, 3), dtype=torch.float64, device="cuda")
+    call("xd_legacy_update_polygons_position", mpos.data_ptr(), A.data_ptr(), verts.data_ptr(), nv,
+         world.data_ptr(), None)
+    ni = d["indice"].shape[0]
+    polygons = torch.zeros(ni * LEGACY_POLYGON.itemsize, dtype=torch.uint8, device="cuda")
+    call("xd_legacy_update_polygons_information", polygons.data_ptr(), _dev(d["indice"]).data_ptr(),
+         world.data_ptr(), ni, None)
+    pos = _dev(d["pos"])
+    data = torch.zeros((n + nv, 4), dtype=torch.float64, device="cuda")
+    call("xd_legacy_mergedata", data.data_ptr(), pos.data_ptr(), n, world.data_ptr(), nv, None)
+    h = torch.zeros(n + nv, dtype=torch.int32, device="cuda")
+    ix = torch.zeros_like(h)
+    call("xd_legacy_calculate_hash_and_index", h.data_ptr(), ix.data_ptr(), data.data_ptr(), n + nv, None)
+    cs = torch.zeros(nc, dtype=torch.int32, device="cuda")
+    ce = torch.zeros_like(cs)
+    so = torch.zeros_like(h)
+    call("xd_legacy_reorder_and_find_cell_start", h.data_ptr(), ix.data_ptr(), cs.data_ptr(), ce.data_ptr(),
+         so.data_ptr(), n + nv, nc, None)
+    force = torch.zeros((n, 3), dtype=torch.float64, device="cuda")
+    moment = torch.zeros_like(force)
+    line = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    total = np.zeros(3)
+    kn, vn, ks, vs, mu = (float(x) for x in d["wall"])
+    call("xd_legacy_shape_hertzian_contact_force", _dev(d["minfo"]).data_ptr(), polygons.data_ptr(),
+         _dev(d["id_set"]).data_ptr(), _dev(d["poly_start"]).data_ptr(), _dev(d["poly_end"]).data_ptr(),
+         kn, vn, ks, vs, mu, line.data_ptr(), pos.data_ptr(), _dev(d["vel"]).data_ptr(),
+         _dev(d["omega"]).data_ptr(), force.data_ptr(), moment.data_ptr(), None, n, so.data_ptr(), cs.data_ptr(),
+         ce.data_ptr(), total.ctypes.data, None)
+    torch.cuda.synchronize()
+    ext = np.abs(d["out_world"]).max()
+    assert np.abs(_h(world) - d["out_world"]).max() <= 1e-15 * ext
+    pg, pr = np.frombuffer(_h(polygons).tobytes(), LEGACY_POLYGON), d["out_polygons"].view(LEGACY_POLYGON)
+    for k in LEGACY_POLYGON.names:
+        assert np.abs(pg[k] - pr[k]).max() <= 1e-15 * max(ext, np.abs(pr[k]).max()), k
+    assert np.array_equal(_h(data), d["out_data"])
+    assert np.array_equal(_h(h, np.uint32), d["out_hash"])
+    assert np.array_equal(_h(so, np.uint32), d["out_sorted"])
+    cs_h = _h(cs, np.uint32)
+    occ = np.flatnonzero(cs_h != 0xFFFFFFFF)
+    assert np.array_equal(occ, d["out_cells"]) and np.array_equal(cs_h[occ], d["out_cstart"])
+    assert np.array_equal(_h(line).astype(bool), d["out_line"])
+    mass = np.pi * 4 / 3 * 2500.0 * d["pos"][:, 3] ** 3
+    assert _err(_h(force), d["out_force"], mass) <= TOL
+    r = d["pos"][:, 3:4]
+    assert _err(_h(moment) / r, d["out_moment"] / r, mass) <= TOL
+    assert np.abs(total - d["out_total"]).max() <= TOL * np.abs(d["out_force"]).sum()
