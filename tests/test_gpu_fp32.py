@@ -130,9 +130,10 @@ def test_fp32_cube_matches_reference_kernels(cuda):
     call("xd_set_symbolic_parameter_f", _rec(d["params_f"], PARAMS_F).ctypes.data)
     S = {k: _dev(d[k]) for k in ("pos", "vel", "omega", "force", "moment", "mass")}
     n = d["pos"].shape[0]
-    call("xd_cube_contact_force_f", 1, _raw_dev(d["planes6"]).data_ptr(),
+    planes6, cp = _raw_dev(d["planes6"]), _raw_dev(d["cp"])   # held until the call has run
+    call("xd_cube_contact_force_f", 1, planes6.data_ptr(),
          *[S[k].data_ptr() for k in ("pos", "vel", "omega", "force", "moment", "mass")], n,
-         _raw_dev(d["cp"]).data_ptr(), 0)
+         cp.data_ptr(), 0)
     torch.cuda.synchronize()
     assert (d["out_force"] != d["force"]).any()
     assert _err(_host(S["force"]), d["out_force"], d["mass"]) <= FORCE_TOL
@@ -161,6 +162,7 @@ def test_fp32_reduction(cuda):
     rng = np.random.Generator(np.random.MT19937(8))
     a = rng.normal(0.0, 1.0, (100_003, 3)).astype(np.float32)
     out = np.zeros(3, np.float32)
-    call("xd_reduction_f3", _dev(a).data_ptr(), a.shape[0], out.ctypes.data, 0)
+    da = _dev(a)
+    call("xd_reduction_f3", da.data_ptr(), a.shape[0], out.ctypes.data, 0)
     ref = a.astype(np.float64).sum(axis=0)
     assert np.abs(out - ref).max() <= 1e-5 * np.abs(a).sum()

@@ -106,7 +106,8 @@ def test_legacy_shape_matches_reference(cuda):
          world.data_ptr(), None)
     ni = d["indice"].shape[0]
     polygons = torch.zeros(ni * LEGACY_POLYGON.itemsize, dtype=torch.uint8, device="cuda")
-    call("xd_legacy_update_polygons_information", polygons.data_ptr(), _dev(d["indice"]).data_ptr(),
+    indice = _dev(d["indice"])
+    call("xd_legacy_update_polygons_information", polygons.data_ptr(), indice.data_ptr(),
          world.data_ptr(), ni, None)
     pos = _dev(d["pos"])
     data = torch.zeros((n + nv, 4), dtype=torch.float64, device="cuda")
@@ -124,10 +125,13 @@ def test_legacy_shape_matches_reference(cuda):
     line = torch.zeros(n, dtype=torch.uint8, device="cuda")
     total = np.zeros(3)
     kn, vn, ks, vs, mu = (float(x) for x in d["wall"])
-    call("xd_legacy_shape_hertzian_contact_force", _dev(d["minfo"]).data_ptr(), polygons.data_ptr(),
-         _dev(d["id_set"]).data_ptr(), _dev(d["poly_start"]).data_ptr(), _dev(d["poly_end"]).data_ptr(),
-         kn, vn, ks, vs, mu, line.data_ptr(), pos.data_ptr(), _dev(d["vel"]).data_ptr(),
-         _dev(d["omega"]).data_ptr(), force.data_ptr(), moment.data_ptr(), None, n, so.data_ptr(), cs.data_ptr(),
+    # device copies held in variables: a tensor freed right after data_ptr()
+    # would let the next one take its memory before the call runs
+    T = {k: _dev(d[k]) for k in ("minfo", "id_set", "poly_start", "poly_end", "vel", "omega")}
+    call("xd_legacy_shape_hertzian_contact_force", T["minfo"].data_ptr(), polygons.data_ptr(),
+         T["id_set"].data_ptr(), T["poly_start"].data_ptr(), T["poly_end"].data_ptr(),
+         kn, vn, ks, vs, mu, line.data_ptr(), pos.data_ptr(), T["vel"].data_ptr(),
+         T["omega"].data_ptr(), force.data_ptr(), moment.data_ptr(), None, n, so.data_ptr(), cs.data_ptr(),
          ce.data_ptr(), total.ctypes.data, None)
     torch.cuda.synchronize()
     ext = np.abs(d["out_world"]).max()
