@@ -151,3 +151,41 @@ def test_legacy_shape_matches_reference(cuda):
     r = d["pos"][:, 3:4]
     assert _err(_h(moment) / r, d["out_moment"] / r, mass) <= TOL
     assert np.abs(total - d["out_total"]).max() <= TOL * np.abs(d["out_force"]).sum()
+
+
+def test_legacy_api_program_matches_reference(cuda, tmp_path):
+    """A program using only the reference's legacy names (tests/cpp/legacy_step.cpp),
+    linked with libxdem_legacy.so, reproduces the fixture's two steps."""
+    import shutil
+    import subprocess
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    pkg = os.path.join(root, "metakonga_gb300")
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    cr = os.path.dirname(os.path.dirname(nvcc))
+    exe = tmp_path / "legacy_step"
+    subprocess.run(["g++", "-O2", "-std=c++17", os.path.join(here, "cpp", "legacy_step.cpp"),
+                    "-I", os.path.join(root, "include"), "-I", os.path.join(cr, "include"),
+                    "-L", pkg, "-lxdem_legacy", "-lxdem", "-L", os.path.join(cr, "lib64"), "-lcudart",
+                    "-Wl,-rpath," + pkg, "-Wl,-rpath," + os.path.join(cr, "lib64"), "-o", str(exe)], check=True)
+    d = np.load(os.path.join(GOLDEN, "legacy_packed_512_cube.npz"))
+    n = d["in_pos"].shape[0]
+    with open(tmp_path / "in.bin", "wb") as f:
+        f.write(np.array([n, int(d["steps"])], np.uint32).tobytes())
+        f.write(d["params"].tobytes())
+        f.write(d["planes"].tobytes())
+        f.write(np.asarray(d["wall"], np.float64).tobytes())
+        for k in ("pos", "vel", "acc", "omega", "alpha"):
+            f.write(np.ascontiguousarray(d["in_" + k]).tobytes())
+    r = subprocess.run([str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin")], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    buf = open(tmp_path / "out.bin", "rb").read()
+    t = int(d["steps"]) - 1
+    off = 0
+    for k, tol in (("pos", 1e-13), ("vel", 1e-9), ("acc", 1e-9), ("omega", 1e-9), ("alpha", 1e-9)):
+        a = np.frombuffer(buf, np.float64, 4 * n, off).reshape(n, 4)
+        off += 32 * n
+        ref = d[f"s{t}_{k}"]
+        assert np.abs(a - ref).max() <= tol * np.abs(ref).max(), k
+    assert np.array_equal(np.frombuffer(buf, np.uint32, n, off), d[f"s{t}_sorted"])
