@@ -1205,7 +1205,7 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
                                                     unsigned* __restrict__ counters,
                                                     unsigned* __restrict__ rec_count,
                                                     unsigned* __restrict__ rec_pairs, unsigned rec_cap,
-                                                    HistTable ht)
+                                                    HistTable ht, int rxn_on)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) counters[CN_REBUILD] = 0;
     const unsigned total = counters[CN_HEAVY];
@@ -1324,11 +1324,11 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
         // (impl:923-1021) in FP64, the normal from the face winding, the wall
         // velocity of the body at the contact point, no particle moment (ir = 0
         // as the reference calls DHSModel); Ft persists across triangles.  The
-        // reaction on each body goes to this particle's own slots of rxn and is
-        // summed over particles in a fixed order afterwards.
+        // reaction on each body accumulates in this particle's own slots of rxn
+        // over the steps and is summed over particles in a fixed order when the
+        // slots are flushed (at a re-binning and at the end of a call).
         const unsigned tc = P.ntri ? __ldg(tcount + i) : 0u;
         if (tc) {
-            for (unsigned q = 0; q < 6 * P.nbodies; ++q) rxn[(size_t)q * n + i] = 0.0;
             const float4 vh = __ldg(M.vh + i), vl = __ldg(M.vl + i);
             const float4 wl = __ldg(M.wl + i), wh = __ldg(M.wh + i);
             const double m = __ldg(mass0 + __float_as_uint(wl.w));
@@ -1378,13 +1378,15 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
                 const d3 fc = Fn + Ft;
                 f += fc;
                 const d3 rm = -cross(po2cp, fc);
-                double* rb = rxn + (size_t)b * 6 * n + i;
-                rb[0] -= fc.x;
-                rb[n] -= fc.y;
-                rb[2 * (size_t)n] -= fc.z;
-                rb[3 * (size_t)n] += rm.x;
-                rb[4 * (size_t)n] += rm.y;
-                rb[5 * (size_t)n] += rm.z;
+                if (rxn_on) {
+                    double* rb = rxn + (size_t)b * 6 * n + i;
+                    rb[0] -= fc.x;
+                    rb[n] -= fc.y;
+                    rb[2 * (size_t)n] -= fc.z;
+                    rb[3 * (size_t)n] += rm.x;
+                    rb[4 * (size_t)n] += rm.y;
+                    rb[5 * (size_t)n] += rm.z;
+                }
             }
             F.x += (float)f.x;
             F.y += (float)f.y;
@@ -1397,8 +1399,8 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Mas
     }
 }
 
-// Body reactions: rxn[(b * 6 + q) * n + i] summed over i in a fixed order and
-// added to the bodies, in one launch.  Each block sums a fixed chunk of i for
+// Body reactions: rxn[(b * 6 + q) * n + i] summed over i in a fixed order,
+// added to the bodies and the slots cleared, in one launch (a flush).  Each block sums a fixed chunk of i for
 // every q (per thread a strided run, then a fixed shuffle tree and the warps
 // in order) into part[q * gridDim.x + block]; the last block to finish adds
 // the blocks' partials in block order.  The order depends only on n and the
@@ -1408,7 +1410,7 @@ constexpr unsigned kRxnThreads = 256;
 
 static unsigned rxn_grid(unsigned n) { return std::max(1u, std::min(kRxnBlocks, (n + kRxnThreads - 1) / kRxnThreads)); }
 
-__global__ void __launch_bounds__(kRxnThreads) k_rxn_sum(const double* __restrict__ rxn, unsigned n, unsigned nbodies,
+__global__ void __launch_bounds__(kRxnThreads) k_rxn_sum(double* __restrict__ rxn, unsigned n, unsigned nbodies,
                                                          double* __restrict__ part, unsigned* __restrict__ counters,
                                                          xd_polygon_mass_info* __restrict__ pmi)
 {
@@ -1422,10 +1424,13 @@ __global__ void __launch_bounds__(kRxnThreads) k_rxn_sum(const double* __restric
         // the six components of one body together: six independent loads per
         // particle and one barrier per body
         double v[6] = { 0.0, 0.0, 0.0, 0.0, 0.0, 0.0 };
-        const double* rb = rxn + (size_t)b * 6 * n;
+        double* rb = rxn + (size_t)b * 6 * n;
         for (unsigned i = b0 + threadIdx.x; i < b1; i += blockDim.x)
 #pragma unroll
-            for (int c = 0; c < 6; ++c) v[c] += rb[(size_t)c * n + i];
+            for (int c = 0; c < 6; ++c) {
+                v[c] += rb[(size_t)c * n + i];
+                rb[(size_t)c * n + i] = 0.0;   // flushed
+            }
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
             for (unsigned o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
@@ -1888,6 +1893,9 @@ int mixed_upload(MixedScene* s, const double* pos, const double* vel, const doub
     s->cur = 0;
     s->cells_clean = false;   // the state is in upload order again: the next step re-bins
     st = reset_history(s, q);   // an uploaded state starts with no springs
+    if (st == XD_OK && s->nbodies)   // nor unflushed body reactions
+        st = cuda_status(cudaMemsetAsync(s->rxn, 0, sizeof(double) * 6 * s->nbodies * (size_t)s->n, q),
+                         "mixed upload");
     if (st != XD_OK) return st;
     st = cuda_status(cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * CN_DECISIONS, q), "mixed upload");
     if (st != XD_OK) return st;
@@ -1990,10 +1998,22 @@ __global__ void __launch_bounds__(256) k_hist_gather(unsigned n, unsigned slots,
     }
 }
 
+// The reactions accumulated in the per-particle slots since the last flush
+// go to the bodies (the slots belong to particle slots, which a re-binning
+// reorders).
+static int flush_reactions(MixedScene* s, cudaStream_t q)
+{
+    if (!s->nbodies || !s->n) return XD_OK;
+    k_rxn_sum<<<rxn_grid(s->n), kRxnThreads, 0, q>>>(s->rxn, s->n, s->nbodies, s->rxn_part, s->counters, s->pmi);
+    return launch_status("mixed body reaction");
+}
+
 static int rebuild(MixedScene* s, cudaStream_t q)
 {
     const unsigned n = s->n;
-    int st = cuda_status(cudaMemsetAsync(s->counters + CN_GAPS, 0, 2 * sizeof(unsigned), q), "mixed re-binning");
+    int st = flush_reactions(s, q);
+    if (st != XD_OK) return st;
+    st = cuda_status(cudaMemsetAsync(s->counters + CN_GAPS, 0, 2 * sizeof(unsigned), q), "mixed re-binning");
     if (st != XD_OK) return st;
     k_mx_keys<<<blocks(n, 256), 256, 0, q>>>(s->P, s->pf, s->keys, s->vals);
     st = launch_status("mixed keys");
@@ -2142,7 +2162,8 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
                                                           s->vcount, s->vlist, s->hlist, s->wmask, s->planes,    \
                                                           s->cps, s->mass0, s->poly, s->pmi, s->tcount, s->tlist, \
                                                           s->tpk_sorted, s->tpt_sorted, s->tpair_cap, s->rxn,   \
-                                                          s->Fc, s->Mc, s->counters, rc, rp, record ? rec_cap : 0u, ht)
+                                                          s->Fc, s->Mc, s->counters, rc, rp, record ? rec_cap : 0u, ht, \
+                                                          MODE == 3 ? 0 : 1)
     if (record) {
         if (hist == 2) XD_MX_CONTACT(true, 2);
         else if (hist == 1) XD_MX_CONTACT(true, 1);
@@ -2154,11 +2175,6 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
     }
 #undef XD_MX_CONTACT
     st = launch_status("mixed contact");
-    if (st == XD_OK && s->nbodies && MODE != 3) {
-        // this step's reaction on the polygon bodies, summed in a fixed order
-        k_rxn_sum<<<rxn_grid(n), kRxnThreads, 0, q>>>(s->rxn, n, s->nbodies, s->rxn_part, s->counters, s->pmi);
-        st = launch_status("mixed body reaction");
-    }
     ph.end(3, q);
     return st;
 }
@@ -2235,11 +2251,16 @@ int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
         for (unsigned t = 1; t < nsteps && st == XD_OK; ++t) st = step_once<1>(s, q, ph, false, 0, nullptr);
         if (st != XD_OK) return st;
     }
-    // the last velocity update
+    // the last velocity update, and the call's body reactions
     ph.begin(0, q);
     k_mx_finish<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[0], s->Fc, s->Mc);
     st = launch_status("mixed finish");
     ph.end(0, q);
+    if (st == XD_OK) {
+        ph.begin(3, q);
+        st = flush_reactions(s, q);
+        ph.end(3, q);
+    }
     return st;
 }
 
@@ -2248,8 +2269,8 @@ unsigned long long mixed_launches(MixedScene* s, unsigned nsteps)
     if (!s || nsteps == 0 || s->n == 0) return 0;
     // per step: advance + contact; + the last velocity update; a step that
     // re-bins adds mixed_rebuild_launches()
-    const unsigned long long per = 2 + (s->nbodies ? 1 : 0);
-    unsigned long long total = per * nsteps + 1;
+    const unsigned long long per = 2;
+    unsigned long long total = per * nsteps + 1 + (s->nbodies ? 1 : 0);
     if (!s->cells_clean) total += mixed_rebuild_launches(s);   // the first step re-bins
     return total;
 }
@@ -2261,6 +2282,7 @@ unsigned long long mixed_rebuild_launches(MixedScene* s)
     // triangles also count, scan, fill, pad, their sort and their lists
     unsigned long long k = (s->n > 1 ? 5ull * s->passes : 0ull) + 6;
     if (s->ntri) k += 5 + 5ull * ((key_bits_for(s->ncell + 1) + 7) / 8);
+    if (s->nbodies) k += 1;   // the reactions flushed first
     return k;
 }
 
