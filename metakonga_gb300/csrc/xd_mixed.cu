@@ -194,7 +194,7 @@ struct MixedScene {
     // host-order transfer buffers
     double* xfer = nullptr;
     bool ready = false;                // grid and buffers set up (first upload)
-    cudaGraphExec_t graph[3] = { nullptr, nullptr, nullptr };   // first step, two steps, one step
+    cudaGraphExec_t graph[5] = {};   // first step; 1, 2, 4 and 8 middle steps
     // tangential-spring history (an extension): [s * n + slot] tables in the
     // state's slot order, permuted with the particles at re-binning
     unsigned hslots = 0;
@@ -1847,7 +1847,7 @@ void mixed_destroy(MixedScene* s)
 {
     if (!s) return;
     cudaDeviceSynchronize();
-    for (int k = 0; k < 3; ++k)
+    for (int k = 0; k < 5; ++k)
         if (s->graph[k]) cudaGraphExecDestroy(s->graph[k]);
     for (void* p : s->allocs) cudaFree(p);
     delete s;
@@ -2179,10 +2179,13 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
     return st;
 }
 
-// Step graphs of a scene: kFirstStep (the first step of a call, MODE 0),
-// kTwoSteps and kOneStep (middle steps, MODE 1); each step has its own
-// conditional re-binning node.
-enum { kFirstStep = 0, kTwoSteps = 1, kOneStep = 2 };
+// Step graphs of a scene: kFirstStep (the first step of a call, MODE 0) and
+// graphs of 1, 2, 4 and 8 middle steps (MODE 1), each step with its own
+// conditional re-binning node; a call replays the first step, then runs of
+// eight, then the binary digits of what is left.
+enum { kFirstStep = 0, kSteps1 = 1, kSteps2 = 2, kSteps4 = 3, kSteps8 = 4, kGraphKinds = 5 };
+
+static unsigned graph_steps(int kind) { return kind == kFirstStep ? 1u : 1u << (kind - 1); }
 
 static int capture_steps(MixedScene* s, int kind)
 {
@@ -2192,22 +2195,19 @@ static int capture_steps(MixedScene* s, int kind)
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     int st = cuda_status(e, "mixed graph capture");
     cudaGraph_t cg = nullptr;
-    cudaGraphConditionalHandle h[2] = { 0, 0 };
+    cudaGraphConditionalHandle h[8] = {};
     if (st == XD_OK) {
         cudaStreamCaptureStatus cst;
         st = cuda_status(cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg), "mixed capture info");
     }
-    const int nh = kind == kTwoSteps ? 2 : 1;
-    for (int k = 0; k < nh && st == XD_OK; ++k)
+    const unsigned nh = graph_steps(kind);
+    for (unsigned k = 0; k < nh && st == XD_OK; ++k)
         st = cuda_status(cudaGraphConditionalHandleCreate(&h[k], cg, 0, cudaGraphCondAssignDefault),
                          "mixed conditional handle");
     const bool clean = s->cells_clean;
     Phases none;
-    if (st == XD_OK) {
-        if (kind == kFirstStep) st = step_once<0>(s, cs, none, false, 0, &h[0]);
-        else st = step_once<1>(s, cs, none, false, 0, &h[0]);
-    }
-    if (st == XD_OK && kind == kTwoSteps) st = step_once<1>(s, cs, none, false, 0, &h[1]);
+    for (unsigned k = 0; k < nh && st == XD_OK; ++k)
+        st = kind == kFirstStep ? step_once<0>(s, cs, none, false, 0, &h[k]) : step_once<1>(s, cs, none, false, 0, &h[k]);
     s->cells_clean = clean;   // capture only recorded the launches
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(cs, &g);
@@ -2240,9 +2240,10 @@ int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
         if (!s->cells_clean)
             st = cuda_status(cudaMemsetAsync(s->counters + CN_REBUILD, 1, 1, q), "mixed re-binning flag");
         if (st == XD_OK) st = launch_steps(s, kFirstStep, q);
-        unsigned t = 1;
-        for (; st == XD_OK && nsteps - t >= 2; t += 2) st = launch_steps(s, kTwoSteps, q);
-        if (st == XD_OK && t < nsteps) st = launch_steps(s, kOneStep, q);
+        unsigned left = nsteps - 1;
+        for (; st == XD_OK && left >= 8; left -= 8) st = launch_steps(s, kSteps8, q);
+        for (int kind = kSteps4; kind >= kSteps1 && st == XD_OK; --kind)
+            if (left & graph_steps(kind)) st = launch_steps(s, kind, q);
         if (st != XD_OK) return st;
         s->cells_clean = true;
     } else {
@@ -2406,7 +2407,7 @@ int mixed_set_history(MixedScene* s, unsigned slots)
         return st;
     }
     // the step graphs hold the table pointers: capture them again
-    for (int k = 0; k < 3; ++k)
+    for (int k = 0; k < 5; ++k)
         if (s->graph[k]) {
             cudaGraphExecDestroy(s->graph[k]);
             s->graph[k] = nullptr;
