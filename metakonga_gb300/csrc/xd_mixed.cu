@@ -2237,7 +2237,11 @@ int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
         // Every step in a graph, re-binning decided on the device: the call
         // never waits for the GPU.  A scene without cells yet (after an
         // upload) is made to re-bin through the same flag.
-        if (!s->cells_clean)
+        // all step graphs are captured at the first call, so that later calls
+        // of any length only replay
+        for (int kind = 0; kind < kGraphKinds && st == XD_OK; ++kind)
+            if (!s->graph[kind]) st = capture_steps(s, kind);
+        if (st == XD_OK && !s->cells_clean)
             st = cuda_status(cudaMemsetAsync(s->counters + CN_REBUILD, 1, 1, q), "mixed re-binning flag");
         if (st == XD_OK) st = launch_steps(s, kFirstStep, q);
         unsigned left = nsteps - 1;
