@@ -7,16 +7,21 @@ the budget next to the scenes already resident, then advances every resident
 scene by up to ``chunk`` steps per tick in one ``engine.step_many`` call: the
 scenes' kernels run side by side on the library's stream pool, so requests
 that arrive while others run join the next tick instead of waiting for the
-GPU to drain.  A scene whose steps are done is downloaded and freed, which
-makes room for the next request.  Each result is the one the scene gives when
-stepped alone (the step sequence of a scene does not depend on how its steps
-are split into calls or on what runs beside it).
+GPU to drain.  Ticks are queued ``depth`` deep: the host counts steps, marks
+each tick with an event and only waits for the oldest mark, so the GPU is fed
+while the host admits, downloads and retires.  A scene whose steps are done is
+downloaded (on a side stream that waits for its last tick only) and freed when
+the device is idle or memory is needed, which makes room for the next
+request.  Each result is the one the scene gives when stepped alone (the step
+sequence of a scene does not depend on how its steps are split into calls or
+on what runs beside it).
 
 The reference runs one model per process (xDynamicsSolver); this loop has no
 counterpart there.
 """
 from __future__ import annotations
 
+import collections
 import dataclasses
 import math
 import time
@@ -85,20 +90,49 @@ class Request:
     result: dict = None
 
 
+class _CudaMarks:
+    """Tick marks: CUDA events on the server's stream, and a side stream for
+    downloads that waits for one mark only."""
+
+    def __init__(self, stream: int):
+        import torch
+        self.torch = torch
+        self.main = torch.cuda.ExternalStream(stream) if stream else torch.cuda.current_stream()
+        self.side = torch.cuda.Stream()
+
+    def mark(self):
+        ev = self.torch.cuda.Event()
+        ev.record(self.main)
+        return ev
+
+    def wait(self, mark) -> None:
+        mark.synchronize()
+
+    def side_after(self, mark) -> int:
+        self.side.wait_event(mark)
+        return self.side.cuda_stream
+
+
 class Server:
     """Continuous-batching DEM server on the current CUDA device.
 
     budget_bytes: device memory the resident scenes may hold together (a
     request larger than the budget is admitted alone when nothing else is
     resident).  chunk: steps per scene per tick; smaller chunks admit new
-    requests sooner, larger ones cost fewer host round trips."""
+    requests sooner, larger ones cost fewer host calls.  depth: ticks queued
+    on the device before the host waits for the oldest (0: wait for each)."""
 
     def __init__(self, budget_bytes: int, chunk: int = 20, mode: int = engine.MODE_MIXED,
-                 stream: int = 0, keep_results: bool = True, clock=time.perf_counter):
+                 stream: int = 0, keep_results: bool = True, clock=time.perf_counter, depth: int = 2,
+                 marks=None):
         if chunk < 1:
             raise ValueError("chunk must be >= 1")
+        if depth < 0:
+            raise ValueError("depth must be >= 0")
         self.budget = int(budget_bytes)
         self.chunk = int(chunk)
+        self.depth = int(depth)
+        self.marks = marks
         self.mode = mode
         self.stream = stream
         self.keep_results = keep_results
@@ -110,6 +144,7 @@ class Server:
         self.ticks = 0
         self.peak_active = 0
         self.wall = 0.0
+        self._to_close: list = []
 
     def submit(self, rid, scene, steps: int, arrival: float = 0.0) -> None:
         if steps < 1:
@@ -118,12 +153,16 @@ class Server:
                                     bytes=estimate_device_bytes(scene, self.mode),
                                     remaining=int(steps)))
 
+    def _fits(self, r: Request, active: list) -> bool:
+        # alone only when nothing else holds device memory
+        return (not active and not self._to_close) or self.used + r.bytes <= self.budget
+
     def _admit(self, now: float, active: list, t0: float) -> None:
         # first come, first served: a request that does not fit holds back the
         # ones behind it, so that a large request is not starved
         while self.pending and self.pending[0].arrival <= now:
             r = self.pending[0]
-            if active and self.used + r.bytes > self.budget:
+            if not self._fits(r, active):
                 break
             self.pending.pop(0)
             r.handle = engine.DeviceScene(r.scene, mode=self.mode)
@@ -134,34 +173,60 @@ class Server:
 
     def run(self) -> list:
         """Serve every submitted request; returns them in completion order."""
+        marks = self.marks if self.marks is not None else _CudaMarks(self.stream)
         self.pending.sort(key=lambda r: r.arrival)
         active: list = []
+        inflight = collections.deque()   # (mark, requests whose last tick it ends)
+        to_close = self._to_close = []    # retired, device memory not yet freed
         t0 = self.clock()
-        while self.pending or active:
-            now = self.clock() - t0
-            self._admit(now, active, t0)
-            if not active:
-                time.sleep(max(0.0, self.pending[0].arrival - (self.clock() - t0)))
-                continue
-            self.peak_active = max(self.peak_active, len(active))
-            counts = [min(self.chunk, r.remaining) for r in active]
-            engine.step_many([r.handle for r in active], counts, check=True, stream=self.stream)
-            self.ticks += 1
-            now = self.clock() - t0
-            still = []
-            for r, c in zip(active, counts):
-                r.remaining -= c
-                if r.remaining:
-                    still.append(r)
-                    continue
+
+        def retire_one():
+            mark, fin = inflight.popleft()
+            marks.wait(mark)
+            for r in fin:
                 if self.keep_results:
-                    r.result = r.handle.download(self.stream)
+                    r.result = r.handle.download(marks.side_after(mark))
+                r.done = self.clock() - t0
+                self.finished.append(r)
+                to_close.append(r)
+
+        def close_finished():
+            # freeing device memory synchronises the device: done when it is idle
+            while inflight:
+                retire_one()
+            for r in to_close:
                 r.handle.close()
                 r.handle = None
-                r.done = self.clock() - t0
                 self.used -= r.bytes
-                self.finished.append(r)
-            active = still
+            to_close.clear()
+
+        while self.pending or active or inflight:
+            now = self.clock() - t0
+            self._admit(now, active, t0)
+            blocked = bool(self.pending and self.pending[0].arrival <= now
+                           and not self._fits(self.pending[0], active))
+            if blocked and to_close:
+                close_finished()
+                continue
+            if active:
+                self.peak_active = max(self.peak_active, len(active))
+                counts = [min(self.chunk, r.remaining) for r in active]
+                engine.step_many([r.handle for r in active], counts, check=False, stream=self.stream)
+                self.ticks += 1
+                fin, still = [], []
+                for r, c in zip(active, counts):
+                    r.remaining -= c
+                    (still if r.remaining else fin).append(r)
+                active = still
+                inflight.append((marks.mark(), fin))
+            while inflight and (len(inflight) > self.depth or not active):
+                retire_one()
+            if not active and not inflight:
+                if to_close:
+                    close_finished()
+                if self.pending:
+                    time.sleep(max(0.0, self.pending[0].arrival - (self.clock() - t0)))
+        close_finished()
         self.wall = self.clock() - t0
         return self.finished
 

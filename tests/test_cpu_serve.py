@@ -25,6 +25,19 @@ class _FakeScene:
         _FakeScene.live -= 1
 
 
+class _Marks:
+    """Tick marks for the fake device: nothing to wait for."""
+
+    def mark(self):
+        return None
+
+    def wait(self, mark):
+        pass
+
+    def side_after(self, mark):
+        return 0
+
+
 class _Clock:
     """Deterministic clock: each tick of the fake batch advances 1 ms."""
 
@@ -61,7 +74,7 @@ def _named(name, n_side=4):
 
 def test_chunks_and_results(fake):
     clock, calls = fake
-    srv = serve.Server(budget_bytes=1 << 40, chunk=4, clock=clock)
+    srv = serve.Server(budget_bytes=1 << 40, chunk=4, clock=clock, marks=_Marks(), depth=0)
     srv.submit("a", _named("a"), 10)
     srv.submit("b", _named("b"), 3)
     done = srv.run()
@@ -74,7 +87,7 @@ def test_chunks_and_results(fake):
 
 def test_late_arrival_joins_running_batch(fake):
     clock, calls = fake
-    srv = serve.Server(budget_bytes=1 << 40, chunk=2, clock=clock)
+    srv = serve.Server(budget_bytes=1 << 40, chunk=2, clock=clock, marks=_Marks(), depth=0)
     srv.submit("a", _named("a"), 20, arrival=0.0)
     srv.submit("b", _named("b"), 4, arrival=0.0035)
     done = srv.run()
@@ -89,11 +102,26 @@ def test_late_arrival_joins_running_batch(fake):
     assert b.done - b.arrival == pytest.approx(0.0025)
 
 
+def test_pipelined_ticks_retire_depth_ticks_later(fake):
+    """With two ticks queued, a finished request is retired (downloaded) when
+    two more ticks have been issued; the issued ticks are the same."""
+    clock, calls = fake
+    srv = serve.Server(budget_bytes=1 << 40, chunk=2, clock=clock, marks=_Marks(), depth=2)
+    srv.submit("a", _named("a"), 20, arrival=0.0)
+    srv.submit("b", _named("b"), 4, arrival=0.0035)
+    done = srv.run()
+    assert calls[4] == [("a", 2), ("b", 2)] and calls[5] == [("a", 2), ("b", 2)]
+    b = [r for r in done if r.rid == "b"][0]
+    assert b.done - b.arrival == pytest.approx(0.0045)
+    assert all(r.result["steps"] == r.steps for r in done)
+    assert _FakeScene.live == 0
+
+
 def test_budget_is_first_come_first_served(fake):
     clock, calls = fake
     big, small = _named("big", 6), _named("s2", 3)
     eb, es = serve.estimate_device_bytes(big), serve.estimate_device_bytes(small)
-    srv = serve.Server(budget_bytes=eb + es - 1, chunk=5, clock=clock)
+    srv = serve.Server(budget_bytes=eb + es - 1, chunk=5, clock=clock, marks=_Marks(), depth=0)
     srv.submit("s1", _named("s1", 3), 5, arrival=0.0)
     srv.submit("big", big, 5, arrival=0.0)
     srv.submit("s2", small, 5, arrival=0.0)
@@ -108,7 +136,7 @@ def test_budget_is_first_come_first_served(fake):
 
 def test_oversized_request_runs_alone(fake):
     clock, calls = fake
-    srv = serve.Server(budget_bytes=1, chunk=5, clock=clock)
+    srv = serve.Server(budget_bytes=1, chunk=5, clock=clock, marks=_Marks(), depth=0)
     srv.submit("x", _named("x"), 5)
     srv.submit("y", _named("y"), 5)
     done = srv.run()
@@ -118,7 +146,7 @@ def test_oversized_request_runs_alone(fake):
 
 def test_idle_server_waits_for_arrivals(fake):
     clock, calls = fake
-    srv = serve.Server(budget_bytes=1 << 40, chunk=5, clock=clock)
+    srv = serve.Server(budget_bytes=1 << 40, chunk=5, clock=clock, marks=_Marks(), depth=0)
     srv.submit("late", _named("late"), 5, arrival=2.0)
     done = srv.run()
     assert done[0].admitted >= 2.0
@@ -127,7 +155,7 @@ def test_idle_server_waits_for_arrivals(fake):
 
 def test_report_percentiles(fake):
     clock, _ = fake
-    srv = serve.Server(budget_bytes=1 << 40, chunk=1, clock=clock)
+    srv = serve.Server(budget_bytes=1 << 40, chunk=1, clock=clock, marks=_Marks(), depth=0)
     for k in range(10):
         srv.submit(k, _named(str(k)), k + 1)
     srv.run()
