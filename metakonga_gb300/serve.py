@@ -238,12 +238,14 @@ class Server:
         lat = np.array([r.done - r.arrival for r in self.finished]) * 1e3
         wait = np.array([r.admitted - r.arrival for r in self.finished]) * 1e3
         work = float(sum(r.scene.np_ * r.steps for r in self.finished))
+        span = max(r.arrival for r in self.finished)
         return {"requests": len(self.finished),
                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                 "p50_wait_ms": float(np.percentile(wait, 50)),
                 "p99_wait_ms": float(np.percentile(wait, 99)),
                 "particle_steps": work, "wall_s": self.wall,
                 "particle_steps_per_s": work / self.wall if self.wall > 0 else 0.0,
+                "offered_particle_steps_per_s": work / span if span > 0 else None,
                 "ticks": self.ticks, "peak_active": self.peak_active,
                 "peak_booked_bytes": self.peak_used}
 
