@@ -492,6 +492,16 @@ unsigned long long xd_scene_launches(xd_scene* scene, unsigned nsteps);
 int xd_scene_rebuilds(xd_scene* scene, unsigned long long* count, unsigned long long* launches_each,
                       void* stream);
 
+/* Kinematic polygon bodies, an extension (the reference moves its bodies
+ * through its multibody solver on the host, one D2H/H2D round trip per
+ * step): with enable != 0, every step first moves each body by its own vel
+ * and omega (as set by xd_scene_set_bodies) over dt -- origin += dt vel, the
+ * Euler parameters p <- q (x) p with q the rotation of angle |omega| dt about
+ * omega, normalised -- and the triangles with it
+ * (cu_updatePolygonObjectData semantics), all on the device.  The mixed form
+ * re-bins when a vertex has moved half the skin. */
+int xd_scene_set_kinematic_bodies(xd_scene* scene, int enable);
+
 /* Tangential-spring history, an extension: the reference's DHSModel
  * (mphysics_cuda_impl.cuh:379-401) keeps no state between steps.  With
  * slots > 0 (at most 32) every particle keeps up to `slots` contacts keyed

@@ -96,6 +96,7 @@ _SIGS = {
     "xd_scene_rebuilds": [vp, vp, vp, vp],
     "xd_scene_step_many": [vp, vp, u32, i32, vp],
     "xd_scene_set_tangential_history": [vp, u32],
+    "xd_scene_set_kinematic_bodies": [vp, i32],
     "xd_scene_download_history": [vp, vp, vp, vp, vp],
     "xd_scene_device_bytes": [vp, vp],
     "xd_scene_phase_times": [vp, vp, vp],

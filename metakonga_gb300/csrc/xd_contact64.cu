@@ -555,6 +555,42 @@ int launch_polygon(const Params& P, const xd_polygon_info* dpi, xd_polygon_mass_
     return launch_status("particle_polygon_collision (reaction)");
 }
 
+// One step of prescribed body motion (an extension; the reference moves its
+// bodies through the multibody solver on the host): origin += dt vel, the
+// Euler parameters p <- q (x) p with q the rotation of angle |omega| dt about
+// omega, normalised.  One thread per body.
+__global__ void k_body_advance(xd_polygon_mass_info* __restrict__ pmi, unsigned nbodies, double dt)
+{
+    const unsigned b = threadIdx.x;
+    if (b >= nbodies) return;
+    xd_polygon_mass_info* m = pmi + b;
+    for (int a = 0; a < 3; ++a) m->origin[a] = m->origin[a] + dt * m->vel[a];
+    const double wx = m->omega[0], wy = m->omega[1], wz = m->omega[2];
+    const double w = sqrt(wx * wx + wy * wy + wz * wz);
+    if (w > 0.0) {
+        const double h = 0.5 * w * dt;
+        const double c = cos(h), sn = sin(h) / w;
+        const double a0 = c, a1 = sn * wx, a2 = sn * wy, a3 = sn * wz;
+        const double p0 = m->ep[0], p1 = m->ep[1], p2 = m->ep[2], p3 = m->ep[3];
+        const double r0 = a0 * p0 - (a1 * p1 + a2 * p2 + a3 * p3);
+        const double r1 = a0 * p1 + p0 * a1 + (a2 * p3 - a3 * p2);
+        const double r2 = a0 * p2 + p0 * a2 + (a3 * p1 - a1 * p3);
+        const double r3 = a0 * p3 + p0 * a3 + (a1 * p2 - a2 * p1);
+        const double nr = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + r3 * r3);
+        m->ep[0] = r0 / nr;
+        m->ep[1] = r1 / nr;
+        m->ep[2] = r2 / nr;
+        m->ep[3] = r3 / nr;
+    }
+}
+
+int launch_body_advance(xd_polygon_mass_info* pmi, unsigned nbodies, double dt, cudaStream_t s)
+{
+    if (nbodies == 0) return XD_OK;
+    k_body_advance<<<1, 32, 0, s>>>(pmi, nbodies, dt);
+    return launch_status("kinematic bodies");
+}
+
 int launch_update_polygon(const xd_polygon_mass_info* dpmi, const double* vlist, double* sphere,
                           xd_polygon_info* dpi, unsigned ntri, cudaStream_t s)
 {

@@ -45,6 +45,7 @@ int launch_polygon(const Params& P, const xd_polygon_info* dpi, xd_polygon_mass_
                    double* moment, const double* mass, const unsigned* sidx,
                    const unsigned* cstart, const unsigned* cend, const xd_contact_property* cp,
                    unsigned nbodies, void* scratch, cudaStream_t s, const HistTable* ht = nullptr);
+int launch_body_advance(xd_polygon_mass_info* pmi, unsigned nbodies, double dt, cudaStream_t s);
 int launch_update_polygon(const xd_polygon_mass_info* dpmi, const double* vlist, double* sphere,
                           xd_polygon_info* dpi, unsigned ntri, cudaStream_t s);
 int reduction_d3(const double* in, unsigned n, double out[3], void* scratch, cudaStream_t s);

@@ -205,6 +205,7 @@ struct MixedScene {
     unsigned long long* hoverflow = nullptr;
     unsigned passes = 0;          // radix passes of one re-binning
     bool use_graphs = true;
+    bool kinematic = false;   // bodies moved by their own vel and omega every step
     unsigned rec_cap_alloc = 0;
     xd_scene_desc desc;
     std::vector<xd_plane_info> host_planes;
@@ -2120,10 +2121,22 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
 {
     const unsigned n = s->n;
     const Master& M = s->m[0];
+    int st = XD_OK;
+    if (s->kinematic && s->ntri && MODE != 3) {
+        // prescribed body motion: pose, triangles, and the re-binning flag
+        // once a vertex has moved half the skin since the last build
+        st = launch_body_advance(s->pmi, s->nbodies, s->P.dt, q);
+        if (st == XD_OK) st = launch_update_polygon(s->pmi, s->vlist_body, s->sphere, s->poly, s->ntri, q);
+        if (st == XD_OK) {
+            k_tri_moved<<<blocks(s->ntri, 256), 256, 0, q>>>(s->P, s->poly, s->tri_ref, s->counters);
+            st = launch_status("mixed mesh moved");
+        }
+        if (st != XD_OK) return st;
+    }
     ph.begin(0, q);
     k_mx_advance<MODE><<<blocks(n, 256), 256, 0, q>>>(s->P, M, s->Fc, s->Mc, s->pref, s->pf, s->qa, s->qb,
                                                       s->counters, cond ? *cond : 0, cond ? 1 : 0);
-    int st = launch_status("mixed advance");
+    st = launch_status("mixed advance");
     ph.end(0, q);
     if (st != XD_OK) return st;
     ph.begin(2, q);
@@ -2274,7 +2287,7 @@ unsigned long long mixed_launches(MixedScene* s, unsigned nsteps)
     if (!s || nsteps == 0 || s->n == 0) return 0;
     // per step: advance + contact; + the last velocity update; a step that
     // re-bins adds mixed_rebuild_launches()
-    const unsigned long long per = 2;
+    const unsigned long long per = 2 + (s->kinematic && s->ntri ? 3 : 0);
     unsigned long long total = per * nsteps + 1 + (s->nbodies ? 1 : 0);
     if (!s->cells_clean) total += mixed_rebuild_launches(s);   // the first step re-bins
     return total;
@@ -2401,6 +2414,19 @@ static int reset_history(MixedScene* s, cudaStream_t q)
     if (st == XD_OK) st = cuda_status(cudaMemsetAsync(s->hdelta, 0, sizeof(double) * 3 * e, q), "mixed history");
     if (st == XD_OK) st = cuda_status(cudaMemsetAsync(s->hoverflow, 0, sizeof(unsigned long long), q), "mixed history");
     return st;
+}
+
+int mixed_set_kinematic(MixedScene* s, bool enable)
+{
+    if (enable && !s->desc.ntri) return set_error(XD_ERR_STATE, "scene_set_kinematic_bodies: no polygon bodies");
+    if (enable != s->kinematic)
+        for (int k = 0; k < 5; ++k)   // the step graphs hold the step's launches
+            if (s->graph[k]) {
+                cudaGraphExecDestroy(s->graph[k]);
+                s->graph[k] = nullptr;
+            }
+    s->kinematic = enable;
+    return XD_OK;
 }
 
 int mixed_set_history(MixedScene* s, unsigned slots)

@@ -34,6 +34,7 @@ int mixed_pair_list(MixedScene* s, unsigned cap_per_particle, unsigned* counts, 
 int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q);
 unsigned long long mixed_device_bytes(MixedScene* s);
 int mixed_set_history(MixedScene* s, unsigned slots);
+int mixed_set_kinematic(MixedScene* s, bool enable);
 int mixed_download_history(MixedScene* s, unsigned* keys, double* delta, unsigned long long* overflow,
                            cudaStream_t q);
 int mixed_set_bodies(MixedScene* s, const xd_polygon_mass_info* pmi, cudaStream_t q);

@@ -37,6 +37,7 @@ struct xd_scene {
     size_t scratch_bytes = 0;
     void* poly_scratch = nullptr;
     bool bodies_dirty = false;
+    bool kinematic = false;   // bodies moved by their own vel and omega every step
     std::vector<void*> allocs;
     unsigned long long bytes = 0;   // device memory held by the FP64 form
     // phase timing
@@ -574,6 +575,9 @@ unsigned long long xd_scene_launches(xd_scene* s, unsigned nsteps)
     unsigned long long total = per * nsteps;
     if (s->bodies_dirty && s->ntri) total += 1;   // mesh update
     total += 1;                                   // first VV position
+    // kinematic bodies: pose and mesh before every step; the step boundary
+    // is then velocity and position as two launches
+    if (s->kinematic && s->ntri) total += 2ull * nsteps + (nsteps - 1);
     return total;
 }
 
@@ -597,6 +601,14 @@ int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
         if (st != XD_OK) return st;
         s->bodies_dirty = false;
     }
+    const bool kin = s->kinematic && s->ntri;
+    auto move_bodies = [&]() {
+        int r = launch_body_advance(s->pmi, s->nbodies, P.dt, q);
+        if (r == XD_OK) r = launch_update_polygon(s->pmi, s->vlist, s->sphere, s->poly, s->ntri, q);
+        return r;
+    };
+    if (kin) st = move_bodies();
+    if (st != XD_OK) return st;
     // VV position of the first step (later ones are fused into the velocity pass)
     {
         PhaseSpan ps(s, 0, q);
@@ -632,12 +644,16 @@ int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
         }
         if (st == XD_OK) {
             PhaseSpan ps(s, 0, q);
-            if (t + 1 < nsteps)
+            if (t + 1 < nsteps && !kin) {
                 st = launch_vv_velocity_position(P, s->pos, s->vel, s->acc, s->omega, s->alpha,
                                                  s->force, s->moment, s->mass, s->inertia, np, q);
-            else
+            } else {
                 st = launch_vv_velocity(P, s->vel, s->acc, s->omega, s->alpha, s->force, s->moment,
                                         s->mass, s->inertia, np, q);
+                // moving bodies come before the next step's position update
+                if (st == XD_OK && t + 1 < nsteps) st = move_bodies();
+                if (st == XD_OK && t + 1 < nsteps) st = launch_vv_position(P, s->pos, s->vel, s->acc, np, q);
+            }
         }
         if (st != XD_OK) return st;
     }
@@ -648,6 +664,15 @@ int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
         if (e != cudaSuccess) return cuda_status(e, "scene_step check");
         if (herr) return set_error(XD_ERR_INVALID, "scene_step: a hash value was >= ncell");
     }
+    return XD_OK;
+}
+
+int xd_scene_set_kinematic_bodies(xd_scene* s, int enable)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_set_kinematic_bodies: null scene");
+    if (s->mixed) return mixed_set_kinematic(s->mixed, enable != 0);
+    if (enable && !s->nbodies) return set_error(XD_ERR_STATE, "scene_set_kinematic_bodies: no polygon bodies");
+    s->kinematic = enable != 0;
     return XD_OK;
 }
 

@@ -167,6 +167,11 @@ class DeviceScene:
     def launches(self, nsteps: int) -> int:
         return int(_lib.lib().xd_scene_launches(self.handle, nsteps))
 
+    def set_kinematic_bodies(self, enable: bool = True):
+        """Move the polygon bodies by their own vel and omega every step, on the
+        device (xd_scene_set_kinematic_bodies)."""
+        call("xd_scene_set_kinematic_bodies", self.handle, 1 if enable else 0)
+
     def set_tangential_history(self, slots: int = 12):
         """Tangential springs kept per contact (xd_scene_set_tangential_history);
         0 restores the reference's DHS model."""

@@ -47,7 +47,7 @@ class _Scene(C.Structure):
         ("hash", _vp), ("index", _vp), ("sorted", _vp), ("cstart", _vp), ("cend", _vp),
         ("cp_pp", _vp), ("nplanes", _u), ("planes", _vp), ("cp_planes", _vp),
         ("ntri", _u), ("poly", _vp), ("sphere", _vp), ("pmi", _vp), ("cp_poly", _vp),
-        ("hist", _vp),
+        ("hist", _vp), ("kinematic", C.c_int), ("nbodies", _u), ("vlist", _vp),
     ]
 
 
@@ -163,6 +163,9 @@ class Oracle:
                                                 _p(mass), _p(sorted_), _p(cstart), _p(cend),
                                                 _p(cp), _u(pos.shape[0]))
 
+    def advance_bodies(self, pmi, dt):
+        self.lib.xdo_advance_bodies(_p(pmi), _u(pmi.shape[0]), C.c_double(dt))
+
     def update_polygon(self, pmi, vlist, sphere, poly):
         self.lib.xdo_update_polygon_object_data(_p(pmi), _p(vlist), _p(sphere), _p(poly),
                                                 _u(poly.shape[0]))
@@ -215,6 +218,8 @@ class Oracle:
         if sc.ntri:
             s.poly, s.sphere = sc.poly.ctypes.data, sc.sphere.ctypes.data
             s.pmi, s.cp_poly = sc.pmi.ctypes.data, sc.cp_poly.ctypes.data
+            s.nbodies = sc.pmi.shape[0]
+            s.vlist = sc.vlist.ctypes.data
         return s
 
     @staticmethod
@@ -224,9 +229,12 @@ class Oracle:
                 "sorted": np.zeros(n, np.uint32), "cstart": np.zeros(sc.ncell, np.uint32),
                 "cend": np.zeros(sc.ncell, np.uint32)}
 
-    def run(self, sc, nsteps: int, cpu_path: bool = False, history: "History" = None):
+    def run(self, sc, nsteps: int, cpu_path: bool = False, history: "History" = None,
+            kinematic: bool = False):
         """Advance ``sc`` (in place) by nsteps whole steps; returns the grid work
-        arrays.  With ``history`` the contacts keep tangential springs."""
+        arrays.  With ``history`` the contacts keep tangential springs; with
+        ``kinematic`` the polygon bodies move by their own vel and omega each
+        step (xdo_advance_bodies)."""
         for a in ("pos", "vel", "acc", "omega", "alpha", "force", "moment", "mass", "inertia"):
             assert getattr(sc, a).flags["C_CONTIGUOUS"]
         work = self._work(sc)
@@ -234,6 +242,10 @@ class Oracle:
         if history is not None:
             assert not cpu_path
             s.hist = C.addressof(history.c)
+        if kinematic:
+            assert not cpu_path and sc.ntri
+            assert sc.vlist.flags["C_CONTIGUOUS"]
+            s.kinematic = 1
         fn = self.lib.xdo_cpu_run_steps if cpu_path else self.lib.xdo_run_steps
         fn(C.byref(s), _u(nsteps))
         return work

@@ -902,6 +902,33 @@ void xdo_hist_polygon(const xdo_params* prm, const xdo_polygon* dpi, xdo_polygon
     }
 }
 
+/* ------------------------------------------------------ kinematic bodies */
+
+void xdo_advance_bodies(xdo_polygon_mass* pmi, unsigned nbodies, double dt)
+{
+    for (unsigned b = 0; b < nbodies; ++b) {
+        xdo_polygon_mass* m = pmi + b;
+        for (int a = 0; a < 3; ++a) m->origin[a] = m->origin[a] + dt * m->vel[a];
+        double wx = m->omega[0], wy = m->omega[1], wz = m->omega[2];
+        double w = sqrt(wx * wx + wy * wy + wz * wz);
+        if (w > 0.0) {
+            double h = 0.5 * w * dt;
+            double c = cos(h), sn = sin(h) / w;
+            double a0 = c, a1 = sn * wx, a2 = sn * wy, a3 = sn * wz;
+            double p0 = m->ep[0], p1 = m->ep[1], p2 = m->ep[2], p3 = m->ep[3];
+            double r0 = a0 * p0 - (a1 * p1 + a2 * p2 + a3 * p3);
+            double r1 = a0 * p1 + p0 * a1 + (a2 * p3 - a3 * p2);
+            double r2 = a0 * p2 + p0 * a2 + (a3 * p1 - a1 * p3);
+            double r3 = a0 * p3 + p0 * a3 + (a1 * p2 - a2 * p1);
+            double nr = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + r3 * r3);
+            m->ep[0] = r0 / nr;
+            m->ep[1] = r1 / nr;
+            m->ep[2] = r2 / nr;
+            m->ep[3] = r3 / nr;
+        }
+    }
+}
+
 /* ------------------------------------------------------------ whole step */
 
 /* dem_simulation::oneStepAnalysis (dem_simulation.cpp:447-469) with
@@ -913,6 +940,10 @@ void xdo_step(xdo_scene* s)
     xdo_params* prm = &s->prm;
     unsigned np = s->np;
     unsigned n = np + s->ntri;
+    if (s->kinematic && s->ntri) {
+        xdo_advance_bodies(s->pmi, s->nbodies, prm->dt);
+        xdo_update_polygon_object_data(s->pmi, s->vlist, s->sphere, s->poly, s->ntri);
+    }
     xdo_vv_update_position(prm, s->pos, s->vel, s->acc, np);
     xdo_calculate_hash_and_index(prm, s->hash, s->index, s->pos, np);
     if (s->ntri)

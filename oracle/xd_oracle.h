@@ -195,7 +195,20 @@ typedef struct xdo_scene {
     xdo_polygon_mass* pmi;
     const xdo_contact_property* cp_poly; /* one per polygon object */
     xdo_history* hist;                   /* NULL: the reference's DHS, no history */
+    /* kinematic bodies (an extension): when set, each step first moves every
+     * polygon body by its own vel and omega over dt (xdo_advance_bodies) and
+     * the triangles with it (xdo_update_polygon_object_data) */
+    int kinematic;
+    unsigned nbodies;
+    const double* vlist;                 /* body-frame vertices [ntri][9] */
 } xdo_scene;
+
+/* One step of prescribed body motion: origin += dt vel; the Euler parameters
+ * (e0 scalar) turned by the rotation of angle |omega| dt about omega,
+ * p <- q (x) p with q = (cos(|omega| dt / 2), sin(|omega| dt / 2) omega / |omega|),
+ * then normalised.  An extension: the reference moves bodies through its
+ * multibody solver on the host. */
+void xdo_advance_bodies(xdo_polygon_mass* pmi, unsigned nbodies, double dt);
 
 void xdo_step(xdo_scene* s);
 void xdo_run_steps(xdo_scene* s, unsigned nsteps);

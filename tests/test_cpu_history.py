@@ -181,3 +181,37 @@ def test_full_table_falls_back_to_fresh_springs(oracle):
                         so, cs, ce, cp, hist)
     assert hist.overflow == 3      # particle 0's second contact, each step
     assert len(hist.contacts(0)) == 1
+
+
+def test_kinematic_body_turns_and_moves_as_prescribed(oracle):
+    """Prescribed body motion (an extension): after n steps at omega about y
+    and velocity v, the Euler parameters are those of the rotation by
+    omega n dt about y, and the origin has moved by v n dt."""
+    from metakonga_gb300.layouts import POLYGON_MASS
+    pmi = np.zeros(1, dtype=POLYGON_MASS)
+    pmi["ep"] = (1.0, 0.0, 0.0, 0.0)
+    pmi["omega"] = (0.0, 2.0, 0.0)
+    pmi["vel"] = (0.01, 0.0, -0.02)
+    dt, n = 5e-6, 4000
+    for _ in range(n):
+        oracle.advance_bodies(pmi, dt)
+    th = 2.0 * n * dt
+    assert np.allclose(pmi["ep"][0], (math.cos(th / 2), 0.0, math.sin(th / 2), 0.0), atol=1e-12)
+    assert np.allclose(pmi["origin"][0], (0.01 * n * dt, 0.0, -0.02 * n * dt), atol=1e-15)
+    assert abs(np.linalg.norm(pmi["ep"][0]) - 1.0) < 1e-15
+
+
+def test_kinematic_drum_moves_its_mesh(oracle):
+    """With kinematic bodies the oracle moves the triangles every step: a
+    vertex of the drum turns about the axis by omega n dt."""
+    from .cases import small_drum
+    sc = small_drum()
+    sc.pmi["vel"] = 0.0
+    sc.pmi["omega"] = (0.0, 3.0, 0.0)
+    p0 = sc.poly["P"][0].copy()
+    oracle.run(sc, 10, kinematic=True)
+    th = 3.0 * 10 * sc.dt
+    # rotation about y by th: x' = x cos + z sin, z' = -x sin + z cos
+    x, y, z = p0
+    want = (x * math.cos(th) + z * math.sin(th), y, -x * math.sin(th) + z * math.cos(th))
+    assert np.allclose(sc.poly["P"][0], want, atol=1e-12)
