@@ -502,6 +502,28 @@ int xd_scene_rebuilds(xd_scene* scene, unsigned long long* count, unsigned long 
  * re-bins when a vertex has moved half the skin. */
 int xd_scene_set_kinematic_bodies(xd_scene* scene, int enable);
 
+/* Particle emitter: the reference's real-time particle creation
+ * (dem_simulation.cpp:210-222 and :321-322 set it up with no particle yet,
+ * :449-450 adds a group before a step; particleManager.cpp:132-145 hands out
+ * the groups made by its plane and circle creators, or one particle at a
+ * time).  The scene's particles are all uploaded (staged at their creation
+ * positions); only the first `active` take part in a step -- the cell grid,
+ * every contact, velocity-Verlet, and the triangle offset in the grid.  Before
+ * the k-th step after this call (k from 1), when period > 0,
+ * (k - 1) % period == 0 and particles remain, the next of the `ngroups` group
+ * sizes joins (one particle when ngroups is 0), up to the particle count.  An
+ * emitted particle starts from its uploaded state.  period = 0 with active =
+ * np turns the emitter off.  Deliberate difference: the reference keeps the
+ * parameter block's np at the total, so until every particle is out its
+ * polygon kernel reads the triangles' grid entries (active + t) as particles
+ * or as the wrong triangle; here the triangles take part from the first step.
+ * Downloads return every particle, the staged ones unchanged;
+ * xd_scene_eval_contacts gives them zero rows. */
+int xd_scene_set_emitter(xd_scene* scene, unsigned active, unsigned period, const unsigned* groups,
+                         unsigned ngroups, void* stream);
+/* The particles that take part in the next step (before its emission). */
+int xd_scene_active(xd_scene* scene, unsigned* active);
+
 /* Tangential-spring history, an extension: the reference's DHSModel
  * (mphysics_cuda_impl.cuh:379-401) keeps no state between steps.  With
  * slots > 0 (at most 32) every particle keeps up to `slots` contacts keyed

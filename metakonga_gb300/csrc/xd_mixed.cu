@@ -133,7 +133,11 @@ struct MixParams {
 }  // namespace
 
 struct MixedScene {
-    unsigned n = 0, nplanes = 0, ncell = 0;
+    // n: the particles that take part in a step (P.n); cap: the particles
+    // held.  They differ only under an emitter: slots [n, cap) then hold the
+    // particles not yet emitted, in id order (no re-binning touches them).
+    unsigned n = 0, cap = 0, nplanes = 0, ncell = 0;
+    unsigned active_req = ~0u;    // active count set before the first upload
     int gx = 0, gy = 0, gz = 0;
     double cs = 0.0;
     MixParams P;
@@ -1567,6 +1571,7 @@ __global__ void __launch_bounds__(256) k_mx_ids(MixParams P, Master M, unsigned*
 static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_host)
 {
     s->n = d.np;
+    s->cap = d.np;
     s->nplanes = d.nplanes;
     if (d.np >= 0x7fffffffu) return set_error(XD_ERR_CAPACITY, "mixed mode: too many particles");
     // grid from the bounding box of particles and walls
@@ -1857,7 +1862,7 @@ void mixed_destroy(MixedScene* s)
 static int ensure_xfer(MixedScene* s)
 {
     if (s->xfer) return XD_OK;
-    return alloc(s, &s->xfer, (size_t)s->n * (4 + 3 * 6 + 2));
+    return alloc(s, &s->xfer, (size_t)s->cap * (4 + 3 * 6 + 2));
 }
 
 static int reset_history(MixedScene* s, cudaStream_t q);
@@ -1872,10 +1877,15 @@ int mixed_upload(MixedScene* s, const double* pos, const double* vel, const doub
         int r = mixed_setup(s, s->desc, pos);
         if (r != XD_OK) return r;
         s->ready = true;
+        if (s->active_req != ~0u) {   // an emitter set before the first upload
+            s->n = s->active_req;
+            s->P.n = s->active_req;
+            s->active_req = ~0u;
+        }
     }
     int st = ensure_xfer(s);
     if (st != XD_OK) return st;
-    size_t n = s->n;
+    size_t n = s->cap;   // every held particle, emitted or not
     double* b = s->xfer;
     double *dpos = b, *dvel = b + 4 * n, *dacc = dvel + 3 * n, *dom = dacc + 3 * n,
            *dal = dom + 3 * n, *dm = dal + 3 * n, *dI = dm + n;
@@ -1895,13 +1905,15 @@ int mixed_upload(MixedScene* s, const double* pos, const double* vel, const doub
     s->cells_clean = false;   // the state is in upload order again: the next step re-bins
     st = reset_history(s, q);   // an uploaded state starts with no springs
     if (st == XD_OK && s->nbodies)   // nor unflushed body reactions
-        st = cuda_status(cudaMemsetAsync(s->rxn, 0, sizeof(double) * 6 * s->nbodies * (size_t)s->n, q),
+        st = cuda_status(cudaMemsetAsync(s->rxn, 0, sizeof(double) * 6 * s->nbodies * (size_t)s->cap, q),
                          "mixed upload");
     if (st != XD_OK) return st;
     st = cuda_status(cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * CN_DECISIONS, q), "mixed upload");
     if (st != XD_OK) return st;
-    k_mx_load<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[0], dpos, dvel, dacc, dom, dal, dm, dI,
-                                                s->mass0, s->pf, s->qa, s->qb);
+    MixParams Pc = s->P;
+    Pc.n = s->cap;
+    k_mx_load<<<blocks(s->cap, 256), 256, 0, q>>>(Pc, s->m[0], dpos, dvel, dacc, dom, dal, dm, dI,
+                                                  s->mass0, s->pf, s->qa, s->qb);
     st = launch_status("mixed upload");
     if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "mixed upload");
     return st;
@@ -1913,13 +1925,15 @@ int mixed_download(MixedScene* s, double* pos, double* vel, double* acc, double*
     if (!s->ready) return set_error(XD_ERR_STATE, "mixed mode: no state uploaded");
     int st = ensure_xfer(s);
     if (st != XD_OK) return st;
-    size_t n = s->n;
+    size_t n = s->cap;
     double* b = s->xfer;
     double *dpos = b, *dvel = b + 4 * n, *dacc = dvel + 3 * n, *dom = dacc + 3 * n,
            *dal = dom + 3 * n, *df = dal + 3 * n, *dmo = df + 3 * n;
     // xfer holds 4n + 18n + 2n doubles: pos, vel, acc, omega, alpha, force, moment fit in 22n
-    k_mx_store<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->mass0, dpos, dvel, dacc, dom,
-                                                 dal, df, dmo);
+    MixParams Pc = s->P;
+    Pc.n = s->cap;
+    k_mx_store<<<blocks(s->cap, 256), 256, 0, q>>>(Pc, s->m[s->cur], s->mass0, dpos, dvel, dacc, dom,
+                                                   dal, df, dmo);
     st = launch_status("mixed download");
     auto cp = [&](double* h, const double* d, size_t cnt) {
         if (st == XD_OK && h)
@@ -1945,14 +1959,15 @@ static HistTable history_table(MixedScene* s)
     h.key = s->hkey;
     h.delta = s->hdelta;
     h.slots = s->hslots;
-    h.n = s->n;
+    h.n = s->cap;   // row stride: the tables hold every particle
     h.overflow = s->hoverflow;
     return h;
 }
 
 // Re-binning with history: the tables follow their particles (new slot i
 // takes old slot perm[i]); the partner keys are original indices and stay.
-__global__ void __launch_bounds__(256) k_hist_permute(unsigned n, unsigned slots, const unsigned* __restrict__ perm,
+__global__ void __launch_bounds__(256) k_hist_permute(unsigned n, unsigned stride, unsigned slots,
+                                                      const unsigned* __restrict__ perm,
                                                       const unsigned* __restrict__ key, const double* __restrict__ delta,
                                                       unsigned* __restrict__ key2, double* __restrict__ delta2)
 {
@@ -1960,7 +1975,7 @@ __global__ void __launch_bounds__(256) k_hist_permute(unsigned n, unsigned slots
     if (i >= n) return;
     const unsigned o = __ldg(perm + i);
     for (unsigned s = 0; s < slots; ++s) {
-        const size_t a = (size_t)s * n + i, b = (size_t)s * n + o;
+        const size_t a = (size_t)s * stride + i, b = (size_t)s * stride + o;
         key2[a] = __ldg(key + b);
         delta2[3 * a + 0] = __ldg(delta + 3 * b + 0);
         delta2[3 * a + 1] = __ldg(delta + 3 * b + 1);
@@ -1968,11 +1983,15 @@ __global__ void __launch_bounds__(256) k_hist_permute(unsigned n, unsigned slots
     }
 }
 
-__global__ void __launch_bounds__(256) k_hist_copy(size_t e, const unsigned* __restrict__ key2,
+// Rows [0, n) of every slot's table (row stride `stride`) back from key2/delta2.
+__global__ void __launch_bounds__(256) k_hist_copy(unsigned n, unsigned stride, unsigned slots,
+                                                   const unsigned* __restrict__ key2,
                                                    const double* __restrict__ delta2, unsigned* __restrict__ key,
                                                    double* __restrict__ delta)
 {
-    for (size_t a = (size_t)blockIdx.x * blockDim.x + threadIdx.x; a < e; a += (size_t)gridDim.x * blockDim.x) {
+    const size_t e = (size_t)slots * n;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < e; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t a = (t / n) * stride + t % n;
         key[a] = key2[a];
         delta[3 * a + 0] = delta2[3 * a + 0];
         delta[3 * a + 1] = delta2[3 * a + 1];
@@ -2002,6 +2021,48 @@ __global__ void __launch_bounds__(256) k_hist_gather(unsigned n, unsigned slots,
 // The reactions accumulated in the per-particle slots since the last flush
 // go to the bodies (the slots belong to particle slots, which a re-binning
 // reorders).
+// The tables of slots [0, n) follow the permutation (new slot -> old slot).
+static int permute_history(MixedScene* s, unsigned n, const unsigned* perm, cudaStream_t q)
+{
+    k_hist_permute<<<blocks(n, 256), 256, 0, q>>>(n, s->cap, s->hslots, perm, s->hkey, s->hdelta, s->hkey2,
+                                                  s->hdelta2);
+    int st = launch_status("mixed history re-binning");
+    if (st != XD_OK) return st;
+    const size_t e = (size_t)s->hslots * n;
+    k_hist_copy<<<(unsigned)std::min<size_t>((e + 255) / 256, 152 * 16), 256, 0, q>>>(n, s->cap, s->hslots, s->hkey2,
+                                                                                     s->hdelta2, s->hkey, s->hdelta);
+    return launch_status("mixed history re-binning");
+}
+
+// inv[id of slot i] = i over all held slots: the permutation back to id order.
+__global__ void __launch_bounds__(256) k_mx_inverse(unsigned cap, Master M, unsigned* __restrict__ inv)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    inv[__float_as_uint(M.wl[i].w)] = i;
+}
+
+static int flush_reactions(MixedScene* s, cudaStream_t q);
+
+// Every held particle back to slot = id (the order an upload leaves), with
+// its history rows; the cells must be re-binned afterwards.
+static int restore_id_order(MixedScene* s, cudaStream_t q)
+{
+    const unsigned cap = s->cap;
+    if (!cap) return XD_OK;
+    int st = flush_reactions(s, q);   // the reaction slots belong to the old order
+    if (st != XD_OK) return st;
+    MixParams Pc = s->P;
+    Pc.n = cap;
+    k_mx_inverse<<<blocks(cap, 256), 256, 0, q>>>(cap, s->m[0], s->vals);
+    k_mx_permute<<<blocks(cap, 256), 256, 0, q>>>(Pc, s->m[0], s->m[1], s->vals);
+    k_mx_copyback<<<blocks(cap, 256), 256, 0, q>>>(Pc, s->m[1], s->m[0], s->pf, s->qa, s->qb);
+    st = launch_status("mixed id order");
+    if (st == XD_OK && s->hslots) st = permute_history(s, cap, s->vals, q);
+    s->cells_clean = false;
+    return st;
+}
+
 static int flush_reactions(MixedScene* s, cudaStream_t q)
 {
     if (!s->nbodies || !s->n) return XD_OK;
@@ -2025,13 +2086,7 @@ static int rebuild(MixedScene* s, cudaStream_t q)
     k_mx_permute<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[0], s->m[1], sv);
     k_mx_copyback<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[1], s->m[0], s->pf, s->qa, s->qb);
     if (s->hslots) {
-        k_hist_permute<<<blocks(n, 256), 256, 0, q>>>(n, s->hslots, sv, s->hkey, s->hdelta, s->hkey2, s->hdelta2);
-        st = launch_status("mixed history re-binning");
-        if (st != XD_OK) return st;
-        const size_t e = (size_t)s->hslots * n;
-        k_hist_copy<<<(unsigned)std::min<size_t>((e + 255) / 256, 152 * 16), 256, 0, q>>>(e, s->hkey2, s->hdelta2,
-                                                                                         s->hkey, s->hdelta);
-        st = launch_status("mixed history re-binning");
+        st = permute_history(s, n, sv, q);
         if (st != XD_OK) return st;
     }
     k_lb_fill<<<blocks(n + 1, 256), 256, 0, q>>>(sk, n, s->ncell, s->lb, s->prev_keys, s->gaps, s->counters);
@@ -2200,6 +2255,17 @@ enum { kFirstStep = 0, kSteps1 = 1, kSteps2 = 2, kSteps4 = 3, kSteps8 = 4, kGrap
 
 static unsigned graph_steps(int kind) { return kind == kFirstStep ? 1u : 1u << (kind - 1); }
 
+constexpr unsigned kGraphMinSteps = 16;
+
+static void destroy_graphs(MixedScene* s)
+{
+    for (int k = 0; k < kGraphKinds; ++k)
+        if (s->graph[k]) {
+            cudaGraphExecDestroy(s->graph[k]);
+            s->graph[k] = nullptr;
+        }
+}
+
 static int capture_steps(MixedScene* s, int kind)
 {
     cudaStream_t cs = nullptr;
@@ -2242,11 +2308,27 @@ static int launch_steps(MixedScene* s, int kind, cudaStream_t q)
 
 int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
 {
-    if (nsteps == 0 || s->n == 0) return XD_OK;
+    if (nsteps == 0) return XD_OK;
     if (!s->ready) return set_error(XD_ERR_STATE, "mixed mode: no state uploaded");
+    if (s->n == 0) {
+        // no particle emitted yet: only the prescribed body motion; the
+        // emission that follows re-bins, triangles included
+        if (!s->kinematic || !s->ntri) return XD_OK;
+        int st = XD_OK;
+        for (unsigned t = 0; t < nsteps && st == XD_OK; ++t) {
+            st = launch_body_advance(s->pmi, s->nbodies, s->P.dt, q);
+            if (st == XD_OK) st = launch_update_polygon(s->pmi, s->vlist_body, s->sphere, s->poly, s->ntri, q);
+        }
+        s->cells_clean = false;
+        return st;
+    }
     int st = update_mesh(s, q);
     if (st != XD_OK) return st;
-    if (s->use_graphs && ph.fn == nullptr) {
+    // graphs pay for their capture over many steps: a short call on a scene
+    // whose graphs are not captured (an emission just changed its particle
+    // count) launches directly
+    const bool graphs = s->use_graphs && ph.fn == nullptr && (s->graph[kFirstStep] || nsteps >= kGraphMinSteps);
+    if (graphs) {
         // Every step in a graph, re-binning decided on the device: the call
         // never waits for the GPU.  A scene without cells yet (after an
         // upload) is made to re-bin through the same flag.
@@ -2318,6 +2400,7 @@ int mixed_rebuilds(MixedScene* s, unsigned long long* out, cudaStream_t q)
 // if needed, and the gather without an update.
 static int current_contacts(MixedScene* s, cudaStream_t q, bool record, unsigned rec_cap)
 {
+    if (!s->n) return XD_OK;   // nothing emitted yet
     Phases none;
     int st = update_mesh(s, q);
     if (st != XD_OK) return st;
@@ -2330,10 +2413,15 @@ int mixed_eval_contacts(MixedScene* s, double* force, double* moment, cudaStream
     int st = ensure_xfer(s);
     if (st == XD_OK) st = current_contacts(s, q, false, 0);
     if (st != XD_OK) return st;
-    size_t n = s->n;
+    size_t n = s->cap;
     double *df = s->xfer, *dm = s->xfer + 3 * n;
-    k_mx_store_forces<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc, df, dm);
-    st = launch_status("mixed store forces");
+    if (s->n < s->cap)   // particles not emitted yet: zero rows
+        st = cuda_status(cudaMemsetAsync(df, 0, sizeof(double) * 6 * n, q), "eval");
+    if (st != XD_OK) return st;
+    if (s->n) {
+        k_mx_store_forces<<<blocks(s->n, 256), 256, 0, q>>>(s->P, s->m[s->cur], s->Fc, s->Mc, df, dm);
+        st = launch_status("mixed store forces");
+    }
     if (st == XD_OK && force)
         st = cuda_status(cudaMemcpyAsync(force, df, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, q), "eval");
     if (st == XD_OK && moment)
@@ -2348,9 +2436,9 @@ int mixed_pair_list(MixedScene* s, unsigned cap_per_particle, unsigned* counts, 
     if (cap_per_particle == 0) return set_error(XD_ERR_INVALID, "pair list: zero capacity");
     if (!s->ready) return set_error(XD_ERR_STATE, "mixed mode: no state uploaded");
     int st = XD_OK;
-    if (!s->rec_count) st = alloc(s, &s->rec_count, s->n);
+    if (!s->rec_count) st = alloc(s, &s->rec_count, s->cap);
     if (st == XD_OK && s->rec_cap_alloc < cap_per_particle) {
-        st = alloc(s, &s->rec_pairs, (size_t)s->n * cap_per_particle);
+        st = alloc(s, &s->rec_pairs, (size_t)s->cap * cap_per_particle);
         s->rec_cap_alloc = cap_per_particle;
     }
     if (st == XD_OK) st = current_contacts(s, q, true, cap_per_particle);
@@ -2366,6 +2454,7 @@ int mixed_pair_list(MixedScene* s, unsigned cap_per_particle, unsigned* counts, 
         st = cuda_status(cudaMemcpyAsync(part.data(), s->rec_pairs, 4 * n * cap_per_particle, cudaMemcpyDeviceToHost, q), "pairs");
     if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "pairs");
     if (st != XD_OK) return st;
+    for (size_t o = n; o < s->cap; ++o) counts[o] = 0;   // not emitted yet
     for (size_t i = 0; i < n; ++i) {
         unsigned o = ids[i];
         counts[o] = cnt[i];
@@ -2416,15 +2505,31 @@ static int reset_history(MixedScene* s, cudaStream_t q)
     return st;
 }
 
+int mixed_set_active(MixedScene* s, unsigned active, bool restore, cudaStream_t q)
+{
+    if (active > s->desc.np) return set_error(XD_ERR_INVALID, "scene emitter: active count above the particle count");
+    if (!s->ready) {   // applied by the first upload
+        s->active_req = active;
+        return XD_OK;
+    }
+    int st = restore ? restore_id_order(s, q) : flush_reactions(s, q);
+    if (st != XD_OK || active == s->n) return st;
+    s->n = active;
+    s->P.n = active;
+    s->cells_clean = false;
+    // the step graphs hold the particle count: replaced once the launches
+    // queued from them have run
+    if (s->graph[kFirstStep]) st = cuda_status(cudaStreamSynchronize(q), "scene emitter");
+    destroy_graphs(s);
+    return st;
+}
+
+unsigned mixed_active(MixedScene* s) { return s->ready ? s->n : (s->active_req != ~0u ? s->active_req : s->desc.np); }
+
 int mixed_set_kinematic(MixedScene* s, bool enable)
 {
     if (enable && !s->desc.ntri) return set_error(XD_ERR_STATE, "scene_set_kinematic_bodies: no polygon bodies");
-    if (enable != s->kinematic)
-        for (int k = 0; k < 5; ++k)   // the step graphs hold the step's launches
-            if (s->graph[k]) {
-                cudaGraphExecDestroy(s->graph[k]);
-                s->graph[k] = nullptr;
-            }
+    if (enable != s->kinematic) destroy_graphs(s);   // the step graphs hold the step's launches
     s->kinematic = enable;
     return XD_OK;
 }
@@ -2436,12 +2541,7 @@ int mixed_set_history(MixedScene* s, unsigned slots)
         if (st == XD_OK) st = cuda_status(cudaDeviceSynchronize(), "mixed history");
         return st;
     }
-    // the step graphs hold the table pointers: capture them again
-    for (int k = 0; k < 5; ++k)
-        if (s->graph[k]) {
-            cudaGraphExecDestroy(s->graph[k]);
-            s->graph[k] = nullptr;
-        }
+    destroy_graphs(s);   // the step graphs hold the table pointers: capture them again
     s->hslots = 0;
     const unsigned n = s->desc.np;   // the particle count (set before the first upload too)
     if (slots == 0 || n == 0) return XD_OK;
@@ -2465,13 +2565,13 @@ int mixed_download_history(MixedScene* s, unsigned* keys, double* delta, unsigne
 {
     if (!s->hslots) return set_error(XD_ERR_STATE, "scene_download_history: history is off");
     if (!s->ready) return set_error(XD_ERR_STATE, "mixed mode: no state uploaded");
-    const size_t e = (size_t)s->hslots * s->n;
+    const size_t e = (size_t)s->hslots * s->cap;
     unsigned* ok = nullptr;
     double* od = nullptr;
     int st = cuda_status(cudaMalloc(&ok, sizeof(unsigned) * e), "scene_download_history");
     if (st == XD_OK) st = cuda_status(cudaMalloc(&od, sizeof(double) * 3 * e), "scene_download_history");
     if (st == XD_OK) {
-        k_hist_gather<<<blocks(s->n, 256), 256, 0, q>>>(s->n, s->hslots, s->m[0], s->hkey, s->hdelta, ok, od);
+        k_hist_gather<<<blocks(s->cap, 256), 256, 0, q>>>(s->cap, s->hslots, s->m[0], s->hkey, s->hdelta, ok, od);
         st = launch_status("scene_download_history");
     }
     if (st == XD_OK && keys)

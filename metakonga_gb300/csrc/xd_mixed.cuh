@@ -35,6 +35,11 @@ int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q);
 unsigned long long mixed_device_bytes(MixedScene* s);
 int mixed_set_history(MixedScene* s, unsigned slots);
 int mixed_set_kinematic(MixedScene* s, bool enable);
+// Emitter support: the particles that take part in a step (slots [active,
+// particle count) keep the staged ones in id order).  restore: first put every
+// particle back in id order (when the emitter is set).
+int mixed_set_active(MixedScene* s, unsigned active, bool restore, cudaStream_t q);
+unsigned mixed_active(MixedScene* s);
 int mixed_download_history(MixedScene* s, unsigned* keys, double* delta, unsigned long long* overflow,
                            cudaStream_t q);
 int mixed_set_bodies(MixedScene* s, const xd_polygon_mass_info* pmi, cudaStream_t q);

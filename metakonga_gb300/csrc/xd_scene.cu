@@ -54,6 +54,12 @@ struct xd_scene {
     unsigned* hist_key = nullptr;
     double* hist_delta = nullptr;
     unsigned long long* hist_overflow = nullptr;
+    // particle emitter: only the first `active` particles take part in a step
+    unsigned active = 0;
+    unsigned emit_period = 0;            // steps between creations; 0: none
+    std::vector<unsigned> emit_groups;   // empty: one particle per creation
+    unsigned emit_next = 0;              // next group to hand out
+    unsigned long long emit_step = 0;    // steps run since the emitter was set
 };
 
 namespace {
@@ -227,6 +233,7 @@ int xd_scene_create(const xd_scene_desc* d, xd_scene** out)
         if (!s) return set_error(XD_ERR_NOMEM, "scene_create: host allocation");
         s->desc = *d;
         s->np = d->np;
+        s->active = d->np;
         s->nplanes = d->nplanes;
         int st = mixed_create(*d, &s->mixed);
         if (st != XD_OK) {
@@ -259,6 +266,7 @@ int xd_scene_create(const xd_scene_desc* d, xd_scene** out)
     s->desc.pmi = nullptr;
     s->desc.cp_poly = nullptr;
     s->np = d->np;
+    s->active = d->np;
     s->ntri = d->ntri;
     s->nbodies = d->ntri ? d->nbodies : 0;
     s->nplanes = d->nplanes;
@@ -452,27 +460,31 @@ int xd_scene_eval_contacts(xd_scene* s, double* force, double* moment, void* str
     if (!s) return set_error(XD_ERR_INVALID, "scene_eval_contacts: null scene");
     cudaStream_t q = static_cast<cudaStream_t>(stream);
     if (s->mixed) return mixed_eval_contacts(s->mixed, force, moment, q);
-    // FP64 mode: contacts added onto zeroed force/moment copies
-    const size_t n = s->np, ng = (size_t)s->np + s->ntri;
+    // FP64 mode: contacts added onto zeroed force/moment copies (rows of
+    // particles not emitted yet stay zero)
+    const size_t n = s->np, na = s->active, ng = na + s->ntri;
     double *f0 = nullptr, *m0 = nullptr;
     int st = cuda_status(cudaMalloc(&f0, sizeof(double) * 6 * (n ? n : 1)), "scene_eval_contacts");
     if (st != XD_OK) return st;
     m0 = f0 + 3 * n;
     auto A = [&](int r) { if (st == XD_OK) st = r; };
     A(cuda_status(cudaMemsetAsync(f0, 0, sizeof(double) * 6 * n, q), "scene_eval_contacts"));
-    const Params& P = s->P;
-    A(launch_hash(P, s->hash, s->index, s->pos, s->np, 0, q));
-    if (s->ntri) A(launch_hash(P, s->hash, s->index, s->sphere, s->ntri, s->np, q));
-    if (st == XD_OK)
-        A(reorder_and_find_cell_start(s->hash, s->index, s->cstart, s->cend, s->sorted, (unsigned)ng,
-                                      s->ncell, s->scratch, q, false));
-    if (st == XD_OK)
-        A(launch_p2p(P, s->pos, s->vel, s->omega, f0, m0, s->mass, s->sorted, s->cstart, s->cend,
-                     s->cp_pp, s->np, q));
-    if (st == XD_OK && s->nplanes)
-        A(launch_planes(P, s->planes, s->cp_planes, 1, s->nplanes, s->pos, s->vel, s->omega, f0, m0,
-                        s->mass, s->np, q));
-    if (st == XD_OK && s->ntri) {
+    Params P = s->P;
+    P.np = (unsigned)na;
+    if (na) {
+        A(launch_hash(P, s->hash, s->index, s->pos, P.np, 0, q));
+        if (s->ntri) A(launch_hash(P, s->hash, s->index, s->sphere, s->ntri, P.np, q));
+        if (st == XD_OK)
+            A(reorder_and_find_cell_start(s->hash, s->index, s->cstart, s->cend, s->sorted, (unsigned)ng,
+                                          s->ncell, s->scratch, q, false));
+        if (st == XD_OK)
+            A(launch_p2p(P, s->pos, s->vel, s->omega, f0, m0, s->mass, s->sorted, s->cstart, s->cend,
+                         s->cp_pp, P.np, q));
+        if (st == XD_OK && s->nplanes)
+            A(launch_planes(P, s->planes, s->cp_planes, 1, s->nplanes, s->pos, s->vel, s->omega, f0, m0,
+                            s->mass, P.np, q));
+    }
+    if (st == XD_OK && s->ntri && na) {
         // the reaction on the bodies is not part of this diagnostic: work on a copy
         xd_polygon_mass_info* tmp = nullptr;
         A(cuda_status(cudaMalloc(&tmp, sizeof(xd_polygon_mass_info) * s->nbodies), "scene_eval_contacts"));
@@ -581,18 +593,14 @@ unsigned long long xd_scene_launches(xd_scene* s, unsigned nsteps)
     return total;
 }
 
-int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
+namespace {
+
+// nsteps whole FP64 steps over the active particles (no emission inside).
+int fp64_steps(xd_scene* s, unsigned nsteps, cudaStream_t q)
 {
-    if (!s) return set_error(XD_ERR_INVALID, "scene_step: null scene");
-    if (nsteps == 0) return XD_OK;
-    cudaStream_t q = static_cast<cudaStream_t>(stream);
-    if (s->mixed) {
-        int r = mixed_step(s->mixed, nsteps, q, phases_of(s));
-        if (r == XD_OK && check) r = cuda_status(cudaStreamSynchronize(q), "scene_step");
-        return r;
-    }
-    const Params& P = s->P;
-    const unsigned np = s->np, ng = s->np + s->ntri;
+    Params P = s->P;
+    P.np = s->active;
+    const unsigned np = s->active, ng = np + s->ntri;
     const HistTable ht = history_of(s);
     const HistTable* hp = s->hist_slots ? &ht : nullptr;
     int st = XD_OK;
@@ -607,6 +615,10 @@ int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
         if (r == XD_OK) r = launch_update_polygon(s->pmi, s->vlist, s->sphere, s->poly, s->ntri, q);
         return r;
     };
+    if (np == 0) {   // nothing emitted yet: only the prescribed body motion
+        for (unsigned t = 0; t < nsteps && kin && st == XD_OK; ++t) st = move_bodies();
+        return st;
+    }
     if (kin) st = move_bodies();
     if (st != XD_OK) return st;
     // VV position of the first step (later ones are fused into the velocity pass)
@@ -657,6 +669,59 @@ int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
         }
         if (st != XD_OK) return st;
     }
+    return XD_OK;
+}
+
+// Emission before the scene's next step, if one is due (particleManager's
+// groups handed out every emit_period steps, dem_simulation.cpp:449-450).
+int emit_before_step(xd_scene* s, cudaStream_t q)
+{
+    const unsigned long long k = s->emit_step + 1;
+    if (!s->emit_period || (k - 1) % s->emit_period != 0 || s->active >= s->np) return XD_OK;
+    unsigned add = 1;
+    if (!s->emit_groups.empty()) add = s->emit_next < s->emit_groups.size() ? s->emit_groups[s->emit_next++] : 0;
+    const unsigned next = add > s->np - s->active ? s->np : s->active + add;
+    if (next == s->active) return XD_OK;
+    s->active = next;
+    return s->mixed ? mixed_set_active(s->mixed, next, false, q) : XD_OK;
+}
+
+// Steps from the scene's next step to the next emission (all of `left` when
+// none can come).
+unsigned steps_to_emission(const xd_scene* s, unsigned left)
+{
+    const bool more = s->emit_period && s->active < s->np &&
+                      (s->emit_groups.empty() || s->emit_next < s->emit_groups.size());
+    if (!more) return left;
+    const unsigned long long k = s->emit_step + 1;   // the next step, 1-based
+    const unsigned long long to = s->emit_period - (k - 1) % s->emit_period;
+    return (unsigned)std::min<unsigned long long>(left, to);
+}
+
+}  // namespace
+
+int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_step: null scene");
+    if (nsteps == 0) return XD_OK;
+    cudaStream_t q = static_cast<cudaStream_t>(stream);
+    // A call is split at the steps that emit particles: each piece ends with
+    // the velocity update of the particles that took part, and the next one
+    // starts with the position update of the grown set, the reference's order.
+    int st = XD_OK;
+    for (unsigned left = nsteps; left && st == XD_OK;) {
+        st = emit_before_step(s, q);
+        if (st != XD_OK) break;
+        const unsigned run = steps_to_emission(s, left);
+        st = s->mixed ? mixed_step(s->mixed, run, q, phases_of(s)) : fp64_steps(s, run, q);
+        s->emit_step += run;
+        left -= run;
+    }
+    if (st != XD_OK) return st;
+    if (s->mixed) {
+        if (check) st = cuda_status(cudaStreamSynchronize(q), "scene_step");
+        return st;
+    }
     if (check) {
         unsigned herr = 0;
         cudaError_t e = cudaMemcpyAsync(&herr, s->scratch, sizeof(unsigned), cudaMemcpyDeviceToHost, q);
@@ -673,6 +738,32 @@ int xd_scene_set_kinematic_bodies(xd_scene* s, int enable)
     if (s->mixed) return mixed_set_kinematic(s->mixed, enable != 0);
     if (enable && !s->nbodies) return set_error(XD_ERR_STATE, "scene_set_kinematic_bodies: no polygon bodies");
     s->kinematic = enable != 0;
+    return XD_OK;
+}
+
+int xd_scene_set_emitter(xd_scene* s, unsigned active, unsigned period, const unsigned* groups, unsigned ngroups,
+                         void* stream)
+{
+    if (!s) return set_error(XD_ERR_INVALID, "scene_set_emitter: null scene");
+    if (active > s->np) return set_error(XD_ERR_INVALID, "scene_set_emitter: active %u above the %u particles", active, s->np);
+    if (ngroups && !groups) return set_error(XD_ERR_INVALID, "scene_set_emitter: groups is null");
+    cudaStream_t q = static_cast<cudaStream_t>(stream);
+    if (s->mixed) {
+        int st = mixed_set_active(s->mixed, active, true, q);
+        if (st != XD_OK) return st;
+    }
+    s->active = active;
+    s->emit_period = period;
+    s->emit_groups.assign(groups, groups + ngroups);
+    s->emit_next = 0;
+    s->emit_step = 0;
+    return XD_OK;
+}
+
+int xd_scene_active(xd_scene* s, unsigned* active)
+{
+    if (!s || !active) return set_error(XD_ERR_INVALID, "scene_active: null argument");
+    *active = s->active;
     return XD_OK;
 }
 

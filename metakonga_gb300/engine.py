@@ -172,6 +172,26 @@ class DeviceScene:
         device (xd_scene_set_kinematic_bodies)."""
         call("xd_scene_set_kinematic_bodies", self.handle, 1 if enable else 0)
 
+    def set_emitter(self, period: int, groups=None, active: int = 0, stream: int = 0):
+        """Emit the staged particles: only the first ``active`` take part; every
+        ``period`` steps (from the next one) the next group of ``groups`` joins,
+        one particle at a time when groups is None (xd_scene_set_emitter)."""
+        if groups is None:
+            g, ng = None, 0
+        else:
+            g = np.ascontiguousarray(groups, dtype=np.uint32)
+            ng = int(g.shape[0])
+            if ng == 0:
+                period = 0
+        call("xd_scene_set_emitter", self.handle, int(active), int(period),
+             g.ctypes.data if ng else None, ng, stream)
+
+    def active(self) -> int:
+        """Particles taking part in the next step (xd_scene_active)."""
+        out = np.zeros(1, np.uint32)
+        call("xd_scene_active", self.handle, out.ctypes.data)
+        return int(out[0])
+
     def set_tangential_history(self, slots: int = 12):
         """Tangential springs kept per contact (xd_scene_set_tangential_history);
         0 restores the reference's DHS model."""

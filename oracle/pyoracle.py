@@ -47,8 +47,13 @@ class _Scene(C.Structure):
         ("hash", _vp), ("index", _vp), ("sorted", _vp), ("cstart", _vp), ("cend", _vp),
         ("cp_pp", _vp), ("nplanes", _u), ("planes", _vp), ("cp_planes", _vp),
         ("ntri", _u), ("poly", _vp), ("sphere", _vp), ("pmi", _vp), ("cp_poly", _vp),
-        ("hist", _vp), ("kinematic", C.c_int), ("nbodies", _u), ("vlist", _vp),
+        ("hist", _vp), ("kinematic", C.c_int), ("nbodies", _u), ("vlist", _vp), ("emit", _vp),
     ]
+
+
+class _Emitter(C.Structure):
+    _fields_ = [("period", _u), ("groups", _vp), ("ngroups", _u), ("next", _u), ("active", _u),
+                ("step", C.c_ulonglong)]
 
 
 class _History(C.Structure):
@@ -77,6 +82,28 @@ class History:
     def contacts(self, i: int) -> dict:
         """{key: delta} of particle i."""
         return {int(k): self.delta[s, i].copy() for s, k in enumerate(self.key[:, i]) if k != HIST_EMPTY}
+
+
+class Emitter:
+    """Particle emitter of a scene (xdo_emitter): the first `active` particles
+    take part; before step k (1-based, counted from construction) with
+    (k - 1) % period == 0 the next group joins (one particle when groups is
+    None).  Keeps its state across ``Oracle.run`` calls."""
+
+    def __init__(self, period: int, groups=None, active: int = 0):
+        self.groups = None if groups is None else np.ascontiguousarray(groups, dtype=np.uint32)
+        ng = 0 if self.groups is None else self.groups.shape[0]
+        self.c = _Emitter(period, self.groups.ctypes.data if ng else None, ng, 0, active, 0)
+        if self.groups is not None and ng == 0:
+            self.c.period = 0
+
+    @property
+    def active(self) -> int:
+        return int(self.c.active)
+
+    @property
+    def step(self) -> int:
+        return int(self.c.step)
 
 
 class Oracle:
@@ -230,11 +257,12 @@ class Oracle:
                 "cend": np.zeros(sc.ncell, np.uint32)}
 
     def run(self, sc, nsteps: int, cpu_path: bool = False, history: "History" = None,
-            kinematic: bool = False):
+            kinematic: bool = False, emitter: "Emitter" = None):
         """Advance ``sc`` (in place) by nsteps whole steps; returns the grid work
         arrays.  With ``history`` the contacts keep tangential springs; with
         ``kinematic`` the polygon bodies move by their own vel and omega each
-        step (xdo_advance_bodies)."""
+        step (xdo_advance_bodies); with ``emitter`` only its active particles
+        take part (xdo_emitter)."""
         for a in ("pos", "vel", "acc", "omega", "alpha", "force", "moment", "mass", "inertia"):
             assert getattr(sc, a).flags["C_CONTIGUOUS"]
         work = self._work(sc)
@@ -246,6 +274,9 @@ class Oracle:
             assert not cpu_path and sc.ntri
             assert sc.vlist.flags["C_CONTIGUOUS"]
             s.kinematic = 1
+        if emitter is not None:
+            assert not cpu_path
+            s.emit = C.addressof(emitter.c)
         fn = self.lib.xdo_cpu_run_steps if cpu_path else self.lib.xdo_run_steps
         fn(C.byref(s), _u(nsteps))
         return work

@@ -935,10 +935,25 @@ void xdo_advance_bodies(xdo_polygon_mass* pmi, unsigned nbodies, double dt)
  * contactManager::deviceCollision (contactManager.cpp:156-185):
  * VV position, grid, particle-particle, planes in name order, polygons,
  * VV velocity (which also resets F = m g, M = 0). */
+unsigned xdo_emitter_before_step(xdo_emitter* e, unsigned np)
+{
+    e->step += 1;
+    if (e->period && (e->step - 1) % e->period == 0 && e->active < np) {
+        unsigned add = 1;
+        if (e->groups) add = e->next < e->ngroups ? e->groups[e->next++] : 0;
+        e->active = add > np - e->active ? np : e->active + add;
+    }
+    return e->active;
+}
+
 void xdo_step(xdo_scene* s)
 {
-    xdo_params* prm = &s->prm;
-    unsigned np = s->np;
+    /* with an emitter the step runs over the active particles, the parameter
+     * block's np included (the polygon pass reads it) */
+    xdo_params local = s->prm;
+    xdo_params* prm = &local;
+    unsigned np = s->emit ? xdo_emitter_before_step(s->emit, s->np) : s->np;
+    local.np = s->emit ? np : s->prm.np;
     unsigned n = np + s->ntri;
     if (s->kinematic && s->ntri) {
         xdo_advance_bodies(s->pmi, s->nbodies, prm->dt);

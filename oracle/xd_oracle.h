@@ -177,6 +177,28 @@ void xdo_hist_polygon(const xdo_params* prm, const xdo_polygon* dpi, xdo_polygon
                       const unsigned* cstart, const unsigned* cend, const xdo_contact_property* cp,
                       xdo_history* h);
 
+/* Particle emitter, the reference's real-time creation
+ * (dem_simulation.cpp:210-222 sets the period, :321-322 starts from no
+ * particle, :449-450 adds a group before a step; particleManager.cpp:132-145
+ * hands out the groups, or one particle at a time): the scene's np particles
+ * are staged in memory and only the first `active` take part in a step.
+ * Before step k (1-based, counted from when the emitter was set), when
+ * period > 0, (k - 1) % period == 0 and active < np, active grows by the next
+ * group size (by one when groups is NULL; by nothing once the groups are used
+ * up), clamped to np.  The grid, the contacts and velocity-Verlet then run
+ * over the active particles, and triangles sit at grid index active + t. */
+typedef struct xdo_emitter {
+    unsigned period;
+    const unsigned* groups;
+    unsigned ngroups;
+    unsigned next;               /* next group to hand out */
+    unsigned active;
+    unsigned long long step;     /* steps run since the emitter was set */
+} xdo_emitter;
+
+/* Advances the emitter by one step and returns the active count of that step. */
+unsigned xdo_emitter_before_step(xdo_emitter* e, unsigned np);
+
 /* ---- one whole step in the reference's order (dem_simulation.cpp:447-469,
  *      contactManager.cpp:156-185) ---- */
 typedef struct xdo_scene {
@@ -201,6 +223,7 @@ typedef struct xdo_scene {
     int kinematic;
     unsigned nbodies;
     const double* vlist;                 /* body-frame vertices [ntri][9] */
+    xdo_emitter* emit;                   /* NULL: every particle takes part */
 } xdo_scene;
 
 /* One step of prescribed body motion: origin += dt vel; the Euler parameters

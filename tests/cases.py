@@ -193,3 +193,152 @@ def legacy_mesh(tri):
     poly_end = np.cumsum(counts).astype(np.uint32)
     poly_start = (poly_end - counts).astype(np.uint32)
     return verts.astype(np.float64), indice, id_set, poly_start, poly_end
+
+
+def emitter_column(n=6, radius=0.005, pitch=0.05, dt=1.0e-5):
+    """n spheres 50 mm apart along x at one height: no contacts, no walls."""
+    from metakonga_gb300.layouts import PLANE
+    pos = np.zeros((n, 4))
+    pos[:, 0] = pitch * np.arange(n) - 0.4
+    pos[:, 2] = 0.3
+    pos[:, 3] = radius
+    return scenes.Scene(name="column", seed=0, dt=dt, steps=0, params=scenes._reference_grid(radius, n, dt),
+                        pos=pos, **scenes._state(pos), cp_pp=scenes._default_property(),
+                        planes=np.zeros(0, dtype=PLANE), plane_names=[],
+                        cp_planes=np.zeros(0, dtype=CONTACT_PROPERTY))
+
+
+EMITTER_MODEL = """MODEL_NAME hopper_fill
+GRAVITY 0 -9.80665 0
+UNIT 0
+SINGLE 0
+
+DEM_MODEL_DATA
+INTEGRATOR 0
+SORT 0
+
+PARTICLES_DATA
+CREATE_SHAPE plane
+NAME emitter
+MATERIAL_TYPE 7
+DIMENSION 0.1 6 0.1
+STARTPOINT 0 0.03 0
+DIRECTION 0 -1 0
+SPACE 0
+RADIUS 0.004 0.004
+MAKING 1 726 0 0.005 0 none
+MATERIAL 1e7 2500 0.3 0
+END_DATA
+
+GEOMETRY_OBJECTS_DATA
+OBJECT plane
+NAME floor
+MATERIAL_TYPE 7
+GEOMETRY_USE 0
+POINT_A 0 0 0
+POINT_B 0 0 0.1
+POINT_C 0.1 0 0.1
+POINT_D 0.1 0 0
+MATERIAL 1e7 0.3 2500 0
+OBJECT plane
+NAME wall_x0
+MATERIAL_TYPE 0
+GEOMETRY_USE 0
+POINT_A 0 0 0
+POINT_B 0 0.2 0
+POINT_C 0 0.2 0.1
+POINT_D 0 0 0.1
+MATERIAL 0 0 0 0
+OBJECT plane
+NAME wall_x1
+MATERIAL_TYPE 0
+GEOMETRY_USE 0
+POINT_A 0.1 0 0
+POINT_B 0.1 0 0.1
+POINT_C 0.1 0.2 0.1
+POINT_D 0.1 0.2 0
+MATERIAL 0 0 0 0
+OBJECT plane
+NAME wall_z0
+MATERIAL_TYPE 0
+GEOMETRY_USE 0
+POINT_A 0 0 0
+POINT_B 0.1 0 0
+POINT_C 0.1 0.2 0
+POINT_D 0 0.2 0
+MATERIAL 0 0 0 0
+OBJECT plane
+NAME wall_z1
+MATERIAL_TYPE 0
+GEOMETRY_USE 0
+POINT_A 0 0 0.1
+POINT_B 0 0.2 0.1
+POINT_C 0.1 0.2 0.1
+POINT_D 0.1 0 0.1
+MATERIAL 0 0 0 0
+END_DATA
+
+CONTACT_ELEMENTS_DATA
+NAME pp
+METHOD 1
+OBJECT0 particles
+OBJECT1 particles
+RESTITUTION 0.7
+RATIO 0.8
+FRICTION 0.3
+COHESION 0
+NAME p_floor
+METHOD 1
+OBJECT0 particles
+OBJECT1 floor
+RESTITUTION 0.6
+RATIO 0.8
+FRICTION 0.4
+COHESION 0
+NAME p_wall0
+METHOD 1
+OBJECT0 particles
+OBJECT1 wall_x0
+RESTITUTION 0.6
+RATIO 0.8
+FRICTION 0.4
+COHESION 0
+NAME p_wall1
+METHOD 1
+OBJECT0 wall_x1
+OBJECT1 particles
+RESTITUTION 0.6
+RATIO 0.8
+FRICTION 0.4
+COHESION 0
+NAME p_wall2
+METHOD 1
+OBJECT0 particles
+OBJECT1 wall_z0
+RESTITUTION 0.6
+RATIO 0.8
+FRICTION 0.4
+COHESION 0
+NAME p_wall3
+METHOD 1
+OBJECT0 particles
+OBJECT1 wall_z1
+RESTITUTION 0.6
+RATIO 0.8
+FRICTION 0.4
+COHESION 0
+END_DATA
+"""
+
+
+def emitter_box(layers=6, drop_speed=2.0):
+    """The plane emitter of EMITTER_MODEL: 6 layers of 11 x 11 spheres
+    (r = 4 mm) staged at y = 30 mm above the floor of a 0.1 m box with steel
+    side walls, one layer every 500 steps (0.005 s at dt = 1e-5), each
+    leaving downwards at drop_speed.  Returns the scene and its emitter."""
+    from metakonga_gb300 import model_file
+    text = EMITTER_MODEL.replace("DIMENSION 0.1 6 0.1", f"DIMENSION 0.1 {layers} 0.1")
+    built = model_file.build_scene(model_file.read_model(text), dt=1.0e-5, seed=17)
+    sc = built.scene
+    sc.vel[:, 1] = -drop_speed
+    return sc, built.emitter
