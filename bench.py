@@ -85,6 +85,7 @@ def _args():
     ap.add_argument("--workload", default="batched", choices=["batched", "served", "box"])
     ap.add_argument("--no-served", action="store_true", help="batched: skip the served stream")
     ap.add_argument("--no-box", action="store_true", help="batched: skip the 1M-box roofline run")
+    ap.add_argument("--no-drum", action="store_true", help="batched: skip the rotating-drum run")
     ap.add_argument("--count", type=int, default=256, help="scenes in the batch")
     ap.add_argument("--requests", type=int, default=32, help="requests of the served stream")
     ap.add_argument("--rate", type=float, default=4.0, help="served arrivals per second")
@@ -582,6 +583,50 @@ def _box_roofline(a, stream, barrier, world, local):
                   "gpu_launches": launches, "cell_rebinnings_in_timed_steps": rebuilds}
 
 
+def _drum(a, stream, steps=200, warmup=3):
+    """The rotating drum at full size (500,000 spheres in a 20,480-triangle
+    cylinder turning at 1 rad/s, the mesh moved on the device every step) in
+    the mixed form, and the same scene's step time in the plain FP64 form."""
+    import torch
+
+    from metakonga_gb300 import engine, scenes
+    sc = scenes.drum_lattice()
+    sh = stream.cuda_stream
+    ds = engine.DeviceScene(sc, mode=engine.MODE_MIXED)
+    ds.set_kinematic_bodies(True)
+    ds.step(warmup, check=True, stream=sh)
+    rb0 = ds.rebuilds(sh)[0]
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ds.step(steps, check=False, stream=sh)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    rebuilds = ds.rebuilds(sh)[0] - rb0
+    ds.close()
+    d64 = engine.DeviceScene(sc, mode=engine.MODE_FP64)
+    d64.set_kinematic_bodies(True)
+    d64.step(1, check=True, stream=sh)
+    e0.record(stream)
+    d64.step(2, check=False, stream=sh)
+    e1.record(stream)
+    e1.synchronize()
+    ms64 = e0.elapsed_time(e1) / 2
+    d64.close()
+    value = sc.np_ * steps / (ms / 1e3)
+    return {"workload": "rotating drum: 500,000 spheres r U[2,4] mm on a jittered FCC lattice from the "
+                        "bottom, closed cylinder R 0.5 m L 0.4 m of 20,480 triangles turning at 1 rad/s "
+                        "(kinematic on the device), wall friction 0.5, dt 5e-6",
+            "value": value, "unit": "particle-steps/s", "ms_per_step": ms / steps, "steps": steps,
+            "cell_rebinnings_in_timed_steps": rebuilds,
+            "plain_fp64": {"value": sc.np_ / (ms64 / 1e3), "ms_per_step": ms64,
+                           "method": "the same scene in the FP64 form (the reference's 128^3 grid of "
+                                     "2 x max(r, triangle circumradius) cells, re-sorted every step), "
+                                     "one warm-up step then 2 device-timed steps"},
+            "ratio": value / (sc.np_ / (ms64 / 1e3))}
+
+
 def _served(a, stream, plain=True):
     """The served request stream: report of the continuous-batching server,
     and the same requests' time alone in the FP64 form."""
@@ -714,6 +759,7 @@ def run_batched(a):
     check = _fp64_check(scs[k_med])
     check["scene"] = k_med
     roof, box = _box_roofline(a, stream, barrier, world, local) if not a.no_box else (None, None)
+    drum = _drum(a, stream) if not a.no_drum and rank == 0 else None
     served = _served(a, stream, plain=not a.no_plain) if rank == 0 and not a.no_served else None
 
     cpu = None
@@ -753,6 +799,7 @@ def run_batched(a):
                       "bytes_per_particle": B_ADVANCE + B_CONTACT["mixed"]},
         "roofline": roof,
         "single_scene_box": box,
+        "drum": drum,
         "served": served,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
