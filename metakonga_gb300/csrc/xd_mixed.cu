@@ -138,6 +138,7 @@ struct MixedScene {
     // particles not yet emitted, in id order (no re-binning touches them).
     unsigned n = 0, cap = 0, nplanes = 0, ncell = 0;
     unsigned active_req = ~0u;    // active count set before the first upload
+    bool emitted = false;         // the particle count has changed since the graphs were made
     int gx = 0, gy = 0, gz = 0;
     double cs = 0.0;
     MixParams P;
@@ -2325,9 +2326,10 @@ int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
     int st = update_mesh(s, q);
     if (st != XD_OK) return st;
     // graphs pay for their capture over many steps: a short call on a scene
-    // whose graphs are not captured (an emission just changed its particle
-    // count) launches directly
-    const bool graphs = s->use_graphs && ph.fn == nullptr && (s->graph[kFirstStep] || nsteps >= kGraphMinSteps);
+    // whose graphs an emission has just dropped (its particle count changed)
+    // launches directly
+    const bool graphs = s->use_graphs && ph.fn == nullptr &&
+                        (!s->emitted || s->graph[kFirstStep] || nsteps >= kGraphMinSteps);
     if (graphs) {
         // Every step in a graph, re-binning decided on the device: the call
         // never waits for the GPU.  A scene without cells yet (after an
@@ -2521,6 +2523,7 @@ int mixed_set_active(MixedScene* s, unsigned active, bool restore, cudaStream_t 
     // queued from them have run
     if (s->graph[kFirstStep]) st = cuda_status(cudaStreamSynchronize(q), "scene emitter");
     destroy_graphs(s);
+    s->emitted = true;
     return st;
 }
 
