@@ -443,6 +443,12 @@ int xd_scene_download_grid(xd_scene* scene, unsigned* hash, unsigned* index, uns
  * Reaction force/moment fields of the uploaded records are kept. */
 int xd_scene_set_bodies(xd_scene* scene, const xd_polygon_mass_info* pmi, void* stream);
 int xd_scene_get_bodies(xd_scene* scene, xd_polygon_mass_info* pmi, void* stream);
+/* Replace the planes (same count and order as the description) from a host
+ * array, as contact_particles_plane::cuda_collision re-uploads a moving
+ * plane's device_plane_info (collision/contact_particles_plane.cpp:33-51).
+ * The plane contact has no wall velocity, as in the reference.  The mixed
+ * form re-bins before its next step (the planes in reach change). */
+int xd_scene_set_planes(xd_scene* scene, const xd_plane_info* planes, void* stream);
 
 /* Advance nsteps whole steps on `stream`.  Returns after enqueueing; a
  * device-side error word is checked (with a synchronisation) only when

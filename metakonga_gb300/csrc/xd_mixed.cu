@@ -1569,6 +1569,8 @@ __global__ void __launch_bounds__(256) k_mx_ids(MixParams P, Master M, unsigned*
 
 // ------------------------------------------------------------------ host
 
+static void plane_prefilter(MixParams& P, const xd_plane_info* planes, unsigned nplanes);
+
 static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_host)
 {
     s->n = d.np;
@@ -1710,14 +1712,7 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
         P.pl_sratio[w] = c.sratio;
         P.pl_fric[w] = c.fric;
     }
-    for (unsigned w = 0; w < d.nplanes; ++w) {
-        const xd_plane_info& p = d.planes[w];
-        double un = sqrt(p.uw[0] * p.uw[0] + p.uw[1] * p.uw[1] + p.uw[2] * p.uw[2]);
-        for (int a = 0; a < 3; ++a) {
-            P.pxw[w][a] = (float)(p.xw[a] - lo[a]);
-            P.pun[w][a] = (float)(p.uw[a] / un);
-        }
-    }
+    plane_prefilter(P, d.planes, d.nplanes);
 
     const size_t n = d.np;
     int st = XD_OK;
@@ -2479,6 +2474,34 @@ int mixed_set_bodies(MixedScene* s, const xd_polygon_mass_info* pmi, cudaStream_
                                          cudaMemcpyHostToDevice, q), "scene_set_bodies");
     if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "scene_set_bodies");
     s->bodies_dirty = true;
+    return st;
+}
+
+// FP32 prefilter copies of the planes (corner relative to the grid origin,
+// unit normal) in the step parameters.
+static void plane_prefilter(MixParams& P, const xd_plane_info* planes, unsigned nplanes)
+{
+    for (unsigned w = 0; w < nplanes; ++w) {
+        const xd_plane_info& p = planes[w];
+        const double un = sqrt(p.uw[0] * p.uw[0] + p.uw[1] * p.uw[1] + p.uw[2] * p.uw[2]);
+        for (int a = 0; a < 3; ++a) {
+            P.pxw[w][a] = (float)(p.xw[a] - P.wo[a]);
+            P.pun[w][a] = (float)(p.uw[a] / un);
+        }
+    }
+}
+
+int mixed_set_planes(MixedScene* s, const xd_plane_info* planes, cudaStream_t q)
+{
+    s->host_planes.assign(planes, planes + s->nplanes);
+    s->desc.planes = s->host_planes.data();
+    if (!s->ready) return XD_OK;   // the set-up takes them from the description
+    int st = cuda_status(cudaMemcpyAsync(s->planes, planes, sizeof(xd_plane_info) * s->nplanes,
+                                         cudaMemcpyHostToDevice, q), "scene_set_planes");
+    if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "scene_set_planes");
+    plane_prefilter(s->P, planes, s->nplanes);
+    s->cells_clean = false;   // the planes in reach of each particle change
+    destroy_graphs(s);        // the step graphs hold the prefilter copies
     return st;
 }
 

@@ -43,6 +43,7 @@ unsigned mixed_active(MixedScene* s);
 int mixed_download_history(MixedScene* s, unsigned* keys, double* delta, unsigned long long* overflow,
                            cudaStream_t q);
 int mixed_set_bodies(MixedScene* s, const xd_polygon_mass_info* pmi, cudaStream_t q);
+int mixed_set_planes(MixedScene* s, const xd_plane_info* planes, cudaStream_t q);
 int mixed_get_bodies(MixedScene* s, xd_polygon_mass_info* pmi, cudaStream_t q);
 
 }  // namespace xd

@@ -445,6 +445,17 @@ int xd_scene_set_bodies(xd_scene* s, const xd_polygon_mass_info* pmi, void* stre
     return st;
 }
 
+int xd_scene_set_planes(xd_scene* s, const xd_plane_info* planes, void* stream)
+{
+    if (!s || !planes) return set_error(XD_ERR_INVALID, "scene_set_planes: null argument");
+    if (!s->nplanes) return set_error(XD_ERR_STATE, "scene_set_planes: scene has no planes");
+    cudaStream_t q = static_cast<cudaStream_t>(stream);
+    if (s->mixed) return mixed_set_planes(s->mixed, planes, q);
+    int st = h2d(s->planes, planes, sizeof(xd_plane_info) * s->nplanes, q);
+    if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "scene_set_planes");
+    return st;
+}
+
 int xd_scene_get_bodies(xd_scene* s, xd_polygon_mass_info* pmi, void* stream)
 {
     if (!s || !pmi) return set_error(XD_ERR_INVALID, "scene_get_bodies: null argument");

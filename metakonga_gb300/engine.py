@@ -18,6 +18,7 @@ os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 from . import _lib
 from ._lib import call
+from .layouts import PLANE
 
 MODE_FP64 = 0
 MODE_MIXED = 1
@@ -171,6 +172,14 @@ class DeviceScene:
         """Move the polygon bodies by their own vel and omega every step, on the
         device (xd_scene_set_kinematic_bodies)."""
         call("xd_scene_set_kinematic_bodies", self.handle, 1 if enable else 0)
+
+    def set_planes(self, planes, stream: int = 0):
+        """Move the walls: a PLANE array of the scene's plane count, in its
+        order (xd_scene_set_planes)."""
+        arr = np.ascontiguousarray(planes, dtype=PLANE)
+        if arr.shape != (self.scene.planes.shape[0],):
+            raise ValueError("set_planes: the scene's plane count and order")
+        call("xd_scene_set_planes", self.handle, arr.ctypes.data, stream)
 
     def set_emitter(self, period: int, groups=None, active: int = 0, stream: int = 0):
         """Emit the staged particles: only the first ``active`` take part; every
