@@ -569,6 +569,23 @@ int xd_scene_step_many(xd_scene* const* scenes, const unsigned* nsteps, unsigned
  * workspace).  No counterpart in the reference. */
 int xd_scene_device_bytes(xd_scene* scene, unsigned long long* bytes);
 
+/* Batches (no counterpart in the reference): mixed-form scenes advanced
+ * together, a step of all of them being one CUDA graph -- one advance launch
+ * over every scene's particles, a re-binning per scene that needs one (a
+ * conditional node per group of 16 scenes, then per scene), one contact
+ * launch over every scene's listed particles.  Each scene's result is the
+ * same, bit for bit, as when it is stepped alone; what a batch saves is the
+ * launch and graph-node cost per scene, which bounds many small scenes.  The
+ * scenes must be uploaded, in the mixed form, without tangential history,
+ * kinematic bodies or an emitter; a batch re-captures itself when one of its
+ * scenes changes (planes, bodies' kinematics, history), and must be
+ * destroyed before its scenes. */
+typedef struct xd_batch xd_batch;
+int xd_batch_create(xd_scene* const* scenes, unsigned count, xd_batch** out);
+/* nsteps whole steps of every scene of the batch, queued on `stream`. */
+int xd_batch_step(xd_batch* batch, unsigned nsteps, int check, void* stream);
+int xd_batch_destroy(xd_batch* batch);
+
 #ifdef __cplusplus
 }
 #endif

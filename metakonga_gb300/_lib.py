@@ -99,6 +99,9 @@ _SIGS = {
     "xd_scene_set_kinematic_bodies": [vp, i32],
     "xd_scene_set_emitter": [vp, u32, u32, vp, u32, vp],
     "xd_scene_set_planes": [vp, vp, vp],
+    "xd_batch_create": [vp, u32, vp],
+    "xd_batch_step": [vp, u32, i32, vp],
+    "xd_batch_destroy": [vp],
     "xd_scene_active": [vp, vp],
     "xd_scene_download_history": [vp, vp, vp, vp, vp],
     "xd_scene_device_bytes": [vp, vp],

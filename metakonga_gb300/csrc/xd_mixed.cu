@@ -139,6 +139,7 @@ struct MixedScene {
     unsigned n = 0, cap = 0, nplanes = 0, ncell = 0;
     unsigned active_req = ~0u;    // active count set before the first upload
     bool emitted = false;         // the particle count has changed since the graphs were made
+    unsigned version = 0;         // raised whenever the step graphs are dropped (parameters changed)
     int gx = 0, gy = 0, gz = 0;
     double cs = 0.0;
     MixParams P;
@@ -495,6 +496,43 @@ __device__ __forceinline__ double drift(const MixParams& P, double x, float vhi,
 // that does not sets CN_REBUILD.  The last block to finish passes the flag to
 // the graph's conditional node (use_cond), one caller as the conditional
 // requires.
+// One slot of the advance (MODE 0: drift; MODE 1: kick with the last
+// contact forces, then drift), its contact view, and whether it has left half
+// the skin since the last build.
+template <int MODE>
+__device__ __forceinline__ bool advance_one(const MixParams& P, const Master& M, const float4* __restrict__ Fc,
+                                            const float4* __restrict__ Mc, const float4* __restrict__ pref,
+                                            float4* __restrict__ pf, longlong2* __restrict__ qa,
+                                            longlong2* __restrict__ qb, const unsigned i)
+{
+    double x = M.x[i], y = M.y[i], z = M.z[i];
+    const double r = M.r[i];
+    if (MODE == 0 || MODE == 1) {
+        float4 vh = M.vh[i], vl = M.vl[i], ab = M.ab[i];
+        if (MODE == 1) {
+            float4 wh = M.wh[i], wl = M.wl[i];
+            float2 b2 = M.b2[i];
+            kick(P, vh, vl, wh, wl, ab, b2, Fc[i], Mc[i]);
+            M.vh[i] = vh;
+            M.vl[i] = vl;
+            M.wh[i] = wh;
+            M.wl[i] = wl;
+            M.ab[i] = ab;
+            M.b2[i] = b2;
+        }
+        x = drift(P, x, vh.x, vl.x, 0, ab.x);
+        y = drift(P, y, vh.y, vl.y, 1, ab.y);
+        z = drift(P, z, vh.z, vl.z, 2, ab.z);
+        M.x[i] = x;
+        M.y[i] = y;
+        M.z[i] = z;
+    }
+    const float4 v = write_view(P, i, x, y, z, r, pf, qa, qb);
+    const float4 r0 = pref[i];
+    const float dx = v.x - r0.x, dy = v.y - r0.y, dz = v.z - r0.z;
+    return !(dx * dx + dy * dy + dz * dz < P.disp2);
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(256) k_mx_advance(MixParams P, Master M, const float4* __restrict__ Fc,
                                                     const float4* __restrict__ Mc,
@@ -506,35 +544,7 @@ __global__ void __launch_bounds__(256) k_mx_advance(MixParams P, Master M, const
 {
     __shared__ bool last;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool out = false;
-    if (i < P.n) {
-        double x = M.x[i], y = M.y[i], z = M.z[i];
-        const double r = M.r[i];
-        if (MODE == 0 || MODE == 1) {
-            float4 vh = M.vh[i], vl = M.vl[i], ab = M.ab[i];
-            if (MODE == 1) {
-                float4 wh = M.wh[i], wl = M.wl[i];
-                float2 b2 = M.b2[i];
-                kick(P, vh, vl, wh, wl, ab, b2, Fc[i], Mc[i]);
-                M.vh[i] = vh;
-                M.vl[i] = vl;
-                M.wh[i] = wh;
-                M.wl[i] = wl;
-                M.ab[i] = ab;
-                M.b2[i] = b2;
-            }
-            x = drift(P, x, vh.x, vl.x, 0, ab.x);
-            y = drift(P, y, vh.y, vl.y, 1, ab.y);
-            z = drift(P, z, vh.z, vl.z, 2, ab.z);
-            M.x[i] = x;
-            M.y[i] = y;
-            M.z[i] = z;
-        }
-        const float4 v = write_view(P, i, x, y, z, r, pf, qa, qb);
-        const float4 r0 = pref[i];
-        const float dx = v.x - r0.x, dy = v.y - r0.y, dz = v.z - r0.z;
-        out = !(dx * dx + dy * dy + dz * dz < P.disp2);
-    }
+    const bool out = i < P.n && advance_one<MODE>(P, M, Fc, Mc, pref, pf, qa, qb, i);
     // only the flag must be visible to the last block: the lanes that set it
     // fence; the state and view writes need no ordering here
     if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31u) == 0) {
@@ -547,7 +557,9 @@ __global__ void __launch_bounds__(256) k_mx_advance(MixParams P, Master M, const
     if (last && threadIdx.x == 0) {
         __threadfence();
         const unsigned f = atomicOr(counters + CN_REBUILD, 0u) ? 1u : 0u;
-        if (use_cond) cudaGraphSetConditional(cond, f);
+        // the handle's default (0, assigned at every graph launch) stands
+        // unless a re-binning is due
+        if (use_cond && f) cudaGraphSetConditional(cond, 1u);
         counters[CN_DONE] = 0;
     }
 }
@@ -604,11 +616,9 @@ __global__ void __launch_bounds__(256) k_mx_copyback(MixParams P, Master S, Mast
 }
 
 // MODE 2: velocity only, in place (the last step of a call).
-__global__ void __launch_bounds__(256) k_mx_finish(MixParams P, Master M, const float4* __restrict__ Fc,
-                                                   const float4* __restrict__ Mc)
+__device__ __forceinline__ void finish_one(const MixParams& P, const Master& M, const float4* __restrict__ Fc,
+                                           const float4* __restrict__ Mc, const unsigned i)
 {
-    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
     float4 vh = M.vh[i], vl = M.vl[i], wh = M.wh[i], wl = M.wl[i], ab = M.ab[i];
     float2 b2 = M.b2[i];
     kick(P, vh, vl, wh, wl, ab, b2, Fc[i], Mc[i]);
@@ -618,6 +628,13 @@ __global__ void __launch_bounds__(256) k_mx_finish(MixParams P, Master M, const 
     M.wl[i] = wl;
     M.ab[i] = ab;
     M.b2[i] = b2;
+}
+
+__global__ void __launch_bounds__(256) k_mx_finish(MixParams P, Master M, const float4* __restrict__ Fc,
+                                                   const float4* __restrict__ Mc)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P.n) finish_one(P, M, Fc, Mc, i);
 }
 
 // ---- cell lower bounds -----------------------------------------------------
@@ -1187,222 +1204,264 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
 constexpr unsigned kContactThreads = 64;
 constexpr unsigned kContactBlocks = 152 * 8;
 
+// The pointers of one scene the contact pass reads and writes.
+struct ContactArgs {
+    Master M;
+    const float4* pf;
+    const longlong2* qa;
+    const longlong2* qb;
+    const unsigned* keys;
+    const unsigned* lb;
+    const unsigned* vcount;
+    const unsigned* vlist;
+    const unsigned* hlist;
+    const unsigned short* wmask;
+    const xd_plane_info* planes;
+    const double* mass0;
+    const xd_polygon_info* poly;
+    const xd_polygon_mass_info* pmi;
+    const unsigned* tcount;
+    const unsigned* tlist;
+    const unsigned* tpk;
+    const unsigned* tpt;
+    unsigned tcap;
+    double* rxn;
+    float4* Fc;
+    float4* Mc;
+    unsigned* counters;
+    unsigned* rec_count;
+    unsigned* rec_pairs;
+    unsigned rec_cap;
+    HistTable ht;
+    int rxn_on;
+};
+
+// The contact pass of one listed particle (slot i): its Verlet-list pairs,
+// planes and triangles, summed in a fixed order into Fc/Mc.
 template <bool RECORD, int HIST>
-__global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Master M, const float4* __restrict__ pf,
-                                                    const longlong2* __restrict__ qa,
-                                                    const longlong2* __restrict__ qb,
-                                                    const unsigned* __restrict__ keys,
-                                                    const unsigned* __restrict__ lb,
-                                                    const unsigned* __restrict__ vcount,
-                                                    const unsigned* __restrict__ vlist,
-                                                    const unsigned* __restrict__ hlist,
-                                                    const unsigned short* __restrict__ wmask,
-                                                    const xd_plane_info* __restrict__ planes,
-                                                    const xd_contact_property* __restrict__ cps,
-                                                    const double* __restrict__ mass0,
-                                                    const xd_polygon_info* __restrict__ poly,
-                                                    const xd_polygon_mass_info* __restrict__ pmi,
-                                                    const unsigned* __restrict__ tcount,
-                                                    const unsigned* __restrict__ tlist,
-                                                    const unsigned* __restrict__ tpk,
-                                                    const unsigned* __restrict__ tpt, unsigned tcap,
-                                                    double* __restrict__ rxn,
-                                                    float4* __restrict__ Fc, float4* __restrict__ Mc,
-                                                    unsigned* __restrict__ counters,
-                                                    unsigned* __restrict__ rec_count,
-                                                    unsigned* __restrict__ rec_pairs, unsigned rec_cap,
-                                                    HistTable ht, int rxn_on)
+__device__ __forceinline__ void contact_entry(const MixParams& P, const ContactArgs& C, const unsigned i)
 {
-    if (blockIdx.x == 0 && threadIdx.x == 0) counters[CN_REBUILD] = 0;
-    const unsigned total = counters[CN_HEAVY];
+    const Master& M = C.M;
+    const float4* __restrict__ pf = C.pf;
+    const longlong2* __restrict__ qa = C.qa;
+    const longlong2* __restrict__ qb = C.qb;
+    const unsigned* __restrict__ keys = C.keys;
+    const unsigned* __restrict__ lb = C.lb;
+    const unsigned* __restrict__ vcount = C.vcount;
+    const unsigned* __restrict__ vlist = C.vlist;
+    const unsigned short* __restrict__ wmask = C.wmask;
+    const xd_plane_info* __restrict__ planes = C.planes;
+    const double* __restrict__ mass0 = C.mass0;
+    const xd_polygon_info* __restrict__ poly = C.poly;
+    const xd_polygon_mass_info* __restrict__ pmi = C.pmi;
+    const unsigned* __restrict__ tcount = C.tcount;
+    const unsigned* __restrict__ tlist = C.tlist;
+    const unsigned* __restrict__ tpk = C.tpk;
+    const unsigned* __restrict__ tpt = C.tpt;
+    const unsigned tcap = C.tcap;
+    double* __restrict__ rxn = C.rxn;
+    float4* __restrict__ Fc = C.Fc;
+    float4* __restrict__ Mc = C.Mc;
+    unsigned* __restrict__ counters = C.counters;
+    unsigned* __restrict__ rec_count = C.rec_count;
+    unsigned* __restrict__ rec_pairs = C.rec_pairs;
+    const unsigned rec_cap = C.rec_cap;
+    const HistTable& ht = C.ht;
+    const int rxn_on = C.rxn_on;
     const unsigned n = P.n;
-    // runs of 32 consecutive list entries (neighbouring slots) go to the warps
-    // of all blocks in turn: every SM gets an equal share however short the list
-    const unsigned warps = gridDim.x * (blockDim.x / 32u);
-    const unsigned gw = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u;
-    for (unsigned t = gw * 32u + (threadIdx.x & 31u); t < total; t += warps * 32u) {
-        const unsigned i = __ldg(hlist + t);
-        const float4 pi = __ldg(pf + i);
-        // the particle's own data is loaded when first needed: most listed
-        // particles have neighbours within the skin but no contact
-        Own I;
-        I.i = i;
-        I.r = pi.w;
-        bool have_q = false, have_v = false;
-        PairAcc A;
-        A.Ft = fk(0.f, 0.f, 0.f);
-        A.Mm = fk(0.f, 0.f, 0.f);
-        A.sumF = fk(0.f, 0.f, 0.f);
-        A.sumM = fk(0.f, 0.f, 0.f);
-        unsigned nc = 0;
-        HistState hs;
-        if (HIST == 1) hist_begin(ht, i, hs);
-        auto add = [&](unsigned j, bool guard) {
-            if (!have_v) {
-                I.vh = __ldg(M.vh + i);
-                I.vl = __ldg(M.vl + i);
-                const float4 w4 = __ldg(M.wh + i);
-                I.w = fk(w4.x, w4.y, w4.z);
-                I.im = I.vh.w;
-                have_v = true;
-            }
-            contact_force<HIST>(P, M, I, j, guard, mass0, pf, qa, qb, counters, A, ht, hs);
-            if (RECORD && nc < rec_cap) rec_pairs[(size_t)i * rec_cap + nc] = j;
-            ++nc;
-        };
-        const unsigned vc = __ldg(vcount + i);
-        if (!(vc & kIncomplete)) {
-            const float rt0 = pi.w + P.tol;
-            for (unsigned k = 0; k < vc; ++k) {
-                const unsigned j = __ldg(vlist + (size_t)k * n + i);
-                const float4 pj = __ldg(pf + j);
-                const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                const float Rt = rt0 + pj.w;
-                if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) >= Rt * Rt) continue;
-                if (!have_q) {
-                    I.qa = __ldg(qa + i);
-                    I.qb = __ldg(qb + i);
-                    have_q = true;
-                }
-                const int c = exact_touch<true>(P, M, i, j, I.qa, I.qb, qa, qb, counters);
-                if (c) add(j, c == 2);
-            }
-        } else {
-            I.qa = __ldg(qa + i);
-            I.qb = __ldg(qb + i);
-            for_each_contact<true>(P, M, i, pi, I.qa, I.qb, __ldg(keys + i), pf, qa, qb, lb, counters, add);
+    const float4 pi = __ldg(pf + i);
+    // the particle's own data is loaded when first needed: most listed
+    // particles have neighbours within the skin but no contact
+    Own I;
+    I.i = i;
+    I.r = pi.w;
+    bool have_q = false, have_v = false;
+    PairAcc A;
+    A.Ft = fk(0.f, 0.f, 0.f);
+    A.Mm = fk(0.f, 0.f, 0.f);
+    A.sumF = fk(0.f, 0.f, 0.f);
+    A.sumM = fk(0.f, 0.f, 0.f);
+    unsigned nc = 0;
+    HistState hs;
+    if (HIST == 1) hist_begin(ht, i, hs);
+    auto add = [&](unsigned j, bool guard) {
+        if (!have_v) {
+            I.vh = __ldg(M.vh + i);
+            I.vl = __ldg(M.vl + i);
+            const float4 w4 = __ldg(M.wh + i);
+            I.w = fk(w4.x, w4.y, w4.z);
+            I.im = I.vh.w;
+            have_v = true;
         }
-        float4 F = make_float4(A.sumF.x, A.sumF.y, A.sumF.z, 0.f);
-        // planes in reach: an FP32 distance to the supporting plane first (the
-        // finite plane is never nearer), the reference's FP64 test after it
-        unsigned wm = __ldg(wmask + i);
+        contact_force<HIST>(P, M, I, j, guard, mass0, pf, qa, qb, counters, A, ht, hs);
+        if (RECORD && nc < rec_cap) rec_pairs[(size_t)i * rec_cap + nc] = j;
+        ++nc;
+    };
+    const unsigned vc = __ldg(vcount + i);
+    if (!(vc & kIncomplete)) {
+        const float rt0 = pi.w + P.tol;
+        for (unsigned k = 0; k < vc; ++k) {
+            const unsigned j = __ldg(vlist + (size_t)k * n + i);
+            const float4 pj = __ldg(pf + j);
+            const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+            const float Rt = rt0 + pj.w;
+            if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) >= Rt * Rt) continue;
+            if (!have_q) {
+                I.qa = __ldg(qa + i);
+                I.qb = __ldg(qb + i);
+                have_q = true;
+            }
+            const int c = exact_touch<true>(P, M, i, j, I.qa, I.qb, qa, qb, counters);
+            if (c) add(j, c == 2);
+        }
+    } else {
+        I.qa = __ldg(qa + i);
+        I.qb = __ldg(qb + i);
+        for_each_contact<true>(P, M, i, pi, I.qa, I.qb, __ldg(keys + i), pf, qa, qb, lb, counters, add);
+    }
+    float4 F = make_float4(A.sumF.x, A.sumF.y, A.sumF.z, 0.f);
+    // planes in reach: an FP32 distance to the supporting plane first (the
+    // finite plane is never nearer), the reference's FP64 test after it
+    unsigned wm = __ldg(wmask + i);
+    for (unsigned mask = wm; mask; mask &= mask - 1u) {
+        const int w = __ffs(mask) - 1;
+        const float hz = (pi.x - P.pxw[w][0]) * P.pun[w][0] + (pi.y - P.pxw[w][1]) * P.pun[w][1] +
+                         (pi.z - P.pxw[w][2]) * P.pun[w][2];
+        if (!(fabsf(hz) < pi.w + P.tol)) wm &= ~(1u << w);
+    }
+    if (wm) {
+        const float4 vh = __ldg(M.vh + i), vl = __ldg(M.vl + i);
+        const float4 wl = __ldg(M.wl + i), wh = __ldg(M.wh + i);
+        const double m = __ldg(mass0 + __float_as_uint(wl.w));
+        const d3 ip = mk(__ldg(M.x + i), __ldg(M.y + i), __ldg(M.z + i));
+        const double r = __ldg(M.r + i);
+        const d3 iv = mk(df_to_d(vh.x, vl.x), df_to_d(vh.y, vl.y), df_to_d(vh.z, vl.z));
+        const d3 iw = mk(df_to_d(wh.x, wl.x), df_to_d(wh.y, wl.y), df_to_d(wh.z, wl.z));
+        d3 f = mk(0, 0, 0);
         for (unsigned mask = wm; mask; mask &= mask - 1u) {
             const int w = __ffs(mask) - 1;
-            const float hz = (pi.x - P.pxw[w][0]) * P.pun[w][0] + (pi.y - P.pxw[w][1]) * P.pun[w][1] +
-                             (pi.z - P.pxw[w][2]) * P.pun[w][2];
-            if (!(fabsf(hz) < pi.w + P.tol)) wm &= ~(1u << w);
-        }
-        if (wm) {
-            const float4 vh = __ldg(M.vh + i), vl = __ldg(M.vl + i);
-            const float4 wl = __ldg(M.wl + i), wh = __ldg(M.wh + i);
-            const double m = __ldg(mass0 + __float_as_uint(wl.w));
-            const d3 ip = mk(__ldg(M.x + i), __ldg(M.y + i), __ldg(M.z + i));
-            const double r = __ldg(M.r + i);
-            const d3 iv = mk(df_to_d(vh.x, vl.x), df_to_d(vh.y, vl.y), df_to_d(vh.z, vl.z));
-            const d3 iw = mk(df_to_d(wh.x, wl.x), df_to_d(wh.y, wl.y), df_to_d(wh.z, wl.z));
-            d3 f = mk(0, 0, 0);
-            for (unsigned mask = wm; mask; mask &= mask - 1u) {
-                const int w = __ffs(mask) - 1;
-                PlaneD pe = load_plane(planes + w);
-                d3 Fn = mk(0, 0, 0), Ft = mk(0, 0, 0), Mo = mk(0, 0, 0);
-                d3 dp = ip - pe.xw;
-                d3 unit = mk(0, 0, 0);
-                d3 wp = mk(dot(dp, pe.u1), dot(dp, pe.u2), dot(dp, pe.uw));
-                double cdist = plane_detection(pe, ip, wp, unit, r);
-                if (cdist > 0) {
-                    d3 dv = P.rolling ? -(iv + cross(iw, r * unit)) : -iv;
-                    // getConstant with the plane's hoisted material terms (Meq = m, Req = r)
-                    xd::Fc c;
-                    c.kn = P.pl_c43Eeq[w] * sqrt(r);
-                    c.vn = sqrt((4.0 * m * c.kn) / P.pl_one_b2[w]);
-                    c.ks = c.kn * P.pl_sratio[w];
-                    c.vs = c.vn * P.pl_sratio[w];
-                    c.mu = P.pl_fric[w];
-                    if (HIST) {
-                        Fn = normal_force(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit);
-                        d3 d;
-                        int sl = -1;
-                        if (HIST == 1) sl = hist_slot(ht, hs, i, kHistPlane | (unsigned)w, d);
-                        else hist_peek(ht, i, kHistPlane | (unsigned)w, d);
-                        hist_tangential(c, 0.0, dv, unit, P.dt, Fn, d, Ft, Mo);
-                        if (HIST == 1) hist_store(ht, sl, i, d);
-                    } else {
-                        dhs(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit, P.dt, Ft, Fn, Mo);
-                    }
-                }
-                f += Fn + Ft;
-            }
-            F.x += (float)f.x;
-            F.y += (float)f.y;
-            F.z += (float)f.z;
-        }
-        // triangles in reach: particle_polygonObject_collision_kernel<1>
-        // (impl:923-1021) in FP64, the normal from the face winding, the wall
-        // velocity of the body at the contact point, no particle moment (ir = 0
-        // as the reference calls DHSModel); Ft persists across triangles.  The
-        // reaction on each body accumulates in this particle's own slots of rxn
-        // over the steps and is summed over particles in a fixed order when the
-        // slots are flushed (at a re-binning and at the end of a call).
-        const unsigned tc = P.ntri ? __ldg(tcount + i) : 0u;
-        if (tc) {
-            const float4 vh = __ldg(M.vh + i), vl = __ldg(M.vl + i);
-            const float4 wl = __ldg(M.wl + i), wh = __ldg(M.wh + i);
-            const double m = __ldg(mass0 + __float_as_uint(wl.w));
-            const d3 ip = mk(__ldg(M.x + i), __ldg(M.y + i), __ldg(M.z + i));
-            const double r = __ldg(M.r + i);
-            const d3 iv = mk(df_to_d(vh.x, vl.x), df_to_d(vh.y, vl.y), df_to_d(vh.z, vl.z));
-            const d3 iw = mk(df_to_d(wh.x, wl.x), df_to_d(wh.y, wl.y), df_to_d(wh.z, wl.z));
-            d3 f = mk(0, 0, 0), Ft = mk(0, 0, 0), Mo = mk(0, 0, 0);
-            const bool listed = !(tc & kIncomplete);
-            unsigned kb = 0, ke = tc;
-            if (!listed) {
-                const unsigned key = __ldg(keys + i);
-                kb = lower_bound_u(tpk, tcap, key);
-                ke = lower_bound_u(tpk, tcap, key + 1u);
-            }
-            for (unsigned k = kb; k < ke; ++k) {
-                const unsigned t = listed ? __ldg(tlist + (size_t)k * n + i) : __ldg(tpt + k);
-                const xd_polygon_info* tri = poly + t;
-                const unsigned b = (unsigned)__ldg(&tri->id);
-                const d3 Pv = tri_vertex(tri->P), Qv = tri_vertex(tri->Q), Rv = tri_vertex(tri->R);
-                const d3 cpt = closest_pt_triangle(Pv, Qv, Rv, ip);
-                const double cdist = r - length(ip - cpt);
-                if (!(cdist > 0)) continue;
-                const d3 po2cp = cpt - tri_vertex(pmi[b].origin);
-                d3 unit = -cross(Qv - Pv, Rv - Pv);
-                unit = unit / length(unit);
-                const d3 pvel = tri_vertex(pmi[b].vel), pom = tri_vertex(pmi[b].omega);
-                const d3 dv = P.rolling ? (pvel + cross(pom, po2cp)) - (iv + cross(iw, r * unit)) : (pvel - iv);
+            PlaneD pe = load_plane(planes + w);
+            d3 Fn = mk(0, 0, 0), Ft = mk(0, 0, 0), Mo = mk(0, 0, 0);
+            d3 dp = ip - pe.xw;
+            d3 unit = mk(0, 0, 0);
+            d3 wp = mk(dot(dp, pe.u1), dot(dp, pe.u2), dot(dp, pe.uw));
+            double cdist = plane_detection(pe, ip, wp, unit, r);
+            if (cdist > 0) {
+                d3 dv = P.rolling ? -(iv + cross(iw, r * unit)) : -iv;
+                // getConstant with the plane's hoisted material terms (Meq = m, Req = r)
                 xd::Fc c;
-                c.kn = P.pb_c43Eeq[b] * sqrt(r);
-                c.vn = sqrt((4.0 * m * c.kn) / P.pb_one_b2[b]);
-                c.ks = c.kn * P.pb_sratio[b];
-                c.vs = c.vn * P.pb_sratio[b];
-                c.mu = P.pb_fric[b];
-                d3 Fn = mk(0, 0, 0);
+                c.kn = P.pl_c43Eeq[w] * sqrt(r);
+                c.vn = sqrt((4.0 * m * c.kn) / P.pl_one_b2[w]);
+                c.ks = c.kn * P.pl_sratio[w];
+                c.vs = c.vn * P.pl_sratio[w];
+                c.mu = P.pl_fric[w];
                 if (HIST) {
                     Fn = normal_force(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit);
                     d3 d;
                     int sl = -1;
-                    if (HIST == 1) sl = hist_slot(ht, hs, i, kHistTri | t, d);
-                    else hist_peek(ht, i, kHistTri | t, d);
+                    if (HIST == 1) sl = hist_slot(ht, hs, i, kHistPlane | (unsigned)w, d);
+                    else hist_peek(ht, i, kHistPlane | (unsigned)w, d);
                     hist_tangential(c, 0.0, dv, unit, P.dt, Fn, d, Ft, Mo);
                     if (HIST == 1) hist_store(ht, sl, i, d);
                 } else {
                     dhs(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit, P.dt, Ft, Fn, Mo);
                 }
-                const d3 fc = Fn + Ft;
-                f += fc;
-                const d3 rm = -cross(po2cp, fc);
-                if (rxn_on) {
-                    double* rb = rxn + (size_t)b * 6 * n + i;
-                    rb[0] -= fc.x;
-                    rb[n] -= fc.y;
-                    rb[2 * (size_t)n] -= fc.z;
-                    rb[3 * (size_t)n] += rm.x;
-                    rb[4 * (size_t)n] += rm.y;
-                    rb[5 * (size_t)n] += rm.z;
-                }
             }
-            F.x += (float)f.x;
-            F.y += (float)f.y;
-            F.z += (float)f.z;
+            f += Fn + Ft;
         }
-        if (HIST == 1) hist_end_all(ht, hs, i);
-        Fc[i] = F;
-        Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
-        if (RECORD) rec_count[i] = nc;
+        F.x += (float)f.x;
+        F.y += (float)f.y;
+        F.z += (float)f.z;
     }
+    // triangles in reach: particle_polygonObject_collision_kernel<1>
+    // (impl:923-1021) in FP64, the normal from the face winding, the wall
+    // velocity of the body at the contact point, no particle moment (ir = 0
+    // as the reference calls DHSModel); Ft persists across triangles.  The
+    // reaction on each body accumulates in this particle's own slots of rxn
+    // over the steps and is summed over particles in a fixed order when the
+    // slots are flushed (at a re-binning and at the end of a call).
+    const unsigned tc = P.ntri ? __ldg(tcount + i) : 0u;
+    if (tc) {
+        const float4 vh = __ldg(M.vh + i), vl = __ldg(M.vl + i);
+        const float4 wl = __ldg(M.wl + i), wh = __ldg(M.wh + i);
+        const double m = __ldg(mass0 + __float_as_uint(wl.w));
+        const d3 ip = mk(__ldg(M.x + i), __ldg(M.y + i), __ldg(M.z + i));
+        const double r = __ldg(M.r + i);
+        const d3 iv = mk(df_to_d(vh.x, vl.x), df_to_d(vh.y, vl.y), df_to_d(vh.z, vl.z));
+        const d3 iw = mk(df_to_d(wh.x, wl.x), df_to_d(wh.y, wl.y), df_to_d(wh.z, wl.z));
+        d3 f = mk(0, 0, 0), Ft = mk(0, 0, 0), Mo = mk(0, 0, 0);
+        const bool listed = !(tc & kIncomplete);
+        unsigned kb = 0, ke = tc;
+        if (!listed) {
+            const unsigned key = __ldg(keys + i);
+            kb = lower_bound_u(tpk, tcap, key);
+            ke = lower_bound_u(tpk, tcap, key + 1u);
+        }
+        for (unsigned k = kb; k < ke; ++k) {
+            const unsigned t = listed ? __ldg(tlist + (size_t)k * n + i) : __ldg(tpt + k);
+            const xd_polygon_info* tri = poly + t;
+            const unsigned b = (unsigned)__ldg(&tri->id);
+            const d3 Pv = tri_vertex(tri->P), Qv = tri_vertex(tri->Q), Rv = tri_vertex(tri->R);
+            const d3 cpt = closest_pt_triangle(Pv, Qv, Rv, ip);
+            const double cdist = r - length(ip - cpt);
+            if (!(cdist > 0)) continue;
+            const d3 po2cp = cpt - tri_vertex(pmi[b].origin);
+            d3 unit = -cross(Qv - Pv, Rv - Pv);
+            unit = unit / length(unit);
+            const d3 pvel = tri_vertex(pmi[b].vel), pom = tri_vertex(pmi[b].omega);
+            const d3 dv = P.rolling ? (pvel + cross(pom, po2cp)) - (iv + cross(iw, r * unit)) : (pvel - iv);
+            xd::Fc c;
+            c.kn = P.pb_c43Eeq[b] * sqrt(r);
+            c.vn = sqrt((4.0 * m * c.kn) / P.pb_one_b2[b]);
+            c.ks = c.kn * P.pb_sratio[b];
+            c.vs = c.vn * P.pb_sratio[b];
+            c.mu = P.pb_fric[b];
+            d3 Fn = mk(0, 0, 0);
+            if (HIST) {
+                Fn = normal_force(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit);
+                d3 d;
+                int sl = -1;
+                if (HIST == 1) sl = hist_slot(ht, hs, i, kHistTri | t, d);
+                else hist_peek(ht, i, kHistTri | t, d);
+                hist_tangential(c, 0.0, dv, unit, P.dt, Fn, d, Ft, Mo);
+                if (HIST == 1) hist_store(ht, sl, i, d);
+            } else {
+                dhs(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit, P.dt, Ft, Fn, Mo);
+            }
+            const d3 fc = Fn + Ft;
+            f += fc;
+            const d3 rm = -cross(po2cp, fc);
+            if (rxn_on) {
+                double* rb = rxn + (size_t)b * 6 * n + i;
+                rb[0] -= fc.x;
+                rb[n] -= fc.y;
+                rb[2 * (size_t)n] -= fc.z;
+                rb[3 * (size_t)n] += rm.x;
+                rb[4 * (size_t)n] += rm.y;
+                rb[5 * (size_t)n] += rm.z;
+            }
+        }
+        F.x += (float)f.x;
+        F.y += (float)f.y;
+        F.z += (float)f.z;
+    }
+    if (HIST == 1) hist_end_all(ht, hs, i);
+    Fc[i] = F;
+    Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
+    if (RECORD) rec_count[i] = nc;
+}
+
+template <bool RECORD, int HIST>
+__global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, ContactArgs C)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) C.counters[CN_REBUILD] = 0;
+    const unsigned total = C.counters[CN_HEAVY];
+    // runs of 32 consecutive list entries (neighbouring slots) go to the warps
+    // of all blocks in turn: every SM gets an equal share however short the list
+    const unsigned warps = gridDim.x * (blockDim.x / 32u);
+    const unsigned gw = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u;
+    for (unsigned t = gw * 32u + (threadIdx.x & 31u); t < total; t += warps * 32u)
+        contact_entry<RECORD, HIST>(P, C, __ldg(C.hlist + t));
 }
 
 // Body reactions: rxn[(b * 6 + q) * n + i] summed over i in a fixed order,
@@ -2166,6 +2225,41 @@ static int capture_conditional(MixedScene* s, cudaStream_t q, cudaGraphCondition
 // a particle has left its skin (or the cells are not set up), then the
 // contact forces.  cond: the conditional handle when capturing into a graph
 // (nullptr for direct launches, where the host reads the flag).
+static ContactArgs contact_args(MixedScene* s, unsigned* rc, unsigned* rp, unsigned rec_cap, const HistTable& ht,
+                                int rxn_on)
+{
+    ContactArgs C;
+    C.M = s->m[0];
+    C.pf = s->pf;
+    C.qa = s->qa;
+    C.qb = s->qb;
+    C.keys = s->prev_keys;
+    C.lb = s->lb;
+    C.vcount = s->vcount;
+    C.vlist = s->vlist;
+    C.hlist = s->hlist;
+    C.wmask = s->wmask;
+    C.planes = s->planes;
+    C.mass0 = s->mass0;
+    C.poly = s->poly;
+    C.pmi = s->pmi;
+    C.tcount = s->tcount;
+    C.tlist = s->tlist;
+    C.tpk = s->tpk_sorted;
+    C.tpt = s->tpt_sorted;
+    C.tcap = s->tpair_cap;
+    C.rxn = s->rxn;
+    C.Fc = s->Fc;
+    C.Mc = s->Mc;
+    C.counters = s->counters;
+    C.rec_count = rc;
+    C.rec_pairs = rp;
+    C.rec_cap = rec_cap;
+    C.ht = ht;
+    C.rxn_on = rxn_on;
+    return C;
+}
+
 template <int MODE>
 static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool record, unsigned rec_cap,
                      const cudaGraphConditionalHandle* cond)
@@ -2221,13 +2315,8 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
         rc = s->rec_count;
         rp = s->rec_pairs;
     }
-#define XD_MX_CONTACT(REC, H)                                                                                   \
-    k_mx_contact<REC, H><<<grid, kContactThreads, 0, q>>>(s->P, M, s->pf, s->qa, s->qb, s->prev_keys, s->lb,     \
-                                                          s->vcount, s->vlist, s->hlist, s->wmask, s->planes,    \
-                                                          s->cps, s->mass0, s->poly, s->pmi, s->tcount, s->tlist, \
-                                                          s->tpk_sorted, s->tpt_sorted, s->tpair_cap, s->rxn,   \
-                                                          s->Fc, s->Mc, s->counters, rc, rp, record ? rec_cap : 0u, ht, \
-                                                          MODE == 3 ? 0 : 1)
+    const ContactArgs C = contact_args(s, rc, rp, record ? rec_cap : 0u, ht, MODE == 3 ? 0 : 1);
+#define XD_MX_CONTACT(REC, H) k_mx_contact<REC, H><<<grid, kContactThreads, 0, q>>>(s->P, C)
     if (record) {
         if (hist == 2) XD_MX_CONTACT(true, 2);
         else if (hist == 1) XD_MX_CONTACT(true, 1);
@@ -2255,6 +2344,7 @@ constexpr unsigned kGraphMinSteps = 16;
 
 static void destroy_graphs(MixedScene* s)
 {
+    ++s->version;   // batches holding this scene capture it again
     for (int k = 0; k < kGraphKinds; ++k)
         if (s->graph[k]) {
             cudaGraphExecDestroy(s->graph[k]);
@@ -2624,6 +2714,447 @@ int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q)
     out[2] = c[CN_NORMALS];
     out[3] = c[CN_SLIPS];
     return st;
+}
+
+// ---- batches: many mixed scenes advanced by shared launches ----------------
+//
+// A step of a batch is one graph: one advance launch over every scene's
+// slots, one decision kernel that reads each scene's re-binning flag, a
+// conditional node per group of kBatchGroup scenes whose body holds a
+// conditional re-binning per scene of the group, and one contact launch over
+// every scene's listed particles.  Each scene runs the same per-slot code as
+// when stepped alone (advance_one, rebuild, contact_entry, finish_one), so its
+// results are the same bits; what changes is that a step costs a handful of
+// graph nodes instead of three per scene (a conditional node costs a few
+// microseconds of the GPU's front end whether or not its body runs).
+
+namespace {
+
+constexpr unsigned kBatchGroup = 16;
+constexpr unsigned kBatchContactBlocks = 152 * 8;
+
+// One scene of a batch as the batch kernels read it.
+struct BatchScene {
+    MixParams P;
+    ContactArgs C;
+    const float4* pref;
+    float4* pf;
+    longlong2* qa;
+    longlong2* qb;
+    unsigned adv_block0;   // first block of this scene in the advance grid
+};
+
+// per-warp copy of the scene a warp of the contact launch works on
+struct WarpScene {
+    MixParams P;
+    ContactArgs C;
+};
+
+__device__ __forceinline__ void copy_words(void* dst, const void* src, unsigned bytes, unsigned t, unsigned nt)
+{
+    const unsigned* a = static_cast<const unsigned*>(src);
+    unsigned* b = static_cast<unsigned*>(dst);
+    for (unsigned k = t; k < bytes / 4u; k += nt) b[k] = __ldg(a + k);
+}
+
+// MODE 0: drift; MODE 1: kick then drift; MODE 2: kick only (the finish).
+template <int MODE>
+__global__ void __launch_bounds__(256) k_batch_advance(const BatchScene* __restrict__ D,
+                                                       const unsigned* __restrict__ block_scene, unsigned nblocks)
+{
+    __shared__ MixParams sP;
+    if (blockIdx.x >= nblocks) return;
+    const unsigned sc = __ldg(block_scene + blockIdx.x);
+    const BatchScene& d = D[sc];
+    copy_words(&sP, &d.P, sizeof(MixParams), threadIdx.x, blockDim.x);
+    __syncthreads();
+    const unsigned i = (blockIdx.x - d.adv_block0) * blockDim.x + threadIdx.x;
+    if (MODE == 2) {
+        if (i < sP.n) finish_one(sP, d.C.M, d.C.Fc, d.C.Mc, i);
+        return;
+    }
+    const bool out = i < sP.n && advance_one<MODE>(sP, d.C.M, d.C.Fc, d.C.Mc, d.pref, d.pf, d.qa, d.qb, i);
+    if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31u) == 0) atomicOr(d.C.counters + CN_REBUILD, 1u);
+}
+
+// Each scene's re-binning flag into flags[] (and cleared for the next step);
+// the groups with a flagged scene open their conditional node.
+__global__ void __launch_bounds__(256) k_batch_decide(const BatchScene* __restrict__ D, unsigned ns,
+                                                      unsigned* __restrict__ flags,
+                                                      const cudaGraphConditionalHandle* __restrict__ hg)
+{
+    __shared__ unsigned any[256];
+    const unsigned ng = (ns + kBatchGroup - 1u) / kBatchGroup;
+    for (unsigned g = threadIdx.x; g < 256u; g += blockDim.x) any[g] = 0;
+    __syncthreads();
+    for (unsigned sc = threadIdx.x; sc < ns; sc += blockDim.x) {
+        unsigned* c = D[sc].C.counters;
+        const unsigned f = c[CN_REBUILD] ? 1u : 0u;
+        c[CN_REBUILD] = 0;
+        flags[sc] = f;
+        if (f) atomicOr(&any[(sc / kBatchGroup) & 255u], 1u);
+    }
+    __syncthreads();
+    for (unsigned g = threadIdx.x; g < ng && g < 256u; g += blockDim.x)
+        if (any[g]) cudaGraphSetConditional(hg[g], 1u);
+}
+
+// Inside a group's body: the flagged scenes of the group open their re-binning.
+__global__ void k_batch_group(const unsigned* __restrict__ flags, unsigned first, unsigned count,
+                              const cudaGraphConditionalHandle* __restrict__ hs)
+{
+    const unsigned t = threadIdx.x;
+    if (t < count && flags[first + t]) cudaGraphSetConditional(hs[first + t], 1u);
+}
+
+// Runs of 32 listed particles per scene, as an exclusive prefix over scenes.
+__global__ void __launch_bounds__(1024) k_batch_chunks(const BatchScene* __restrict__ D, unsigned ns,
+                                                       unsigned* __restrict__ chunk_start)
+{
+    __shared__ unsigned c[1024];
+    __shared__ unsigned carry;
+    if (threadIdx.x == 0) carry = 0;
+    for (unsigned base = 0; base < ns; base += 1024u) {
+        const unsigned sc = base + threadIdx.x;
+        const unsigned h = sc < ns ? D[sc].C.counters[CN_HEAVY] : 0u;
+        c[threadIdx.x] = (h + 31u) / 32u;
+        __syncthreads();
+        // inclusive scan (Hillis-Steele)
+        for (unsigned off = 1; off < 1024u; off <<= 1) {
+            const unsigned v = threadIdx.x >= off ? c[threadIdx.x - off] : 0u;
+            __syncthreads();
+            c[threadIdx.x] += v;
+            __syncthreads();
+        }
+        if (sc < ns) chunk_start[sc + 1] = carry + c[threadIdx.x];
+        __syncthreads();
+        if (threadIdx.x == 0) carry += c[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) chunk_start[0] = 0;
+}
+
+// The contact pass of every scene: the warps share the runs of all scenes'
+// lists in contiguous ranges; a warp loads the scene of a run into its own
+// shared-memory slot when the scene changes.
+__global__ void __launch_bounds__(kContactThreads) k_batch_contact(const BatchScene* __restrict__ D, unsigned ns,
+                                                                   const unsigned* __restrict__ chunk_start)
+{
+    __shared__ WarpScene ws[kContactThreads / 32];
+    const unsigned lane = threadIdx.x & 31u, wb = threadIdx.x / 32u;
+    WarpScene& W = ws[wb];
+    const unsigned warps = gridDim.x * (kContactThreads / 32u);
+    const unsigned gw = blockIdx.x * (kContactThreads / 32u) + wb;
+    const unsigned total = __ldg(chunk_start + ns);
+    const unsigned per = (total + warps - 1u) / warps;
+    const unsigned c0 = gw * per, c1 = min(total, c0 + per);
+    unsigned cur = 0xffffffffu, lo = 0, heavy = 0;
+    for (unsigned ch = c0; ch < c1; ++ch) {
+        if (cur == 0xffffffffu || ch >= __ldg(chunk_start + cur + 1)) {
+            // the scene holding run ch: the last s with chunk_start[s] <= ch
+            unsigned a = 0, b = ns;
+            while (b - a > 1u) {
+                const unsigned m = (a + b) / 2u;
+                if (__ldg(chunk_start + m) <= ch) a = m;
+                else b = m;
+            }
+            cur = a;
+            lo = __ldg(chunk_start + cur);
+            __syncwarp();
+            copy_words(&W.P, &D[cur].P, sizeof(MixParams), lane, 32u);
+            copy_words(&W.C, &D[cur].C, sizeof(ContactArgs), lane, 32u);
+            __syncwarp();
+            heavy = W.C.counters[CN_HEAVY];
+        }
+        const unsigned t = (ch - lo) * 32u + lane;
+        if (t < heavy) contact_entry<false, 0>(W.P, W.C, __ldg(W.C.hlist + t));
+    }
+}
+
+}  // namespace
+
+struct MixedBatch {
+    std::vector<MixedScene*> scenes;
+    std::vector<unsigned> versions;
+    BatchScene* d_scenes = nullptr;
+    unsigned* d_block_scene = nullptr;
+    unsigned nblocks = 0;
+    unsigned* d_flags = nullptr;
+    unsigned* d_chunks = nullptr;
+    cudaGraphConditionalHandle* d_handles[2] = {};   // per step kind: groups, then scenes
+    cudaGraphExec_t step_graph[2] = {};              // 0: first step of a call (drift), 1: later steps
+    cudaGraphExec_t finish_graph = nullptr;          // last kick and the body reactions
+    bool captured = false;
+};
+
+namespace {
+
+void free_batch_graphs(MixedBatch* b)
+{
+    for (auto& g : b->step_graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    if (b->finish_graph) cudaGraphExecDestroy(b->finish_graph);
+    b->finish_graph = nullptr;
+    for (auto& h : b->d_handles)
+        if (h) {
+            cudaFree(h);
+            h = nullptr;
+        }
+    for (void* p : { (void*)b->d_scenes, (void*)b->d_block_scene, (void*)b->d_flags, (void*)b->d_chunks })
+        if (p) cudaFree(p);
+    b->d_scenes = nullptr;
+    b->d_block_scene = nullptr;
+    b->d_flags = nullptr;
+    b->d_chunks = nullptr;
+    b->captured = false;
+}
+
+// A conditional (if) node in graph g after deps; its body is captured from
+// what body(stream, body_graph) launches.
+template <typename Body>
+int add_conditional(cudaGraph_t g, const cudaGraphNode_t* deps, size_t nd, cudaGraphConditionalHandle h, Body body,
+                    cudaGraphNode_t* node)
+{
+    cudaGraphNodeParams np = { cudaGraphNodeTypeConditional };
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    int st = cuda_status(cudaGraphAddNode(node, g, deps, nullptr, nd, &np), "batch conditional node");
+    if (st != XD_OK) return st;
+    cudaGraph_t bg = np.conditional.phGraph_out[0];
+    cudaStream_t bs = nullptr;
+    st = cuda_status(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking), "batch conditional stream");
+    if (st != XD_OK) return st;
+    st = cuda_status(cudaStreamBeginCaptureToGraph(bs, bg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+                     "batch conditional capture");
+    if (st == XD_OK) {
+        const int r = body(bs, bg);
+        cudaGraph_t out = nullptr;
+        st = cuda_status(cudaStreamEndCapture(bs, &out), "batch conditional capture");
+        if (r != XD_OK) st = r;
+    }
+    cudaStreamDestroy(bs);
+    return st;
+}
+
+int current_deps(cudaStream_t q, cudaGraph_t* g, std::vector<cudaGraphNode_t>* deps)
+{
+    cudaStreamCaptureStatus cst;
+    const cudaGraphNode_t* d = nullptr;
+    size_t nd = 0;
+    int st = cuda_status(cudaStreamGetCaptureInfo(q, &cst, nullptr, g, &d, nullptr, &nd), "batch capture info");
+    if (st == XD_OK) deps->assign(d, d + nd);
+    return st;
+}
+
+// One batch step graph: advance, decision, the groups' conditional
+// re-binnings (side by side), run prefix, contact.
+int capture_batch_step(MixedBatch* b, int mode)
+{
+    const unsigned ns = (unsigned)b->scenes.size();
+    const unsigned ng = (ns + kBatchGroup - 1) / kBatchGroup;
+    std::vector<cudaGraphConditionalHandle> h(ng + ns, 0);
+    cudaStream_t cs = nullptr;
+    int st = cuda_status(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "batch capture stream");
+    if (st != XD_OK) return st;
+    st = cuda_status(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "batch capture");
+    cudaGraph_t cg = nullptr;
+    std::vector<cudaGraphNode_t> deps;
+    if (st == XD_OK) st = current_deps(cs, &cg, &deps);
+    for (unsigned g = 0; g < ng && st == XD_OK; ++g)
+        st = cuda_status(cudaGraphConditionalHandleCreate(&h[g], cg, 0, cudaGraphCondAssignDefault),
+                         "batch conditional handle");
+    if (st == XD_OK) {
+        if (mode == 0)
+            k_batch_advance<0><<<b->nblocks, 256, 0, cs>>>(b->d_scenes, b->d_block_scene, b->nblocks);
+        else
+            k_batch_advance<1><<<b->nblocks, 256, 0, cs>>>(b->d_scenes, b->d_block_scene, b->nblocks);
+        k_batch_decide<<<1, 256, 0, cs>>>(b->d_scenes, ns, b->d_flags, b->d_handles[mode]);
+        st = launch_status("batch advance");
+    }
+    if (st == XD_OK) st = current_deps(cs, &cg, &deps);
+    std::vector<cudaGraphNode_t> groups(ng, nullptr);
+    for (unsigned g = 0; g < ng && st == XD_OK; ++g) {
+        const unsigned first = g * kBatchGroup, count = std::min(kBatchGroup, ns - first);
+        auto group_body = [&](cudaStream_t bs, cudaGraph_t bg) {
+            int r = XD_OK;
+            for (unsigned k = 0; k < count && r == XD_OK; ++k)
+                r = cuda_status(cudaGraphConditionalHandleCreate(&h[ng + first + k], bg, 0, cudaGraphCondAssignDefault),
+                                "batch conditional handle");
+            if (r != XD_OK) return r;
+            k_batch_group<<<1, 32, 0, bs>>>(b->d_flags, first, count, b->d_handles[mode] + ng);
+            r = launch_status("batch group");
+            cudaGraph_t bgc = nullptr;
+            std::vector<cudaGraphNode_t> gd;
+            if (r == XD_OK) r = current_deps(bs, &bgc, &gd);
+            for (unsigned k = 0; k < count && r == XD_OK; ++k) {
+                MixedScene* sc = b->scenes[first + k];
+                cudaGraphNode_t node = nullptr;
+                r = add_conditional(bgc, gd.data(), gd.size(), h[ng + first + k],
+                                    [sc](cudaStream_t rs, cudaGraph_t) { return rebuild(sc, rs); }, &node);
+            }
+            return r;
+        };
+        st = add_conditional(cg, deps.data(), deps.size(), h[g], group_body, &groups[g]);
+    }
+    if (st == XD_OK && ng)
+        st = cuda_status(cudaStreamUpdateCaptureDependencies(cs, groups.data(), nullptr, ng,
+                                                             cudaStreamSetCaptureDependencies),
+                         "batch capture dependencies");
+    if (st == XD_OK) {
+        k_batch_chunks<<<1, 1024, 0, cs>>>(b->d_scenes, ns, b->d_chunks);
+        k_batch_contact<<<kBatchContactBlocks, kContactThreads, 0, cs>>>(b->d_scenes, ns, b->d_chunks);
+        st = launch_status("batch contact");
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(cs, &graph);
+    if (st == XD_OK) st = cuda_status(e, "batch capture");
+    if (st == XD_OK) st = cuda_status(cudaGraphInstantiate(&b->step_graph[mode], graph, 0), "batch graph instantiate");
+    if (graph) cudaGraphDestroy(graph);
+    if (st == XD_OK)
+        st = cuda_status(cudaMemcpy(b->d_handles[mode], h.data(), sizeof(cudaGraphConditionalHandle) * h.size(),
+                                    cudaMemcpyHostToDevice), "batch handles");
+    if (st == XD_OK) st = cuda_status(cudaGraphUpload(b->step_graph[mode], cs), "batch graph upload");
+    if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(cs), "batch graph upload");
+    cudaStreamDestroy(cs);
+    return st;
+}
+
+int capture_batch_finish(MixedBatch* b)
+{
+    cudaStream_t cs = nullptr;
+    int st = cuda_status(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "batch capture stream");
+    if (st != XD_OK) return st;
+    st = cuda_status(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "batch capture");
+    if (st == XD_OK) {
+        k_batch_advance<2><<<b->nblocks, 256, 0, cs>>>(b->d_scenes, b->d_block_scene, b->nblocks);
+        st = launch_status("batch finish");
+    }
+    for (size_t k = 0; k < b->scenes.size() && st == XD_OK; ++k) st = flush_reactions(b->scenes[k], cs);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(cs, &graph);
+    if (st == XD_OK) st = cuda_status(e, "batch capture");
+    if (st == XD_OK) st = cuda_status(cudaGraphInstantiate(&b->finish_graph, graph, 0), "batch graph instantiate");
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    return st;
+}
+
+// Device descriptors of the scenes as they are now, and the step graphs.
+int prepare_batch(MixedBatch* b)
+{
+    free_batch_graphs(b);
+    const unsigned ns = (unsigned)b->scenes.size();
+    std::vector<BatchScene> hs(ns);
+    std::vector<unsigned> block_scene;
+    for (unsigned k = 0; k < ns; ++k) {
+        MixedScene* sc = b->scenes[k];
+        BatchScene& d = hs[k];
+        memset(&d, 0, sizeof(d));
+        d.P = sc->P;
+        d.C = contact_args(sc, nullptr, nullptr, 0u, history_table(sc), 1);
+        d.pref = sc->pref;
+        d.pf = sc->pf;
+        d.qa = sc->qa;
+        d.qb = sc->qb;
+        d.adv_block0 = (unsigned)block_scene.size();
+        block_scene.insert(block_scene.end(), blocks(sc->n, 256), k);
+    }
+    b->nblocks = (unsigned)block_scene.size();
+    const unsigned ng = (ns + kBatchGroup - 1) / kBatchGroup;
+    int st = XD_OK;
+    auto M = [&](auto** p, size_t count, const char* what) {
+        if (st == XD_OK) st = cuda_status(cudaMalloc(p, sizeof(**p) * (count ? count : 1)), what);
+    };
+    M(&b->d_scenes, ns, "batch scenes");
+    M(&b->d_block_scene, block_scene.size(), "batch blocks");
+    M(&b->d_flags, ns, "batch flags");
+    M(&b->d_chunks, ns + 1, "batch runs");
+    M(&b->d_handles[0], ng + ns, "batch handles");
+    M(&b->d_handles[1], ng + ns, "batch handles");
+    if (st == XD_OK)
+        st = cuda_status(cudaMemcpy(b->d_block_scene, block_scene.data(), sizeof(unsigned) * block_scene.size(),
+                                    cudaMemcpyHostToDevice), "batch blocks");
+    if (st == XD_OK) st = capture_batch_step(b, 0);
+    if (st == XD_OK) st = capture_batch_step(b, 1);
+    if (st == XD_OK) st = capture_batch_finish(b);
+    // the descriptors after the captures: capturing a re-binning fixes the
+    // triangle sort's output buffers of a scene that has not re-binned yet
+    for (unsigned k = 0; k < ns && st == XD_OK; ++k) {
+        MixedScene* sc = b->scenes[k];
+        hs[k].C.tpk = sc->tpk_sorted;
+        hs[k].C.tpt = sc->tpt_sorted;
+    }
+    if (st == XD_OK)
+        st = cuda_status(cudaMemcpy(b->d_scenes, hs.data(), sizeof(BatchScene) * ns, cudaMemcpyHostToDevice),
+                         "batch scenes");
+    if (st != XD_OK) {
+        free_batch_graphs(b);
+        return st;
+    }
+    b->versions.resize(ns);
+    for (unsigned k = 0; k < ns; ++k) b->versions[k] = b->scenes[k]->version;
+    b->captured = true;
+    return XD_OK;
+}
+
+}  // namespace
+
+int mixed_batch_create(MixedScene* const* scenes, unsigned count, MixedBatch** out)
+{
+    *out = nullptr;
+    if (count == 0 || count > 256u * kBatchGroup)
+        return set_error(XD_ERR_INVALID, "batch: 1 to %u scenes", 256u * kBatchGroup);
+    for (unsigned k = 0; k < count; ++k) {
+        const MixedScene* sc = scenes[k];
+        if (!sc->ready) return set_error(XD_ERR_STATE, "batch: scene %u has no state uploaded", k);
+        if (sc->hslots) return set_error(XD_ERR_STATE, "batch: scene %u keeps tangential history", k);
+        if (sc->kinematic) return set_error(XD_ERR_STATE, "batch: scene %u has kinematic bodies", k);
+        for (unsigned j = 0; j < k; ++j)
+            if (scenes[j] == sc) return set_error(XD_ERR_INVALID, "batch: scene %u given twice", k);
+    }
+    MixedBatch* b = new (std::nothrow) MixedBatch();
+    if (!b) return set_error(XD_ERR_NOMEM, "batch: host allocation");
+    b->scenes.assign(scenes, scenes + count);
+    *out = b;
+    return XD_OK;
+}
+
+void mixed_batch_destroy(MixedBatch* b)
+{
+    if (!b) return;
+    free_batch_graphs(b);
+    delete b;
+}
+
+int mixed_batch_step(MixedBatch* b, unsigned nsteps, cudaStream_t q)
+{
+    if (nsteps == 0) return XD_OK;
+    bool stale = !b->captured;
+    for (size_t k = 0; k < b->scenes.size() && !stale; ++k) stale = b->versions[k] != b->scenes[k]->version;
+    int st = XD_OK;
+    if (stale) {
+        st = cuda_status(cudaStreamSynchronize(q), "batch");   // graphs in flight finish first
+        if (st == XD_OK) st = prepare_batch(b);
+        if (st != XD_OK) return st;
+    }
+    for (MixedScene* sc : b->scenes) {
+        if (!sc->ready) return set_error(XD_ERR_STATE, "batch: a scene has no state uploaded");
+        st = update_mesh(sc, q);
+        if (st == XD_OK && !sc->cells_clean)
+            st = cuda_status(cudaMemsetAsync(sc->counters + CN_REBUILD, 1, 1, q), "batch re-binning flag");
+        if (st != XD_OK) return st;
+    }
+    st = cuda_status(cudaGraphLaunch(b->step_graph[0], q), "batch graph launch");
+    for (unsigned t = 1; t < nsteps && st == XD_OK; ++t)
+        st = cuda_status(cudaGraphLaunch(b->step_graph[1], q), "batch graph launch");
+    if (st == XD_OK) st = cuda_status(cudaGraphLaunch(b->finish_graph, q), "batch graph launch");
+    if (st != XD_OK) return st;
+    for (MixedScene* sc : b->scenes) sc->cells_clean = true;
+    return XD_OK;
 }
 
 }  // namespace xd

@@ -40,6 +40,14 @@ int mixed_set_kinematic(MixedScene* s, bool enable);
 // particle back in id order (when the emitter is set).
 int mixed_set_active(MixedScene* s, unsigned active, bool restore, cudaStream_t q);
 unsigned mixed_active(MixedScene* s);
+
+// Batches: scenes advanced together by shared launches, each with the results
+// it has when stepped alone.  Scenes with history or kinematic bodies are not
+// batched.
+struct MixedBatch;
+int mixed_batch_create(MixedScene* const* scenes, unsigned count, MixedBatch** out);
+void mixed_batch_destroy(MixedBatch* b);
+int mixed_batch_step(MixedBatch* b, unsigned nsteps, cudaStream_t q);
 int mixed_download_history(MixedScene* s, unsigned* keys, double* delta, unsigned long long* overflow,
                            cudaStream_t q);
 int mixed_set_bodies(MixedScene* s, const xd_polygon_mass_info* pmi, cudaStream_t q);

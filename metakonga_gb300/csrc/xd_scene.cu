@@ -846,6 +846,53 @@ int xd_scene_step_many(xd_scene* const* scenes, const unsigned* nsteps, unsigned
     return st;
 }
 
+struct xd_batch {
+    MixedBatch* mixed = nullptr;
+};
+
+int xd_batch_create(xd_scene* const* scenes, unsigned count, xd_batch** out)
+{
+    if (!scenes || !out) return set_error(XD_ERR_INVALID, "batch_create: null argument");
+    *out = nullptr;
+    std::vector<MixedScene*> ms(count);
+    for (unsigned k = 0; k < count; ++k) {
+        xd_scene* s = scenes[k];
+        if (!s) return set_error(XD_ERR_INVALID, "batch_create: null scene %u", k);
+        if (!s->mixed) return set_error(XD_ERR_STATE, "batch_create: scene %u is not in the mixed form", k);
+        if (s->emit_period || s->active != s->np)
+            return set_error(XD_ERR_STATE, "batch_create: scene %u has an emitter", k);
+        ms[k] = s->mixed;
+    }
+    MixedBatch* b = nullptr;
+    int st = mixed_batch_create(ms.data(), count, &b);
+    if (st != XD_OK) return st;
+    xd_batch* h = new (std::nothrow) xd_batch();
+    if (!h) {
+        mixed_batch_destroy(b);
+        return set_error(XD_ERR_NOMEM, "batch_create: host allocation");
+    }
+    h->mixed = b;
+    *out = h;
+    return XD_OK;
+}
+
+int xd_batch_step(xd_batch* b, unsigned nsteps, int check, void* stream)
+{
+    if (!b) return set_error(XD_ERR_INVALID, "batch_step: null batch");
+    cudaStream_t q = static_cast<cudaStream_t>(stream);
+    int st = mixed_batch_step(b->mixed, nsteps, q);
+    if (st == XD_OK && check) st = cuda_status(cudaStreamSynchronize(q), "batch_step");
+    return st;
+}
+
+int xd_batch_destroy(xd_batch* b)
+{
+    if (!b) return XD_OK;
+    mixed_batch_destroy(b->mixed);
+    delete b;
+    return XD_OK;
+}
+
 int xd_scene_device_bytes(xd_scene* s, unsigned long long* bytes)
 {
     if (!s || !bytes) return set_error(XD_ERR_INVALID, "scene_device_bytes: null argument");

@@ -250,3 +250,33 @@ def step_many(scenes, nsteps, check: bool = False, stream: int = 0) -> None:
     handles = (C.c_void_p * k)(*[s.handle.value for s in scenes])
     counts = np.ascontiguousarray(nsteps, dtype=np.uint32)
     call("xd_scene_step_many", C.cast(handles, C.c_void_p), counts.ctypes.data, k, 1 if check else 0, stream)
+
+
+class Batch:
+    """Mixed-form DeviceScenes advanced together (xd_batch_*): every step of
+    every scene in one CUDA graph, each scene's result the same bits as when
+    it is stepped alone.  Close it before its scenes."""
+
+    def __init__(self, scenes):
+        self.scenes = list(scenes)
+        k = len(self.scenes)
+        if len({id(s) for s in self.scenes}) != k:
+            raise ValueError("Batch: a scene appears twice")
+        handles = (C.c_void_p * k)(*[s.handle.value for s in self.scenes])
+        out = C.c_void_p()
+        call("xd_batch_create", C.cast(handles, C.c_void_p), k, C.byref(out))
+        self.handle = out
+
+    def step(self, nsteps: int, check: bool = False, stream: int = 0) -> None:
+        call("xd_batch_step", self.handle, int(nsteps), 1 if check else 0, stream)
+
+    def close(self) -> None:
+        if self.handle:
+            call("xd_batch_destroy", self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

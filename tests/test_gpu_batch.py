@@ -1,0 +1,72 @@
+"""Batches (xd_batch_*, engine.Batch): scenes advanced together by shared
+launches give, scene by scene, the same bits as each scene stepped alone --
+particle state, re-binnings and the body reactions -- across calls of any
+length, with re-binnings inside the calls, and after a scene's walls move
+(the batch captures itself again)."""
+import numpy as np
+import pytest
+
+from metakonga_gb300 import engine, scenes
+
+from .cases import packed_scene, small_drum, small_hopper
+
+pytestmark = pytest.mark.gpu
+
+
+def _scenes():
+    rng = np.random.Generator(np.random.MT19937(41))
+    out = [small_hopper(n=1500, seed=5), scenes.hopper(n=900, seed=8), scenes.hopper(n=3000, seed=9),
+           packed_scene(n_side=6), small_drum(n=400, seed=6)]
+    for sc in out:
+        # fast enough that every scene re-bins within the calls
+        sc.vel[:] += rng.normal(0.0, 1.5, sc.vel.shape)
+    return out
+
+
+def _run(split, batched, moved=None):
+    scs = _scenes()
+    ds = [engine.DeviceScene(sc, mode=engine.MODE_MIXED) for sc in scs]
+    b = engine.Batch(ds) if batched else None
+    for c, k in enumerate(split):
+        if moved is not None and c == 1:
+            planes = scs[3].planes.copy()
+            planes[0]["xw"][2] += 2e-4
+            for f in ("w2", "w3", "w4"):
+                planes[0][f][2] += 2e-4
+            ds[3].set_planes(planes)
+        if batched:
+            b.step(k, check=True)
+        else:
+            for d in ds:
+                d.step(k, check=True)
+    out = [(d.download(), d.rebuilds()[0], d.get_bodies() if d.ntri else None) for d in ds]
+    if b:
+        b.close()
+    for d in ds:
+        d.close()
+    return out
+
+
+@pytest.mark.parametrize("moved", [None, True])
+def test_batch_equals_each_scene_alone(cuda, moved):
+    alone = _run((5, 27, 16), False, moved)
+    batch = _run((5, 27, 16), True, moved)
+    assert all(r > 1 for _, r, _ in alone), [r for _, r, _ in alone]
+    for (a, ra, ba), (b, rb, bb) in zip(alone, batch):
+        assert ra == rb
+        for k in ("pos", "vel", "omega", "acc"):
+            assert np.array_equal(a[k], b[k]), k
+        if ba is not None:
+            assert ba.tobytes() == bb.tobytes()
+
+
+def test_batch_refuses_history_and_plain_scenes(cuda):
+    sc = packed_scene(n_side=4)
+    d1 = engine.DeviceScene(sc, mode=engine.MODE_MIXED)
+    d2 = engine.DeviceScene(sc, mode=engine.MODE_FP64)
+    d1.set_tangential_history(4)
+    for group in ([d1], [d2]):
+        with pytest.raises(Exception):
+            engine.Batch(group)
+    d1.close()
+    d2.close()
