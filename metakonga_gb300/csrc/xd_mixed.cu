@@ -3033,9 +3033,29 @@ int capture_batch_finish(MixedBatch* b)
         k_batch_advance<2><<<b->nblocks, 256, 0, cs>>>(b->d_scenes, b->d_block_scene, b->nblocks);
         st = launch_status("batch finish");
     }
-    for (size_t k = 0; k < b->scenes.size() && st == XD_OK; ++k) st = flush_reactions(b->scenes[k], cs);
+    // the scenes' body reactions side by side: branches forked from the kick
+    constexpr int kBranches = 16;
+    cudaStream_t br[kBranches] = {};
+    cudaEvent_t ev[kBranches + 1] = {};
+    for (int j = 0; j < kBranches && st == XD_OK; ++j)
+        st = cuda_status(cudaStreamCreateWithFlags(&br[j], cudaStreamNonBlocking), "batch capture stream");
+    for (int j = 0; j <= kBranches && st == XD_OK; ++j)
+        st = cuda_status(cudaEventCreateWithFlags(&ev[j], cudaEventDisableTiming), "batch capture event");
+    if (st == XD_OK) st = cuda_status(cudaEventRecord(ev[kBranches], cs), "batch capture fork");
+    for (int j = 0; j < kBranches && st == XD_OK; ++j)
+        st = cuda_status(cudaStreamWaitEvent(br[j], ev[kBranches], 0), "batch capture fork");
+    for (size_t k = 0; k < b->scenes.size() && st == XD_OK; ++k)
+        st = flush_reactions(b->scenes[k], br[k % kBranches]);
+    for (int j = 0; j < kBranches && st == XD_OK; ++j) {
+        st = cuda_status(cudaEventRecord(ev[j], br[j]), "batch capture join");
+        if (st == XD_OK) st = cuda_status(cudaStreamWaitEvent(cs, ev[j], 0), "batch capture join");
+    }
     cudaGraph_t graph = nullptr;
     const cudaError_t e = cudaStreamEndCapture(cs, &graph);
+    for (int j = 0; j < kBranches; ++j)
+        if (br[j]) cudaStreamDestroy(br[j]);
+    for (int j = 0; j <= kBranches; ++j)
+        if (ev[j]) cudaEventDestroy(ev[j]);
     if (st == XD_OK) st = cuda_status(e, "batch capture");
     if (st == XD_OK) st = cuda_status(cudaGraphInstantiate(&b->finish_graph, graph, 0), "batch graph instantiate");
     if (graph) cudaGraphDestroy(graph);
