@@ -110,13 +110,14 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _traffic_from_profiles(name):
-    """Per-launch DRAM bytes of a kernel from its committed ncu summary."""
+def _traffic_from_profiles(name, key="traffic_bytes_per_launch_full_scene"):
+    """Per-launch DRAM bytes of a kernel (or another figure named by key) from
+    its committed ncu summary."""
     p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.strip().startswith("traffic_bytes_per_launch_full_scene:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].strip())
             except ValueError:
@@ -703,6 +704,32 @@ def run_batched(a):
     value = world * n_tot * a.steps / (ms / 1e3)
     rb1 = [d.rebuilds(sh) for d in ds]
     rebuilds = sum(b[0] - r[0] for r, b in zip(rb0, rb1))
+
+    # the batch's dominant kernel, timed live: the same kernels launched
+    # directly with CUDA events around each advance and contact launch
+    ksteps = max(3, min(a.steps, 20))
+    batch.set_timing(True)
+    batch.step(ksteps, check=True, stream=sh)
+    kt = batch.kernel_times()
+    batch.set_timing(False)
+    adv_ms = kt["advance"][0] / max(kt["advance"][1], 1)
+    con_ms = kt["contact"][0] / max(kt["contact"][1], 1)
+    peak, peak_kind = _peaks()
+    tpp = _traffic_from_profiles("advance_batch_hopper.md", "traffic_bytes_per_particle")
+    achieved = n_tot * B_ADVANCE / (adv_ms / 1e3) / 1e9
+    roof = {"bound": "hbm",
+            "kernel": "k_batch_advance<1> (velocity-Verlet kick and drift, contact view and skin test of "
+                      "every scene's spheres in one launch)",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+            "traffic": tpp * n_tot if tpp else None, "bytes_per_particle": B_ADVANCE, "avg_launch_ms": adv_ms,
+            "launches_timed": kt["advance"][1],
+            "contact_pass": {"kernel": "k_batch_contact (every scene's listed spheres in one launch)",
+                             "avg_launch_ms": con_ms, "bytes_per_particle_full_pass": B_CONTACT["mixed"],
+                             "achieved_full_pass_gbs": n_tot * B_CONTACT["mixed"] / (con_ms / 1e3) / 1e9},
+            "workload": f"the {len(scs)}-hopper batch, {n_tot:,} spheres; {ksteps} steps with direct launches "
+                        "after the timed ones (events cannot split the step graph)",
+            "traffic_note": "profiles/advance_batch_hopper.md: DRAM bytes per sphere of one launch on a "
+                            "64-hopper batch, times the spheres here"}
     # per step: advance, decision, run prefix and contact over all scenes; per
     # call the finish and each scene's body-reaction sum; per re-binning its
     # kernels and its group's decision kernel
@@ -744,7 +771,6 @@ def run_batched(a):
 
     # the batch step's algorithmic bytes: the advance and a full contact pass per sphere
     batch_bytes = n_tot * (B_ADVANCE + B_CONTACT["mixed"])
-    peak, peak_kind = _peaks()
     batch_gbs = batch_bytes / (ms / a.steps / 1e3) / 1e9
     batch.close()
     for d in ds:
@@ -767,7 +793,9 @@ def run_batched(a):
     # FP64 check on the median-size scene, in a state with contacts
     check = _fp64_check(scs[k_med])
     check["scene"] = k_med
-    roof, box = _box_roofline(a, stream, barrier, world, local) if not a.no_box else (None, None)
+    box_roof, box = _box_roofline(a, stream, barrier, world, local) if not a.no_box else (None, None)
+    if box:
+        box["roofline"] = box_roof
     drum = _drum(a, stream) if not a.no_drum and rank == 0 else None
     served = _served(a, stream, plain=not a.no_plain) if rank == 0 and not a.no_served else None
 

@@ -585,6 +585,16 @@ int xd_batch_create(xd_scene* const* scenes, unsigned count, xd_batch** out);
 /* nsteps whole steps of every scene of the batch, queued on `stream`. */
 int xd_batch_step(xd_batch* batch, unsigned nsteps, int check, void* stream);
 int xd_batch_destroy(xd_batch* batch);
+/* Kernel timing of a batch: while enabled, xd_batch_step launches the step's
+ * kernels directly (the same kernels; the re-binning flags are read on the
+ * host) with CUDA events around the advance of every step but a call's first
+ * and around every contact launch.  xd_batch_kernel_times returns their
+ * summed milliseconds and launch counts, [0] advance and [1] contact, since
+ * timing was enabled.  XDEM_NO_GRAPHS=1 in the environment also makes a batch
+ * launch directly (profilers list no kernel inside a graph with conditional
+ * nodes). */
+int xd_batch_set_timing(xd_batch* batch, int enable);
+int xd_batch_kernel_times(xd_batch* batch, double ms[2], unsigned long long launches[2]);
 
 #ifdef __cplusplus
 }

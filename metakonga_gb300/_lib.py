@@ -102,6 +102,8 @@ _SIGS = {
     "xd_batch_create": [vp, u32, vp],
     "xd_batch_step": [vp, u32, i32, vp],
     "xd_batch_destroy": [vp],
+    "xd_batch_set_timing": [vp, i32],
+    "xd_batch_kernel_times": [vp, vp, vp],
     "xd_scene_active": [vp, vp],
     "xd_scene_download_history": [vp, vp, vp, vp, vp],
     "xd_scene_device_bytes": [vp, vp],

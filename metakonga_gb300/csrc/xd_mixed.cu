@@ -2795,8 +2795,9 @@ __global__ void __launch_bounds__(256) k_batch_decide(const BatchScene* __restri
         if (f) atomicOr(&any[(sc / kBatchGroup) & 255u], 1u);
     }
     __syncthreads();
-    for (unsigned g = threadIdx.x; g < ng && g < 256u; g += blockDim.x)
-        if (any[g]) cudaGraphSetConditional(hg[g], 1u);
+    if (hg)   // inside the step graph (the direct path reads flags[] on the host)
+        for (unsigned g = threadIdx.x; g < ng && g < 256u; g += blockDim.x)
+            if (any[g]) cudaGraphSetConditional(hg[g], 1u);
 }
 
 // Inside a group's body: the flagged scenes of the group open their re-binning.
@@ -2885,6 +2886,14 @@ struct MixedBatch {
     cudaGraphExec_t step_graph[2] = {};              // 0: first step of a call (drift), 1: later steps
     cudaGraphExec_t finish_graph = nullptr;          // last kick and the body reactions
     bool captured = false;
+    // direct launches (profilers; kernel timing): CUDA events around the
+    // later steps' advance and every contact launch
+    bool direct = false;
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> spans;
+    double ms[2] = {};
+    unsigned long long launches[2] = {};
 };
 
 namespace {
@@ -3139,6 +3148,8 @@ int mixed_batch_create(MixedScene* const* scenes, unsigned count, MixedBatch** o
     MixedBatch* b = new (std::nothrow) MixedBatch();
     if (!b) return set_error(XD_ERR_NOMEM, "batch: host allocation");
     b->scenes.assign(scenes, scenes + count);
+    const char* ng = getenv("XDEM_NO_GRAPHS");
+    b->direct = ng && ng[0] && ng[0] != '0';
     *out = b;
     return XD_OK;
 }
@@ -3147,7 +3158,92 @@ void mixed_batch_destroy(MixedBatch* b)
 {
     if (!b) return;
     free_batch_graphs(b);
+    for (cudaEvent_t e : b->ev_pool) cudaEventDestroy(e);
     delete b;
+}
+
+namespace {
+
+cudaEvent_t batch_event(MixedBatch* b, size_t k)
+{
+    while (b->ev_pool.size() <= k) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        b->ev_pool.push_back(e);
+    }
+    return b->ev_pool[k];
+}
+
+// The batch step by direct launches: the same kernels as the step graph, the
+// re-binning flags read on the host after each advance.
+int batch_step_direct(MixedBatch* b, unsigned nsteps, cudaStream_t q)
+{
+    const unsigned ns = (unsigned)b->scenes.size();
+    std::vector<unsigned> flags(ns);
+    size_t nev = 0;
+    int st = XD_OK;
+    auto span = [&](int kind, auto launch) {
+        cudaEvent_t e0 = b->timing ? batch_event(b, nev++) : nullptr;
+        cudaEvent_t e1 = b->timing ? batch_event(b, nev++) : nullptr;
+        if (e0) cudaEventRecord(e0, q);
+        launch();
+        if (e1) cudaEventRecord(e1, q);
+        if (e0 && e1) b->spans.push_back({ kind, { e0, e1 } });
+    };
+    for (unsigned t = 0; t < nsteps && st == XD_OK; ++t) {
+        if (t == 0) {
+            k_batch_advance<0><<<b->nblocks, 256, 0, q>>>(b->d_scenes, b->d_block_scene, b->nblocks);
+        } else {
+            span(0, [&] { k_batch_advance<1><<<b->nblocks, 256, 0, q>>>(b->d_scenes, b->d_block_scene, b->nblocks); });
+        }
+        k_batch_decide<<<1, 256, 0, q>>>(b->d_scenes, ns, b->d_flags, nullptr);
+        st = launch_status("batch advance");
+        if (st == XD_OK)
+            st = cuda_status(cudaMemcpyAsync(flags.data(), b->d_flags, sizeof(unsigned) * ns, cudaMemcpyDeviceToHost, q),
+                             "batch flags");
+        if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "batch flags");
+        for (unsigned k = 0; k < ns && st == XD_OK; ++k)
+            if (flags[k]) st = rebuild(b->scenes[k], q);
+        if (st != XD_OK) break;
+        k_batch_chunks<<<1, 1024, 0, q>>>(b->d_scenes, ns, b->d_chunks);
+        span(1, [&] { k_batch_contact<<<kBatchContactBlocks, kContactThreads, 0, q>>>(b->d_scenes, ns, b->d_chunks); });
+        st = launch_status("batch contact");
+    }
+    if (st == XD_OK) {
+        k_batch_advance<2><<<b->nblocks, 256, 0, q>>>(b->d_scenes, b->d_block_scene, b->nblocks);
+        st = launch_status("batch finish");
+    }
+    for (unsigned k = 0; k < ns && st == XD_OK; ++k) st = flush_reactions(b->scenes[k], q);
+    if (st == XD_OK && b->timing) {
+        st = cuda_status(cudaStreamSynchronize(q), "batch timing");
+        for (auto& sp : b->spans) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, sp.second.first, sp.second.second) == cudaSuccess) {
+                b->ms[sp.first] += ms;
+                b->launches[sp.first] += 1;
+            }
+        }
+        b->spans.clear();
+    }
+    return st;
+}
+
+}  // namespace
+
+int mixed_batch_set_timing(MixedBatch* b, bool enable)
+{
+    b->timing = enable;
+    b->ms[0] = b->ms[1] = 0.0;
+    b->launches[0] = b->launches[1] = 0;
+    return XD_OK;
+}
+
+void mixed_batch_kernel_times(MixedBatch* b, double ms[2], unsigned long long launches[2])
+{
+    for (int k = 0; k < 2; ++k) {
+        ms[k] = b->ms[k];
+        launches[k] = b->launches[k];
+    }
 }
 
 int mixed_batch_step(MixedBatch* b, unsigned nsteps, cudaStream_t q)
@@ -3168,10 +3264,14 @@ int mixed_batch_step(MixedBatch* b, unsigned nsteps, cudaStream_t q)
             st = cuda_status(cudaMemsetAsync(sc->counters + CN_REBUILD, 1, 1, q), "batch re-binning flag");
         if (st != XD_OK) return st;
     }
-    st = cuda_status(cudaGraphLaunch(b->step_graph[0], q), "batch graph launch");
-    for (unsigned t = 1; t < nsteps && st == XD_OK; ++t)
-        st = cuda_status(cudaGraphLaunch(b->step_graph[1], q), "batch graph launch");
-    if (st == XD_OK) st = cuda_status(cudaGraphLaunch(b->finish_graph, q), "batch graph launch");
+    if (b->direct || b->timing) {
+        st = batch_step_direct(b, nsteps, q);
+    } else {
+        st = cuda_status(cudaGraphLaunch(b->step_graph[0], q), "batch graph launch");
+        for (unsigned t = 1; t < nsteps && st == XD_OK; ++t)
+            st = cuda_status(cudaGraphLaunch(b->step_graph[1], q), "batch graph launch");
+        if (st == XD_OK) st = cuda_status(cudaGraphLaunch(b->finish_graph, q), "batch graph launch");
+    }
     if (st != XD_OK) return st;
     for (MixedScene* sc : b->scenes) sc->cells_clean = true;
     return XD_OK;

@@ -885,6 +885,19 @@ int xd_batch_step(xd_batch* b, unsigned nsteps, int check, void* stream)
     return st;
 }
 
+int xd_batch_set_timing(xd_batch* b, int enable)
+{
+    if (!b) return set_error(XD_ERR_INVALID, "batch_set_timing: null batch");
+    return mixed_batch_set_timing(b->mixed, enable != 0);
+}
+
+int xd_batch_kernel_times(xd_batch* b, double ms[2], unsigned long long launches[2])
+{
+    if (!b || !ms || !launches) return set_error(XD_ERR_INVALID, "batch_kernel_times: null argument");
+    mixed_batch_kernel_times(b->mixed, ms, launches);
+    return XD_OK;
+}
+
 int xd_batch_destroy(xd_batch* b)
 {
     if (!b) return XD_OK;

@@ -270,6 +270,18 @@ class Batch:
     def step(self, nsteps: int, check: bool = False, stream: int = 0) -> None:
         call("xd_batch_step", self.handle, int(nsteps), 1 if check else 0, stream)
 
+    def set_timing(self, enable: bool = True) -> None:
+        """Direct launches with CUDA events around the advance and contact
+        launches (xd_batch_set_timing)."""
+        call("xd_batch_set_timing", self.handle, 1 if enable else 0)
+
+    def kernel_times(self) -> dict:
+        """{"advance": (ms, launches), "contact": (ms, launches)} since timing was enabled."""
+        ms = np.zeros(2)
+        n = np.zeros(2, np.uint64)
+        call("xd_batch_kernel_times", self.handle, ms.ctypes.data, n.ctypes.data)
+        return {"advance": (float(ms[0]), int(n[0])), "contact": (float(ms[1]), int(n[1]))}
+
     def close(self) -> None:
         if self.handle:
             call("xd_batch_destroy", self.handle)

@@ -23,10 +23,12 @@ def _scenes():
     return out
 
 
-def _run(split, batched, moved=None):
+def _run(split, batched, moved=None, timed=False):
     scs = _scenes()
     ds = [engine.DeviceScene(sc, mode=engine.MODE_MIXED) for sc in scs]
     b = engine.Batch(ds) if batched else None
+    if timed:
+        b.set_timing(True)
     for c, k in enumerate(split):
         if moved is not None and c == 1:
             planes = scs[3].planes.copy()
@@ -40,6 +42,11 @@ def _run(split, batched, moved=None):
             for d in ds:
                 d.step(k, check=True)
     out = [(d.download(), d.rebuilds()[0], d.get_bodies() if d.ntri else None) for d in ds]
+    if timed:
+        kt = b.kernel_times()
+        steps = sum(split)
+        assert kt["advance"][1] == steps - len(split) and kt["contact"][1] == steps
+        assert kt["advance"][0] > 0 and kt["contact"][0] > 0
     if b:
         b.close()
     for d in ds:
@@ -47,10 +54,12 @@ def _run(split, batched, moved=None):
     return out
 
 
-@pytest.mark.parametrize("moved", [None, True])
-def test_batch_equals_each_scene_alone(cuda, moved):
+@pytest.mark.parametrize("moved,timed", [(None, False), (True, False), (None, True)])
+def test_batch_equals_each_scene_alone(cuda, moved, timed):
+    """timed: the batch's direct launches with kernel events (the same
+    kernels as its step graphs)."""
     alone = _run((5, 27, 16), False, moved)
-    batch = _run((5, 27, 16), True, moved)
+    batch = _run((5, 27, 16), True, moved, timed)
     assert all(r > 1 for _, r, _ in alone), [r for _, r, _ in alone]
     for (a, ra, ba), (b, rb, bb) in zip(alone, batch):
         assert ra == rb
