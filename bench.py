@@ -725,7 +725,10 @@ def run_batched(a):
             "launches_timed": kt["advance"][1],
             "contact_pass": {"kernel": "k_batch_contact (every scene's listed spheres in one launch)",
                              "avg_launch_ms": con_ms, "bytes_per_particle_full_pass": B_CONTACT["mixed"],
-                             "achieved_full_pass_gbs": n_tot * B_CONTACT["mixed"] / (con_ms / 1e3) / 1e9},
+                             "achieved_full_pass_gbs": n_tot * B_CONTACT["mixed"] / (con_ms / 1e3) / 1e9,
+                             "note": "a full pass's bytes over the launch time; above the copy peak when, "
+                                     "as here, only part of the spheres are listed (those with neighbours "
+                                     "or walls within the skin)"},
             "workload": f"the {len(scs)}-hopper batch, {n_tot:,} spheres; {ksteps} steps with direct launches "
                         "after the timed ones (events cannot split the step graph)",
             "traffic_note": "profiles/advance_batch_hopper.md: DRAM bytes per sphere of one launch on a "
