@@ -755,13 +755,14 @@ def run_batched(a):
     d2h = sum(sum(h[k].numel() * 8 for k in keys) for h in host)
 
     def e2e_job():
+        # copies queued on the stream (pinned buffers), one wait at the end
         for d, h in zip(ds, host):
-            call("xd_scene_upload", d.handle, *[h[k].data_ptr() for k in
-                                                ("pos", "vel", "acc", "omega", "alpha", "force",
-                                                 "moment", "mass", "inertia")], sh)
+            call("xd_scene_upload_async", d.handle, *[h[k].data_ptr() for k in
+                                                      ("pos", "vel", "acc", "omega", "alpha", "force",
+                                                       "moment", "mass", "inertia")], sh)
         batch.step(a.steps, check=False, stream=sh)
         for d, h in zip(ds, host):
-            call("xd_scene_download", d.handle, *[h[k].data_ptr() for k in keys], None, None, sh)
+            call("xd_scene_download_async", d.handle, *[h[k].data_ptr() for k in keys], None, None, sh)
         torch.cuda.current_stream().synchronize()
         stream.synchronize()
 

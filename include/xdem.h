@@ -422,6 +422,16 @@ int xd_scene_upload(xd_scene* scene, const double* pos, const double* vel, const
                     void* stream);
 int xd_scene_download(xd_scene* scene, double* pos, double* vel, double* acc, double* omega,
                       double* alpha, double* force, double* moment, void* stream);
+/* The same copies queued on `stream` without waiting for them: the host
+ * arrays must stay untouched (upload) or unread (download) until the stream
+ * has passed this point; with pinned host memory the copies overlap the
+ * host's next calls.  A scene's first upload sets its grid up and waits. */
+int xd_scene_upload_async(xd_scene* scene, const double* pos, const double* vel, const double* acc,
+                          const double* omega, const double* alpha, const double* force,
+                          const double* moment, const double* mass, const double* inertia,
+                          void* stream);
+int xd_scene_download_async(xd_scene* scene, double* pos, double* vel, double* acc, double* omega,
+                            double* alpha, double* force, double* moment, void* stream);
 
 /* Device pointers of the scene's state, in the reference layouts (for
  * zero-copy access); any output may be NULL. */

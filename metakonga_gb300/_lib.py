@@ -82,6 +82,8 @@ _SIGS = {
     "xd_scene_destroy": [vp],
     "xd_scene_upload": [vp] * 10 + [vp],
     "xd_scene_download": [vp] * 8 + [vp],
+    "xd_scene_upload_async": [vp] * 10 + [vp],
+    "xd_scene_download_async": [vp] * 8 + [vp],
     "xd_scene_device_state": [vp] * 10,
     "xd_scene_device_grid": [vp] * 6,
     "xd_scene_download_grid": [vp] * 6 + [vp],

@@ -1924,7 +1924,7 @@ static int reset_history(MixedScene* s, cudaStream_t q);
 
 int mixed_upload(MixedScene* s, const double* pos, const double* vel, const double* acc,
                  const double* omega, const double* alpha, const double* mass,
-                 const double* inertia, cudaStream_t q)
+                 const double* inertia, cudaStream_t q, bool sync)
 {
     if (!pos || !vel || !acc || !omega || !alpha || !mass || !inertia)
         return set_error(XD_ERR_INVALID, "mixed mode: upload needs pos, vel, acc, omega, alpha, mass, inertia");
@@ -1970,12 +1970,12 @@ int mixed_upload(MixedScene* s, const double* pos, const double* vel, const doub
     k_mx_load<<<blocks(s->cap, 256), 256, 0, q>>>(Pc, s->m[0], dpos, dvel, dacc, dom, dal, dm, dI,
                                                   s->mass0, s->pf, s->qa, s->qb);
     st = launch_status("mixed upload");
-    if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "mixed upload");
+    if (st == XD_OK && sync) st = cuda_status(cudaStreamSynchronize(q), "mixed upload");
     return st;
 }
 
 int mixed_download(MixedScene* s, double* pos, double* vel, double* acc, double* omega,
-                   double* alpha, double* force, double* moment, cudaStream_t q)
+                   double* alpha, double* force, double* moment, cudaStream_t q, bool sync)
 {
     if (!s->ready) return set_error(XD_ERR_STATE, "mixed mode: no state uploaded");
     int st = ensure_xfer(s);
@@ -2001,7 +2001,7 @@ int mixed_download(MixedScene* s, double* pos, double* vel, double* acc, double*
     cp(alpha, dal, 3 * n);
     cp(force, df, 3 * n);
     cp(moment, dmo, 3 * n);
-    if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "mixed download");
+    if (st == XD_OK && sync) st = cuda_status(cudaStreamSynchronize(q), "mixed download");
     return st;
 }
 

@@ -21,9 +21,9 @@ int mixed_create(const xd_scene_desc& d, MixedScene** out);
 void mixed_destroy(MixedScene* s);
 int mixed_upload(MixedScene* s, const double* pos, const double* vel, const double* acc,
                  const double* omega, const double* alpha, const double* mass,
-                 const double* inertia, cudaStream_t q);
+                 const double* inertia, cudaStream_t q, bool sync = true);
 int mixed_download(MixedScene* s, double* pos, double* vel, double* acc, double* omega,
-                   double* alpha, double* force, double* moment, cudaStream_t q);
+                   double* alpha, double* force, double* moment, cudaStream_t q, bool sync = true);
 int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph);
 unsigned long long mixed_launches(MixedScene* s, unsigned nsteps);
 unsigned long long mixed_rebuild_launches(MixedScene* s);

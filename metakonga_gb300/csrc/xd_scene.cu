@@ -341,13 +341,13 @@ int xd_scene_destroy(xd_scene* s)
     return cuda_status(e, "scene_destroy");
 }
 
-int xd_scene_upload(xd_scene* s, const double* pos, const double* vel, const double* acc,
-                    const double* omega, const double* alpha, const double* force,
-                    const double* moment, const double* mass, const double* inertia, void* stream)
+static int scene_upload(xd_scene* s, const double* pos, const double* vel, const double* acc,
+                        const double* omega, const double* alpha, const double* force,
+                    const double* moment, const double* mass, const double* inertia, void* stream, bool sync)
 {
     if (!s) return set_error(XD_ERR_INVALID, "scene_upload: null scene");
     cudaStream_t q = static_cast<cudaStream_t>(stream);
-    if (s->mixed) return mixed_upload(s->mixed, pos, vel, acc, omega, alpha, mass, inertia, q);
+    if (s->mixed) return mixed_upload(s->mixed, pos, vel, acc, omega, alpha, mass, inertia, q, sync);
     size_t n = s->np;
     int st = XD_OK;
     auto A = [&](int r) { if (st == XD_OK) st = r; };
@@ -360,16 +360,30 @@ int xd_scene_upload(xd_scene* s, const double* pos, const double* vel, const dou
     A(h2d(s->moment, moment, sizeof(double) * 3 * n, q));
     A(h2d(s->mass, mass, sizeof(double) * n, q));
     A(h2d(s->inertia, inertia, sizeof(double) * n, q));
-    if (st == XD_OK) A(cuda_status(cudaStreamSynchronize(q), "scene_upload"));
+    if (st == XD_OK && sync) A(cuda_status(cudaStreamSynchronize(q), "scene_upload"));
     return st;
 }
 
-int xd_scene_download(xd_scene* s, double* pos, double* vel, double* acc, double* omega,
-                      double* alpha, double* force, double* moment, void* stream)
+int xd_scene_upload(xd_scene* s, const double* pos, const double* vel, const double* acc, const double* omega,
+                    const double* alpha, const double* force, const double* moment, const double* mass,
+                    const double* inertia, void* stream)
+{
+    return scene_upload(s, pos, vel, acc, omega, alpha, force, moment, mass, inertia, stream, true);
+}
+
+int xd_scene_upload_async(xd_scene* s, const double* pos, const double* vel, const double* acc, const double* omega,
+                          const double* alpha, const double* force, const double* moment, const double* mass,
+                          const double* inertia, void* stream)
+{
+    return scene_upload(s, pos, vel, acc, omega, alpha, force, moment, mass, inertia, stream, false);
+}
+
+static int scene_download(xd_scene* s, double* pos, double* vel, double* acc, double* omega,
+                      double* alpha, double* force, double* moment, void* stream, bool sync)
 {
     if (!s) return set_error(XD_ERR_INVALID, "scene_download: null scene");
     cudaStream_t q = static_cast<cudaStream_t>(stream);
-    if (s->mixed) return mixed_download(s->mixed, pos, vel, acc, omega, alpha, force, moment, q);
+    if (s->mixed) return mixed_download(s->mixed, pos, vel, acc, omega, alpha, force, moment, q, sync);
     size_t n = s->np;
     int st = XD_OK;
     auto A = [&](int r) { if (st == XD_OK) st = r; };
@@ -380,8 +394,20 @@ int xd_scene_download(xd_scene* s, double* pos, double* vel, double* acc, double
     A(d2h(alpha, s->alpha, sizeof(double) * 3 * n, q));
     A(d2h(force, s->force, sizeof(double) * 3 * n, q));
     A(d2h(moment, s->moment, sizeof(double) * 3 * n, q));
-    if (st == XD_OK) A(cuda_status(cudaStreamSynchronize(q), "scene_download"));
+    if (st == XD_OK && sync) A(cuda_status(cudaStreamSynchronize(q), "scene_download"));
     return st;
+}
+
+int xd_scene_download(xd_scene* s, double* pos, double* vel, double* acc, double* omega, double* alpha,
+                      double* force, double* moment, void* stream)
+{
+    return scene_download(s, pos, vel, acc, omega, alpha, force, moment, stream, true);
+}
+
+int xd_scene_download_async(xd_scene* s, double* pos, double* vel, double* acc, double* omega, double* alpha,
+                            double* force, double* moment, void* stream)
+{
+    return scene_download(s, pos, vel, acc, omega, alpha, force, moment, stream, false);
 }
 
 int xd_scene_device_state(xd_scene* s, double** pos, double** vel, double** acc, double** omega,

@@ -79,3 +79,29 @@ def test_batch_refuses_history_and_plain_scenes(cuda):
             engine.Batch(group)
     d1.close()
     d2.close()
+
+
+def test_async_copies_round_trip(cuda):
+    """xd_scene_upload_async / xd_scene_download_async: queued on the stream,
+    the same data as the waiting copies once the stream is synchronised."""
+    import torch
+
+    from metakonga_gb300._lib import call
+    sc = small_hopper(n=1500, seed=5)
+    d = engine.DeviceScene(sc, mode=engine.MODE_MIXED)
+    d.step(3, check=True)
+    ref = d.download()
+    keys = ("pos", "vel", "acc", "omega", "alpha")
+    host = {k: torch.from_numpy(np.ascontiguousarray(ref[k])).pin_memory() for k in keys}
+    for k in ("force", "moment", "mass", "inertia"):
+        host[k] = torch.from_numpy(np.ascontiguousarray(getattr(sc, k))).pin_memory()
+    out = {k: torch.empty_like(host[k]).pin_memory() for k in keys}
+    stream = torch.cuda.Stream()
+    call("xd_scene_upload_async", d.handle, *[host[k].data_ptr() for k in
+                                              ("pos", "vel", "acc", "omega", "alpha", "force", "moment",
+                                               "mass", "inertia")], stream.cuda_stream)
+    call("xd_scene_download_async", d.handle, *[out[k].data_ptr() for k in keys], None, None, stream.cuda_stream)
+    stream.synchronize()
+    for k in keys:
+        assert np.array_equal(out[k].numpy(), ref[k]), k
+    d.close()
