@@ -165,6 +165,7 @@ struct MixedScene {
     double* vlist_body = nullptr; // body-frame vertices [ntri][9]
     xd_polygon_mass_info* pmi = nullptr;
     float* tri_ref = nullptr;     // vertices at the last build, FP32 relative to the grid origin
+    float4* tbound = nullptr;     // bounding sphere of each triangle at the last build (same frame)
     unsigned* tcells = nullptr;   // cells per triangle, then their exclusive scan [ntri + 1]
     unsigned* tpk = nullptr;      // (cell, triangle) pairs [tpair_cap]: keys, triangles
     unsigned* tpt = nullptr;
@@ -808,7 +809,7 @@ __device__ __forceinline__ void tri_box(const MixParams& P, const xd_polygon_inf
 // Cells per triangle (tcells[ntri] = 0 for the scan) and the build vertices.
 __global__ void __launch_bounds__(256) k_tri_count(MixParams P, const xd_polygon_info* __restrict__ poly,
                                                    unsigned* __restrict__ tcells,
-                                                   float* __restrict__ tri_ref)
+                                                   float* __restrict__ tri_ref, float4* __restrict__ tbound)
 {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t > P.ntri) return;
@@ -820,6 +821,15 @@ __global__ void __launch_bounds__(256) k_tri_count(MixParams P, const xd_polygon
     float v[9];
     tri_box(P, poly + t, lo, hi, v);
     for (int k = 0; k < 9; ++k) tri_ref[9 * (size_t)t + k] = v[k];
+    // bounding sphere for the list build: centroid and farthest vertex
+    const float gx = (v[0] + v[3] + v[6]) * (1.f / 3.f), gy = (v[1] + v[4] + v[7]) * (1.f / 3.f),
+                gz = (v[2] + v[5] + v[8]) * (1.f / 3.f);
+    float rb = 0.f;
+    for (int k = 0; k < 3; ++k) {
+        const float dx = v[3 * k] - gx, dy = v[3 * k + 1] - gy, dz = v[3 * k + 2] - gz;
+        rb = fmaxf(rb, sqrtf(dx * dx + dy * dy + dz * dz));
+    }
+    tbound[t] = make_float4(gx, gy, gz, rb);
     tcells[t] = (unsigned)((hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1));
 }
 
@@ -909,6 +919,7 @@ __global__ void __launch_bounds__(256) k_tri_build(MixParams P, Master M, const 
                                                    const unsigned* __restrict__ tpk,
                                                    const unsigned* __restrict__ tpt, unsigned cap,
                                                    const xd_polygon_info* __restrict__ poly,
+                                                   const float4* __restrict__ tbound,
                                                    unsigned* __restrict__ tcount, unsigned* __restrict__ tlist)
 {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -916,11 +927,18 @@ __global__ void __launch_bounds__(256) k_tri_build(MixParams P, Master M, const 
     const unsigned key = __ldg(keys + i);
     const unsigned b = lower_bound_u(tpk, cap, key), e = lower_bound_u(tpk, cap, key + 1u);
     const d3 ip = mk(M.x[i], M.y[i], M.z[i]);
+    const float pr[3] = { (float)(ip.x - P.wo[0]), (float)(ip.y - P.wo[1]), (float)(ip.z - P.wo[2]) };
     const double lim = M.r[i] + (double)(P.vcut);
     const unsigned n = P.n;
     unsigned c = 0;
     for (unsigned k = b; k < e; ++k) {
         const unsigned t = __ldg(tpt + k);
+        // the triangle's bounding sphere first: one farther than lim (by more
+        // than the FP32 error) holds no point within lim, and the FP64 closest
+        // point is skipped
+        const float4 bs = __ldg(tbound + t);
+        const float sx = bs.x - pr[0], sy = bs.y - pr[1], sz = bs.z - pr[2];
+        if (sqrtf(sx * sx + sy * sy + sz * sz) - bs.w > (float)lim + 1e-5f) continue;
         const xd_polygon_info* tri = poly + t;
         const d3 cp = closest_pt_triangle(tri_vertex(tri->P), tri_vertex(tri->Q), tri_vertex(tri->R), ip);
         if (length(ip - cp) < lim) {
@@ -1517,13 +1535,18 @@ __global__ void __launch_bounds__(kRxnThreads) k_rxn_sum(double* __restrict__ rx
     __syncthreads();
     if (!last) return;
     __threadfence();
-    if (threadIdx.x < nq) {
-        const unsigned q = threadIdx.x;
+    // the block partials of each component: a warp per component, lane l
+    // summing partials l, l + 32, ... and a fixed shuffle tree (the same
+    // order every time; the loads overlap instead of forming one chain)
+    for (unsigned q = wid; q < nq; q += blockDim.x / 32u) {
         double t = 0.0;
-        for (unsigned k = 0; k < gridDim.x; ++k) t += __ldcg(part + (size_t)q * gridDim.x + k);
-        const unsigned b = q / 6, c = q % 6;
-        if (c < 3) pmi[b].force[c] += t;
-        else pmi[b].moment[c - 3] += t;
+        for (unsigned k = lane; k < gridDim.x; k += 32u) t += __ldcg(part + (size_t)q * gridDim.x + k);
+        for (unsigned o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) {
+            const unsigned b = q / 6, c = q % 6;
+            if (c < 3) pmi[b].force[c] += t;
+            else pmi[b].moment[c - 3] += t;
+        }
     }
     if (threadIdx.x == 0) counters[CN_RXN] = 0;
 }
@@ -1835,6 +1858,7 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
         A(alloc(s, &s->vlist_body, 9 * (size_t)s->ntri));
         A(alloc(s, &s->pmi, s->nbodies));
         A(alloc(s, &s->tri_ref, 9 * (size_t)s->ntri));
+        A(alloc(s, &s->tbound, (size_t)s->ntri));
         A(alloc(s, &s->tcells, (size_t)s->ntri + 1));
         A(alloc(s, &s->tpk, s->tpair_cap));
         A(alloc(s, &s->tpt, s->tpair_cap));
@@ -2150,7 +2174,7 @@ static int rebuild(MixedScene* s, cudaStream_t q)
     if (st == XD_OK && s->ntri) {
         // triangles: (cell, triangle) pairs sorted by cell, then each particle's list
         const unsigned T = s->ntri, cap = s->tpair_cap;
-        k_tri_count<<<blocks(T + 1, 256), 256, 0, q>>>(s->P, s->poly, s->tcells, s->tri_ref);
+        k_tri_count<<<blocks(T + 1, 256), 256, 0, q>>>(s->P, s->poly, s->tcells, s->tri_ref, s->tbound);
         k_scan1<<<1, 1024, 0, q>>>(s->tcells, T + 1);
         k_tri_fill<<<blocks(T, 256), 256, 0, q>>>(s->P, s->poly, s->tcells, cap, s->tpk, s->tpt);
         k_tri_pad<<<blocks(cap, 256), 256, 0, q>>>(s->tcells, T, cap, s->ncell, s->tpk, s->tpt);
@@ -2161,8 +2185,8 @@ static int rebuild(MixedScene* s, cudaStream_t q)
         if (st != XD_OK) return st;
         s->tpk_sorted = tk;
         s->tpt_sorted = tt;
-        k_tri_build<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[0], s->prev_keys, tk, tt, cap, s->poly, s->tcount,
-                                                   s->tlist);
+        k_tri_build<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[0], s->prev_keys, tk, tt, cap, s->poly, s->tbound,
+                                                   s->tcount, s->tlist);
         st = launch_status("mixed triangle lists");
     }
     if (st != XD_OK) return st;
