@@ -3181,6 +3181,7 @@ int mixed_batch_create(MixedScene* const* scenes, unsigned count, MixedBatch** o
 void mixed_batch_destroy(MixedBatch* b)
 {
     if (!b) return;
+    cudaDeviceSynchronize();   // steps queued from the batch's graphs run first
     free_batch_graphs(b);
     for (cudaEvent_t e : b->ev_pool) cudaEventDestroy(e);
     delete b;

@@ -4,10 +4,11 @@ batching of their steps.
 A ``Server`` takes requests (a scene and a step count) that arrive over time.
 It admits a request as soon as the device memory the scene will hold fits in
 the budget next to the scenes already resident, then advances every resident
-scene by up to ``chunk`` steps per tick in one ``engine.step_many`` call: the
-scenes' kernels run side by side on the library's stream pool, so requests
-that arrive while others run join the next tick instead of waiting for the
-GPU to drain.  Ticks are queued ``depth`` deep: the host counts steps, marks
+scene by up to ``chunk`` steps per tick: as one ``engine.Batch`` (every step of
+every resident scene in one CUDA graph) when they all take the same number of
+steps and can be batched, else in one ``engine.step_many`` call (the scenes'
+kernels side by side on the library's stream pool).  Requests that arrive
+while others run join the next tick instead of waiting for the GPU to drain.  Ticks are queued ``depth`` deep: the host counts steps, marks
 each tick with an event and only waits for the oldest mark, so the GPU is fed
 while the host admits, downloads and retires.  A scene whose steps are done is
 downloaded (on a side stream that waits for its last tick only) and freed when
@@ -120,11 +121,13 @@ class Server:
     request larger than the budget is admitted alone when nothing else is
     resident).  chunk: steps per scene per tick; smaller chunks admit new
     requests sooner, larger ones cost fewer host calls.  depth: ticks queued
-    on the device before the host waits for the oldest (0: wait for each)."""
+    on the device before the host waits for the oldest (0: wait for each).
+    batch: step the resident scenes as an engine.Batch when they can be (the
+    batch is made again whenever the resident set changes)."""
 
     def __init__(self, budget_bytes: int, chunk: int = 20, mode: int = engine.MODE_MIXED,
                  stream: int = 0, keep_results: bool = True, clock=time.perf_counter, depth: int = 2,
-                 marks=None):
+                 marks=None, batch: bool = True):
         if chunk < 1:
             raise ValueError("chunk must be >= 1")
         if depth < 0:
@@ -145,6 +148,33 @@ class Server:
         self.peak_active = 0
         self.wall = 0.0
         self._to_close: list = []
+        self.use_batch = batch
+        self._batch = None
+        self._batch_key = None
+        self.batched_ticks = 0
+
+    def _drop_batch(self) -> None:
+        if self._batch is not None:
+            self._batch.close()   # waits for the steps queued from it
+        self._batch = None
+        self._batch_key = None
+
+    def _step(self, active: list, counts: list) -> None:
+        handles = [r.handle for r in active]
+        if self.use_batch and len(active) > 1 and len(set(counts)) == 1:
+            key = tuple(id(h) for h in handles)
+            if key != self._batch_key:
+                self._drop_batch()
+                self._batch_key = key
+                try:
+                    self._batch = engine.Batch(handles)
+                except Exception:
+                    self._batch = None   # not batchable (history, kinematics, FP64 form)
+            if self._batch is not None:
+                self._batch.step(counts[0], check=False, stream=self.stream)
+                self.batched_ticks += 1
+                return
+        engine.step_many(handles, counts, check=False, stream=self.stream)
 
     def submit(self, rid, scene, steps: int, arrival: float = 0.0) -> None:
         if steps < 1:
@@ -194,6 +224,7 @@ class Server:
             # freeing device memory synchronises the device: done when it is idle
             while inflight:
                 retire_one()
+            self._drop_batch()   # before any of its scenes
             for r in to_close:
                 r.handle.close()
                 r.handle = None
@@ -211,7 +242,7 @@ class Server:
             if active:
                 self.peak_active = max(self.peak_active, len(active))
                 counts = [min(self.chunk, r.remaining) for r in active]
-                engine.step_many([r.handle for r in active], counts, check=False, stream=self.stream)
+                self._step(active, counts)
                 self.ticks += 1
                 fin, still = [], []
                 for r, c in zip(active, counts):
@@ -227,6 +258,7 @@ class Server:
                 if self.pending:
                     time.sleep(max(0.0, self.pending[0].arrival - (self.clock() - t0)))
         close_finished()
+        self._drop_batch()
         self.wall = self.clock() - t0
         return self.finished
 
@@ -246,7 +278,7 @@ class Server:
                 "particle_steps": work, "wall_s": self.wall,
                 "particle_steps_per_s": work / self.wall if self.wall > 0 else 0.0,
                 "offered_particle_steps_per_s": work / span if span > 0 else None,
-                "ticks": self.ticks, "peak_active": self.peak_active,
+                "ticks": self.ticks, "batched_ticks": self.batched_ticks, "peak_active": self.peak_active,
                 "peak_booked_bytes": self.peak_used}
 
 

@@ -12,6 +12,7 @@ from .cases import packed_scene
 
 class _FakeScene:
     live = 0
+    batches = []
 
     def __init__(self, sc, mode=engine.MODE_MIXED):
         self.sc = sc
@@ -22,6 +23,8 @@ class _FakeScene:
         return {"steps": self.steps}
 
     def close(self):
+        # a scene is never freed while a batch holding it is alive
+        assert not any(self in b.handles for b in _FakeScene.batches if not b.closed)
         _FakeScene.live -= 1
 
 
@@ -59,8 +62,23 @@ def fake(monkeypatch):
             h.steps += c
         clock.t += 1e-3
 
+    class _FakeBatch:
+        def __init__(self, handles):
+            self.handles = list(handles)
+            self.closed = False
+            _FakeScene.batches.append(self)
+
+        def step(self, k, check=False, stream=0):
+            assert not self.closed
+            step_many(self.handles, [k] * len(self.handles))
+
+        def close(self):
+            self.closed = True
+
     monkeypatch.setattr(engine, "DeviceScene", _FakeScene)
     monkeypatch.setattr(engine, "step_many", step_many)
+    monkeypatch.setattr(engine, "Batch", _FakeBatch)
+    _FakeScene.batches = []
     monkeypatch.setattr(serve.time, "sleep", lambda s: setattr(clock, "t", clock.t + max(s, 0.0)))
     _FakeScene.live = 0
     return clock, calls
@@ -205,3 +223,31 @@ def test_hopper_geometry():
     pr = cKDTree(sc.pos[:, :3]).query_pairs(0.008, output_type="ndarray")
     dist = np.linalg.norm(sc.pos[pr[:, 0], :3] - sc.pos[pr[:, 1], :3], axis=1)
     assert np.all(dist >= sc.pos[pr[:, 0], 3] + sc.pos[pr[:, 1], 3])
+
+
+def test_resident_scenes_step_as_a_batch(fake):
+    """Ticks where every resident scene takes the same step count go through
+    one batch per resident set (made again when the set changes); uneven
+    ticks fall back to step_many; every batch is closed before its scenes."""
+    clock, calls = fake
+    srv = serve.Server(budget_bytes=1 << 40, chunk=4, clock=clock, marks=_Marks(), depth=0)
+    srv.submit("a", _named("a"), 12)
+    srv.submit("b", _named("b"), 6)
+    srv.submit("c", _named("c"), 8, arrival=0.0015)
+    done = srv.run()
+    assert {r.rid: r.result["steps"] for r in done} == {"a": 12, "b": 6, "c": 8}
+    rep = srv.report()
+    assert 0 < rep["batched_ticks"] < rep["ticks"]
+    assert len(_FakeScene.batches) >= 2 and all(b.closed for b in _FakeScene.batches)
+    assert _FakeScene.live == 0
+    # the batches held the resident sets of their ticks
+    assert {tuple(h.sc.name for h in b.handles) for b in _FakeScene.batches} == {("a", "b"), ("a", "c")}
+
+
+def test_batching_off_steps_side_by_side(fake):
+    clock, calls = fake
+    srv = serve.Server(budget_bytes=1 << 40, chunk=4, clock=clock, marks=_Marks(), depth=0, batch=False)
+    srv.submit("a", _named("a"), 8)
+    srv.submit("b", _named("b"), 8)
+    srv.run()
+    assert srv.report()["batched_ticks"] == 0 and not _FakeScene.batches
