@@ -5,8 +5,8 @@ A ``Server`` takes requests (a scene and a step count) that arrive over time.
 It admits a request as soon as the device memory the scene will hold fits in
 the budget next to the scenes already resident, then advances every resident
 scene by up to ``chunk`` steps per tick: as one ``engine.Batch`` (every step of
-every resident scene in one CUDA graph) when they all take the same number of
-steps and can be batched, else in one ``engine.step_many`` call (the scenes'
+every resident scene in one CUDA graph) when asked to and they all take the
+same number of steps and can be batched, else in one ``engine.step_many`` call (the scenes'
 kernels side by side on the library's stream pool).  Requests that arrive
 while others run join the next tick instead of waiting for the GPU to drain.  Ticks are queued ``depth`` deep: the host counts steps, marks
 each tick with an event and only waits for the oldest mark, so the GPU is fed
@@ -122,12 +122,16 @@ class Server:
     resident).  chunk: steps per scene per tick; smaller chunks admit new
     requests sooner, larger ones cost fewer host calls.  depth: ticks queued
     on the device before the host waits for the oldest (0: wait for each).
-    batch: step the resident scenes as an engine.Batch when they can be (the
-    batch is made again whenever the resident set changes)."""
+    batch: step the resident scenes as an engine.Batch when they can be.  The
+    batch is made again whenever the resident set changes, which waits for
+    the device and captures its graphs; with a few resident scenes whose set
+    changes every few ticks that costs more than it saves (measured on the
+    served stream of the bench: p50 latency 1.43 s batched against 1.02 s),
+    so it is off by default."""
 
     def __init__(self, budget_bytes: int, chunk: int = 20, mode: int = engine.MODE_MIXED,
                  stream: int = 0, keep_results: bool = True, clock=time.perf_counter, depth: int = 2,
-                 marks=None, batch: bool = True):
+                 marks=None, batch: bool = False):
         if chunk < 1:
             raise ValueError("chunk must be >= 1")
         if depth < 0:

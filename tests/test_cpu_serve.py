@@ -230,7 +230,7 @@ def test_resident_scenes_step_as_a_batch(fake):
     one batch per resident set (made again when the set changes); uneven
     ticks fall back to step_many; every batch is closed before its scenes."""
     clock, calls = fake
-    srv = serve.Server(budget_bytes=1 << 40, chunk=4, clock=clock, marks=_Marks(), depth=0)
+    srv = serve.Server(budget_bytes=1 << 40, chunk=4, clock=clock, marks=_Marks(), depth=0, batch=True)
     srv.submit("a", _named("a"), 12)
     srv.submit("b", _named("b"), 6)
     srv.submit("c", _named("c"), 8, arrival=0.0015)
@@ -246,7 +246,7 @@ def test_resident_scenes_step_as_a_batch(fake):
 
 def test_batching_off_steps_side_by_side(fake):
     clock, calls = fake
-    srv = serve.Server(budget_bytes=1 << 40, chunk=4, clock=clock, marks=_Marks(), depth=0, batch=False)
+    srv = serve.Server(budget_bytes=1 << 40, chunk=4, clock=clock, marks=_Marks(), depth=0)
     srv.submit("a", _named("a"), 8)
     srv.submit("b", _named("b"), 8)
     srv.run()

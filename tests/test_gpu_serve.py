@@ -64,11 +64,14 @@ def test_step_many_in_chunks_equals_one_call(cuda):
         d.close()
 
 
-def test_served_results_equal_alone(cuda):
+@pytest.mark.parametrize("batch", [False, True])
+def test_served_results_equal_alone(cuda, batch):
+    """Served side by side (step_many) or as batches of the resident set: the
+    results are the scenes' own."""
     mix = _mix()
     steps = [23, 17, 30]
     ref = [_alone(sc, s, engine.MODE_MIXED) for sc, s in zip(mix, steps)]
-    srv = serve.Server(budget_bytes=1 << 34, chunk=7)
+    srv = serve.Server(budget_bytes=1 << 34, chunk=7, batch=batch)
     for k, (sc, s) in enumerate(zip(mix, steps)):
         srv.submit(k, sc, s, arrival=0.0)
     done = srv.run()
@@ -78,6 +81,7 @@ def test_served_results_equal_alone(cuda):
     rep = srv.report()
     assert rep["requests"] == 3 and rep["p99_ms"] >= rep["p50_ms"] > 0
     assert rep["peak_active"] == 3
+    assert (rep["batched_ticks"] > 0) == batch
 
 
 def test_memory_estimate_bounds_the_allocation(cuda):
