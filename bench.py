@@ -82,7 +82,7 @@ def _args():
     ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"],
                     help="scene form for the headline value (the other is reported beside it)")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 side measurement")
-    ap.add_argument("--workload", default="batched", choices=["batched", "served", "box"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "served", "box", "drum"])
     ap.add_argument("--no-served", action="store_true", help="batched: skip the served stream")
     ap.add_argument("--no-box", action="store_true", help="batched: skip the 1M-box roofline run")
     ap.add_argument("--no-drum", action="store_true", help="batched: skip the rotating-drum run")
@@ -585,7 +585,7 @@ def _box_roofline(a, stream, barrier, world, local):
                   "gpu_launches": launches, "cell_rebinnings_in_timed_steps": rebuilds}
 
 
-def _drum(a, stream, steps=200, warmup=3):
+def _drum(a, stream, steps=200, warmup=3, plain=True):
     """The rotating drum at full size (500,000 spheres in a 20,480-triangle
     cylinder turning at 1 rad/s, the mesh moved on the device every step) in
     the mixed form, and the same scene's step time in the plain FP64 form."""
@@ -607,6 +607,10 @@ def _drum(a, stream, steps=200, warmup=3):
     ms = e0.elapsed_time(e1)
     rebuilds = ds.rebuilds(sh)[0] - rb0
     ds.close()
+    value = sc.np_ * steps / (ms / 1e3)
+    if not plain:
+        return {"value": value, "unit": "particle-steps/s", "ms_per_step": ms / steps, "steps": steps,
+                "cell_rebinnings_in_timed_steps": rebuilds}
     d64 = engine.DeviceScene(sc, mode=engine.MODE_FP64)
     d64.set_kinematic_bodies(True)
     d64.step(1, check=True, stream=sh)
@@ -616,7 +620,6 @@ def _drum(a, stream, steps=200, warmup=3):
     e1.synchronize()
     ms64 = e0.elapsed_time(e1) / 2
     d64.close()
-    value = sc.np_ * steps / (ms / 1e3)
     return {"workload": "rotating drum: 500,000 spheres r U[2,4] mm on a jittered FCC lattice from the "
                         "bottom, closed cylinder R 0.5 m L 0.4 m of 20,480 triangles turning at 1 rad/s "
                         "(kinematic on the device), wall friction 0.5, dt 5e-6",
@@ -876,6 +879,28 @@ def run_served(a):
     print(json.dumps(line), flush=True)
 
 
+def run_drum(a):
+    """The rotating drum on its own (the batched line carries it as "drum")."""
+    import torch
+    world, rank, local, barrier = _torch_setup()
+    stream = torch.cuda.Stream()
+    clk = ClockSampler(local)
+    with clk:
+        d = _drum(a, stream, steps=a.steps, warmup=a.warmup, plain=not a.no_plain)
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": d["value"], "unit": METRIC, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": d["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic (seeded MT19937 jittered FCC lattice in a cylinder of triangles)",
+        "config": {"workload": "rotating_drum_500k", "particles": 500_000, "triangles": 20_480,
+                   "dt": 5e-6, "mode": "mixed", "l2": "state > L2 (no flush)"},
+        "drum": d, "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = _args()
     if a.impl == "reference":
@@ -884,6 +909,8 @@ def main():
         run_batched(a)
     elif a.workload == "served":
         run_served(a)
+    elif a.workload == "drum":
+        run_drum(a)
     else:
         run_ours(a)
 
