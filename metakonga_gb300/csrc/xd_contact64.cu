@@ -595,7 +595,8 @@ int launch_update_polygon(const xd_polygon_mass_info* dpmi, const double* vlist,
                           xd_polygon_info* dpi, unsigned ntri, cudaStream_t s)
 {
     if (ntri == 0) return XD_OK;
-    k_update_polygon<<<div_up(ntri, 256), 256, 0, s>>>(dpmi, vlist, sphere, dpi, ntri);
+    // FP64-heavy and short: small blocks spread the triangles over every SM
+    k_update_polygon<<<div_up(ntri, 64), 64, 0, s>>>(dpmi, vlist, sphere, dpi, ntri);
     return launch_status("update_polygon_object_data");
 }
 

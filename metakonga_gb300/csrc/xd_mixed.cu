@@ -1488,7 +1488,7 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Con
 // in order) into part[q * gridDim.x + block]; the last block to finish adds
 // the blocks' partials in block order.  The order depends only on n and the
 // grid, so a scene's reaction is the same in every run.
-constexpr unsigned kRxnBlocks = 152;
+constexpr unsigned kRxnBlocks = 152 * 4;   // enough warps in flight to stream the slots from HBM
 constexpr unsigned kRxnThreads = 256;
 
 static unsigned rxn_grid(unsigned n) { return std::max(1u, std::min(kRxnBlocks, (n + kRxnThreads - 1) / kRxnThreads)); }
