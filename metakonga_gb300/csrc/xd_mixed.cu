@@ -1222,6 +1222,54 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
 constexpr unsigned kContactThreads = 64;
 constexpr unsigned kContactBlocks = 152 * 8;
 
+// Squared distance from the origin to triangle abc in FP32 (the closest-point
+// regions of Ericson, Real-Time Collision Detection 5.1.5, with the query
+// point at the origin).  A pre-test only: the distance is continuous across
+// the regions, so a region misjudged by rounding moves it by rounding only.
+__device__ __forceinline__ float tri_dist2_f(float ax, float ay, float az, float bx, float by, float bz, float cx,
+                                             float cy, float cz)
+{
+    const float abx = bx - ax, aby = by - ay, abz = bz - az;
+    const float acx = cx - ax, acy = cy - ay, acz = cz - az;
+    const float d1 = -(abx * ax + aby * ay + abz * az), d2 = -(acx * ax + acy * ay + acz * az);
+    if (d1 <= 0.f && d2 <= 0.f) return ax * ax + ay * ay + az * az;
+    const float d3 = -(abx * bx + aby * by + abz * bz), d4 = -(acx * bx + acy * by + acz * bz);
+    if (d3 >= 0.f && d4 <= d3) return bx * bx + by * by + bz * bz;
+    const float vc = d1 * d4 - d3 * d2;
+    float qx, qy, qz;
+    if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
+        const float v = d1 / (d1 - d3);
+        qx = ax + v * abx;
+        qy = ay + v * aby;
+        qz = az + v * abz;
+        return qx * qx + qy * qy + qz * qz;
+    }
+    const float d5 = -(abx * cx + aby * cy + abz * cz), d6 = -(acx * cx + acy * cy + acz * cz);
+    if (d6 >= 0.f && d5 <= d6) return cx * cx + cy * cy + cz * cz;
+    const float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
+        const float w = d2 / (d2 - d6);
+        qx = ax + w * acx;
+        qy = ay + w * acy;
+        qz = az + w * acz;
+        return qx * qx + qy * qy + qz * qz;
+    }
+    const float va = d3 * d6 - d5 * d4;
+    if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
+        const float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        qx = bx + w * (cx - bx);
+        qy = by + w * (cy - by);
+        qz = bz + w * (cz - bz);
+        return qx * qx + qy * qy + qz * qz;
+    }
+    const float den = 1.f / (va + vb + vc);
+    const float v = vb * den, w = vc * den;
+    qx = ax + v * abx + w * acx;
+    qy = ay + v * aby + w * acy;
+    qz = az + v * abz + w * acz;
+    return qx * qx + qy * qy + qz * qz;
+}
+
 // The pointers of one scene the contact pass reads and writes.
 struct ContactArgs {
     Master M;
@@ -1420,6 +1468,19 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
             const xd_polygon_info* tri = poly + t;
             const unsigned b = (unsigned)__ldg(&tri->id);
             const d3 Pv = tri_vertex(tri->P), Qv = tri_vertex(tri->Q), Rv = tri_vertex(tri->R);
+            {
+                // FP32 pre-test relative to the sphere: a triangle farther than r
+                // (plus a margin far above the FP32 error) is one the FP64 test below
+                // skips as well
+                const float ax = (float)(Pv.x - ip.x), ay = (float)(Pv.y - ip.y), az = (float)(Pv.z - ip.z);
+                const float bx = (float)(Qv.x - ip.x), by = (float)(Qv.y - ip.y), bz = (float)(Qv.z - ip.z);
+                const float cx = (float)(Rv.x - ip.x), cy = (float)(Rv.y - ip.y), cz = (float)(Rv.z - ip.z);
+                const float d2f = tri_dist2_f(ax, ay, az, bx, by, bz, cx, cy, cz);
+                const float span = fabsf(ax) + fabsf(ay) + fabsf(az) + fabsf(bx) + fabsf(by) + fabsf(bz) + fabsf(cx) +
+                                   fabsf(cy) + fabsf(cz);
+                const float lim = (float)r + 1e-6f + 1e-5f * span;
+                if (d2f > lim * lim && d2f < 3.0e38f) continue;
+            }
             const d3 cpt = closest_pt_triangle(Pv, Qv, Rv, ip);
             const double cdist = r - length(ip - cpt);
             if (!(cdist > 0)) continue;
