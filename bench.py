@@ -789,6 +789,7 @@ def run_batched(a):
     if a.settle_steps:
         batch.step(a.settle_steps, check=True, stream=sh)
         rbd0 = sum(d.rebuilds(sh)[0] for d in ds)
+        cnt0 = [d.counters(sh) for d in ds]
         barrier()
         ev0.record(stream)
         batch.step(a.steps, check=False, stream=sh)
@@ -796,6 +797,9 @@ def run_batched(a):
         barrier()
         dms = _max_over_ranks(ev0.elapsed_time(ev1), world)
         drb = sum(d.rebuilds(sh)[0] for d in ds) - rbd0
+        cnt1 = [d.counters(sh) for d in ds]
+        fp64 = {k: sum(c1[k] - c0[k] for c0, c1 in zip(cnt0, cnt1)) / a.steps
+                for k in ("fp64_decisions", "fp64_normal_forces", "fp64_slips")}
         batch.set_timing(True)
         batch.step(ksteps, check=True, stream=sh)
         dkt = batch.kernel_times()
@@ -806,6 +810,7 @@ def run_batched(a):
                  "advance_ms": dkt["advance"][0] / max(dkt["advance"][1], 1),
                  "contact_ms": dkt["contact"][0] / max(dkt["contact"][1], 1),
                  "listed_fraction": listed / n_tot,
+                 "fp64_rechecks_per_step": fp64,
                  "note": "the same 50 steps timed after the spheres fell for the given steps "
                          "(dt 5e-6): contacts throughout the piles"}
     batch.close()
