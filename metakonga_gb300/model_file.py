@@ -27,7 +27,6 @@ are reported in ``Built.ignored``, and polygon shapes other than STL ASCII
 from __future__ import annotations
 
 import dataclasses
-import math
 import os
 
 import numpy as np
@@ -91,9 +90,6 @@ class _Tokens:
         if i == j:
             raise ValueError("model file ends inside a section")
         return t[i:j]
-
-    def words(self, k: int) -> list:
-        return [self.word() for _ in range(k)]
 
     def num(self, kind=float):
         w = self.word()
