@@ -81,7 +81,9 @@ enum {
     CN_SLIPS = 6,      // FP64 slip rechecks (cumulative)
     CN_REBUILDS = 7,   // re-binnings (cumulative)
     CN_RXN = 8,        // blocks of k_rxn_sum done (the last one finishes the sum)
-    kCounters = 9
+    CN_HTRI = 9,       // listed particles with triangles in reach: hlist[0, CN_HTRI)
+    CN_HBACK = 10,     // the other listed particles: hlist[n - CN_HBACK, n)
+    kCounters = 11
 };
 
 struct Master {
@@ -996,7 +998,7 @@ __global__ void __launch_bounds__(256) k_mx_build(MixParams P, const float4* __r
     __shared__ uint2 rows[9][256];
     const unsigned tid = threadIdx.x;
     const unsigned i = blockIdx.x * blockDim.x + tid;
-    bool heavy = false;
+    bool heavy = false, tri = false;
     if (i < P.n) {
         const float4 pi = __ldg(pf + i);
         pref[i] = pi;
@@ -1051,9 +1053,24 @@ __global__ void __launch_bounds__(256) k_mx_build(MixParams P, const float4* __r
             ++nv;
         }
         vcount[i] = nv > kVerletCap ? (kVerletCap | kIncomplete) : nv;
-        heavy = nv > 0 || wm != 0u || (P.ntri && __ldg(tcount + i) != 0u);
+        tri = P.ntri && __ldg(tcount + i) != 0u;
+        heavy = nv > 0 || wm != 0u || tri;
     }
-    warp_append(heavy, i, hlist, counters + CN_HEAVY);
+    // the spheres with triangles in reach first, the others from the end:
+    // the contact pass's warps then run the FP64 triangle work side by side
+    // instead of on a few lanes each
+    warp_append(heavy && tri, i, hlist, counters + CN_HTRI);
+    const unsigned bal = __ballot_sync(0xffffffffu, heavy && !tri);
+    if (bal) {
+        const unsigned lane = threadIdx.x & 31u;
+        const int leader = __ffs(bal) - 1;
+        unsigned base = 0;
+        if ((int)lane == leader) base = atomicAdd(counters + CN_HBACK, (unsigned)__popc(bal));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (heavy && !tri) hlist[P.n - 1u - (base + __popc(bal & ((1u << lane) - 1u)))] = i;
+    }
+    const unsigned hb = __ballot_sync(0xffffffffu, heavy);
+    if (hb && (threadIdx.x & 31u) == 0) atomicAdd(counters + CN_HEAVY, (unsigned)__popc(hb));
 }
 
 // Per-particle contact state carried across the pairs of one particle (the
@@ -1268,6 +1285,13 @@ __device__ __forceinline__ float tri_dist2_f(float ax, float ay, float az, float
     qy = ay + v * aby + w * acy;
     qz = az + v * abz + w * acz;
     return qx * qx + qy * qy + qz * qz;
+}
+
+// Entry t of the listed particles: the ones with triangles in reach fill the
+// list from the front (front of them), the others from the end.
+__device__ __forceinline__ unsigned list_index(unsigned t, unsigned front, unsigned n)
+{
+    return t < front ? t : n - 1u - (t - front);
 }
 
 // The pointers of one scene the contact pass reads and writes.
@@ -1534,13 +1558,13 @@ template <bool RECORD, int HIST>
 __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, ContactArgs C)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) C.counters[CN_REBUILD] = 0;
-    const unsigned total = C.counters[CN_HEAVY];
-    // runs of 32 consecutive list entries (neighbouring slots) go to the warps
-    // of all blocks in turn: every SM gets an equal share however short the list
+    const unsigned total = C.counters[CN_HEAVY], front = C.counters[CN_HTRI];
+    // runs of 32 consecutive list entries go to the warps of all blocks in
+    // turn: every SM gets an equal share however short the list
     const unsigned warps = gridDim.x * (blockDim.x / 32u);
     const unsigned gw = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u;
     for (unsigned t = gw * 32u + (threadIdx.x & 31u); t < total; t += warps * 32u)
-        contact_entry<RECORD, HIST>(P, C, __ldg(C.hlist + t));
+        contact_entry<RECORD, HIST>(P, C, __ldg(C.hlist + list_index(t, front, P.n)));
 }
 
 // Body reactions: rxn[(b * 6 + q) * n + i] summed over i in a fixed order,
@@ -2216,6 +2240,8 @@ static int rebuild(MixedScene* s, cudaStream_t q)
     int st = flush_reactions(s, q);
     if (st != XD_OK) return st;
     st = cuda_status(cudaMemsetAsync(s->counters + CN_GAPS, 0, 2 * sizeof(unsigned), q), "mixed re-binning");
+    if (st == XD_OK)
+        st = cuda_status(cudaMemsetAsync(s->counters + CN_HTRI, 0, 2 * sizeof(unsigned), q), "mixed re-binning");
     if (st != XD_OK) return st;
     k_mx_keys<<<blocks(n, 256), 256, 0, q>>>(s->P, s->pf, s->keys, s->vals);
     st = launch_status("mixed keys");
@@ -2934,7 +2960,7 @@ __global__ void __launch_bounds__(kContactThreads) k_batch_contact(const BatchSc
     const unsigned total = __ldg(chunk_start + ns);
     const unsigned per = (total + warps - 1u) / warps;
     const unsigned c0 = gw * per, c1 = min(total, c0 + per);
-    unsigned cur = 0xffffffffu, lo = 0, heavy = 0;
+    unsigned cur = 0xffffffffu, lo = 0, heavy = 0, front = 0;
     for (unsigned ch = c0; ch < c1; ++ch) {
         if (cur == 0xffffffffu || ch >= __ldg(chunk_start + cur + 1)) {
             // the scene holding run ch: the last s with chunk_start[s] <= ch
@@ -2951,9 +2977,10 @@ __global__ void __launch_bounds__(kContactThreads) k_batch_contact(const BatchSc
             copy_words(&W.C, &D[cur].C, sizeof(ContactArgs), lane, 32u);
             __syncwarp();
             heavy = W.C.counters[CN_HEAVY];
+            front = W.C.counters[CN_HTRI];
         }
         const unsigned t = (ch - lo) * 32u + lane;
-        if (t < heavy) contact_entry<false, 0>(W.P, W.C, __ldg(W.C.hlist + t));
+        if (t < heavy) contact_entry<false, 0>(W.P, W.C, __ldg(W.C.hlist + list_index(t, front, W.P.n)));
     }
 }
 
