@@ -1480,6 +1480,9 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
         const d3 iv = mk(df_to_d(vh.x, vl.x), df_to_d(vh.y, vl.y), df_to_d(vh.z, vl.z));
         const d3 iw = mk(df_to_d(wh.x, wl.x), df_to_d(wh.y, wl.y), df_to_d(wh.z, wl.z));
         d3 f = mk(0, 0, 0), Ft = mk(0, 0, 0), Mo = mk(0, 0, 0);
+        const double sr = sqrt(r);
+        unsigned cb = 0xffffffffu;
+        xd::Fc cc;
         const bool listed = !(tc & kIncomplete);
         unsigned kb = 0, ke = tc;
         if (!listed) {
@@ -1513,12 +1516,17 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
             unit = unit / length(unit);
             const d3 pvel = tri_vertex(pmi[b].vel), pom = tri_vertex(pmi[b].omega);
             const d3 dv = P.rolling ? (pvel + cross(pom, po2cp)) - (iv + cross(iw, r * unit)) : (pvel - iv);
-            xd::Fc c;
-            c.kn = P.pb_c43Eeq[b] * sqrt(r);
-            c.vn = sqrt((4.0 * m * c.kn) / P.pb_one_b2[b]);
-            c.ks = c.kn * P.pb_sratio[b];
-            c.vs = c.vn * P.pb_sratio[b];
-            c.mu = P.pb_fric[b];
+            if (b != cb) {
+                // getConstant with the body's hoisted material terms (Meq = m,
+                // Req = r): the same for every triangle of the body
+                cc.kn = P.pb_c43Eeq[b] * sr;
+                cc.vn = sqrt((4.0 * m * cc.kn) / P.pb_one_b2[b]);
+                cc.ks = cc.kn * P.pb_sratio[b];
+                cc.vs = cc.vn * P.pb_sratio[b];
+                cc.mu = P.pb_fric[b];
+                cb = b;
+            }
+            const xd::Fc& c = cc;
             d3 Fn = mk(0, 0, 0);
             if (HIST) {
                 Fn = normal_force(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit);
