@@ -1329,8 +1329,7 @@ struct ContactArgs {
 // The contact pass of one listed particle (slot i): its Verlet-list pairs,
 // planes and triangles, summed in a fixed order into Fc/Mc.
 template <bool RECORD, int HIST>
-__device__ __forceinline__ void contact_entry(const MixParams& P, const ContactArgs& C, const unsigned i,
-                                              unsigned* cand, unsigned& ncand)
+__device__ __forceinline__ void contact_entry(const MixParams& P, const ContactArgs& C, const unsigned i)
 {
     const Master& M = C.M;
     const float4* __restrict__ pf = C.pf;
@@ -1486,10 +1485,6 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
         xd::Fc cc;
         const bool listed = !(tc & kIncomplete);
         unsigned kb = 0, ke = tc;
-        // without history, a complete list goes to the warp's shared pass
-        // (coop_triangles): only the triangles that pass the FP32 pre-test
-        // are handed over, in list order
-        const bool handover = HIST == 0 && listed;
         if (!listed) {
             const unsigned key = __ldg(keys + i);
             kb = lower_bound_u(tpk, tcap, key);
@@ -1512,10 +1507,6 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
                                    fabsf(cy) + fabsf(cz);
                 const float lim = (float)r + 1e-6f + 1e-5f * span;
                 if (d2f > lim * lim && d2f < 3.0e38f) continue;
-            }
-            if (handover) {
-                cand[ncand++] = t;
-                continue;
             }
             const d3 cpt = closest_pt_triangle(Pv, Qv, Rv, ip);
             const double cdist = r - length(ip - cpt);
@@ -1561,153 +1552,14 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
                 rb[5 * (size_t)n] += rm.z;
             }
         }
-        if (!handover) {
-            F.x += (float)f.x;
-            F.y += (float)f.y;
-            F.z += (float)f.z;
-        }
+        F.x += (float)f.x;
+        F.y += (float)f.y;
+        F.z += (float)f.z;
     }
     if (HIST == 1) hist_end_all(ht, hs, i);
     Fc[i] = F;
     Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
     if (RECORD) rec_count[i] = nc;
-}
-
-// One triangle against one sphere: the FP64 contact of
-// particle_polygonObject_collision_kernel<1> as in contact_entry's own loop.
-// False when they do not touch; else Fn, the contact point relative to the
-// body's origin and, when DHS forms one (ft_set), the tangential force.
-__device__ __forceinline__ bool tri_contact(const MixParams& P, const xd_polygon_info* __restrict__ tri,
-                                            const xd_polygon_mass_info* __restrict__ pmi, const d3& ip,
-                                            const d3& iv, const d3& iw, double r, double sr, double m, d3& Fn,
-                                            d3& Ft, bool& ft_set, d3& po2cp, unsigned& b)
-{
-    b = (unsigned)__ldg(&tri->id);
-    const d3 Pv = tri_vertex(tri->P), Qv = tri_vertex(tri->Q), Rv = tri_vertex(tri->R);
-    const d3 cpt = closest_pt_triangle(Pv, Qv, Rv, ip);
-    const double cdist = r - length(ip - cpt);
-    if (!(cdist > 0)) return false;
-    po2cp = cpt - tri_vertex(pmi[b].origin);
-    d3 unit = -cross(Qv - Pv, Rv - Pv);
-    unit = unit / length(unit);
-    const d3 pvel = tri_vertex(pmi[b].vel), pom = tri_vertex(pmi[b].omega);
-    const d3 dv = P.rolling ? (pvel + cross(pom, po2cp)) - (iv + cross(iw, r * unit)) : (pvel - iv);
-    xd::Fc c;
-    c.kn = P.pb_c43Eeq[b] * sr;
-    c.vn = sqrt((4.0 * m * c.kn) / P.pb_one_b2[b]);
-    c.ks = c.kn * P.pb_sratio[b];
-    c.vs = c.vn * P.pb_sratio[b];
-    c.mu = P.pb_fric[b];
-    const double nan = __longlong_as_double(0x7ff8000000000000ll);
-    Ft = mk(nan, nan, nan);
-    d3 Mo = mk(0, 0, 0);
-    dhs(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit, P.dt, Ft, Fn, Mo);
-    ft_set = !isnan(Ft.x);
-    return true;
-}
-
-struct TriItem {
-    d3 Fn, Ft, pc;
-    unsigned b, flags;   // flags: 1 touching, 2 a new tangential force
-};
-
-struct TriShared {
-    unsigned cand[32 * kTriCap];   // the warp's handed-over triangles, lane after lane
-    TriItem item[32];
-};
-
-// The triangle contacts handed over by the lanes of a warp (all 32 lanes
-// call this): the warp computes them 32 at a time, every lane on one
-// (sphere, triangle) pair, and each lane then takes its own pairs' results in
-// list order -- the tangential force persisting across triangles, the
-// reaction slots and the force sum exactly as contact_entry's own loop.
-__device__ __forceinline__ void coop_triangles(const MixParams& P, const ContactArgs& C, const bool active,
-                                               const unsigned i, const unsigned* cand, const unsigned ncand,
-                                               TriShared& S)
-{
-    constexpr unsigned full = 0xffffffffu;
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned cnt = active ? ncand : 0u;
-    unsigned incl = cnt;
-    for (unsigned o = 1; o < 32u; o <<= 1) {
-        const unsigned v = __shfl_up_sync(full, incl, o);
-        if (lane >= o) incl += v;
-    }
-    const unsigned excl = incl - cnt;
-    const unsigned total = __shfl_sync(full, incl, 31);
-    if (total == 0) return;
-    for (unsigned k = 0; k < cnt; ++k) S.cand[excl + k] = cand[k];
-    const Master& M = C.M;
-    double px = 0, py = 0, pz = 0, vx = 0, vy = 0, vz = 0, wx = 0, wy = 0, wz = 0, r = 0, sr = 0, m = 0;
-    if (cnt) {
-        const float4 vh = __ldg(M.vh + i), vl = __ldg(M.vl + i);
-        const float4 wl = __ldg(M.wl + i), wh = __ldg(M.wh + i);
-        m = __ldg(C.mass0 + __float_as_uint(wl.w));
-        px = __ldg(M.x + i);
-        py = __ldg(M.y + i);
-        pz = __ldg(M.z + i);
-        r = __ldg(M.r + i);
-        sr = sqrt(r);
-        vx = df_to_d(vh.x, vl.x);
-        vy = df_to_d(vh.y, vl.y);
-        vz = df_to_d(vh.z, vl.z);
-        wx = df_to_d(wh.x, wl.x);
-        wy = df_to_d(wh.y, wl.y);
-        wz = df_to_d(wh.z, wl.z);
-    }
-    __syncwarp();
-    d3 f = mk(0, 0, 0), Ftr = mk(0, 0, 0);
-    const unsigned n = P.n;
-    for (unsigned base = 0; base < total; base += 32u) {
-        const unsigned item = base + lane;
-        // the lane owning pair `item`: the last lane whose first pair is at or before it
-        unsigned owner = 0;
-        for (unsigned bit = 16; bit; bit >>= 1) {
-            const unsigned e = __shfl_sync(full, excl, owner + bit);
-            if (e <= item) owner += bit;
-        }
-        const d3 ip = mk(__shfl_sync(full, px, owner), __shfl_sync(full, py, owner), __shfl_sync(full, pz, owner));
-        const d3 iv = mk(__shfl_sync(full, vx, owner), __shfl_sync(full, vy, owner), __shfl_sync(full, vz, owner));
-        const d3 iw = mk(__shfl_sync(full, wx, owner), __shfl_sync(full, wy, owner), __shfl_sync(full, wz, owner));
-        const double orr = __shfl_sync(full, r, owner), osr = __shfl_sync(full, sr, owner);
-        const double om = __shfl_sync(full, m, owner);
-        TriItem res;
-        res.flags = 0;
-        if (item < total) {
-            bool set = false;
-            if (tri_contact(P, C.poly + S.cand[item], C.pmi, ip, iv, iw, orr, osr, om, res.Fn, res.Ft, set, res.pc,
-                            res.b))
-                res.flags = 1u | (set ? 2u : 0u);
-        }
-        S.item[lane] = res;
-        __syncwarp();
-        const unsigned k1 = min(incl, base + 32u);
-        for (unsigned k = max(excl, base); k < k1; ++k) {
-            const TriItem& it = S.item[k - base];
-            if (!(it.flags & 1u)) continue;
-            if (it.flags & 2u) Ftr = it.Ft;
-            const d3 fc = it.Fn + Ftr;
-            f += fc;
-            const d3 rm = -cross(it.pc, fc);
-            if (C.rxn_on) {
-                double* rb = C.rxn + (size_t)it.b * 6 * n + i;
-                rb[0] -= fc.x;
-                rb[n] -= fc.y;
-                rb[2 * (size_t)n] -= fc.z;
-                rb[3 * (size_t)n] += rm.x;
-                rb[4 * (size_t)n] += rm.y;
-                rb[5 * (size_t)n] += rm.z;
-            }
-        }
-        __syncwarp();
-    }
-    if (cnt) {
-        float4 F = C.Fc[i];
-        F.x += (float)f.x;
-        F.y += (float)f.y;
-        F.z += (float)f.z;
-        C.Fc[i] = F;
-    }
 }
 
 template <bool RECORD, int HIST>
@@ -1719,17 +1571,8 @@ __global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, Con
     // turn: every SM gets an equal share however short the list
     const unsigned warps = gridDim.x * (blockDim.x / 32u);
     const unsigned gw = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u;
-    __shared__ TriShared tsh[kContactThreads / 32];
-    // warp-uniform trips: the triangle pass needs every lane
-    for (unsigned base = gw * 32u; base < total; base += warps * 32u) {
-        const unsigned t = base + (threadIdx.x & 31u);
-        const bool act = t < total;
-        const unsigned i = act ? __ldg(C.hlist + list_index(t, front, P.n)) : 0u;
-        unsigned cand[kTriCap];
-        unsigned ncand = 0;
-        if (act) contact_entry<RECORD, HIST>(P, C, i, cand, ncand);
-        if (HIST == 0) coop_triangles(P, C, act, i, cand, ncand, tsh[threadIdx.x / 32u]);
-    }
+    for (unsigned t = gw * 32u + (threadIdx.x & 31u); t < total; t += warps * 32u)
+        contact_entry<RECORD, HIST>(P, C, __ldg(C.hlist + list_index(t, front, P.n)));
 }
 
 // Body reactions: rxn[(b * 6 + q) * n + i] summed over i in a fixed order,
@@ -3118,7 +2961,6 @@ __global__ void __launch_bounds__(kContactThreads) k_batch_contact(const BatchSc
                                                                    const unsigned* __restrict__ chunk_start)
 {
     __shared__ WarpScene ws[kContactThreads / 32];
-    __shared__ TriShared tsh[kContactThreads / 32];
     const unsigned lane = threadIdx.x & 31u, wb = threadIdx.x / 32u;
     WarpScene& W = ws[wb];
     const unsigned warps = gridDim.x * (kContactThreads / 32u);
@@ -3146,12 +2988,7 @@ __global__ void __launch_bounds__(kContactThreads) k_batch_contact(const BatchSc
             front = W.C.counters[CN_HTRI];
         }
         const unsigned t = (ch - lo) * 32u + lane;
-        const bool act = t < heavy;
-        const unsigned i = act ? __ldg(W.C.hlist + list_index(t, front, W.P.n)) : 0u;
-        unsigned cand[kTriCap];
-        unsigned ncand = 0;
-        if (act) contact_entry<false, 0>(W.P, W.C, i, cand, ncand);
-        coop_triangles(W.P, W.C, act, i, cand, ncand, tsh[wb]);
+        if (t < heavy) contact_entry<false, 0>(W.P, W.C, __ldg(W.C.hlist + list_index(t, front, W.P.n)));
     }
 }
 
