@@ -3374,6 +3374,11 @@ int mixed_batch_step(MixedBatch* b, unsigned nsteps, cudaStream_t q)
     for (size_t k = 0; k < b->scenes.size() && !stale; ++k) stale = b->versions[k] != b->scenes[k]->version;
     int st = XD_OK;
     if (stale) {
+        for (size_t k = 0; k < b->scenes.size(); ++k) {
+            const MixedScene* sc = b->scenes[k];
+            if (sc->hslots || sc->kinematic)
+                return set_error(XD_ERR_STATE, "batch: scene %u now keeps history or kinematic bodies", (unsigned)k);
+        }
         st = cuda_status(cudaStreamSynchronize(q), "batch");   // graphs in flight finish first
         if (st == XD_OK) st = prepare_batch(b);
         if (st != XD_OK) return st;

@@ -874,6 +874,7 @@ int xd_scene_step_many(xd_scene* const* scenes, const unsigned* nsteps, unsigned
 
 struct xd_batch {
     MixedBatch* mixed = nullptr;
+    std::vector<xd_scene*> scenes;
 };
 
 int xd_batch_create(xd_scene* const* scenes, unsigned count, xd_batch** out)
@@ -898,6 +899,7 @@ int xd_batch_create(xd_scene* const* scenes, unsigned count, xd_batch** out)
         return set_error(XD_ERR_NOMEM, "batch_create: host allocation");
     }
     h->mixed = b;
+    h->scenes.assign(scenes, scenes + count);
     *out = h;
     return XD_OK;
 }
@@ -905,6 +907,9 @@ int xd_batch_create(xd_scene* const* scenes, unsigned count, xd_batch** out)
 int xd_batch_step(xd_batch* b, unsigned nsteps, int check, void* stream)
 {
     if (!b) return set_error(XD_ERR_INVALID, "batch_step: null batch");
+    for (size_t k = 0; k < b->scenes.size(); ++k)
+        if (b->scenes[k]->emit_period || b->scenes[k]->active != b->scenes[k]->np)
+            return set_error(XD_ERR_STATE, "batch_step: scene %u has an emitter", (unsigned)k);
     cudaStream_t q = static_cast<cudaStream_t>(stream);
     int st = mixed_batch_step(b->mixed, nsteps, q);
     if (st == XD_OK && check) st = cuda_status(cudaStreamSynchronize(q), "batch_step");

@@ -69,6 +69,28 @@ def test_batch_equals_each_scene_alone(cuda, moved, timed):
             assert ba.tobytes() == bb.tobytes()
 
 
+def test_batch_refuses_scenes_changed_after_creation(cuda):
+    """A scene given history, kinematic bodies or an emitter after the batch
+    was made: the batch's next step fails instead of ignoring the change."""
+    for change in ("history", "kinematic", "emitter"):
+        sc = small_drum(n=200, seed=3)
+        ds = [engine.DeviceScene(sc, mode=engine.MODE_MIXED), engine.DeviceScene(packed_scene(n_side=4),
+                                                                               mode=engine.MODE_MIXED)]
+        b = engine.Batch(ds)
+        b.step(2, check=True)
+        if change == "history":
+            ds[0].set_tangential_history(4)
+        elif change == "kinematic":
+            ds[0].set_kinematic_bodies(True)
+        else:
+            ds[0].set_emitter(10, [50, 50], active=100)
+        with pytest.raises(Exception):
+            b.step(2, check=True)
+        b.close()
+        for d in ds:
+            d.close()
+
+
 def test_batch_refuses_history_and_plain_scenes(cuda):
     sc = packed_scene(n_side=4)
     d1 = engine.DeviceScene(sc, mode=engine.MODE_MIXED)
