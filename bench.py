@@ -212,6 +212,9 @@ def _cpu_scene(spec):
     scene k of the count-scene hopper batch."""
     if spec[0] == "box":
         return _scene(spec[1])
+    if spec[0] == "settle":
+        from metakonga_gb300 import scenes
+        return scenes.settle_box()
     from metakonga_gb300 import scenes
     return scenes.hopper(**scenes.hopper_batch(count=spec[1])[spec[2]])
 
@@ -633,6 +636,36 @@ def _drum(a, stream, steps=200, warmup=3, plain=True):
             "ratio": value / (sc.np_ / (ms64 / 1e3))}
 
 
+def _settle_small(stream, steps=1000, cpu=True):
+    """The reference's CPU-runnable case: the 8,000-sphere lattice settle in a
+    box of five planes (FP64, dt 1e-5) in both forms on the GPU, and the
+    reference CPU path on the host beside it."""
+    import torch
+
+    from metakonga_gb300 import engine, scenes
+    sc = scenes.settle_box()
+    sh = stream.cuda_stream
+    out = {"workload": "settle_box_8000: 20x20x20 lattice, pitch 11 mm, r 5 mm, five plane walls, dt 1e-5",
+           "steps": steps}
+    for name, mode in (("fp64", engine.MODE_FP64), ("mixed", engine.MODE_MIXED)):
+        ds = engine.DeviceScene(sc, mode=mode)
+        ds.step(3, check=True, stream=sh)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ds.step(steps, check=False, stream=sh)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        ds.close()
+        out[name] = {"value": sc.np_ * steps / (ms / 1e3), "ms_per_step": ms / steps}
+    if cpu:
+        vals, times = cpu_baseline([("settle", 0)], 20)
+        out["reference_cpu_path"] = {"value": vals[0], "cores": 1, "sample": f"20 steps, {times[0]:.2f} s"}
+        out["fp64_vs_cpu"] = out["fp64"]["value"] / vals[0]
+    return out
+
+
 def _served(a, stream, plain=True):
     """The served request stream: report of the continuous-batching server,
     and the same requests' time alone in the FP64 form."""
@@ -834,6 +867,7 @@ def run_batched(a):
     check = _fp64_check(scs[k_med])
     check["scene"] = k_med
     box_roof, box = _box_roofline(a, stream, barrier, world, local) if not a.no_box else (None, None)
+    settle = _settle_small(stream, cpu=not a.no_cpu_baseline) if rank == 0 and not a.no_box else None
     if box:
         box["roofline"] = box_roof
     drum = _drum(a, stream) if not a.no_drum and rank == 0 else None
@@ -879,6 +913,7 @@ def run_batched(a):
                       "bytes_per_particle": B_ADVANCE + B_CONTACT["mixed"]},
         "roofline": roof,
         "single_scene_box": box,
+        "settle_8000": settle,
         "drum": drum,
         "served": served,
         "cpu_baseline": cpu,
