@@ -2,6 +2,7 @@
 // (dem_simulation::oneStepAnalysis, dem_simulation.cpp:447-469).
 #include <cuda_runtime.h>
 
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -60,6 +61,11 @@ struct xd_scene {
     std::vector<unsigned> emit_groups;   // empty: one particle per creation
     unsigned emit_next = 0;              // next group to hand out
     unsigned long long emit_step = 0;    // steps run since the emitter was set
+    // FP64 step graphs: 8 middle steps, one middle step, the last step of a
+    // call; captured for `graphs_np` particles and the history setting
+    cudaGraphExec_t graphs[3] = {};
+    unsigned graphs_np = ~0u;
+    bool use_graphs = true;
 };
 
 namespace {
@@ -112,8 +118,19 @@ HistTable history_of(xd_scene* s)
     return h;
 }
 
+void free_fp64_graphs(xd_scene* s)
+{
+    for (auto& g : s->graphs)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    s->graphs_np = ~0u;
+}
+
 void free_scene(xd_scene* s)
 {
+    free_fp64_graphs(s);
     free_history(s);
     if (s->mixed) mixed_destroy(s->mixed);
     s->mixed = nullptr;
@@ -268,6 +285,10 @@ int xd_scene_create(const xd_scene_desc* d, xd_scene** out)
     s->np = d->np;
     s->active = d->np;
     s->ntri = d->ntri;
+    {
+        const char* ng = getenv("XDEM_NO_GRAPHS");
+        s->use_graphs = !(ng && ng[0] && ng[0] != '0');
+    }
     s->nbodies = d->ntri ? d->nbodies : 0;
     s->nplanes = d->nplanes;
     s->ncell = h.ncell;
@@ -664,48 +685,83 @@ int fp64_steps(xd_scene* s, unsigned nsteps, cudaStream_t q)
         st = launch_vv_position(P, s->pos, s->vel, s->acc, np, q);
     }
     if (st != XD_OK) return st;
-    for (unsigned t = 0; t < nsteps; ++t) {
+    // one step: grid, contacts, and the velocity update, fused with the next
+    // step's position update unless `last`
+    auto one_step = [&](bool last, cudaStream_t qq) {
+        int r = XD_OK;
         {
-            PhaseSpan ps(s, 1, q);
-            st = launch_hash(P, s->hash, s->index, s->pos, np, 0, q);
-            if (st == XD_OK && s->ntri) st = launch_hash(P, s->hash, s->index, s->sphere, s->ntri, np, q);
+            PhaseSpan ps(s, 1, qq);
+            r = launch_hash(P, s->hash, s->index, s->pos, np, 0, qq);
+            if (r == XD_OK && s->ntri) r = launch_hash(P, s->hash, s->index, s->sphere, s->ntri, np, qq);
         }
-        if (st == XD_OK) {
-            PhaseSpan ps(s, 2, q);
-            st = reorder_and_find_cell_start(s->hash, s->index, s->cstart, s->cend, s->sorted, ng,
-                                             s->ncell, s->scratch, q, false);
+        if (r == XD_OK) {
+            PhaseSpan ps(s, 2, qq);
+            r = reorder_and_find_cell_start(s->hash, s->index, s->cstart, s->cend, s->sorted, ng, s->ncell,
+                                            s->scratch, qq, false);
         }
-        if (st == XD_OK) {
-            PhaseSpan ps(s, 3, q);
-            st = launch_p2p(P, s->pos, s->vel, s->omega, s->force, s->moment, s->mass, s->sorted,
-                            s->cstart, s->cend, s->cp_pp, np, q, hp);
+        if (r == XD_OK) {
+            PhaseSpan ps(s, 3, qq);
+            r = launch_p2p(P, s->pos, s->vel, s->omega, s->force, s->moment, s->mass, s->sorted, s->cstart,
+                           s->cend, s->cp_pp, np, qq, hp);
         }
-        if (st == XD_OK && s->nplanes) {
-            PhaseSpan ps(s, 4, q);
-            st = launch_planes(P, s->planes, s->cp_planes, 1, s->nplanes, s->pos, s->vel, s->omega,
-                               s->force, s->moment, s->mass, np, q, hp);
+        if (r == XD_OK && s->nplanes) {
+            PhaseSpan ps(s, 4, qq);
+            r = launch_planes(P, s->planes, s->cp_planes, 1, s->nplanes, s->pos, s->vel, s->omega, s->force,
+                              s->moment, s->mass, np, qq, hp);
         }
-        if (st == XD_OK && s->ntri) {
-            PhaseSpan ps(s, 5, q);
-            st = launch_polygon(P, s->poly, s->pmi, s->pos, s->vel, s->omega, s->force, s->moment,
-                                s->mass, s->sorted, s->cstart, s->cend, s->cp_poly, s->nbodies,
-                                s->poly_scratch, q, hp);
+        if (r == XD_OK && s->ntri) {
+            PhaseSpan ps(s, 5, qq);
+            r = launch_polygon(P, s->poly, s->pmi, s->pos, s->vel, s->omega, s->force, s->moment, s->mass,
+                               s->sorted, s->cstart, s->cend, s->cp_poly, s->nbodies, s->poly_scratch, qq, hp);
         }
-        if (st == XD_OK) {
-            PhaseSpan ps(s, 0, q);
-            if (t + 1 < nsteps && !kin) {
-                st = launch_vv_velocity_position(P, s->pos, s->vel, s->acc, s->omega, s->alpha,
-                                                 s->force, s->moment, s->mass, s->inertia, np, q);
+        if (r == XD_OK) {
+            PhaseSpan ps(s, 0, qq);
+            if (!last && !kin) {
+                r = launch_vv_velocity_position(P, s->pos, s->vel, s->acc, s->omega, s->alpha, s->force,
+                                                s->moment, s->mass, s->inertia, np, qq);
             } else {
-                st = launch_vv_velocity(P, s->vel, s->acc, s->omega, s->alpha, s->force, s->moment,
-                                        s->mass, s->inertia, np, q);
+                r = launch_vv_velocity(P, s->vel, s->acc, s->omega, s->alpha, s->force, s->moment, s->mass,
+                                       s->inertia, np, qq);
                 // moving bodies come before the next step's position update
-                if (st == XD_OK && t + 1 < nsteps) st = move_bodies();
-                if (st == XD_OK && t + 1 < nsteps) st = launch_vv_position(P, s->pos, s->vel, s->acc, np, q);
+                if (r == XD_OK && !last) r = move_bodies();
+                if (r == XD_OK && !last) r = launch_vv_position(P, s->pos, s->vel, s->acc, np, qq);
             }
         }
-        if (st != XD_OK) return st;
+        return r;
+    };
+    if (!s->use_graphs || s->timing || kin || nsteps < 4) {
+        for (unsigned t = 0; t < nsteps && st == XD_OK; ++t) st = one_step(t + 1 == nsteps, q);
+        return st;
     }
+    // the steps as CUDA graphs (no host decision inside a step): captured at
+    // the first call and whenever the particle count changed
+    if (s->graphs_np != np) {
+        free_fp64_graphs(s);
+        for (int kind = 0; kind < 3 && st == XD_OK; ++kind) {
+            cudaStream_t cs = nullptr;
+            st = cuda_status(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "scene graph stream");
+            if (st != XD_OK) break;
+            st = cuda_status(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "scene graph capture");
+            const unsigned count = kind == 0 ? 8u : 1u;
+            for (unsigned k = 0; k < count && st == XD_OK; ++k) st = one_step(kind == 2, cs);
+            cudaGraph_t g = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(cs, &g);
+            if (st == XD_OK) st = cuda_status(e, "scene graph capture");
+            if (st == XD_OK) st = cuda_status(cudaGraphInstantiate(&s->graphs[kind], g, 0), "scene graph instantiate");
+            if (g) cudaGraphDestroy(g);
+            cudaStreamDestroy(cs);
+        }
+        if (st != XD_OK) {
+            free_fp64_graphs(s);
+            return st;
+        }
+        s->graphs_np = np;
+    }
+    unsigned mid = nsteps - 1;
+    for (; mid >= 8 && st == XD_OK; mid -= 8) st = cuda_status(cudaGraphLaunch(s->graphs[0], q), "scene graph launch");
+    for (; mid > 0 && st == XD_OK; --mid) st = cuda_status(cudaGraphLaunch(s->graphs[1], q), "scene graph launch");
+    if (st == XD_OK) st = cuda_status(cudaGraphLaunch(s->graphs[2], q), "scene graph launch");
+    if (st != XD_OK) return st;
     return XD_OK;
 }
 
@@ -811,6 +867,8 @@ int xd_scene_set_tangential_history(xd_scene* s, unsigned slots)
         return set_error(XD_ERR_INVALID, "scene_set_tangential_history: at most %u contacts per particle",
                          kHistMaxSlots);
     if (s->mixed) return mixed_set_history(s->mixed, slots);
+    cudaDeviceSynchronize();   // the step graphs hold the tables: replaced after what is queued
+    free_fp64_graphs(s);
     free_history(s);
     if (slots == 0 || s->np == 0) return XD_OK;
     const size_t e = (size_t)slots * s->np;
