@@ -784,8 +784,18 @@ def run_batched(a):
     host = []
     for d, sc in zip(ds, scs):
         st = d.download(sh)
-        h = {k: torch.from_numpy(np.ascontiguousarray(st[k])).pin_memory() for k in keys}
-        for k in ("force", "moment", "mass", "inertia"):
+        # one pinned block per scene, the arrays back to back in the order the
+        # library stages them (pos, vel, acc, omega, alpha, mass, inertia): the
+        # upload and the download then go as one copy each
+        n = sc.np_
+        block = torch.empty(18 * n, dtype=torch.float64).pin_memory()
+        h, off = {}, 0
+        for k, w in (("pos", 4), ("vel", 3), ("acc", 3), ("omega", 3), ("alpha", 3), ("mass", 1), ("inertia", 1)):
+            h[k] = block[off:off + w * n]
+            src = st[k] if k in keys else getattr(sc, k)
+            h[k].copy_(torch.from_numpy(np.ascontiguousarray(src).reshape(-1)))
+            off += w * n
+        for k in ("force", "moment"):
             h[k] = torch.from_numpy(np.ascontiguousarray(getattr(sc, k))).pin_memory()
         host.append(h)
     h2d = sum(sum(h[k].numel() * 8 for k in keys + ("mass", "inertia")) for h in host)

@@ -2039,6 +2039,39 @@ static int ensure_xfer(MixedScene* s)
 
 static int reset_history(MixedScene* s, cudaStream_t q);
 
+// Host <-> transfer-buffer copies of several arrays: arrays the caller keeps
+// back to back in the buffer's own order go as one copy (a null host array
+// is skipped and ends a run).
+struct CopyPart {
+    double* dev;
+    double* host;
+    size_t count;
+};
+
+static int copy_runs(const CopyPart* parts, int k, bool to_device, cudaStream_t q, const char* what)
+{
+    int st = XD_OK;
+    for (int a = 0; a < k && st == XD_OK;) {
+        if (!parts[a].host || !parts[a].count) {
+            ++a;
+            continue;
+        }
+        int e = a + 1;
+        size_t n = parts[a].count;
+        while (e < k && parts[e].host && parts[e].host == parts[a].host + n && parts[e].dev == parts[a].dev + n) {
+            n += parts[e].count;
+            ++e;
+        }
+        st = cuda_status(to_device ? cudaMemcpyAsync(parts[a].dev, parts[a].host, sizeof(double) * n,
+                                                     cudaMemcpyHostToDevice, q)
+                                   : cudaMemcpyAsync(parts[a].host, parts[a].dev, sizeof(double) * n,
+                                                     cudaMemcpyDeviceToHost, q),
+                         what);
+        a = e;
+    }
+    return st;
+}
+
 int mixed_upload(MixedScene* s, const double* pos, const double* vel, const double* acc,
                  const double* omega, const double* alpha, const double* mass,
                  const double* inertia, cudaStream_t q, bool sync)
@@ -2061,17 +2094,11 @@ int mixed_upload(MixedScene* s, const double* pos, const double* vel, const doub
     double* b = s->xfer;
     double *dpos = b, *dvel = b + 4 * n, *dacc = dvel + 3 * n, *dom = dacc + 3 * n,
            *dal = dom + 3 * n, *dm = dal + 3 * n, *dI = dm + n;
-    auto cp = [&](double* d, const double* h, size_t cnt) {
-        if (st == XD_OK)
-            st = cuda_status(cudaMemcpyAsync(d, h, sizeof(double) * cnt, cudaMemcpyHostToDevice, q), "mixed upload");
-    };
-    cp(dpos, pos, 4 * n);
-    cp(dvel, vel, 3 * n);
-    cp(dacc, acc, 3 * n);
-    cp(dom, omega, 3 * n);
-    cp(dal, alpha, 3 * n);
-    cp(dm, mass, n);
-    cp(dI, inertia, n);
+    const CopyPart parts[7] = { { dpos, const_cast<double*>(pos), 4 * n },   { dvel, const_cast<double*>(vel), 3 * n },
+                                { dacc, const_cast<double*>(acc), 3 * n },   { dom, const_cast<double*>(omega), 3 * n },
+                                { dal, const_cast<double*>(alpha), 3 * n },  { dm, const_cast<double*>(mass), n },
+                                { dI, const_cast<double*>(inertia), n } };
+    st = copy_runs(parts, 7, true, q, "mixed upload");
     if (st != XD_OK) return st;
     s->cur = 0;
     s->cells_clean = false;   // the state is in upload order again: the next step re-bins
@@ -2107,17 +2134,10 @@ int mixed_download(MixedScene* s, double* pos, double* vel, double* acc, double*
     k_mx_store<<<blocks(s->cap, 256), 256, 0, q>>>(Pc, s->m[s->cur], s->mass0, dpos, dvel, dacc, dom,
                                                    dal, df, dmo);
     st = launch_status("mixed download");
-    auto cp = [&](double* h, const double* d, size_t cnt) {
-        if (st == XD_OK && h)
-            st = cuda_status(cudaMemcpyAsync(h, d, sizeof(double) * cnt, cudaMemcpyDeviceToHost, q), "mixed download");
-    };
-    cp(pos, dpos, 4 * n);
-    cp(vel, dvel, 3 * n);
-    cp(acc, dacc, 3 * n);
-    cp(omega, dom, 3 * n);
-    cp(alpha, dal, 3 * n);
-    cp(force, df, 3 * n);
-    cp(moment, dmo, 3 * n);
+    const CopyPart parts[7] = { { dpos, pos, 4 * n }, { dvel, vel, 3 * n },  { dacc, acc, 3 * n },
+                                { dom, omega, 3 * n }, { dal, alpha, 3 * n }, { df, force, 3 * n },
+                                { dmo, moment, 3 * n } };
+    if (st == XD_OK) st = copy_runs(parts, 7, false, q, "mixed download");
     if (st == XD_OK && sync) st = cuda_status(cudaStreamSynchronize(q), "mixed download");
     return st;
 }
