@@ -462,7 +462,9 @@ int xd_scene_set_planes(xd_scene* scene, const xd_plane_info* planes, void* stre
 
 /* Advance nsteps whole steps on `stream`.  Returns after enqueueing; a
  * device-side error word is checked (with a synchronisation) only when
- * `check` is non-zero. */
+ * `check` is non-zero.  Both forms replay the steps as CUDA graphs captured
+ * at the scene's first call (the FP64 form for calls of four steps or more);
+ * XDEM_NO_GRAPHS=1 in the environment launches the same kernels directly. */
 int xd_scene_step(xd_scene* scene, unsigned nsteps, int check, void* stream);
 
 /* Per-phase timing with CUDA events recorded on the step's stream.  Phases:
