@@ -2869,7 +2869,8 @@ int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q)
 
 namespace {
 
-constexpr unsigned kBatchGroup = 16;
+constexpr unsigned kBatchGroup = 32;
+constexpr unsigned kBatchGraphSteps = 4;   // later steps captured per graph launch
 constexpr unsigned kBatchContactBlocks = 152 * 8;
 
 // One scene of a batch as the batch kernels read it.
@@ -3022,8 +3023,9 @@ struct MixedBatch {
     unsigned nblocks = 0;
     unsigned* d_flags = nullptr;
     unsigned* d_chunks = nullptr;
-    cudaGraphConditionalHandle* d_handles[2] = {};   // per step kind: groups, then scenes
-    cudaGraphExec_t step_graph[2] = {};              // 0: first step of a call (drift), 1: later steps
+    cudaGraphConditionalHandle* d_handles[3] = {};   // per graph kind and step: groups, then scenes
+    cudaGraphExec_t step_graph[3] = {};              // 0: first step of a call (drift); 1: one later step;
+                                                     // 2: kBatchGraphSteps later steps
     cudaGraphExec_t finish_graph = nullptr;          // last kick and the body reactions
     bool captured = false;
     // direct launches (profilers; kernel timing): CUDA events around the
@@ -3101,11 +3103,13 @@ int current_deps(cudaStream_t q, cudaGraph_t* g, std::vector<cudaGraphNode_t>* d
 
 // One batch step graph: advance, decision, the groups' conditional
 // re-binnings (side by side), run prefix, contact.
-int capture_batch_step(MixedBatch* b, int mode)
+int capture_batch_step(MixedBatch* b, int kind)
 {
     const unsigned ns = (unsigned)b->scenes.size();
     const unsigned ng = (ns + kBatchGroup - 1) / kBatchGroup;
-    std::vector<cudaGraphConditionalHandle> h(ng + ns, 0);
+    const unsigned nsteps = kind == 2 ? kBatchGraphSteps : 1u;
+    const unsigned per = ng + ns;   // handles of one step: groups, then scenes
+    std::vector<cudaGraphConditionalHandle> h((size_t)per * nsteps, 0);
     cudaStream_t cs = nullptr;
     int st = cuda_status(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "batch capture stream");
     if (st != XD_OK) return st;
@@ -3113,60 +3117,66 @@ int capture_batch_step(MixedBatch* b, int mode)
     cudaGraph_t cg = nullptr;
     std::vector<cudaGraphNode_t> deps;
     if (st == XD_OK) st = current_deps(cs, &cg, &deps);
-    for (unsigned g = 0; g < ng && st == XD_OK; ++g)
-        st = cuda_status(cudaGraphConditionalHandleCreate(&h[g], cg, 0, cudaGraphCondAssignDefault),
-                         "batch conditional handle");
-    if (st == XD_OK) {
-        if (mode == 0)
-            k_batch_advance<0><<<b->nblocks, 256, 0, cs>>>(b->d_scenes, b->d_block_scene, b->nblocks);
-        else
-            k_batch_advance<1><<<b->nblocks, 256, 0, cs>>>(b->d_scenes, b->d_block_scene, b->nblocks);
-        k_batch_decide<<<1, 256, 0, cs>>>(b->d_scenes, ns, b->d_flags, b->d_handles[mode]);
-        st = launch_status("batch advance");
-    }
-    if (st == XD_OK) st = current_deps(cs, &cg, &deps);
-    std::vector<cudaGraphNode_t> groups(ng, nullptr);
-    for (unsigned g = 0; g < ng && st == XD_OK; ++g) {
-        const unsigned first = g * kBatchGroup, count = std::min(kBatchGroup, ns - first);
-        auto group_body = [&](cudaStream_t bs, cudaGraph_t bg) {
-            int r = XD_OK;
-            for (unsigned k = 0; k < count && r == XD_OK; ++k)
-                r = cuda_status(cudaGraphConditionalHandleCreate(&h[ng + first + k], bg, 0, cudaGraphCondAssignDefault),
-                                "batch conditional handle");
-            if (r != XD_OK) return r;
-            k_batch_group<<<1, 32, 0, bs>>>(b->d_flags, first, count, b->d_handles[mode] + ng);
-            r = launch_status("batch group");
-            cudaGraph_t bgc = nullptr;
-            std::vector<cudaGraphNode_t> gd;
-            if (r == XD_OK) r = current_deps(bs, &bgc, &gd);
-            for (unsigned k = 0; k < count && r == XD_OK; ++k) {
-                MixedScene* sc = b->scenes[first + k];
-                cudaGraphNode_t node = nullptr;
-                r = add_conditional(bgc, gd.data(), gd.size(), h[ng + first + k],
-                                    [sc](cudaStream_t rs, cudaGraph_t) { return rebuild(sc, rs); }, &node);
-            }
-            return r;
-        };
-        st = add_conditional(cg, deps.data(), deps.size(), h[g], group_body, &groups[g]);
-    }
-    if (st == XD_OK && ng)
-        st = cuda_status(cudaStreamUpdateCaptureDependencies(cs, groups.data(), nullptr, ng,
-                                                             cudaStreamSetCaptureDependencies),
-                         "batch capture dependencies");
-    if (st == XD_OK) {
-        k_batch_chunks<<<1, 1024, 0, cs>>>(b->d_scenes, ns, b->d_chunks);
-        k_batch_contact<<<kBatchContactBlocks, kContactThreads, 0, cs>>>(b->d_scenes, ns, b->d_chunks);
-        st = launch_status("batch contact");
+    for (unsigned step = 0; step < nsteps && st == XD_OK; ++step) {
+        cudaGraphConditionalHandle* hs = h.data() + (size_t)step * per;
+        cudaGraphConditionalHandle* dh = b->d_handles[kind] + (size_t)step * per;
+        for (unsigned g = 0; g < ng && st == XD_OK; ++g)
+            st = cuda_status(cudaGraphConditionalHandleCreate(&hs[g], cg, 0, cudaGraphCondAssignDefault),
+                             "batch conditional handle");
+        if (st == XD_OK) {
+            if (kind == 0)
+                k_batch_advance<0><<<b->nblocks, 256, 0, cs>>>(b->d_scenes, b->d_block_scene, b->nblocks);
+            else
+                k_batch_advance<1><<<b->nblocks, 256, 0, cs>>>(b->d_scenes, b->d_block_scene, b->nblocks);
+            k_batch_decide<<<1, 256, 0, cs>>>(b->d_scenes, ns, b->d_flags, dh);
+            st = launch_status("batch advance");
+        }
+        if (st == XD_OK) st = current_deps(cs, &cg, &deps);
+        std::vector<cudaGraphNode_t> groups(ng, nullptr);
+        for (unsigned g = 0; g < ng && st == XD_OK; ++g) {
+            const unsigned first = g * kBatchGroup, count = std::min(kBatchGroup, ns - first);
+            auto group_body = [&](cudaStream_t bs, cudaGraph_t bg) {
+                int r = XD_OK;
+                for (unsigned k = 0; k < count && r == XD_OK; ++k)
+                    r = cuda_status(cudaGraphConditionalHandleCreate(&hs[ng + first + k], bg, 0,
+                                                                     cudaGraphCondAssignDefault),
+                                    "batch conditional handle");
+                if (r != XD_OK) return r;
+                k_batch_group<<<1, 32, 0, bs>>>(b->d_flags, first, count, dh + ng);
+                r = launch_status("batch group");
+                cudaGraph_t bgc = nullptr;
+                std::vector<cudaGraphNode_t> gd;
+                if (r == XD_OK) r = current_deps(bs, &bgc, &gd);
+                for (unsigned k = 0; k < count && r == XD_OK; ++k) {
+                    MixedScene* sc = b->scenes[first + k];
+                    cudaGraphNode_t node = nullptr;
+                    r = add_conditional(bgc, gd.data(), gd.size(), hs[ng + first + k],
+                                        [sc](cudaStream_t rs, cudaGraph_t) { return rebuild(sc, rs); }, &node);
+                }
+                return r;
+            };
+            st = add_conditional(cg, deps.data(), deps.size(), hs[g], group_body, &groups[g]);
+        }
+        if (st == XD_OK && ng)
+            st = cuda_status(cudaStreamUpdateCaptureDependencies(cs, groups.data(), nullptr, ng,
+                                                                 cudaStreamSetCaptureDependencies),
+                             "batch capture dependencies");
+        if (st == XD_OK) {
+            k_batch_chunks<<<1, 1024, 0, cs>>>(b->d_scenes, ns, b->d_chunks);
+            k_batch_contact<<<kBatchContactBlocks, kContactThreads, 0, cs>>>(b->d_scenes, ns, b->d_chunks);
+            st = launch_status("batch contact");
+        }
+        if (st == XD_OK) st = current_deps(cs, &cg, &deps);
     }
     cudaGraph_t graph = nullptr;
     const cudaError_t e = cudaStreamEndCapture(cs, &graph);
     if (st == XD_OK) st = cuda_status(e, "batch capture");
-    if (st == XD_OK) st = cuda_status(cudaGraphInstantiate(&b->step_graph[mode], graph, 0), "batch graph instantiate");
+    if (st == XD_OK) st = cuda_status(cudaGraphInstantiate(&b->step_graph[kind], graph, 0), "batch graph instantiate");
     if (graph) cudaGraphDestroy(graph);
     if (st == XD_OK)
-        st = cuda_status(cudaMemcpy(b->d_handles[mode], h.data(), sizeof(cudaGraphConditionalHandle) * h.size(),
+        st = cuda_status(cudaMemcpy(b->d_handles[kind], h.data(), sizeof(cudaGraphConditionalHandle) * h.size(),
                                     cudaMemcpyHostToDevice), "batch handles");
-    if (st == XD_OK) st = cuda_status(cudaGraphUpload(b->step_graph[mode], cs), "batch graph upload");
+    if (st == XD_OK) st = cuda_status(cudaGraphUpload(b->step_graph[kind], cs), "batch graph upload");
     if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(cs), "batch graph upload");
     cudaStreamDestroy(cs);
     return st;
@@ -3244,11 +3254,11 @@ int prepare_batch(MixedBatch* b)
     M(&b->d_chunks, ns + 1, "batch runs");
     M(&b->d_handles[0], ng + ns, "batch handles");
     M(&b->d_handles[1], ng + ns, "batch handles");
+    M(&b->d_handles[2], (size_t)(ng + ns) * kBatchGraphSteps, "batch handles");
     if (st == XD_OK)
         st = cuda_status(cudaMemcpy(b->d_block_scene, block_scene.data(), sizeof(unsigned) * block_scene.size(),
                                     cudaMemcpyHostToDevice), "batch blocks");
-    if (st == XD_OK) st = capture_batch_step(b, 0);
-    if (st == XD_OK) st = capture_batch_step(b, 1);
+    for (int kind = 0; kind < 3 && st == XD_OK; ++kind) st = capture_batch_step(b, kind);
     if (st == XD_OK) st = capture_batch_finish(b);
     // the descriptors after the captures: capturing a re-binning fixes the
     // triangle sort's output buffers of a scene that has not re-binned yet
@@ -3414,7 +3424,10 @@ int mixed_batch_step(MixedBatch* b, unsigned nsteps, cudaStream_t q)
         st = batch_step_direct(b, nsteps, q);
     } else {
         st = cuda_status(cudaGraphLaunch(b->step_graph[0], q), "batch graph launch");
-        for (unsigned t = 1; t < nsteps && st == XD_OK; ++t)
+        unsigned left = nsteps - 1;
+        for (; left >= kBatchGraphSteps && st == XD_OK; left -= kBatchGraphSteps)
+            st = cuda_status(cudaGraphLaunch(b->step_graph[2], q), "batch graph launch");
+        for (; left > 0 && st == XD_OK; --left)
             st = cuda_status(cudaGraphLaunch(b->step_graph[1], q), "batch graph launch");
         if (st == XD_OK) st = cuda_status(cudaGraphLaunch(b->finish_graph, q), "batch graph launch");
     }
