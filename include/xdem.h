@@ -584,7 +584,7 @@ int xd_scene_device_bytes(xd_scene* scene, unsigned long long* bytes);
 /* Batches (no counterpart in the reference): mixed-form scenes advanced
  * together, a step of all of them being one CUDA graph -- one advance launch
  * over every scene's particles, a re-binning per scene that needs one (a
- * conditional node per group of 16 scenes, then per scene), one contact
+ * conditional node per group of 32 scenes, then per scene), one contact
  * launch over every scene's listed particles.  Each scene's result is the
  * same, bit for bit, as when it is stepped alone; what a batch saves is the
  * launch and graph-node cost per scene, which bounds many small scenes.  The
