@@ -906,7 +906,7 @@ def run_batched(a):
                    "particles_min": min(sc.np_ for sc in scs), "particles_max": max(sc.np_ for sc in scs),
                    "triangles_per_scene": int(scs[0].ntri), "dt": 5e-6, "mode": "mixed",
                    "grid": "one grid per scene sized to its cone, cell 2 r_max + skin",
-                   "stepping": ("xd_batch: one CUDA graph per batch step -- one advance and one contact "
+                   "stepping": ("xd_batch: CUDA graphs of one or four batch steps -- one advance and one contact "
                                 "launch over all scenes, each scene's re-binning behind conditional nodes"),
                    "l2": "batch state > L2 (no flush)", "device_bytes": dev_bytes,
                    "generation_s": gen_s, "parallelism": f"replicas x{world}"},
