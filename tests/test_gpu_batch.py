@@ -127,3 +127,42 @@ def test_async_copies_round_trip(cuda):
     for k in keys:
         assert np.array_equal(out[k].numpy(), ref[k]), k
     d.close()
+
+
+def test_state_copies_from_one_block(cuda):
+    """Arrays kept back to back in the library's staging order (pos, vel, acc,
+    omega, alpha, mass, inertia) go as one copy each way; the state is the
+    same as with separate arrays."""
+    import torch
+
+    from metakonga_gb300._lib import call
+    sc = small_hopper(n=1500, seed=5)
+    d = engine.DeviceScene(sc, mode=engine.MODE_MIXED)
+    d.step(4, check=True)
+    ref = d.download()
+    n = sc.np_
+    block = torch.empty(18 * n, dtype=torch.float64).pin_memory()
+    views, off = {}, 0
+    for k, w in (("pos", 4), ("vel", 3), ("acc", 3), ("omega", 3), ("alpha", 3), ("mass", 1), ("inertia", 1)):
+        views[k] = block[off:off + w * n]
+        src = ref[k] if k in ref else getattr(sc, k)
+        views[k].copy_(torch.from_numpy(np.ascontiguousarray(src).reshape(-1)))
+        off += w * n
+    force = torch.from_numpy(np.ascontiguousarray(sc.force)).pin_memory()
+    moment = torch.from_numpy(np.ascontiguousarray(sc.moment)).pin_memory()
+    stream = torch.cuda.Stream()
+    call("xd_scene_upload_async", d.handle, views["pos"].data_ptr(), views["vel"].data_ptr(), views["acc"].data_ptr(),
+         views["omega"].data_ptr(), views["alpha"].data_ptr(), force.data_ptr(), moment.data_ptr(),
+         views["mass"].data_ptr(), views["inertia"].data_ptr(), stream.cuda_stream)
+    out = torch.zeros(16 * n, dtype=torch.float64).pin_memory()
+    o = {}
+    off = 0
+    for k, w in (("pos", 4), ("vel", 3), ("acc", 3), ("omega", 3), ("alpha", 3)):
+        o[k] = out[off:off + w * n]
+        off += w * n
+    call("xd_scene_download_async", d.handle, *[o[k].data_ptr() for k in ("pos", "vel", "acc", "omega", "alpha")],
+         None, None, stream.cuda_stream)
+    stream.synchronize()
+    for k in o:
+        assert np.array_equal(o[k].numpy(), np.ascontiguousarray(ref[k]).reshape(-1)), k
+    d.close()
