@@ -8,6 +8,8 @@
 #include <new>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "xd_grid.cuh"
 #include "xd_internal.cuh"
 #include "xd_mixed.cuh"
@@ -69,6 +71,13 @@ struct xd_scene {
 };
 
 namespace {
+
+// An NVTX range over a host call (profilers show the library's calls on the
+// timeline; without a profiler attached it costs a function-pointer check).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
 
 template <typename T>
 int dalloc(xd_scene* s, T** p, size_t count)
@@ -795,6 +804,7 @@ unsigned steps_to_emission(const xd_scene* s, unsigned left)
 
 int xd_scene_step(xd_scene* s, unsigned nsteps, int check, void* stream)
 {
+    NvtxRange range("xd_scene_step");
     if (!s) return set_error(XD_ERR_INVALID, "scene_step: null scene");
     if (nsteps == 0) return XD_OK;
     cudaStream_t q = static_cast<cudaStream_t>(stream);
@@ -904,6 +914,7 @@ int xd_scene_download_history(xd_scene* s, unsigned* keys, double* delta, unsign
 
 int xd_scene_step_many(xd_scene* const* scenes, const unsigned* nsteps, unsigned count, int check, void* stream)
 {
+    NvtxRange range("xd_scene_step_many");
     if (count == 0) return XD_OK;
     if (!scenes || !nsteps) return set_error(XD_ERR_INVALID, "scene_step_many: null array");
     for (unsigned i = 0; i < count; ++i)
@@ -964,6 +975,7 @@ int xd_batch_create(xd_scene* const* scenes, unsigned count, xd_batch** out)
 
 int xd_batch_step(xd_batch* b, unsigned nsteps, int check, void* stream)
 {
+    NvtxRange range("xd_batch_step");
     if (!b) return set_error(XD_ERR_INVALID, "batch_step: null batch");
     for (size_t k = 0; k < b->scenes.size(); ++k)
         if (b->scenes[k]->emit_period || b->scenes[k]->active != b->scenes[k]->np)

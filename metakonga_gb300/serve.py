@@ -89,6 +89,7 @@ class Request:
     remaining: int = 0
     handle: object = None
     result: dict = None
+    error: str = None                    # why the request failed (it is then not stepped further)
 
 
 class _CudaMarks:
@@ -146,6 +147,7 @@ class Server:
         self.clock = clock
         self.pending: list = []
         self.finished: list = []
+        self.failed: list = []
         self.used = 0
         self.peak_used = 0
         self.ticks = 0
@@ -199,7 +201,13 @@ class Server:
             if not self._fits(r, active):
                 break
             self.pending.pop(0)
-            r.handle = engine.DeviceScene(r.scene, mode=self.mode)
+            try:
+                r.handle = engine.DeviceScene(r.scene, mode=self.mode)
+            except Exception as e:   # a scene the library refuses fails alone
+                r.error = f"admission: {e}"
+                r.admitted = r.done = self.clock() - t0
+                self.failed.append(r)
+                continue
             r.admitted = self.clock() - t0
             self.used += r.bytes
             self.peak_used = max(self.peak_used, self.used)
@@ -220,6 +228,10 @@ class Server:
             for r in fin:
                 if self.keep_results:
                     r.result = r.handle.download(marks.side_after(mark))
+                    # a state that blew up (non-finite positions or velocities)
+                    # is reported as failed, the other requests unaffected
+                    if not all(np.isfinite(r.result[k]).all() for k in ("pos", "vel") if k in r.result):
+                        r.error = "non-finite state"
                 r.done = self.clock() - t0
                 self.finished.append(r)
                 to_close.append(r)
@@ -270,7 +282,7 @@ class Server:
         """Completion latency (arrival to result) percentiles in ms, waiting
         time before admission, and the aggregate particle-steps/s."""
         if not self.finished:
-            return {"requests": 0}
+            return {"requests": 0, "failed_admission": len(self.failed)}
         lat = np.array([r.done - r.arrival for r in self.finished]) * 1e3
         wait = np.array([r.admitted - r.arrival for r in self.finished]) * 1e3
         work = float(sum(r.scene.np_ * r.steps for r in self.finished))
@@ -282,6 +294,8 @@ class Server:
                 "particle_steps": work, "wall_s": self.wall,
                 "particle_steps_per_s": work / self.wall if self.wall > 0 else 0.0,
                 "offered_particle_steps_per_s": work / span if span > 0 else None,
+                "failed_admission": len(self.failed),
+                "non_finite": sum(1 for r in self.finished if r.error),
                 "ticks": self.ticks, "batched_ticks": self.batched_ticks, "peak_active": self.peak_active,
                 "peak_booked_bytes": self.peak_used}
 

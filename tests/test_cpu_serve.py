@@ -15,12 +15,17 @@ class _FakeScene:
     batches = []
 
     def __init__(self, sc, mode=engine.MODE_MIXED):
+        if getattr(sc, "refuse", False):
+            raise RuntimeError("scene refused")
         self.sc = sc
         self.steps = 0
         _FakeScene.live += 1
 
     def download(self, stream=0):
-        return {"steps": self.steps}
+        out = {"steps": self.steps}
+        if getattr(self.sc, "blow_up", False):
+            out["pos"] = np.array([[0.0, float("nan"), 0.0, 1.0]])
+        return out
 
     def close(self):
         # a scene is never freed while a batch holding it is alive
@@ -251,3 +256,24 @@ def test_batching_off_steps_side_by_side(fake):
     srv.submit("b", _named("b"), 8)
     srv.run()
     assert srv.report()["batched_ticks"] == 0 and not _FakeScene.batches
+
+
+def test_failed_requests_leave_the_others_alone(fake):
+    """A scene the library refuses fails at admission and one whose state
+    blows up is reported non-finite; the other requests run to completion."""
+    clock, calls = fake
+    srv = serve.Server(budget_bytes=1 << 40, chunk=4, clock=clock, marks=_Marks(), depth=0)
+    bad, nan, good = _named("bad"), _named("nan"), _named("good")
+    bad.refuse = True
+    nan.blow_up = True
+    srv.submit("bad", bad, 8)
+    srv.submit("nan", nan, 8)
+    srv.submit("good", good, 8)
+    done = srv.run()
+    assert {r.rid for r in done} == {"nan", "good"}
+    assert [r.rid for r in srv.failed] == ["bad"] and srv.failed[0].error.startswith("admission")
+    errs = {r.rid: r.error for r in done}
+    assert errs["nan"] == "non-finite state" and errs["good"] is None
+    rep = srv.report()
+    assert rep["failed_admission"] == 1 and rep["non_finite"] == 1 and rep["requests"] == 2
+    assert _FakeScene.live == 0
