@@ -316,14 +316,6 @@ __global__ void k_polygon_reaction_final(const double* __restrict__ partials, un
 // ----------------------------------------------------------- mesh update
 
 // toGlobal(double3&, double4&) (impl:1898-1909)
-__device__ __forceinline__ d3 to_global(d3 v, double ex, double ey, double ez, double ew)
-{
-    d3 r0 = mk(2.0 * (ex * ex + ey * ey - 0.5), 2.0 * (ey * ez - ex * ew), 2.0 * (ey * ew + ex * ez));
-    d3 r1 = mk(2.0 * (ey * ez + ex * ew), 2.0 * (ex * ex + ez * ez - 0.5), 2.0 * (ez * ew - ex * ey));
-    d3 r2 = mk(2.0 * (ey * ew - ex * ez), 2.0 * (ez * ew + ex * ey), 2.0 * (ex * ex + ew * ew - 0.5));
-    return mk(r0.x * v.x + r0.y * v.y + r0.z * v.z, r1.x * v.x + r1.y * v.y + r1.z * v.z,
-              r2.x * v.x + r2.y * v.y + r2.z * v.z);
-}
 
 // updatePolygonObjectData_kernel (impl:1911-1956); t = 0 where the
 // reference leaves it uninitialised (all three determinants <= 1e-13).
@@ -335,35 +327,8 @@ __global__ void __launch_bounds__(256) k_update_polygon(const xd_polygon_mass_in
 {
     unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= ntri) return;
-    size_t s = (size_t)id * 9;
-    int mid = dpi[id].id;
-    d3 o = ldp(dpmi[mid].origin);
-    const double* ep = dpmi[mid].ep;
-    double ex = __ldg(ep), ey = __ldg(ep + 1), ez = __ldg(ep + 2), ew = __ldg(ep + 3);
-    d3 Pv = o + to_global(ldp(vlist + s + 0), ex, ey, ez, ew);
-    d3 Qv = o + to_global(ldp(vlist + s + 3), ex, ey, ez, ew);
-    d3 Rv = o + to_global(ldp(vlist + s + 6), ex, ey, ez, ew);
-    d3 V = Qv - Pv, W = Rv - Pv;
-    d3 N = cross(V, W);
-    N = N / length(N);
-    d3 M1 = 0.5 * (Qv + Pv);
-    d3 M2 = 0.5 * (Rv + Pv);
-    d3 D1 = cross(N, V), D2 = cross(N, W);
-    double t = 0.0;
-    if (fabs(D1.x * D2.y - D1.y * D2.x) > 1E-13)
-        t = (D2.x * (M1.y - M2.y)) / (D1.x * D2.y - D1.y * D2.x) - (D2.y * (M1.x - M2.x)) / (D1.x * D2.y - D1.y * D2.x);
-    else if (fabs(D1.x * D2.z - D1.z * D2.x) > 1E-13)
-        t = (D2.x * (M1.z - M2.z)) / (D1.x * D2.z - D1.z * D2.x) - (D2.z * (M1.x - M2.x)) / (D1.x * D2.z - D1.z * D2.x);
-    else if (fabs(D1.y * D2.z - D1.z * D2.y) > 1E-13)
-        t = (D2.y * (M1.z - M2.z)) / (D1.y * D2.z - D1.z * D2.y) - (D2.z * (M1.y - M2.y)) / (D1.y * D2.z - D1.z * D2.y);
-    d3 ctri = M1 + t * D1;
-    double* sp = sphere + 4 * (size_t)id;
-    sp[0] = ctri.x;
-    sp[1] = ctri.y;
-    sp[2] = ctri.z;
-    st3(dpi[id].P, 0, Pv);
-    st3(dpi[id].Q, 0, Qv);
-    st3(dpi[id].R, 0, Rv);
+    d3 Pv, Qv, Rv;
+    update_polygon_one(dpmi, vlist, sphere, dpi, id, Pv, Qv, Rv);
 }
 
 // ----------------------------------------------------------- reductionD3
@@ -589,6 +554,44 @@ int launch_body_advance(xd_polygon_mass_info* pmi, unsigned nbodies, double dt, 
     if (nbodies == 0) return XD_OK;
     k_body_advance<<<1, 32, 0, s>>>(pmi, nbodies, dt);
     return launch_status("kinematic bodies");
+}
+
+// The mesh update and, for the mixed form, whether a vertex has moved from
+// its position at the last list build (ref: FP32, relative to the grid origin
+// wo) by disp2 or more: *flag is raised then.
+__global__ void __launch_bounds__(64) k_mesh_move(const xd_polygon_mass_info* __restrict__ dpmi,
+                                                  const double* __restrict__ vlist, double* __restrict__ sphere,
+                                                  xd_polygon_info* __restrict__ dpi, unsigned ntri,
+                                                  const float* __restrict__ ref, double wo0, double wo1, double wo2,
+                                                  float disp2, unsigned* __restrict__ flag)
+{
+    const unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+    bool out = false;
+    if (id < ntri) {
+        d3 V[3];
+        update_polygon_one(dpmi, vlist, sphere, dpi, id, V[0], V[1], V[2]);
+        const double wo[3] = { wo0, wo1, wo2 };
+        for (int k = 0; k < 3; ++k) {
+            const double c[3] = { V[k].x, V[k].y, V[k].z };
+            float d2 = 0.f;
+            for (int a = 0; a < 3; ++a) {
+                const float d = (float)(c[a] - wo[a]) - ref[9 * (size_t)id + 3 * k + a];
+                d2 += d * d;
+            }
+            out |= !(d2 < disp2);
+        }
+    }
+    if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31u) == 0) atomicOr(flag, 1u);
+}
+
+int launch_mesh_move(const xd_polygon_mass_info* dpmi, const double* vlist, double* sphere, xd_polygon_info* dpi,
+                     unsigned ntri, const float* ref, const double wo[3], float disp2, unsigned* flag,
+                     cudaStream_t s)
+{
+    if (ntri == 0) return XD_OK;
+    k_mesh_move<<<div_up(ntri, 64), 64, 0, s>>>(dpmi, vlist, sphere, dpi, ntri, ref, wo[0], wo[1], wo[2], disp2,
+                                               flag);
+    return launch_status("mesh move");
 }
 
 int launch_update_polygon(const xd_polygon_mass_info* dpmi, const double* vlist, double* sphere,

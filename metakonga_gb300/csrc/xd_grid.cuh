@@ -48,6 +48,11 @@ int launch_polygon(const Params& P, const xd_polygon_info* dpi, xd_polygon_mass_
 int launch_body_advance(xd_polygon_mass_info* pmi, unsigned nbodies, double dt, cudaStream_t s);
 int launch_update_polygon(const xd_polygon_mass_info* dpmi, const double* vlist, double* sphere,
                           xd_polygon_info* dpi, unsigned ntri, cudaStream_t s);
+// The mesh update with the mixed form's moved check in one launch (see
+// k_mesh_move): *flag raised when a vertex moved disp2 or more from ref.
+int launch_mesh_move(const xd_polygon_mass_info* dpmi, const double* vlist, double* sphere, xd_polygon_info* dpi,
+                     unsigned ntri, const float* ref, const double wo[3], float disp2, unsigned* flag,
+                     cudaStream_t s);
 int reduction_d3(const double* in, unsigned n, double out[3], void* scratch, cudaStream_t s);
 size_t reduction_scratch_bytes(unsigned n);
 size_t pair_list_scratch_bytes(unsigned np);

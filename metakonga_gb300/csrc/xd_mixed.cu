@@ -951,27 +951,6 @@ __global__ void __launch_bounds__(256) k_tri_build(MixParams P, Master M, const 
     tcount[i] = c > kTriCap ? (kTriCap | kIncomplete) : c;
 }
 
-// After a mesh update: has any vertex moved half the skin since the build?
-__global__ void __launch_bounds__(256) k_tri_moved(MixParams P, const xd_polygon_info* __restrict__ poly,
-                                                   const float* __restrict__ tri_ref,
-                                                   unsigned* __restrict__ counters)
-{
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    bool out = false;
-    if (t < P.ntri) {
-        const double* V[3] = { poly[t].P, poly[t].Q, poly[t].R };
-        for (int k = 0; k < 3; ++k) {
-            float d2 = 0.f;
-            for (int a = 0; a < 3; ++a) {
-                const float d = (float)(V[k][a] - P.wo[a]) - tri_ref[9 * (size_t)t + 3 * k + a];
-                d2 += d * d;
-            }
-            out |= !(d2 < P.disp2);
-        }
-    }
-    if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31u) == 0) atomicOr(counters + CN_REBUILD, 1u);
-}
-
 // Verlet list build (steps that re-bin the cells), one thread per particle:
 // the nine neighbour rows' slot ranges, trimmed to the cells within reach,
 // are staged in shared memory and visited as one flattened loop (rows z then
@@ -2317,10 +2296,8 @@ static int rebuild(MixedScene* s, cudaStream_t q)
 static int update_mesh(MixedScene* s, cudaStream_t q)
 {
     if (!s->ntri || !s->bodies_dirty) return XD_OK;
-    int st = launch_update_polygon(s->pmi, s->vlist_body, s->sphere, s->poly, s->ntri, q);
-    if (st != XD_OK) return st;
-    k_tri_moved<<<blocks(s->ntri, 256), 256, 0, q>>>(s->P, s->poly, s->tri_ref, s->counters);
-    st = launch_status("mixed mesh moved");
+    const int st = launch_mesh_move(s->pmi, s->vlist_body, s->sphere, s->poly, s->ntri, s->tri_ref, s->P.wo,
+                                    s->P.disp2, s->counters + CN_REBUILD, q);
     if (st == XD_OK) s->bodies_dirty = false;
     return st;
 }
@@ -2410,11 +2387,9 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
         // prescribed body motion: pose, triangles, and the re-binning flag
         // once a vertex has moved half the skin since the last build
         st = launch_body_advance(s->pmi, s->nbodies, s->P.dt, q);
-        if (st == XD_OK) st = launch_update_polygon(s->pmi, s->vlist_body, s->sphere, s->poly, s->ntri, q);
-        if (st == XD_OK) {
-            k_tri_moved<<<blocks(s->ntri, 256), 256, 0, q>>>(s->P, s->poly, s->tri_ref, s->counters);
-            st = launch_status("mixed mesh moved");
-        }
+        if (st == XD_OK)
+            st = launch_mesh_move(s->pmi, s->vlist_body, s->sphere, s->poly, s->ntri, s->tri_ref, s->P.wo,
+                                  s->P.disp2, s->counters + CN_REBUILD, q);
         if (st != XD_OK) return st;
     }
     ph.begin(0, q);

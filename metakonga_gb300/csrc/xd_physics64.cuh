@@ -331,4 +331,58 @@ __device__ __forceinline__ d3 closest_pt_triangle(d3 a, d3 b, d3 c, d3 p)
     return (a + v * ab) + w * ac;
 }
 
+
+// ---------------------------------------------- mesh update
+//
+__device__ __forceinline__ d3 ldp3(const double* a) { return mk(__ldg(a), __ldg(a + 1), __ldg(a + 2)); }
+
+// Body frame to world frame by the Euler parameters (e0 = ex scalar).
+__device__ __forceinline__ d3 to_global(d3 v, double ex, double ey, double ez, double ew)
+{
+    d3 r0 = mk(2.0 * (ex * ex + ey * ey - 0.5), 2.0 * (ey * ez - ex * ew), 2.0 * (ey * ew + ex * ez));
+    d3 r1 = mk(2.0 * (ey * ez + ex * ew), 2.0 * (ex * ex + ez * ez - 0.5), 2.0 * (ez * ew - ex * ey));
+    d3 r2 = mk(2.0 * (ey * ew - ex * ez), 2.0 * (ez * ew + ex * ey), 2.0 * (ex * ex + ew * ew - 0.5));
+    return mk(r0.x * v.x + r0.y * v.y + r0.z * v.z, r1.x * v.x + r1.y * v.y + r1.z * v.z,
+              r2.x * v.x + r2.y * v.y + r2.z * v.z);
+}
+
+// updatePolygonObjectData_kernel (impl:1911-1956) for triangle id: the world
+// vertices from the body's pose, the circumcentre, and the triangle record;
+// the new vertices are returned as well.
+__device__ __forceinline__ void update_polygon_one(const xd_polygon_mass_info* __restrict__ dpmi,
+                                                   const double* __restrict__ vlist, double* __restrict__ sphere,
+                                                   xd_polygon_info* __restrict__ dpi, unsigned id, d3& Pv, d3& Qv,
+                                                   d3& Rv)
+{
+    size_t s = (size_t)id * 9;
+    int mid = dpi[id].id;
+    d3 o = ldp3(dpmi[mid].origin);
+    const double* ep = dpmi[mid].ep;
+    double ex = __ldg(ep), ey = __ldg(ep + 1), ez = __ldg(ep + 2), ew = __ldg(ep + 3);
+    Pv = o + to_global(ldp3(vlist + s + 0), ex, ey, ez, ew);
+    Qv = o + to_global(ldp3(vlist + s + 3), ex, ey, ez, ew);
+    Rv = o + to_global(ldp3(vlist + s + 6), ex, ey, ez, ew);
+    d3 V = Qv - Pv, W = Rv - Pv;
+    d3 N = cross(V, W);
+    N = N / length(N);
+    d3 M1 = 0.5 * (Qv + Pv);
+    d3 M2 = 0.5 * (Rv + Pv);
+    d3 D1 = cross(N, V), D2 = cross(N, W);
+    double t = 0.0;
+    if (fabs(D1.x * D2.y - D1.y * D2.x) > 1E-13)
+        t = (D2.x * (M1.y - M2.y)) / (D1.x * D2.y - D1.y * D2.x) - (D2.y * (M1.x - M2.x)) / (D1.x * D2.y - D1.y * D2.x);
+    else if (fabs(D1.x * D2.z - D1.z * D2.x) > 1E-13)
+        t = (D2.x * (M1.z - M2.z)) / (D1.x * D2.z - D1.z * D2.x) - (D2.z * (M1.x - M2.x)) / (D1.x * D2.z - D1.z * D2.x);
+    else if (fabs(D1.y * D2.z - D1.z * D2.y) > 1E-13)
+        t = (D2.y * (M1.z - M2.z)) / (D1.y * D2.z - D1.z * D2.y) - (D2.z * (M1.y - M2.y)) / (D1.y * D2.z - D1.z * D2.y);
+    d3 ctri = M1 + t * D1;
+    double* sp = sphere + 4 * (size_t)id;
+    sp[0] = ctri.x;
+    sp[1] = ctri.y;
+    sp[2] = ctri.z;
+    st3(dpi[id].P, 0, Pv);
+    st3(dpi[id].Q, 0, Qv);
+    st3(dpi[id].R, 0, Rv);
+}
+
 }  // namespace xd
