@@ -118,6 +118,9 @@ struct MixParams {
     float tol;           // prefilter tolerance (m)
     float c43Eeq, one_b2, sratio, fric;
     double c43Eeq_d, one_b2_d;   // the same constants in FP64 (rechecks)
+    // cohesionForce (impl:259-279): coh and its Eeq = (1 - pri^2)/Ei + (1 - prj^2)/Ej
+    float coh, coh_eeq;
+    double coh_d, coh_eeq_d;
     long long guard_q;   // guard band in fixed-point units
     int nplanes;
     float pxw[kMaxPlanes][3];   // plane corner relative to the grid origin (FP32)
@@ -1146,12 +1149,18 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     // DHSModel (impl:379-401)
     const float fsn = -kn * (delta * sqrtf(delta));
     const float fdn = vn * rvu;
-    float fn = fsn + fdn;
-    if (fabsf(fn) < 0.03f * fmaxf(fabsf(fsn), fabsf(fdn))) {
-        // The elastic and damping terms nearly cancel (the normal force of an
-        // unloading contact crossing zero): FP32 rounding of each term would
-        // dominate the small sum, so it is formed in FP64, with the overlap
-        // and normal from the FP64 positions.
+    float fca = 0.f;
+    if (P.coh != 0.f) {
+        // cohesionForce (impl:259-279): coh pi rc^2, rc^3 = 3 Req (-fsn) Eeq / 4
+        const float rc = cbrtf((3.0f * Req * (-fsn)) / (4.0f * (1.0f / P.coh_eeq)));
+        fca = P.coh * (3.14159265358979f * rc * rc);
+    }
+    float fn = fsn + fca + fdn;
+    if (fabsf(fn) < 0.03f * fmaxf(fmaxf(fabsf(fsn), fabsf(fdn)), fca)) {
+        // The elastic, cohesive and damping terms nearly cancel (the normal
+        // force of an unloading contact crossing zero): FP32 rounding of each
+        // term would dominate the small sum, so it is formed in FP64, with
+        // the overlap and normal from the FP64 positions.
         atomicAdd(counters + CN_NORMALS, 1u);
         const double px = __ldg(M.x + j) - __ldg(M.x + i);
         const double py = __ldg(M.y + j) - __ldg(M.y + i);
@@ -1173,7 +1182,13 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
         const double Meqd = (mi * mj) / (mi + mj), Reqd = (ri * rj) / (ri + rj);
         const double knd = P.c43Eeq_d * sqrt(Reqd);
         const double vnd = sqrt((4.0 * Meqd * knd) / P.one_b2_d);
-        fn = (float)(-knd * (dl * sqrt(dl)) + vnd * (rvx * ux + rvy * uy + rvz * uz));
+        const double fsnd = -knd * (dl * sqrt(dl));
+        double fcad = 0.0;
+        if (P.coh_d != 0.0) {
+            const double rc = pow((3.0 * Reqd * (-fsnd)) / (4.0 * (1.0 / P.coh_eeq_d)), 1.0 / 3.0);
+            fcad = P.coh_d * (M_PI * rc * rc);
+        }
+        fn = (float)(fsnd + fcad + vnd * (rvx * ux + rvy * uy + rvz * uz));
     }
     const f3 Fn = fn * u;
     if (HIST) {
@@ -1838,6 +1853,10 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     P.one_b2 = (float)P.one_b2_d;
     P.sratio = (float)cp.sratio;
     P.fric = (float)cp.fric;
+    P.coh_d = cp.coh;
+    P.coh_eeq_d = cp.coh != 0.0 ? ((1.0 - cp.pri * cp.pri) / cp.Ei) + ((1.0 - cp.prj * cp.prj) / cp.Ej) : 0.0;
+    P.coh = (float)P.coh_d;
+    P.coh_eeq = (float)P.coh_eeq_d;
     P.guard_q = (long long)ceil(kGuard * kQ);
     P.nplanes = (int)d.nplanes;
     P.rolling = d.params.rollingCondition ? 1 : 0;
@@ -1958,21 +1977,19 @@ int mixed_create(const xd_scene_desc& d, MixedScene** out)
         return set_error(XD_ERR_INVALID, "mixed mode: triangles given without mesh arrays");
     if (d.ntri && d.nbodies > (unsigned)kMaxBodies)
         return set_error(XD_ERR_INVALID, "mixed mode: at most %d polygon bodies", kMaxBodies);
-    for (unsigned b = 0; d.ntri && b < d.nbodies; ++b)
-        if (d.cp_poly[b].coh != 0.0)
-            return set_error(XD_ERR_INVALID, "mixed mode: cohesion is not supported (body %u)", b);
     for (unsigned t = 0; t < d.ntri; ++t)
         if (d.poly[t].id < 0 || (unsigned)d.poly[t].id >= d.nbodies)
             return set_error(XD_ERR_INVALID, "mixed mode: triangle %u names body %d of %u", t, d.poly[t].id,
                              d.nbodies);
     if (d.nplanes > (unsigned)kMaxPlanes)
         return set_error(XD_ERR_INVALID, "mixed mode: at most %d planes", kMaxPlanes);
-    if (d.cp_pp.coh != 0.0) return set_error(XD_ERR_INVALID, "mixed mode: cohesion is not supported");
     if (d.nplanes && (!d.planes || !d.cp_planes))
         return set_error(XD_ERR_INVALID, "mixed mode: planes given without arrays");
     for (unsigned w = 0; w < d.nplanes; ++w)
         if (d.cp_planes[w].coh != 0.0)
-            return set_error(XD_ERR_INVALID, "mixed mode: cohesion is not supported (plane %u)", w);
+            return set_error(XD_ERR_INVALID,
+                             "mixed mode: plane cohesion is not supported (plane %u; the reference's plane "
+                             "kernel forms it with zero radii and moduli)", w);
     MixedScene* s = new (std::nothrow) MixedScene();
     if (!s) return set_error(XD_ERR_NOMEM, "mixed scene: host allocation");
     s->desc = d;
