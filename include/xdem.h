@@ -81,6 +81,14 @@ typedef struct xd_plane_info {
     double u1[3], u2[3], uw[3], xw[3], pa[3], pb[3], w2[3], w3[3], w4[3];
 } xd_plane_info;
 
+/* device_cylinder_info (mphysics_cuda_dec.cuh:67-76), 176 bytes (ep at
+ * offset 144: the reference's double4 is 16-byte aligned) */
+typedef struct xd_cylinder_info {
+    double len, rbase, rtop;
+    double pbase[3], ptop[3], origin[3], vel[3], omega[3];
+    double ep[4];
+} xd_cylinder_info;
+
 /* device_polygon_info (mphysics_cuda_dec.cuh:32-41), 152 bytes */
 typedef struct xd_polygon_info {
     int id;
@@ -236,6 +244,21 @@ int xd_plane_contact_force(int tcm, const xd_plane_info* plane, const double* po
                            const double* vel, const double* omega, double* force, double* moment,
                            const double* mass, unsigned np, const xd_contact_property* cp,
                            void* stream);
+
+/* cu_cylinder_hertzian_contact_force (mphysics_cuda_dec.cuh:149-155;
+ * def.cu:181-200; cylinder_hertzian_contact_force_kernel, impl:652-760): one
+ * cylinder (device pointer) against every particle, DHS with Meq = m and
+ * Req = r, the contact depth rounded to FP32 as the reference's detection
+ * returns it.  Adds to force/moment; writes each particle's reaction on the
+ * cylinder to mf[i] = -Fn and mm[i] = (cp - mpos) x -Fn (mpos: one double[3]
+ * on the device).  The reference also zeroes mf[0] and mm[0] from every
+ * thread, racing with particle 0's store; here slot 0 holds particle 0's
+ * reaction.  Its _mf/_mm outputs are never written by the reference and have
+ * no counterpart here. */
+int xd_cylinder_contact_force(int tcm, const xd_cylinder_info* cyl, const double* pos,
+                              const double* vel, const double* omega, double* force, double* moment,
+                              const double* mass, unsigned np, const xd_contact_property* cp,
+                              const double* mpos, double* mf, double* mm, void* stream);
 
 /* cu_cube_contact_force (mphysics_cuda_dec.cuh:135-139; def.cu:158-179):
  * the six planes of a cube (device array of 6), applied in order. */

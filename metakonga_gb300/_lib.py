@@ -51,6 +51,7 @@ _SIGS = {
     "xd_calculate_p2p": [i32] + [vp] * 10 + [u32, vp],
     "xd_plane_contact_force": [i32] + [vp] * 7 + [u32, vp, vp],
     "xd_cube_contact_force": [i32] + [vp] * 7 + [u32, vp, vp],
+    "xd_cylinder_contact_force": [i32] + [vp] * 7 + [u32] + [vp] * 5,
     "xd_planes_contact_force": [i32, vp, vp, u32] + [vp] * 6 + [u32, vp],
     "xd_particle_polygon_collision": [i32] + [vp] * 13 + [u32, u32, vp],
     "xd_set_symbolic_parameter_f": [vp],

@@ -15,6 +15,8 @@
 
 static_assert(sizeof(device_parameters) == sizeof(xd_device_parameters), "device_parameters layout");
 static_assert(sizeof(device_plane_info) == sizeof(xd_plane_info), "device_plane_info layout");
+static_assert(sizeof(device_cylinder_info) == sizeof(xd_cylinder_info) && offsetof(device_cylinder_info, ep) == 144,
+              "device_cylinder_info layout");
 static_assert(sizeof(device_polygon_info) == sizeof(xd_polygon_info), "device_polygon_info layout");
 static_assert(sizeof(device_polygon_mass_info) == sizeof(xd_polygon_mass_info), "mass info layout");
 static_assert(sizeof(device_contact_property) == sizeof(xd_contact_property), "property layout");
@@ -104,13 +106,16 @@ void cu_particle_polygonObject_collision(const int tcm, device_polygon_info* dpi
                                   kDefaultStream);
 }
 
-void cu_cylinder_hertzian_contact_force(const int, device_cylinder_info*, double*, double*, double*,
-                                        double*, double*, double*, unsigned int,
-                                        device_contact_property*, double3*, double3*, double3*,
-                                        double3&, double3&)
+void cu_cylinder_hertzian_contact_force(const int tcm, device_cylinder_info* cyl, double* pos, double* vel,
+                                        double* omega, double* force, double* moment, double* mass,
+                                        unsigned int np, device_contact_property* cp, double3* mpos,
+                                        double3* mf, double3* mm, double3&, double3&)
 {
-    // no caller in the reference application (contactManager never creates it)
-    not_provided("cu_cylinder_hertzian_contact_force");
+    // the reference's wrapper leaves _mf and _mm unwritten (def.cu:181-200)
+    xd_cylinder_contact_force(tcm, reinterpret_cast<const xd_cylinder_info*>(cyl), pos, vel, omega, force,
+                              moment, mass, np, reinterpret_cast<const xd_contact_property*>(cp),
+                              reinterpret_cast<const double*>(mpos), reinterpret_cast<double*>(mf),
+                              reinterpret_cast<double*>(mm), kDefaultStream);
 }
 
 double3 reductionD3(double3* in, unsigned int np)

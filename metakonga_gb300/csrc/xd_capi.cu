@@ -303,6 +303,20 @@ int xd_plane_contact_force(int tcm, const xd_plane_info* plane, const double* po
     return launch_planes(*PP, plane, cp, 0, 1, pos, vel, omega, force, moment, mass, np, S(s));
 }
 
+int xd_cylinder_contact_force(int tcm, const xd_cylinder_info* cyl, const double* pos,
+                              const double* vel, const double* omega, double* force, double* moment,
+                              const double* mass, unsigned np, const xd_contact_property* cp,
+                              const double* mpos, double* mf, double* mm, void* s)
+{
+    XD_NEED_PARAMS("cylinder_contact_force");
+    XD_REQUIRE(tcm == 1, "cylinder_contact_force: only tcm = 1 (DHS) is provided");
+    if (np == 0) return XD_OK;
+    XD_REQUIRE(cyl && pos && vel && omega && force && moment && mass && cp && mpos && mf && mm,
+               "cylinder_contact_force: null pointer");
+    XD_REQUIRE(aligned16(pos), "cylinder_contact_force: pos must be 16-byte aligned");
+    return launch_cylinder(*PP, cyl, cp, pos, vel, omega, force, moment, mass, np, mpos, mf, mm, S(s));
+}
+
 int xd_cube_contact_force(int tcm, const xd_plane_info* planes6, const double* pos,
                           const double* vel, const double* omega, double* force, double* moment,
                           const double* mass, unsigned np, const xd_contact_property* cp, void* s)

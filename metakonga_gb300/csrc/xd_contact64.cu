@@ -162,6 +162,104 @@ __global__ void __launch_bounds__(128) k_planes(Params P, const xd_plane_info* _
     st3(moment, id, mo);
 }
 
+// ---------------------------------------------------------------- cylinder
+
+// particle_cylinder_contact_detection (impl:652-719): the contact depth (the
+// reference returns it as float), the unit normal u towards the cylinder and
+// the contact point cp.  Rows A1..A3 of the Euler-parameter matrix
+// (makeTFM_1..3, impl:624-637); toLocal multiplies by the transpose.
+__device__ __forceinline__ double cylinder_detection(const xd_cylinder_info& cy, d3 p, double r, d3& u, d3& cp)
+{
+    const d3 pbase = mk(cy.pbase[0], cy.pbase[1], cy.pbase[2]);
+    const d3 ptop = mk(cy.ptop[0], cy.ptop[1], cy.ptop[2]);
+    const d3 ab = ptop - pbase;
+    const double t = dot(p - pbase, ab) / dot(ab, ab);
+    d3 c = pbase + t * ab;
+    double dist = length(p - c);
+    if (t >= 0 && t <= 1) {
+        u = (c - p) / dist;
+        cp = c - cy.rbase * u;
+        return (double)(float)(cy.rtop + r - dist);
+    }
+    if (dist < cy.rbase) {
+        const d3 o2c = mk(cy.origin[0], cy.origin[1], cy.origin[2]) - c;
+        const double lo = length(o2c);
+        u = o2c / lo;
+        cp = c - cy.rbase * u;
+        return (double)(float)(cy.len * 0.5 + r - lo);
+    }
+    const double ex = cy.ep[0], ey = cy.ep[1], ez = cy.ep[2], ew = cy.ep[3];
+    const d3 A1 = mk(2.0 * (ex * ex + ey * ey - 0.5), 2.0 * (ey * ez - ex * ew), 2.0 * (ey * ew + ex * ez));
+    const d3 A2 = mk(2.0 * (ey * ez + ex * ew), 2.0 * (ex * ex + ez * ez - 0.5), 2.0 * (ez * ew - ex * ey));
+    const d3 A3 = mk(2.0 * (ey * ew - ex * ez), 2.0 * (ez * ew + ex * ey), 2.0 * (ex * ex + ew * ew - 0.5));
+    d3 v = p - ptop;
+    d3 at = mk(A1.x * v.x + A2.x * v.y + A3.x * v.z, A1.y * v.x + A2.y * v.y + A3.y * v.z,
+               A1.z * v.x + A2.z * v.y + A3.z * v.z);
+    cp = ptop;
+    if (fabs(at.y) > cy.len) {
+        v = p - pbase;
+        at = mk(A1.x * v.x + A2.x * v.y + A3.x * v.z, A1.y * v.x + A2.y * v.y + A3.y * v.z,
+                A1.z * v.x + A2.z * v.y + A3.z * v.z);
+        cp = pbase;
+    }
+    const double ang = atan(at.x / at.z);
+    if ((ang < 0 && at.z < 0) || (ang > 0 && at.x < 0 && at.z < 0)) c.x = cy.rbase * sin(-ang);
+    else c.x = cy.rbase * sin(ang);
+    c.z = cy.rbase * cos(ang);
+    if ((at.z < 0 && c.z > 0) || (at.z > 0 && c.z < 0)) c.z = -c.z;
+    c.y = 0.;
+    cp = cp + mk(dot(A1, c), dot(A2, c), dot(A3, c));
+    const d3 dis = cp - p;
+    dist = length(dis);
+    u = dis / dist;
+    if (dist < r) return (double)(float)(r - dist);
+    return -1.0;
+}
+
+// cylinder_hertzian_contact_force_kernel<1> (impl:721-760), one thread per
+// particle.
+__global__ void __launch_bounds__(256) k_cylinder(Params P, const xd_cylinder_info* __restrict__ cyl,
+                                                  const xd_contact_property* __restrict__ cps,
+                                                  const double* __restrict__ pos, const double* __restrict__ vel,
+                                                  const double* __restrict__ omega, double* __restrict__ force,
+                                                  double* __restrict__ moment, const double* __restrict__ mass,
+                                                  unsigned np, const double* __restrict__ mpos,
+                                                  double* __restrict__ mf, double* __restrict__ mm)
+{
+    const unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= np) return;
+    const xd_cylinder_info cy = *cyl;
+    const double m = __ldg(mass + id);
+    const d4 ip = ld4(pos, id);
+    const d3 ivel = ld3(vel, id), iomega = ld3(omega, id);
+    d3 unit = mk(0, 0, 0), cpt = mk(0, 0, 0);
+    const double cdist = cylinder_detection(cy, xyz(ip), ip.w, unit, cpt);
+    const d3 si = cpt - mk(__ldg(mpos), __ldg(mpos + 1), __ldg(mpos + 2));
+    const d3 cy2cp = cpt - mk(cy.origin[0], cy.origin[1], cy.origin[2]);
+    d3 Ft = mk(0, 0, 0), Fn = mk(0, 0, 0), M = mk(0, 0, 0);
+    if (cdist > 0) {
+        const d3 dv = mk(cy.vel[0], cy.vel[1], cy.vel[2]) + cross(mk(cy.omega[0], cy.omega[1], cy.omega[2]), cy2cp) -
+                      (ivel + cross(iomega, ip.w * unit));
+        const PairConst pc = load_pair_const(cps);
+        const Fc c = get_constant(pc, ip.w, 0.0, m, 0.0);
+        dhs(c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit, P.dt, Ft, Fn, M);
+    }
+    st3(force, id, ld3rw(force, id) + (Fn + Ft));
+    st3(moment, id, ld3rw(moment, id) + M);
+    st3(mf, id, -Fn);
+    st3(mm, id, cross(si, -Fn));
+}
+
+int launch_cylinder(const Params& P, const xd_cylinder_info* cyl, const xd_contact_property* cp,
+                    const double* pos, const double* vel, const double* omega, double* force,
+                    double* moment, const double* mass, unsigned np, const double* mpos, double* mf,
+                    double* mm, cudaStream_t s)
+{
+    if (np == 0) return XD_OK;
+    k_cylinder<<<div_up(np, 256), 256, 0, s>>>(P, cyl, cp, pos, vel, omega, force, moment, mass, np, mpos, mf, mm);
+    return launch_status("cylinder contact");
+}
+
 // ---------------------------------------------------------------- polygons
 
 __device__ __forceinline__ d3 ldp(const double* a) { return mk(__ldg(a), __ldg(a + 1), __ldg(a + 2)); }

@@ -35,6 +35,10 @@ int launch_p2p(const Params& P, const double* pos, const double* vel, const doub
                double* force, double* moment, const double* mass, const unsigned* sorted,
                const unsigned* cstart, const unsigned* cend, const xd_contact_property* cp,
                unsigned np, cudaStream_t s, const HistTable* ht = nullptr);
+int launch_cylinder(const Params& P, const xd_cylinder_info* cyl, const xd_contact_property* cp,
+                    const double* pos, const double* vel, const double* omega, double* force,
+                    double* moment, const double* mass, unsigned np, const double* mpos, double* mf,
+                    double* mm, cudaStream_t s);
 int launch_planes(const Params& P, const xd_plane_info* planes, const xd_contact_property* cps,
                   unsigned cp_stride, unsigned nplanes, const double* pos, const double* vel,
                   const double* omega, double* force, double* moment, const double* mass,

@@ -39,6 +39,14 @@ CONTACT_PROPERTY = np.dtype({
     "itemsize": 88,
 })
 
+# device_cylinder_info (mphysics_cuda_dec.cuh:67-76): 176 bytes, ep at 144
+CYLINDER = np.dtype({
+    "names": ["len", "rbase", "rtop", "pbase", "ptop", "origin", "vel", "omega", "ep"],
+    "formats": ["<f8", "<f8", "<f8", ("<f8", 3), ("<f8", 3), ("<f8", 3), ("<f8", 3), ("<f8", 3), ("<f8", 4)],
+    "offsets": [0, 8, 16, 24, 48, 72, 96, 120, 144],
+    "itemsize": 176,
+})
+
 PLANE = np.dtype({
     "names": ["l1", "l2", "u1", "u2", "uw", "xw", "pa", "pb", "w2", "w3", "w4"],
     "formats": ["<f8", "<f8"] + [V3] * 9,

@@ -117,7 +117,7 @@ class Oracle:
         for name in ("xdo_calculate_hash_and_index", "xdo_calculate_hash_and_index_polysphere",
                      "xdo_reorder_and_find_cell_start", "xdo_vv_update_position",
                      "xdo_vv_update_velocity", "xdo_calculate_p2p", "xdo_plane_contact_force",
-                     "xdo_cube_contact_force", "xdo_particle_polygon_collision",
+                     "xdo_cube_contact_force", "xdo_particle_polygon_collision", "xdo_cylinder_contact_force",
                      "xdo_update_polygon_object_data", "xdo_step", "xdo_run_steps",
                      "xdo_cpu_step", "xdo_cpu_run_steps", "xdo_contact_magnitudes"):
             getattr(L, name).restype = None
@@ -178,6 +178,11 @@ class Oracle:
     def plane(self, prm, plane, pos, vel, omega, force, moment, mass, cp):
         self.lib.xdo_plane_contact_force(_p(prm), _p(plane), _p(pos), _p(vel), _p(omega), _p(force),
                                          _p(moment), _p(mass), _u(pos.shape[0]), _p(cp))
+
+    def cylinder(self, prm, cyl, pos, vel, omega, force, moment, mass, cp, mpos, mf, mm):
+        self.lib.xdo_cylinder_contact_force(_p(prm), _p(cyl), _p(pos), _p(vel), _p(omega), _p(force),
+                                            _p(moment), _p(mass), _u(pos.shape[0]), _p(cp), _p(mpos),
+                                            _p(mf), _p(mm))
 
     def cube(self, prm, planes6, pos, vel, omega, force, moment, mass, cp):
         self.lib.xdo_cube_contact_force(_p(prm), _p(planes6), _p(pos), _p(vel), _p(omega),

@@ -482,6 +482,86 @@ void xdo_plane_contact_force(const xdo_params* prm, const xdo_plane* plane, cons
     }
 }
 
+/* particle_cylinder_contact_detection (impl:652-719).  The reference returns
+ * the depth as float; the rows A1..A3 are makeTFM_1..3 (impl:624-637), toLocal
+ * multiplies by their transpose, toGlobal by the rows. */
+static double cylinder_detection(const xdo_cylinder* cy, v3 p, double r, v3* u, v3* cp)
+{
+    v3 pbase = ld3(cy->pbase), ptop = ld3(cy->ptop);
+    v3 ab = sub(ptop, pbase);
+    double t = dot(sub(p, pbase), ab) / dot(ab, ab);
+    v3 c = add(pbase, scl(t, ab));
+    double dist = len(sub(p, c));
+    if (t >= 0 && t <= 1) {
+        *u = dvd(sub(c, p), dist);
+        *cp = sub(c, scl(cy->rbase, *u));
+        return (double)(float)(cy->rtop + r - dist);
+    }
+    if (dist < cy->rbase) {
+        v3 o2c = sub(ld3(cy->origin), c);
+        double lo = len(o2c);
+        *u = dvd(o2c, lo);
+        *cp = sub(c, scl(cy->rbase, *u));
+        return (double)(float)(cy->len * 0.5 + r - lo);
+    }
+    double ex = cy->ep[0], ey = cy->ep[1], ez = cy->ep[2], ew = cy->ep[3];
+    v3 A1 = mk(2.0 * (ex * ex + ey * ey - 0.5), 2.0 * (ey * ez - ex * ew), 2.0 * (ey * ew + ex * ez));
+    v3 A2 = mk(2.0 * (ey * ez + ex * ew), 2.0 * (ex * ex + ez * ez - 0.5), 2.0 * (ez * ew - ex * ey));
+    v3 A3 = mk(2.0 * (ey * ew - ex * ez), 2.0 * (ez * ew + ex * ey), 2.0 * (ex * ex + ew * ew - 0.5));
+    v3 v = sub(p, ptop);
+    v3 at = mk(A1.x * v.x + A2.x * v.y + A3.x * v.z, A1.y * v.x + A2.y * v.y + A3.y * v.z,
+               A1.z * v.x + A2.z * v.y + A3.z * v.z);
+    *cp = ptop;
+    if (fabs(at.y) > cy->len) {
+        v = sub(p, pbase);
+        at = mk(A1.x * v.x + A2.x * v.y + A3.x * v.z, A1.y * v.x + A2.y * v.y + A3.y * v.z,
+                A1.z * v.x + A2.z * v.y + A3.z * v.z);
+        *cp = pbase;
+    }
+    double ang = atan(at.x / at.z);
+    if (ang < 0 && at.z < 0) c.x = cy->rbase * sin(-ang);
+    else if (ang > 0 && at.x < 0 && at.z < 0) c.x = cy->rbase * sin(-ang);
+    else c.x = cy->rbase * sin(ang);
+    c.z = cy->rbase * cos(ang);
+    if (at.z < 0 && c.z > 0) c.z = -c.z;
+    else if (at.z > 0 && c.z < 0) c.z = -c.z;
+    c.y = 0.;
+    *cp = add(*cp, mk(dot(A1, c), dot(A2, c), dot(A3, c)));
+    v3 dis = sub(*cp, p);
+    dist = len(dis);
+    *u = dvd(dis, dist);
+    if (dist < r) return (double)(float)(r - dist);
+    return -1.0;
+}
+
+/* cylinder_hertzian_contact_force_kernel<1> (impl:721-760) for every particle;
+ * mf/mm: each particle's reaction on the cylinder (slot 0 included). */
+void xdo_cylinder_contact_force(const xdo_params* prm, const xdo_cylinder* cy, const double* pos,
+                                const double* vel, const double* omega, double* force, double* moment,
+                                const double* mass, unsigned np, const xdo_contact_property* cp,
+                                const double mpos[3], double* mf, double* mm)
+{
+    for (unsigned id = 0; id < np; ++id) {
+        const double* p4 = pos + 4 * (size_t)id;
+        double r = p4[3];
+        v3 ivel = ld3(vel + 3 * (size_t)id), iomega = ld3(omega + 3 * (size_t)id);
+        v3 unit = mk(0, 0, 0), cpt = mk(0, 0, 0);
+        double cdist = cylinder_detection(cy, ld3(p4), r, &unit, &cpt);
+        v3 si = sub(cpt, ld3(mpos));
+        v3 cy2cp = sub(cpt, ld3(cy->origin));
+        v3 Ft = mk(0, 0, 0), Fn = mk(0, 0, 0), M = mk(0, 0, 0);
+        if (cdist > 0) {
+            v3 dv = sub(add(ld3(cy->vel), cross(ld3(cy->omega), cy2cp)), add(ivel, cross(iomega, scl(r, unit))));
+            fconst c = get_constant(r, 0.0, mass[id], 0.0, cp);
+            dhs_model(&c, 0, 0, 0, 0, 0, 0, 0.0, cdist, dv, unit, prm->dt, &Ft, &Fn, &M);
+        }
+        acc3(force + 3 * (size_t)id, add(Fn, Ft));
+        acc3(moment + 3 * (size_t)id, M);
+        st3(mf + 3 * (size_t)id, neg(Fn));
+        st3(mm + 3 * (size_t)id, cross(si, neg(Fn)));
+    }
+}
+
 /* cu_cube_contact_force (def.cu:158-179): six plane launches in order. */
 void xdo_cube_contact_force(const xdo_params* prm, const xdo_plane* planes6, const double* pos,
                             const double* vel, const double* omega, double* force,

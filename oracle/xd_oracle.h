@@ -61,6 +61,13 @@ typedef struct xdo_plane {
     double u1[3], u2[3], uw[3], xw[3], pa[3], pb[3], w2[3], w3[3], w4[3];
 } xdo_plane;
 
+/* include/mphysics_cuda_dec.cuh:67-76 (device_cylinder_info), 176 bytes */
+typedef struct xdo_cylinder {
+    double len, rbase, rtop;
+    double pbase[3], ptop[3], origin[3], vel[3], omega[3];
+    double ep[4];
+} xdo_cylinder;
+
 /* include/mphysics_cuda_dec.cuh:32-41 (device_polygon_info), 152 bytes */
 typedef struct xdo_polygon {
     int id;
@@ -109,6 +116,10 @@ void xdo_plane_contact_force(const xdo_params* prm, const xdo_plane* plane, cons
                              const double* vel, const double* omega, double* force,
                              double* moment, const double* mass, unsigned np,
                              const xdo_contact_property* cp);
+void xdo_cylinder_contact_force(const xdo_params* prm, const xdo_cylinder* cy, const double* pos,
+                                const double* vel, const double* omega, double* force, double* moment,
+                                const double* mass, unsigned np, const xdo_contact_property* cp,
+                                const double mpos[3], double* mf, double* mm);
 void xdo_cube_contact_force(const xdo_params* prm, const xdo_plane* planes6, const double* pos,
                             const double* vel, const double* omega, double* force,
                             double* moment, const double* mass, unsigned np,

@@ -1,0 +1,58 @@
+"""The oracle's restatement of cylinder_hertzian_contact_force_kernel<1>
+(impl:721-760) on cases worked by hand, and the spread of its cloud over the
+three contact regions."""
+import math
+
+import numpy as np
+
+
+from .cylinder_case import cloud, cylinder
+
+
+def _run(oracle, c):
+    n = c["pos"].shape[0]
+    f, m, mf, mm = (np.zeros((n, 3)) for _ in range(4))
+    oracle.cylinder(c["prm"], c["cyl"], c["pos"], c["vel"], c["omega"], f, m, c["mass"], c["cp"], c["mpos"],
+                    mf, mm)
+    return f, m, mf, mm
+
+
+def test_lateral_contact_at_rest(oracle):
+    cyl, _ = cylinder(origin=(0.0, 0.1, 0.0), angle=0.0, vel=(0, 0, 0), omega=(0, 0, 0))
+    c = cloud(n=4)
+    # one sphere of r 4 mm 1 mm into the side at mid-height, at rest; one far off
+    c["cyl"] = cyl
+    c["pos"] = np.array([[0.053, 0.1, 0.0, 0.004], [0.3, 0.1, 0.0, 0.004]])
+    c["vel"] = np.zeros((2, 3))
+    c["omega"] = np.zeros((2, 3))
+    c["mass"] = c["mass"][:2]
+    c["mpos"] = np.array([0.0, 0.0, 0.0])
+    f, m, mf, mm = _run(oracle, c)
+    cp = c["cp"][0]
+    eeq = cp["Ei"] * cp["Ej"] / (cp["Ei"] * (1 - cp["prj"] ** 2) + cp["Ej"] * (1 - cp["pri"] ** 2))
+    kn = 4.0 / 3.0 * eeq * math.sqrt(0.004)               # Req = r against a cylinder
+    depth = float(np.float32(0.05 + 0.004 - 0.053))       # the detection's float result
+    fn = kn * depth ** 1.5
+    np.testing.assert_allclose(f[0], (fn, 0, 0), rtol=1e-12, atol=1e-12 * fn)
+    assert np.array_equal(m[0], np.zeros(3))               # no slip: no tangential force
+    np.testing.assert_allclose(mf[0], (-fn, 0, 0), rtol=1e-12, atol=1e-12 * fn)
+    # reaction moment about mpos: (contact point - mpos) x mf, contact point (0.05, 0.1, 0)
+    np.testing.assert_allclose(mm[0], np.cross((0.05, 0.1, 0.0), (-fn, 0, 0)), rtol=1e-12, atol=1e-12 * fn)
+    assert not f[1].any() and not mf[1].any() and not mm[1].any()
+
+
+def test_cloud_reaches_every_region(oracle):
+    c = cloud()
+    f, m, mf, mm = _run(oracle, c)
+    cyl = c["cyl"][0]
+    ab = cyl["ptop"] - cyl["pbase"]
+    t = (c["pos"][:, :3] - cyl["pbase"]) @ ab / (ab @ ab)
+    radial = np.linalg.norm(c["pos"][:, :3] - (cyl["pbase"] + t[:, None] * ab), axis=1)
+    hit = np.linalg.norm(f, axis=1) > 0
+    lateral = hit & (t >= 0) & (t <= 1)
+    cap = hit & ~((t >= 0) & (t <= 1)) & (radial < cyl["rbase"])
+    rim = hit & ~((t >= 0) & (t <= 1)) & (radial >= cyl["rbase"])
+    assert lateral.sum() > 100 and cap.sum() > 20 and rim.sum() > 5, (lateral.sum(), cap.sum(), rim.sum())
+    assert np.isfinite(f).all() and np.isfinite(mm).all()
+    # the reaction is minus the normal force; the particle also gets the tangential part
+    assert np.array_equal(np.linalg.norm(mf, axis=1) > 0, hit)
