@@ -13,9 +13,10 @@
  *     argument, CUDA error) is recorded and can be read with xd_last_error()
  *     (xdem.h) instead of exiting the process;
  *   - tcm = 1 (the DHS model the application runs) is the only contact model.
- * The single-precision overloads (mphysics_cuda_dec.cuh:164-300) are
- * declared for source compatibility; they record XD_ERR_INVALID ("single
- * precision not provided") and do nothing.  The double-precision
+ * The single-precision overloads (mphysics_cuda_dec.cuh:164-300) run the
+ * xd_*_f twins, except cu_cylinder_hertzian_contact_force(float*), whose
+ * declaration names the FP64 cylinder struct (the reference defines it with
+ * the float one): it records XD_ERR_INVALID ("not provided").  The double-precision
  * cu_updatePolygonObjectData(device_polygon_mass_info*, ...) declared among
  * them (:296-298) is the mesh update the application calls and is provided.
  */
@@ -179,7 +180,7 @@ void cu_updatePolygonObjectData(
     double *vList, double* sph, device_polygon_info* poly,
     device_polygon_mass_info* dpmi, unsigned int np);
 
-/* single precision (mphysics_cuda_dec.cuh:164-300): declared, not provided */
+/* single precision (mphysics_cuda_dec.cuh:164-300): the xd_*_f twins */
 struct device_parameters_f
 {
     unsigned int np;
