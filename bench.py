@@ -1,43 +1,49 @@
 """Benchmark: particle-steps/s of the DEM contact step on one GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload batched|served|box]
+                    [--workload batched|served|box|drum]
 
 Workloads (seeded synthetic input; every scene is generated here):
   batched  (default) 256 independent hopper-discharge scenes: particle counts
            log-uniform in [2,000, 200,000] (11.56 M spheres in all), r ~ U[2, 4]
            mm, a 60-degree cone of 4,096 triangles above a plane floor, orifice
-           U[6, 12] diameters, friction U[0.2, 0.6], dt = 5e-6 s.  A step
-           advances every scene by one time step; the scenes run side by side
-           (xd_scene_step_many) in the mixed form.
+           U[6, 12] diameters, friction U[0.2, 0.6], dt = 5e-6 s.  Each hopper
+           is generated as a lattice with its orifice gated, settled into a bed
+           (metakonga_gb300.prepare.settle, untimed), and the gate opened: the
+           timed steps are the discharge of packed beds.  A step advances every
+           scene by one time step through one batch (xd_batch) in the mixed
+           form.
   served   a Poisson stream of settle-box and hopper requests, particle counts
            log-uniform in [1,000, 500,000], step counts U[1,000, 20,000],
            admitted under a 150 GB device-memory budget by the continuous-
            batching server; p50/p99 completion latency and particle-steps/s.
   box      the 1,000,000-sphere polydisperse settle (r ~ U[2, 4] mm in a
            1 x 1 x 2 m box of five plane walls, dt = 5e-6 s), one scene.
+  drum     the 500,000-sphere rotating drum (20,480 triangles turning).
 
 The default (batched) line carries:
-  value        particle-steps/s of the batch, device-timed (CUDA events on
-               the launching stream; the batch's state, ~15 GB, is far larger
-               than L2, so no flush is needed between steps);
+  value        particle-steps/s of the settled batch, device-timed (CUDA
+               events on the launching stream; the batch's state, ~15 GB, is
+               far larger than L2, so no flush is needed between steps);
   e2e          the same through the public API with host buffers: each
                scene's state uploaded from pinned host memory, K steps, the
                state downloaded (all inside the timed region);
+  roofline     the batch step's dominant kernel -- k_batch_contact (the
+               contact pass over every scene's listed spheres) on packed beds,
+               k_batch_advance<1> otherwise -- timed per launch with CUDA
+               events, its algorithmic bytes over that time against the
+               measured HBM peak; both kernels' figures are under "kernels";
+  lattice_start the same batch from its generated lattice (little contact);
   plain_fp64   the same scenes run one at a time in the FP64 form (the
                reference's algorithm and grid), and the ratio to it;
   fp64_check   per-particle contact-force error of the mixed form against the
-               FP64 form on one scene of the batch after the timed steps;
+               FP64 form on the median scene's settled bed;
   served       the served stream (p50/p99 ms, particle-steps/s, and the same
                requests' time alone in the FP64 form);
-  roofline     the mixed form's dominant kernel (k_mx_advance) timed per
-               launch on the 1M-sphere box, whose state streams from HBM
-               every step, against the measured HBM peak; batch_hbm gives the
-               batch step's algorithmic bytes over its time;
   cpu_baseline the reference's CPU path (restated in the oracle, one thread)
-               on one scene of the batch.
---impl reference runs that CPU path on the host cores instead (one scene per
-core, drawn from the same batch) and prints the same metric.
+               on the median scene's settled bed.
+--impl reference runs that CPU path on the host cores instead (one replica of
+the median scene per core) and prints the same metric.
 Under torchrun each rank advances its own replica of the workload (scenes
 shard with no exchange); value is the sum over ranks over the max rank time.
 """
@@ -67,6 +73,9 @@ B_CONTACT = {"fp64": 140, "mixed": 116}   # algorithmic bytes per particle, cont
 # reads x y z r (32), vh vl wh wl ab (80), b2 (8), Fc Mc (32), pref (16) = 168;
 # writes x y z (24), vh vl wh wl ab (80), b2 (8), pf qa qb (48) = 160.
 B_ADVANCE = 328
+# k_batch_contact / k_mx_contact, per listed sphere: reads pf 16, qa qb 32, vh vl 32, wh wl 32,
+# hlist 4, vcount 4, tcount 4, wmask 2; writes Fc Mc 32 = 158 B; plus 4 B per list entry
+B_LISTED = 158
 
 
 def _args():
@@ -85,8 +94,10 @@ def _args():
     ap.add_argument("--no-served", action="store_true", help="batched: skip the served stream")
     ap.add_argument("--no-box", action="store_true", help="batched: skip the 1M-box roofline run")
     ap.add_argument("--no-drum", action="store_true", help="batched: skip the rotating-drum run")
-    ap.add_argument("--settle-steps", type=int, default=4000,
-                    help="batched: steps before the dense-contact timing (0: skip it)")
+    ap.add_argument("--prep-steps", type=int, default=5000,
+                    help="settled beds: preparation steps (prepare.settle) before the timed run (0: none)")
+    ap.add_argument("--prep-dt", type=float, default=4e-5, help="time step of the preparation")
+    ap.add_argument("--no-lattice", action="store_true", help="batched: skip the lattice-start timing")
     ap.add_argument("--count", type=int, default=256, help="scenes in the batch")
     ap.add_argument("--requests", type=int, default=32, help="requests of the served stream")
     ap.add_argument("--rate", type=float, default=4.0, help="served arrivals per second")
@@ -208,37 +219,56 @@ def _scene(n):
 
 
 def _cpu_scene(spec):
-    """("box", n) -> the n-sphere polydisperse box; ("hopper", count, k) ->
-    scene k of the count-scene hopper batch."""
+    """("box", n) -> the n-sphere polydisperse box; ("settle",) -> the
+    8,000-sphere settle; ("scene", Scene) -> that scene as it stands."""
+    from metakonga_gb300 import scenes
     if spec[0] == "box":
         return _scene(spec[1])
     if spec[0] == "settle":
-        from metakonga_gb300 import scenes
         return scenes.settle_box()
-    from metakonga_gb300 import scenes
-    return scenes.hopper(**scenes.hopper_batch(count=spec[1])[spec[2]])
+    return spec[1]
+
+
+def host_cpu():
+    """The host CPU model and the cores this process may use."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.TimeoutExpired):
+        pass
+    try:
+        cores = len(os.sched_getaffinity(0))
+    except AttributeError:
+        cores = os.cpu_count() or 1
+    return {"cpu_model": model, "cores_available": cores}
 
 
 def _cpu_worker(args):
-    """One CPU-path replica (spawned process): builds its scene once, then
-    times `samples` runs of `steps` steps; returns (particles*steps, [seconds])."""
+    """One CPU-path replica (spawned process): its scene once, the oracle's
+    grid work arrays once (outside the timed calls), then `samples` timed runs
+    of `steps` steps; returns (particles * steps, [seconds])."""
     spec, steps, samples = args
     sys.path.insert(0, ROOT)
     from oracle.pyoracle import Oracle
     sc = _cpu_scene(spec)
     o = Oracle()
+    work = o.work_arrays(sc)
     times = []
     for _ in range(samples):
         t0 = time.perf_counter()
-        o.run(sc, steps, cpu_path=True)
+        o.run(sc, steps, cpu_path=True, work=work)
         times.append(time.perf_counter() - t0)
     return sc.np_ * steps, times
 
 
 def cpu_baseline(specs, steps, samples=1):
-    """Reference CPU path throughput: one replica per spec (one process each
-    when there are several), each timing `samples` runs of `steps` steps; per
-    sample, value = sum of particle-steps / slowest replica."""
+    """Reference CPU path throughput: one replica per spec (one spawned process
+    each when there are several), each timing `samples` runs of `steps` steps;
+    per sample, value = sum of particle-steps / slowest replica."""
     import multiprocessing as mp
     if len(specs) == 1:
         done, times = _cpu_worker((specs[0], steps, samples))
@@ -254,51 +284,70 @@ def cpu_baseline(specs, steps, samples=1):
     return vals, walls
 
 
-def _batch_cpu_specs(count, cores, limit=50_000, seed=11):
-    """Scenes of the batch for the CPU replicas: a seeded draw (without
-    replacement while it lasts) among the scenes of at most `limit` spheres,
-    so that a sample stays within seconds."""
+def _median_index(specs):
     import numpy as np
+    return int(np.argsort([d["n"] for d in specs])[len(specs) // 2])
 
-    from metakonga_gb300 import scenes
-    ns = np.array([d["n"] for d in scenes.hopper_batch(count=count)])
-    pool = np.flatnonzero(ns <= limit)
-    rng = np.random.Generator(np.random.MT19937(seed))
-    pick = rng.permutation(pool)
-    pick = np.resize(pick, cores)
-    return [("hopper", count, int(k)) for k in pick], int(ns[pick].sum())
+
+def _settled_hoppers(specs, a, stream):
+    """The batch's hoppers as settled beds with the orifice open: each scene
+    generated with its gate closed, settled by prepare.settle (a.prep_steps
+    steps of a.prep_dt in one batch), the gates then opened."""
+    from metakonga_gb300 import prepare, scenes
+    scs = [scenes.hopper(gate=True, **d) for d in specs]
+    if a.prep_steps:
+        prepare.settle(scs, a.prep_steps, dt=a.prep_dt, stream=stream)
+    prepare.open_gates(scs)
+    return scs
 
 
 def run_reference(a):
+    """The reference's CPU path (the oracle's restatement, single-threaded as
+    the reference is) on the host cores: one replica of the workload's median
+    scene per core, in the same state as the GPU arm's cpu_baseline."""
     world, rank, _ = _dist()
     if rank != 0:
         return
-    cores = os.cpu_count() or 1
-    steps = a.cpu_steps or 1
+    host = host_cpu()
+    cores = host["cores_available"]
+    steps = a.cpu_steps or 10
     t0 = time.perf_counter()
     if a.workload == "box":
-        specs = [("box", a.n)] * cores
+        spec = ("box", a.n)
         workload, cfg = WORKLOAD, {"particles": a.n, "grid": "128^3 wrapped"}
-        sample = (f"{steps} step(s) of the {a.n}-sphere scene per sample, one single-threaded "
-                  f"replica per core ({cores})")
-        per_sample = a.n * cores
+        n_one = a.n
+        what = f"the {a.n}-sphere box"
     else:
-        specs, per_sample = _batch_cpu_specs(a.count, cores)
+        import torch
+
+        from metakonga_gb300 import prepare, scenes
+        specs = scenes.hopper_batch(count=a.count)
+        k = _median_index(specs)
+        sc = scenes.hopper(gate=True, **specs[k])
+        if a.prep_steps:
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+            prepare.settle(sc, a.prep_steps, dt=a.prep_dt)
+        prepare.open_gates(sc)
+        spec = ("scene", sc)
+        n_one = sc.np_
         workload = BATCH_WORKLOAD if a.workload == "batched" else SERVED_WORKLOAD
-        cfg = {"scenes": a.count, "grid": "128^3 wrapped, cell 2 x max(r, triangle circumradius)"}
-        sample = (f"{steps} step(s) per sample of {cores} hopper scenes of the {a.count}-scene batch "
-                  f"(a seeded draw among those of <= 50,000 spheres; {per_sample} spheres), one "
-                  f"single-threaded scene per core ({cores})")
-    vals, walls = cpu_baseline(specs, steps, samples=a.warmup + a.steps)
+        cfg = {"scenes": a.count, "grid": "128^3 wrapped, cell 2 x max(r, triangle circumradius)",
+               "state": "settled bed, orifice open (prepare.settle on the GPU, untimed)"}
+        what = (f"scene {k} of the {a.count}-scene batch ({n_one} spheres, the median; the GPU arm's "
+                f"cpu_baseline scene)")
+    vals, walls = cpu_baseline([spec] * cores, steps, samples=a.warmup + a.steps)
     vals = vals[a.warmup:]
     v = statistics.median(vals)
+    sample = (f"{steps} steps per sample of {what}, one single-threaded replica per core ({cores}); "
+              f"grid work arrays allocated once per replica, outside the timed calls")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": a.gpus,
-        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * per_sample / v,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * n_one * cores / v,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded MT19937 scenes)",
         "config": dict({"workload": workload, "dt": 5e-6, "l2": "state > L2 (no flush)"}, **cfg),
-        "cpu_baseline": {"value": v, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": v, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample,
+                         "per_core": v / cores, "host": host},
         "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": time.perf_counter() - t0,
     }
@@ -537,21 +586,23 @@ def _fp64_alone(scs, steps, stream):
     return out
 
 
-def _fp64_check(sc, squeeze=0.92, seed=29):
+def _fp64_check(sc, squeeze=0.92, seed=29, spin=True):
     """Contact forces of the mixed form against the FP64 form on one state:
-    scene `sc` squeezed towards its centroid by `squeeze` (the lattice pitch
-    falls below the larger diameters, so that neighbouring spheres overlap)
-    with random velocities and spins; per particle
-    |F_mixed - F_fp64| / max(|F_fp64|, m g), and the same for the torque / r."""
+    scene `sc` squeezed towards its centroid by `squeeze` (1: as it stands),
+    with spin=True random velocities and spins; per particle
+    |F_mixed - F_fp64| / max(|F_fp64|, m g) (stricter than the gate's
+    max(sum_c |F_c|, m g): |F| <= sum_c |F_c|), and the same for the torque / r."""
     import numpy as np
 
     from metakonga_gb300 import engine
     st = sc.copy()
-    rng = np.random.Generator(np.random.MT19937(seed))
-    c = st.pos[:, :3].mean(axis=0)
-    st.pos[:, :3] = c + (st.pos[:, :3] - c) * squeeze
-    st.vel[:] = rng.normal(0.0, 0.2, st.vel.shape)
-    st.omega[:] = rng.normal(0.0, 20.0, st.omega.shape)
+    if squeeze != 1.0:
+        c = st.pos[:, :3].mean(axis=0)
+        st.pos[:, :3] = c + (st.pos[:, :3] - c) * squeeze
+    if spin:
+        rng = np.random.Generator(np.random.MT19937(seed))
+        st.vel[:] = rng.normal(0.0, 0.2, st.vel.shape)
+        st.omega[:] = rng.normal(0.0, 20.0, st.omega.shape)
     out = []
     for mode in (engine.MODE_MIXED, engine.MODE_FP64):
         d = engine.DeviceScene(st, mode=mode)
@@ -563,11 +614,11 @@ def _fp64_check(sc, squeeze=0.92, seed=29):
     r = st.pos[:, 3]
     merr = np.linalg.norm((m_m - m_r) / r[:, None], axis=1) / den
     touching = np.linalg.norm(f_r, axis=1) > 0
+    state = (f"scene squeezed by {squeeze} towards its centroid" if squeeze != 1.0 else "the scene's state") + \
+        (", velocities N(0, 0.2) m/s, spins N(0, 20) rad/s" if spin else "")
     return {"particles": int(st.np_), "touching": int(touching.sum()),
             "max_force_err": float(err.max()), "p999_force_err": float(np.percentile(err, 99.9)),
-            "max_torque_over_r_err": float(merr.max()),
-            "state": f"scene squeezed by {squeeze} towards its centroid, velocities N(0, 0.2) m/s, "
-                     "spins N(0, 20) rad/s",
+            "max_torque_over_r_err": float(merr.max()), "state": state,
             "normaliser": "max(|F_fp64|, m g) per particle", "tolerance": 2e-5}
 
 
@@ -706,6 +757,43 @@ def _served(a, stream, plain=True):
     return rep
 
 
+def _time_batch(batch, steps, stream, barrier, world, clock_index=None):
+    """Device time of `steps` batch steps (CUDA events on the launching
+    stream, barriers on both sides, max over ranks); with clock_index the
+    SM clocks are sampled meanwhile."""
+    import torch
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(clock_index) if clock_index is not None else None
+    barrier()
+    if clk:
+        clk.__enter__()
+    ev0.record(stream)
+    batch.step(steps, check=False, stream=stream.cuda_stream)
+    ev1.record(stream)
+    barrier()
+    if clk:
+        clk.__exit__(None, None, None)
+    ms = _max_over_ranks(ev0.elapsed_time(ev1), world)
+    return ms, (clk.summary() if clk else None)
+
+
+def _batch_contact_bytes(ds, sh):
+    """Algorithmic bytes of one contact pass over a batch: per listed sphere
+    its own state and list counts read (B_LISTED) and its force and torque
+    written, plus 4 B per Verlet-list and triangle-list entry read; the
+    neighbours' data count as cache-resident (0 B), the unlisted spheres are
+    not visited.  Also the listed count and the mean list lengths."""
+    listed = ventries = tentries = 0
+    for d in ds:
+        st = d.stats(sh)
+        listed += st["contact_list"]
+        ventries += st["verlet_entries"]
+        tentries += st["triangle_entries"]
+    return (listed * B_LISTED + 4 * (ventries + tentries), listed,
+            ventries / max(listed, 1), tentries / max(listed, 1))
+
+
 def run_batched(a):
     import numpy as np
     import torch
@@ -715,35 +803,55 @@ def run_batched(a):
     world, rank, local, barrier = _torch_setup()
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
-    t0 = time.perf_counter()
+    peak, peak_kind = _peaks()
     specs = scenes.hopper_batch(count=a.count)
-    scs = [scenes.hopper(**d) for d in specs]
-    gen_s = time.perf_counter() - t0
+    k_med = _median_index(specs)
+
+    # ---- the batch as generated (a loose lattice falling): beside the headline
+    lattice = None
+    if not a.no_lattice:
+        scs_l = [scenes.hopper(**d) for d in specs]
+        ds_l = [engine.DeviceScene(sc, mode=engine.MODE_MIXED) for sc in scs_l]
+        b_l = engine.Batch(ds_l)
+        b_l.step(a.warmup, check=True, stream=sh)
+        ms_l, _ = _time_batch(b_l, a.steps, stream, barrier, world)
+        n_l = sum(sc.np_ for sc in scs_l)
+        lattice = {"value": world * n_l * a.steps / (ms_l / 1e3), "unit": METRIC, "ms_per_step": ms_l / a.steps,
+                   "listed_fraction": sum(d.stats(sh)["contact_list"] for d in ds_l) / n_l,
+                   "state": "the hoppers as generated: jittered lattices (pitch >= 2.04 r_max, no contact) "
+                            f"falling, {a.warmup} warm-up steps in"}
+        b_l.close()
+        for d in ds_l:
+            d.close()
+        del ds_l, scs_l
+        torch.cuda.empty_cache()
+
+    # ---- the headline: settled beds discharging through the opened orifice
+    t0 = time.perf_counter()
+    scs = _settled_hoppers(specs, a, sh)
+    torch.cuda.synchronize()
+    prep_s = time.perf_counter() - t0
     n_tot = sum(sc.np_ for sc in scs)
     ds = [engine.DeviceScene(sc, mode=engine.MODE_MIXED) for sc in scs]
     dev_bytes = sum(d.device_bytes() for d in ds)
-    # every scene's steps together: one CUDA graph per batch step (captured
-    # at the first call, which the warm-up makes)
     batch = engine.Batch(ds)
     batch.step(a.warmup, check=True, stream=sh)
-    barrier()
     rb0 = [d.rebuilds(sh) for d in ds]
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    clk = ClockSampler(local)
-    barrier()
-    with clk:
-        ev0.record(stream)
-        batch.step(a.steps, check=False, stream=sh)
-        ev1.record(stream)
-        barrier()
-    ms = _max_over_ranks(ev0.elapsed_time(ev1), world)
+    st0 = [d.stats(sh) for d in ds]
+    ms, clocks = _time_batch(batch, a.steps, stream, barrier, world, clock_index=local)
     value = world * n_tot * a.steps / (ms / 1e3)
     rb1 = [d.rebuilds(sh) for d in ds]
+    st1 = [d.stats(sh) for d in ds]
     rebuilds = sum(b[0] - r[0] for r, b in zip(rb0, rb1))
+    rechecks = {k: sum(y[k] - x[k] for x, y in zip(st0, st1)) / a.steps
+                for k in ("fp64_decisions", "fp64_normal_forces", "fp64_slips", "fp64_wall_regions")}
+    contact_bytes, listed, vlen, tlen = _batch_contact_bytes(ds, sh)
+    pick = [int(i) for i in np.argsort([sc.np_ for sc in scs])[[len(scs) // 8, len(scs) // 2, -1]]]
+    coord = {str(scs[i].np_): ds[i].pair_list(cap=32).shape[0] / scs[i].np_ for i in pick}
 
-    # the batch's dominant kernel, timed live: the same kernels launched
-    # directly with CUDA events around each advance and contact launch
+    # the kernels timed live: the same steps launched directly with CUDA
+    # events around each advance and contact launch (events cannot split the
+    # step graph)
     ksteps = max(3, min(a.steps, 20))
     batch.set_timing(True)
     batch.step(ksteps, check=True, stream=sh)
@@ -751,32 +859,40 @@ def run_batched(a):
     batch.set_timing(False)
     adv_ms = kt["advance"][0] / max(kt["advance"][1], 1)
     con_ms = kt["contact"][0] / max(kt["contact"][1], 1)
-    peak, peak_kind = _peaks()
-    tpp = _traffic_from_profiles("advance_batch_hopper.md", "traffic_bytes_per_particle")
-    achieved = n_tot * B_ADVANCE / (adv_ms / 1e3) / 1e9
-    roof = {"bound": "hbm",
-            "kernel": "k_batch_advance<1> (velocity-Verlet kick and drift, contact view and skin test of "
-                      "every scene's spheres in one launch)",
-            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-            "traffic": tpp * n_tot if tpp else None, "bytes_per_particle": B_ADVANCE, "avg_launch_ms": adv_ms,
-            "launches_timed": kt["advance"][1],
-            "contact_pass": {"kernel": "k_batch_contact (every scene's listed spheres in one launch)",
-                             "avg_launch_ms": con_ms, "bytes_per_particle_full_pass": B_CONTACT["mixed"],
-                             "achieved_full_pass_gbs": n_tot * B_CONTACT["mixed"] / (con_ms / 1e3) / 1e9,
-                             "note": "a full pass's bytes over the launch time; above the copy peak when, "
-                                     "as here, only part of the spheres are listed (those with neighbours "
-                                     "or walls within the skin)"},
-            "workload": f"the {len(scs)}-hopper batch, {n_tot:,} spheres; {ksteps} steps with direct launches "
-                        "after the timed ones (events cannot split the step graph)",
-            "traffic_note": "profiles/advance_batch_hopper.md: DRAM bytes per sphere of one launch on a "
-                            "64-hopper batch, times the spheres here"}
+    adv_gbs = n_tot * B_ADVANCE / (adv_ms / 1e3) / 1e9
+    con_gbs = contact_bytes / (con_ms / 1e3) / 1e9
+    adv_traffic = _traffic_from_profiles("advance_batch_hopper.md", "traffic_bytes_per_particle")
+    con_traffic = _traffic_from_profiles("contact_batch_hopper_dense.md", "traffic_bytes_per_listed_sphere")
+    kernels = {
+        "advance": {"kernel": "k_batch_advance<1> (velocity-Verlet kick and drift, contact view and skin test of "
+                              "every scene's spheres in one launch)",
+                    "avg_launch_ms": adv_ms, "bytes": n_tot * B_ADVANCE, "bytes_per_particle": B_ADVANCE,
+                    "achieved": adv_gbs, "frac": adv_gbs / peak,
+                    "traffic": adv_traffic * n_tot if adv_traffic else None},
+        "contact": {"kernel": "k_batch_contact (every scene's listed spheres in one launch: pairs over the Verlet "
+                              "lists, planes and triangles in reach)",
+                    "avg_launch_ms": con_ms, "bytes": contact_bytes, "listed": listed,
+                    "bytes_per_listed_sphere": contact_bytes / max(listed, 1),
+                    "mean_verlet_entries": vlen, "mean_triangle_entries": tlen,
+                    "achieved": con_gbs, "frac": con_gbs / peak,
+                    "traffic": con_traffic * listed if con_traffic else None},
+    }
+    dom = "contact" if con_ms >= adv_ms else "advance"
+    dk = kernels[dom]
+    roof = {"bound": "hbm", "kernel": dk["kernel"], "achieved": dk["achieved"], "peak": peak, "unit": "GB/s",
+            "frac": dk["frac"], "peak_kind": peak_kind, "traffic": dk["traffic"], "avg_launch_ms": dk["avg_launch_ms"],
+            "launches_timed": kt[dom][1],
+            "algorithmic_bytes_per_launch": dk["bytes"],
+            "workload": f"the {len(scs)} settled hoppers ({n_tot:,} spheres); {ksteps} steps with direct "
+                        "launches after the timed ones",
+            "kernels": kernels,
+            "traffic_note": "DRAM bytes per unit of one ncu-captured launch (profiles/advance_batch_hopper.md per "
+                            "sphere, profiles/contact_batch_hopper_dense.md per listed sphere) times the units here"}
     # per step: advance, decision, run prefix and contact over all scenes; per
     # call the finish and each scene's body-reaction sum; per re-binning its
     # kernels and its group's decision kernel
     launches = (4 * a.steps + 1 + sum(1 for sc in scs if sc.ntri)
                 + sum((b[0] - r[0]) * (b[1] + 1) for r, b in zip(rb0, rb1)))
-
-    k_med = int(np.argsort([sc.np_ for sc in scs])[len(scs) // 2])
 
     # e2e: every scene's state uploaded from pinned host memory, K steps, the
     # state downloaded; the downloaded state is the next upload's input
@@ -819,42 +935,6 @@ def run_batched(a):
     barrier()
     e2e_s = _max_over_ranks(time.perf_counter() - t1, world)
     e2e_value = world * n_tot * a.steps / e2e_s
-
-    # the batch step's algorithmic bytes: the advance and a full contact pass per sphere
-    batch_bytes = n_tot * (B_ADVANCE + B_CONTACT["mixed"])
-    batch_gbs = batch_bytes / (ms / a.steps / 1e3) / 1e9
-
-    # the same batch once the spheres have fallen onto each other: the
-    # lattice's gaps close within a few thousand steps, and the contact pass
-    # then lists most spheres
-    dense = None
-    if a.settle_steps:
-        batch.step(a.settle_steps, check=True, stream=sh)
-        rbd0 = sum(d.rebuilds(sh)[0] for d in ds)
-        cnt0 = [d.counters(sh) for d in ds]
-        barrier()
-        ev0.record(stream)
-        batch.step(a.steps, check=False, stream=sh)
-        ev1.record(stream)
-        barrier()
-        dms = _max_over_ranks(ev0.elapsed_time(ev1), world)
-        drb = sum(d.rebuilds(sh)[0] for d in ds) - rbd0
-        cnt1 = [d.counters(sh) for d in ds]
-        fp64 = {k: sum(c1[k] - c0[k] for c0, c1 in zip(cnt0, cnt1)) / a.steps
-                for k in ("fp64_decisions", "fp64_normal_forces", "fp64_slips")}
-        batch.set_timing(True)
-        batch.step(ksteps, check=True, stream=sh)
-        dkt = batch.kernel_times()
-        batch.set_timing(False)
-        listed = sum(d.counters(sh)["contact_list"] for d in ds)
-        dense = {"value": world * n_tot * a.steps / (dms / 1e3), "unit": METRIC, "ms_per_step": dms / a.steps,
-                 "after_steps": a.settle_steps, "cell_rebinnings_in_timed_steps": drb,
-                 "advance_ms": dkt["advance"][0] / max(dkt["advance"][1], 1),
-                 "contact_ms": dkt["contact"][0] / max(dkt["contact"][1], 1),
-                 "listed_fraction": listed / n_tot,
-                 "fp64_rechecks_per_step": fp64,
-                 "note": "the same 50 steps timed after the spheres fell for the given steps "
-                         "(dt 5e-6): contacts throughout the piles"}
     batch.close()
     for d in ds:
         d.close()
@@ -868,13 +948,13 @@ def run_batched(a):
         fp64_ms = sum(per)
         plain = {"value": world * n_tot / (fp64_ms / 1e3), "unit": METRIC,
                  "ms_per_batch_step": fp64_ms,
-                 "method": "each scene alone in the FP64 form (the reference's algorithm: 128^3 grid "
+                 "method": "each settled scene alone in the FP64 form (the reference's algorithm: 128^3 grid "
                            "of 2 x max(r, triangle circumradius) cells, re-sorted every step), one "
                            f"warm-up step then {psteps} device-timed steps; ms summed over scenes",
                  "ratio": value / (world * n_tot / (fp64_ms / 1e3))}
 
-    # FP64 check on the median-size scene, in a state with contacts
-    check = _fp64_check(scs[k_med])
+    # FP64 check on the median scene's settled bed
+    check = _fp64_check(scs[k_med], squeeze=1.0, spin=False)
     check["scene"] = k_med
     box_roof, box = _box_roofline(a, stream, barrier, world, local) if not a.no_box else (None, None)
     settle = _settle_small(stream, cpu=not a.no_cpu_baseline) if rank == 0 and not a.no_box else None
@@ -885,12 +965,13 @@ def run_batched(a):
 
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
-        k_cpu = k_med
-        csteps = a.cpu_steps or 100
-        vals, times = cpu_baseline([("hopper", a.count, k_cpu)], csteps, samples=1)
+        csteps = a.cpu_steps or 20
+        vals, times = cpu_baseline([("scene", scs[k_med])], csteps, samples=1)
         cpu = {"value": vals[0], "unit": METRIC, "cores": 1, "kind": "port",
-               "sample": f"{csteps} steps of scene {k_cpu} of the batch ({scs[k_cpu].np_} spheres), "
-                         f"reference CPU path (restated, single thread), {times[0]:.1f} s"}
+               "sample": f"{csteps} steps of scene {k_med} of the batch ({scs[k_med].np_} spheres, the median; "
+                         f"its settled bed as timed here), reference CPU path (restated, single thread, "
+                         f"polygon contacts included), {times[0]:.1f} s",
+               "host": host_cpu()}
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
@@ -901,33 +982,36 @@ def run_batched(a):
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
-        "data": "synthetic (seeded MT19937 scenes: jittered lattices in cones of triangles)",
+        "data": "synthetic (seeded MT19937 scenes: settled beds in cones of triangles)",
         "config": {"workload": BATCH_WORKLOAD, "scenes": len(scs), "particles": n_tot,
                    "particles_min": min(sc.np_ for sc in scs), "particles_max": max(sc.np_ for sc in scs),
                    "triangles_per_scene": int(scs[0].ntri), "dt": 5e-6, "mode": "mixed",
+                   "state": (f"settled beds discharging: each hopper filled as a lattice with its orifice gated, "
+                             f"settled by {a.prep_steps} steps of {a.prep_dt:g} s in the mixed form "
+                             f"({prep_s:.0f} s, untimed), the gate then opened; {a.warmup} warm-up steps"),
+                   "listed_fraction": listed / n_tot,
+                   "mean_coordination": coord,
+                   "fp64_rechecks_per_step": rechecks,
                    "grid": "one grid per scene sized to its cone, cell 2 r_max + skin",
                    "stepping": ("xd_batch: CUDA graphs of one or four batch steps -- one advance and one contact "
                                 "launch over all scenes, each scene's re-binning behind conditional nodes"),
                    "l2": "batch state > L2 (no flush)", "device_bytes": dev_bytes,
-                   "generation_s": gen_s, "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d / a.steps,
                 "d2h_bytes_per_step": d2h / a.steps, "h2d_bytes_per_job": h2d, "d2h_bytes_per_job": d2h,
                 "job": f"upload all {len(scs)} states from pinned host memory, {a.steps} steps, download"},
         "gpu_launches": launches,
         "cell_rebinnings_in_timed_steps": rebuilds,
+        "lattice_start": lattice,
         "plain_fp64": plain,
         "fp64_check": check,
-        "dense": dense,
-        "batch_hbm": {"bytes_per_step": batch_bytes, "achieved_gbs": batch_gbs, "peak": peak,
-                      "frac": batch_gbs / peak, "peak_kind": peak_kind,
-                      "bytes_per_particle": B_ADVANCE + B_CONTACT["mixed"]},
         "roofline": roof,
         "single_scene_box": box,
         "settle_8000": settle,
         "drum": drum,
         "served": served,
         "cpu_baseline": cpu,
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
 

@@ -210,12 +210,16 @@ int xd_reorder_and_find_cell_start(unsigned* hash, unsigned* index, unsigned* cs
  * scratch comes from a fixed device array inside the library instead of
  * cudaMalloc, and the call allocates nothing.  Limits and rules:
  *   - at most XD_NOALLOC_MAX_ENTRIES entries (n); larger n -> XD_ERR_CAPACITY;
- *   - the array (about 9.4 MB) stays on every device that loads the library
- *     until the process exits;
+ *   - the array (about 9.4 MB) stays on every device that uses it until the
+ *     process exits.  Under lazy module loading (the CUDA default) the driver
+ *     reserves it at the first call on a device, so a caller whose own pool
+ *     takes the device's memory makes one call first (n = 0 only clears the
+ *     cell arrays and serves as that set-up) or sets
+ *     CUDA_MODULE_LOADING=EAGER; later calls reserve nothing;
  *   - all calls share the array: calls that overlap on the GPU (other
  *     streams or host threads) race, so serialise them;
- *   - a device's first call looks up the array's device address, so make it
- *     before any stream capture on that device.
+ *   - every call looks up the array's device address on the current device;
+ *     make a device's first call before any stream capture on that device.
  * Same arguments, results and status codes as xd_reorder_and_find_cell_start. */
 #define XD_NOALLOC_MAX_ENTRIES (1u << 20)
 int xd_reorder_and_find_cell_start_noalloc(unsigned* hash, unsigned* index, unsigned* cstart,
@@ -518,6 +522,35 @@ int xd_scene_pair_list(xd_scene* scene, unsigned cap, unsigned* counts, unsigned
  * (cumulative), [3] slips formed in FP64 because the rotation term cancels
  * most of the tangential velocity (cumulative). */
 int xd_scene_counters(xd_scene* scene, unsigned long long out[4], void* stream);
+
+/* Mixed-mode diagnostics (no counterpart in the reference), the first
+ * `count` of: [0..3] as xd_scene_counters; [4] wall contacts (planes and
+ * triangles) decided by the FP64 region test instead of the FP64 plane
+ * distance of a clear face contact (cumulative); [5] re-binnings
+ * (cumulative); [6] listed particles with triangles in reach; [7] Verlet
+ * lists and [8] triangle lists over their capacity at the last build (those
+ * particles' contacts are searched in the cells); [9] Verlet-list and [10]
+ * triangle-list entries at the last build.  Zeros for an FP64 scene. */
+#define XD_STATS_COUNT 11
+int xd_scene_stats(xd_scene* scene, unsigned long long* out, unsigned count, void* stream);
+
+/* Mixed-mode tuning (no counterpart in the reference, whose grid and launch
+ * shapes are fixed: dem_simulation.cpp:259-261): the skin width over the
+ * largest radius (cells are 2 r_max + skin wide; a larger skin re-bins less
+ * often but lists more neighbours), the Verlet-list and triangle-list
+ * capacities per particle (a fuller list makes that particle's contact pass
+ * search its cells instead), and the contact pass's block size.  Set before
+ * the scene's first upload (XD_ERR_STATE after); a batch launches its
+ * contact pass with its first scene's block size.  Defaults: 0.1, 48, 16, 64.
+ * metakonga_gb300.tune chooses them per scene shape. */
+typedef struct xd_tuning {
+    float skin_factor;          /* [0.02, 1] */
+    unsigned verlet_cap;        /* [8, 256] */
+    unsigned triangle_cap;      /* [4, 128] */
+    unsigned contact_threads;   /* 32, 64 or 128 */
+} xd_tuning;
+int xd_scene_set_tuning(xd_scene* scene, const xd_tuning* tuning);
+int xd_scene_get_tuning(xd_scene* scene, xd_tuning* tuning);
 
 /* Number of kernel launches one xd_scene_step of nsteps issues, not counting
  * the cell re-binnings the mixed mode decides on the device (see

@@ -96,6 +96,9 @@ _SIGS = {
     "xd_scene_eval_contacts": [vp, vp, vp, vp],
     "xd_scene_pair_list": [vp, u32, vp, vp, vp],
     "xd_scene_counters": [vp, vp, vp],
+    "xd_scene_stats": [vp, vp, u32, vp],
+    "xd_scene_set_tuning": [vp, vp],
+    "xd_scene_get_tuning": [vp, vp],
     "xd_scene_rebuilds": [vp, vp, vp, vp],
     "xd_scene_step_many": [vp, vp, u32, i32, vp],
     "xd_scene_set_tangential_history": [vp, u32],

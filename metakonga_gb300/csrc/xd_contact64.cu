@@ -656,18 +656,20 @@ int launch_body_advance(xd_polygon_mass_info* pmi, unsigned nbodies, double dt, 
 
 // The mesh update and, for the mixed form, whether a vertex has moved from
 // its position at the last list build (ref: FP32, relative to the grid origin
-// wo) by disp2 or more: *flag is raised then.
+// wo) by disp2 or more: *flag is raised then.  rec (the mixed form's
+// triangle records) is rewritten from the new vertices.
 __global__ void __launch_bounds__(64) k_mesh_move(const xd_polygon_mass_info* __restrict__ dpmi,
                                                   const double* __restrict__ vlist, double* __restrict__ sphere,
                                                   xd_polygon_info* __restrict__ dpi, unsigned ntri,
                                                   const float* __restrict__ ref, double wo0, double wo1, double wo2,
-                                                  float disp2, unsigned* __restrict__ flag)
+                                                  float disp2, unsigned* __restrict__ flag, TriRec* __restrict__ rec)
 {
     const unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
     bool out = false;
     if (id < ntri) {
         d3 V[3];
         update_polygon_one(dpmi, vlist, sphere, dpi, id, V[0], V[1], V[2]);
+        if (rec) write_tri_rec(rec + id, V[0], V[1], V[2], (unsigned)dpi[id].id);
         const double wo[3] = { wo0, wo1, wo2 };
         for (int k = 0; k < 3; ++k) {
             const double c[3] = { V[k].x, V[k].y, V[k].z };
@@ -684,12 +686,29 @@ __global__ void __launch_bounds__(64) k_mesh_move(const xd_polygon_mass_info* __
 
 int launch_mesh_move(const xd_polygon_mass_info* dpmi, const double* vlist, double* sphere, xd_polygon_info* dpi,
                      unsigned ntri, const float* ref, const double wo[3], float disp2, unsigned* flag,
-                     cudaStream_t s)
+                     TriRec* rec, cudaStream_t s)
 {
     if (ntri == 0) return XD_OK;
     k_mesh_move<<<div_up(ntri, 64), 64, 0, s>>>(dpmi, vlist, sphere, dpi, ntri, ref, wo[0], wo[1], wo[2], disp2,
-                                               flag);
+                                               flag, rec);
     return launch_status("mesh move");
+}
+
+// The mixed form's triangle records of the mesh as it stands.
+__global__ void __launch_bounds__(64) k_tri_records(const xd_polygon_info* __restrict__ dpi, unsigned ntri,
+                                                    TriRec* __restrict__ rec)
+{
+    const unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= ntri) return;
+    const xd_polygon_info* t = dpi + id;
+    write_tri_rec(rec + id, ldp3(t->P), ldp3(t->Q), ldp3(t->R), (unsigned)__ldg(&t->id));
+}
+
+int launch_tri_records(const xd_polygon_info* dpi, unsigned ntri, TriRec* rec, cudaStream_t s)
+{
+    if (ntri == 0) return XD_OK;
+    k_tri_records<<<div_up(ntri, 64), 64, 0, s>>>(dpi, ntri, rec);
+    return launch_status("triangle records");
 }
 
 int launch_update_polygon(const xd_polygon_mass_info* dpmi, const double* vlist, double* sphere,

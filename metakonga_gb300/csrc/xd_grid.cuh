@@ -53,10 +53,14 @@ int launch_body_advance(xd_polygon_mass_info* pmi, unsigned nbodies, double dt, 
 int launch_update_polygon(const xd_polygon_mass_info* dpmi, const double* vlist, double* sphere,
                           xd_polygon_info* dpi, unsigned ntri, cudaStream_t s);
 // The mesh update with the mixed form's moved check in one launch (see
-// k_mesh_move): *flag raised when a vertex moved disp2 or more from ref.
+// k_mesh_move): *flag raised when a vertex moved disp2 or more from ref; rec
+// (nullable) receives the triangle records of the new pose.
+struct TriRec;
 int launch_mesh_move(const xd_polygon_mass_info* dpmi, const double* vlist, double* sphere, xd_polygon_info* dpi,
                      unsigned ntri, const float* ref, const double wo[3], float disp2, unsigned* flag,
-                     cudaStream_t s);
+                     TriRec* rec, cudaStream_t s);
+// The mixed form's triangle records of a mesh as it stands.
+int launch_tri_records(const xd_polygon_info* dpi, unsigned ntri, TriRec* rec, cudaStream_t s);
 int reduction_d3(const double* in, unsigned n, double out[3], void* scratch, cudaStream_t s);
 size_t reduction_scratch_bytes(unsigned n);
 size_t pair_list_scratch_bytes(unsigned np);

@@ -65,8 +65,12 @@ constexpr double kQ = 68719476736.0;           // 2^36 fixed-point units per met
 constexpr float kU = 1.4551915228366852e-11f;  // 2^-36 m
 constexpr double kGuard = 2e-10;               // metres: FP64 decision inside this band
 constexpr double kMagic = 6755399441055744.0;  // 1.5 * 2^52
-constexpr unsigned kVerletCap = 48;            // neighbours per particle kept in the Verlet list
-constexpr unsigned kTriCap = 16;               // triangles per particle kept in its list
+constexpr unsigned kVerletCap = 48;            // default: neighbours per particle kept in the Verlet list
+constexpr unsigned kTriCap = 16;               // default: triangles per particle kept in its list
+constexpr float kSkinFactor = 0.1f;            // default: skin width over the largest radius
+constexpr unsigned kContactThreads = 64;       // default block size of the contact pass
+constexpr unsigned kContactMaxThreads = 128;   // the largest block size a scene may choose
+constexpr unsigned kContactWarpsTotal = 152 * 16;   // warps of a full contact grid (every SM, 16 warps each)
 constexpr int kMaxBodies = 8;                  // polygon bodies of a mixed scene
 constexpr unsigned kGuardBit = 0x80000000u;    // list entry decided by the FP64 test
 
@@ -83,7 +87,12 @@ enum {
     CN_RXN = 8,        // blocks of k_rxn_sum done (the last one finishes the sum)
     CN_HTRI = 9,       // listed particles with triangles in reach: hlist[0, CN_HTRI)
     CN_HBACK = 10,     // the other listed particles: hlist[n - CN_HBACK, n)
-    kCounters = 11
+    CN_WALLS = 11,     // wall contacts decided by the FP64 region test (cumulative)
+    CN_VINC = 12,      // Verlet lists over their capacity at the last build (the pass searches the cells)
+    CN_TINC = 13,      // triangle lists over their capacity at the last build
+    CN_VSUM = 14,      // Verlet-list entries at the last build
+    CN_TSUM = 15,      // triangle-list entries at the last build
+    kCounters = 16
 };
 
 struct Master {
@@ -118,6 +127,7 @@ struct MixParams {
     float tol;           // prefilter tolerance (m)
     float c43Eeq, one_b2, sratio, fric;
     double c43Eeq_d, one_b2_d;   // the same constants in FP64 (rechecks)
+    float2 c43Eeq_p, one_b2_p;   // and as float pairs (hi + lo)
     // cohesionForce (impl:259-279): coh and its Eeq = (1 - pri^2)/Ei + (1 - prj^2)/Ej
     float coh, coh_eeq;
     double coh_d, coh_eeq_d;
@@ -130,9 +140,21 @@ struct MixParams {
     float wall_tol;
     int rolling;         // rollingCondition: rotation terms in the relative velocity
     unsigned ntri, nbodies;
+    unsigned vcap, tcap; // Verlet-list and triangle-list capacities per particle
     float tri_reach;     // a triangle is registered in every cell within this of its box
     double pb_c43Eeq[kMaxBodies], pb_one_b2[kMaxBodies];   // getConstant's terms per polygon body
     double pb_sratio[kMaxBodies], pb_fric[kMaxBodies];
+};
+
+// Per-plane record of the contact pass (written whenever the planes are
+// set): the corner xw and the unit normal uw / |uw| in FP64 (a face contact's
+// distance is (x - xw) . n, impl:557-560), and the edge directions and
+// lengths in FP32 for the region test.
+struct __align__(16) PlaneRec {
+    double xw[3];
+    double n[3];
+    float u1[3], u2[3];
+    float l1, l2;
 };
 
 }  // namespace
@@ -142,6 +164,9 @@ struct MixedScene {
     // held.  They differ only under an emitter: slots [n, cap) then hold the
     // particles not yet emitted, in id order (no re-binning touches them).
     unsigned n = 0, cap = 0, nplanes = 0, ncell = 0;
+    // tuning (xd_scene_set_tuning, before the first upload)
+    float skin_factor = kSkinFactor;
+    unsigned vcap = kVerletCap, tcap = kTriCap, cthreads = kContactThreads;
     unsigned active_req = ~0u;    // active count set before the first upload
     bool emitted = false;         // the particle count has changed since the graphs were made
     unsigned version = 0;         // raised whenever the step graphs are dropped (parameters changed)
@@ -161,7 +186,7 @@ struct MixedScene {
     unsigned* hlist = nullptr;    // particles with neighbours or planes in reach
     unsigned short* wmask = nullptr;   // planes in reach of each particle
     unsigned* vcount = nullptr;   // Verlet neighbours per particle (| kIncomplete: overflow)
-    unsigned* vlist = nullptr;    // [kVerletCap][n]: neighbour slots in search order
+    unsigned* vlist = nullptr;    // [vcap][n]: neighbour slots in search order
     float4* pref = nullptr;       // FP32 positions at the last list build
     // triangle meshes (FP64, world frame) and their polygon bodies
     unsigned ntri = 0, nbodies = 0;
@@ -171,6 +196,7 @@ struct MixedScene {
     xd_polygon_mass_info* pmi = nullptr;
     float* tri_ref = nullptr;     // vertices at the last build, FP32 relative to the grid origin
     float4* tbound = nullptr;     // bounding sphere of each triangle at the last build (same frame)
+    TriRec* trec = nullptr;       // the contact pass's triangle records of the current pose
     unsigned* tcells = nullptr;   // cells per triangle, then their exclusive scan [ntri + 1]
     unsigned* tpk = nullptr;      // (cell, triangle) pairs [tpair_cap]: keys, triangles
     unsigned* tpt = nullptr;
@@ -179,7 +205,7 @@ struct MixedScene {
     unsigned* tpk_sorted = nullptr;   // the sort's outputs (fixed for the scene)
     unsigned* tpt_sorted = nullptr;
     unsigned* tcount = nullptr;   // triangles in reach per particle (| kIncomplete: overflow)
-    unsigned* tlist = nullptr;    // [kTriCap][n]: triangle ids in id order
+    unsigned* tlist = nullptr;    // [tcap][n]: triangle ids in id order
     double* rxn = nullptr;        // reaction on the bodies per particle [nbodies][6][n]
     double* rxn_part = nullptr;   // block partials of its fixed-order sum
     bool bodies_dirty = false;
@@ -198,6 +224,7 @@ struct MixedScene {
     unsigned* sorted_keys = nullptr;
     // walls
     xd_plane_info* planes = nullptr;
+    PlaneRec* prec = nullptr;     // the contact pass's plane records
     xd_contact_property* cps = nullptr;
     unsigned* counters = nullptr;
     // pair recording
@@ -333,7 +360,8 @@ __device__ __forceinline__ void df_diff(float ah, float bh, float dlo, float& s,
 // contact normal cancels; here it is carried with ~2^-44 relative error and
 // rounded once.
 __device__ __forceinline__ float normal_speed(const float s[3], const float t[3], const int dq[3],
-                                              float d0, long long D2)
+                                              float d0, long long D2, float& q0_out, float& q1_out,
+                                              float& c_out)
 {
     float hi = 0.f, lo = 0.f;
 #pragma unroll
@@ -359,7 +387,127 @@ __device__ __forceinline__ float normal_speed(const float s[3], const float t[3]
     float qp, qpe;
     two_prod(q0, d0, qp, qpe);
     const float rem = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(nv, qp), qpe), nl), __fmul_rn(q0, c));
-    return __fadd_rn(q0, __fdiv_rn(rem, d0));
+    q0_out = q0;
+    q1_out = __fdiv_rn(rem, d0);
+    c_out = c;
+    return __fadd_rn(q0, q1_out);
+}
+
+// ---- pair arithmetic for the rolling slip ---------------------------------
+
+__device__ __forceinline__ dfl df_make(float a, float b)
+{
+    dfl r;
+    two_sum(a, b, r.hi, r.lo);
+    return r;
+}
+__device__ __forceinline__ dfl df_neg(dfl a) { return dfl{ -a.hi, -a.lo }; }
+__device__ __forceinline__ dfl df_sub(dfl a, dfl b) { return df_add(a, df_neg(b)); }
+
+// 1 / (d0 + c) as a pair: r0 = 1 / d0 refined by one Newton step (the
+// residual 1 - d0 r0 of a rounded reciprocal is exact in one FMA).
+__device__ __forceinline__ dfl df_inv(float d0, float c)
+{
+    const float r0 = __fdiv_rn(1.0f, d0);
+    const float res = __fsub_rn(__fmaf_rn(-d0, r0, 1.0f), __fmul_rn(c, r0));
+    dfl r;
+    fast_two_sum(r0, __fmul_rn(r0, res), r.hi, r.lo);
+    return r;
+}
+
+// A fixed-point length (units of 2^-36 m, |q| < 2^44) as an exact pair.
+__device__ __forceinline__ dfl q_to_df(long long q)
+{
+    return df_make(__fmul_rn(__int2float_rn((int)(q >> 20)), 0x1p-16f),
+                   __fmul_rn(__int2float_rn((int)(q & 0xfffff)), 0x1p-36f));
+}
+
+// The slip e = rv - (rv . u) u of a pair in pair arithmetic (about 2^-44 of
+// its terms), rounded once: rv = dv - W x u with W = rj wj + ri wi
+// (impl:455), dv = s + t exact, u = dq / |dq| from the exact integer
+// separation (|dq| = d0 + c), the radii from their fixed-point values, the
+// angular velocities from their hi/lo pairs, and the normal speed q0 + q1.
+// Used where the FP32 rotation term's rounding could matter (rolling).
+__device__ __noinline__ f3 slip_pair(const float s[3], const float t[3], const int dq[3], float d0, float c,
+                                     float q0, float q1, long long qri, long long qrj, float4 wih, float4 wil,
+                                     float4 wjh, float4 wjl)
+{
+    const dfl inv = df_inv(d0, c);
+    dfl u[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float qh = __int2float_rn(dq[k]);
+        const float ql = __int2float_rn(dq[k] - __float2int_rn(qh));
+        u[k] = df_mul(df_make(qh, ql), inv);
+    }
+    const dfl ri = q_to_df(qri), rj = q_to_df(qrj);
+    const dfl W[3] = { df_add(df_mul(rj, dfl{ wjh.x, wjl.x }), df_mul(ri, dfl{ wih.x, wil.x })),
+                       df_add(df_mul(rj, dfl{ wjh.y, wjl.y }), df_mul(ri, dfl{ wih.y, wil.y })),
+                       df_add(df_mul(rj, dfl{ wjh.z, wjl.z }), df_mul(ri, dfl{ wih.z, wil.z })) };
+    const dfl wu[3] = { df_sub(df_mul(W[1], u[2]), df_mul(W[2], u[1])),
+                        df_sub(df_mul(W[2], u[0]), df_mul(W[0], u[2])),
+                        df_sub(df_mul(W[0], u[1]), df_mul(W[1], u[0])) };
+    const dfl rvu = df_make(q0, q1);
+    float e[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const dfl v = df_sub(df_sub(df_make(s[k], t[k]), wu[k]), df_mul(rvu, u[k]));
+        e[k] = __fadd_rn(v.hi, v.lo);
+    }
+    return fk(e[0], e[1], e[2]);
+}
+
+// a / b and sqrt(a) in pair arithmetic (one correction step each)
+__device__ __forceinline__ dfl df_div(dfl a, dfl b)
+{
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const dfl r = df_sub(a, df_mul(b, dfl{ q1, 0.f }));
+    dfl q;
+    fast_two_sum(q1, __fdiv_rn(r.hi, b.hi), q.hi, q.lo);
+    return q;
+}
+__device__ __forceinline__ dfl df_sqrt(dfl a)
+{
+    if (!(a.hi > 0.f)) return dfl{ 0.f, 0.f };
+    const float s0 = __fsqrt_rn(a.hi);
+    float p, pe;
+    two_prod(s0, s0, p, pe);
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), pe), a.lo);
+    dfl q;
+    fast_two_sum(s0, __fdiv_rn(r, __fmul_rn(2.f, s0)), q.hi, q.lo);
+    return q;
+}
+// an FP64 value as a float pair
+__device__ __forceinline__ dfl d_to_df(double x)
+{
+    const float h = __double2float_rn(x);
+    return dfl{ h, __double2float_rn(x - (double)h) };
+}
+
+// The normal force -kn d^1.5 + vn (dv . u) of pair (i, j) in pair arithmetic
+// (about 2^-44 of its terms), for contacts whose FP32 terms nearly cancel:
+// the overlap (ri + rj) - |xj - xi| from the FP64 positions and radii (the
+// reference's expression, impl:449-452), getConstant's Req and Meq from the
+// FP64 radii and masses (impl:238-246), the normal speed q0 + q1.  No
+// cohesion (the cohesive recheck is FP64).
+__device__ __noinline__ float normal_pair(const MixParams& P, const Master& M, const double* __restrict__ mass0,
+                                          unsigned i, unsigned j, unsigned idi, unsigned idj, float q0, float q1)
+{
+    const dfl X = d_to_df(__ldg(M.x + j) - __ldg(M.x + i));
+    const dfl Y = d_to_df(__ldg(M.y + j) - __ldg(M.y + i));
+    const dfl Z = d_to_df(__ldg(M.z + j) - __ldg(M.z + i));
+    const dfl d = df_sqrt(df_add(df_add(df_mul(X, X), df_mul(Y, Y)), df_mul(Z, Z)));
+    const dfl ri = d_to_df(__ldg(M.r + i)), rj = d_to_df(__ldg(M.r + j));
+    const dfl rs = df_add(ri, rj);
+    const dfl delta = df_sub(rs, d);
+    const dfl mi = d_to_df(__ldg(mass0 + idi)), mj = d_to_df(__ldg(mass0 + idj));
+    const dfl Req = df_div(df_mul(ri, rj), rs);
+    const dfl Meq = df_div(df_mul(mi, mj), df_add(mi, mj));
+    const dfl kn = df_mul(df_of(P.c43Eeq_p), df_sqrt(Req));
+    const dfl vn = df_sqrt(df_div(df_mul(df_mul(dfl{ 4.f, 0.f }, Meq), kn), df_of(P.one_b2_p)));
+    const dfl fsn = df_neg(df_mul(kn, df_mul(delta, df_sqrt(delta))));
+    const dfl fn = df_add(fsn, df_mul(vn, df_make(q0, q1)));
+    return __fadd_rn(fn.hi, fn.lo);
 }
 
 // ---- fixed point and the contact view --------------------------------------
@@ -433,6 +581,23 @@ __device__ __forceinline__ void warp_append(bool take, const T& v, T* __restrict
     if ((int)lane == leader) base = atomicAdd(cnt, (unsigned)__popc(bal));
     base = __shfl_sync(0xffffffffu, base, leader);
     if (take) list[base + __popc(bal & ((1u << lane) - 1u))] = v;
+}
+
+// Adds one to a diagnostic counter for each lane that calls it, one atomic
+// per group of converged lanes (a shared address would otherwise serialise
+// every lane's increment).
+__device__ __forceinline__ void count_one(unsigned* c)
+{
+    const unsigned m = __activemask();
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(c, (unsigned)__popc(m));
+}
+
+// Adds v of each converged lane to a diagnostic counter, one atomic per group.
+__device__ __forceinline__ void count_add(unsigned* c, unsigned v)
+{
+    const unsigned m = __activemask();
+    const unsigned t = __reduce_add_sync(m, v);
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1) && t) atomicAdd(c, t);
 }
 
 // ---- integration -----------------------------------------------------------
@@ -723,7 +888,7 @@ __device__ __forceinline__ int exact_touch(const MixParams& P, const Master& M, 
     const long long band = 2 * Rq * P.guard_q;
     if (N > band) return 1;
     if (N < -band) return 0;
-    if (COUNT) atomicAdd(counters + CN_DECISIONS, 1u);
+    if (COUNT) count_one(counters + CN_DECISIONS);
     return fp64_cdist(M, i, j) > 0 ? 2 : 0;
 }
 
@@ -919,46 +1084,107 @@ __device__ __forceinline__ unsigned lower_bound_u(const unsigned* __restrict__ a
 
 __device__ __forceinline__ d3 tri_vertex(const double* v) { return mk(__ldg(v), __ldg(v + 1), __ldg(v + 2)); }
 
-// Per particle: the triangles of its cell within r + skin (FP64 closest point).
-__global__ void __launch_bounds__(256) k_tri_build(MixParams P, Master M, const unsigned* __restrict__ keys,
+// Squared distance from the origin to triangle abc in FP32 (the closest-point
+// regions of Ericson, Real-Time Collision Detection 5.1.5, with the query
+// point at the origin).  The distance is continuous across the regions, so a
+// region misjudged by rounding moves it by rounding only.  face: the closest
+// point is inside the face with every barycentric coordinate above 1e-5, far
+// beyond the FP32 rounding, so the FP64 region test of the reference takes its
+// face branch as well.
+__device__ __forceinline__ float tri_dist2_f(float ax, float ay, float az, float bx, float by, float bz, float cx,
+                                             float cy, float cz, bool& face)
+{
+    face = false;
+    const float abx = bx - ax, aby = by - ay, abz = bz - az;
+    const float acx = cx - ax, acy = cy - ay, acz = cz - az;
+    const float d1 = -(abx * ax + aby * ay + abz * az), d2 = -(acx * ax + acy * ay + acz * az);
+    if (d1 <= 0.f && d2 <= 0.f) return ax * ax + ay * ay + az * az;
+    const float d3 = -(abx * bx + aby * by + abz * bz), d4 = -(acx * bx + acy * by + acz * bz);
+    if (d3 >= 0.f && d4 <= d3) return bx * bx + by * by + bz * bz;
+    const float vc = d1 * d4 - d3 * d2;
+    float qx, qy, qz;
+    if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
+        const float v = d1 / (d1 - d3);
+        qx = ax + v * abx;
+        qy = ay + v * aby;
+        qz = az + v * abz;
+        return qx * qx + qy * qy + qz * qz;
+    }
+    const float d5 = -(abx * cx + aby * cy + abz * cz), d6 = -(acx * cx + acy * cy + acz * cz);
+    if (d6 >= 0.f && d5 <= d6) return cx * cx + cy * cy + cz * cz;
+    const float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
+        const float w = d2 / (d2 - d6);
+        qx = ax + w * acx;
+        qy = ay + w * acy;
+        qz = az + w * acz;
+        return qx * qx + qy * qy + qz * qz;
+    }
+    const float va = d3 * d6 - d5 * d4;
+    if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
+        const float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        qx = bx + w * (cx - bx);
+        qy = by + w * (cy - by);
+        qz = bz + w * (cz - bz);
+        return qx * qx + qy * qy + qz * qz;
+    }
+    const float den = 1.f / (va + vb + vc);
+    const float v = vb * den, w = vc * den;
+    face = va * den > 1e-5f && v > 1e-5f && w > 1e-5f;
+    qx = ax + v * abx + w * acx;
+    qy = ay + v * aby + w * acy;
+    qz = az + v * abz + w * acz;
+    return qx * qx + qy * qy + qz * qz;
+}
+
+// Per particle: the triangles of its cell within r + skin, in id order.  The
+// test is FP32 (vertices and centre relative to the grid origin, rounded
+// within about 1e-7 m) with a 1e-5 m margin: a list may hold a triangle just
+// out of reach (the contact pass decides each contact exactly), never miss
+// one within it.
+__global__ void __launch_bounds__(256) k_tri_build(MixParams P, const float4* __restrict__ pf,
+                                                   const unsigned* __restrict__ keys,
                                                    const unsigned* __restrict__ tpk,
                                                    const unsigned* __restrict__ tpt, unsigned cap,
-                                                   const xd_polygon_info* __restrict__ poly,
+                                                   const float* __restrict__ tri_ref,
                                                    const float4* __restrict__ tbound,
-                                                   unsigned* __restrict__ tcount, unsigned* __restrict__ tlist)
+                                                   unsigned* __restrict__ tcount, unsigned* __restrict__ tlist,
+                                                   unsigned* __restrict__ counters)
 {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const unsigned key = __ldg(keys + i);
     const unsigned b = lower_bound_u(tpk, cap, key), e = lower_bound_u(tpk, cap, key + 1u);
-    const d3 ip = mk(M.x[i], M.y[i], M.z[i]);
-    const float pr[3] = { (float)(ip.x - P.wo[0]), (float)(ip.y - P.wo[1]), (float)(ip.z - P.wo[2]) };
-    const double lim = M.r[i] + (double)(P.vcut);
+    const float4 p = __ldg(pf + i);
+    const float lim = p.w + P.vcut + 1e-5f;
     const unsigned n = P.n;
     unsigned c = 0;
     for (unsigned k = b; k < e; ++k) {
         const unsigned t = __ldg(tpt + k);
-        // the triangle's bounding sphere first: one farther than lim (by more
-        // than the FP32 error) holds no point within lim, and the FP64 closest
-        // point is skipped
+        // the triangle's bounding sphere first
         const float4 bs = __ldg(tbound + t);
-        const float sx = bs.x - pr[0], sy = bs.y - pr[1], sz = bs.z - pr[2];
-        if (sqrtf(sx * sx + sy * sy + sz * sz) - bs.w > (float)lim + 1e-5f) continue;
-        const xd_polygon_info* tri = poly + t;
-        const d3 cp = closest_pt_triangle(tri_vertex(tri->P), tri_vertex(tri->Q), tri_vertex(tri->R), ip);
-        if (length(ip - cp) < lim) {
-            if (c < kTriCap) tlist[(size_t)c * n + i] = t;
+        const float sx = bs.x - p.x, sy = bs.y - p.y, sz = bs.z - p.z;
+        if (sqrtf(sx * sx + sy * sy + sz * sz) - bs.w > lim) continue;
+        const float* v = tri_ref + 9 * (size_t)t;
+        bool face;
+        const float d2 = tri_dist2_f(__ldg(v) - p.x, __ldg(v + 1) - p.y, __ldg(v + 2) - p.z, __ldg(v + 3) - p.x,
+                                     __ldg(v + 4) - p.y, __ldg(v + 5) - p.z, __ldg(v + 6) - p.x,
+                                     __ldg(v + 7) - p.y, __ldg(v + 8) - p.z, face);
+        if (d2 < lim * lim || !(d2 < 3.0e38f)) {
+            if (c < P.tcap) tlist[(size_t)c * n + i] = t;
             ++c;
         }
     }
-    tcount[i] = c > kTriCap ? (kTriCap | kIncomplete) : c;
+    tcount[i] = c > P.tcap ? (P.tcap | kIncomplete) : c;
+    if (c > P.tcap) count_one(counters + CN_TINC);
+    count_add(counters + CN_TSUM, min(c, P.tcap));
 }
 
 // Verlet list build (steps that re-bin the cells), one thread per particle:
 // the nine neighbour rows' slot ranges, trimmed to the cells within reach,
 // are staged in shared memory and visited as one flattened loop (rows z then
 // y, slots ascending: the reference's order); every j with
-// |pj - pi| < ri + rj + vcut (FP32) is listed.  More than kVerletCap marks the
+// |pj - pi| < ri + rj + vcut (FP32) is listed.  More than P.vcap marks the
 // list incomplete (the contact pass then searches the cells).  Also records
 // the build positions for the skin test, each particle's planes in reach
 // (within r + skin), zero contact force, and the list of the particles with
@@ -1031,10 +1257,12 @@ __global__ void __launch_bounds__(256) k_mx_build(MixParams P, const float4* __r
             const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
             const float Rt = rt0 + pj.w;
             if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) >= Rt * Rt || j == i) continue;
-            if (nv < kVerletCap) vlist[(size_t)nv * n + i] = j;
+            if (nv < P.vcap) vlist[(size_t)nv * n + i] = j;
             ++nv;
         }
-        vcount[i] = nv > kVerletCap ? (kVerletCap | kIncomplete) : nv;
+        vcount[i] = nv > P.vcap ? (P.vcap | kIncomplete) : nv;
+        if (nv > P.vcap) count_one(counters + CN_VINC);
+        count_add(counters + CN_VSUM, min(nv, P.vcap));
         tri = P.ntri && __ldg(tcount + i) != 0u;
         heavy = nv > 0 || wm != 0u || tri;
     }
@@ -1068,7 +1296,34 @@ struct Own {
     float4 vh, vl;
     f3 w;
     float r, im;   // radius, 1/m
+    float wfloor;  // m g: the smallest force scale of the particle's contacts
 };
+
+// When an FP32 contact force term is re-formed in FP64.  The per-particle
+// force error is judged against max(sum_c |F_c|, m g); each contact's FP32
+// error is kept below kForceTol of its own scale max(|Fn|, m g), so that the
+// handful of contacts of a particle stay well inside the 2e-5 gate.
+//  * normal force: the FP32 terms carry about kTermErr of the largest term;
+//  * slip: the FP32 rotation term w x r u carries about kRotErr of its
+//    magnitude; below the Coulomb cap the tangential force moves by
+//    (ks dt + vs) times that, at the cap its direction turns by that over |e|.
+constexpr float kForceTol = 2e-6f;
+constexpr float kTermErr = 5e-7f;
+constexpr float kRotErr = 7e-7f;
+
+__device__ __forceinline__ bool normal_needs_fp64(float term_max, float fn_abs, float wfloor)
+{
+    return kTermErr * term_max > kForceTol * fmaxf(fn_abs, wfloor);
+}
+
+__device__ __forceinline__ bool slip_needs_fp64(float wt2, float ee, float lin, float mu, float fn_abs, float wfloor)
+{
+    if (!(wt2 > 0.f)) return false;
+    const float wt = sqrtf(wt2), me = sqrtf(ee);
+    const float scale = kForceTol * fmaxf(fn_abs, wfloor);
+    if (lin * me >= mu * fn_abs) return kRotErr * wt * mu * fn_abs > scale * me;   // at the cap
+    return kRotErr * wt * lin > scale;
+}
 
 // The force of one contact (i, j).  getConstant TCM = 1 (impl:238-246) and
 // DHSModel (impl:379-401) in FP32: the overlap from the exact integer
@@ -1117,29 +1372,10 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     const f3 rv = dv + wterm;
     // rv . u = dv . u (the rotation term is perpendicular to u), in double-float
     const int dqi[3] = { (int)ddx, (int)ddy, (int)ddz };
-    const float rvu = normal_speed(dvs, dvt, dqi, dn, D2);
+    float rq0, rq1, rqc;
+    const float rvu = normal_speed(dvs, dvt, dqi, dn, D2, rq0, rq1, rqc);
     f3 ev = rv - rvu * u;
     float ee = fdot(ev, ev);
-    if (ee < 0.0025f * fdot(wterm, wterm)) {
-        // rolling: the rotation term cancels most of the slip; form the slip in
-        // FP64 (FP32 rounding of the terms would dominate)
-        atomicAdd(counters + CN_SLIPS, 1u);
-        const double dd = sqrt((double)D2);
-        const double ux = (double)ddx / dd, uy = (double)ddy / dd, uz = (double)ddz / dd;
-        const double ri = __ldg(M.r + i), rj = __ldg(M.r + j);
-        const float4 wil = __ldg(M.wl + i), wjl = __ldg(M.wl + j);
-        const double wix = df_to_d(I.w.x, wil.x), wiy = df_to_d(I.w.y, wil.y), wiz = df_to_d(I.w.z, wil.z);
-        const double wjx = df_to_d(wj.x, wjl.x), wjy = df_to_d(wj.y, wjl.y), wjz = df_to_d(wj.z, wjl.z);
-        const double dvx = (double)dvs[0] + (double)dvt[0];
-        const double dvy = (double)dvs[1] + (double)dvt[1];
-        const double dvz = (double)dvs[2] + (double)dvt[2];
-        const double rx = dvx - rj * (wjy * uz - wjz * uy) - ri * (wiy * uz - wiz * uy);
-        const double ry = dvy - rj * (wjz * ux - wjx * uz) - ri * (wiz * ux - wix * uz);
-        const double rz = dvz - rj * (wjx * uy - wjy * ux) - ri * (wix * uy - wiy * ux);
-        const double ru = rx * ux + ry * uy + rz * uz;
-        ev = fk((float)(rx - ru * ux), (float)(ry - ru * uy), (float)(rz - ru * uz));
-        ee = fdot(ev, ev);
-    }
     // getConstant, TCM = 1 (impl:238-246)
     const float Meq = 1.0f / (I.im + jim);   // m_i m_j / (m_i + m_j)
     const float Req = (ir * jr) / (ir + jr);
@@ -1156,39 +1392,39 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
         fca = P.coh * (3.14159265358979f * rc * rc);
     }
     float fn = fsn + fca + fdn;
-    if (fabsf(fn) < 0.03f * fmaxf(fmaxf(fabsf(fsn), fabsf(fdn)), fca)) {
-        // The elastic, cohesive and damping terms nearly cancel (the normal
-        // force of an unloading contact crossing zero): FP32 rounding of each
-        // term would dominate the small sum, so it is formed in FP64, with
-        // the overlap and normal from the FP64 positions.
-        atomicAdd(counters + CN_NORMALS, 1u);
-        const double px = __ldg(M.x + j) - __ldg(M.x + i);
-        const double py = __ldg(M.y + j) - __ldg(M.y + i);
-        const double pz = __ldg(M.z + j) - __ldg(M.z + i);
-        const double dd = sqrt(px * px + py * py + pz * pz);
-        const double ux = px / dd, uy = py / dd, uz = pz / dd;
-        const double dl = fp64_cdist(M, i, j);
-        const double ri = __ldg(M.r + i), rj = __ldg(M.r + j);
-        const float4 wil = __ldg(M.wl + i), wjl = __ldg(M.wl + j);
-        const double mi = __ldg(mass0 + __float_as_uint(wil.w)), mj = __ldg(mass0 + __float_as_uint(wjl.w));
-        const double wix = df_to_d(I.w.x, wil.x), wiy = df_to_d(I.w.y, wil.y), wiz = df_to_d(I.w.z, wil.z);
-        const double wjx = df_to_d(wj.x, wjl.x), wjy = df_to_d(wj.y, wjl.y), wjz = df_to_d(wj.z, wjl.z);
-        const double dvx = (double)dvs[0] + (double)dvt[0];
-        const double dvy = (double)dvs[1] + (double)dvt[1];
-        const double dvz = (double)dvs[2] + (double)dvt[2];
-        const double rvx = dvx - rj * (wjy * uz - wjz * uy) - ri * (wiy * uz - wiz * uy);
-        const double rvy = dvy - rj * (wjz * ux - wjx * uz) - ri * (wiz * ux - wix * uz);
-        const double rvz = dvz - rj * (wjx * uy - wjy * ux) - ri * (wix * uy - wiy * ux);
-        const double Meqd = (mi * mj) / (mi + mj), Reqd = (ri * rj) / (ri + rj);
-        const double knd = P.c43Eeq_d * sqrt(Reqd);
-        const double vnd = sqrt((4.0 * Meqd * knd) / P.one_b2_d);
-        const double fsnd = -knd * (dl * sqrt(dl));
-        double fcad = 0.0;
-        if (P.coh_d != 0.0) {
+    if (normal_needs_fp64(fmaxf(fmaxf(fabsf(fsn), fabsf(fdn)), fca), fabsf(fn), I.wfloor)) {
+        // The elastic, (cohesive) and damping terms nearly cancel (the
+        // normal force of an unloading contact crossing zero): FP32 rounding
+        // of each term would dominate the small sum, so it is formed again
+        // in pair arithmetic (in FP64 with cohesion), with the overlap from
+        // the FP64 positions.
+        count_one(counters + CN_NORMALS);
+        const unsigned idi = __float_as_uint(__ldg(M.wl + i).w), idj = __float_as_uint(__ldg(M.wl + j).w);
+        if (P.coh == 0.f) {
+            fn = normal_pair(P, M, mass0, i, j, idi, idj, rq0, rq1);
+        } else {
+            const double dl = fp64_cdist(M, i, j);
+            const double ri = __ldg(M.r + i), rj = __ldg(M.r + j);
+            const double mi = __ldg(mass0 + idi), mj = __ldg(mass0 + idj);
+            const double Meqd = (mi * mj) / (mi + mj), Reqd = (ri * rj) / (ri + rj);
+            const double knd = P.c43Eeq_d * sqrt(Reqd);
+            const double vnd = sqrt((4.0 * Meqd * knd) / P.one_b2_d);
+            const double fsnd = -knd * (dl * sqrt(dl));
             const double rc = pow((3.0 * Reqd * (-fsnd)) / (4.0 * (1.0 / P.coh_eeq_d)), 1.0 / 3.0);
-            fcad = P.coh_d * (M_PI * rc * rc);
+            const double fcad = P.coh_d * (M_PI * rc * rc);
+            // rv . u = dv . u (the rotation term is perpendicular to u)
+            fn = (float)(fsnd + fcad + vnd * ((double)rq0 + (double)rq1));
         }
-        fn = (float)(fsnd + fcad + vnd * (rvx * ux + rvy * uy + rvz * uz));
+    }
+    // The slip in FP64 where the FP32 rounding of the rotation term (about
+    // kRotErr of |w x r|) could move the tangential force by more than
+    // kForceTol of the contact's force scale max(|Fn|, m_i g): a sliding
+    // contact (Coulomb cap) whose slip nearly cancels, or a fast spin.
+    if (P.rolling && slip_needs_fp64(fdot(wterm, wterm), ee, ks * dt + vs, P.fric, fabsf(fn), I.wfloor)) {
+        count_one(counters + CN_SLIPS);
+        ev = slip_pair(dvs, dvt, dqi, dn, rqc, rq0, rq1, I.qb.y, qbj.y, make_float4(I.w.x, I.w.y, I.w.z, 0.f),
+                       __ldg(M.wl + i), wj4, __ldg(M.wl + j));
+        ee = fdot(ev, ev);
     }
     const f3 Fn = fn * u;
     if (HIST) {
@@ -1230,56 +1466,7 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
 // plane_contact_force_kernel<1> (impl:572-621) for the planes in reach, in
 // FP64, in plane order (the others are out of reach and add exactly zero).
 // Block 0 clears CN_REBUILD for the next step's skin test.
-constexpr unsigned kContactThreads = 64;
-constexpr unsigned kContactBlocks = 152 * 8;
 
-// Squared distance from the origin to triangle abc in FP32 (the closest-point
-// regions of Ericson, Real-Time Collision Detection 5.1.5, with the query
-// point at the origin).  A pre-test only: the distance is continuous across
-// the regions, so a region misjudged by rounding moves it by rounding only.
-__device__ __forceinline__ float tri_dist2_f(float ax, float ay, float az, float bx, float by, float bz, float cx,
-                                             float cy, float cz)
-{
-    const float abx = bx - ax, aby = by - ay, abz = bz - az;
-    const float acx = cx - ax, acy = cy - ay, acz = cz - az;
-    const float d1 = -(abx * ax + aby * ay + abz * az), d2 = -(acx * ax + acy * ay + acz * az);
-    if (d1 <= 0.f && d2 <= 0.f) return ax * ax + ay * ay + az * az;
-    const float d3 = -(abx * bx + aby * by + abz * bz), d4 = -(acx * bx + acy * by + acz * bz);
-    if (d3 >= 0.f && d4 <= d3) return bx * bx + by * by + bz * bz;
-    const float vc = d1 * d4 - d3 * d2;
-    float qx, qy, qz;
-    if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
-        const float v = d1 / (d1 - d3);
-        qx = ax + v * abx;
-        qy = ay + v * aby;
-        qz = az + v * abz;
-        return qx * qx + qy * qy + qz * qz;
-    }
-    const float d5 = -(abx * cx + aby * cy + abz * cz), d6 = -(acx * cx + acy * cy + acz * cz);
-    if (d6 >= 0.f && d5 <= d6) return cx * cx + cy * cy + cz * cz;
-    const float vb = d5 * d2 - d1 * d6;
-    if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
-        const float w = d2 / (d2 - d6);
-        qx = ax + w * acx;
-        qy = ay + w * acy;
-        qz = az + w * acz;
-        return qx * qx + qy * qy + qz * qz;
-    }
-    const float va = d3 * d6 - d5 * d4;
-    if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
-        const float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
-        qx = bx + w * (cx - bx);
-        qy = by + w * (cy - by);
-        qz = bz + w * (cz - bz);
-        return qx * qx + qy * qy + qz * qz;
-    }
-    const float den = 1.f / (va + vb + vc);
-    const float v = vb * den, w = vc * den;
-    qx = ax + v * abx + w * acx;
-    qy = ay + v * aby + w * acy;
-    qz = az + v * abz + w * acz;
-    return qx * qx + qy * qy + qz * qz;
-}
 
 // Entry t of the listed particles: the ones with triangles in reach fill the
 // list from the front (front of them), the others from the end.
@@ -1301,8 +1488,10 @@ struct ContactArgs {
     const unsigned* hlist;
     const unsigned short* wmask;
     const xd_plane_info* planes;
+    const PlaneRec* prec;
     const double* mass0;
     const xd_polygon_info* poly;
+    const TriRec* trec;
     const xd_polygon_mass_info* pmi;
     const unsigned* tcount;
     const unsigned* tlist;
@@ -1319,6 +1508,219 @@ struct ContactArgs {
     HistTable ht;
     int rxn_on;
 };
+
+// ---- wall contacts in FP32 ------------------------------------------------
+
+// Metres: a wall contact whose FP64 plane distance is within this of touching
+// is decided by the reference's FP64 region test (the plane distance and the
+// reference's closest-point chain differ by a few 1e-16 m).
+constexpr double kWallGuard = 1e-13;
+
+// One wall contact's force: DHSModel (impl:379-401) with Req = r, Meq = m and
+// no particle moment, as the plane and polygon kernels call it (ir = 0).
+// cd: the overlap (FP64), u: the unit normal (FP64), dvd: the relative
+// velocity without the particle's rotation term, in FP64 (wall velocity
+// minus the particle's); the rotation term -(w x r u) is added in FP32 (it
+// is perpendicular to u, so the normal speed dv . u is dvd . u, formed in
+// FP64: a sliding sphere's dv is nearly perpendicular to u).  Ft is in/out:
+// the polygon kernel keeps it across triangles when a slip is exactly zero.
+// The normal force and the rolling slip are formed again in FP64 when their
+// FP32 terms nearly cancel, as for particle pairs.
+struct WallK {
+    float kn, vn, ks, vs, mu;
+    const double* c43Eeq;   // getConstant's FP64 terms (for the rechecks)
+    const double* one_b2;
+};
+
+__device__ __forceinline__ WallK wall_constants(const double* c43Eeq, const double* one_b2, double sratio,
+                                                double fric, float rf, float mf)
+{
+    WallK k;
+    k.kn = (float)*c43Eeq * sqrtf(rf);
+    k.vn = sqrtf((4.0f * mf * k.kn) / (float)*one_b2);
+    k.ks = k.kn * (float)sratio;
+    k.vs = k.vn * (float)sratio;
+    k.mu = (float)fric;
+    k.c43Eeq = c43Eeq;
+    k.one_b2 = one_b2;
+    return k;
+}
+
+__device__ __forceinline__ f3 wall_force(const MixParams& P, const WallK& k, double cd, d3 u, d3 dvd, double r,
+                                         double m, float rf, float wfloor, const float4& wh, const float4& wl,
+                                         unsigned* __restrict__ counters, f3& Ft)
+{
+    const float df = (float)cd;
+    const f3 uf = fk((float)u.x, (float)u.y, (float)u.z);
+    const double rvu_d = dvd.x * u.x + dvd.y * u.y + dvd.z * u.z;
+    const float rvu = (float)rvu_d;
+    const f3 wterm = P.rolling ? fcross(fk(wh.x, wh.y, wh.z), (-rf) * uf) : fk(0.f, 0.f, 0.f);
+    const f3 dvf = fk((float)dvd.x, (float)dvd.y, (float)dvd.z) + wterm;
+    f3 ev = dvf - rvu * uf;
+    float ee = fdot(ev, ev);
+    const float fsn = -k.kn * (df * sqrtf(df));
+    const float fdn = k.vn * rvu;
+    float fn = fsn + fdn;
+    if (normal_needs_fp64(fmaxf(fabsf(fsn), fabsf(fdn)), fabsf(fn), wfloor)) {
+        // the terms nearly cancel: formed again in pair arithmetic
+        count_one(counters + CN_NORMALS);
+        const dfl R = d_to_df(r), D = d_to_df(cd);
+        const dfl kn = df_mul(d_to_df(*k.c43Eeq), df_sqrt(R));
+        const dfl vn = df_sqrt(df_div(df_mul(df_mul(dfl{ 4.f, 0.f }, d_to_df(m)), kn), d_to_df(*k.one_b2)));
+        const dfl f = df_add(df_neg(df_mul(kn, df_mul(D, df_sqrt(D)))), df_mul(vn, d_to_df(rvu_d)));
+        fn = __fadd_rn(f.hi, f.lo);
+    }
+    if (P.rolling && slip_needs_fp64(fdot(wterm, wterm), ee, k.ks * P.dtf + k.vs, k.mu, fabsf(fn), wfloor)) {
+        // the rotation term cancels most of the slip
+        count_one(counters + CN_SLIPS);
+        const d3 iw = mk(df_to_d(wh.x, wl.x), df_to_d(wh.y, wl.y), df_to_d(wh.z, wl.z));
+        const d3 dv = dvd - cross(iw, r * u);
+        const double dn = dot(dv, u);
+        ev = fk((float)(dv.x - dn * u.x), (float)(dv.y - dn * u.y), (float)(dv.z - dn * u.z));
+        ee = fdot(ev, ev);
+    }
+    const float mag_e = sqrtf(ee);
+    if (mag_e != 0.f) {
+        // dv . s = |e| (s the unit slip direction)
+        Ft = fminf(k.ks * (mag_e * P.dtf) + k.vs * mag_e, k.mu * fabsf(fn)) * ((1.0f / mag_e) * ev);
+    }
+    return fn * uf + Ft;
+}
+
+// The wall contacts of listed particle i (the reference's DHS model, no
+// history): its planes in reach (plane_contact_force_kernel<1>,
+// impl:572-621; each plane starts from Ft = 0, as each is its own launch
+// there), then its triangles (particle_polygonObject_collision_kernel<1>,
+// impl:923-1021; Ft kept across triangles, the normal from the face winding,
+// the wall velocity of the body at the contact point, the reaction summed per
+// particle into rxn).  A contact whose closest point is clearly inside the
+// face in the FP32 region test (relative to the sphere centre) is found by
+// one FP64 plane distance; every other contact, and any within kWallGuard of
+// touching, by the reference's FP64 region test, rounded per operation, so
+// every contact decision is the reference's.  The forces are FP32
+// (wall_force).
+__device__ __forceinline__ f3 walls_fp32(const MixParams& P, const ContactArgs& C, const unsigned i, const float4 pi,
+                                      const unsigned wm, const unsigned tc)
+{
+    const Master& M = C.M;
+    unsigned* __restrict__ counters = C.counters;
+    const float4 vh = __ldg(M.vh + i), vl = __ldg(M.vl + i), wh = __ldg(M.wh + i), wl = __ldg(M.wl + i);
+    const double m = __ldg(C.mass0 + __float_as_uint(wl.w));
+    const float mf = (float)m;
+    const float wfloor = mf * sqrtf(P.gf[0] * P.gf[0] + P.gf[1] * P.gf[1] + P.gf[2] * P.gf[2]);
+    const d3 ip = mk(__ldg(M.x + i), __ldg(M.y + i), __ldg(M.z + i));
+    const double r = __ldg(M.r + i);
+    const float rf = pi.w;
+    const d3 iv = mk(df_to_d(vh.x, vl.x), df_to_d(vh.y, vl.y), df_to_d(vh.z, vl.z));
+    f3 f = fk(0.f, 0.f, 0.f);
+    for (unsigned mask = wm; mask; mask &= mask - 1u) {
+        const int w = __ffs(mask) - 1;
+        const PlaneRec* pr = C.prec + w;
+        const d3 dp = ip - mk(__ldg(pr->xw), __ldg(pr->xw + 1), __ldg(pr->xw + 2));
+        const float dx = (float)dp.x, dy = (float)dp.y, dz = (float)dp.z;
+        const float wx = dx * __ldg(pr->u1) + dy * __ldg(pr->u1 + 1) + dz * __ldg(pr->u1 + 2);
+        const float wy = dx * __ldg(pr->u2) + dy * __ldg(pr->u2 + 1) + dz * __ldg(pr->u2 + 2);
+        const float l1 = __ldg(&pr->l1), l2 = __ldg(&pr->l2);
+        const float mg = 1e-6f * (fabsf(dx) + fabsf(dy) + fabsf(dz) + l1 + l2);
+        double cd = -1.0;
+        d3 unit;
+        bool exact = true;
+        if (wx > mg && wx < l1 - mg && wy > mg && wy < l2 - mg) {
+            // inside the rectangle: the face region (impl:557-560)
+            const d3 n = mk(__ldg(pr->n), __ldg(pr->n + 1), __ldg(pr->n + 2));
+            const double h = dp.x * n.x + dp.y * n.y + dp.z * n.z;
+            cd = r - fabs(h);
+            if (cd < -kWallGuard) continue;
+            if (cd > kWallGuard && fabs(h) > 1e-12) {
+                exact = false;
+                unit = h < 0.0 ? n : -n;
+            }
+        }
+        if (exact) {
+            count_one(counters + CN_WALLS);
+            const PlaneD pe = load_plane(C.planes + w);
+            cd = plane_detection(pe, ip, plane_coords(pe, ip), unit, r);
+            if (!(cd > 0)) continue;
+        }
+        const WallK k = wall_constants(P.pl_c43Eeq + w, P.pl_one_b2 + w, P.pl_sratio[w], P.pl_fric[w], rf, mf);
+        f3 Ft = fk(0.f, 0.f, 0.f);
+        f = f + wall_force(P, k, cd, unit, -iv, r, m, rf, wfloor, wh, wl, counters, Ft);
+    }
+    if (tc) {
+        const unsigned n = P.n;
+        const bool listed = !(tc & kIncomplete);
+        unsigned kb = 0, ke = tc;
+        if (!listed) {
+            const unsigned key = __ldg(C.keys + i);
+            kb = lower_bound_u(C.tpk, C.tcap, key);
+            ke = lower_bound_u(C.tpk, C.tcap, key + 1u);
+        }
+        f3 Ft = fk(0.f, 0.f, 0.f);
+        unsigned cb = 0xffffffffu;
+        WallK k;
+        for (unsigned kk = kb; kk < ke; ++kk) {
+            const unsigned t = listed ? __ldg(C.tlist + (size_t)kk * n + i) : __ldg(C.tpt + kk);
+            const TriRec* tr = C.trec + t;
+            const d3 sp = ip - mk(__ldg(tr->p), __ldg(tr->p + 1), __ldg(tr->p + 2));   // x - P
+            const float sx = (float)sp.x, sy = (float)sp.y, sz = (float)sp.z;
+            const float qx = __ldg(tr->q) - sx, qy = __ldg(tr->q + 1) - sy, qz = __ldg(tr->q + 2) - sz;
+            const float cx = __ldg(tr->r) - sx, cy = __ldg(tr->r + 1) - sy, cz = __ldg(tr->r + 2) - sz;
+            bool face;
+            const float d2f = tri_dist2_f(-sx, -sy, -sz, qx, qy, qz, cx, cy, cz, face);
+            {
+                // out of reach by more than the FP32 error: no contact in FP64 either
+                const float span = fabsf(sx) + fabsf(sy) + fabsf(sz) + fabsf(qx) + fabsf(qy) + fabsf(qz) +
+                                   fabsf(cx) + fabsf(cy) + fabsf(cz);
+                const float lim = rf + 1e-6f + 1e-5f * span;
+                if (d2f > lim * lim && d2f < 3.0e38f) continue;
+            }
+            const d3 u = mk(__ldg(tr->n), __ldg(tr->n + 1), __ldg(tr->n + 2));
+            double cd = -1.0;
+            d3 cpt;
+            bool exact = true;
+            if (face) {
+                const double h = sp.x * u.x + sp.y * u.y + sp.z * u.z;   // n . (x - P)
+                cd = r - fabs(h);
+                if (cd < -kWallGuard) continue;
+                if (cd > kWallGuard) {
+                    exact = false;
+                    cpt = ip - h * u;
+                }
+            }
+            if (exact) {
+                count_one(counters + CN_WALLS);
+                const xd_polygon_info* tri = C.poly + t;
+                cpt = closest_pt_triangle(tri_vertex(tri->P), tri_vertex(tri->Q), tri_vertex(tri->R), ip);
+                cd = rn::sub(r, rn::length(rn::sub(ip, cpt)));
+                if (!(cd > 0)) continue;
+            }
+            const unsigned b = __ldg(&tr->body);
+            if (b != cb) {
+                // getConstant with the body's hoisted material terms (Meq = m,
+                // Req = r): the same for every triangle of the body
+                k = wall_constants(P.pb_c43Eeq + b, P.pb_one_b2 + b, P.pb_sratio[b], P.pb_fric[b], rf, mf);
+                cb = b;
+            }
+            const xd_polygon_mass_info* body = C.pmi + b;
+            const d3 po2cp = cpt - tri_vertex(body->origin);
+            const d3 pvel = tri_vertex(body->vel);
+            const d3 dvd = P.rolling ? (pvel + cross(tri_vertex(body->omega), po2cp)) - iv : pvel - iv;
+            const f3 fc = wall_force(P, k, cd, u, dvd, r, m, rf, wfloor, wh, wl, counters, Ft);
+            f = f + fc;
+            if (C.rxn_on) {
+                const f3 rm = fcross(fc, fk((float)po2cp.x, (float)po2cp.y, (float)po2cp.z));   // -(po2cp x fc)
+                double* rb = C.rxn + (size_t)b * 6 * n + i;
+                rb[0] -= (double)fc.x;
+                rb[n] -= (double)fc.y;
+                rb[2 * (size_t)n] -= (double)fc.z;
+                rb[3 * (size_t)n] += (double)rm.x;
+                rb[4 * (size_t)n] += (double)rm.y;
+                rb[5 * (size_t)n] += (double)rm.z;
+            }
+        }
+    }
+    return f;
+}
 
 // The contact pass of one listed particle (slot i): its Verlet-list pairs,
 // planes and triangles, summed in a fixed order into Fc/Mc.
@@ -1375,6 +1777,7 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
             const float4 w4 = __ldg(M.wh + i);
             I.w = fk(w4.x, w4.y, w4.z);
             I.im = I.vh.w;
+            I.wfloor = sqrtf(P.gf[0] * P.gf[0] + P.gf[1] * P.gf[1] + P.gf[2] * P.gf[2]) / I.im;
             have_v = true;
         }
         contact_force<HIST>(P, M, I, j, guard, mass0, pf, qa, qb, counters, A, ht, hs);
@@ -1412,6 +1815,19 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
         const float hz = (pi.x - P.pxw[w][0]) * P.pun[w][0] + (pi.y - P.pxw[w][1]) * P.pun[w][1] +
                          (pi.z - P.pxw[w][2]) * P.pun[w][2];
         if (!(fabsf(hz) < pi.w + P.tol)) wm &= ~(1u << w);
+    }
+    if (HIST == 0) {
+        const unsigned tc0 = P.ntri ? __ldg(tcount + i) : 0u;
+        if (wm || tc0) {
+            const f3 fw = walls_fp32(P, C, i, pi, wm, tc0);
+            F.x += fw.x;
+            F.y += fw.y;
+            F.z += fw.z;
+        }
+        Fc[i] = F;
+        Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
+        if (RECORD) rec_count[i] = nc;
+        return;
     }
     if (wm) {
         const float4 vh = __ldg(M.vh + i), vl = __ldg(M.vl + i);
@@ -1496,7 +1912,8 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
                 const float ax = (float)(Pv.x - ip.x), ay = (float)(Pv.y - ip.y), az = (float)(Pv.z - ip.z);
                 const float bx = (float)(Qv.x - ip.x), by = (float)(Qv.y - ip.y), bz = (float)(Qv.z - ip.z);
                 const float cx = (float)(Rv.x - ip.x), cy = (float)(Rv.y - ip.y), cz = (float)(Rv.z - ip.z);
-                const float d2f = tri_dist2_f(ax, ay, az, bx, by, bz, cx, cy, cz);
+                bool face;
+                const float d2f = tri_dist2_f(ax, ay, az, bx, by, bz, cx, cy, cz, face);
                 const float span = fabsf(ax) + fabsf(ay) + fabsf(az) + fabsf(bx) + fabsf(by) + fabsf(bz) + fabsf(cx) +
                                    fabsf(cy) + fabsf(cz);
                 const float lim = (float)r + 1e-6f + 1e-5f * span;
@@ -1557,7 +1974,7 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
 }
 
 template <bool RECORD, int HIST>
-__global__ void __launch_bounds__(kContactThreads) k_mx_contact(MixParams P, ContactArgs C)
+__global__ void __launch_bounds__(kContactMaxThreads) k_mx_contact(MixParams P, ContactArgs C)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) C.counters[CN_REBUILD] = 0;
     const unsigned total = C.counters[CN_HEAVY], front = C.counters[CN_HTRI];
@@ -1736,6 +2153,29 @@ __global__ void __launch_bounds__(256) k_mx_ids(MixParams P, Master M, unsigned*
 
 }  // namespace
 
+__global__ void k_plane_recs(const xd_plane_info* __restrict__ planes, unsigned nplanes, PlaneRec* __restrict__ out)
+{
+    const unsigned w = threadIdx.x;
+    if (w >= nplanes) return;
+    const PlaneD pe = load_plane(planes + w);
+    const d3 uu = rn::divs(pe.uw, rn::length(pe.uw));
+    PlaneRec r;
+    r.xw[0] = pe.xw.x; r.xw[1] = pe.xw.y; r.xw[2] = pe.xw.z;
+    r.n[0] = uu.x; r.n[1] = uu.y; r.n[2] = uu.z;
+    r.u1[0] = (float)pe.u1.x; r.u1[1] = (float)pe.u1.y; r.u1[2] = (float)pe.u1.z;
+    r.u2[0] = (float)pe.u2.x; r.u2[1] = (float)pe.u2.y; r.u2[2] = (float)pe.u2.z;
+    r.l1 = (float)pe.l1;
+    r.l2 = (float)pe.l2;
+    out[w] = r;
+}
+
+static int launch_plane_recs(const xd_plane_info* planes, unsigned nplanes, PlaneRec* out, cudaStream_t q)
+{
+    if (!nplanes) return XD_OK;
+    k_plane_recs<<<1, 32, 0, q>>>(planes, nplanes, out);
+    return launch_status("plane records");
+}
+
 // ------------------------------------------------------------------ host
 
 static void plane_prefilter(MixParams& P, const xd_plane_info* planes, unsigned nplanes);
@@ -1795,7 +2235,7 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     // error of the FP32 position estimates that place particles (a few ulp of
     // the extent): two touching particles, each within half the skin of its
     // assigned cell, always have neighbouring assigned cells.
-    const double skin = 0.1 * rmax;
+    const double skin = (double)s->skin_factor * rmax;
     s->cs = 2.0 * rmax * 1.001 + skin + extent * 0x1p-19;
     double margin = 2.0 * s->cs;
     int g[3];
@@ -1851,6 +2291,8 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     P.one_b2_d = 1.0 + beta * beta;
     P.c43Eeq = (float)P.c43Eeq_d;
     P.one_b2 = (float)P.one_b2_d;
+    P.c43Eeq_p = df_split(P.c43Eeq_d);
+    P.one_b2_p = df_split(P.one_b2_d);
     P.sratio = (float)cp.sratio;
     P.fric = (float)cp.fric;
     P.coh_d = cp.coh;
@@ -1862,6 +2304,8 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     P.rolling = d.params.rollingCondition ? 1 : 0;
     P.ntri = d.ntri;
     P.nbodies = d.ntri ? d.nbodies : 0;
+    P.vcap = s->vcap;
+    P.tcap = s->tcap;
     // a particle within r + skin of a triangle has its centre within this of
     // the triangle's bounding box
     P.tri_reach = (float)(rmax + skin) + 2.0f * P.tol;
@@ -1912,7 +2356,7 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     A(alloc(s, &s->hlist, n));
     A(alloc(s, &s->wmask, n));
     A(alloc(s, &s->vcount, n));
-    A(alloc(s, &s->vlist, n * kVerletCap));
+    A(alloc(s, &s->vlist, n * s->vcap));
     A(alloc(s, &s->pref, n));
     A(alloc(s, &s->keys, n));
     A(alloc(s, &s->vals, n));
@@ -1924,12 +2368,15 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     A(alloc(s, &scr, radix_sort_scratch_bytes((unsigned)n)));
     s->sort_scratch = scr;
     A(alloc(s, &s->planes, s->nplanes));
+    A(alloc(s, &s->prec, s->nplanes));
     A(alloc(s, &s->cps, s->nplanes));
     A(alloc(s, &s->counters, kCounters));
     s->passes = (key_bits_for(s->ncell) + 7) / 8;
     if (st == XD_OK) A(cuda_status(cudaMemset(s->counters, 0, sizeof(unsigned) * kCounters), "mixed counters"));
     if (st == XD_OK && s->nplanes) {
         A(cuda_status(cudaMemcpy(s->planes, d.planes, sizeof(xd_plane_info) * s->nplanes, cudaMemcpyHostToDevice), "mixed planes"));
+        A(launch_plane_recs(s->planes, s->nplanes, s->prec, 0));
+        A(cuda_status(cudaStreamSynchronize(0), "mixed planes"));
         A(cuda_status(cudaMemcpy(s->cps, d.cp_planes, sizeof(xd_contact_property) * s->nplanes, cudaMemcpyHostToDevice), "mixed planes"));
     }
     if (st == XD_OK && d.ntri) {
@@ -1950,6 +2397,7 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
         A(alloc(s, &s->pmi, s->nbodies));
         A(alloc(s, &s->tri_ref, 9 * (size_t)s->ntri));
         A(alloc(s, &s->tbound, (size_t)s->ntri));
+        A(alloc(s, &s->trec, (size_t)s->ntri));
         A(alloc(s, &s->tcells, (size_t)s->ntri + 1));
         A(alloc(s, &s->tpk, s->tpair_cap));
         A(alloc(s, &s->tpt, s->tpair_cap));
@@ -1957,7 +2405,7 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
         A(alloc(s, &tscr, radix_sort_scratch_bytes(s->tpair_cap)));
         s->tsort_scratch = tscr;
         A(alloc(s, &s->tcount, n));
-        A(alloc(s, &s->tlist, n * kTriCap));
+        A(alloc(s, &s->tlist, n * s->tcap));
         A(alloc(s, &s->rxn, (size_t)6 * s->nbodies * n));
         A(alloc(s, &s->rxn_part, (size_t)6 * s->nbodies * kRxnBlocks));
         if (st == XD_OK) {
@@ -1965,6 +2413,8 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
             A(cuda_status(cudaMemcpy(s->sphere, d.sphere, sizeof(double) * 4 * s->ntri, cudaMemcpyHostToDevice), "mixed mesh"));
             A(cuda_status(cudaMemcpy(s->vlist_body, d.vlist, sizeof(double) * 9 * s->ntri, cudaMemcpyHostToDevice), "mixed mesh"));
             A(cuda_status(cudaMemcpy(s->pmi, d.pmi, sizeof(xd_polygon_mass_info) * s->nbodies, cudaMemcpyHostToDevice), "mixed mesh"));
+            A(launch_tri_records(s->poly, s->ntri, s->trec, 0));
+            A(cuda_status(cudaStreamSynchronize(0), "mixed mesh"));
         }
     }
     return st;
@@ -2266,6 +2716,8 @@ static int rebuild(MixedScene* s, cudaStream_t q)
     st = cuda_status(cudaMemsetAsync(s->counters + CN_GAPS, 0, 2 * sizeof(unsigned), q), "mixed re-binning");
     if (st == XD_OK)
         st = cuda_status(cudaMemsetAsync(s->counters + CN_HTRI, 0, 2 * sizeof(unsigned), q), "mixed re-binning");
+    if (st == XD_OK)
+        st = cuda_status(cudaMemsetAsync(s->counters + CN_VINC, 0, 4 * sizeof(unsigned), q), "mixed re-binning");
     if (st != XD_OK) return st;
     k_mx_keys<<<blocks(n, 256), 256, 0, q>>>(s->P, s->pf, s->keys, s->vals);
     st = launch_status("mixed keys");
@@ -2296,8 +2748,8 @@ static int rebuild(MixedScene* s, cudaStream_t q)
         if (st != XD_OK) return st;
         s->tpk_sorted = tk;
         s->tpt_sorted = tt;
-        k_tri_build<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[0], s->prev_keys, tk, tt, cap, s->poly, s->tbound,
-                                                   s->tcount, s->tlist);
+        k_tri_build<<<blocks(n, 256), 256, 0, q>>>(s->P, s->pf, s->prev_keys, tk, tt, cap, s->tri_ref, s->tbound,
+                                                   s->tcount, s->tlist, s->counters);
         st = launch_status("mixed triangle lists");
     }
     if (st != XD_OK) return st;
@@ -2314,7 +2766,7 @@ static int update_mesh(MixedScene* s, cudaStream_t q)
 {
     if (!s->ntri || !s->bodies_dirty) return XD_OK;
     const int st = launch_mesh_move(s->pmi, s->vlist_body, s->sphere, s->poly, s->ntri, s->tri_ref, s->P.wo,
-                                    s->P.disp2, s->counters + CN_REBUILD, q);
+                                    s->P.disp2, s->counters + CN_REBUILD, s->trec, q);
     if (st == XD_OK) s->bodies_dirty = false;
     return st;
 }
@@ -2373,8 +2825,10 @@ static ContactArgs contact_args(MixedScene* s, unsigned* rc, unsigned* rp, unsig
     C.hlist = s->hlist;
     C.wmask = s->wmask;
     C.planes = s->planes;
+    C.prec = s->prec;
     C.mass0 = s->mass0;
     C.poly = s->poly;
+    C.trec = s->trec;
     C.pmi = s->pmi;
     C.tcount = s->tcount;
     C.tlist = s->tlist;
@@ -2406,7 +2860,7 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
         st = launch_body_advance(s->pmi, s->nbodies, s->P.dt, q);
         if (st == XD_OK)
             st = launch_mesh_move(s->pmi, s->vlist_body, s->sphere, s->poly, s->ntri, s->tri_ref, s->P.wo,
-                                  s->P.disp2, s->counters + CN_REBUILD, q);
+                                  s->P.disp2, s->counters + CN_REBUILD, s->trec, q);
         if (st != XD_OK) return st;
     }
     ph.begin(0, q);
@@ -2434,7 +2888,8 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
     s->cells_clean = true;
     ph.begin(3, q);
     // the list holds at most n particles: no more warps than that
-    const unsigned grid = std::max(1u, std::min(kContactBlocks, (n + kContactThreads - 1) / kContactThreads));
+    const unsigned ct = s->cthreads;
+    const unsigned grid = std::max(1u, std::min(kContactWarpsTotal * 32u / ct, (n + ct - 1) / ct));
     // tangential springs: updated by a step, read only by the diagnostic evaluation (MODE 3)
     const HistTable ht = history_table(s);
     const int hist = s->hslots ? (MODE == 3 ? 2 : 1) : 0;
@@ -2447,7 +2902,7 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
         rp = s->rec_pairs;
     }
     const ContactArgs C = contact_args(s, rc, rp, record ? rec_cap : 0u, ht, MODE == 3 ? 0 : 1);
-#define XD_MX_CONTACT(REC, H) k_mx_contact<REC, H><<<grid, kContactThreads, 0, q>>>(s->P, C)
+#define XD_MX_CONTACT(REC, H) k_mx_contact<REC, H><<<grid, ct, 0, q>>>(s->P, C)
     if (record) {
         if (hist == 2) XD_MX_CONTACT(true, 2);
         else if (hist == 1) XD_MX_CONTACT(true, 1);
@@ -2536,6 +2991,7 @@ int mixed_step(MixedScene* s, unsigned nsteps, cudaStream_t q, const Phases& ph)
             st = launch_body_advance(s->pmi, s->nbodies, s->P.dt, q);
             if (st == XD_OK) st = launch_update_polygon(s->pmi, s->vlist_body, s->sphere, s->poly, s->ntri, q);
         }
+        if (st == XD_OK) st = launch_tri_records(s->poly, s->ntri, s->trec, q);
         s->cells_clean = false;
         return st;
     }
@@ -2719,6 +3175,7 @@ int mixed_set_planes(MixedScene* s, const xd_plane_info* planes, cudaStream_t q)
     if (!s->ready) return XD_OK;   // the set-up takes them from the description
     int st = cuda_status(cudaMemcpyAsync(s->planes, planes, sizeof(xd_plane_info) * s->nplanes,
                                          cudaMemcpyHostToDevice, q), "scene_set_planes");
+    if (st == XD_OK) st = launch_plane_recs(s->planes, s->nplanes, s->prec, q);
     if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "scene_set_planes");
     plane_prefilter(s->P, planes, s->nplanes);
     s->cells_clean = false;   // the planes in reach of each particle change
@@ -2772,6 +3229,33 @@ int mixed_set_active(MixedScene* s, unsigned active, bool restore, cudaStream_t 
 }
 
 unsigned mixed_active(MixedScene* s) { return s->ready ? s->n : (s->active_req != ~0u ? s->active_req : s->desc.np); }
+
+int mixed_set_tuning(MixedScene* s, const xd_tuning* t)
+{
+    if (s->ready) return set_error(XD_ERR_STATE, "scene_set_tuning: set before the first upload");
+    if (!(t->skin_factor >= 0.02f && t->skin_factor <= 1.0f))
+        return set_error(XD_ERR_INVALID, "scene_set_tuning: skin factor %g outside [0.02, 1]", (double)t->skin_factor);
+    if (t->verlet_cap < 8 || t->verlet_cap > 256)
+        return set_error(XD_ERR_INVALID, "scene_set_tuning: Verlet capacity %u outside [8, 256]", t->verlet_cap);
+    if (t->triangle_cap < 4 || t->triangle_cap > 128)
+        return set_error(XD_ERR_INVALID, "scene_set_tuning: triangle capacity %u outside [4, 128]", t->triangle_cap);
+    if (t->contact_threads != 32 && t->contact_threads != 64 && t->contact_threads != 128)
+        return set_error(XD_ERR_INVALID, "scene_set_tuning: contact block of %u threads (32, 64 or 128)",
+                         t->contact_threads);
+    s->skin_factor = t->skin_factor;
+    s->vcap = t->verlet_cap;
+    s->tcap = t->triangle_cap;
+    s->cthreads = t->contact_threads;
+    return XD_OK;
+}
+
+void mixed_get_tuning(const MixedScene* s, xd_tuning* t)
+{
+    t->skin_factor = s->skin_factor;
+    t->verlet_cap = s->vcap;
+    t->triangle_cap = s->tcap;
+    t->contact_threads = s->cthreads;
+}
 
 int mixed_set_kinematic(MixedScene* s, bool enable)
 {
@@ -2847,6 +3331,25 @@ int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q)
     return st;
 }
 
+int mixed_stats(MixedScene* s, unsigned long long* out, cudaStream_t q)
+{
+    unsigned c[kCounters] = {};
+    int st = cuda_status(cudaMemcpyAsync(c, s->counters, sizeof(c), cudaMemcpyDeviceToHost, q), "scene_stats");
+    if (st == XD_OK) st = cuda_status(cudaStreamSynchronize(q), "scene_stats");
+    out[0] = c[CN_HEAVY];
+    out[1] = c[CN_DECISIONS];
+    out[2] = c[CN_NORMALS];
+    out[3] = c[CN_SLIPS];
+    out[4] = c[CN_WALLS];
+    out[5] = c[CN_REBUILDS];
+    out[6] = c[CN_HTRI];
+    out[7] = c[CN_VINC];
+    out[8] = c[CN_TINC];
+    out[9] = c[CN_VSUM];
+    out[10] = c[CN_TSUM];
+    return st;
+}
+
 // ---- batches: many mixed scenes advanced by shared launches ----------------
 //
 // A step of a batch is one graph: one advance launch over every scene's
@@ -2863,7 +3366,7 @@ namespace {
 
 constexpr unsigned kBatchGroup = 32;
 constexpr unsigned kBatchGraphSteps = 4;   // later steps captured per graph launch
-constexpr unsigned kBatchContactBlocks = 152 * 8;
+
 
 // One scene of a batch as the batch kernels read it.
 struct BatchScene {
@@ -2970,14 +3473,14 @@ __global__ void __launch_bounds__(1024) k_batch_chunks(const BatchScene* __restr
 // The contact pass of every scene: the warps share the runs of all scenes'
 // lists in contiguous ranges; a warp loads the scene of a run into its own
 // shared-memory slot when the scene changes.
-__global__ void __launch_bounds__(kContactThreads) k_batch_contact(const BatchScene* __restrict__ D, unsigned ns,
+__global__ void __launch_bounds__(kContactMaxThreads) k_batch_contact(const BatchScene* __restrict__ D, unsigned ns,
                                                                    const unsigned* __restrict__ chunk_start)
 {
-    __shared__ WarpScene ws[kContactThreads / 32];
+    __shared__ WarpScene ws[kContactMaxThreads / 32];
     const unsigned lane = threadIdx.x & 31u, wb = threadIdx.x / 32u;
     WarpScene& W = ws[wb];
-    const unsigned warps = gridDim.x * (kContactThreads / 32u);
-    const unsigned gw = blockIdx.x * (kContactThreads / 32u) + wb;
+    const unsigned warps = gridDim.x * (blockDim.x / 32u);
+    const unsigned gw = blockIdx.x * (blockDim.x / 32u) + wb;
     const unsigned total = __ldg(chunk_start + ns);
     const unsigned per = (total + warps - 1u) / warps;
     const unsigned c0 = gw * per, c1 = min(total, c0 + per);
@@ -3020,6 +3523,7 @@ struct MixedBatch {
                                                      // 2: kBatchGraphSteps later steps
     cudaGraphExec_t finish_graph = nullptr;          // last kick and the body reactions
     bool captured = false;
+    unsigned cthreads = kContactThreads;             // block size of the shared contact launch
     // direct launches (profilers; kernel timing): CUDA events around the
     // later steps' advance and every contact launch
     bool direct = false;
@@ -3155,7 +3659,7 @@ int capture_batch_step(MixedBatch* b, int kind)
                              "batch capture dependencies");
         if (st == XD_OK) {
             k_batch_chunks<<<1, 1024, 0, cs>>>(b->d_scenes, ns, b->d_chunks);
-            k_batch_contact<<<kBatchContactBlocks, kContactThreads, 0, cs>>>(b->d_scenes, ns, b->d_chunks);
+            k_batch_contact<<<kContactWarpsTotal * 32u / b->cthreads, b->cthreads, 0, cs>>>(b->d_scenes, ns, b->d_chunks);
             st = launch_status("batch contact");
         }
         if (st == XD_OK) st = current_deps(cs, &cg, &deps);
@@ -3290,6 +3794,7 @@ int mixed_batch_create(MixedScene* const* scenes, unsigned count, MixedBatch** o
     MixedBatch* b = new (std::nothrow) MixedBatch();
     if (!b) return set_error(XD_ERR_NOMEM, "batch: host allocation");
     b->scenes.assign(scenes, scenes + count);
+    b->cthreads = scenes[0]->cthreads;   // the first scene's choice (one launch serves all)
     const char* ng = getenv("XDEM_NO_GRAPHS");
     b->direct = ng && ng[0] && ng[0] != '0';
     *out = b;
@@ -3349,7 +3854,7 @@ int batch_step_direct(MixedBatch* b, unsigned nsteps, cudaStream_t q)
             if (flags[k]) st = rebuild(b->scenes[k], q);
         if (st != XD_OK) break;
         k_batch_chunks<<<1, 1024, 0, q>>>(b->d_scenes, ns, b->d_chunks);
-        span(1, [&] { k_batch_contact<<<kBatchContactBlocks, kContactThreads, 0, q>>>(b->d_scenes, ns, b->d_chunks); });
+        span(1, [&] { k_batch_contact<<<kContactWarpsTotal * 32u / b->cthreads, b->cthreads, 0, q>>>(b->d_scenes, ns, b->d_chunks); });
         st = launch_status("batch contact");
     }
     if (st == XD_OK) {

@@ -32,6 +32,9 @@ int mixed_eval_contacts(MixedScene* s, double* force, double* moment, cudaStream
 int mixed_pair_list(MixedScene* s, unsigned cap_per_particle, unsigned* counts, unsigned* partners,
                     cudaStream_t q);
 int mixed_counters(MixedScene* s, unsigned long long* out, cudaStream_t q);
+int mixed_stats(MixedScene* s, unsigned long long* out, cudaStream_t q);
+int mixed_set_tuning(MixedScene* s, const xd_tuning* t);
+void mixed_get_tuning(const MixedScene* s, xd_tuning* t);
 unsigned long long mixed_device_bytes(MixedScene* s);
 int mixed_set_history(MixedScene* s, unsigned slots);
 int mixed_set_kinematic(MixedScene* s, bool enable);

@@ -18,13 +18,21 @@
 //   cleared by each call; every other scratch byte is written before it is
 //   read.  Calls whose work overlaps on the GPU (different streams, or
 //   different host threads) race on the array: serialise them.
-// * In host code the array's name is only a host-side stand-in, so the
-//   device address is taken with cudaGetSymbolAddress once per device, with
-//   that device current, on that device's first call.  That first call should
-//   therefore come before any stream capture on the device.
+// * In host code the array's name is only a host-side stand-in, so every call
+//   takes the device address with cudaGetSymbolAddress, with the caller's
+//   device current (a call with n = 0 included), and checks its return code.
+//   The address is not cached: after cudaDeviceReset the array has a new one.
+// * The library is built without relocatable device code, so this file is a
+//   CUDA module of its own.  Under lazy module loading (the default of CUDA
+//   12.2 and later) the driver reserves the array's memory only when the
+//   module is first used, which is this entry point's first call on a
+//   device.  A caller that hands out all device memory from its own pool
+//   must therefore make one call on each device before the pool takes its
+//   memory -- a call with n = 0 only clears the cell arrays and serves as
+//   that set-up -- or run with CUDA_MODULE_LOADING=EAGER.  That first call
+//   should also come before any stream capture on the device.  Later calls
+//   reserve nothing.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "xd_grid.cuh"
 #include "xd_internal.cuh"
@@ -44,27 +52,13 @@ constexpr size_t kScratchBytes = 256 + al256(4 * kMax) + al256(4 * kMax) + al256
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_addr[kMaxDevices] = {};
-
-// Device address of g_noalloc_scratch on the current device (set-up on the
-// device's first call).
+// Device address of g_noalloc_scratch on the current device.
 int scratch_address(void** out)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return xd::cuda_status(e, "reorder_noalloc: cudaGetDevice");
-    if (dev < 0 || dev >= kMaxDevices)
-        return xd::set_error(XD_ERR_INVALID, "reorder_noalloc: device ordinal %d out of range", dev);
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return xd::cuda_status(e, "reorder_noalloc: cudaGetSymbolAddress");
-        g_addr[dev] = p;
-    }
-    *out = g_addr[dev];
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return xd::cuda_status(e, "reorder_noalloc: cudaGetSymbolAddress");
+    *out = p;
     return XD_OK;
 }
 

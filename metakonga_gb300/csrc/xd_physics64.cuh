@@ -253,84 +253,146 @@ __device__ __forceinline__ PlaneD load_plane(const xd_plane_info* p)
 
 __device__ __forceinline__ int sgn(double L) { return L < 0 ? -1 : 1; }
 
+// Vector arithmetic with every operation rounded on its own (no multiply-add
+// contraction whatever the translation unit's flags), left to right as the
+// reference's operators: the region tests below give the same bits in the
+// FP64 form (built with --fmad=false) and in the mixed form's FP64 fallbacks.
+namespace rn {
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ d3 add(d3 a, d3 b) { return mk(add(a.x, b.x), add(a.y, b.y), add(a.z, b.z)); }
+__device__ __forceinline__ d3 sub(d3 a, d3 b) { return mk(sub(a.x, b.x), sub(a.y, b.y), sub(a.z, b.z)); }
+__device__ __forceinline__ d3 scale(double s, d3 a) { return mk(mul(s, a.x), mul(s, a.y), mul(s, a.z)); }
+__device__ __forceinline__ d3 divs(d3 a, double s) { return mk(div(a.x, s), div(a.y, s), div(a.z, s)); }
+__device__ __forceinline__ double dot(d3 a, d3 b) { return add(add(mul(a.x, b.x), mul(a.y, b.y)), mul(a.z, b.z)); }
+__device__ __forceinline__ double length(d3 a) { return __dsqrt_rn(rn::dot(a, a)); }
+__device__ __forceinline__ d3 cross(d3 a, d3 b)
+{
+    return mk(sub(mul(a.y, b.z), mul(a.z, b.y)), sub(mul(a.z, b.x), mul(a.x, b.z)), sub(mul(a.x, b.y), mul(a.y, b.x)));
+}
+}  // namespace rn
+
 // particle_plane_contact_detection (impl:487-570); pow(x, 2.0) is x * x
 // (IEEE: the correctly rounded square).
 __device__ __forceinline__ double plane_detection(const PlaneD& pe, d3 xp, d3 wp, d3& u, double r)
 {
-    double a_l1 = (wp.x - pe.l1) * (wp.x - pe.l1);
-    double b_l2 = (wp.y - pe.l2) * (wp.y - pe.l2);
-    double sqa = wp.x * wp.x;
-    double sqb = wp.y * wp.y;
-    double sqc = wp.z * wp.z;
-    double sqr = r * r;
+    const double a_l1 = rn::mul(rn::sub(wp.x, pe.l1), rn::sub(wp.x, pe.l1));
+    const double b_l2 = rn::mul(rn::sub(wp.y, pe.l2), rn::sub(wp.y, pe.l2));
+    const double sqa = rn::mul(wp.x, wp.x);
+    const double sqb = rn::mul(wp.y, wp.y);
+    const double sqc = rn::mul(wp.z, wp.z);
+    const double sqr = rn::mul(r, r);
     if (fabs(wp.z) < r && (wp.x > 0 && wp.x < pe.l1) && (wp.y > 0 && wp.y < pe.l2)) {
-        d3 dp = xp - pe.xw;
-        d3 uu = pe.uw / length(pe.uw);
-        int pp = -sgn(dot(dp, pe.uw));
-        u = (double)pp * uu;
-        return r - fabs(dot(dp, u));
+        const d3 dp = rn::sub(xp, pe.xw);
+        const d3 uu = rn::divs(pe.uw, rn::length(pe.uw));
+        const int pp = -sgn(rn::dot(dp, pe.uw));
+        u = rn::scale((double)pp, uu);
+        return rn::sub(r, fabs(rn::dot(dp, u)));
     }
-    if (wp.x < 0 && wp.y < 0 && (sqa + sqb + sqc) < sqr) {
-        d3 X = xp - pe.xw; double h = length(X); u = X / h; return r - h;
-    } else if (wp.x > pe.l1 && wp.y < 0 && (a_l1 + sqb + sqc) < sqr) {
-        d3 X = xp - pe.w2; double h = length(X); u = X / h; return r - h;
-    } else if (wp.x > pe.l1 && wp.y > pe.l2 && (a_l1 + b_l2 + sqc) < sqr) {
-        d3 X = xp - pe.w3; double h = length(X); u = X / h; return r - h;
-    } else if (wp.x < 0 && wp.y > pe.l2 && (sqa + b_l2 + sqc) < sqr) {
-        d3 X = xp - pe.w4; double h = length(X); u = X / h; return r - h;
+    if (wp.x < 0 && wp.y < 0 && rn::add(rn::add(sqa, sqb), sqc) < sqr) {
+        const d3 X = rn::sub(xp, pe.xw); const double h = rn::length(X); u = rn::divs(X, h); return rn::sub(r, h);
+    } else if (wp.x > pe.l1 && wp.y < 0 && rn::add(rn::add(a_l1, sqb), sqc) < sqr) {
+        const d3 X = rn::sub(xp, pe.w2); const double h = rn::length(X); u = rn::divs(X, h); return rn::sub(r, h);
+    } else if (wp.x > pe.l1 && wp.y > pe.l2 && rn::add(rn::add(a_l1, b_l2), sqc) < sqr) {
+        const d3 X = rn::sub(xp, pe.w3); const double h = rn::length(X); u = rn::divs(X, h); return rn::sub(r, h);
+    } else if (wp.x < 0 && wp.y > pe.l2 && rn::add(rn::add(sqa, b_l2), sqc) < sqr) {
+        const d3 X = rn::sub(xp, pe.w4); const double h = rn::length(X); u = rn::divs(X, h); return rn::sub(r, h);
     }
     d3 X, wj;
-    if ((wp.x > 0 && wp.x < pe.l1) && wp.y < 0 && (sqb + sqc) < sqr) {
-        X = xp - pe.xw; wj = pe.w2 - pe.xw;
-    } else if ((wp.x > 0 && wp.x < pe.l1) && wp.y > pe.l2 && (b_l2 + sqc) < sqr) {
-        X = xp - pe.w4; wj = pe.w3 - pe.w4;
-    } else if ((wp.x > 0 && wp.y < pe.l2) && wp.x < 0 && (sqr + sqc) < sqr) {
-        X = xp - pe.xw; wj = pe.w4 - pe.xw;
-    } else if ((wp.x > 0 && wp.y < pe.l2) && wp.x > pe.l1 && (a_l1 + sqc) < sqr) {
-        X = xp - pe.w2; wj = pe.w3 - pe.w2;
+    if ((wp.x > 0 && wp.x < pe.l1) && wp.y < 0 && rn::add(sqb, sqc) < sqr) {
+        X = rn::sub(xp, pe.xw); wj = rn::sub(pe.w2, pe.xw);
+    } else if ((wp.x > 0 && wp.x < pe.l1) && wp.y > pe.l2 && rn::add(b_l2, sqc) < sqr) {
+        X = rn::sub(xp, pe.w4); wj = rn::sub(pe.w3, pe.w4);
+    } else if ((wp.x > 0 && wp.y < pe.l2) && wp.x < 0 && rn::add(sqr, sqc) < sqr) {
+        X = rn::sub(xp, pe.xw); wj = rn::sub(pe.w4, pe.xw);
+    } else if ((wp.x > 0 && wp.y < pe.l2) && wp.x > pe.l1 && rn::add(a_l1, sqc) < sqr) {
+        X = rn::sub(xp, pe.w2); wj = rn::sub(pe.w3, pe.w2);
     } else {
         return -1.0;
     }
-    d3 us = wj / length(wj);
-    d3 hs = X - (dot(X, us)) * us;
-    double h = length(hs);
-    u = (-hs) / h;
-    return r - h;
+    const d3 us = rn::divs(wj, rn::length(wj));
+    const d3 hs = rn::sub(X, rn::scale(rn::dot(X, us), us));
+    const double h = rn::length(hs);
+    u = rn::divs(mk(-hs.x, -hs.y, -hs.z), h);
+    return rn::sub(r, h);
+}
+
+// The reference's plane-frame coordinates wp = (dp.u1, dp.u2, dp.uw) of
+// dp = xp - xw (plane_contact_force_kernel, impl:596-600), rounded per operation.
+__device__ __forceinline__ d3 plane_coords(const PlaneD& pe, d3 xp)
+{
+    const d3 dp = rn::sub(xp, pe.xw);
+    return mk(rn::dot(dp, pe.u1), rn::dot(dp, pe.u2), rn::dot(dp, pe.uw));
 }
 
 // closestPtPointTriangle (impl:837-899)
 __device__ __forceinline__ d3 closest_pt_triangle(d3 a, d3 b, d3 c, d3 p)
 {
-    d3 ab = b - a, ac = c - a, ap = p - a;
-    double d1 = dot(ab, ap), d2 = dot(ac, ap);
+    const d3 ab = rn::sub(b, a), ac = rn::sub(c, a), ap = rn::sub(p, a);
+    const double d1 = rn::dot(ab, ap), d2 = rn::dot(ac, ap);
     if (d1 <= 0.0 && d2 <= 0.0) return a;
-    d3 bp = p - b;
-    double d3_ = dot(ab, bp), d4 = dot(ac, bp);
+    const d3 bp = rn::sub(p, b);
+    const double d3_ = rn::dot(ab, bp), d4 = rn::dot(ac, bp);
     if (d3_ >= 0.0 && d4 <= d3_) return b;
-    double vc = d1 * d4 - d3_ * d2;
+    const double vc = rn::sub(rn::mul(d1, d4), rn::mul(d3_, d2));
     if (vc <= 0.0 && d1 >= 0.0 && d3_ <= 0.0) {
-        double v = d1 / (d1 - d3_);
-        return a + v * ab;
+        const double v = rn::div(d1, rn::sub(d1, d3_));
+        return rn::add(a, rn::scale(v, ab));
     }
-    d3 cp = p - c;
-    double d5 = dot(ab, cp), d6 = dot(ac, cp);
+    const d3 cp = rn::sub(p, c);
+    const double d5 = rn::dot(ab, cp), d6 = rn::dot(ac, cp);
     if (d6 >= 0.0 && d5 <= d6) return c;
-    double vb = d5 * d2 - d1 * d6;
+    const double vb = rn::sub(rn::mul(d5, d2), rn::mul(d1, d6));
     if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
-        double w = d2 / (d2 - d6);
-        return a + w * ac;
+        const double w = rn::div(d2, rn::sub(d2, d6));
+        return rn::add(a, rn::scale(w, ac));
     }
-    double va = d3_ * d6 - d5 * d4;
-    if (va <= 0.0 && (d4 - d3_) >= 0.0 && (d5 - d6) >= 0.0) {
-        double w = (d4 - d3_) / ((d4 - d3_) + (d5 - d6));
-        return b + w * (c - b);
+    const double va = rn::sub(rn::mul(d3_, d6), rn::mul(d5, d4));
+    if (va <= 0.0 && rn::sub(d4, d3_) >= 0.0 && rn::sub(d5, d6) >= 0.0) {
+        const double w = rn::div(rn::sub(d4, d3_), rn::add(rn::sub(d4, d3_), rn::sub(d5, d6)));
+        return rn::add(b, rn::scale(w, rn::sub(c, b)));
     }
-    double denom = 1.0 / (va + vb + vc);
-    double v = vb * denom;
-    double w = vc * denom;
-    return (a + v * ab) + w * ac;
+    const double denom = rn::div(1.0, rn::add(rn::add(va, vb), vc));
+    const double v = rn::mul(vb, denom);
+    const double w = rn::mul(vc, denom);
+    return rn::add(rn::add(a, rn::scale(v, ab)), rn::scale(w, ac));
 }
 
+// The face normal particle_polygonObject_collision_kernel<1> pushes along
+// (impl:985-987): -(Q - P) x (R - P), normalised.
+__device__ __forceinline__ d3 triangle_normal(d3 P, d3 Q, d3 R)
+{
+    const d3 c = rn::cross(rn::sub(Q, P), rn::sub(R, P));
+    const d3 u = mk(-c.x, -c.y, -c.z);
+    return rn::divs(u, rn::length(u));
+}
+
+// Per-triangle record of the mixed form's contact pass, written whenever a
+// mesh is placed: vertex P and the face normal in FP64 (the plane distance
+// of a face contact is n . (x - P)), the edges Q - P and R - P in FP32 (the
+// region test relative to the sphere), and the polygon body.
+struct __align__(16) TriRec {
+    double p[3];
+    double n[3];
+    float q[3], r[3];
+    unsigned body;
+    unsigned pad;
+};
+
+__device__ __forceinline__ void write_tri_rec(TriRec* __restrict__ out, d3 P, d3 Q, d3 R, unsigned body)
+{
+    const d3 n = triangle_normal(P, Q, R);
+    TriRec t;
+    t.p[0] = P.x; t.p[1] = P.y; t.p[2] = P.z;
+    t.n[0] = n.x; t.n[1] = n.y; t.n[2] = n.z;
+    t.q[0] = (float)rn::sub(Q.x, P.x); t.q[1] = (float)rn::sub(Q.y, P.y); t.q[2] = (float)rn::sub(Q.z, P.z);
+    t.r[0] = (float)rn::sub(R.x, P.x); t.r[1] = (float)rn::sub(R.y, P.y); t.r[2] = (float)rn::sub(R.z, P.z);
+    t.body = body;
+    t.pad = 0;
+    *out = t;
+}
 
 // ---------------------------------------------- mesh update
 //

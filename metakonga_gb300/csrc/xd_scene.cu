@@ -588,6 +588,34 @@ int xd_scene_counters(xd_scene* s, unsigned long long out[4], void* stream)
     return mixed_counters(s->mixed, out, static_cast<cudaStream_t>(stream));
 }
 
+int xd_scene_stats(xd_scene* s, unsigned long long* out, unsigned count, void* stream)
+{
+    if (!s || (!out && count)) return set_error(XD_ERR_INVALID, "scene_stats: null argument");
+    if (count > XD_STATS_COUNT) return set_error(XD_ERR_INVALID, "scene_stats: at most %d values", XD_STATS_COUNT);
+    unsigned long long v[XD_STATS_COUNT] = {};
+    if (s->mixed) {
+        const int st = mixed_stats(s->mixed, v, static_cast<cudaStream_t>(stream));
+        if (st != XD_OK) return st;
+    }
+    for (unsigned i = 0; i < count; ++i) out[i] = v[i];
+    return XD_OK;
+}
+
+int xd_scene_set_tuning(xd_scene* s, const xd_tuning* t)
+{
+    if (!s || !t) return set_error(XD_ERR_INVALID, "scene_set_tuning: null argument");
+    if (!s->mixed) return set_error(XD_ERR_STATE, "scene_set_tuning: an FP64 scene has no tunable parameters");
+    return mixed_set_tuning(s->mixed, t);
+}
+
+int xd_scene_get_tuning(xd_scene* s, xd_tuning* t)
+{
+    if (!s || !t) return set_error(XD_ERR_INVALID, "scene_get_tuning: null argument");
+    if (!s->mixed) return set_error(XD_ERR_STATE, "scene_get_tuning: an FP64 scene has no tunable parameters");
+    mixed_get_tuning(s->mixed, t);
+    return XD_OK;
+}
+
 int xd_scene_rebuilds(xd_scene* s, unsigned long long* count, unsigned long long* launches_each,
                       void* stream)
 {

@@ -42,8 +42,22 @@ def _addr(a):
     return None if a is None or a.size == 0 else a.ctypes.data
 
 
+class Tuning(C.Structure):
+    """xd_tuning: skin width over r_max, Verlet/triangle list capacities, and
+    the contact pass's block size (mixed form; set before the first upload)."""
+    _fields_ = [("skin_factor", C.c_float), ("verlet_cap", C.c_uint), ("triangle_cap", C.c_uint),
+                ("contact_threads", C.c_uint)]
+
+    def as_dict(self) -> dict:
+        return {k: (round(float(getattr(self, k)), 6) if k == "skin_factor" else int(getattr(self, k)))
+                for k, _ in self._fields_}
+
+
+DEFAULT_TUNING = {"skin_factor": 0.1, "verlet_cap": 48, "triangle_cap": 16, "contact_threads": 64}
+
+
 class DeviceScene:
-    def __init__(self, scene, mode: int = MODE_FP64):
+    def __init__(self, scene, mode: int = MODE_FP64, tuning: dict = None):
         if _lib.lib().xd_sizeof(b"xd_scene_desc") != C.sizeof(_Desc):
             raise RuntimeError("xd_scene_desc layout mismatch between binding and library")
         self.scene = scene
@@ -72,7 +86,16 @@ class DeviceScene:
         h = C.c_void_p()
         call("xd_scene_create", C.addressof(d), C.addressof(h))
         self.handle = h
+        if tuning is not None:
+            t = Tuning(**dict(DEFAULT_TUNING, **tuning))
+            call("xd_scene_set_tuning", self.handle, C.addressof(t))
         self.upload(scene)
+
+    def tuning(self) -> dict:
+        """The scene's tuning (mixed form)."""
+        t = Tuning()
+        call("xd_scene_get_tuning", self.handle, C.addressof(t))
+        return t.as_dict()
 
     def upload(self, sc, stream: int = 0):
         arrs = [np.ascontiguousarray(getattr(sc, f)) for f in
@@ -157,6 +180,17 @@ class DeviceScene:
         call("xd_scene_counters", self.handle, out.ctypes.data, stream)
         return {"contact_list": int(out[0]), "fp64_decisions": int(out[1]),
                 "fp64_normal_forces": int(out[2]), "fp64_slips": int(out[3])}
+
+    STATS = ("contact_list", "fp64_decisions", "fp64_normal_forces", "fp64_slips", "fp64_wall_regions",
+             "rebinnings", "listed_with_triangles", "verlet_overflows", "triangle_overflows",
+             "verlet_entries", "triangle_entries")
+
+    def stats(self, stream: int = 0) -> dict:
+        """Mixed-form diagnostics (xd_scene_stats): the counters above, FP64
+        wall region tests, re-binnings, and list overflows at the last build."""
+        out = np.zeros(len(self.STATS), np.uint64)
+        call("xd_scene_stats", self.handle, out.ctypes.data, len(self.STATS), stream)
+        return {k: int(v) for k, v in zip(self.STATS, out)}
 
     def rebuilds(self, stream: int = 0):
         """(re-binnings so far, kernel launches per re-binning) of a mixed scene."""

@@ -452,13 +452,15 @@ def drum(n: int = 4000, seed: int = 11, rmin: float = 0.003, rmax: float = 0.005
 def drum_lattice(n: int = 500_000, seed: int = 13, rmin: float = 0.002, rmax: float = 0.004,
                  radius: float = 0.5, length: float = 0.4, omega: float = 1.0, n_theta: int = 242,
                  n_z: int = 20, n_ring: int = 30, wall_friction: float = 0.5, dt: float = 5.0e-6,
-                 steps: int = 50_000) -> Scene:
+                 steps: int = 50_000, slab: float = None) -> Scene:
     """The rotating drum at full size: ``n`` spheres on a jittered FCC lattice
     (nearest neighbours 2.04 r_max apart) filling the drum from the bottom, in
     the closed 20,480-triangle cylinder of ``drum`` turning at ``omega`` about
     its (y) axis.  Radii U[2, 4] mm: 500,000 such spheres settle to about a
     third of the drum's volume (mean sphere volume 1.26e-7 m^3, packing
-    ~0.6); spheres of 3-5 mm would need 45 % of the drum as solid."""
+    ~0.6); spheres of 3-5 mm would need 45 % of the drum as solid.  ``slab``
+    fills only the lattice sites within slab / 2 of the drum's mid-plane
+    (an axial slab of the bed, in the full mesh)."""
     rng = _rng(seed)
     tri = cylinder_mesh(radius, length, n_theta, n_z, n_ring)
     d = 2.04 * rmax
@@ -471,7 +473,7 @@ def drum_lattice(n: int = 500_000, seed: int = 13, rmin: float = 0.002, rmax: fl
     gx, gy, gz = np.meshgrid(ks, ky, ks, indexing="ij")
     cells = np.stack([gx.ravel(), gy.ravel(), gz.ravel()], axis=1).astype(np.float64)
     pts = (cells[:, None, :] + base[None, :, :]).reshape(-1, 3) * a
-    ok = (pts[:, 0] ** 2 + pts[:, 2] ** 2 < rin * rin) & (np.abs(pts[:, 1]) < half)
+    ok = (pts[:, 0] ** 2 + pts[:, 2] ** 2 < rin * rin) & (np.abs(pts[:, 1]) < (half if slab is None else slab / 2))
     pts = pts[ok]
     if pts.shape[0] < n:
         raise ValueError(f"drum_lattice: {pts.shape[0]} lattice sites, {n} requested")
@@ -549,7 +551,7 @@ def _mesh_arrays(tri: np.ndarray, body: int = 0):
 def hopper(n: int = 20_000, seed: int = 3, orifice: float = 8.0, fric: float = 0.4,
            rmin: float = 0.002, rmax: float = 0.004, wall_angle_deg: float = 60.0,
            n_theta: int = 64, n_z: int = 32, steps: int = 10_000, dt: float = 5.0e-6,
-           packing: float = 0.25) -> Scene:
+           packing: float = 0.25, gate: bool = False) -> Scene:
     """Hopper discharge: n spheres, r ~ U[rmin, rmax], on a jittered cubic
     lattice (no overlaps) inside a conical hopper whose wall rises at
     ``wall_angle_deg`` from the horizontal; the orifice (at z = 0) is
@@ -557,7 +559,10 @@ def hopper(n: int = 20_000, seed: int = 3, orifice: float = 8.0, fric: float = 0
     below it.  The cone is a fixed polygon body of n_theta x n_z x 2
     triangles; its top radius is chosen so that the spheres (the lattice
     pitch gives the packing fraction, at most ``packing``) fill the lower 60%
-    of its volume.  Particle-particle friction is ``fric``, as is the wall's."""
+    of its volume.  Particle-particle friction is ``fric``, as is the wall's.
+    ``gate`` adds a second plane that closes the orifice (z = 0), so that the
+    spheres can fill and settle into a bed before the discharge;
+    ``open_gate`` gives the planes with it moved out of the way."""
     rng = _rng(seed)
     d_mean = rmin + rmax
     r_o = 0.5 * orifice * d_mean
@@ -623,13 +628,30 @@ def hopper(n: int = 20_000, seed: int = 3, orifice: float = 8.0, fric: float = 0
     zf = -max(0.1, 10.0 * d_mean)
     w = r_top + 0.1
     floor = define_plane((-w, -w, zf), (w, -w, zf), (w, w, zf), (-w, w, zf))
-    planes = np.array([floor], dtype=PLANE)
+    walls, names = [floor], ["floor"]
+    if gate:
+        g = r_o + 2.0 * rmax
+        walls.append(define_plane((-g, -g, 0.0), (g, -g, 0.0), (g, g, 0.0), (-g, g, 0.0)))
+        names.append("gate")
+    planes = np.array(walls, dtype=PLANE)
     maxr = max(rmax, float(sphere[:, 3].max()))
     return Scene(name="hopper", seed=seed, dt=dt, steps=steps,
                  params=_reference_grid(maxr, n, dt), pos=pos, **_state(pos),
-                 cp_pp=cp, planes=planes, plane_names=["floor"],
-                 cp_planes=np.array([cp], dtype=CONTACT_PROPERTY), poly=poly, sphere=sphere,
-                 vlist=vlist, pmi=pmi, cp_poly=np.array([cp], dtype=CONTACT_PROPERTY))
+                 cp_pp=cp, planes=planes, plane_names=names,
+                 cp_planes=np.array([cp] * len(names), dtype=CONTACT_PROPERTY), poly=poly,
+                 sphere=sphere, vlist=vlist, pmi=pmi, cp_poly=np.array([cp], dtype=CONTACT_PROPERTY))
+
+
+def open_gate(sc: Scene) -> np.ndarray:
+    """The planes of a gated ``hopper`` with the gate moved 2 cm below the
+    floor, where no sphere reaches it (the orifice open)."""
+    planes = sc.planes.copy()
+    k = sc.plane_names.index("gate")
+    floor = planes[sc.plane_names.index("floor")]
+    drop = np.array([0.0, 0.0, float(floor["xw"][2]) - 0.02])
+    g = planes[k]
+    planes[k] = define_plane(g["xw"] + drop, g["w2"] + drop, g["w3"] + drop, g["w4"] + drop)
+    return planes
 
 
 def hopper_batch(count: int = 256, seed: int = 1, n_min: int = 2_000, n_max: int = 200_000):

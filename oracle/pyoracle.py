@@ -261,16 +261,21 @@ class Oracle:
                 "sorted": np.zeros(n, np.uint32), "cstart": np.zeros(sc.ncell, np.uint32),
                 "cend": np.zeros(sc.ncell, np.uint32)}
 
+    def work_arrays(self, sc):
+        """Grid work arrays for ``run`` (allocate once, reuse across calls)."""
+        return self._work(sc)
+
     def run(self, sc, nsteps: int, cpu_path: bool = False, history: "History" = None,
-            kinematic: bool = False, emitter: "Emitter" = None):
+            kinematic: bool = False, emitter: "Emitter" = None, work=None):
         """Advance ``sc`` (in place) by nsteps whole steps; returns the grid work
-        arrays.  With ``history`` the contacts keep tangential springs; with
-        ``kinematic`` the polygon bodies move by their own vel and omega each
-        step (xdo_advance_bodies); with ``emitter`` only its active particles
-        take part (xdo_emitter)."""
+        arrays (``work`` if given, else new ones).  With ``history`` the
+        contacts keep tangential springs; with ``kinematic`` the polygon bodies
+        move by their own vel and omega each step (xdo_advance_bodies); with
+        ``emitter`` only its active particles take part (xdo_emitter)."""
         for a in ("pos", "vel", "acc", "omega", "alpha", "force", "moment", "mass", "inertia"):
             assert getattr(sc, a).flags["C_CONTIGUOUS"]
-        work = self._work(sc)
+        if work is None:
+            work = self._work(sc)
         s = self._scene_struct(sc, work)
         if history is not None:
             assert not cpu_path

@@ -1123,14 +1123,45 @@ static void cpu_dhs(const fconst* c, double friction, double cdist, v3 cp, v3 dv
  * (contact_particles_plane.cpp:209-236) and
  * contact_particles_particles::cppCollision
  * (contact_particles_particles.cpp:53-89), velocity_verlet::updateVelocity
- * CPU branch (velocity_verlet.cpp:44-66).  Polygon contacts are not part of
- * the CPU baseline.  The start/end loop of _detection reads one element past
- * the sorted keys (neighborhood_cell.cpp:76); the restatement treats that
- * element as a key that differs from the last one. */
+ * CPU branch (velocity_verlet.cpp:44-66).  Triangle spheres join the grid
+ * after the particles (neighborhood_cell.cpp:44-50) and grid entries k >= np
+ * are polygon contacts, contact_particles_polygonObjects::cppolyCollision
+ * (contact_particles_polygonObjects.cpp:202-256): closest point
+ * (particle_polygon_contact_detection, :540-606), the face-winding normal,
+ * moment arm rcon u with rcon = r - cdist / 2, wall velocity
+ * v_body + w_body x (cp - origin), the reaction -F added to the body.  The
+ * start/end loop of _detection reads one element past the sorted keys
+ * (neighborhood_cell.cpp:76); the restatement treats that element as a key
+ * that differs from the last one. */
+static void cpu_poly_contact(const xdo_scene* s, unsigned t, double r, double m, v3 p, v3 v, v3 o, v3* F,
+                             v3* M)
+{
+    const xdo_polygon* tri = s->poly + t;
+    const unsigned b = (unsigned)tri->id;
+    xdo_polygon_mass* pm = s->pmi + b;
+    const xdo_contact_property* cp = s->cp_poly + b;
+    v3 P = ld3(tri->P), Q = ld3(tri->Q), R = ld3(tri->R);
+    v3 cpt = closest_pt_triangle(P, Q, R, p);
+    v3 po2cp = sub(cpt, ld3(pm->origin));
+    double cdist = r - len(sub(p, cpt));
+    if (!(cdist > 0)) return;
+    v3 u = neg(cross(sub(Q, P), sub(R, P)));
+    u = dvd(u, len(u));
+    double rcon = r - 0.5 * cdist;
+    v3 dv = sub(add(ld3(pm->vel), cross(ld3(pm->omega), po2cp)), add(v, cross(o, scl(r, u))));
+    fconst c = get_constant(r, 0.0, m, 0.0, cp);
+    v3 mf, mm = mk(0, 0, 0);
+    cpu_dhs(&c, cp->fric, cdist, scl(rcon, u), dv, u, s->prm.dt, &mf, &mm);
+    *F = add(*F, mf);
+    *M = add(*M, mm);
+    acc3(pm->force, neg(mf));
+}
+
 void xdo_cpu_step(xdo_scene* s)
 {
     xdo_params* prm = &s->prm;
     unsigned np = s->np;
+    const unsigned ng = np + s->ntri;
     double dt = prm->dt;
     double sqt_dt = 0.5 * dt * dt;
     for (unsigned i = 0; i < np; i++) {
@@ -1139,19 +1170,22 @@ void xdo_cpu_step(xdo_scene* s)
         v3 new_p = add(add(old_p, scl(dt, ld3(s->vel + 3 * (size_t)i))), scl(sqt_dt, ld3(s->acc + 3 * (size_t)i)));
         p[0] = new_p.x; p[1] = new_p.y; p[2] = new_p.z;
     }
-    for (unsigned i = 0; i < np; i++) {
+    for (unsigned i = 0; i < ng; i++) {
         int c[3];
-        const double* p = s->pos + 4 * (size_t)i;
+        const double* p = i < np ? s->pos + 4 * (size_t)i : s->sphere + 4 * (size_t)(i - np);
         cpu_hash(prm, p[0], p[1], p[2], c);
         s->hash[i] = cpu_get_hash(prm, c);
         s->index[i] = i;
     }
-    stable_sort_by_key(s->hash, s->index, np);
+    stable_sort_by_key(s->hash, s->index, ng);
     memset(s->cstart, 0xff, sizeof(unsigned) * (size_t)prm->ncell);
     memset(s->cend, 0, sizeof(unsigned) * (size_t)prm->ncell);
-    for (unsigned b = 0; b < np;) {
+    for (unsigned i = 0; i < s->nbodies && s->ntri; ++i) {
+        s->pmi[i].force[0] = s->pmi[i].force[1] = s->pmi[i].force[2] = 0.0;
+    }
+    for (unsigned b = 0; b < ng;) {
         unsigned e = b + 1;
-        while (e < np && s->hash[e] == s->hash[b]) e++;
+        while (e < ng && s->hash[e] == s->hash[b]) e++;
         s->cstart[s->hash[b]] = b;
         s->cend[s->hash[b]] = e;
         for (unsigned j = b; j < e; j++) s->sorted[j] = s->index[j];
@@ -1189,7 +1223,11 @@ void xdo_cpu_step(xdo_scene* s)
                     unsigned eid = s->cend[h];
                     for (unsigned j = sid; j < eid; j++) {
                         unsigned k = s->sorted[j];
-                        if (i == k || k >= np) continue;
+                        if (k >= np) {
+                            cpu_poly_contact(s, k - np, r, m, p, v, o, &F, &M);
+                            continue;
+                        }
+                        if (i == k) continue;
                         const double* q4 = s->pos + 4 * (size_t)k;
                         v3 jp = ld3(q4);
                         double jr = q4[3];

@@ -203,6 +203,33 @@ def test_cpu_path_runs_and_differs_as_documented(oracle):
     assert not np.array_equal(a.vel, b.vel)
 
 
+def test_cpu_path_polygon_contact_closed_form(oracle):
+    """The reference CPU path's polygon contact (cppolyCollision): a sphere at
+    rest overlapping one horizontal triangle by delta gets the Hertz force
+    kn delta^1.5 along the face normal (Req = r, kn = 4/3 Eeq sqrt(r)), and
+    the body the opposite reaction."""
+    from metakonga_gb300.layouts import POLYGON_MASS
+    sc = scenes.settle_box(n_side=1)
+    r, delta = 0.005, 1e-4
+    sc.pos[:] = (0.0, 0.0, r - delta, r)
+    sc.vel[:] = 0.0
+    sc.acc[:] = 0.0
+    sc.planes, sc.cp_planes, sc.plane_names = sc.planes[:0], sc.cp_planes[:0], []
+    tri = np.array([[[-0.01, -0.01, 0.0], [0.01, -0.01, 0.0], [0.0, 0.01, 0.0]]])
+    sc.poly, sc.sphere, sc.vlist = scenes._mesh_arrays(tri)
+    sc.pmi = np.zeros(1, dtype=POLYGON_MASS)
+    sc.pmi["ep"] = (1.0, 0.0, 0.0, 0.0)
+    sc.cp_poly = sc.cp_pp.reshape(1).copy()
+    sc.params["cell_size"] = 0.025
+    oracle.run(sc, 1, cpu_path=True)
+    cp = sc.cp_poly[0]
+    eeq = cp["Ei"] * cp["Ej"] / (cp["Ei"] * (1 - cp["prj"] ** 2) + cp["Ej"] * (1 - cp["pri"] ** 2))
+    fn = 4.0 / 3.0 * eeq * np.sqrt(r) * delta ** 1.5
+    m = sc.mass[0]
+    np.testing.assert_allclose(sc.acc[0], (0.0, 0.0, fn / m - 9.81), rtol=1e-12, atol=1e-9)
+    np.testing.assert_allclose(sc.pmi["force"][0], (0.0, 0.0, -fn), rtol=1e-12, atol=1e-12 * fn)
+
+
 def test_struct_layouts(oracle):
     expect = {"params": 112, "plane": 232, "polygon": 152, "polygon_mass": 160,
               "contact_property": 88}

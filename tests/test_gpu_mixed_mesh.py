@@ -4,10 +4,11 @@ The drum case presses spheres against a coarse cylinder mesh (face, edge and
 vertex contacts); the hopper case presses them against a 4,096-triangle cone
 above a plane floor.  Gates: particle pair lists equal the oracle's; per-particle
 contact force (pairs + triangles) within 2e-5 of max(sum_c |F_c|, m g), the sum
-over every contact of the particle, triangles included; the
-reaction on the polygon body after one step within 1e-9 of its scale (the
-triangle contacts are FP64 in both); a mesh moved by xd_scene_set_bodies is
-seen at its new pose."""
+over every contact of the particle, triangles included; the reaction on the
+polygon body after one step within 1e-6 of its scale (the mixed form's
+triangle forces are FP32, each within about 1e-7 of the FP64 force; the
+reaction is their sum); a mesh moved by xd_scene_set_bodies is seen at its
+new pose."""
 import numpy as np
 import pytest
 
@@ -84,7 +85,7 @@ def test_mixed_hopper_pairs_and_forces(cuda, oracle):
 
 def test_mixed_drum_body_reaction_one_step(cuda, oracle):
     """One step from the uploaded state: the reaction added to the body equals
-    the oracle step's (the triangle contacts are FP64 in both forms)."""
+    the oracle step's within 1e-6 of its scale (FP32 triangle forces summed)."""
     sc = small_drum()
     sc.pmi["force"] = 0
     sc.pmi["moment"] = 0
@@ -99,8 +100,8 @@ def test_mixed_drum_body_reaction_one_step(cuda, oracle):
     fs = np.abs(ref.pmi["force"]).max()
     ms = np.abs(ref.pmi["moment"]).max()
     assert fs > 0
-    assert np.abs(got["force"] - ref.pmi["force"]).max() <= 1e-9 * fs
-    assert np.abs(got["moment"] - ref.pmi["moment"]).max() <= 1e-9 * ms
+    assert np.abs(got["force"] - ref.pmi["force"]).max() <= 1e-6 * fs
+    assert np.abs(got["moment"] - ref.pmi["moment"]).max() <= 1e-6 * ms
 
 
 def test_mixed_mesh_follows_set_bodies(cuda, oracle):

@@ -14,12 +14,16 @@ pytestmark = pytest.mark.gpu
 
 
 def _state_err(got, ref, mass):
+    """Relative state errors; "force" is the last step's force m a (the
+    velocity update stores a = F / m and resets F to m g, as the reference's
+    kernel does, so the force arrays themselves hold m g after a step)."""
     out = {}
     for k in ("pos", "vel", "omega"):
         a, b = np.asarray(got[k]), np.asarray(ref[k])
         scale = np.abs(b).max() + 1e-300
         out[k] = float(np.abs(a - b).max() / scale)
-    out["force"] = force_error(got["force"], ref["force"], mass)
+    m = np.asarray(mass)[:, None]
+    out["force"] = force_error(np.asarray(got["acc"]) * m, np.asarray(ref["acc"]) * m, mass)
     return out
 
 

@@ -6,7 +6,9 @@ or a process held to a fixed memory budget): its sort scratch is a fixed
 device array inside libxdem.  The test calls it through the C ABI twice in a
 row, on different inputs, and checks each result bit for bit against the
 ordinary entry point (integer results, so the tolerance is zero); then it
-checks the size limit.  This file is collected last so that a run stopping at
+checks the size limit, and that a later call leaves the device's free memory
+unchanged (under lazy module loading the first call on a device is the one
+that brings in the fixed array).  This file is collected last so that a run stopping at
 the first failure has already run every other test; it also passes alone.
 """
 import numpy as np
@@ -77,3 +79,27 @@ def test_noalloc_rejects_more_than_the_maximum():
         call("xd_reorder_and_find_cell_start_noalloc", ptr(h), ptr(ix), ptr(cs), ptr(ce), ptr(so), n,
              ncell, dem.stream_handle())
     assert ei.value.status == 4 and "maximum" in str(ei.value)
+
+
+def test_noalloc_later_call_takes_no_device_memory():
+    """After a set-up call with n = 0, a full-size call changes nothing in the
+    device's free memory: the scratch is the fixed array, not an allocation."""
+    n, ncell = 500_000, 128 ** 3
+    h, ix = _hashes(n, 3, ncell)
+    cs = torch.zeros(ncell, dtype=torch.int32, device="cuda")
+    ce = torch.zeros(ncell, dtype=torch.int32, device="cuda")
+    so = torch.zeros(n, dtype=torch.int32, device="cuda")
+    # the set-up call: no entries, only the cell arrays are cleared
+    call("xd_reorder_and_find_cell_start_noalloc", None, None, ptr(cs), ptr(ce), None, 0, ncell,
+         dem.stream_handle())
+    torch.cuda.synchronize()
+    assert int((cs == -1).sum()) == ncell and int(ce.abs().sum()) == 0
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(2):
+        call("xd_reorder_and_find_cell_start_noalloc", ptr(h), ptr(ix), ptr(cs), ptr(ce), ptr(so), n,
+             ncell, dem.stream_handle())
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 == free0, (free0, free1)
+    # sorted_index is a permutation of the entries' indices
+    assert torch.equal(torch.sort(so).values, torch.arange(n, device="cuda", dtype=torch.int32))
