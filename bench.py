@@ -103,6 +103,7 @@ def _args():
     ap.add_argument("--rate", type=float, default=4.0, help="served arrivals per second")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="served device-memory budget")
     ap.add_argument("--chunk", type=int, default=50, help="served steps per scene per tick")
+    ap.add_argument("--rates", default="", help="served: comma-separated arrival rates to sweep")
     return ap.parse_args()
 
 
@@ -717,9 +718,28 @@ def _settle_small(stream, steps=1000, cpu=True):
     return out
 
 
+def _serve_once(scs, reqs, rate, a, stream, mode):
+    """One served run of the request stream at `rate` arrivals per second;
+    mode "cohorts" (batches per admission wave) or "side_by_side"."""
+    from metakonga_gb300 import serve
+    arrivals = serve.poisson_arrivals(len(reqs), rate, seed=5)
+    srv = serve.Server(budget_bytes=int(a.budget_gb * 1e9), chunk=a.chunk, stream=stream.cuda_stream,
+                       keep_results=True, cohorts=(mode == "cohorts"))
+    for k, (r, sc) in enumerate(zip(reqs, scs)):
+        srv.submit(k, sc, r["steps"], arrival=float(arrivals[k]))
+    srv.run()
+    rep = srv.report()
+    return {"rate_per_s": rate, "mode": mode, "offered_particle_steps_per_s": rep["offered_particle_steps_per_s"],
+            "particle_steps_per_s": rep["particle_steps_per_s"], "p50_ms": rep["p50_ms"], "p99_ms": rep["p99_ms"],
+            "p99_wait_ms": rep["p99_wait_ms"], "peak_active": rep["peak_active"],
+            "batched_ticks": rep["batched_ticks"], "batches_made": rep["batches_made"], "ticks": rep["ticks"]}
+
+
 def _served(a, stream, plain=True):
-    """The served request stream: report of the continuous-batching server,
-    and the same requests' time alone in the FP64 form."""
+    """The served request stream: report of the continuous-batching server
+    (cohorts), the same stream served side by side, a sweep of arrival rates
+    when a.rates lists them, and the same requests' time alone in the FP64
+    form."""
     from metakonga_gb300 import scenes, serve
     t0 = time.perf_counter()
     reqs = scenes.served_requests(count=a.requests, seed=4)
@@ -727,7 +747,7 @@ def _served(a, stream, plain=True):
     gen_s = time.perf_counter() - t0
     arrivals = serve.poisson_arrivals(len(reqs), a.rate, seed=5)
     srv = serve.Server(budget_bytes=int(a.budget_gb * 1e9), chunk=a.chunk, stream=stream.cuda_stream,
-                       keep_results=True)
+                       keep_results=True, cohorts=True)
     for k, (r, sc) in enumerate(zip(reqs, scs)):
         srv.submit(k, sc, r["steps"], arrival=float(arrivals[k]))
     clk = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
@@ -743,7 +763,11 @@ def _served(a, stream, plain=True):
     rep["steps"] = [int(r["steps"]) for r in reqs]
     rep["kinds"] = [r["kind"] for r in reqs]
     rep["e2e_note"] = ("latency from arrival to the downloaded result: scene upload, steps and "
-                       "download through the public API (DeviceScene, engine.step_many)")
+                       "download through the public API (DeviceScene, engine.Batch per cohort)")
+    rep["side_by_side"] = _serve_once(scs, reqs, a.rate, a, stream, "side_by_side")
+    if a.rates:
+        rep["sweep"] = [_serve_once(scs, reqs, float(x), a, stream, m)
+                        for x in a.rates.split(",") for m in ("cohorts", "side_by_side")]
     if plain:
         per = _fp64_alone(scs, 2, stream)
         alone_s = sum(r["steps"] * ms / 1e3 for r, ms in zip(reqs, per))

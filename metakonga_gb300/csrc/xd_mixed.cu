@@ -180,6 +180,7 @@ struct MixedScene {
     float4* pf = nullptr;
     longlong2* qa = nullptr;
     longlong2* qb = nullptr;
+    float4* pr = nullptr;         // quantisation residuals of x, y, z and r (metres)
     float4* Fc = nullptr;
     float4* Mc = nullptr;
     // Verlet lists (slots of the current cell order, rebuilt with the cells)
@@ -528,14 +529,30 @@ __device__ __forceinline__ float q_to_f(long long q)
                      __fmul_rn(__int2float_rn((int)(q & 0xfffff)), 0x1p-36f));
 }
 
+// The quantisation residual x - (wo + q 2^-36) in metres of a fixed-point
+// coordinate formed as t = fma(x, 2^36, off): the FMA's rounding error,
+// recovered by a second FMA (off - t is exact: both lie in [2^52, 2^53)).
+__device__ __forceinline__ float fixed_residual(double x, double off, long long q)
+{
+    const double t = __longlong_as_double(q + __double_as_longlong(kMagic));
+    return (float)__fma_rn(x, kQ, off - t) * 0x1p-36f;
+}
+
+// The contact view of slot i: FP32 position and radius (pf), the int64 fixed
+// point (qa, qb) that decides contacts exactly, and the residuals of the
+// fixed point (pr) that restore the FP64 positions' overlap and normal to
+// about 1e-18 m in the force.
 __device__ __forceinline__ float4 write_view(const MixParams& P, unsigned i, double x, double y,
                                              double z, double r, float4* __restrict__ pf,
-                                             longlong2* __restrict__ qa, longlong2* __restrict__ qb)
+                                             longlong2* __restrict__ qa, longlong2* __restrict__ qb,
+                                             float4* __restrict__ pr)
 {
     const long long qx = fixed_q(x, P.qoff[0]), qy = fixed_q(y, P.qoff[1]), qz = fixed_q(z, P.qoff[2]);
     const long long qr = fixed_q(r, kMagic);
     qa[i] = make_longlong2(qx, qy);
     qb[i] = make_longlong2(qz, qr);
+    pr[i] = make_float4(fixed_residual(x, P.qoff[0], qx), fixed_residual(y, P.qoff[1], qy),
+                        fixed_residual(z, P.qoff[2], qz), fixed_residual(r, kMagic, qr));
     const float4 v = make_float4(q_to_f(qx), q_to_f(qy), q_to_f(qz), (float)r);
     pf[i] = v;
     return v;
@@ -674,7 +691,8 @@ template <int MODE>
 __device__ __forceinline__ bool advance_one(const MixParams& P, const Master& M, const float4* __restrict__ Fc,
                                             const float4* __restrict__ Mc, const float4* __restrict__ pref,
                                             float4* __restrict__ pf, longlong2* __restrict__ qa,
-                                            longlong2* __restrict__ qb, const unsigned i)
+                                            longlong2* __restrict__ qb, float4* __restrict__ pr,
+                                            const unsigned i)
 {
     double x = M.x[i], y = M.y[i], z = M.z[i];
     const double r = M.r[i];
@@ -698,7 +716,7 @@ __device__ __forceinline__ bool advance_one(const MixParams& P, const Master& M,
         M.y[i] = y;
         M.z[i] = z;
     }
-    const float4 v = write_view(P, i, x, y, z, r, pf, qa, qb);
+    const float4 v = write_view(P, i, x, y, z, r, pf, qa, qb, pr);
     const float4 r0 = pref[i];
     const float dx = v.x - r0.x, dy = v.y - r0.y, dz = v.z - r0.z;
     return !(dx * dx + dy * dy + dz * dz < P.disp2);
@@ -709,13 +727,13 @@ __global__ void __launch_bounds__(256) k_mx_advance(MixParams P, Master M, const
                                                     const float4* __restrict__ Mc,
                                                     const float4* __restrict__ pref,
                                                     float4* __restrict__ pf, longlong2* __restrict__ qa,
-                                                    longlong2* __restrict__ qb,
+                                                    longlong2* __restrict__ qb, float4* __restrict__ pr,
                                                     unsigned* __restrict__ counters,
                                                     cudaGraphConditionalHandle cond, int use_cond)
 {
     __shared__ bool last;
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool out = i < P.n && advance_one<MODE>(P, M, Fc, Mc, pref, pf, qa, qb, i);
+    const bool out = i < P.n && advance_one<MODE>(P, M, Fc, Mc, pref, pf, qa, qb, pr, i);
     // only the flag must be visible to the last block: the lanes that set it
     // fence; the state and view writes need no ordering here
     if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31u) == 0) {
@@ -768,7 +786,7 @@ __global__ void __launch_bounds__(256) k_mx_permute(MixParams P, Master S, Maste
 // Re-binning, 3: back into the state arrays, with the contact view.
 __global__ void __launch_bounds__(256) k_mx_copyback(MixParams P, Master S, Master D,
                                                      float4* __restrict__ pf, longlong2* __restrict__ qa,
-                                                     longlong2* __restrict__ qb)
+                                                     longlong2* __restrict__ qb, float4* __restrict__ pr)
 {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
@@ -783,7 +801,7 @@ __global__ void __launch_bounds__(256) k_mx_copyback(MixParams P, Master S, Mast
     D.wl[i] = S.wl[i];
     D.ab[i] = S.ab[i];
     D.b2[i] = S.b2[i];
-    write_view(P, i, x, y, z, r, pf, qa, qb);
+    write_view(P, i, x, y, z, r, pf, qa, qb, pr);
 }
 
 // MODE 2: velocity only, in place (the last step of a call).
@@ -1297,6 +1315,7 @@ struct Own {
     f3 w;
     float r, im;   // radius, 1/m
     float wfloor;  // m g: the smallest force scale of the particle's contacts
+    float4 pr;     // residuals of its fixed-point position and radius (metres)
 };
 
 // When an FP32 contact force term is re-formed in FP64.  The per-particle
@@ -1339,6 +1358,7 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
                                               const float4* __restrict__ pf,
                                               const longlong2* __restrict__ qa,
                                               const longlong2* __restrict__ qb,
+                                              const float4* __restrict__ pr,
                                               unsigned* __restrict__ counters, PairAcc& A,
                                               const HistTable& ht, HistState& hs)
 {
@@ -1357,6 +1377,13 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     }
     const float inv = 1.0f / dn;
     const f3 u = fk((float)ddx * inv, (float)ddy * inv, (float)ddz * inv);
+    // The fixed point's residuals restore the FP64 positions: the overlap
+    // gains (e_ri + e_rj) - u . (e_j - e_i) (the 2^-36 m grid alone would move
+    // a light contact's overlap by up to ~3e-11 m, a part in 1e5 of 3e-6 m)
+    const float4 ej = __ldg(pr + j);
+    const f3 de = fk(ej.x - I.pr.x, ej.y - I.pr.y, ej.z - I.pr.z);
+    const float ude = fdot(u, de);
+    if (!guard) delta += (I.pr.w + ej.w) - ude;
     const float4 vj4 = __ldg(M.vh + j), vjl = __ldg(M.vl + j), wj4 = __ldg(M.wh + j);
     const f3 wj = fk(wj4.x, wj4.y, wj4.z);
     const float jr = __ldg(pf + j).w, jim = vj4.w;
@@ -1373,7 +1400,13 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     // rv . u = dv . u (the rotation term is perpendicular to u), in double-float
     const int dqi[3] = { (int)ddx, (int)ddy, (int)ddz };
     float rq0, rq1, rqc;
-    const float rvu = normal_speed(dvs, dvt, dqi, dn, D2, rq0, rq1, rqc);
+    float rvu = normal_speed(dvs, dvt, dqi, dn, D2, rq0, rq1, rqc);
+    {
+        // and the normal's turn (de - (u . de) u) / |d| in the normal speed
+        const float cr = (fdot(dv, de) - rvu * ude) * (inv * (1.0f / kU));
+        rq1 += cr;
+        rvu = rq0 + rq1;
+    }
     f3 ev = rv - rvu * u;
     float ee = fdot(ev, ev);
     // getConstant, TCM = 1 (impl:238-246)
@@ -1481,6 +1514,7 @@ struct ContactArgs {
     const float4* pf;
     const longlong2* qa;
     const longlong2* qb;
+    const float4* pr;
     const unsigned* keys;
     const unsigned* lb;
     const unsigned* vcount;
@@ -1778,9 +1812,10 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
             I.w = fk(w4.x, w4.y, w4.z);
             I.im = I.vh.w;
             I.wfloor = sqrtf(P.gf[0] * P.gf[0] + P.gf[1] * P.gf[1] + P.gf[2] * P.gf[2]) / I.im;
+            I.pr = __ldg(C.pr + i);
             have_v = true;
         }
-        contact_force<HIST>(P, M, I, j, guard, mass0, pf, qa, qb, counters, A, ht, hs);
+        contact_force<HIST>(P, M, I, j, guard, mass0, pf, qa, qb, C.pr, counters, A, ht, hs);
         if (RECORD && nc < rec_cap) rec_pairs[(size_t)i * rec_cap + nc] = j;
         ++nc;
     };
@@ -2065,7 +2100,8 @@ __global__ void __launch_bounds__(256) k_mx_load(MixParams P, Master M, const do
                                                  const double* __restrict__ mass,
                                                  const double* __restrict__ inertia,
                                                  double* __restrict__ mass0, float4* __restrict__ pf,
-                                                 longlong2* __restrict__ qa, longlong2* __restrict__ qb)
+                                                 longlong2* __restrict__ qa, longlong2* __restrict__ qb,
+                                                 float4* __restrict__ pr)
 {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
@@ -2093,7 +2129,7 @@ __global__ void __launch_bounds__(256) k_mx_load(MixParams P, Master M, const do
     M.ab[i] = make_float4((float)(acc[i3 + 0] - P.g[0]), (float)(acc[i3 + 1] - P.g[1]),
                           (float)(acc[i3 + 2] - P.g[2]), (float)alpha[i3 + 0]);
     M.b2[i] = make_float2((float)alpha[i3 + 1], (float)alpha[i3 + 2]);
-    write_view(P, i, x, y, z, r, pf, qa, qb);
+    write_view(P, i, x, y, z, r, pf, qa, qb, pr);
 }
 
 __global__ void __launch_bounds__(256) k_mx_store(MixParams P, Master M, const double* __restrict__ mass0,
@@ -2351,6 +2387,7 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     A(alloc(s, &s->pf, n));
     A(alloc(s, &s->qa, n));
     A(alloc(s, &s->qb, n));
+    A(alloc(s, &s->pr, n));
     A(alloc(s, &s->Fc, n));
     A(alloc(s, &s->Mc, n));
     A(alloc(s, &s->hlist, n));
@@ -2558,7 +2595,7 @@ int mixed_upload(MixedScene* s, const double* pos, const double* vel, const doub
     MixParams Pc = s->P;
     Pc.n = s->cap;
     k_mx_load<<<blocks(s->cap, 256), 256, 0, q>>>(Pc, s->m[0], dpos, dvel, dacc, dom, dal, dm, dI,
-                                                  s->mass0, s->pf, s->qa, s->qb);
+                                                  s->mass0, s->pf, s->qa, s->qb, s->pr);
     st = launch_status("mixed upload");
     if (st == XD_OK && sync) st = cuda_status(cudaStreamSynchronize(q), "mixed upload");
     return st;
@@ -2694,7 +2731,7 @@ static int restore_id_order(MixedScene* s, cudaStream_t q)
     Pc.n = cap;
     k_mx_inverse<<<blocks(cap, 256), 256, 0, q>>>(cap, s->m[0], s->vals);
     k_mx_permute<<<blocks(cap, 256), 256, 0, q>>>(Pc, s->m[0], s->m[1], s->vals);
-    k_mx_copyback<<<blocks(cap, 256), 256, 0, q>>>(Pc, s->m[1], s->m[0], s->pf, s->qa, s->qb);
+    k_mx_copyback<<<blocks(cap, 256), 256, 0, q>>>(Pc, s->m[1], s->m[0], s->pf, s->qa, s->qb, s->pr);
     st = launch_status("mixed id order");
     if (st == XD_OK && s->hslots) st = permute_history(s, cap, s->vals, q);
     s->cells_clean = false;
@@ -2726,7 +2763,7 @@ static int rebuild(MixedScene* s, cudaStream_t q)
     st = radix_sort_pairs(s->keys, s->vals, n, key_bits_for(s->ncell), s->sort_scratch, q, &sk, &sv);
     if (st != XD_OK) return st;
     k_mx_permute<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[0], s->m[1], sv);
-    k_mx_copyback<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[1], s->m[0], s->pf, s->qa, s->qb);
+    k_mx_copyback<<<blocks(n, 256), 256, 0, q>>>(s->P, s->m[1], s->m[0], s->pf, s->qa, s->qb, s->pr);
     if (s->hslots) {
         st = permute_history(s, n, sv, q);
         if (st != XD_OK) return st;
@@ -2818,6 +2855,7 @@ static ContactArgs contact_args(MixedScene* s, unsigned* rc, unsigned* rp, unsig
     C.pf = s->pf;
     C.qa = s->qa;
     C.qb = s->qb;
+    C.pr = s->pr;
     C.keys = s->prev_keys;
     C.lb = s->lb;
     C.vcount = s->vcount;
@@ -2864,7 +2902,7 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
         if (st != XD_OK) return st;
     }
     ph.begin(0, q);
-    k_mx_advance<MODE><<<blocks(n, 256), 256, 0, q>>>(s->P, M, s->Fc, s->Mc, s->pref, s->pf, s->qa, s->qb,
+    k_mx_advance<MODE><<<blocks(n, 256), 256, 0, q>>>(s->P, M, s->Fc, s->Mc, s->pref, s->pf, s->qa, s->qb, s->pr,
                                                       s->counters, cond ? *cond : 0, cond ? 1 : 0);
     st = launch_status("mixed advance");
     ph.end(0, q);
@@ -3376,6 +3414,7 @@ struct BatchScene {
     float4* pf;
     longlong2* qa;
     longlong2* qb;
+    float4* pr;
     unsigned adv_block0;   // first block of this scene in the advance grid
 };
 
@@ -3408,7 +3447,7 @@ __global__ void __launch_bounds__(256) k_batch_advance(const BatchScene* __restr
         if (i < sP.n) finish_one(sP, d.C.M, d.C.Fc, d.C.Mc, i);
         return;
     }
-    const bool out = i < sP.n && advance_one<MODE>(sP, d.C.M, d.C.Fc, d.C.Mc, d.pref, d.pf, d.qa, d.qb, i);
+    const bool out = i < sP.n && advance_one<MODE>(sP, d.C.M, d.C.Fc, d.C.Mc, d.pref, d.pf, d.qa, d.qb, d.pr, i);
     if (__any_sync(0xffffffffu, out) && (threadIdx.x & 31u) == 0) atomicOr(d.C.counters + CN_REBUILD, 1u);
 }
 
@@ -3735,6 +3774,7 @@ int prepare_batch(MixedBatch* b)
         d.pf = sc->pf;
         d.qa = sc->qa;
         d.qb = sc->qb;
+        d.pr = sc->pr;
         d.adv_block0 = (unsigned)block_scene.size();
         block_scene.insert(block_scene.end(), blocks(sc->n, 256), k);
     }

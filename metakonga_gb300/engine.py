@@ -112,6 +112,26 @@ class DeviceScene:
                                                   "moment")], stream)
         return out
 
+    def download_async(self, stream: int = 0):
+        """Queue the state's download on `stream` into pinned host memory, in
+        stream order (a later step on the stream cannot change what it
+        copies); returns a function that, once the stream has passed the
+        copy, gives the state as download() does."""
+        import torch
+        n = self.np
+        shapes = (("pos", 4), ("vel", 3), ("acc", 3), ("omega", 3), ("alpha", 3))
+        block = torch.empty(16 * n, dtype=torch.float64).pin_memory()
+        views, off = {}, 0
+        for k, w in shapes:
+            views[k] = block[off:off + w * n]
+            off += w * n
+        call("xd_scene_download_async", self.handle, *[views[k].data_ptr() for k, _ in shapes], None, None,
+             stream)
+
+        def result():
+            return {k: views[k].numpy().reshape(n, w).copy() for k, w in shapes}
+        return result
+
     def device_state(self) -> dict:
         ptrs = [C.c_void_p() for _ in range(9)]
         call("xd_scene_device_state", self.handle, *[C.addressof(p) for p in ptrs])

@@ -90,6 +90,19 @@ class Request:
     handle: object = None
     result: dict = None
     error: str = None                    # why the request failed (it is then not stepped further)
+    fetch: object = None                 # cohorts: gives the result once its download has run
+    held: bool = False                   # cohorts: finished, but its scene is still in a cohort's batch
+
+
+class _Cohort:
+    """Requests admitted together and stepped as one batch.  A member that
+    finishes has its state downloaded in stream order and stays in the batch
+    (stepped on, its result already taken) until enough of the cohort has
+    finished to make a new batch worth its capture."""
+
+    def __init__(self, reqs):
+        self.reqs = list(reqs)
+        self.batch = None                # engine.Batch, None (not made yet) or False (not batchable)
 
 
 class _CudaMarks:
@@ -128,11 +141,20 @@ class Server:
     the device and captures its graphs; with a few resident scenes whose set
     changes every few ticks that costs more than it saves (measured on the
     served stream of the bench: p50 latency 1.43 s batched against 1.02 s),
-    so it is off by default."""
+    so it is off by default.
+    cohorts: the requests admitted in one tick form a cohort stepped as one
+    engine.Batch for as long as it lives: each tick advances a cohort by the
+    chunk or up to its next member's last step, a finished member's state is
+    downloaded in stream order and the member rides along until more than
+    `dead_fraction` of the cohort's particles have finished (then the cohort
+    is made again from its live members); more than `max_cohorts` cohorts
+    are merged into one.  Batches are then made per admission wave and per
+    re-forming, not per change of the resident set."""
 
     def __init__(self, budget_bytes: int, chunk: int = 20, mode: int = engine.MODE_MIXED,
                  stream: int = 0, keep_results: bool = True, clock=time.perf_counter, depth: int = 2,
-                 marks=None, batch: bool = False):
+                 marks=None, batch: bool = False, cohorts: bool = False, max_cohorts: int = 4,
+                 dead_fraction: float = 0.5):
         if chunk < 1:
             raise ValueError("chunk must be >= 1")
         if depth < 0:
@@ -158,6 +180,11 @@ class Server:
         self._batch = None
         self._batch_key = None
         self.batched_ticks = 0
+        self.use_cohorts = cohorts
+        self.max_cohorts = int(max_cohorts)
+        self.dead_fraction = float(dead_fraction)
+        self._cohorts: list = []
+        self.batches_made = 0
 
     def _drop_batch(self) -> None:
         if self._batch is not None:
@@ -181,6 +208,76 @@ class Server:
                 self.batched_ticks += 1
                 return
         engine.step_many(handles, counts, check=False, stream=self.stream)
+
+    # ---- cohorts ---------------------------------------------------------
+
+    def _tick_cohorts(self) -> list:
+        """One tick of every cohort; returns the requests that finished."""
+        fin = []
+        for c in self._cohorts:
+            live = [r for r in c.reqs if r.remaining > 0]
+            if not live:
+                continue
+            k = min(self.chunk, min(r.remaining for r in live))
+            if c.batch is None and len(c.reqs) > 1:
+                try:
+                    c.batch = engine.Batch([r.handle for r in c.reqs])
+                    self.batches_made += 1
+                except Exception:
+                    c.batch = False   # not batchable (history, kinematics, FP64 form)
+            if c.batch:
+                c.batch.step(k, check=False, stream=self.stream)
+                self.batched_ticks += 1
+            else:
+                engine.step_many([r.handle for r in live], [k] * len(live), check=False, stream=self.stream)
+            for r in live:
+                r.remaining -= k
+                if r.remaining == 0:
+                    fin.append(r)
+                    if self.keep_results:
+                        r.fetch = r.handle.download_async(self.stream)
+                    r.held = bool(c.batch)
+        return fin
+
+    def _reform_cohorts(self, force: bool = False) -> None:
+        """Cohorts whose finished members hold more than dead_fraction of
+        their particles (all of them with force) are made again from their
+        live members; more than max_cohorts are merged into one.  Closing a
+        batch waits for its queued steps; the finished members' scenes are
+        then free to close."""
+        keep = []
+        for c in self._cohorts:
+            dead = [r for r in c.reqs if r.remaining == 0]
+            live = [r for r in c.reqs if r.remaining > 0]
+            if dead:
+                n_dead = sum(r.scene.np_ for r in dead)
+                n_all = sum(r.scene.np_ for r in c.reqs)
+                if force or not live or not c.batch or n_dead > self.dead_fraction * n_all:
+                    if c.batch:
+                        c.batch.close()
+                    c.batch = None
+                    for r in dead:
+                        r.held = False
+                    c.reqs = live
+            if c.reqs:
+                keep.append(c)
+        if len(keep) > self.max_cohorts:
+            for c in keep:
+                if c.batch:
+                    c.batch.close()
+                for r in c.reqs:
+                    if r.remaining == 0:
+                        r.held = False
+            keep = [_Cohort([r for c in keep for r in c.reqs if r.remaining > 0])]
+        self._cohorts = keep
+
+    def _close_cohorts(self) -> None:
+        for c in self._cohorts:
+            if c.batch:
+                c.batch.close()
+            for r in c.reqs:
+                r.held = False
+        self._cohorts = []
 
     def submit(self, rid, scene, steps: int, arrival: float = 0.0) -> None:
         if steps < 1:
@@ -227,7 +324,8 @@ class Server:
             marks.wait(mark)
             for r in fin:
                 if self.keep_results:
-                    r.result = r.handle.download(marks.side_after(mark))
+                    r.result = r.fetch() if r.fetch is not None else r.handle.download(marks.side_after(mark))
+                    r.fetch = None
                     # a state that blew up (non-finite positions or velocities)
                     # is reported as failed, the other requests unaffected
                     if not all(np.isfinite(r.result[k]).all() for k in ("pos", "vel") if k in r.result):
@@ -241,38 +339,53 @@ class Server:
             while inflight:
                 retire_one()
             self._drop_batch()   # before any of its scenes
+            held = [r for r in to_close if r.held]   # still inside a cohort's batch
             for r in to_close:
+                if r.held:
+                    continue
                 r.handle.close()
                 r.handle = None
                 self.used -= r.bytes
-            to_close.clear()
+            to_close[:] = held
 
         while self.pending or active or inflight:
             now = self.clock() - t0
+            n_before = len(active)
             self._admit(now, active, t0)
+            if self.use_cohorts and len(active) > n_before:
+                self._cohorts.append(_Cohort(active[n_before:]))
             blocked = bool(self.pending and self.pending[0].arrival <= now
                            and not self._fits(self.pending[0], active))
             if blocked and to_close:
+                if any(r.held for r in to_close):
+                    self._reform_cohorts(force=True)   # their memory is needed now
                 close_finished()
                 continue
             if active:
                 self.peak_active = max(self.peak_active, len(active))
-                counts = [min(self.chunk, r.remaining) for r in active]
-                self._step(active, counts)
+                if self.use_cohorts:
+                    fin = self._tick_cohorts()
+                    active = [r for r in active if r.remaining > 0]
+                    self._reform_cohorts()
+                else:
+                    counts = [min(self.chunk, r.remaining) for r in active]
+                    self._step(active, counts)
+                    fin, still = [], []
+                    for r, c in zip(active, counts):
+                        r.remaining -= c
+                        (still if r.remaining else fin).append(r)
+                    active = still
                 self.ticks += 1
-                fin, still = [], []
-                for r, c in zip(active, counts):
-                    r.remaining -= c
-                    (still if r.remaining else fin).append(r)
-                active = still
                 inflight.append((marks.mark(), fin))
             while inflight and (len(inflight) > self.depth or not active):
                 retire_one()
             if not active and not inflight:
+                self._close_cohorts()
                 if to_close:
                     close_finished()
                 if self.pending:
                     time.sleep(max(0.0, self.pending[0].arrival - (self.clock() - t0)))
+        self._close_cohorts()
         close_finished()
         self._drop_batch()
         self.wall = self.clock() - t0
@@ -296,7 +409,8 @@ class Server:
                 "offered_particle_steps_per_s": work / span if span > 0 else None,
                 "failed_admission": len(self.failed),
                 "non_finite": sum(1 for r in self.finished if r.error),
-                "ticks": self.ticks, "batched_ticks": self.batched_ticks, "peak_active": self.peak_active,
+                "ticks": self.ticks, "batched_ticks": self.batched_ticks, "batches_made": self.batches_made,
+                "peak_active": self.peak_active,
                 "peak_booked_bytes": self.peak_used}
 
 

@@ -27,6 +27,11 @@ class _FakeScene:
             out["pos"] = np.array([[0.0, float("nan"), 0.0, 1.0]])
         return out
 
+    def download_async(self, stream=0):
+        # the copy is queued in stream order: it sees the steps issued so far
+        snap = self.download(stream)
+        return lambda: snap
+
     def close(self):
         # a scene is never freed while a batch holding it is alive
         assert not any(self in b.handles for b in _FakeScene.batches if not b.closed)
@@ -277,3 +282,50 @@ def test_failed_requests_leave_the_others_alone(fake):
     rep = srv.report()
     assert rep["failed_admission"] == 1 and rep["non_finite"] == 1 and rep["requests"] == 2
     assert _FakeScene.live == 0
+
+
+def test_cohorts_batch_per_admission_wave(fake):
+    """Requests admitted together form one cohort stepped as one batch; a
+    member that finishes keeps its result (taken in stream order) while it
+    rides along, and the batch is made once for the cohort's life."""
+    clock, calls = fake
+    srv = serve.Server(budget_bytes=1 << 40, chunk=4, clock=clock, marks=_Marks(), depth=0, cohorts=True)
+    srv.submit("a", _named("a"), 12)
+    srv.submit("b", _named("b"), 6)
+    done = srv.run()
+    assert {r.rid: r.result["steps"] for r in done} == {"a": 12, "b": 6}
+    # ticks of 4, 2 (b ends), 4, 2 (a ends), all through the cohort's batch
+    assert [c[0][1] for c in calls] == [4, 2, 4, 2]
+    assert all(len(c) == 2 for c in calls)
+    rep = srv.report()
+    assert rep["batches_made"] == 1 and rep["batched_ticks"] == 4
+    assert all(b.closed for b in _FakeScene.batches) and _FakeScene.live == 0 and srv.used == 0
+
+
+def test_cohorts_waves_and_merging(fake):
+    """Late arrivals form cohorts of their own; past max_cohorts the live
+    members are merged into one cohort (one new batch)."""
+    clock, calls = fake
+    srv = serve.Server(budget_bytes=1 << 40, chunk=2, clock=clock, marks=_Marks(), depth=0, cohorts=True,
+                       max_cohorts=2)
+    for k, t in enumerate((0.0, 0.0, 0.0025, 0.0025, 0.0045, 0.0045)):
+        srv.submit(f"r{k}", _named(f"r{k}"), 12, arrival=t)
+    done = srv.run()
+    assert sorted(r.result["steps"] for r in done) == [12] * 6
+    # three waves of two; the third wave pushes the count past 2 and merges
+    assert any(len(b.handles) > 2 for b in _FakeScene.batches)
+    assert all(b.closed for b in _FakeScene.batches) and _FakeScene.live == 0
+
+
+def test_cohort_members_free_their_memory_when_needed(fake):
+    """A finished member held in a cohort's batch gives its memory back when
+    the next request needs it."""
+    clock, calls = fake
+    one = serve.estimate_device_bytes(_named("a"))
+    srv = serve.Server(budget_bytes=int(2.5 * one), chunk=2, clock=clock, marks=_Marks(), depth=0, cohorts=True)
+    srv.submit("a", _named("a"), 20)
+    srv.submit("b", _named("b"), 2)
+    srv.submit("c", _named("c"), 4, arrival=0.0015)
+    done = srv.run()
+    assert {r.rid: r.result["steps"] for r in done} == {"a": 20, "b": 2, "c": 4}
+    assert srv.peak_used <= int(2.5 * one) and _FakeScene.live == 0

@@ -64,14 +64,15 @@ def test_step_many_in_chunks_equals_one_call(cuda):
         d.close()
 
 
-@pytest.mark.parametrize("batch", [False, True])
+@pytest.mark.parametrize("batch", [False, True, "cohorts"])
 def test_served_results_equal_alone(cuda, batch):
-    """Served side by side (step_many) or as batches of the resident set: the
+    """Served side by side (step_many), as batches of the resident set, or as
+    cohorts (finished members riding along in their cohort's batch): the
     results are the scenes' own."""
     mix = _mix()
     steps = [23, 17, 30]
     ref = [_alone(sc, s, engine.MODE_MIXED) for sc, s in zip(mix, steps)]
-    srv = serve.Server(budget_bytes=1 << 34, chunk=7, batch=batch)
+    srv = serve.Server(budget_bytes=1 << 34, chunk=7, batch=batch is True, cohorts=batch == "cohorts")
     for k, (sc, s) in enumerate(zip(mix, steps)):
         srv.submit(k, sc, s, arrival=0.0)
     done = srv.run()
@@ -81,7 +82,7 @@ def test_served_results_equal_alone(cuda, batch):
     rep = srv.report()
     assert rep["requests"] == 3 and rep["p99_ms"] >= rep["p50_ms"] > 0
     assert rep["peak_active"] == 3
-    assert (rep["batched_ticks"] > 0) == batch
+    assert (rep["batched_ticks"] > 0) == bool(batch)
 
 
 def test_memory_estimate_bounds_the_allocation(cuda):
