@@ -79,6 +79,15 @@ __global__ void __launch_bounds__(256) k_cell_bounds(const unsigned* __restrict_
     if (id == n - 1) cend[h] = id + 1;
 }
 
+int launch_cell_bounds_sorted(unsigned* hash, unsigned* index, unsigned* cstart, unsigned* cend,
+                              unsigned* sorted_index, unsigned n, unsigned ncell, unsigned* err, cudaStream_t s)
+{
+    if (n == 0) return XD_OK;
+    k_cell_bounds<<<div_up(n, 256), 256, 0, s>>>(hash, index, hash, index, cstart, cend, sorted_index, n, ncell,
+                                                 err);
+    return launch_status("cell bounds");
+}
+
 unsigned key_bits_for(unsigned ncell)
 {
     unsigned bits = 0;

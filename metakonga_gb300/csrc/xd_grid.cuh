@@ -15,6 +15,11 @@ struct HistTable;   // xd_physics64.cuh: tangential-spring history of a scene
 int launch_hash(const Params& P, unsigned* hash, unsigned* index, const double* pos, unsigned n,
                 unsigned sid, cudaStream_t s);
 int launch_fill_cells(unsigned* cstart, unsigned* cend, unsigned ncell, cudaStream_t s);
+// The cell ranges of n keys already sorted in hash (with their values in
+// index): cstart/cend at the runs' ends, sorted_index = index; a key >= ncell
+// is skipped and raises *err.  Cells without keys are left as they are.
+int launch_cell_bounds_sorted(unsigned* hash, unsigned* index, unsigned* cstart, unsigned* cend,
+                              unsigned* sorted_index, unsigned n, unsigned ncell, unsigned* err, cudaStream_t s);
 int reorder_and_find_cell_start(unsigned* hash, unsigned* index, unsigned* cstart, unsigned* cend,
                                 unsigned* sorted_index, unsigned n, unsigned ncell, void* scratch,
                                 cudaStream_t s, bool check);

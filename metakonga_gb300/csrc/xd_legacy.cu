@@ -1,21 +1,32 @@
 // The legacy DEM interface of the reference (include/cu_dem_dec.cuh,
-// launchers source/cu_dem_def.cu, kernels include/cu_dem_impl.cuh), restated
-// for the parSIM classes that call it.  See include/xdem_legacy.h for the
-// layouts and the reference behaviour kept on purpose.
+// launchers source/cu_dem_def.cu, kernels include/cu_dem_impl.cuh) on this
+// library's own parts.  See include/xdem_legacy.h for the layouts and the
+// reference behaviour kept on purpose.
 //
-// Compiled with --fmad=false.  The vector helpers follow cu_dem_impl.cuh:10-72
-// (component-wise, left to right; vector / scalar multiplies by the
-// reciprocal), so each expression is evaluated as the reference writes it.
+// * Grid: the shared hash kernel and stable radix sort (the legacy hash call
+//   hashes the np + nsp rows of the merged array and sorts the first np), and
+//   the shared cell-range kernel over the sorted keys.
+// * Contacts: one warp per particle walks the particle's 27 cells in the
+//   reference's order (z, y, x), 32 candidates at a time, lane l taking the
+//   cell's entries l, l + 32, ...  The pair law is the shared DHS model
+//   (xd_physics64.cuh, with the legacy block's global kn, vn, ks, vs and mu),
+//   of which a legacy particle keeps the normal force and the shear force's
+//   moment; each lane sums its own contacts and the warp adds the lanes in a
+//   fixed shuffle tree (the reference sums in search order: the two orders
+//   differ in the last bits only).  The shape passes keep the first contact
+//   in search order, found by a ballot over the lanes.
+// * The shape call's force sum is the library's deterministic reduction.
+//
+// Compiled with --fmad=false.
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <cstdint>
-#include <cstring>
 #include <mutex>
 
 #include "../../include/xdem_legacy.h"
 #include "xd_grid.cuh"
 #include "xd_internal.cuh"
+#include "xd_physics64.cuh"
 
 static_assert(sizeof(xd_legacy_parameters) == 144, "legacy device_parameters layout");
 static_assert(sizeof(xd_legacy_plane_info) == 160, "legacy device_plane_info layout");
@@ -25,281 +36,230 @@ static_assert(sizeof(xd_legacy_mass_info) == 48, "cu_mass_info layout");
 namespace xd {
 namespace {
 
-std::mutex g_l_mu;
-bool g_have_l = false;
-xd_legacy_parameters g_l;
+std::mutex g_legacy_mu;
+bool g_legacy_set = false;
+xd_legacy_parameters g_legacy;
 
-struct LP {
-    unsigned np, nsp, ncell, gx, gy, gz;
-    double dt, half2dt, cs;
-    double g[3], wo[3];
-    double kn, vn, ks, vs, mu, coh;
+// The legacy block as the shared grid parameters plus its contact law.
+struct Legacy {
+    Params P;
+    Fc law;          // global kn, vn, ks, vs, mu of the legacy block
+    double coh;      // cohesive
 };
 
-struct v3 {
-    double x, y, z;
-};
-__device__ __forceinline__ v3 V(double x, double y, double z) { return v3{ x, y, z }; }
-__device__ __forceinline__ v3 operator*(double a, v3 b) { return V(a * b.x, a * b.y, a * b.z); }
-__device__ __forceinline__ void operator+=(v3& a, v3 b) { a.x += b.x; a.y += b.y; a.z += b.z; }
-__device__ __forceinline__ v3 operator+(v3 a, v3 b) { return V(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ v3 operator-(v3 a, v3 b) { return V(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ v3 operator-(v3 a) { return V(-a.x, -a.y, -a.z); }
-__device__ __forceinline__ double len(v3 v) { return sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
-__device__ __forceinline__ double dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ v3 cross(v3 a, v3 b)
+bool legacy_block(Legacy* out)
 {
-    return V(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-}
-__device__ __forceinline__ v3 operator/(v3 a, double b)
-{
-    double inv = 1 / b;
-    return V(a.x * inv, a.y * inv, a.z * inv);
-}
-__device__ __forceinline__ v3 ld4(const double* a, size_t i) { return V(a[4 * i], a[4 * i + 1], a[4 * i + 2]); }
-__device__ __forceinline__ v3 ld3(const double* a, size_t i) { return V(a[3 * i], a[3 * i + 1], a[3 * i + 2]); }
-__device__ __forceinline__ v3 ldv(const double* a) { return V(a[0], a[1], a[2]); }
-__device__ __forceinline__ void add3(double* a, size_t i, v3 b)
-{
-    a[3 * i] += b.x;
-    a[3 * i + 1] += b.y;
-    a[3 * i + 2] += b.z;
+    std::lock_guard<std::mutex> lk(g_legacy_mu);
+    if (!g_legacy_set) return false;
+    const xd_legacy_parameters& h = g_legacy;
+    Legacy L{};
+    L.P.rolling = true;
+    L.P.np = h.np;
+    L.P.nsphere = h.nsp;
+    L.P.ncell = h.ncell;
+    L.P.gx = h.grid_size[0];
+    L.P.gy = h.grid_size[1];
+    L.P.gz = h.grid_size[2];
+    L.P.dt = h.dt;
+    L.P.half2dt = h.half2dt;
+    L.P.cs = h.cell_size;
+    L.P.cohesion = h.cohesive;
+    for (int a = 0; a < 3; ++a) {
+        L.P.g[a] = h.gravity[a];
+        L.P.wo[a] = h.world_origin[a];
+    }
+    L.law = Fc{ h.kn, h.vn, h.ks, h.vs, h.mu };
+    L.coh = h.cohesive;
+    *out = L;
+    return true;
 }
 
-// calcGridPos / calcGridHash (impl:73-91)
-__device__ __forceinline__ unsigned cell_hash(const LP& P, v3 p, int dx, int dy, int dz)
+// rows of the legacy state: double4 (x, y, z, w)
+__device__ __forceinline__ d3 row4(const double* a, size_t i) { return ldv(a + 4 * i); }
+__device__ __forceinline__ void set_row4(double* a, size_t i, d3 v)
 {
-    int cx = (int)floor((p.x - P.wo[0]) / P.cs) + dx;
-    int cy = (int)floor((p.y - P.wo[1]) / P.cs) + dy;
-    int cz = (int)floor((p.z - P.wo[2]) / P.cs) + dz;
-    unsigned x = (unsigned)cx & (P.gx - 1u), y = (unsigned)cy & (P.gy - 1u), z = (unsigned)cz & (P.gz - 1u);
-    return __umul24(__umul24(z, P.gy), P.gx) + __umul24(y, P.gx) + x;
+    double* p = a + 4 * i;
+    p[0] = v.x;
+    p[1] = v.y;
+    p[2] = v.z;
+}
+
+// warp sums in a fixed order (the same bits every run)
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ d3 warp_sum(d3 v) { return mk(warp_sum(v.x), warp_sum(v.y), warp_sum(v.z)); }
+
+// Calls fn(k) for the grid entries of particle ip's 27 cells in the
+// reference's order, lane l of the warp taking entries l, l + 32, ... of each
+// cell; stop() (warp-uniform) ends the walk after a round of 32.
+template <typename Fn, typename Stop>
+__device__ __forceinline__ void warp_cells(const Params& P, d3 ip, const unsigned* __restrict__ sorted,
+                                           const unsigned* __restrict__ cstart, const unsigned* __restrict__ cend,
+                                           Fn fn, Stop stop)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const int3 gp = grid_pos(P, ip.x, ip.y, ip.z);
+    for (int z = -1; z <= 1; z++)
+        for (int y = -1; y <= 1; y++)
+            for (int x = -1; x <= 1; x++) {
+                const unsigned h = grid_hash(P, gp.x + x, gp.y + y, gp.z + z);
+                const unsigned st = __ldg(cstart + h);
+                if (st == 0xffffffffu) continue;
+                const unsigned en = __ldg(cend + h);
+                for (unsigned base = st; base < en; base += 32u) {
+                    const unsigned j = base + lane;
+                    fn(j < en ? __ldg(sorted + j) : 0xffffffffu);
+                    if (stop()) return;
+                }
+            }
 }
 
 // ------------------------------------------------------------ integrator
 
-__global__ void k_l_vv_position(LP P, double* __restrict__ pos, const double* __restrict__ vel,
-                                const double* __restrict__ acc)
+// vv_update_position_kernel (impl:93-107): x += dt v + half2dt a
+__global__ void __launch_bounds__(256) k_legacy_drift(Params P, double* __restrict__ pos,
+                                                      const double* __restrict__ vel,
+                                                      const double* __restrict__ acc)
 {
-    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= P.np) return;
-    v3 p = ld4(pos, id);
-    v3 v = ld4(vel, id), a = ld4(acc, id);
-    p += P.dt * v + P.half2dt * a;
-    pos[4 * (size_t)id] = p.x;
-    pos[4 * (size_t)id + 1] = p.y;
-    pos[4 * (size_t)id + 2] = p.z;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.np) return;
+    set_row4(pos, i, row4(pos, i) + (P.dt * row4(vel, i) + P.half2dt * row4(acc, i)));
 }
 
-__global__ void k_l_vv_velocity(LP P, double* __restrict__ vel, double* __restrict__ acc, double* __restrict__ omega,
-                                double* __restrict__ alpha, const double* __restrict__ force,
-                                const double* __restrict__ moment)
+// vv_update_velocity_kernel (impl:109-140): two half kicks around the new
+// accelerations a = F / acc.w and alpha = M / alpha.w; the rows' w keep the
+// mass and inertia (vel.w and omega.w become 0)
+__global__ void __launch_bounds__(256) k_legacy_kick(Params P, double* __restrict__ vel, double* __restrict__ acc,
+                                                     double* __restrict__ omega, double* __restrict__ alpha,
+                                                     const double* __restrict__ force,
+                                                     const double* __restrict__ moment)
 {
-    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= P.np) return;
-    const size_t q = 4 * (size_t)id;
-    v3 v = ld4(vel, id), a = ld4(acc, id), av = ld4(omega, id), aa = ld4(alpha, id);
-    double mass = acc[q + 3], inertia = alpha[q + 3];
-    v += 0.5 * P.dt * a;
-    av += 0.5 * P.dt * aa;
-    a = (1 / mass) * ld3(force, id);
-    aa = (1 / inertia) * ld3(moment, id);
-    v += 0.5 * P.dt * a;
-    av += 0.5 * P.dt * aa;
-    vel[q] = v.x; vel[q + 1] = v.y; vel[q + 2] = v.z; vel[q + 3] = 0;
-    omega[q] = av.x; omega[q + 1] = av.y; omega[q + 2] = av.z; omega[q + 3] = 0;
-    acc[q] = a.x; acc[q + 1] = a.y; acc[q + 2] = a.z; acc[q + 3] = mass;
-    alpha[q] = aa.x; alpha[q + 1] = aa.y; alpha[q + 2] = aa.z; alpha[q + 3] = inertia;
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.np) return;
+    const size_t q = 4 * (size_t)i;
+    const double m = acc[q + 3], I = alpha[q + 3];
+    const double h = 0.5 * P.dt;
+    const d3 a1 = (1 / m) * ldv(force + 3 * (size_t)i), b1 = (1 / I) * ldv(moment + 3 * (size_t)i);
+    const d3 v = (row4(vel, i) + h * row4(acc, i)) + h * a1;
+    const d3 w = (row4(omega, i) + h * row4(alpha, i)) + h * b1;
+    set_row4(vel, i, v);
+    set_row4(omega, i, w);
+    set_row4(acc, i, a1);
+    set_row4(alpha, i, b1);
+    vel[q + 3] = 0.0;
+    omega[q + 3] = 0.0;
 }
 
-// ------------------------------------------------------------ grid
+// ------------------------------------------------------------ contacts
 
-__global__ void k_l_hash(LP P, unsigned* __restrict__ hash, unsigned* __restrict__ index,
-                         const double* __restrict__ pos)
+// One legacy pair contact of particle i (radius ir) with j: the DHS model's
+// normal force into F and its shear force's moment into M (calForce,
+// impl:231-252).  The unit normal is relative_pos times 1 / dist as the
+// legacy operators divide (impl:68-72).
+__device__ __forceinline__ void legacy_pair(const Legacy& L, double ir, double jr, d3 ip, d3 jp, d3 iv, d3 jv,
+                                            d3 iw, d3 jw, d3& F, d3& M)
 {
-    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= P.np + P.nsp) return;
-    hash[id] = cell_hash(P, ld4(pos, id), 0, 0, 0);
-    index[id] = id;
-}
-
-// reorderDataAndFindCellStart_kernel (impl:156-196) over np + nsp entries;
-// the neighbour in the sorted list is read directly instead of through
-// shared memory (same values)
-__global__ void k_l_cell_bounds(LP P, const unsigned* __restrict__ hash, const unsigned* __restrict__ index,
-                                unsigned* __restrict__ cstart, unsigned* __restrict__ cend,
-                                unsigned* __restrict__ sorted_index)
-{
-    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned tnp = P.np + P.nsp;
-    if (id >= tnp) return;
-    const unsigned h = hash[id];
-    if (id == 0 || h != hash[id - 1]) {
-        cstart[h] = id;
-        if (id > 0) cend[hash[id - 1]] = id;
+    const d3 rp = jp - ip;
+    const double dist = length(rp);
+    const double cd = (ir + jr) - dist;
+    const d3 unit = (1 / dist) * rp;
+    const d3 rv = jv + cross(jw, -jr * unit) - (iv + cross(iw, ir * unit));
+    if (cd > 0) {
+        d3 Ft = mk(0, 0, 0), Fn, Mp = mk(0, 0, 0);
+        dhs(L.law, ir, jr, 0, 0, 0, 0, 0.0, cd, rv, unit, L.P.dt, Ft, Fn, Mp);
+        F += Fn;
+        M += Mp;
+        return;
     }
-    if (id == tnp - 1) cend[h] = id + 1;
-    sorted_index[id] = index[id];
+    if (L.coh == 0) return;
+    // apart within the 27 cells with cohesion (impl:211-229): the cohesive
+    // pull coh / mu along the normal when the would-be normal force lies in
+    // (-coh / mu, 0), and a moment from the capped shear
+    const Fc& c = L.law;
+    const double pull = L.coh / c.mu;
+    const double fn = -c.kn * pow(-cd, 1.5) + c.vn * dot(rv, unit);
+    if (fn < 0 && fn > -pull) F += pull * unit;
+    const d3 e = rv - dot(rv, unit) * unit;
+    const double me = length(e);
+    if (me != 0.0) {
+        const d3 s = (1 / me) * e;
+        const double fs = fmin(c.ks * (me * L.P.dt) + c.vs * dot(rv, s), c.mu * fn);
+        if (fs < fn * c.mu + L.coh) M += cross(ir * unit, (fn * c.mu + L.coh) * s);
+    }
 }
 
-// ------------------------------------------------------------ particle-particle
-
-// calForce (impl:198-252)
-__device__ __forceinline__ bool cal_force(const LP& P, double ir, double jr, v3 ipos, v3 jpos, v3 ivel, v3 jvel,
-                                          v3 iomega, v3 jomega, v3& force, v3& moment)
+// calculate_p2p_kernel (impl:254-327): force += m g + the normal forces of
+// the particle's contacts, moment += the shear moments; one warp a particle.
+__global__ void __launch_bounds__(256) k_legacy_p2p(Legacy L, const double* __restrict__ pos,
+                                                    const double* __restrict__ vel, const double* __restrict__ acc,
+                                                    const double* __restrict__ omega, double* __restrict__ force,
+                                                    double* __restrict__ moment, const unsigned* __restrict__ sorted,
+                                                    const unsigned* __restrict__ cstart,
+                                                    const unsigned* __restrict__ cend)
 {
-    v3 relative_pos = jpos - ipos;
-    double dist = len(relative_pos);
-    double collid_dist = (ir + jr) - dist;
-    if (collid_dist <= 0) {
-        if (P.coh == 0) return false;
-        double tu = P.coh / P.mu;
-        v3 unit = relative_pos / dist;
-        v3 relative_vel = jvel + cross(jomega, -jr * unit) - (ivel + cross(iomega, ir * unit));
-        double Fn = (-P.kn * pow(-collid_dist, 1.5) + P.vn * dot(relative_vel, unit));
-        if (Fn < 0 && Fn > -tu) force += tu * unit;
-        v3 e = relative_vel - dot(relative_vel, unit) * unit;
-        double mag_e = len(e);
-        if (mag_e) {
-            v3 s_hat = e / mag_e;
-            double ds = mag_e * P.dt;
-            double Fs = fmin(P.ks * ds + P.vs * (dot(relative_vel, s_hat)), P.mu * Fn);
-            if (Fs < Fn * P.mu + P.coh) moment += cross(ir * unit, (Fn * P.mu + P.coh) * s_hat);
-        }
-        return false;
+    const unsigned id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (id >= L.P.np) return;
+    const unsigned np = L.P.np;
+    const d3 ip = row4(pos, id), iv = row4(vel, id), iw = row4(omega, id);
+    const double ir = __ldg(pos + 4 * (size_t)id + 3);
+    d3 F = mk(0, 0, 0), M = mk(0, 0, 0);
+    warp_cells(
+        L.P, ip, sorted, cstart, cend,
+        [&](unsigned k) {
+            if (k == 0xffffffffu || k == id || k >= np) return;
+            legacy_pair(L, ir, __ldg(pos + 4 * (size_t)k + 3), ip, row4(pos, k), iv, row4(vel, k), iw,
+                        row4(omega, k), F, M);
+        },
+        [] { return false; });
+    F = warp_sum(F);
+    M = warp_sum(M);
+    if ((threadIdx.x & 31u) == 0) {
+        const d3 g = __ldg(acc + 4 * (size_t)id + 3) * mk(L.P.g[0], L.P.g[1], L.P.g[2]);
+        double* f = force + 3 * (size_t)id;
+        double* m = moment + 3 * (size_t)id;
+        const d3 t = g + F;
+        f[0] += t.x; f[1] += t.y; f[2] += t.z;
+        m[0] += M.x; m[1] += M.y; m[2] += M.z;
     }
-    v3 unit = relative_pos / dist;
-    v3 relative_vel = jvel + cross(jomega, -jr * unit) - (ivel + cross(iomega, ir * unit));
-    v3 single_force = (-P.kn * pow(collid_dist, 1.5) + P.vn * dot(relative_vel, unit)) * unit;
-    v3 single_moment = V(0, 0, 0);
-    v3 e = relative_vel - dot(relative_vel, unit) * unit;
-    double mag_e = len(e);
-    if (mag_e) {
-        v3 s_hat = e / mag_e;
-        double ds = mag_e * P.dt;
-        v3 shear_force = fmin(P.ks * ds + P.vs * (dot(relative_vel, s_hat)), P.mu * len(single_force)) * s_hat;
-        single_moment = cross(ir * unit, shear_force);
-    }
-    force += single_force;
-    moment += single_moment;
-    return true;
 }
 
-__global__ void __launch_bounds__(128) k_l_p2p(LP P, const double* __restrict__ pos, const double* __restrict__ vel,
-                                               const double* __restrict__ acc, const double* __restrict__ omega,
-                                               double* __restrict__ force, double* __restrict__ moment,
-                                               const unsigned* __restrict__ sorted, const unsigned* __restrict__ cstart,
-                                               const unsigned* __restrict__ cend)
+// cube_hertzian_contact_force_kernel (impl:329-378): the face contacts of
+// the six planes (the shared face-region test), each adding its normal
+// force and its shear force's moment.
+__global__ void __launch_bounds__(128) k_legacy_cube(Legacy L, const xd_legacy_plane_info* __restrict__ planes, Fc c,
+                                                     const double* __restrict__ pos, const double* __restrict__ vel,
+                                                     const double* __restrict__ omega, double* __restrict__ force,
+                                                     double* __restrict__ moment)
 {
-    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= P.np) return;
-    v3 ipos = ld4(pos, id), ivel = ld4(vel, id), iomega = ld4(omega, id);
-    double ir = pos[4 * (size_t)id + 3];
-    v3 m_force = acc[4 * (size_t)id + 3] * V(P.g[0], P.g[1], P.g[2]);
-    v3 m_moment = V(0, 0, 0);
-    for (int z = -1; z <= 1; z++)
-        for (int y = -1; y <= 1; y++)
-            for (int x = -1; x <= 1; x++) {
-                unsigned h = cell_hash(P, ipos, x, y, z);
-                unsigned st = cstart[h];
-                if (st == 0xffffffffu) continue;
-                unsigned en = cend[h];
-                for (unsigned j = st; j < en; j++) {
-                    unsigned k = sorted[j];
-                    if (id == k || k >= P.np) continue;
-                    cal_force(P, ir, pos[4 * (size_t)k + 3], ipos, ld4(pos, k), ivel, ld4(vel, k), iomega,
-                              ld4(omega, k), m_force, m_moment);
-                }
-            }
-    add3(force, id, m_force);
-    add3(moment, id, m_moment);
-}
-
-// ------------------------------------------------------------ cube
-
-__global__ void __launch_bounds__(128) k_l_cube(LP P, const xd_legacy_plane_info* __restrict__ planes, double kn,
-                                                double vn, double ks, double vs, double mu,
-                                                const double* __restrict__ pos, const double* __restrict__ vel,
-                                                const double* __restrict__ omega, double* __restrict__ force,
-                                                double* __restrict__ moment)
-{
-    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= P.np) return;
-    double r = pos[4 * (size_t)id + 3];
-    v3 ipos = ld4(pos, id), ivel = ld4(vel, id), iomega = ld4(omega, id);
-    v3 m_force = V(0, 0, 0), m_moment = V(0, 0, 0);
-    for (int i = 0; i < 6; i++) {
-        const xd_legacy_plane_info& pl = planes[i];
-        v3 xw = ldv(pl.xw), uw = ldv(pl.uw);
-        v3 dp = ipos - xw;
-        v3 wp = V(dot(dp, ldv(pl.u1)), dot(dp, ldv(pl.u2)), dot(dp, uw));
-        if (fabs(wp.z) < r && (wp.x > 0 && wp.x < pl.l1) && (wp.y > 0 && wp.y < pl.l2)) {
-            const int sg = dot(ipos - xw, uw) < 0 ? -1 : 1;
-            v3 unit = (double)(-sg) * (uw / len(uw));
-            double collid_dist = r - fabs(dot(ipos - xw, unit));
-            v3 dv = -(ivel + cross(iomega, r * unit));
-            v3 single_force = (-kn * pow(collid_dist, 1.5) + vn * dot(dv, unit)) * unit;
-            v3 e = dv - dot(dv, unit) * unit;
-            double mag_e = len(e);
-            if (mag_e) {
-                v3 s_hat = e / mag_e;
-                double ds = mag_e * P.dt;
-                v3 shear_force = fmin(ks * ds + vs * dot(dv, s_hat), mu * len(single_force)) * s_hat;
-                m_moment += cross(r * unit, shear_force);
-            }
-            m_force += single_force;
-        }
+    const unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= L.P.np) return;
+    const double r = __ldg(pos + 4 * (size_t)id + 3);
+    const d3 ip = row4(pos, id), iv = row4(vel, id), iw = row4(omega, id);
+    d3 F = mk(0, 0, 0), M = mk(0, 0, 0);
+    for (int w = 0; w < 6; w++) {
+        const xd_legacy_plane_info& pl = planes[w];
+        PlaneD pe;
+        pe.l1 = pl.l1;
+        pe.l2 = pl.l2;
+        pe.u1 = ldv(pl.u1);
+        pe.u2 = ldv(pl.u2);
+        pe.uw = ldv(pl.uw);
+        pe.xw = ldv(pl.xw);
+        if (!plane_face_region(pe, plane_coords(pe, ip), r)) continue;
+        d3 unit;
+        const double cd = plane_face_depth(pe, ip, unit, r);
+        d3 Ft = mk(0, 0, 0), Fn, Mp = mk(0, 0, 0);
+        dhs(c, r, 0, 0, 0, 0, 0, 0.0, cd, -(iv + cross(iw, r * unit)), unit, L.P.dt, Ft, Fn, Mp);
+        F += Fn;
+        M += Mp;
     }
-    add3(force, id, m_force);
-    add3(moment, id, m_moment);
-}
-
-// ------------------------------------------------------------ shapes
-
-// ClosestPtPointTriangle with the region code wc: 0 vertex, 1 edge, 2 face (impl:380-441)
-__device__ __forceinline__ v3 closest_wc(v3 p, v3 a, v3 b, v3 c, int& wc)
-{
-    v3 ab = b - a, ac = c - a, ap = p - a;
-    double d1 = dot(ab, ap), d2 = dot(ac, ap);
-    if (d1 <= 0.0 && d2 <= 0.0) { wc = 0; return a; }
-    v3 bp = p - b;
-    double d3 = dot(ab, bp), d4 = dot(ac, bp);
-    if (d3 >= 0.0 && d4 <= d3) { wc = 0; return b; }
-    double vc = d1 * d4 - d3 * d2;
-    if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
-        wc = 1;
-        double v = d1 / (d1 - d3);
-        return a + v * ab;
-    }
-    v3 cp = p - c;
-    double d5 = dot(ab, cp), d6 = dot(ac, cp);
-    if (d6 >= 0.0 && d5 <= d6) { wc = 0; return c; }
-    double vb = d5 * d2 - d1 * d6;
-    if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
-        wc = 1;
-        double w = d2 / (d2 - d6);
-        return a + w * ac;
-    }
-    double va = d3 * d6 - d5 * d4;
-    if (va <= 0.0 && (d4 - d3) >= 0.0 && (d5 - d6) >= 0.0) {
-        wc = 1;
-        double w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
-        return b + w * (c - b);
-    }
-    wc = 2;
-    double denom = 1.0 / (va + vb + vc);
-    double v = vb * denom, w = vc * denom;
-    return a + v * ab + w * ac;
-}
-
-// isIntersect2Lines (impl:443-452)
-__device__ __forceinline__ bool intersect2(double x1, double x2, double x3, double x4, double y1, double y2,
-                                           double y3, double y4)
-{
-    double div = (y4 - y3) * (x2 - x1) - (x4 - x3) * (y2 - y1);
-    double t = ((x4 - x3) * (y1 - y3) - (y4 - y3) * (x1 - x3)) / div;
-    double s = ((x2 - x1) * (y1 - y3) - (y2 - y1) * (x1 - x3)) / div;
-    return (t >= 0 && t <= 1) || (s >= 0 && s <= 1);
+    double* f = force + 3 * (size_t)id;
+    double* m = moment + 3 * (size_t)id;
+    f[0] += F.x; f[1] += F.y; f[2] += F.z;
+    m[0] += M.x; m[1] += M.y; m[2] += M.z;
 }
 
 struct Shape {
@@ -308,240 +268,142 @@ struct Shape {
     const unsigned* id_set;
     const unsigned* poly_start;
     const unsigned* poly_end;
-    double kn, vn, ks, vs, mu;
+    Fc law;
 };
 
-__device__ __forceinline__ v3 shape_force(const LP& P, const Shape& S, double r, double collid_dist, v3 unit, v3 vel,
-                                          v3 omega, v3& moment_out)
+// The first contact of vertex entry k's polygons for the pass (face: the
+// closest point in a face region; edge: at a vertex or an edge), its overlap
+// and unit normal (face: -N / |N|; edge: towards the closest point).
+__device__ __forceinline__ bool shape_candidate(const Params& P, const Shape& S, unsigned k, d3 ip, double r,
+                                                bool face, double& cd, d3& unit)
 {
-    v3 dv = ldv(S.mi->vel) - (vel + cross(omega, r * unit));
-    v3 single_force = (-S.kn * pow(collid_dist, 1.5) + S.vn * dot(dv, unit)) * unit;
-    v3 e = dv - dot(dv, unit) * unit;
-    double mag_e = len(e);
-    if (mag_e) {
-        v3 s_hat = e / mag_e;
-        double ds = mag_e * P.dt;
-        v3 shear_force = fmin(S.ks * ds + S.vs * dot(dv, s_hat), S.mu * len(single_force)) * s_hat;
-        moment_out = cross(r * unit, shear_force);
+    const unsigned v = k - P.np;
+    for (unsigned q = __ldg(S.poly_start + v); q < __ldg(S.poly_end + v); q++) {
+        const xd_legacy_polygon& po = S.polygons[__ldg(S.id_set + q)];
+        int region;
+        const d3 cpt = closest_pt_triangle_region(ldv(po.P), ldv(po.Q), ldv(po.R), ip, region);
+        const d3 sp = ip - cpt;
+        const double dist = length(sp);
+        const double d = r - dist;
+        if (d <= 0) continue;
+        if (face ? region != 2 : region == 2) continue;
+        cd = d;
+        if (face) {
+            const d3 N = ldv(po.N);
+            unit = -((1 / length(N)) * N);
+        } else {
+            unit = -((1 / dist) * sp);
+        }
+        return true;
     }
-    return single_force;
+    return false;
 }
 
-// shpae_hertzian_contact_force_kernel with calculateTriangleParticleContactForce
-// (impl:454-526, 676-762): the first face contact through the polygons of
-// the vertices in the 27 cells
-__global__ void __launch_bounds__(128) k_l_shape_face(LP P, Shape S, bool* __restrict__ isLineContact,
+// shpae_hertzian_contact_force_kernel and shape_line_or_edge_contact_force_kernel
+// (impl:454-674): the face pass takes each particle's first face contact in
+// search order; the edge pass, for the particles the face pass left, the
+// first edge or vertex contact.  The body moves with mi.vel; the particle
+// keeps the normal force and the shear force's moment.
+template <bool FACE>
+__global__ void __launch_bounds__(256) k_legacy_shape(Legacy L, Shape S, bool* __restrict__ line,
                                                       const double* __restrict__ pos, const double* __restrict__ vel,
                                                       const double* __restrict__ omega, double* __restrict__ force,
                                                       double* __restrict__ moment, const unsigned* __restrict__ sorted,
                                                       const unsigned* __restrict__ cstart,
                                                       const unsigned* __restrict__ cend)
 {
-    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= P.np) return;
-    isLineContact[id] = false;
-    v3 ipos = ld4(pos, id), ivel = ld4(vel, id), iomega = ld4(omega, id);
-    double ir = pos[4 * (size_t)id + 3];
-    int count = 0;
-    v3 plane_normal = V(0, 0, 0), plane_cp = V(0, 0, 0);   // the last face contact (at most one is kept)
-    v3 m_force = V(0, 0, 0), m_moment = V(0, 0, 0);
-    for (int z = -1; z <= 1; z++)
-        for (int y = -1; y <= 1; y++)
-            for (int x = -1; x <= 1; x++) {
-                unsigned h = cell_hash(P, ipos, x, y, z);
-                unsigned st = cstart[h];
-                if (st == 0xffffffffu) continue;
-                unsigned en = cend[h];
-                for (unsigned j = st; j < en; j++) {
-                    unsigned k = sorted[j];
-                    if (id == k || k < P.np) continue;
-                    const unsigned vtx = k - P.np;
-                    for (unsigned q = S.poly_start[vtx]; q < S.poly_end[vtx]; q++) {
-                        const xd_legacy_polygon& po = S.polygons[S.id_set[q]];
-                        int wc = -1;
-                        v3 contact_point = closest_wc(ipos, ldv(po.P), ldv(po.Q), ldv(po.R), wc);
-                        v3 sp = ipos - contact_point;
-                        double dist = len(sp);
-                        v3 p_unit = -ldv(po.N) / len(ldv(po.N));
-                        double collid_dist = ir - dist;
-                        if (collid_dist <= 0) continue;
-                        if (wc != 2) continue;
-                        if (count) {
-                            v3 ep1 = plane_cp + 10000 * plane_normal;
-                            v3 ep2 = contact_point + 10000 * p_unit;
-                            if (!intersect2(plane_cp.x, ep1.x, contact_point.x, ep2.x, plane_cp.y, ep1.y,
-                                            contact_point.y, ep2.y))
-                                continue;
-                        }
-                        m_force += shape_force(P, S, ir, collid_dist, p_unit, ivel, iomega, m_moment);
-                        plane_cp = contact_point;
-                        plane_normal = p_unit;
-                        ++count;
-                        add3(force, id, m_force);
-                        add3(moment, id, m_moment);
-                        isLineContact[id] = true;
-                        return;
-                    }
-                }
-            }
-}
-
-// shape_line_or_edge_contact_force_kernel with
-// calculateTriangleLineOrEdgeParticleContactForce (impl:528-674): particles
-// without a face contact take their first edge or vertex contact
-__global__ void __launch_bounds__(128) k_l_shape_edge(LP P, Shape S, bool* __restrict__ isLineContact,
-                                                      const double* __restrict__ pos, const double* __restrict__ vel,
-                                                      const double* __restrict__ omega, double* __restrict__ force,
-                                                      double* __restrict__ moment, const unsigned* __restrict__ sorted,
-                                                      const unsigned* __restrict__ cstart,
-                                                      const unsigned* __restrict__ cend)
-{
-    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= P.np) return;
-    if (isLineContact[id]) return;
-    v3 ipos = ld4(pos, id), ivel = ld4(vel, id), iomega = ld4(omega, id);
-    double ir = pos[4 * (size_t)id + 3];
-    v3 l_moment = V(0, 0, 0);
-    for (int z = -1; z <= 1; z++)
-        for (int y = -1; y <= 1; y++)
-            for (int x = -1; x <= 1; x++) {
-                unsigned h = cell_hash(P, ipos, x, y, z);
-                unsigned st = cstart[h];
-                if (st == 0xffffffffu) continue;
-                unsigned en = cend[h];
-                for (unsigned j = st; j < en; j++) {
-                    unsigned k = sorted[j];
-                    if (id == k || k < P.np) continue;
-                    const unsigned vtx = k - P.np;
-                    for (unsigned q = S.poly_start[vtx]; q < S.poly_end[vtx]; q++) {
-                        const xd_legacy_polygon& po = S.polygons[S.id_set[q]];
-                        int wc = -1;
-                        v3 contact_point = closest_wc(ipos, ldv(po.P), ldv(po.Q), ldv(po.R), wc);
-                        v3 sp = ipos - contact_point;
-                        double dist = len(sp);
-                        v3 s_unit = -sp / dist;
-                        double collid_dist = ir - dist;
-                        if (collid_dist <= 0) continue;
-                        if (wc != 0 && wc != 1) continue;
-                        v3 l_force = shape_force(P, S, ir, collid_dist, s_unit, ivel, iomega, l_moment);
-                        isLineContact[id] = true;
-                        add3(force, id, l_force);
-                        add3(moment, id, l_moment);
-                        return;
-                    }
-                }
-            }
-}
-
-// the shape call's force sum over the particles, in a fixed order
-constexpr unsigned kLRed = 256;
-__global__ void __launch_bounds__(kLRed) k_l_sum_partial(const double* __restrict__ f, unsigned n,
-                                                         double* __restrict__ part)
-{
-    __shared__ double s[3][kLRed];
-    double a[3] = { 0.0, 0.0, 0.0 };
-    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        for (int c = 0; c < 3; ++c) a[c] += f[3 * (size_t)i + c];
-    for (int c = 0; c < 3; ++c) s[c][threadIdx.x] = a[c];
-    __syncthreads();
-    for (unsigned o = kLRed / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o)
-            for (int c = 0; c < 3; ++c) s[c][threadIdx.x] += s[c][threadIdx.x + o];
-        __syncthreads();
+    const unsigned id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (id >= L.P.np) return;
+    const unsigned lane = threadIdx.x & 31u;
+    if (FACE) {
+        if (lane == 0) line[id] = false;
+    } else if (line[id]) {
+        return;
     }
-    if (threadIdx.x < 3) part[3 * blockIdx.x + threadIdx.x] = s[threadIdx.x][0];
-}
-
-__global__ void k_l_sum_final(const double* __restrict__ part, unsigned nb, double* __restrict__ out)
-{
-    unsigned c = threadIdx.x;
-    if (c >= 3) return;
-    double t = 0.0;
-    for (unsigned b = 0; b < nb; ++b) t += part[3 * b + c];
-    out[c] = t;
+    const d3 ip = row4(pos, id);
+    const double r = __ldg(pos + 4 * (size_t)id + 3);
+    bool found = false;
+    warp_cells(
+        L.P, ip, sorted, cstart, cend,
+        [&](unsigned k) {
+            double cd = 0.0;
+            d3 unit = mk(0, 0, 0);
+            const bool hit = k != 0xffffffffu && k != id && k >= L.P.np &&
+                             shape_candidate(L.P, S, k, ip, r, FACE, cd, unit);
+            const unsigned bal = __ballot_sync(0xffffffffu, hit);
+            if (!bal) return;
+            found = true;
+            if ((int)lane != __ffs(bal) - 1) return;
+            const d3 iv = row4(vel, id), iw = row4(omega, id);
+            const d3 dv = ldv(S.mi->vel) - (iv + cross(iw, r * unit));
+            d3 Ft = mk(0, 0, 0), Fn, Mp = mk(0, 0, 0);
+            dhs(S.law, r, 0, 0, 0, 0, 0, 0.0, cd, dv, unit, L.P.dt, Ft, Fn, Mp);
+            double* f = force + 3 * (size_t)id;
+            double* m = moment + 3 * (size_t)id;
+            f[0] += Fn.x; f[1] += Fn.y; f[2] += Fn.z;
+            m[0] += Mp.x; m[1] += Mp.y; m[2] += Mp.z;
+            line[id] = true;
+        },
+        [&] { return found; });
 }
 
 // ------------------------------------------------------------ meshes
 
-__global__ void k_l_polygons_position(const double* __restrict__ mpos, const double* __restrict__ A,
-                                      const double* __restrict__ lv, unsigned nv, double* __restrict__ pos)
+// cu_update_polygons_position (impl:764-780): v = mpos + A l
+__global__ void __launch_bounds__(256) k_legacy_place(const double* __restrict__ mpos, const double* __restrict__ A,
+                                                      const double* __restrict__ local, unsigned nv,
+                                                      double* __restrict__ pos)
 {
-    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= nv) return;
-    v3 l = ld3(lv, id);
-    double tx = A[0] * l.x + A[1] * l.y + A[2] * l.z;
-    double ty = A[3] * l.x + A[4] * l.y + A[5] * l.z;
-    double tz = A[6] * l.x + A[7] * l.y + A[8] * l.z;
-    pos[3 * (size_t)id] = mpos[0] + tx;
-    pos[3 * (size_t)id + 1] = mpos[1] + ty;
-    pos[3 * (size_t)id + 2] = mpos[2] + tz;
+    const d3 l = ldv(local + 3 * (size_t)id);
+    const d3 t = mk(dot(ldv(A), l), dot(ldv(A + 3), l), dot(ldv(A + 6), l));
+    st3(pos, id, ldv(mpos) + t);
 }
 
-__global__ void k_l_polygons_information(xd_legacy_polygon* __restrict__ polygons, const unsigned* __restrict__ indice,
-                                         const double* __restrict__ pos, unsigned ni)
+// cu_update_polygons_information (impl:798-817): vertices, edges and the
+// (unnormalised) normal of each polygon from its vertex indices
+__global__ void __launch_bounds__(256) k_legacy_polygons(xd_legacy_polygon* __restrict__ polygons,
+                                                         const unsigned* __restrict__ indice,
+                                                         const double* __restrict__ pos, unsigned ni)
 {
-    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= ni) return;
-    v3 P = ld3(pos, indice[3 * (size_t)id]), Q = ld3(pos, indice[3 * (size_t)id + 1]),
-       R = ld3(pos, indice[3 * (size_t)id + 2]);
-    v3 Vv = Q - P, W = R - P, N = cross(Vv, W);
+    const d3 P = ldv(pos + 3 * (size_t)indice[3 * (size_t)id]);
+    const d3 Q = ldv(pos + 3 * (size_t)indice[3 * (size_t)id + 1]);
+    const d3 R = ldv(pos + 3 * (size_t)indice[3 * (size_t)id + 2]);
     xd_legacy_polygon& o = polygons[id];
-    o.P[0] = P.x; o.P[1] = P.y; o.P[2] = P.z;
-    o.Q[0] = Q.x; o.Q[1] = Q.y; o.Q[2] = Q.z;
-    o.R[0] = R.x; o.R[1] = R.y; o.R[2] = R.z;
-    o.V[0] = Vv.x; o.V[1] = Vv.y; o.V[2] = Vv.z;
-    o.W[0] = W.x; o.W[1] = W.y; o.W[2] = W.z;
-    o.N[0] = N.x; o.N[1] = N.y; o.N[2] = N.z;
+    st3(o.P, 0, P);
+    st3(o.Q, 0, Q);
+    st3(o.R, 0, R);
+    st3(o.V, 0, Q - P);
+    st3(o.W, 0, R - P);
+    st3(o.N, 0, cross(Q - P, R - P));
 }
 
-__global__ void k_l_mergedata(double* __restrict__ data, const double* __restrict__ pos, unsigned np,
-                              const double* __restrict__ vertice, unsigned snp)
+// cu_mergedata (impl:782-796): the particles' rows, then the vertices as (x, y, z, -1)
+__global__ void __launch_bounds__(256) k_legacy_merge(double* __restrict__ data, const double* __restrict__ pos,
+                                                      unsigned np, const double* __restrict__ vertice,
+                                                      unsigned snp)
 {
-    unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= np + snp) return;
     double* d = data + 4 * (size_t)id;
     if (id < np) {
-        d[0] = pos[4 * (size_t)id];
-        d[1] = pos[4 * (size_t)id + 1];
-        d[2] = pos[4 * (size_t)id + 2];
-        d[3] = pos[4 * (size_t)id + 3];
+        for (int a = 0; a < 4; ++a) d[a] = pos[4 * (size_t)id + a];
     } else {
-        v3 v = ld3(vertice, id - np);
-        d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = -1.0;
+        const d3 v = ldv(vertice + 3 * (size_t)(id - np));
+        d[0] = v.x;
+        d[1] = v.y;
+        d[2] = v.z;
+        d[3] = -1.0;
     }
-}
-
-bool legacy_params(LP* out)
-{
-    std::lock_guard<std::mutex> lk(g_l_mu);
-    if (!g_have_l) return false;
-    const xd_legacy_parameters& h = g_l;
-    LP p;
-    p.np = h.np;
-    p.nsp = h.nsp;
-    p.ncell = h.ncell;
-    p.gx = h.grid_size[0];
-    p.gy = h.grid_size[1];
-    p.gz = h.grid_size[2];
-    p.dt = h.dt;
-    p.half2dt = h.half2dt;
-    p.cs = h.cell_size;
-    for (int a = 0; a < 3; ++a) {
-        p.g[a] = h.gravity[a];
-        p.wo[a] = h.world_origin[a];
-    }
-    p.kn = h.kn;
-    p.vn = h.vn;
-    p.ks = h.ks;
-    p.vs = h.vs;
-    p.mu = h.mu;
-    p.coh = h.cohesive;
-    *out = p;
-    return true;
 }
 
 inline cudaStream_t S_(void* s) { return static_cast<cudaStream_t>(s); }
 inline unsigned nblk(unsigned n, unsigned b) { return n ? (n + b - 1) / b : 1u; }
+// blocks of 256 threads, one warp per particle
+inline unsigned warp_blocks(unsigned n) { return nblk(n, 8u); }
 
 }  // namespace
 }  // namespace xd
@@ -553,9 +415,9 @@ using namespace xd;
         if (!(cond)) return set_error(XD_ERR_INVALID, __VA_ARGS__); \
     } while (0)
 
-#define XL_PARAMS(name)                                                                              \
-    LP PL;                                                                                           \
-    if (!legacy_params(&PL))                                                                         \
+#define XL_BLOCK(name)                                                                               \
+    Legacy L;                                                                                        \
+    if (!legacy_block(&L))                                                                           \
         return set_error(XD_ERR_STATE, "%s: xd_legacy_set_symbolic_parameter was not called", name)
 
 extern "C" {
@@ -567,19 +429,19 @@ int xd_legacy_set_symbolic_parameter(const xd_legacy_parameters* h)
     for (int a = 0; a < 3; ++a)
         XL_REQUIRE(h->grid_size[a] && !(h->grid_size[a] & (h->grid_size[a] - 1)),
                    "legacy_set_symbolic_parameter: grid sizes must be powers of two");
-    std::lock_guard<std::mutex> lk(g_l_mu);
-    g_l = *h;
-    g_have_l = true;
+    std::lock_guard<std::mutex> lk(g_legacy_mu);
+    g_legacy = *h;
+    g_legacy_set = true;
     return XD_OK;
 }
 
 int xd_legacy_vv_update_position(double* pos, const double* vel, const double* acc, unsigned np, void* s)
 {
     (void)np;
-    XL_PARAMS("legacy_vv_update_position");
-    if (PL.np == 0) return XD_OK;
+    XL_BLOCK("legacy_vv_update_position");
+    if (L.P.np == 0) return XD_OK;
     XL_REQUIRE(pos && vel && acc, "legacy_vv_update_position: null pointer");
-    k_l_vv_position<<<nblk(PL.np, 256), 256, 0, S_(s)>>>(PL, pos, vel, acc);
+    k_legacy_drift<<<nblk(L.P.np, 256), 256, 0, S_(s)>>>(L.P, pos, vel, acc);
     return launch_status("legacy_vv_update_position");
 }
 
@@ -587,50 +449,47 @@ int xd_legacy_vv_update_velocity(double* vel, double* acc, double* omega, double
                                  const double* moment, unsigned np, void* s)
 {
     (void)np;
-    XL_PARAMS("legacy_vv_update_velocity");
-    if (PL.np == 0) return XD_OK;
+    XL_BLOCK("legacy_vv_update_velocity");
+    if (L.P.np == 0) return XD_OK;
     XL_REQUIRE(vel && acc && omega && alpha && force && moment, "legacy_vv_update_velocity: null pointer");
-    k_l_vv_velocity<<<nblk(PL.np, 256), 256, 0, S_(s)>>>(PL, vel, acc, omega, alpha, force, moment);
+    k_legacy_kick<<<nblk(L.P.np, 256), 256, 0, S_(s)>>>(L.P, vel, acc, omega, alpha, force, moment);
     return launch_status("legacy_vv_update_velocity");
 }
 
 int xd_legacy_calculate_hash_and_index(unsigned* hash, unsigned* index, const double* pos, unsigned np, void* s)
 {
-    XL_PARAMS("legacy_calculate_hash_and_index");
+    XL_BLOCK("legacy_calculate_hash_and_index");
     XL_REQUIRE(hash && index && pos, "legacy_calculate_hash_and_index: null pointer");
-    const unsigned n = PL.np + PL.nsp;
-    if (n) k_l_hash<<<nblk(n, 256), 256, 0, S_(s)>>>(PL, hash, index, pos);
-    int st = launch_status("legacy_calculate_hash_and_index");
+    int st = launch_hash(L.P, hash, index, pos, L.P.np + L.P.nsphere, 0, S_(s));
     if (st != XD_OK || np <= 1) return st;
-    // the launcher sorts the first np entries (def.cu:65-67), stably by hash
+    // the launcher sorts the first np entries (def.cu:65-67), stably by hash;
     // wrapped hashes are below gx gy gz
-    const unsigned bits = key_bits_for(PL.gx * PL.gy * PL.gz);
     void* ws = workspace(radix_sort_scratch_bytes(np), &st);
     if (!ws) return st;
     unsigned *ok = nullptr, *ov = nullptr;
-    st = radix_sort_pairs(hash, index, np, bits, ws, S_(s), &ok, &ov);
-    if (st != XD_OK) return st;
-    if (ok != hash) {
-        cudaError_t e = cudaMemcpyAsync(hash, ok, sizeof(unsigned) * (size_t)np, cudaMemcpyDeviceToDevice, S_(s));
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(index, ov, sizeof(unsigned) * (size_t)np, cudaMemcpyDeviceToDevice, S_(s));
-        return cuda_status(e, "legacy_calculate_hash_and_index copy-back");
-    }
-    return XD_OK;
+    st = radix_sort_pairs(hash, index, np, key_bits_for(L.P.gx * L.P.gy * L.P.gz), ws, S_(s), &ok, &ov);
+    if (st != XD_OK || ok == hash) return st;
+    cudaError_t e = cudaMemcpyAsync(hash, ok, sizeof(unsigned) * (size_t)np, cudaMemcpyDeviceToDevice, S_(s));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(index, ov, sizeof(unsigned) * (size_t)np, cudaMemcpyDeviceToDevice, S_(s));
+    return cuda_status(e, "legacy_calculate_hash_and_index copy-back");
 }
 
 int xd_legacy_reorder_and_find_cell_start(unsigned* hash, unsigned* index, unsigned* cstart, unsigned* cend,
                                           unsigned* sorted_index, unsigned np, unsigned nc, void* s)
 {
     (void)np;
-    XL_PARAMS("legacy_reorder_and_find_cell_start");
+    XL_BLOCK("legacy_reorder_and_find_cell_start");
     XL_REQUIRE(hash && index && cstart && cend && sorted_index, "legacy_reorder_and_find_cell_start: null pointer");
+    // cstart only is reset (def.cu:71-90); the shared cell-range kernel then
+    // marks the runs of the sorted keys (a key >= nc is skipped)
     int st = cuda_status(cudaMemsetAsync(cstart, 0xff, sizeof(unsigned) * (size_t)nc, S_(s)),
                          "legacy_reorder_and_find_cell_start");
     if (st != XD_OK) return st;
-    const unsigned n = PL.np + PL.nsp;
-    if (n) k_l_cell_bounds<<<nblk(n, 256), 256, 0, S_(s)>>>(PL, hash, index, cstart, cend, sorted_index);
-    return launch_status("legacy_reorder_and_find_cell_start");
+    void* ws = workspace(256, &st);
+    if (!ws) return st;
+    return launch_cell_bounds_sorted(hash, index, cstart, cend, sorted_index, L.P.np + L.P.nsphere, nc,
+                                     static_cast<unsigned*>(ws), S_(s));
 }
 
 int xd_legacy_calculate_p2p(const double* pos, const double* vel, const double* acc, const double* omega,
@@ -640,12 +499,12 @@ int xd_legacy_calculate_p2p(const double* pos, const double* vel, const double* 
     (void)alpha;
     (void)np;
     (void)cRun;
-    XL_PARAMS("legacy_calculate_p2p");
-    if (PL.np == 0) return XD_OK;
+    XL_BLOCK("legacy_calculate_p2p");
+    if (L.P.np == 0) return XD_OK;
     XL_REQUIRE(pos && vel && acc && omega && force && moment && sorted_index && cstart && cend,
                "legacy_calculate_p2p: null pointer");
-    k_l_p2p<<<nblk(PL.np, 128), 128, 0, S_(s)>>>(PL, pos, vel, acc, omega, force, moment, sorted_index, cstart,
-                                                  cend);
+    k_legacy_p2p<<<warp_blocks(L.P.np), 256, 0, S_(s)>>>(L, pos, vel, acc, omega, force, moment, sorted_index,
+                                                         cstart, cend);
     return launch_status("legacy_calculate_p2p");
 }
 
@@ -656,10 +515,11 @@ int xd_legacy_cube_hertzian_contact_force(const xd_legacy_plane_info* planes, do
 {
     (void)isLineContact;
     (void)np;
-    XL_PARAMS("legacy_cube_hertzian_contact_force");
-    if (PL.np == 0) return XD_OK;
+    XL_BLOCK("legacy_cube_hertzian_contact_force");
+    if (L.P.np == 0) return XD_OK;
     XL_REQUIRE(planes && pos && vel && omega && force && moment, "legacy_cube_hertzian_contact_force: null pointer");
-    k_l_cube<<<nblk(PL.np, 128), 128, 0, S_(s)>>>(PL, planes, kn, vn, ks, vs, mu, pos, vel, omega, force, moment);
+    k_legacy_cube<<<nblk(L.P.np, 128), 128, 0, S_(s)>>>(L, planes, Fc{ kn, vn, ks, vs, mu }, pos, vel, omega, force,
+                                                         moment);
     return launch_status("legacy_cube_hertzian_contact_force");
 }
 
@@ -674,35 +534,26 @@ int xd_legacy_shape_hertzian_contact_force(const xd_legacy_mass_info* minfo, con
     (void)bforce;
     XL_REQUIRE(out, "legacy_shape_hertzian_contact_force: null output");
     out[0] = out[1] = out[2] = 0.0;
-    XL_PARAMS("legacy_shape_hertzian_contact_force");
+    XL_BLOCK("legacy_shape_hertzian_contact_force");
     XL_REQUIRE(minfo && polygons && id_set && poly_start && poly_end && isLineContact && pos && vel && omega &&
                    force && moment && sorted_id && cell_start && cell_end,
                "legacy_shape_hertzian_contact_force: null pointer");
     int st = cuda_status(cudaMemsetAsync(force, 0, sizeof(double) * 3 * (size_t)np, S_(s)), "legacy shape");
     if (st == XD_OK) st = cuda_status(cudaMemsetAsync(moment, 0, sizeof(double) * 3 * (size_t)np, S_(s)), "legacy shape");
     if (st != XD_OK) return st;
-    Shape S{ minfo, polygons, id_set, poly_start, poly_end, kn, vn, ks, vs, mu };
-    if (PL.np) {
-        k_l_shape_face<<<nblk(PL.np, 128), 128, 0, S_(s)>>>(PL, S, isLineContact, pos, vel, omega, force, moment,
-                                                            sorted_id, cell_start, cell_end);
-        k_l_shape_edge<<<nblk(PL.np, 128), 128, 0, S_(s)>>>(PL, S, isLineContact, pos, vel, omega, force, moment,
-                                                            sorted_id, cell_start, cell_end);
+    const Shape S{ minfo, polygons, id_set, poly_start, poly_end, Fc{ kn, vn, ks, vs, mu } };
+    if (L.P.np) {
+        k_legacy_shape<true><<<warp_blocks(L.P.np), 256, 0, S_(s)>>>(L, S, isLineContact, pos, vel, omega, force,
+                                                                    moment, sorted_id, cell_start, cell_end);
+        k_legacy_shape<false><<<warp_blocks(L.P.np), 256, 0, S_(s)>>>(L, S, isLineContact, pos, vel, omega, force,
+                                                                     moment, sorted_id, cell_start, cell_end);
         st = launch_status("legacy_shape_hertzian_contact_force");
         if (st != XD_OK) return st;
     }
     if (np == 0) return XD_OK;
-    const unsigned nb = std::min(1024u, nblk(np, kLRed));
-    void* ws = workspace(sizeof(double) * (3 * (size_t)nb + 4), &st);
+    void* ws = workspace(reduction_scratch_bytes(np), &st);
     if (!ws) return st;
-    double* part = static_cast<double*>(ws);
-    double* dout = part + 3 * (size_t)nb;
-    k_l_sum_partial<<<nb, kLRed, 0, S_(s)>>>(force, np, part);
-    k_l_sum_final<<<1, 32, 0, S_(s)>>>(part, nb, dout);
-    st = launch_status("legacy_shape_hertzian_contact_force (sum)");
-    if (st != XD_OK) return st;
-    cudaError_t e = cudaMemcpyAsync(out, dout, sizeof(double) * 3, cudaMemcpyDeviceToHost, S_(s));
-    if (e == cudaSuccess) e = cudaStreamSynchronize(S_(s));
-    return cuda_status(e, "legacy_shape_hertzian_contact_force (sum)");
+    return reduction_d3(force, np, out, ws, S_(s));
 }
 
 int xd_legacy_update_polygons_position(const double* mpos, const double* A, const double* local_vertice,
@@ -710,7 +561,7 @@ int xd_legacy_update_polygons_position(const double* mpos, const double* A, cons
 {
     if (nvertex == 0) return XD_OK;
     XL_REQUIRE(mpos && A && local_vertice && pos, "legacy_update_polygons_position: null pointer");
-    k_l_polygons_position<<<nblk(nvertex, 256), 256, 0, S_(s)>>>(mpos, A, local_vertice, nvertex, pos);
+    k_legacy_place<<<nblk(nvertex, 256), 256, 0, S_(s)>>>(mpos, A, local_vertice, nvertex, pos);
     return launch_status("legacy_update_polygons_position");
 }
 
@@ -719,7 +570,7 @@ int xd_legacy_update_polygons_information(xd_legacy_polygon* polygons, const uns
 {
     if (ni == 0) return XD_OK;
     XL_REQUIRE(polygons && indice && pos, "legacy_update_polygons_information: null pointer");
-    k_l_polygons_information<<<nblk(ni, 256), 256, 0, S_(s)>>>(polygons, indice, pos, ni);
+    k_legacy_polygons<<<nblk(ni, 256), 256, 0, S_(s)>>>(polygons, indice, pos, ni);
     return launch_status("legacy_update_polygons_information");
 }
 
@@ -728,7 +579,7 @@ int xd_legacy_mergedata(double* data, const double* pos, unsigned np, const doub
 {
     if (np + snp == 0) return XD_OK;
     XL_REQUIRE(data && (pos || !np) && (vertice || !snp), "legacy_mergedata: null pointer");
-    k_l_mergedata<<<nblk(np + snp, 256), 256, 0, S_(s)>>>(data, pos, np, vertice, snp);
+    k_legacy_merge<<<nblk(np + snp, 256), 256, 0, S_(s)>>>(data, pos, np, vertice, snp);
     return launch_status("legacy_mergedata");
 }
 

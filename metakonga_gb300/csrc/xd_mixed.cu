@@ -1324,8 +1324,10 @@ struct Own {
 // handful of contacts of a particle stay well inside the 2e-5 gate.
 //  * normal force: the FP32 terms carry about kTermErr of the largest term;
 //  * slip: the FP32 rotation term w x r u carries about kRotErr of its
-//    magnitude; below the Coulomb cap the tangential force moves by
-//    (ks dt + vs) times that, at the cap its direction turns by that over |e|.
+//    terms' size |w| r (not of its value: a spin about the normal leaves a
+//    small cross product of large terms); below the Coulomb cap the
+//    tangential force moves by (ks dt + vs) times that, at the cap its
+//    direction turns by that over |e|.
 constexpr float kForceTol = 2e-6f;
 constexpr float kTermErr = 5e-7f;
 constexpr float kRotErr = 7e-7f;
@@ -1335,10 +1337,10 @@ __device__ __forceinline__ bool normal_needs_fp64(float term_max, float fn_abs, 
     return kTermErr * term_max > kForceTol * fmaxf(fn_abs, wfloor);
 }
 
-__device__ __forceinline__ bool slip_needs_fp64(float wt2, float ee, float lin, float mu, float fn_abs, float wfloor)
+__device__ __forceinline__ bool slip_needs_fp64(float wt, float ee, float lin, float mu, float fn_abs, float wfloor)
 {
-    if (!(wt2 > 0.f)) return false;
-    const float wt = sqrtf(wt2), me = sqrtf(ee);
+    if (!(wt > 0.f)) return false;
+    const float me = sqrtf(ee);
     const float scale = kForceTol * fmaxf(fn_abs, wfloor);
     if (lin * me >= mu * fn_abs) return kRotErr * wt * mu * fn_abs > scale * me;   // at the cap
     return kRotErr * wt * lin > scale;
@@ -1453,7 +1455,8 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     // kRotErr of |w x r|) could move the tangential force by more than
     // kForceTol of the contact's force scale max(|Fn|, m_i g): a sliding
     // contact (Coulomb cap) whose slip nearly cancels, or a fast spin.
-    if (P.rolling && slip_needs_fp64(fdot(wterm, wterm), ee, ks * dt + vs, P.fric, fabsf(fn), I.wfloor)) {
+    if (P.rolling && slip_needs_fp64(sqrtf(fdot(I.w, I.w)) * ir + sqrtf(fdot(wj, wj)) * jr, ee, ks * dt + vs, P.fric,
+                                     fabsf(fn), I.wfloor)) {
         count_one(counters + CN_SLIPS);
         ev = slip_pair(dvs, dvt, dqi, dn, rqc, rq0, rq1, I.qb.y, qbj.y, make_float4(I.w.x, I.w.y, I.w.z, 0.f),
                        __ldg(M.wl + i), wj4, __ldg(M.wl + j));
@@ -1604,7 +1607,8 @@ __device__ __forceinline__ f3 wall_force(const MixParams& P, const WallK& k, dou
         const dfl f = df_add(df_neg(df_mul(kn, df_mul(D, df_sqrt(D)))), df_mul(vn, d_to_df(rvu_d)));
         fn = __fadd_rn(f.hi, f.lo);
     }
-    if (P.rolling && slip_needs_fp64(fdot(wterm, wterm), ee, k.ks * P.dtf + k.vs, k.mu, fabsf(fn), wfloor)) {
+    if (P.rolling && slip_needs_fp64(sqrtf(wh.x * wh.x + wh.y * wh.y + wh.z * wh.z) * rf, ee, k.ks * P.dtf + k.vs,
+                                     k.mu, fabsf(fn), wfloor)) {
         // the rotation term cancels most of the slip
         count_one(counters + CN_SLIPS);
         const d3 iw = mk(df_to_d(wh.x, wl.x), df_to_d(wh.y, wl.y), df_to_d(wh.z, wl.z));

@@ -274,6 +274,23 @@ __device__ __forceinline__ d3 cross(d3 a, d3 b)
 }
 }  // namespace rn
 
+// The face region of a finite plane (impl:506-513): the overlap r - |dp . u|
+// with u = uw / |uw| turned against the side of xp (-sgn(dp . uw)).
+__device__ __forceinline__ double plane_face_depth(const PlaneD& pe, d3 xp, d3& u, double r)
+{
+    const d3 dp = rn::sub(xp, pe.xw);
+    const d3 uu = rn::divs(pe.uw, rn::length(pe.uw));
+    const int pp = -sgn(rn::dot(dp, pe.uw));
+    u = rn::scale((double)pp, uu);
+    return rn::sub(r, fabs(rn::dot(dp, u)));
+}
+
+// whether wp (plane-frame coordinates) lies in the face region
+__device__ __forceinline__ bool plane_face_region(const PlaneD& pe, d3 wp, double r)
+{
+    return fabs(wp.z) < r && (wp.x > 0 && wp.x < pe.l1) && (wp.y > 0 && wp.y < pe.l2);
+}
+
 // particle_plane_contact_detection (impl:487-570); pow(x, 2.0) is x * x
 // (IEEE: the correctly rounded square).
 __device__ __forceinline__ double plane_detection(const PlaneD& pe, d3 xp, d3 wp, d3& u, double r)
@@ -284,13 +301,7 @@ __device__ __forceinline__ double plane_detection(const PlaneD& pe, d3 xp, d3 wp
     const double sqb = rn::mul(wp.y, wp.y);
     const double sqc = rn::mul(wp.z, wp.z);
     const double sqr = rn::mul(r, r);
-    if (fabs(wp.z) < r && (wp.x > 0 && wp.x < pe.l1) && (wp.y > 0 && wp.y < pe.l2)) {
-        const d3 dp = rn::sub(xp, pe.xw);
-        const d3 uu = rn::divs(pe.uw, rn::length(pe.uw));
-        const int pp = -sgn(rn::dot(dp, pe.uw));
-        u = rn::scale((double)pp, uu);
-        return rn::sub(r, fabs(rn::dot(dp, u)));
-    }
+    if (plane_face_region(pe, wp, r)) return plane_face_depth(pe, xp, u, r);
     if (wp.x < 0 && wp.y < 0 && rn::add(rn::add(sqa, sqb), sqc) < sqr) {
         const d3 X = rn::sub(xp, pe.xw); const double h = rn::length(X); u = rn::divs(X, h); return rn::sub(r, h);
     } else if (wp.x > pe.l1 && wp.y < 0 && rn::add(rn::add(a_l1, sqb), sqc) < sqr) {
@@ -327,23 +338,30 @@ __device__ __forceinline__ d3 plane_coords(const PlaneD& pe, d3 xp)
     return mk(rn::dot(dp, pe.u1), rn::dot(dp, pe.u2), rn::dot(dp, pe.uw));
 }
 
-// closestPtPointTriangle (impl:837-899)
-__device__ __forceinline__ d3 closest_pt_triangle(d3 a, d3 b, d3 c, d3 p)
+// closestPtPointTriangle (impl:837-899), Ericson's region test; region: 0 a
+// vertex, 1 an edge, 2 the face (the legacy shape kernels branch on it,
+// cu_dem_impl.cuh:380-441).
+__device__ __forceinline__ d3 closest_pt_triangle_region(d3 a, d3 b, d3 c, d3 p, int& region)
 {
     const d3 ab = rn::sub(b, a), ac = rn::sub(c, a), ap = rn::sub(p, a);
     const double d1 = rn::dot(ab, ap), d2 = rn::dot(ac, ap);
+    region = 0;
     if (d1 <= 0.0 && d2 <= 0.0) return a;
     const d3 bp = rn::sub(p, b);
     const double d3_ = rn::dot(ab, bp), d4 = rn::dot(ac, bp);
     if (d3_ >= 0.0 && d4 <= d3_) return b;
     const double vc = rn::sub(rn::mul(d1, d4), rn::mul(d3_, d2));
+    region = 1;
     if (vc <= 0.0 && d1 >= 0.0 && d3_ <= 0.0) {
         const double v = rn::div(d1, rn::sub(d1, d3_));
         return rn::add(a, rn::scale(v, ab));
     }
     const d3 cp = rn::sub(p, c);
     const double d5 = rn::dot(ab, cp), d6 = rn::dot(ac, cp);
-    if (d6 >= 0.0 && d5 <= d6) return c;
+    if (d6 >= 0.0 && d5 <= d6) {
+        region = 0;
+        return c;
+    }
     const double vb = rn::sub(rn::mul(d5, d2), rn::mul(d1, d6));
     if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
         const double w = rn::div(d2, rn::sub(d2, d6));
@@ -354,10 +372,17 @@ __device__ __forceinline__ d3 closest_pt_triangle(d3 a, d3 b, d3 c, d3 p)
         const double w = rn::div(rn::sub(d4, d3_), rn::add(rn::sub(d4, d3_), rn::sub(d5, d6)));
         return rn::add(b, rn::scale(w, rn::sub(c, b)));
     }
+    region = 2;
     const double denom = rn::div(1.0, rn::add(rn::add(va, vb), vc));
     const double v = rn::mul(vb, denom);
     const double w = rn::mul(vc, denom);
     return rn::add(rn::add(a, rn::scale(v, ab)), rn::scale(w, ac));
+}
+
+__device__ __forceinline__ d3 closest_pt_triangle(d3 a, d3 b, d3 c, d3 p)
+{
+    int region;
+    return closest_pt_triangle_region(a, b, c, p, region);
 }
 
 // The face normal particle_polygonObject_collision_kernel<1> pushes along

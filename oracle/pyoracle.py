@@ -357,6 +357,11 @@ class RefKernels:
                                      _p(moment), _p(mass), _p(sorted_), _p(cstart), _p(cend),
                                      _p(cp), _u(pos.shape[0]))
 
+    def cylinder(self, prm, cyl, pos, vel, omega, force, moment, mass, cp, mpos, mf, mm):
+        self.set_params(prm)
+        self.lib.xdref_cylinder_contact_force(_p(cyl), _p(pos), _p(vel), _p(omega), _p(force), _p(moment),
+                                              _p(mass), _u(pos.shape[0]), _p(cp), _p(mpos), _p(mf), _p(mm))
+
     def plane(self, prm, plane, pos, vel, omega, force, moment, mass, cp):
         self.set_params(prm)
         self.lib.xdref_plane_contact_force(C.c_int(1), _p(plane), _p(pos), _p(vel), _p(omega),

@@ -155,6 +155,20 @@ void xdref_cube_contact_force(int tcm, device_plane_info* planes, double* pos, d
         xdref_plane_contact_force(tcm, planes + i, pos, vel, omega, force, moment, mass, np, cp);
 }
 
+/* def.cu:181-200 (cu_cylinder_hertzian_contact_force, TCM = 1): mf and mm
+ * are per-particle rows; every thread also zeroes row 0 (impl:732-733), so
+ * after the sequential launch row 0 holds zero unless np == 1. */
+void xdref_cylinder_contact_force(device_cylinder_info* cyl, double* pos, double* vel, double* omega,
+                                  double* force, double* moment, double* mass, unsigned np,
+                                  device_contact_property* cp, double* mpos, double* mf, double* mm)
+{
+    launch(np, 512, [&] {
+        cylinder_hertzian_contact_force_kernel<1>(cyl, (double4*)pos, (double3*)vel, (double3*)omega,
+                                                  (double3*)force, (double3*)moment, cp, mass, (double3*)mpos,
+                                                  (double3*)mf, (double3*)mm, np);
+    });
+}
+
 /* def.cu:203-221 */
 void xdref_particle_polygon_collision(int tcm, device_polygon_info* dpi, double* dsph,
                                       device_polygon_mass_info* dpmi, double* pos, double* vel,

@@ -56,3 +56,27 @@ def test_cloud_reaches_every_region(oracle):
     assert np.isfinite(f).all() and np.isfinite(mm).all()
     # the reaction is minus the normal force; the particle also gets the tangential part
     assert np.array_equal(np.linalg.norm(mf, axis=1) > 0, hit)
+
+
+def test_oracle_cylinder_equals_reference_kernel(oracle):
+    """Pin: the restatement against the reference's own cylinder kernel
+    (cylinder_hertzian_contact_force_kernel<1>, built as host code) on the
+    cloud, every region (lateral, end caps, rims): forces, moments and the
+    per-particle reactions bit for bit.  Row 0 of the reaction is left out:
+    every thread of the reference kernel zeroes it (impl:732-733)."""
+    import pytest
+    from oracle.pyoracle import RefKernels
+    if not RefKernels.available():
+        pytest.skip("reference kernels not built here (oracle/_ref needs the reference tree)")
+    ref = RefKernels()
+    c = cloud()
+    outs = []
+    for fn in (oracle.cylinder, ref.cylinder):
+        n = c["pos"].shape[0]
+        f, m, mf, mm = (np.zeros((n, 3)) for _ in range(4))
+        fn(c["prm"], c["cyl"], c["pos"], c["vel"], c["omega"], f, m, c["mass"], c["cp"], c["mpos"], mf, mm)
+        outs.append((f, m, mf, mm))
+    (f, m, mf, mm), (rf, rm, rmf, rmm) = outs
+    assert np.abs(f).max() > 0
+    assert np.array_equal(f, rf) and np.array_equal(m, rm)
+    assert np.array_equal(mf[1:], rmf[1:]) and np.array_equal(mm[1:], rmm[1:])

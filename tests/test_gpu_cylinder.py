@@ -2,7 +2,8 @@
 oracle on the cloud of tests/cylinder_case.py: forces, moments and the
 per-particle reaction on the cylinder within 1e-12 of each particle's force
 scale (the device atan/sin/cos and the oracle's libm may differ in the last
-place); the C++ drop-in name gives the same bits."""
+place); the C++ drop-in name (cu_cylinder_hertzian_contact_force, called by
+a program linked with libxdem_mphysics.so) gives the same bits."""
 
 import numpy as np
 import pytest
@@ -53,3 +54,41 @@ def test_cylinder_refuses_hmc(cuda):
     with pytest.raises(XdemError):
         call("xd_cylinder_contact_force", 0, ptr(t), ptr(t), ptr(t), ptr(t), ptr(t), ptr(t), ptr(t), 8, ptr(t),
              ptr(t), ptr(t), ptr(t), dem.stream_handle())
+
+
+def test_cylinder_drop_in_name_gives_the_same_bits(cuda, tmp_path):
+    import os
+    import shutil
+    import subprocess
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    pkg = os.path.join(root, "metakonga_gb300")
+    cr = os.path.dirname(os.path.dirname(shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"))
+    exe = tmp_path / "cylinder_call"
+    subprocess.run(["g++", "-O2", "-std=c++17", os.path.join(here, "cpp", "cylinder_call.cpp"),
+                    "-I", os.path.join(root, "include"), "-I", os.path.join(cr, "include"),
+                    "-L", pkg, "-lxdem_mphysics", "-lxdem", "-L", os.path.join(cr, "lib64"), "-lcudart",
+                    "-Wl,-rpath," + pkg, "-Wl,-rpath," + os.path.join(cr, "lib64"), "-o", str(exe)], check=True)
+    c = cloud()
+    n = c["pos"].shape[0]
+    f0 = c["mass"][:, None] * np.array([0.0, -9.81, 0.0])
+    with open(tmp_path / "in.bin", "wb") as fh:
+        fh.write(np.array([n], np.uint32).tobytes())
+        for a in (c["prm"], c["cyl"], c["cp"], np.asarray(c["mpos"], np.float64), c["pos"], c["vel"], c["omega"],
+                  f0, np.zeros((n, 3)), c["mass"]):
+            fh.write(np.ascontiguousarray(a).tobytes())
+    r = subprocess.run([str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin")], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(tmp_path / "out.bin", np.float64).reshape(4, n, 3)
+    d = {k: dem.to_dev(v) for k, v in (("pos", c["pos"]), ("vel", c["vel"]), ("omega", c["omega"]),
+                                       ("mass", c["mass"]), ("cyl", c["cyl"]), ("cp", c["cp"]),
+                                       ("mpos", c["mpos"]), ("force", f0), ("moment", np.zeros((n, 3))),
+                                       ("mf", np.zeros((n, 3))), ("mm", np.zeros((n, 3))))}
+    dem.set_symbolic_parameter(c["prm"])
+    call("xd_cylinder_contact_force", 1, ptr(d["cyl"]), ptr(d["pos"]), ptr(d["vel"]), ptr(d["omega"]),
+         ptr(d["force"]), ptr(d["moment"]), ptr(d["mass"]), n, ptr(d["cp"]), ptr(d["mpos"]), ptr(d["mf"]),
+         ptr(d["mm"]), dem.stream_handle())
+    torch.cuda.synchronize()
+    for k, g in zip(("force", "moment", "mf", "mm"), got):
+        assert np.array_equal(g, d[k].cpu().numpy()), k
