@@ -541,13 +541,17 @@ int xd_scene_stats(xd_scene* scene, unsigned long long* out, unsigned count, voi
  * capacities per particle (a fuller list makes that particle's contact pass
  * search its cells instead), and the contact pass's block size.  Set before
  * the scene's first upload (XD_ERR_STATE after); a batch launches its
- * contact pass with its first scene's block size.  Defaults: 0.1, 48, 16, 64.
+ * contact pass with its first scene's block size and pair pass.  Defaults:
+ * 0.1, 48, 16, 64, 1.
  * metakonga_gb300.tune chooses them per scene shape. */
 typedef struct xd_tuning {
     float skin_factor;          /* [0.02, 1] */
     unsigned verlet_cap;        /* [8, 256] */
     unsigned triangle_cap;      /* [4, 128] */
     unsigned contact_threads;   /* 32, 64 or 128 */
+    unsigned contact_mode;      /* pair pass: 0 a thread per listed particle, 1 warp-cooperative (the
+                                   warp's contacts spread one per lane, summed per particle in list
+                                   order: the same bits as 0) */
 } xd_tuning;
 int xd_scene_set_tuning(xd_scene* scene, const xd_tuning* tuning);
 int xd_scene_get_tuning(xd_scene* scene, xd_tuning* tuning);

@@ -70,6 +70,7 @@ constexpr unsigned kTriCap = 16;               // default: triangles per particl
 constexpr float kSkinFactor = 0.1f;            // default: skin width over the largest radius
 constexpr unsigned kContactThreads = 64;       // default block size of the contact pass
 constexpr unsigned kContactMaxThreads = 128;   // the largest block size a scene may choose
+constexpr unsigned kContactMode = 1;           // default pair pass: warp-cooperative
 constexpr unsigned kContactWarpsTotal = 152 * 16;   // warps of a full contact grid (every SM, 16 warps each)
 constexpr int kMaxBodies = 8;                  // polygon bodies of a mixed scene
 constexpr unsigned kGuardBit = 0x80000000u;    // list entry decided by the FP64 test
@@ -167,6 +168,7 @@ struct MixedScene {
     // tuning (xd_scene_set_tuning, before the first upload)
     float skin_factor = kSkinFactor;
     unsigned vcap = kVerletCap, tcap = kTriCap, cthreads = kContactThreads;
+    unsigned cmode = kContactMode;   // 0: a thread per listed particle; 1: warp-cooperative pairs
     unsigned active_req = ~0u;    // active count set before the first upload
     bool emitted = false;         // the particle count has changed since the graphs were made
     unsigned version = 0;         // raised whenever the step graphs are dropped (parameters changed)
@@ -282,6 +284,16 @@ __device__ __forceinline__ f3 operator+(f3 a, f3 b) { return fk(a.x + b.x, a.y +
 __device__ __forceinline__ f3 operator-(f3 a, f3 b) { return fk(a.x - b.x, a.y - b.y, a.z - b.z); }
 __device__ __forceinline__ f3 operator*(float s, f3 a) { return fk(s * a.x, s * a.y, s * a.z); }
 __device__ __forceinline__ float fdot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 fadd_rn(f3 a, f3 b)
+{
+    return fk(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z));
+}
+// a x b with every product and difference rounded on its own
+__device__ __forceinline__ f3 fcross_rn(f3 a, f3 b)
+{
+    return fk(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)), __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
+              __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
 __device__ __forceinline__ f3 fcross(f3 a, f3 b)
 {
     return fk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
@@ -1307,6 +1319,13 @@ struct PairAcc {
     f3 Ft, Mm, sumF, sumM;
 };
 
+// One pair contact's terms: the normal force, and -- when its slip is not
+// zero -- the tangential force and moment that replace the carried ones.
+struct PairOut {
+    f3 Fn, Ft, Mm;
+    bool slip;
+};
+
 // Own data of particle i for its force loop.
 struct Own {
     unsigned i;
@@ -1354,7 +1373,9 @@ __device__ __forceinline__ bool slip_needs_fp64(float wt, float ee, float lin, f
 // HIST: 0 the reference's DHS; 1 tangential springs kept in the table (an
 // extension, formed in FP64 from the FP32 normal, slip and normal force);
 // 2 the same read-only (diagnostic evaluation).
-template <int HIST>
+// OUT: the contact's terms go to *o instead of the running sums in A (the
+// warp-cooperative pass sums them in list order afterwards; see accumulate).
+template <int HIST, bool OUT = false>
 __device__ __forceinline__ void contact_force(const MixParams& P, const Master& M, const Own& I,
                                               unsigned j, bool guard, const double* __restrict__ mass0,
                                               const float4* __restrict__ pf,
@@ -1362,7 +1383,7 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
                                               const longlong2* __restrict__ qb,
                                               const float4* __restrict__ pr,
                                               unsigned* __restrict__ counters, PairAcc& A,
-                                              const HistTable& ht, HistState& hs)
+                                              const HistTable& ht, HistState& hs, PairOut* o = nullptr)
 {
     const unsigned i = I.i;
     const float dt = P.dtf;
@@ -1462,7 +1483,10 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
                        __ldg(M.wl + i), wj4, __ldg(M.wl + j));
         ee = fdot(ev, ev);
     }
-    const f3 Fn = fn * u;
+    // products and sums rounded one by one (no contraction into the sums), so
+    // that the per-particle and the warp-cooperative pair passes, which sum
+    // these terms in different places, give the same bits
+    const f3 Fn = fk(__fmul_rn(fn, u.x), __fmul_rn(fn, u.y), __fmul_rn(fn, u.z));
     if (HIST) {
         // the partner's key is its original index
         const unsigned key = __float_as_uint(__ldg(M.wl + j).w);
@@ -1484,15 +1508,42 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
         A.Mm = fk((float)Md.x, (float)Md.y, (float)Md.z);
     } else {
         const float mag_e = sqrtf(ee);
-        if (mag_e != 0.f) {
-            const f3 sh = (1.0f / mag_e) * ev;
-            // dv . sh = |e| exactly (sh is the unit slip direction)
-            A.Ft = fminf(ks * (mag_e * dt) + vs * mag_e, P.fric * fabsf(fn)) * sh;
-            A.Mm = fcross(ir * u, A.Ft);
+        if (OUT) {
+            o->Fn = Fn;
+            o->slip = mag_e != 0.f;
         }
+        if (mag_e != 0.f) {
+            const float ie = 1.0f / mag_e;
+            const f3 sh = fk(__fmul_rn(ie, ev.x), __fmul_rn(ie, ev.y), __fmul_rn(ie, ev.z));
+            // dv . sh = |e| exactly (sh is the unit slip direction)
+            const float ft = fminf(ks * (mag_e * dt) + vs * mag_e, P.fric * fabsf(fn));
+            const f3 Ft = fk(__fmul_rn(ft, sh.x), __fmul_rn(ft, sh.y), __fmul_rn(ft, sh.z));
+            const f3 Mm = fcross_rn(fk(__fmul_rn(ir, u.x), __fmul_rn(ir, u.y), __fmul_rn(ir, u.z)), Ft);
+            if (OUT) {
+                o->Ft = Ft;
+                o->Mm = Mm;
+                return;
+            }
+            A.Ft = Ft;
+            A.Mm = Mm;
+        }
+        if (OUT) return;
     }
-    A.sumF = A.sumF + (Fn + A.Ft);
-    A.sumM = A.sumM + A.Mm;
+    A.sumF = fadd_rn(A.sumF, fadd_rn(Fn, A.Ft));
+    A.sumM = fadd_rn(A.sumM, A.Mm);
+}
+
+// Adds one contact's terms to the particle's sums, as contact_force does in
+// its own loop: a contact with zero slip keeps the tangential force and
+// moment of the one before it (impl:390-400).
+__device__ __forceinline__ void accumulate(PairAcc& A, const PairOut& o)
+{
+    if (o.slip) {
+        A.Ft = o.Ft;
+        A.Mm = o.Mm;
+    }
+    A.sumF = fadd_rn(A.sumF, fadd_rn(o.Fn, A.Ft));
+    A.sumM = fadd_rn(A.sumM, A.Mm);
 }
 
 // Contact forces of the particles on the heavy list (the others keep the
@@ -2012,7 +2063,180 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
     if (RECORD) rec_count[i] = nc;
 }
 
-template <bool RECORD, int HIST>
+// ---- the warp-cooperative pair pass ------------------------------------------
+//
+// In a packed bed every listed particle has several contacts, and a thread
+// per particle leaves most lanes idle while the warp runs the longest list.
+// Here the 32 particles of a warp are done together in rounds.  Each lane
+// first scans its own particle's Verlet list (or its cells) and keeps up to
+// kCoopSlots touching partners in shared memory; then the warp's partners,
+// in lane order, are spread over the lanes, one contact per lane, each
+// forming its contact's force with contact_force; and each particle's lane
+// adds its own contacts' terms in its list order (accumulate).  The sums are
+// therefore the same bits as the per-particle pass's.  A lane with more
+// than kCoopSlots contacts goes on in the next round where it stopped.
+
+constexpr unsigned kCoopSlots = 16;
+
+struct CoopBuf {
+    unsigned cand[32 * kCoopSlots];   // lane L's partners at [L * kCoopSlots, ...)
+    float res[10][32];                // one contact per lane: Fn, Ft, Mm, slip
+};
+
+// Own data of slot i as contact_force reads it.
+__device__ __forceinline__ Own load_own(const MixParams& P, const ContactArgs& C, unsigned i)
+{
+    Own I;
+    I.i = i;
+    I.r = __ldg(C.pf + i).w;
+    I.qa = __ldg(C.qa + i);
+    I.qb = __ldg(C.qb + i);
+    I.vh = __ldg(C.M.vh + i);
+    I.vl = __ldg(C.M.vl + i);
+    const float4 w4 = __ldg(C.M.wh + i);
+    I.w = fk(w4.x, w4.y, w4.z);
+    I.im = I.vh.w;
+    I.wfloor = sqrtf(P.gf[0] * P.gf[0] + P.gf[1] * P.gf[1] + P.gf[2] * P.gf[2]) / I.im;
+    I.pr = __ldg(C.pr + i);
+    return I;
+}
+
+// The contact pass of list entries (valid lanes: slot i) without tangential
+// history, every lane of the warp taking part: pairs cooperatively, then
+// each particle's planes and triangles (walls_fp32) by its own lane.
+__device__ __forceinline__ void contact_entry_coop(const MixParams& P, const ContactArgs& C, bool valid, unsigned i,
+                                                   CoopBuf& B)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned n = P.n;
+    float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+    unsigned vc = 0;
+    longlong2 qai = make_longlong2(0, 0), qbi = make_longlong2(0, 0);
+    if (valid) {
+        pi = __ldg(C.pf + i);
+        vc = __ldg(C.vcount + i);
+        qai = __ldg(C.qa + i);
+        qbi = __ldg(C.qb + i);
+    }
+    const bool incomplete = (vc & kIncomplete) != 0u;
+    PairAcc A;
+    A.Ft = fk(0.f, 0.f, 0.f);
+    A.Mm = fk(0.f, 0.f, 0.f);
+    A.sumF = fk(0.f, 0.f, 0.f);
+    A.sumM = fk(0.f, 0.f, 0.f);
+    HistState hs;
+    unsigned kpos = 0, done = 0;
+    bool more = valid;
+    unsigned* mine = B.cand + lane * kCoopSlots;
+    while (__any_sync(0xffffffffu, more)) {
+        // this lane's next partners, in its search order
+        unsigned cnt = 0;
+        if (more) {
+            if (!incomplete) {
+                const float rt0 = pi.w + P.tol;
+                for (; kpos < vc && cnt < kCoopSlots; ++kpos) {
+                    const unsigned j = __ldg(C.vlist + (size_t)kpos * n + i);
+                    const float4 pj = __ldg(C.pf + j);
+                    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                    const float Rt = rt0 + pj.w;
+                    if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) >= Rt * Rt) continue;
+                    const int c = exact_touch<true>(P, C.M, i, j, qai, qbi, C.qa, C.qb, C.counters);
+                    if (c) mine[cnt++] = j | (c == 2 ? kGuardBit : 0u);
+                }
+                more = kpos < vc;
+            } else {
+                // the cells: searched again from the start each round, the
+                // partners before `done` skipped
+                unsigned seen = 0;
+                for_each_contact<true>(P, C.M, i, pi, qai, qbi, __ldg(C.keys + i), C.pf, C.qa, C.qb, C.lb,
+                                       C.counters, [&](unsigned j, bool guard) {
+                                           if (seen >= done && cnt < kCoopSlots)
+                                               mine[cnt++] = j | (guard ? kGuardBit : 0u);
+                                           ++seen;
+                                       });
+                done += cnt;
+                more = seen > done;
+            }
+        }
+        __syncwarp();
+        // the round's contacts in lane order: lane L owns [off, off + cnt)
+        unsigned incl = cnt;
+#pragma unroll
+        for (unsigned o = 1; o < 32u; o <<= 1) {
+            const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const unsigned off = incl - cnt;
+        const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+        for (unsigned base = 0; base < total; base += 32u) {
+            const unsigned c = base + lane;
+            // the owner of contact c: the last lane whose range starts at or before c
+            unsigned L = 0;
+#pragma unroll
+            for (unsigned b = 16; b; b >>= 1) {
+                const unsigned o = __shfl_sync(0xffffffffu, off, L + b);
+                if (o <= c) L += b;
+            }
+            const unsigned offL = __shfl_sync(0xffffffffu, off, L);
+            const unsigned iL = __shfl_sync(0xffffffffu, i, L);
+            if (c < total) {
+                const unsigned e = B.cand[L * kCoopSlots + (c - offL)];
+                const Own I = load_own(P, C, iL);
+                PairOut o;
+                contact_force<0, true>(P, C.M, I, e & ~kGuardBit, (e & kGuardBit) != 0u, C.mass0, C.pf, C.qa,
+                                       C.qb, C.pr, C.counters, A, C.ht, hs, &o);
+                B.res[0][lane] = o.Fn.x;
+                B.res[1][lane] = o.Fn.y;
+                B.res[2][lane] = o.Fn.z;
+                B.res[9][lane] = o.slip ? 1.f : 0.f;
+                if (o.slip) {
+                    B.res[3][lane] = o.Ft.x;
+                    B.res[4][lane] = o.Ft.y;
+                    B.res[5][lane] = o.Ft.z;
+                    B.res[6][lane] = o.Mm.x;
+                    B.res[7][lane] = o.Mm.y;
+                    B.res[8][lane] = o.Mm.z;
+                }
+            }
+            __syncwarp();
+            const unsigned q1 = min(off + cnt, base + 32u);
+            for (unsigned q = max(off, base); q < q1; ++q) {
+                const unsigned k = q - base;
+                PairOut o;
+                o.Fn = fk(B.res[0][k], B.res[1][k], B.res[2][k]);
+                o.slip = B.res[9][k] != 0.f;
+                if (o.slip) {
+                    o.Ft = fk(B.res[3][k], B.res[4][k], B.res[5][k]);
+                    o.Mm = fk(B.res[6][k], B.res[7][k], B.res[8][k]);
+                }
+                accumulate(A, o);
+            }
+            __syncwarp();
+        }
+    }
+    if (!valid) return;
+    float4 F = make_float4(A.sumF.x, A.sumF.y, A.sumF.z, 0.f);
+    unsigned wm = __ldg(C.wmask + i);
+    for (unsigned mask = wm; mask; mask &= mask - 1u) {
+        const int w = __ffs(mask) - 1;
+        const float hz = (pi.x - P.pxw[w][0]) * P.pun[w][0] + (pi.y - P.pxw[w][1]) * P.pun[w][1] +
+                         (pi.z - P.pxw[w][2]) * P.pun[w][2];
+        if (!(fabsf(hz) < pi.w + P.tol)) wm &= ~(1u << w);
+    }
+    const unsigned tc0 = P.ntri ? __ldg(C.tcount + i) : 0u;
+    if (wm || tc0) {
+        const f3 fw = walls_fp32(P, C, i, pi, wm, tc0);
+        F.x += fw.x;
+        F.y += fw.y;
+        F.z += fw.z;
+    }
+    C.Fc[i] = F;
+    C.Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
+}
+
+// COOP: the warp-cooperative pair pass (no history, no recording; dynamic
+// shared memory of one CoopBuf per warp).
+template <bool RECORD, int HIST, bool COOP>
 __global__ void __launch_bounds__(kContactMaxThreads) k_mx_contact(MixParams P, ContactArgs C)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) C.counters[CN_REBUILD] = 0;
@@ -2021,6 +2245,16 @@ __global__ void __launch_bounds__(kContactMaxThreads) k_mx_contact(MixParams P, 
     // turn: every SM gets an equal share however short the list
     const unsigned warps = gridDim.x * (blockDim.x / 32u);
     const unsigned gw = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u;
+    if (COOP) {
+        extern __shared__ CoopBuf coop_buf[];
+        CoopBuf& B = coop_buf[threadIdx.x / 32u];
+        for (unsigned t0 = gw * 32u; t0 < total; t0 += warps * 32u) {
+            const unsigned t = t0 + (threadIdx.x & 31u);
+            const bool valid = t < total;
+            contact_entry_coop(P, C, valid, valid ? __ldg(C.hlist + list_index(t, front, P.n)) : 0u, B);
+        }
+        return;
+    }
     for (unsigned t = gw * 32u + (threadIdx.x & 31u); t < total; t += warps * 32u)
         contact_entry<RECORD, HIST>(P, C, __ldg(C.hlist + list_index(t, front, P.n)));
 }
@@ -2944,7 +3178,7 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
         rp = s->rec_pairs;
     }
     const ContactArgs C = contact_args(s, rc, rp, record ? rec_cap : 0u, ht, MODE == 3 ? 0 : 1);
-#define XD_MX_CONTACT(REC, H) k_mx_contact<REC, H><<<grid, ct, 0, q>>>(s->P, C)
+#define XD_MX_CONTACT(REC, H) k_mx_contact<REC, H, false><<<grid, ct, 0, q>>>(s->P, C)
     if (record) {
         if (hist == 2) XD_MX_CONTACT(true, 2);
         else if (hist == 1) XD_MX_CONTACT(true, 1);
@@ -2952,6 +3186,8 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
     } else {
         if (hist == 2) XD_MX_CONTACT(false, 2);
         else if (hist == 1) XD_MX_CONTACT(false, 1);
+        else if (s->cmode == 1)
+            k_mx_contact<false, 0, true><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(s->P, C);
         else XD_MX_CONTACT(false, 0);
     }
 #undef XD_MX_CONTACT
@@ -3284,6 +3520,9 @@ int mixed_set_tuning(MixedScene* s, const xd_tuning* t)
     if (t->contact_threads != 32 && t->contact_threads != 64 && t->contact_threads != 128)
         return set_error(XD_ERR_INVALID, "scene_set_tuning: contact block of %u threads (32, 64 or 128)",
                          t->contact_threads);
+    if (t->contact_mode > 1)
+        return set_error(XD_ERR_INVALID, "scene_set_tuning: contact mode %u (0 or 1)", t->contact_mode);
+    s->cmode = t->contact_mode;
     s->skin_factor = t->skin_factor;
     s->vcap = t->verlet_cap;
     s->tcap = t->triangle_cap;
@@ -3297,6 +3536,7 @@ void mixed_get_tuning(const MixedScene* s, xd_tuning* t)
     t->verlet_cap = s->vcap;
     t->triangle_cap = s->tcap;
     t->contact_threads = s->cthreads;
+    t->contact_mode = s->cmode;
 }
 
 int mixed_set_kinematic(MixedScene* s, bool enable)
@@ -3408,6 +3648,7 @@ namespace {
 
 constexpr unsigned kBatchGroup = 32;
 constexpr unsigned kBatchGraphSteps = 4;   // later steps captured per graph launch
+constexpr unsigned kBatchGrab = 2;         // runs of 32 listed particles a contact warp takes at a time
 
 
 // One scene of a batch as the batch kernels read it.
@@ -3510,24 +3751,34 @@ __global__ void __launch_bounds__(1024) k_batch_chunks(const BatchScene* __restr
         if (threadIdx.x == 0) carry += c[1023];
         __syncthreads();
     }
-    if (threadIdx.x == 0) chunk_start[0] = 0;
+    if (threadIdx.x == 0) {
+        chunk_start[0] = 0;
+        chunk_start[ns + 1] = 0;   // the contact launch's next free run
+    }
 }
 
-// The contact pass of every scene: the warps share the runs of all scenes'
-// lists in contiguous ranges; a warp loads the scene of a run into its own
-// shared-memory slot when the scene changes.
+// The contact pass of every scene: each warp takes the next kBatchGrab runs
+// of all scenes' lists from a counter (chunk_start[ns + 1], cleared by
+// k_batch_chunks) until none are left, so that warps that drew cheap runs
+// take more; a run's result does not depend on which warp computes it.  A
+// warp loads the scene of a run into its own shared-memory slot when the
+// scene changes.
+template <bool COOP>
 __global__ void __launch_bounds__(kContactMaxThreads) k_batch_contact(const BatchScene* __restrict__ D, unsigned ns,
-                                                                   const unsigned* __restrict__ chunk_start)
+                                                                   unsigned* __restrict__ chunk_start)
 {
     __shared__ WarpScene ws[kContactMaxThreads / 32];
     const unsigned lane = threadIdx.x & 31u, wb = threadIdx.x / 32u;
     WarpScene& W = ws[wb];
-    const unsigned warps = gridDim.x * (blockDim.x / 32u);
-    const unsigned gw = blockIdx.x * (blockDim.x / 32u) + wb;
     const unsigned total = __ldg(chunk_start + ns);
-    const unsigned per = (total + warps - 1u) / warps;
-    const unsigned c0 = gw * per, c1 = min(total, c0 + per);
+    unsigned* next = chunk_start + ns + 1;
     unsigned cur = 0xffffffffu, lo = 0, heavy = 0, front = 0;
+    for (;;) {
+    unsigned c0 = 0;
+    if (lane == 0) c0 = atomicAdd(next, kBatchGrab);
+    c0 = __shfl_sync(0xffffffffu, c0, 0);
+    if (c0 >= total) break;
+    const unsigned c1 = min(total, c0 + kBatchGrab);
     for (unsigned ch = c0; ch < c1; ++ch) {
         if (cur == 0xffffffffu || ch >= __ldg(chunk_start + cur + 1)) {
             // the scene holding run ch: the last s with chunk_start[s] <= ch
@@ -3547,7 +3798,15 @@ __global__ void __launch_bounds__(kContactMaxThreads) k_batch_contact(const Batc
             front = W.C.counters[CN_HTRI];
         }
         const unsigned t = (ch - lo) * 32u + lane;
-        if (t < heavy) contact_entry<false, 0>(W.P, W.C, __ldg(W.C.hlist + list_index(t, front, W.P.n)));
+        if (COOP) {
+            extern __shared__ CoopBuf coop_buf[];
+            const bool valid = t < heavy;
+            contact_entry_coop(W.P, W.C, valid, valid ? __ldg(W.C.hlist + list_index(t, front, W.P.n)) : 0u,
+                               coop_buf[wb]);
+        } else if (t < heavy) {
+            contact_entry<false, 0>(W.P, W.C, __ldg(W.C.hlist + list_index(t, front, W.P.n)));
+        }
+    }
     }
 }
 
@@ -3567,6 +3826,7 @@ struct MixedBatch {
     cudaGraphExec_t finish_graph = nullptr;          // last kick and the body reactions
     bool captured = false;
     unsigned cthreads = kContactThreads;             // block size of the shared contact launch
+    unsigned cmode = kContactMode;                   // its pair pass (the first scene's choice)
     // direct launches (profilers; kernel timing): CUDA events around the
     // later steps' advance and every contact launch
     bool direct = false;
@@ -3576,6 +3836,16 @@ struct MixedBatch {
     double ms[2] = {};
     unsigned long long launches[2] = {};
 };
+
+// The batch's contact launch: every scene's listed particles.
+static void launch_batch_contact(const MixedBatch* b, unsigned ns, cudaStream_t q)
+{
+    const unsigned ct = b->cthreads, grid = kContactWarpsTotal * 32u / ct;
+    if (b->cmode == 1)
+        k_batch_contact<true><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(b->d_scenes, ns, b->d_chunks);
+    else
+        k_batch_contact<false><<<grid, ct, 0, q>>>(b->d_scenes, ns, b->d_chunks);
+}
 
 namespace {
 
@@ -3702,7 +3972,7 @@ int capture_batch_step(MixedBatch* b, int kind)
                              "batch capture dependencies");
         if (st == XD_OK) {
             k_batch_chunks<<<1, 1024, 0, cs>>>(b->d_scenes, ns, b->d_chunks);
-            k_batch_contact<<<kContactWarpsTotal * 32u / b->cthreads, b->cthreads, 0, cs>>>(b->d_scenes, ns, b->d_chunks);
+            launch_batch_contact(b, ns, cs);
             st = launch_status("batch contact");
         }
         if (st == XD_OK) st = current_deps(cs, &cg, &deps);
@@ -3791,7 +4061,7 @@ int prepare_batch(MixedBatch* b)
     M(&b->d_scenes, ns, "batch scenes");
     M(&b->d_block_scene, block_scene.size(), "batch blocks");
     M(&b->d_flags, ns, "batch flags");
-    M(&b->d_chunks, ns + 1, "batch runs");
+    M(&b->d_chunks, ns + 2, "batch runs");
     M(&b->d_handles[0], ng + ns, "batch handles");
     M(&b->d_handles[1], ng + ns, "batch handles");
     M(&b->d_handles[2], (size_t)(ng + ns) * kBatchGraphSteps, "batch handles");
@@ -3838,7 +4108,8 @@ int mixed_batch_create(MixedScene* const* scenes, unsigned count, MixedBatch** o
     MixedBatch* b = new (std::nothrow) MixedBatch();
     if (!b) return set_error(XD_ERR_NOMEM, "batch: host allocation");
     b->scenes.assign(scenes, scenes + count);
-    b->cthreads = scenes[0]->cthreads;   // the first scene's choice (one launch serves all)
+    b->cthreads = scenes[0]->cthreads;   // the first scene's choices (one launch serves all)
+    b->cmode = scenes[0]->cmode;
     const char* ng = getenv("XDEM_NO_GRAPHS");
     b->direct = ng && ng[0] && ng[0] != '0';
     *out = b;
@@ -3898,7 +4169,7 @@ int batch_step_direct(MixedBatch* b, unsigned nsteps, cudaStream_t q)
             if (flags[k]) st = rebuild(b->scenes[k], q);
         if (st != XD_OK) break;
         k_batch_chunks<<<1, 1024, 0, q>>>(b->d_scenes, ns, b->d_chunks);
-        span(1, [&] { k_batch_contact<<<kContactWarpsTotal * 32u / b->cthreads, b->cthreads, 0, q>>>(b->d_scenes, ns, b->d_chunks); });
+        span(1, [&] { launch_batch_contact(b, ns, q); });
         st = launch_status("batch contact");
     }
     if (st == XD_OK) {

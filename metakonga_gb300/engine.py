@@ -46,14 +46,15 @@ class Tuning(C.Structure):
     """xd_tuning: skin width over r_max, Verlet/triangle list capacities, and
     the contact pass's block size (mixed form; set before the first upload)."""
     _fields_ = [("skin_factor", C.c_float), ("verlet_cap", C.c_uint), ("triangle_cap", C.c_uint),
-                ("contact_threads", C.c_uint)]
+                ("contact_threads", C.c_uint), ("contact_mode", C.c_uint)]
 
     def as_dict(self) -> dict:
         return {k: (round(float(getattr(self, k)), 6) if k == "skin_factor" else int(getattr(self, k)))
                 for k, _ in self._fields_}
 
 
-DEFAULT_TUNING = {"skin_factor": 0.1, "verlet_cap": 48, "triangle_cap": 16, "contact_threads": 64}
+DEFAULT_TUNING = {"skin_factor": 0.1, "verlet_cap": 48, "triangle_cap": 16, "contact_threads": 64,
+                  "contact_mode": 1}
 
 
 class DeviceScene:

@@ -1,7 +1,7 @@
 """Autotuner for the mixed form: skin width, list capacities, contact block.
 
 The reference fixes its grid (128^3 cells of twice the largest radius,
-dem_simulation.cpp:259-261) and its launch shapes.  The mixed form has four
+dem_simulation.cpp:259-261) and its launch shapes.  The mixed form has five
 choices that trade against each other differently per scene:
 
 * the skin width (cells are 2 r_max + skin wide).  A wider skin re-bins less
@@ -9,7 +9,10 @@ choices that trade against each other differently per scene:
   holds more neighbours, and the contact pass tests them all each step;
 * the Verlet-list and triangle-list capacities: a particle whose list
   overflows has its contact pass search the cells instead (correct, slower);
-* the contact pass's block size (32, 64 or 128 threads).
+* the contact pass's block size (32, 64 or 128 threads);
+* its pair pass: a thread per listed particle (best when few particles touch
+  anything) or warp-cooperative (the warp's contacts spread one per lane:
+  best in packed beds).
 
 ``tune`` times candidate settings on a short window of the scene's own steps
 (CUDA events, the same step graphs a run replays) and keeps the fastest; the
@@ -17,7 +20,8 @@ list capacities are raised where the defaults' lists overflowed.  Results
 are cached in a JSON file keyed by the scene's shape -- particle count
 (octave), radius spread, walls and triangles, packing -- so that similar
 scenes reuse them (``tuned``).  Every setting gives the same contacts: the
-choices change only how the contact pass finds them.
+choices change only how the contact pass finds them (and the two pair
+passes give the same bits).
 """
 from __future__ import annotations
 
@@ -32,6 +36,7 @@ from . import engine
 
 SKINS = (0.05, 0.1, 0.2, 0.35)
 THREADS = (32, 64, 128)
+MODES = (0, 1)
 
 
 def cache_path() -> str:
@@ -124,6 +129,14 @@ def tune(sc, steps: int = 200, warm: int = 20, store: bool = True) -> dict:
             best, best_ms = cand, ms
     for th in THREADS:
         cand = dict(best, contact_threads=th)
+        if any(c == cand for _, c in results):
+            continue
+        ms, _ = _time(sc, cand, warm, steps)
+        results.append((ms, cand))
+        if ms < best_ms:
+            best, best_ms = cand, ms
+    for mode in MODES:
+        cand = dict(best, contact_mode=mode)
         if any(c == cand for _, c in results):
             continue
         ms, _ = _time(sc, cand, warm, steps)

@@ -26,6 +26,8 @@ def _packed():
     {"skin_factor": 0.35, "verlet_cap": 8, "triangle_cap": 4, "contact_threads": 32},   # lists overflow
     {"skin_factor": 0.05, "contact_threads": 128},
     {"skin_factor": 0.2, "verlet_cap": 96},
+    {"contact_mode": 0},
+    {"contact_mode": 0, "verlet_cap": 8},
 ])
 def test_tuned_settings_give_the_oracle_contacts(cuda, oracle, tuning):
     sc = _packed()
@@ -73,3 +75,39 @@ def test_autotuner_times_and_caches(cuda, monkeypatch, tmp_path):
     d = engine.DeviceScene(sc, mode=engine.MODE_MIXED, tuning=tune.tuned(sc))
     d.step(10, check=True)
     d.close()
+
+
+@pytest.mark.parametrize("case", ["packed", "packed_cells", "hopper_bed"])
+def test_contact_modes_give_the_same_bits(cuda, case):
+    """The warp-cooperative pair pass (contact_mode 1) sums each particle's
+    contacts in its list order, as the per-particle pass does: the states
+    after 20 steps and the contact forces are the same bits.  packed: up to
+    ~30 contacts per sphere (several rounds of kCoopSlots); packed_cells:
+    Verlet lists over capacity (the cell search, searched again per round);
+    hopper_bed: a settled bed against the cone's triangles and the floor."""
+    from metakonga_gb300 import prepare
+    extra = {}
+    if case == "hopper_bed":
+        sc = scenes.hopper(n=6000, seed=12, gate=True)
+        prepare.settle(sc, 3000, dt=4e-5)
+        prepare.open_gates(sc)
+    else:
+        sc = _packed()
+        if case == "packed_cells":
+            extra = {"verlet_cap": 8}
+    out = []
+    for mode in (0, 1):
+        d = engine.DeviceScene(sc, mode=engine.MODE_MIXED, tuning=dict(extra, contact_mode=mode))
+        d.step(20, check=True)
+        st = d.download()
+        f, m = d.eval_contacts()
+        stats = d.stats()
+        d.close()
+        out.append((st, f, m, stats))
+    (s0, f0, m0, t0), (s1, f1, m1, t1) = out
+    assert np.abs(f0).max() > 0
+    for k in ("pos", "vel", "omega"):
+        assert np.array_equal(s0[k], s1[k]), k
+    assert np.array_equal(f0, f1) and np.array_equal(m0, m1)
+    if case == "packed_cells":
+        assert t1["verlet_overflows"] > 0
