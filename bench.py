@@ -71,11 +71,11 @@ SERVED_WORKLOAD = "served_settle_and_hopper_requests"
 B_CONTACT = {"fp64": 140, "mixed": 116}   # algorithmic bytes per particle, contact kernel
 # k_mx_advance (the mixed form's dominant kernel), per particle and middle step:
 # reads x y z r (32), vh vl wh wl ab (80), b2 (8), Fc Mc (32), pref (16) = 168;
-# writes x y z (24), vh vl wh wl ab (80), b2 (8), pf qa qb (48) = 160.
-B_ADVANCE = 328
-# k_batch_contact / k_mx_contact, per listed sphere: reads pf 16, qa qb 32, vh vl 32, wh wl 32,
-# hlist 4, vcount 4, tcount 4, wmask 2; writes Fc Mc 32 = 158 B; plus 4 B per list entry
-B_LISTED = 158
+# writes x y z (24), vh vl wh wl ab (80), b2 (8), pf qa qb pr (64) = 176.
+B_ADVANCE = 344
+# k_batch_contact / k_mx_contact, per listed sphere: reads pf 16, qa qb 32, pr 16, vh vl 32, wh wl 32,
+# hlist 4, vcount 4, tcount 4, wmask 2; writes Fc Mc 32 = 174 B; plus 4 B per list entry
+B_LISTED = 174
 
 
 def _args():
@@ -90,7 +90,8 @@ def _args():
     ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"],
                     help="scene form for the headline value (the other is reported beside it)")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 side measurement")
-    ap.add_argument("--workload", default="batched", choices=["batched", "served", "box", "drum"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "served", "box", "drum", "hopper"])
+    ap.add_argument("--hopper-n", type=int, default=100_000, help="hopper workload: spheres")
     ap.add_argument("--no-served", action="store_true", help="batched: skip the served stream")
     ap.add_argument("--no-box", action="store_true", help="batched: skip the 1M-box roofline run")
     ap.add_argument("--no-drum", action="store_true", help="batched: skip the rotating-drum run")
@@ -104,6 +105,8 @@ def _args():
     ap.add_argument("--budget-gb", type=float, default=150.0, help="served device-memory budget")
     ap.add_argument("--chunk", type=int, default=50, help="served steps per scene per tick")
     ap.add_argument("--rates", default="", help="served: comma-separated arrival rates to sweep")
+    ap.add_argument("--no-tune", action="store_true", help="batched: default tuning, no autotuner run")
+    ap.add_argument("--tune-steps", type=int, default=50, help="batched: autotuner window (steps per candidate)")
     return ap.parse_args()
 
 
@@ -529,6 +532,11 @@ def run_ours(a):
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "cell_rebinnings_in_timed_steps": rebuilds,
+        "autotune": tuned,
+        "step_beyond_kernels_ms": {"value": other_ms, "of_step": other_ms / (ms / a.steps),
+                                   "note": "ms per batch step minus the advance and contact launches' live "
+                                           "times: re-binnings, the decision kernel, run prefix, graph and "
+                                           "conditional nodes -- the most a persistent kernel could save"},
         "roofline": roof,
         "phase_ms_per_launch": phase_ms,
         "other_form": plain,
@@ -620,7 +628,10 @@ def _fp64_check(sc, squeeze=0.92, seed=29, spin=True):
     return {"particles": int(st.np_), "touching": int(touching.sum()),
             "max_force_err": float(err.max()), "p999_force_err": float(np.percentile(err, 99.9)),
             "max_torque_over_r_err": float(merr.max()), "state": state,
-            "normaliser": "max(|F_fp64|, m g) per particle", "tolerance": 2e-5}
+            "normaliser": "max(|F_fp64|, m g) per particle",
+            "gate_note": ("the parity tests gate at 2e-5 of max(sum_c |F_c|, m g); this normaliser is the net "
+                          "force, about m g in a resting bed whose contacts each carry several m g, so it reads "
+                          "a few times stricter there")}
 
 
 def _box_roofline(a, stream, barrier, world, local):
@@ -637,8 +648,53 @@ def _box_roofline(a, stream, barrier, world, local):
     roof["workload"] = ("polydisperse_box_settle, 1,000,000 spheres (one scene, launched directly for "
                         "its phase events: the batch's launches sit inside one graph per step, which "
                         "events cannot split)")
-    return roof, {"value": world * sc.np_ * a.steps / (ms / 1e3), "ms_per_step": ms / a.steps,
-                  "gpu_launches": launches, "cell_rebinnings_in_timed_steps": rebuilds}
+    out = {"value": world * sc.np_ * a.steps / (ms / 1e3), "ms_per_step": ms / a.steps,
+           "gpu_launches": launches, "cell_rebinnings_in_timed_steps": rebuilds}
+    if not a.no_plain:
+        out["plain_fp64"] = _fp64_timed(sc, stream, 5)
+        out["plain_fp64_own_grid"] = _fp64_timed(_own_grid(sc), stream, 5)
+        out["plain_fp64_own_grid"]["grid"] = ("the FP64 form on a grid that holds the box unwrapped: cells of "
+                                              "2 r_max, power-of-two dimensions covering the particles (the "
+                                              "reference's 128^3 grid wraps the box's 250 cells of height onto "
+                                              "128, two spheres' worth per cell)")
+        out["ratio_to_plain_fp64_own_grid"] = out["value"] / out["plain_fp64_own_grid"]["value"]
+    return roof, out
+
+
+def _own_grid(sc):
+    """The scene with a grid that covers its particles without wrapping:
+    the reference's cell (2 r_max), power-of-two dimensions, the origin one
+    cell below the lowest particle."""
+    import numpy as np
+    s = sc.copy()
+    cell = float(sc.params["cell_size"])
+    lo = sc.pos[:, :3].min(axis=0) - cell
+    hi = sc.pos[:, :3].max(axis=0) + cell
+    g = [1 << int(np.ceil(np.log2(max(2.0, (h - l) / cell)))) for l, h in zip(lo, hi)]
+    s.params["grid"] = g
+    s.params["ncell"] = int(np.prod(g))
+    s.params["world_origin"] = lo
+    return s
+
+
+def _fp64_timed(sc, stream, steps, warmup=1):
+    """The scene in the FP64 form: device time of `steps` steps after
+    `warmup`."""
+    import torch
+
+    from metakonga_gb300 import engine
+    d = engine.DeviceScene(sc, mode=engine.MODE_FP64)
+    d.step(warmup, check=True, stream=stream.cuda_stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    d.step(steps, check=False, stream=stream.cuda_stream)
+    e1.record(stream)
+    e1.synchronize()
+    d.close()
+    ms = e0.elapsed_time(e1) / steps
+    return {"value": sc.np_ / (ms / 1e3), "ms_per_step": ms,
+            "grid": [int(x) for x in sc.params["grid"]], "cell": float(sc.params["cell_size"])}
 
 
 def _drum(a, stream, steps=200, warmup=3, plain=True):
@@ -737,9 +793,10 @@ def _serve_once(scs, reqs, rate, a, stream, mode):
 
 def _served(a, stream, plain=True):
     """The served request stream: report of the continuous-batching server
-    (cohorts), the same stream served side by side, a sweep of arrival rates
-    when a.rates lists them, and the same requests' time alone in the FP64
-    form."""
+    stepping its resident scenes side by side (the faster mode on this
+    stream), the same stream served in cohorts (a shared-launch batch per
+    admission wave), a sweep of arrival rates in both modes when a.rates
+    lists them, and the same requests' time alone in the FP64 form."""
     from metakonga_gb300 import scenes, serve
     t0 = time.perf_counter()
     reqs = scenes.served_requests(count=a.requests, seed=4)
@@ -747,7 +804,7 @@ def _served(a, stream, plain=True):
     gen_s = time.perf_counter() - t0
     arrivals = serve.poisson_arrivals(len(reqs), a.rate, seed=5)
     srv = serve.Server(budget_bytes=int(a.budget_gb * 1e9), chunk=a.chunk, stream=stream.cuda_stream,
-                       keep_results=True, cohorts=True)
+                       keep_results=True)
     for k, (r, sc) in enumerate(zip(reqs, scs)):
         srv.submit(k, sc, r["steps"], arrival=float(arrivals[k]))
     clk = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
@@ -762,9 +819,10 @@ def _served(a, stream, plain=True):
     rep["particles"] = [int(sc.np_) for sc in scs]
     rep["steps"] = [int(r["steps"]) for r in reqs]
     rep["kinds"] = [r["kind"] for r in reqs]
+    rep["mode"] = "side_by_side"
     rep["e2e_note"] = ("latency from arrival to the downloaded result: scene upload, steps and "
-                       "download through the public API (DeviceScene, engine.Batch per cohort)")
-    rep["side_by_side"] = _serve_once(scs, reqs, a.rate, a, stream, "side_by_side")
+                       "download through the public API (DeviceScene, xd_scene_step_many)")
+    rep["cohorts"] = _serve_once(scs, reqs, a.rate, a, stream, "cohorts")
     if a.rates:
         rep["sweep"] = [_serve_once(scs, reqs, float(x), a, stream, m)
                         for x in a.rates.split(",") for m in ("cohorts", "side_by_side")]
@@ -856,7 +914,21 @@ def run_batched(a):
     torch.cuda.synchronize()
     prep_s = time.perf_counter() - t0
     n_tot = sum(sc.np_ for sc in scs)
-    ds = [engine.DeviceScene(sc, mode=engine.MODE_MIXED) for sc in scs]
+    # the autotuner on the scene at the particle-weighted median (half the
+    # spheres are in larger scenes), its choice applied to every scene
+    tuned = None
+    tuning = dict(engine.DEFAULT_TUNING)
+    if not a.no_tune:
+        from metakonga_gb300 import tune
+        order = np.argsort([sc.np_ for sc in scs])
+        cum = np.cumsum([scs[k].np_ for k in order])
+        k_w = int(order[int(np.searchsorted(cum, cum[-1] / 2))])
+        tr = tune.tune(scs[k_w], steps=a.tune_steps, warm=5, store=False)
+        tuning = dict(tr["tuning"])
+        tuned = {"scene": k_w, "particles": int(scs[k_w].np_), "choice": tuning,
+                 "scene_ms_per_step": tr["ms_per_step"], "scene_default_ms_per_step": tr["default_ms_per_step"],
+                 "candidates": tr["candidates"], "window_steps": tr["window_steps"], "seconds": tr["seconds"]}
+    ds = [engine.DeviceScene(sc, mode=engine.MODE_MIXED, tuning=tuning) for sc in scs]
     dev_bytes = sum(d.device_bytes() for d in ds)
     batch = engine.Batch(ds)
     batch.step(a.warmup, check=True, stream=sh)
@@ -882,7 +954,13 @@ def run_batched(a):
     kt = batch.kernel_times()
     batch.set_timing(False)
     adv_ms = kt["advance"][0] / max(kt["advance"][1], 1)
-    con_ms = kt["contact"][0] / max(kt["contact"][1], 1)
+    pair_ms = kt["contact"][0] / max(kt["contact"][1], 1)
+    wall_ms = kt["walls"][0] / max(kt["contact"][1], 1)   # per step (0 without a wall pass)
+    con_ms = pair_ms + wall_ms
+    # what a step costs beyond its two big kernels (the decision kernel, run
+    # prefix, graph and conditional nodes, and the re-binnings): the most a
+    # persistent batch kernel could save
+    other_ms = ms / a.steps - adv_ms - con_ms
     adv_gbs = n_tot * B_ADVANCE / (adv_ms / 1e3) / 1e9
     con_gbs = contact_bytes / (con_ms / 1e3) / 1e9
     adv_traffic = _traffic_from_profiles("advance_batch_hopper.md", "traffic_bytes_per_particle")
@@ -893,9 +971,11 @@ def run_batched(a):
                     "avg_launch_ms": adv_ms, "bytes": n_tot * B_ADVANCE, "bytes_per_particle": B_ADVANCE,
                     "achieved": adv_gbs, "frac": adv_gbs / peak,
                     "traffic": adv_traffic * n_tot if adv_traffic else None},
-        "contact": {"kernel": "k_batch_contact (every scene's listed spheres in one launch: pairs over the Verlet "
-                              "lists, planes and triangles in reach)",
-                    "avg_launch_ms": con_ms, "bytes": contact_bytes, "listed": listed,
+        "contact": {"kernel": "k_batch_contact<1> + <2> (every scene's listed spheres: the cooperative pair pass "
+                              "over the Verlet lists in one launch, then the wall pass over the listed spheres "
+                              "with planes or triangles in reach in another)",
+                    "avg_launch_ms": con_ms, "pair_pass_ms": pair_ms, "wall_pass_ms": wall_ms,
+                    "bytes": contact_bytes, "listed": listed,
                     "bytes_per_listed_sphere": contact_bytes / max(listed, 1),
                     "mean_verlet_entries": vlen, "mean_triangle_entries": tlen,
                     "achieved": con_gbs, "frac": con_gbs / peak,
@@ -915,7 +995,8 @@ def run_batched(a):
     # per step: advance, decision, run prefix and contact over all scenes; per
     # call the finish and each scene's body-reaction sum; per re-binning its
     # kernels and its group's decision kernel
-    launches = (4 * a.steps + 1 + sum(1 for sc in scs if sc.ntri)
+    walls_pass = 1 if tuning.get("contact_mode", 1) == 1 else 0   # the cooperative pass's wall launch
+    launches = ((4 + walls_pass) * a.steps + 1 + sum(1 for sc in scs if sc.ntri)
                 + sum((b[0] - r[0]) * (b[1] + 1) for r, b in zip(rb0, rb1)))
 
     # e2e: every scene's state uploaded from pinned host memory, K steps, the
@@ -980,6 +1061,23 @@ def run_batched(a):
     # FP64 check on the median scene's settled bed
     check = _fp64_check(scs[k_med], squeeze=1.0, spin=False)
     check["scene"] = k_med
+    # the batch with the default tuning, for the autotuner's gain
+    if tuned is not None:
+        if tuning != engine.DEFAULT_TUNING:
+            ds0 = [engine.DeviceScene(sc, mode=engine.MODE_MIXED) for sc in scs]
+            b0 = engine.Batch(ds0)
+            b0.step(a.warmup, check=True, stream=sh)
+            ms0, _ = _time_batch(b0, a.steps, stream, barrier, world)
+            b0.close()
+            for d in ds0:
+                d.close()
+            del ds0
+            torch.cuda.empty_cache()
+            tuned["batch_default_ms_per_step"] = ms0 / a.steps
+        else:
+            tuned["batch_default_ms_per_step"] = ms / a.steps
+        tuned["batch_ms_per_step"] = ms / a.steps
+        tuned["gain"] = tuned["batch_default_ms_per_step"] / tuned["batch_ms_per_step"]
     box_roof, box = _box_roofline(a, stream, barrier, world, local) if not a.no_box else (None, None)
     settle = _settle_small(stream, cpu=not a.no_cpu_baseline) if rank == 0 and not a.no_box else None
     if box:
@@ -1026,6 +1124,11 @@ def run_batched(a):
                 "job": f"upload all {len(scs)} states from pinned host memory, {a.steps} steps, download"},
         "gpu_launches": launches,
         "cell_rebinnings_in_timed_steps": rebuilds,
+        "autotune": tuned,
+        "step_beyond_kernels_ms": {"value": other_ms, "of_step": other_ms / (ms / a.steps),
+                                   "note": "ms per batch step minus the advance and contact launches' live "
+                                           "times: re-binnings, the decision kernel, run prefix, graph and "
+                                           "conditional nodes -- the most a persistent kernel could save"},
         "lattice_start": lattice,
         "plain_fp64": plain,
         "fp64_check": check,
@@ -1088,6 +1191,79 @@ def run_drum(a):
     print(json.dumps(line), flush=True)
 
 
+def _settled_hopper(n, seed=5, prep_steps=5000, prep_dt=4e-5):
+    """One hopper of n spheres as a settled bed with its orifice open (the
+    batch's preparation), cached in the temp directory so that a profiler's
+    run of this workload loads it instead of launching the preparation."""
+    import tempfile
+
+    import numpy as np
+
+    from metakonga_gb300 import prepare, scenes
+    sc = scenes.hopper(n=n, seed=seed, gate=True)
+    path = os.path.join(tempfile.gettempdir(), f"xdem_hopper_settled_{n}_seed{seed}_{prep_steps}.npz")
+    keys = ("pos", "vel", "acc", "omega", "alpha")
+    try:
+        z = np.load(path)
+        for k in keys:
+            getattr(sc, k)[:] = z[k]
+    except (OSError, KeyError, ValueError):
+        prepare.settle(sc, prep_steps, dt=prep_dt)
+        try:
+            np.savez(path, **{k: getattr(sc, k) for k in keys})
+        except OSError:
+            pass
+    prepare.open_gates(sc)
+    return sc
+
+
+def run_hopper(a):
+    """One settled hopper (a.hopper_n spheres, the batch's preparation) in
+    the mixed form, its contact pass timed per kernel: the workload the
+    contact-pass profiles are taken on."""
+    import torch
+
+    from metakonga_gb300 import engine
+    world, rank, local, barrier = _torch_setup()
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    sc = _settled_hopper(a.hopper_n, prep_steps=a.prep_steps, prep_dt=a.prep_dt)
+    d = engine.DeviceScene(sc, mode=engine.MODE_MIXED)
+    d.step(a.warmup, check=True, stream=sh)
+    st0 = d.stats(sh)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(local)
+    with clk:
+        e0.record(stream)
+        d.step(a.steps, check=False, stream=sh)
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    st1 = d.stats(sh)
+    d.set_timing(True)
+    d.step(a.steps, check=False, stream=sh)
+    ph = d.phase_times()
+    d.set_timing(False)
+    d.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": world * sc.np_ * a.steps / (ms / 1e3), "unit": METRIC, "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic (seeded MT19937 hopper, settled with its orifice gated, then opened)",
+        "config": {"workload": f"hopper_settled_{sc.np_}", "particles": int(sc.np_), "triangles": int(sc.ntri),
+                   "dt": 5e-6, "mode": "mixed", "l2": "state < L2 (a single-scene profile case)"},
+        "phases_ms": {k: v[0] / max(v[1], 1) for k, v in ph.items() if v[1]},
+        "per_step": {k: (st1[k] - st0[k]) / a.steps for k in ("fp64_decisions", "fp64_normal_forces",
+                                                              "fp64_slips", "fp64_wall_regions")},
+        "listed": st1["contact_list"], "listed_with_walls": st1["listed_with_triangles"],
+        "verlet_entries": st1["verlet_entries"], "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = _args()
     if a.impl == "reference":
@@ -1098,6 +1274,8 @@ def main():
         run_served(a)
     elif a.workload == "drum":
         run_drum(a)
+    elif a.workload == "hopper":
+        run_hopper(a)
     else:
         run_ours(a)
 

@@ -661,12 +661,13 @@ int xd_batch_destroy(xd_batch* batch);
  * kernels directly (the same kernels; the re-binning flags are read on the
  * host) with CUDA events around the advance of every step but a call's first
  * and around every contact launch.  xd_batch_kernel_times returns their
- * summed milliseconds and launch counts, [0] advance and [1] contact, since
- * timing was enabled.  XDEM_NO_GRAPHS=1 in the environment also makes a batch
+ * summed milliseconds and launch counts, [0] advance, [1] pair pass (the
+ * whole contact pass in contact_mode 0) and [2] wall pass, since timing was
+ * enabled.  XDEM_NO_GRAPHS=1 in the environment also makes a batch
  * launch directly (profilers list no kernel inside a graph with conditional
  * nodes). */
 int xd_batch_set_timing(xd_batch* batch, int enable);
-int xd_batch_kernel_times(xd_batch* batch, double ms[2], unsigned long long launches[2]);
+int xd_batch_kernel_times(xd_batch* batch, double ms[3], unsigned long long launches[3]);
 
 #ifdef __cplusplus
 }

@@ -86,7 +86,7 @@ enum {
     CN_SLIPS = 6,      // FP64 slip rechecks (cumulative)
     CN_REBUILDS = 7,   // re-binnings (cumulative)
     CN_RXN = 8,        // blocks of k_rxn_sum done (the last one finishes the sum)
-    CN_HTRI = 9,       // listed particles with triangles in reach: hlist[0, CN_HTRI)
+    CN_HTRI = 9,       // listed particles with walls (planes, triangles) in reach: hlist[0, CN_HTRI)
     CN_HBACK = 10,     // the other listed particles: hlist[n - CN_HBACK, n)
     CN_WALLS = 11,     // wall contacts decided by the FP64 region test (cumulative)
     CN_VINC = 12,      // Verlet lists over their capacity at the last build (the pass searches the cells)
@@ -905,13 +905,10 @@ __device__ __forceinline__ double fp64_cdist(const Master& M, unsigned i, unsign
 // integer separation against the radii, and the FP64 guard band.  Returns 0
 // (no contact), 1 (contact) or 2 (contact decided by the FP64 test).
 template <bool COUNT>
-__device__ __forceinline__ int exact_touch(const MixParams& P, const Master& M, unsigned i, unsigned j,
-                                           const longlong2& qai, const longlong2& qbi,
-                                           const longlong2* __restrict__ qa,
-                                           const longlong2* __restrict__ qb,
-                                           unsigned* __restrict__ counters)
+__device__ __forceinline__ int exact_touch_q(const MixParams& P, const Master& M, unsigned i, unsigned j,
+                                             const longlong2& qai, const longlong2& qbi, const longlong2& qaj,
+                                             const longlong2& qbj, unsigned* __restrict__ counters)
 {
-    const longlong2 qaj = __ldg(qa + j), qbj = __ldg(qb + j);
     const long long ddx = qaj.x - qai.x, ddy = qaj.y - qai.y, ddz = qbj.x - qbi.x;
     const long long Rq = qbi.y + qbj.y;
     const long long N = Rq * Rq - (ddx * ddx + ddy * ddy + ddz * ddz);
@@ -920,6 +917,16 @@ __device__ __forceinline__ int exact_touch(const MixParams& P, const Master& M, 
     if (N < -band) return 0;
     if (COUNT) count_one(counters + CN_DECISIONS);
     return fp64_cdist(M, i, j) > 0 ? 2 : 0;
+}
+
+template <bool COUNT>
+__device__ __forceinline__ int exact_touch(const MixParams& P, const Master& M, unsigned i, unsigned j,
+                                           const longlong2& qai, const longlong2& qbi,
+                                           const longlong2* __restrict__ qa,
+                                           const longlong2* __restrict__ qb,
+                                           unsigned* __restrict__ counters)
+{
+    return exact_touch_q<COUNT>(P, M, i, j, qai, qbi, __ldg(qa + j), __ldg(qb + j), counters);
 }
 
 // The candidate test of pair (i, j): FP32 prefilter, then the exact test.
@@ -1293,12 +1300,13 @@ __global__ void __launch_bounds__(256) k_mx_build(MixParams P, const float4* __r
         vcount[i] = nv > P.vcap ? (P.vcap | kIncomplete) : nv;
         if (nv > P.vcap) count_one(counters + CN_VINC);
         count_add(counters + CN_VSUM, min(nv, P.vcap));
-        tri = P.ntri && __ldg(tcount + i) != 0u;
-        heavy = nv > 0 || wm != 0u || tri;
+        tri = (P.ntri && __ldg(tcount + i) != 0u) || wm != 0u;   // walls in reach
+        heavy = nv > 0 || tri;
     }
-    // the spheres with triangles in reach first, the others from the end:
-    // the contact pass's warps then run the FP64 triangle work side by side
-    // instead of on a few lanes each
+    // the spheres with walls (planes or triangles) in reach first, the others
+    // from the end: the wall pass takes the front of the list, and in the
+    // per-particle pass the warps run the wall work side by side instead of
+    // on a few lanes each
     warp_append(heavy && tri, i, hlist, counters + CN_HTRI);
     const unsigned bal = __ballot_sync(0xffffffffu, heavy && !tri);
     if (bal) {
@@ -1634,9 +1642,16 @@ __device__ __forceinline__ WallK wall_constants(const double* c43Eeq, const doub
     return k;
 }
 
-__device__ __forceinline__ f3 wall_force(const MixParams& P, const WallK& k, double cd, d3 u, d3 dvd, double r,
-                                         double m, float rf, float wfloor, const float4& wh, const float4& wl,
-                                         unsigned* __restrict__ counters, f3& Ft)
+// One wall contact's terms: the normal force and, when the slip is not zero,
+// the tangential force (else the one carried from the contact before stays).
+struct WallOut {
+    f3 Fn, Ft;
+    bool slip;
+};
+
+__device__ __forceinline__ WallOut wall_force(const MixParams& P, const WallK& k, double cd, d3 u, d3 dvd, double r,
+                                              double m, float rf, float wfloor, const float4& wh, const float4& wl,
+                                              unsigned* __restrict__ counters)
 {
     const float df = (float)cd;
     const f3 uf = fk((float)u.x, (float)u.y, (float)u.z);
@@ -1668,12 +1683,207 @@ __device__ __forceinline__ f3 wall_force(const MixParams& P, const WallK& k, dou
         ev = fk((float)(dv.x - dn * u.x), (float)(dv.y - dn * u.y), (float)(dv.z - dn * u.z));
         ee = fdot(ev, ev);
     }
+    WallOut o;
+    // products rounded one by one, so that the per-particle and the
+    // cooperative wall passes, which add these terms in different places,
+    // give the same bits
+    o.Fn = fk(__fmul_rn(fn, uf.x), __fmul_rn(fn, uf.y), __fmul_rn(fn, uf.z));
     const float mag_e = sqrtf(ee);
-    if (mag_e != 0.f) {
+    o.slip = mag_e != 0.f;
+    if (o.slip) {
         // dv . s = |e| (s the unit slip direction)
-        Ft = fminf(k.ks * (mag_e * P.dtf) + k.vs * mag_e, k.mu * fabsf(fn)) * ((1.0f / mag_e) * ev);
+        const float ft = fminf(k.ks * (mag_e * P.dtf) + k.vs * mag_e, k.mu * fabsf(fn));
+        const float ie = 1.0f / mag_e;
+        o.Ft = fk(__fmul_rn(ft, __fmul_rn(ie, ev.x)), __fmul_rn(ft, __fmul_rn(ie, ev.y)),
+                  __fmul_rn(ft, __fmul_rn(ie, ev.z)));
     }
-    return fn * uf + Ft;
+    return o;
+}
+
+// The wall data of particle i that its wall contacts read.
+struct WallOwn {
+    float4 pi, vh, vl, wh, wl;
+    d3 ip, iv;
+    double r, m;
+    float mf, wfloor;
+};
+
+__device__ __forceinline__ WallOwn load_wall_own(const MixParams& P, const ContactArgs& C, unsigned i)
+{
+    const Master& M = C.M;
+    WallOwn o;
+    o.pi = __ldg(C.pf + i);
+    o.vh = __ldg(M.vh + i);
+    o.vl = __ldg(M.vl + i);
+    o.wh = __ldg(M.wh + i);
+    o.wl = __ldg(M.wl + i);
+    o.m = __ldg(C.mass0 + __float_as_uint(o.wl.w));
+    o.mf = (float)o.m;
+    o.wfloor = o.mf * sqrtf(P.gf[0] * P.gf[0] + P.gf[1] * P.gf[1] + P.gf[2] * P.gf[2]);
+    o.ip = mk(__ldg(M.x + i), __ldg(M.y + i), __ldg(M.z + i));
+    o.r = __ldg(M.r + i);
+    o.iv = mk(df_to_d(o.vh.x, o.vl.x), df_to_d(o.vh.y, o.vl.y), df_to_d(o.vh.z, o.vl.z));
+    return o;
+}
+
+// One wall candidate's result: kind 0 none, 1 plane, 2 triangle (of body b,
+// po2cp its contact point from the body's origin, FP32).
+struct WallRes {
+    unsigned kind, b;
+    WallOut o;
+    f3 po2cp;
+};
+
+constexpr unsigned kWallPlane = 0x80000000u;   // candidate code: plane w is kWallPlane | w, triangle t is t
+
+// Wall candidate `code` of particle i: plane_contact_force_kernel<1>
+// (impl:572-621) for a plane, particle_polygonObject_collision_kernel<1>
+// (impl:923-1021) for a triangle.  A contact whose closest point is clearly
+// inside the face in the FP32 region test (relative to the sphere centre)
+// is found by one FP64 plane distance; every other contact, and any within
+// kWallGuard of touching, by the reference's FP64 region test, rounded per
+// operation, so every contact decision is the reference's.
+__device__ __forceinline__ WallRes wall_eval(const MixParams& P, const ContactArgs& C, const WallOwn& w,
+                                             unsigned code)
+{
+    unsigned* __restrict__ counters = C.counters;
+    const float rf = w.pi.w;
+    WallRes res;
+    res.kind = 0;
+    if (code & kWallPlane) {
+        const unsigned pw = code & ~kWallPlane;
+        const PlaneRec* pr = C.prec + pw;
+        const d3 dp = w.ip - mk(__ldg(pr->xw), __ldg(pr->xw + 1), __ldg(pr->xw + 2));
+        const float dx = (float)dp.x, dy = (float)dp.y, dz = (float)dp.z;
+        const float wx = dx * __ldg(pr->u1) + dy * __ldg(pr->u1 + 1) + dz * __ldg(pr->u1 + 2);
+        const float wy = dx * __ldg(pr->u2) + dy * __ldg(pr->u2 + 1) + dz * __ldg(pr->u2 + 2);
+        const float l1 = __ldg(&pr->l1), l2 = __ldg(&pr->l2);
+        const float mg = 1e-6f * (fabsf(dx) + fabsf(dy) + fabsf(dz) + l1 + l2);
+        double cd = -1.0;
+        d3 unit;
+        bool exact = true;
+        if (wx > mg && wx < l1 - mg && wy > mg && wy < l2 - mg) {
+            // inside the rectangle: the face region (impl:557-560)
+            const d3 n = mk(__ldg(pr->n), __ldg(pr->n + 1), __ldg(pr->n + 2));
+            const double h = dp.x * n.x + dp.y * n.y + dp.z * n.z;
+            cd = w.r - fabs(h);
+            if (cd < -kWallGuard) return res;
+            if (cd > kWallGuard && fabs(h) > 1e-12) {
+                exact = false;
+                unit = h < 0.0 ? n : -n;
+            }
+        }
+        if (exact) {
+            count_one(counters + CN_WALLS);
+            const PlaneD pe = load_plane(C.planes + pw);
+            cd = plane_detection(pe, w.ip, plane_coords(pe, w.ip), unit, w.r);
+            if (!(cd > 0)) return res;
+        }
+        const WallK k = wall_constants(P.pl_c43Eeq + pw, P.pl_one_b2 + pw, P.pl_sratio[pw], P.pl_fric[pw], rf, w.mf);
+        res.kind = 1;
+        res.o = wall_force(P, k, cd, unit, -w.iv, w.r, w.m, rf, w.wfloor, w.wh, w.wl, counters);
+        return res;
+    }
+    const unsigned t = code;
+    const TriRec* tr = C.trec + t;
+    const d3 sp = w.ip - mk(__ldg(tr->p), __ldg(tr->p + 1), __ldg(tr->p + 2));   // x - P
+    const float sx = (float)sp.x, sy = (float)sp.y, sz = (float)sp.z;
+    const float qx = __ldg(tr->q) - sx, qy = __ldg(tr->q + 1) - sy, qz = __ldg(tr->q + 2) - sz;
+    const float cx = __ldg(tr->r) - sx, cy = __ldg(tr->r + 1) - sy, cz = __ldg(tr->r + 2) - sz;
+    bool face;
+    const float d2f = tri_dist2_f(-sx, -sy, -sz, qx, qy, qz, cx, cy, cz, face);
+    {
+        // out of reach by more than the FP32 error: no contact in FP64 either
+        const float span = fabsf(sx) + fabsf(sy) + fabsf(sz) + fabsf(qx) + fabsf(qy) + fabsf(qz) + fabsf(cx) +
+                           fabsf(cy) + fabsf(cz);
+        const float lim = rf + 1e-6f + 1e-5f * span;
+        if (d2f > lim * lim && d2f < 3.0e38f) return res;
+    }
+    const d3 u = mk(__ldg(tr->n), __ldg(tr->n + 1), __ldg(tr->n + 2));
+    double cd = -1.0;
+    d3 cpt;
+    bool exact = true;
+    if (face) {
+        const double h = sp.x * u.x + sp.y * u.y + sp.z * u.z;   // n . (x - P)
+        cd = w.r - fabs(h);
+        if (cd < -kWallGuard) return res;
+        if (cd > kWallGuard) {
+            exact = false;
+            cpt = w.ip - h * u;
+        }
+    }
+    if (exact) {
+        count_one(counters + CN_WALLS);
+        const xd_polygon_info* tri = C.poly + t;
+        cpt = closest_pt_triangle(tri_vertex(tri->P), tri_vertex(tri->Q), tri_vertex(tri->R), w.ip);
+        cd = rn::sub(w.r, rn::length(rn::sub(w.ip, cpt)));
+        if (!(cd > 0)) return res;
+    }
+    const unsigned b = __ldg(&tr->body);
+    // getConstant with the body's hoisted material terms (Meq = m, Req = r)
+    const WallK k = wall_constants(P.pb_c43Eeq + b, P.pb_one_b2 + b, P.pb_sratio[b], P.pb_fric[b], rf, w.mf);
+    const xd_polygon_mass_info* body = C.pmi + b;
+    const d3 po2cp = cpt - tri_vertex(body->origin);
+    const d3 pvel = tri_vertex(body->vel);
+    const d3 dvd = P.rolling ? (pvel + cross(tri_vertex(body->omega), po2cp)) - w.iv : pvel - w.iv;
+    res.kind = 2;
+    res.b = b;
+    res.o = wall_force(P, k, cd, u, dvd, w.r, w.m, rf, w.wfloor, w.wh, w.wl, counters);
+    res.po2cp = fk((float)po2cp.x, (float)po2cp.y, (float)po2cp.z);
+    return res;
+}
+
+// The reaction of a particle's run of triangle contacts on one body, added
+// to the particle's slots of rxn when the body changes and at the end
+// (consecutive contacts on the same body are summed in registers first: the
+// slots are read and written once per run instead of once per contact).
+struct RxnAcc {
+    unsigned b;
+    double v[6];
+};
+
+__device__ __forceinline__ void rxn_flush(const ContactArgs& C, unsigned n, unsigned i, RxnAcc& a)
+{
+    if (a.b == 0xffffffffu) return;
+    double* rb = C.rxn + (size_t)a.b * 6 * n + i;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) rb[(size_t)q * n] += a.v[q];
+    a.b = 0xffffffffu;
+}
+
+// Adds one wall result to particle i's wall force f, in candidate order: a
+// plane starts from Ft = 0 (each plane is its own launch in the reference);
+// triangles carry Ft from one to the next when a slip is exactly zero; the
+// reaction on the triangle's body (-fc and -(po2cp x fc)) goes to the run
+// accumulator a.
+__device__ __forceinline__ void wall_add(const ContactArgs& C, unsigned n, unsigned i, const WallRes& r, f3& f,
+                                         f3& Ftri, RxnAcc& a)
+{
+    if (r.kind == 0) return;
+    f3 Ft;
+    if (r.kind == 1) {
+        Ft = r.o.slip ? r.o.Ft : fk(0.f, 0.f, 0.f);
+    } else {
+        if (r.o.slip) Ftri = r.o.Ft;
+        Ft = Ftri;
+    }
+    const f3 fc = fadd_rn(r.o.Fn, Ft);
+    f = fadd_rn(f, fc);
+    if (r.kind == 2 && C.rxn_on) {
+        if (a.b != r.b) {
+            rxn_flush(C, n, i, a);
+            a.b = r.b;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) a.v[q] = 0.0;
+        }
+        const f3 rm = fcross_rn(fc, r.po2cp);   // -(po2cp x fc)
+        a.v[0] -= (double)fc.x;
+        a.v[1] -= (double)fc.y;
+        a.v[2] -= (double)fc.z;
+        a.v[3] += (double)rm.x;
+        a.v[4] += (double)rm.y;
+        a.v[5] += (double)rm.z;
+    }
 }
 
 // The wall contacts of listed particle i (the reference's DHS model, no
@@ -1691,50 +1901,12 @@ __device__ __forceinline__ f3 wall_force(const MixParams& P, const WallK& k, dou
 __device__ __forceinline__ f3 walls_fp32(const MixParams& P, const ContactArgs& C, const unsigned i, const float4 pi,
                                       const unsigned wm, const unsigned tc)
 {
-    const Master& M = C.M;
-    unsigned* __restrict__ counters = C.counters;
-    const float4 vh = __ldg(M.vh + i), vl = __ldg(M.vl + i), wh = __ldg(M.wh + i), wl = __ldg(M.wl + i);
-    const double m = __ldg(C.mass0 + __float_as_uint(wl.w));
-    const float mf = (float)m;
-    const float wfloor = mf * sqrtf(P.gf[0] * P.gf[0] + P.gf[1] * P.gf[1] + P.gf[2] * P.gf[2]);
-    const d3 ip = mk(__ldg(M.x + i), __ldg(M.y + i), __ldg(M.z + i));
-    const double r = __ldg(M.r + i);
-    const float rf = pi.w;
-    const d3 iv = mk(df_to_d(vh.x, vl.x), df_to_d(vh.y, vl.y), df_to_d(vh.z, vl.z));
-    f3 f = fk(0.f, 0.f, 0.f);
-    for (unsigned mask = wm; mask; mask &= mask - 1u) {
-        const int w = __ffs(mask) - 1;
-        const PlaneRec* pr = C.prec + w;
-        const d3 dp = ip - mk(__ldg(pr->xw), __ldg(pr->xw + 1), __ldg(pr->xw + 2));
-        const float dx = (float)dp.x, dy = (float)dp.y, dz = (float)dp.z;
-        const float wx = dx * __ldg(pr->u1) + dy * __ldg(pr->u1 + 1) + dz * __ldg(pr->u1 + 2);
-        const float wy = dx * __ldg(pr->u2) + dy * __ldg(pr->u2 + 1) + dz * __ldg(pr->u2 + 2);
-        const float l1 = __ldg(&pr->l1), l2 = __ldg(&pr->l2);
-        const float mg = 1e-6f * (fabsf(dx) + fabsf(dy) + fabsf(dz) + l1 + l2);
-        double cd = -1.0;
-        d3 unit;
-        bool exact = true;
-        if (wx > mg && wx < l1 - mg && wy > mg && wy < l2 - mg) {
-            // inside the rectangle: the face region (impl:557-560)
-            const d3 n = mk(__ldg(pr->n), __ldg(pr->n + 1), __ldg(pr->n + 2));
-            const double h = dp.x * n.x + dp.y * n.y + dp.z * n.z;
-            cd = r - fabs(h);
-            if (cd < -kWallGuard) continue;
-            if (cd > kWallGuard && fabs(h) > 1e-12) {
-                exact = false;
-                unit = h < 0.0 ? n : -n;
-            }
-        }
-        if (exact) {
-            count_one(counters + CN_WALLS);
-            const PlaneD pe = load_plane(C.planes + w);
-            cd = plane_detection(pe, ip, plane_coords(pe, ip), unit, r);
-            if (!(cd > 0)) continue;
-        }
-        const WallK k = wall_constants(P.pl_c43Eeq + w, P.pl_one_b2 + w, P.pl_sratio[w], P.pl_fric[w], rf, mf);
-        f3 Ft = fk(0.f, 0.f, 0.f);
-        f = f + wall_force(P, k, cd, unit, -iv, r, m, rf, wfloor, wh, wl, counters, Ft);
-    }
+    const WallOwn w = load_wall_own(P, C, i);
+    f3 f = fk(0.f, 0.f, 0.f), Ftri = fk(0.f, 0.f, 0.f);
+    RxnAcc ra;
+    ra.b = 0xffffffffu;
+    for (unsigned mask = wm; mask; mask &= mask - 1u)
+        wall_add(C, P.n, i, wall_eval(P, C, w, kWallPlane | (unsigned)(__ffs(mask) - 1)), f, Ftri, ra);
     if (tc) {
         const unsigned n = P.n;
         const bool listed = !(tc & kIncomplete);
@@ -1744,69 +1916,11 @@ __device__ __forceinline__ f3 walls_fp32(const MixParams& P, const ContactArgs& 
             kb = lower_bound_u(C.tpk, C.tcap, key);
             ke = lower_bound_u(C.tpk, C.tcap, key + 1u);
         }
-        f3 Ft = fk(0.f, 0.f, 0.f);
-        unsigned cb = 0xffffffffu;
-        WallK k;
         for (unsigned kk = kb; kk < ke; ++kk) {
             const unsigned t = listed ? __ldg(C.tlist + (size_t)kk * n + i) : __ldg(C.tpt + kk);
-            const TriRec* tr = C.trec + t;
-            const d3 sp = ip - mk(__ldg(tr->p), __ldg(tr->p + 1), __ldg(tr->p + 2));   // x - P
-            const float sx = (float)sp.x, sy = (float)sp.y, sz = (float)sp.z;
-            const float qx = __ldg(tr->q) - sx, qy = __ldg(tr->q + 1) - sy, qz = __ldg(tr->q + 2) - sz;
-            const float cx = __ldg(tr->r) - sx, cy = __ldg(tr->r + 1) - sy, cz = __ldg(tr->r + 2) - sz;
-            bool face;
-            const float d2f = tri_dist2_f(-sx, -sy, -sz, qx, qy, qz, cx, cy, cz, face);
-            {
-                // out of reach by more than the FP32 error: no contact in FP64 either
-                const float span = fabsf(sx) + fabsf(sy) + fabsf(sz) + fabsf(qx) + fabsf(qy) + fabsf(qz) +
-                                   fabsf(cx) + fabsf(cy) + fabsf(cz);
-                const float lim = rf + 1e-6f + 1e-5f * span;
-                if (d2f > lim * lim && d2f < 3.0e38f) continue;
-            }
-            const d3 u = mk(__ldg(tr->n), __ldg(tr->n + 1), __ldg(tr->n + 2));
-            double cd = -1.0;
-            d3 cpt;
-            bool exact = true;
-            if (face) {
-                const double h = sp.x * u.x + sp.y * u.y + sp.z * u.z;   // n . (x - P)
-                cd = r - fabs(h);
-                if (cd < -kWallGuard) continue;
-                if (cd > kWallGuard) {
-                    exact = false;
-                    cpt = ip - h * u;
-                }
-            }
-            if (exact) {
-                count_one(counters + CN_WALLS);
-                const xd_polygon_info* tri = C.poly + t;
-                cpt = closest_pt_triangle(tri_vertex(tri->P), tri_vertex(tri->Q), tri_vertex(tri->R), ip);
-                cd = rn::sub(r, rn::length(rn::sub(ip, cpt)));
-                if (!(cd > 0)) continue;
-            }
-            const unsigned b = __ldg(&tr->body);
-            if (b != cb) {
-                // getConstant with the body's hoisted material terms (Meq = m,
-                // Req = r): the same for every triangle of the body
-                k = wall_constants(P.pb_c43Eeq + b, P.pb_one_b2 + b, P.pb_sratio[b], P.pb_fric[b], rf, mf);
-                cb = b;
-            }
-            const xd_polygon_mass_info* body = C.pmi + b;
-            const d3 po2cp = cpt - tri_vertex(body->origin);
-            const d3 pvel = tri_vertex(body->vel);
-            const d3 dvd = P.rolling ? (pvel + cross(tri_vertex(body->omega), po2cp)) - iv : pvel - iv;
-            const f3 fc = wall_force(P, k, cd, u, dvd, r, m, rf, wfloor, wh, wl, counters, Ft);
-            f = f + fc;
-            if (C.rxn_on) {
-                const f3 rm = fcross(fc, fk((float)po2cp.x, (float)po2cp.y, (float)po2cp.z));   // -(po2cp x fc)
-                double* rb = C.rxn + (size_t)b * 6 * n + i;
-                rb[0] -= (double)fc.x;
-                rb[n] -= (double)fc.y;
-                rb[2 * (size_t)n] -= (double)fc.z;
-                rb[3 * (size_t)n] += (double)rm.x;
-                rb[4 * (size_t)n] += (double)rm.y;
-                rb[5 * (size_t)n] += (double)rm.z;
-            }
+            wall_add(C, n, i, wall_eval(P, C, w, t), f, Ftri, ra);
         }
+        rxn_flush(C, n, i, ra);
     }
     return f;
 }
@@ -2134,14 +2248,32 @@ __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const Con
         if (more) {
             if (!incomplete) {
                 const float rt0 = pi.w + P.tol;
-                for (; kpos < vc && cnt < kCoopSlots; ++kpos) {
-                    const unsigned j = __ldg(C.vlist + (size_t)kpos * n + i);
-                    const float4 pj = __ldg(C.pf + j);
-                    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                    const float Rt = rt0 + pj.w;
-                    if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) >= Rt * Rt) continue;
-                    const int c = exact_touch<true>(P, C.M, i, j, qai, qbi, C.qa, C.qb, C.counters);
-                    if (c) mine[cnt++] = j | (c == 2 ? kGuardBit : 0u);
+                // four list entries at a time, their loads issued together
+                // (the partner's view and fixed point are loaded whether or
+                // not the prefilter passes: most entries touch in a bed)
+                while (kpos < vc && cnt < kCoopSlots) {
+                    unsigned jj[4];
+                    float4 pp[4];
+                    longlong2 aa[4], bb[4];
+#pragma unroll
+                    for (unsigned q = 0; q < 4u; ++q)
+                        jj[q] = kpos + q < vc ? __ldg(C.vlist + (size_t)(kpos + q) * n + i) : i;
+#pragma unroll
+                    for (unsigned q = 0; q < 4u; ++q) {
+                        pp[q] = __ldg(C.pf + jj[q]);
+                        aa[q] = __ldg(C.qa + jj[q]);
+                        bb[q] = __ldg(C.qb + jj[q]);
+                    }
+#pragma unroll
+                    for (unsigned q = 0; q < 4u; ++q) {
+                        if (kpos >= vc || cnt >= kCoopSlots) break;
+                        ++kpos;
+                        const float dx = pp[q].x - pi.x, dy = pp[q].y - pi.y, dz = pp[q].z - pi.z;
+                        const float Rt = rt0 + pp[q].w;
+                        if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) >= Rt * Rt) continue;
+                        const int c = exact_touch_q<true>(P, C.M, i, jj[q], qai, qbi, aa[q], bb[q], C.counters);
+                        if (c) mine[cnt++] = jj[q] | (c == 2 ? kGuardBit : 0u);
+                    }
                 }
                 more = kpos < vc;
             } else {
@@ -2215,23 +2347,127 @@ __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const Con
         }
     }
     if (!valid) return;
-    float4 F = make_float4(A.sumF.x, A.sumF.y, A.sumF.z, 0.f);
-    unsigned wm = __ldg(C.wmask + i);
-    for (unsigned mask = wm; mask; mask &= mask - 1u) {
-        const int w = __ffs(mask) - 1;
-        const float hz = (pi.x - P.pxw[w][0]) * P.pun[w][0] + (pi.y - P.pxw[w][1]) * P.pun[w][1] +
-                         (pi.z - P.pxw[w][2]) * P.pun[w][2];
-        if (!(fabsf(hz) < pi.w + P.tol)) wm &= ~(1u << w);
-    }
-    const unsigned tc0 = P.ntri ? __ldg(C.tcount + i) : 0u;
-    if (wm || tc0) {
-        const f3 fw = walls_fp32(P, C, i, pi, wm, tc0);
-        F.x += fw.x;
-        F.y += fw.y;
-        F.z += fw.z;
-    }
-    C.Fc[i] = F;
+    // the walls are added by the wall pass (walls_entry)
+    C.Fc[i] = make_float4(A.sumF.x, A.sumF.y, A.sumF.z, 0.f);
     C.Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
+}
+
+// The wall pass after the cooperative pair pass, warp-cooperative as well:
+// the listed particles with walls in reach (the front of the list) list
+// their wall candidates (planes in reach, then their triangles) into the
+// warp's buffer, the candidates are spread one per lane (wall_eval), and
+// each particle's lane adds its results in candidate order (wall_add) and
+// then its wall force to its pair force -- the additions the per-particle
+// pass makes after its pairs (F += walls).  A launch of its own: the wall
+// code's FP64 region tests and registers stay out of the pair pass.
+__device__ __forceinline__ void walls_entry_coop(const MixParams& P, const ContactArgs& C, bool valid, unsigned i,
+                                                 CoopBuf& B)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned n = P.n;
+    unsigned wm = 0, kb = 0, ke = 0;
+    bool listed = true;
+    if (valid) {
+        const float4 pi = __ldg(C.pf + i);
+        wm = __ldg(C.wmask + i);
+        for (unsigned mask = wm; mask; mask &= mask - 1u) {
+            const int w = __ffs(mask) - 1;
+            const float hz = (pi.x - P.pxw[w][0]) * P.pun[w][0] + (pi.y - P.pxw[w][1]) * P.pun[w][1] +
+                             (pi.z - P.pxw[w][2]) * P.pun[w][2];
+            if (!(fabsf(hz) < pi.w + P.tol)) wm &= ~(1u << w);
+        }
+        const unsigned tc = P.ntri ? __ldg(C.tcount + i) : 0u;
+        listed = !(tc & kIncomplete);
+        ke = tc;
+        if (!listed) {
+            const unsigned key = __ldg(C.keys + i);
+            kb = lower_bound_u(C.tpk, C.tcap, key);
+            ke = lower_bound_u(C.tpk, C.tcap, key + 1u);
+        }
+    }
+    const bool any = wm || kb < ke;
+    f3 f = fk(0.f, 0.f, 0.f), Ftri = fk(0.f, 0.f, 0.f);
+    RxnAcc ra;
+    ra.b = 0xffffffffu;
+    unsigned* mine = B.cand + lane * kCoopSlots;
+    bool more = any;
+    while (__any_sync(0xffffffffu, more)) {
+        unsigned cnt = 0;
+        for (; more && wm && cnt < kCoopSlots; wm &= wm - 1u) mine[cnt++] = kWallPlane | (unsigned)(__ffs(wm) - 1);
+        for (; more && kb < ke && cnt < kCoopSlots; ++kb)
+            mine[cnt++] = listed ? __ldg(C.tlist + (size_t)kb * n + i) : __ldg(C.tpt + kb);
+        more = more && (wm || kb < ke);
+        __syncwarp();
+        unsigned incl = cnt;
+#pragma unroll
+        for (unsigned o = 1; o < 32u; o <<= 1) {
+            const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const unsigned off = incl - cnt;
+        const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+        for (unsigned base = 0; base < total; base += 32u) {
+            const unsigned c = base + lane;
+            unsigned L = 0;
+#pragma unroll
+            for (unsigned b = 16; b; b >>= 1) {
+                const unsigned o = __shfl_sync(0xffffffffu, off, L + b);
+                if (o <= c) L += b;
+            }
+            const unsigned offL = __shfl_sync(0xffffffffu, off, L);
+            const unsigned iL = __shfl_sync(0xffffffffu, i, L);
+            if (c < total) {
+                const WallOwn w = load_wall_own(P, C, iL);
+                const WallRes r = wall_eval(P, C, w, B.cand[L * kCoopSlots + (c - offL)]);
+                B.res[0][lane] = r.o.Fn.x;
+                B.res[1][lane] = r.o.Fn.y;
+                B.res[2][lane] = r.o.Fn.z;
+                B.res[3][lane] = r.o.Ft.x;
+                B.res[4][lane] = r.o.Ft.y;
+                B.res[5][lane] = r.o.Ft.z;
+                B.res[6][lane] = r.po2cp.x;
+                B.res[7][lane] = r.po2cp.y;
+                B.res[8][lane] = r.po2cp.z;
+                B.res[9][lane] = __uint_as_float(r.kind | (r.kind && r.o.slip ? 4u : 0u) | (r.b << 3));
+            }
+            __syncwarp();
+            const unsigned q1 = min(off + cnt, base + 32u);
+            for (unsigned q = max(off, base); q < q1; ++q) {
+                const unsigned k = q - base;
+                const unsigned code = __float_as_uint(B.res[9][k]);
+                WallRes r;
+                r.kind = code & 3u;
+                r.b = code >> 3;
+                r.o.slip = (code & 4u) != 0u;
+                r.o.Fn = fk(B.res[0][k], B.res[1][k], B.res[2][k]);
+                r.o.Ft = fk(B.res[3][k], B.res[4][k], B.res[5][k]);
+                r.po2cp = fk(B.res[6][k], B.res[7][k], B.res[8][k]);
+                wall_add(C, n, i, r, f, Ftri, ra);
+            }
+            __syncwarp();
+        }
+    }
+    if (!valid || !any) return;
+    rxn_flush(C, n, i, ra);
+    float4 F = C.Fc[i];
+    F.x += f.x;
+    F.y += f.y;
+    F.z += f.z;
+    C.Fc[i] = F;
+}
+
+__global__ void __launch_bounds__(kContactMaxThreads) k_mx_walls(MixParams P, ContactArgs C)
+{
+    extern __shared__ CoopBuf coop_buf[];
+    CoopBuf& B = coop_buf[threadIdx.x / 32u];
+    const unsigned front = C.counters[CN_HTRI];
+    const unsigned warps = gridDim.x * (blockDim.x / 32u);
+    const unsigned gw = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u;
+    for (unsigned t0 = gw * 32u; t0 < front; t0 += warps * 32u) {
+        const unsigned t = t0 + (threadIdx.x & 31u);
+        const bool valid = t < front;
+        walls_entry_coop(P, C, valid, valid ? __ldg(C.hlist + t) : 0u, B);
+    }
 }
 
 // COOP: the warp-cooperative pair pass (no history, no recording; dynamic
@@ -3186,9 +3422,10 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
     } else {
         if (hist == 2) XD_MX_CONTACT(false, 2);
         else if (hist == 1) XD_MX_CONTACT(false, 1);
-        else if (s->cmode == 1)
+        else if (s->cmode == 1) {
             k_mx_contact<false, 0, true><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(s->P, C);
-        else XD_MX_CONTACT(false, 0);
+            if (s->P.nplanes || s->P.ntri) k_mx_walls<<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(s->P, C);
+        } else XD_MX_CONTACT(false, 0);
     }
 #undef XD_MX_CONTACT
     st = launch_status("mixed contact");
@@ -3321,7 +3558,9 @@ unsigned long long mixed_launches(MixedScene* s, unsigned nsteps)
     if (!s || nsteps == 0 || s->n == 0) return 0;
     // per step: advance + contact; + the last velocity update; a step that
     // re-bins adds mixed_rebuild_launches()
-    const unsigned long long per = 2 + (s->kinematic && s->ntri ? 3 : 0);
+    // (and the wall pass after a cooperative pair pass)
+    const unsigned long long per = 2 + (s->kinematic && s->ntri ? 3 : 0) +
+                                   (s->cmode == 1 && (s->P.nplanes || s->P.ntri) ? 1 : 0);
     unsigned long long total = per * nsteps + 1 + (s->nbodies ? 1 : 0);
     if (!s->cells_clean) total += mixed_rebuild_launches(s);   // the first step re-bins
     return total;
@@ -3727,16 +3966,18 @@ __global__ void k_batch_group(const unsigned* __restrict__ flags, unsigned first
     if (t < count && flags[first + t]) cudaGraphSetConditional(hs[first + t], 1u);
 }
 
-// Runs of 32 listed particles per scene, as an exclusive prefix over scenes.
-__global__ void __launch_bounds__(1024) k_batch_chunks(const BatchScene* __restrict__ D, unsigned ns,
-                                                       unsigned* __restrict__ chunk_start)
+// Runs of 32 listed particles per scene, as an exclusive prefix over scenes,
+// of counter word `cw` (CN_HEAVY: every listed particle; CN_HTRI: those with
+// walls in reach) into runs[0, ns]; runs[ns + 1] (the launch's next free
+// run) cleared.
+__device__ void batch_runs(const BatchScene* __restrict__ D, unsigned ns, unsigned cw, unsigned* __restrict__ runs,
+                           unsigned* c, unsigned& carry)
 {
-    __shared__ unsigned c[1024];
-    __shared__ unsigned carry;
     if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
     for (unsigned base = 0; base < ns; base += 1024u) {
         const unsigned sc = base + threadIdx.x;
-        const unsigned h = sc < ns ? D[sc].C.counters[CN_HEAVY] : 0u;
+        const unsigned h = sc < ns ? D[sc].C.counters[cw] : 0u;
         c[threadIdx.x] = (h + 31u) / 32u;
         __syncthreads();
         // inclusive scan (Hillis-Steele)
@@ -3746,15 +3987,27 @@ __global__ void __launch_bounds__(1024) k_batch_chunks(const BatchScene* __restr
             c[threadIdx.x] += v;
             __syncthreads();
         }
-        if (sc < ns) chunk_start[sc + 1] = carry + c[threadIdx.x];
+        if (sc < ns) runs[sc + 1] = carry + c[threadIdx.x];
         __syncthreads();
         if (threadIdx.x == 0) carry += c[1023];
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        chunk_start[0] = 0;
-        chunk_start[ns + 1] = 0;   // the contact launch's next free run
+        runs[0] = 0;
+        runs[ns + 1] = 0;
     }
+    __syncthreads();
+}
+
+// The runs of the contact launch (chunk_start) and of the wall launch
+// (chunk_start + ns + 2).
+__global__ void __launch_bounds__(1024) k_batch_chunks(const BatchScene* __restrict__ D, unsigned ns,
+                                                       unsigned* __restrict__ chunk_start)
+{
+    __shared__ unsigned c[1024];
+    __shared__ unsigned carry;
+    batch_runs(D, ns, CN_HEAVY, chunk_start, c, carry);
+    batch_runs(D, ns, CN_HTRI, chunk_start + ns + 2, c, carry);
 }
 
 // The contact pass of every scene: each warp takes the next kBatchGrab runs
@@ -3763,7 +4016,9 @@ __global__ void __launch_bounds__(1024) k_batch_chunks(const BatchScene* __restr
 // take more; a run's result does not depend on which warp computes it.  A
 // warp loads the scene of a run into its own shared-memory slot when the
 // scene changes.
-template <bool COOP>
+// KIND 0: the per-particle contact pass; 1: the cooperative pair pass; 2:
+// the wall pass (runs over the front of each scene's list).
+template <int KIND>
 __global__ void __launch_bounds__(kContactMaxThreads) k_batch_contact(const BatchScene* __restrict__ D, unsigned ns,
                                                                    unsigned* __restrict__ chunk_start)
 {
@@ -3798,11 +4053,15 @@ __global__ void __launch_bounds__(kContactMaxThreads) k_batch_contact(const Batc
             front = W.C.counters[CN_HTRI];
         }
         const unsigned t = (ch - lo) * 32u + lane;
-        if (COOP) {
+        if (KIND == 1) {
             extern __shared__ CoopBuf coop_buf[];
             const bool valid = t < heavy;
             contact_entry_coop(W.P, W.C, valid, valid ? __ldg(W.C.hlist + list_index(t, front, W.P.n)) : 0u,
                                coop_buf[wb]);
+        } else if (KIND == 2) {
+            extern __shared__ CoopBuf coop_buf[];
+            const bool valid = t < front;
+            walls_entry_coop(W.P, W.C, valid, valid ? __ldg(W.C.hlist + t) : 0u, coop_buf[wb]);
         } else if (t < heavy) {
             contact_entry<false, 0>(W.P, W.C, __ldg(W.C.hlist + list_index(t, front, W.P.n)));
         }
@@ -3827,24 +4086,40 @@ struct MixedBatch {
     bool captured = false;
     unsigned cthreads = kContactThreads;             // block size of the shared contact launch
     unsigned cmode = kContactMode;                   // its pair pass (the first scene's choice)
+    bool walls = false;                              // a scene has planes or triangles (a wall pass)
     // direct launches (profilers; kernel timing): CUDA events around the
     // later steps' advance and every contact launch
     bool direct = false;
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> spans;
-    double ms[2] = {};
-    unsigned long long launches[2] = {};
+    double ms[3] = {};                               // advance, pair pass, wall pass
+    unsigned long long launches[3] = {};
 };
 
 // The batch's contact launch: every scene's listed particles.
-static void launch_batch_contact(const MixedBatch* b, unsigned ns, cudaStream_t q)
+static void launch_batch_pairs(const MixedBatch* b, unsigned ns, cudaStream_t q)
 {
     const unsigned ct = b->cthreads, grid = kContactWarpsTotal * 32u / ct;
     if (b->cmode == 1)
-        k_batch_contact<true><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(b->d_scenes, ns, b->d_chunks);
+        k_batch_contact<1><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(b->d_scenes, ns, b->d_chunks);
     else
-        k_batch_contact<false><<<grid, ct, 0, q>>>(b->d_scenes, ns, b->d_chunks);
+        k_batch_contact<0><<<grid, ct, 0, q>>>(b->d_scenes, ns, b->d_chunks);
+}
+
+// The wall pass after a cooperative pair pass (none otherwise: the
+// per-particle pass does its walls itself).
+static void launch_batch_walls(const MixedBatch* b, unsigned ns, cudaStream_t q)
+{
+    const unsigned ct = b->cthreads, grid = kContactWarpsTotal * 32u / ct;
+    if (b->cmode == 1 && b->walls)
+        k_batch_contact<2><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(b->d_scenes, ns, b->d_chunks + ns + 2);
+}
+
+static void launch_batch_contact(const MixedBatch* b, unsigned ns, cudaStream_t q)
+{
+    launch_batch_pairs(b, ns, q);
+    launch_batch_walls(b, ns, q);
 }
 
 namespace {
@@ -4061,7 +4336,7 @@ int prepare_batch(MixedBatch* b)
     M(&b->d_scenes, ns, "batch scenes");
     M(&b->d_block_scene, block_scene.size(), "batch blocks");
     M(&b->d_flags, ns, "batch flags");
-    M(&b->d_chunks, ns + 2, "batch runs");
+    M(&b->d_chunks, 2 * (ns + 2), "batch runs");
     M(&b->d_handles[0], ng + ns, "batch handles");
     M(&b->d_handles[1], ng + ns, "batch handles");
     M(&b->d_handles[2], (size_t)(ng + ns) * kBatchGraphSteps, "batch handles");
@@ -4110,6 +4385,7 @@ int mixed_batch_create(MixedScene* const* scenes, unsigned count, MixedBatch** o
     b->scenes.assign(scenes, scenes + count);
     b->cthreads = scenes[0]->cthreads;   // the first scene's choices (one launch serves all)
     b->cmode = scenes[0]->cmode;
+    for (unsigned k = 0; k < count; ++k) b->walls = b->walls || scenes[k]->P.nplanes || scenes[k]->P.ntri;
     const char* ng = getenv("XDEM_NO_GRAPHS");
     b->direct = ng && ng[0] && ng[0] != '0';
     *out = b;
@@ -4169,7 +4445,8 @@ int batch_step_direct(MixedBatch* b, unsigned nsteps, cudaStream_t q)
             if (flags[k]) st = rebuild(b->scenes[k], q);
         if (st != XD_OK) break;
         k_batch_chunks<<<1, 1024, 0, q>>>(b->d_scenes, ns, b->d_chunks);
-        span(1, [&] { launch_batch_contact(b, ns, q); });
+        span(1, [&] { launch_batch_pairs(b, ns, q); });
+        if (b->cmode == 1 && b->walls) span(2, [&] { launch_batch_walls(b, ns, q); });
         st = launch_status("batch contact");
     }
     if (st == XD_OK) {
@@ -4196,14 +4473,14 @@ int batch_step_direct(MixedBatch* b, unsigned nsteps, cudaStream_t q)
 int mixed_batch_set_timing(MixedBatch* b, bool enable)
 {
     b->timing = enable;
-    b->ms[0] = b->ms[1] = 0.0;
-    b->launches[0] = b->launches[1] = 0;
+    b->ms[0] = b->ms[1] = b->ms[2] = 0.0;
+    b->launches[0] = b->launches[1] = b->launches[2] = 0;
     return XD_OK;
 }
 
-void mixed_batch_kernel_times(MixedBatch* b, double ms[2], unsigned long long launches[2])
+void mixed_batch_kernel_times(MixedBatch* b, double ms[3], unsigned long long launches[3])
 {
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < 3; ++k) {
         ms[k] = b->ms[k];
         launches[k] = b->launches[k];
     }
@@ -4222,6 +4499,8 @@ int mixed_batch_step(MixedBatch* b, unsigned nsteps, cudaStream_t q)
                 return set_error(XD_ERR_STATE, "batch: scene %u now keeps history or kinematic bodies", (unsigned)k);
         }
         st = cuda_status(cudaStreamSynchronize(q), "batch");   // graphs in flight finish first
+        b->walls = false;
+        for (const MixedScene* sc : b->scenes) b->walls = b->walls || sc->P.nplanes || sc->P.ntri;
         if (st == XD_OK) st = prepare_batch(b);
         if (st != XD_OK) return st;
     }

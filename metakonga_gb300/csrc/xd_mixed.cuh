@@ -52,7 +52,7 @@ int mixed_batch_create(MixedScene* const* scenes, unsigned count, MixedBatch** o
 void mixed_batch_destroy(MixedBatch* b);
 int mixed_batch_step(MixedBatch* b, unsigned nsteps, cudaStream_t q);
 int mixed_batch_set_timing(MixedBatch* b, bool enable);
-void mixed_batch_kernel_times(MixedBatch* b, double ms[2], unsigned long long launches[2]);
+void mixed_batch_kernel_times(MixedBatch* b, double ms[3], unsigned long long launches[3]);
 int mixed_download_history(MixedScene* s, unsigned* keys, double* delta, unsigned long long* overflow,
                            cudaStream_t q);
 int mixed_set_bodies(MixedScene* s, const xd_polygon_mass_info* pmi, cudaStream_t q);

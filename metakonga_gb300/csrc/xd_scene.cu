@@ -1020,7 +1020,7 @@ int xd_batch_set_timing(xd_batch* b, int enable)
     return mixed_batch_set_timing(b->mixed, enable != 0);
 }
 
-int xd_batch_kernel_times(xd_batch* b, double ms[2], unsigned long long launches[2])
+int xd_batch_kernel_times(xd_batch* b, double ms[3], unsigned long long launches[3])
 {
     if (!b || !ms || !launches) return set_error(XD_ERR_INVALID, "batch_kernel_times: null argument");
     mixed_batch_kernel_times(b->mixed, ms, launches);

@@ -331,11 +331,14 @@ class Batch:
         call("xd_batch_set_timing", self.handle, 1 if enable else 0)
 
     def kernel_times(self) -> dict:
-        """{"advance": (ms, launches), "contact": (ms, launches)} since timing was enabled."""
-        ms = np.zeros(2)
-        n = np.zeros(2, np.uint64)
+        """{"advance": (ms, launches), "contact": (ms, launches), "walls": (ms, launches)} since
+        timing was enabled: the advance, the pair pass (the whole contact pass in contact_mode
+        0) and the wall pass that follows a cooperative pair pass."""
+        ms = np.zeros(3)
+        n = np.zeros(3, np.uint64)
         call("xd_batch_kernel_times", self.handle, ms.ctypes.data, n.ctypes.data)
-        return {"advance": (float(ms[0]), int(n[0])), "contact": (float(ms[1]), int(n[1]))}
+        return {"advance": (float(ms[0]), int(n[0])), "contact": (float(ms[1]), int(n[1])),
+                "walls": (float(ms[2]), int(n[2]))}
 
     def close(self) -> None:
         if self.handle:

@@ -102,10 +102,13 @@ def _time(sc, tuning, warm, steps):
         d.close()
 
 
-def tune(sc, steps: int = 200, warm: int = 20, store: bool = True) -> dict:
+def tune(sc, steps: int = 200, warm: int = 20, store: bool = True, min_gain: float = 0.03) -> dict:
     """Times the candidates on `steps` steps of the scene (after `warm`
     steps) and returns {"tuning", "ms_per_step", "default_ms_per_step",
-    "candidates", "key", "seconds"}; stores the choice in the cache."""
+    "candidates", "key", "seconds"}; stores the choice in the cache.  A
+    candidate replaces the choice so far only when it is faster by more than
+    `min_gain` (timing noise and re-binnings falling in or out of the window
+    move a short window by a few per cent)."""
     t0 = time.perf_counter()
     base = dict(engine.DEFAULT_TUNING)
     ms0, st0 = _time(sc, base, warm, steps)
@@ -125,7 +128,7 @@ def tune(sc, steps: int = 200, warm: int = 20, store: bool = True) -> dict:
             continue
         ms, _ = _time(sc, cand, warm, steps)
         results.append((ms, cand))
-        if ms < best_ms:
+        if ms < best_ms * (1.0 - min_gain):
             best, best_ms = cand, ms
     for th in THREADS:
         cand = dict(best, contact_threads=th)
@@ -133,7 +136,7 @@ def tune(sc, steps: int = 200, warm: int = 20, store: bool = True) -> dict:
             continue
         ms, _ = _time(sc, cand, warm, steps)
         results.append((ms, cand))
-        if ms < best_ms:
+        if ms < best_ms * (1.0 - min_gain):
             best, best_ms = cand, ms
     for mode in MODES:
         cand = dict(best, contact_mode=mode)
@@ -141,7 +144,7 @@ def tune(sc, steps: int = 200, warm: int = 20, store: bool = True) -> dict:
             continue
         ms, _ = _time(sc, cand, warm, steps)
         results.append((ms, cand))
-        if ms < best_ms:
+        if ms < best_ms * (1.0 - min_gain):
             best, best_ms = cand, ms
     out = {"key": shape_key(sc), "tuning": best, "ms_per_step": best_ms, "default_ms_per_step": ms0,
            "candidates": [{"tuning": c, "ms_per_step": m} for m, c in results],

@@ -47,6 +47,9 @@ def _run(split, batched, moved=None, timed=False):
         steps = sum(split)
         assert kt["advance"][1] == steps - len(split) and kt["contact"][1] == steps
         assert kt["advance"][0] > 0 and kt["contact"][0] > 0
+        # the scenes have walls: the cooperative pair pass (the default) is
+        # followed by a wall pass every step
+        assert kt["walls"][1] == steps and kt["walls"][0] > 0
     if b:
         b.close()
     for d in ds:
