@@ -1,7 +1,7 @@
 """Benchmark: particle-steps/s of the DEM contact step on one GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload batched|served|box|drum]
+                    [--workload batched|served|box|drum|hopper]
 
 Workloads (seeded synthetic input; every scene is generated here):
   batched  (default) 256 independent hopper-discharge scenes: particle counts
@@ -20,6 +20,8 @@ Workloads (seeded synthetic input; every scene is generated here):
   box      the 1,000,000-sphere polydisperse settle (r ~ U[2, 4] mm in a
            1 x 1 x 2 m box of five plane walls, dt = 5e-6 s), one scene.
   drum     the 500,000-sphere rotating drum (20,480 triangles turning).
+  hopper   one settled hopper (--hopper-n spheres, the batch's preparation,
+           cached in the temp directory): the contact-pass profiles' workload.
 
 The default (batched) line carries:
   value        particle-steps/s of the settled batch, device-timed (CUDA
@@ -28,18 +30,29 @@ The default (batched) line carries:
   e2e          the same through the public API with host buffers: each
                scene's state uploaded from pinned host memory, K steps, the
                state downloaded (all inside the timed region);
-  roofline     the batch step's dominant kernel -- k_batch_contact (the
-               contact pass over every scene's listed spheres) on packed beds,
+  roofline     the batch step's dominant kernel -- the contact pass
+               (k_batch_contact: the cooperative pair pass and the wall pass
+               over every scene's listed spheres) on packed beds,
                k_batch_advance<1> otherwise -- timed per launch with CUDA
                events, its algorithmic bytes over that time against the
                measured HBM peak; both kernels' figures are under "kernels";
-  lattice_start the same batch from its generated lattice (little contact);
+  autotune     the autotuner's choice on the particle-weighted median scene
+               and the batch's time with it against the defaults;
+  step_beyond_kernels_ms  a step's time outside its advance, pair and wall
+               launches (re-binnings, decisions, graph nodes);
+  lattice_start the same batch from its generated lattice (little contact),
+               and after 4,000 steps of falling ("fallen_4000");
   plain_fp64   the same scenes run one at a time in the FP64 form (the
                reference's algorithm and grid), and the ratio to it;
   fp64_check   per-particle contact-force error of the mixed form against the
                FP64 form on the median scene's settled bed;
-  served       the served stream (p50/p99 ms, particle-steps/s, and the same
-               requests' time alone in the FP64 form);
+  single_scene_box, settle_8000, drum  those workloads' own figures (the
+               box with the FP64 form on the reference's and on an unwrapped
+               grid);
+  served       the served stream stepped side by side (p50/p99 ms,
+               particle-steps/s), the same stream in cohorts, a sweep of
+               arrival rates with --rates, and the same requests' time alone
+               in the FP64 form;
   cpu_baseline the reference's CPU path (restated in the oracle, one thread)
                on the median scene's settled bed.
 --impl reference runs that CPU path on the host cores instead (one replica of
@@ -573,9 +586,11 @@ def _max_over_ranks(x, world):
     return float(t.item())
 
 
-def _fp64_alone(scs, steps, stream):
+def _fp64_alone(scs, steps, stream, own_grid=False):
     """Each scene alone in the plain FP64 form (one warm-up step, then `steps`
-    device-timed steps): its ms per step."""
+    device-timed steps): its ms per step.  own_grid: the particles on a grid
+    of their own (cells of the largest diameter, unwrapped), the triangles on
+    the reference's (xd_scene_set_particle_grid)."""
     import torch
 
     from metakonga_gb300 import engine
@@ -583,6 +598,8 @@ def _fp64_alone(scs, steps, stream):
     out = []
     for sc in scs:
         d = engine.DeviceScene(sc, mode=engine.MODE_FP64)
+        if own_grid:
+            d.set_particle_grid()
         d.step(1, check=True, stream=sh)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -902,6 +919,21 @@ def run_batched(a):
                    "listed_fraction": sum(d.stats(sh)["contact_list"] for d in ds_l) / n_l,
                    "state": "the hoppers as generated: jittered lattices (pitch >= 2.04 r_max, no contact) "
                             f"falling, {a.warmup} warm-up steps in"}
+        # the same lattices after 4,000 steps (20 ms) of falling: the lowest
+        # layers piled on the cones and the floor
+        b_l.step(4000, check=True, stream=sh)
+        ms_f, _ = _time_batch(b_l, a.steps, stream, barrier, world)
+        b_l.set_timing(True)
+        b_l.step(max(3, min(a.steps, 20)), check=False, stream=sh)
+        kt_f = b_l.kernel_times()
+        b_l.set_timing(False)
+        nf = max(kt_f["contact"][1], 1)
+        lattice["fallen_4000"] = {
+            "value": world * n_l * a.steps / (ms_f / 1e3), "unit": METRIC, "ms_per_step": ms_f / a.steps,
+            "listed_fraction": sum(d.stats(sh)["contact_list"] for d in ds_l) / n_l,
+            "pair_pass_ms": kt_f["contact"][0] / nf, "wall_pass_ms": kt_f["walls"][0] / nf,
+            "advance_ms": kt_f["advance"][0] / max(kt_f["advance"][1], 1),
+            "state": "the lattices after 4,000 more steps of falling at dt 5e-6"}
         b_l.close()
         for d in ds_l:
             d.close()
@@ -964,7 +996,7 @@ def run_batched(a):
     adv_gbs = n_tot * B_ADVANCE / (adv_ms / 1e3) / 1e9
     con_gbs = contact_bytes / (con_ms / 1e3) / 1e9
     adv_traffic = _traffic_from_profiles("advance_batch_hopper.md", "traffic_bytes_per_particle")
-    con_traffic = _traffic_from_profiles("contact_batch_hopper_dense.md", "traffic_bytes_per_listed_sphere")
+    con_traffic = _traffic_from_profiles("contact_mixed_hopper_settled.md", "traffic_bytes_per_listed_sphere")
     kernels = {
         "advance": {"kernel": "k_batch_advance<1> (velocity-Verlet kick and drift, contact view and skin test of "
                               "every scene's spheres in one launch)",
@@ -991,7 +1023,8 @@ def run_batched(a):
                         "launches after the timed ones",
             "kernels": kernels,
             "traffic_note": "DRAM bytes per unit of one ncu-captured launch (profiles/advance_batch_hopper.md per "
-                            "sphere, profiles/contact_batch_hopper_dense.md per listed sphere) times the units here"}
+                            "sphere, profiles/contact_mixed_hopper_settled.md per listed sphere, pair and wall "
+                            "passes) times the units here"}
     # per step: advance, decision, run prefix and contact over all scenes; per
     # call the finish and each scene's body-reaction sum; per re-binning its
     # kernels and its group's decision kernel
@@ -1057,6 +1090,14 @@ def run_batched(a):
                            "of 2 x max(r, triangle circumradius) cells, re-sorted every step), one "
                            f"warm-up step then {psteps} device-timed steps; ms summed over scenes",
                  "ratio": value / (world * n_tot / (fp64_ms / 1e3))}
+        per_g = _fp64_alone(scs, psteps, stream, own_grid=True)
+        fp64g_ms = sum(per_g)
+        plain["own_grid"] = {
+            "value": world * n_tot / (fp64g_ms / 1e3), "unit": METRIC, "ms_per_batch_step": fp64g_ms,
+            "method": "the same, with the particles on a grid of their own (cells of the largest diameter, "
+                      "power-of-two dimensions holding the bed unwrapped) and the triangles on the reference's "
+                      "(xd_scene_set_particle_grid): the FP64 form on particle cells of the mixed form's size",
+            "ratio": value / (world * n_tot / (fp64g_ms / 1e3))}
 
     # FP64 check on the median scene's settled bed
     check = _fp64_check(scs[k_med], squeeze=1.0, spin=False)
@@ -1131,6 +1172,7 @@ def run_batched(a):
                                            "conditional nodes -- the most a persistent kernel could save"},
         "lattice_start": lattice,
         "plain_fp64": plain,
+        "plain_fp64_own_grid": plain["own_grid"] if plain else None,
         "fp64_check": check,
         "roofline": roof,
         "single_scene_box": box,

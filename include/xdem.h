@@ -602,6 +602,18 @@ int xd_scene_set_emitter(xd_scene* scene, unsigned active, unsigned period, cons
 /* The particles that take part in the next step (before its emission). */
 int xd_scene_active(xd_scene* scene, unsigned* active);
 
+/* FP64 form: a grid of its own for the particles (power-of-two dimensions,
+ * cell size, origin), while the triangles stay on the scene's grid.  The
+ * reference hashes particles and triangle circumspheres into one grid whose
+ * cell must hold the largest circumsphere (dem_simulation.cpp:259-261), so a
+ * mesh of large triangles makes every particle search cells many times its
+ * size; with this call the particle pairs are searched in cells of the
+ * particles' own size (at least the largest diameter: the caller's choice,
+ * as the reference's cell size is) and the triangles as before.  The pair
+ * sums then run in another order: results equal the reference's within the
+ * FP64 rounding of a reordered sum.  No counterpart in the reference. */
+int xd_scene_set_particle_grid(xd_scene* scene, const unsigned grid[3], double cell_size, const double origin[3]);
+
 /* Tangential-spring history, an extension: the reference's DHSModel
  * (mphysics_cuda_impl.cuh:379-401) keeps no state between steps.  With
  * slots > 0 (at most 32) every particle keeps up to `slots` contacts keyed

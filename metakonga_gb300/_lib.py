@@ -102,6 +102,7 @@ _SIGS = {
     "xd_scene_rebuilds": [vp, vp, vp, vp],
     "xd_scene_step_many": [vp, vp, u32, i32, vp],
     "xd_scene_set_tangential_history": [vp, u32],
+    "xd_scene_set_particle_grid": [vp, vp, C.c_double, vp],
     "xd_scene_set_kinematic_bodies": [vp, i32],
     "xd_scene_set_emitter": [vp, u32, u32, vp, u32, vp],
     "xd_scene_set_planes": [vp, vp, vp],

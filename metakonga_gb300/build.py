@@ -33,6 +33,11 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 # FP64 translation units whose results must match the reference's arithmetic
 # are compiled without multiply-add contraction.
 NO_FMAD = {"xd_grid.cu", "xd_integrate.cu", "xd_contact64.cu", "xd_twin32.cu", "xd_legacy.cu"}
+# The mixed form's FP32 contact arithmetic carries its own error bounds and
+# corrects its pair-arithmetic quotients and roots: approximate FP32 division
+# and square root there (about 2 ulp, a few instructions instead of an IEEE
+# sequence with a slow path).
+FAST_DIV = {"xd_mixed.cu"}
 
 CUDA_SOURCES = ["xd_capi.cu", "xd_sort.cu", "xd_grid.cu", "xd_integrate.cu", "xd_contact64.cu",
                 "xd_scene.cu", "xd_noalloc.cu", "xd_mixed.cu", "xd_twin32.cu", "xd_legacy.cu"]
@@ -50,11 +55,14 @@ def _compile(src: str) -> str:
     srcp = os.path.join(CSRC, src)
     deps = [srcp] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
     deps.append(os.path.join(INCLUDE, "xdem.h"))
+    deps.append(os.path.abspath(__file__))   # the flags
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
     flags = list(NVCC_COMMON)
     if src in NO_FMAD:
         flags.append("--fmad=false")
+    if src in FAST_DIV:
+        flags += ["-prec-div=false", "-prec-sqrt=false"]
     cmd = [nvcc(), "-c", srcp, "-o", obj] + flags
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -394,14 +394,14 @@ __device__ __forceinline__ float normal_speed(const float s[3], const float t[3]
     two_prod(d0, d0, p, pe);
     const float D2h = __ll2float_rn(D2);
     const float D2l = __ll2float_rn(D2 - __float2ll_rn(D2h));
-    const float c = __fdiv_rn(__fadd_rn(__fsub_rn(__fsub_rn(D2h, p), pe), D2l), __fmul_rn(2.f, d0));
+    const float c = __fadd_rn(__fsub_rn(__fsub_rn(D2h, p), pe), D2l) / __fmul_rn(2.f, d0);
     // (nv + nl) / (d0 + c)
-    const float q0 = __fdiv_rn(nv, d0);
+    const float q0 = nv / d0;   // any close quotient: its residual is exact below
     float qp, qpe;
     two_prod(q0, d0, qp, qpe);
     const float rem = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(nv, qp), qpe), nl), __fmul_rn(q0, c));
     q0_out = q0;
-    q1_out = __fdiv_rn(rem, d0);
+    q1_out = rem / d0;
     c_out = c;
     return __fadd_rn(q0, q1_out);
 }
@@ -421,7 +421,7 @@ __device__ __forceinline__ dfl df_sub(dfl a, dfl b) { return df_add(a, df_neg(b)
 // residual 1 - d0 r0 of a rounded reciprocal is exact in one FMA).
 __device__ __forceinline__ dfl df_inv(float d0, float c)
 {
-    const float r0 = __fdiv_rn(1.0f, d0);
+    const float r0 = 1.0f / d0;   // refined by the Newton step
     const float res = __fsub_rn(__fmaf_rn(-d0, r0, 1.0f), __fmul_rn(c, r0));
     dfl r;
     fast_two_sum(r0, __fmul_rn(r0, res), r.hi, r.lo);
@@ -470,24 +470,29 @@ __device__ __noinline__ f3 slip_pair(const float s[3], const float t[3], const i
     return fk(e[0], e[1], e[2]);
 }
 
-// a / b and sqrt(a) in pair arithmetic (one correction step each)
+// a / b and sqrt(a) in pair arithmetic (one correction step each).  This
+// file is compiled with approximate FP32 division and square root
+// (-prec-div=false -prec-sqrt=false, about 2 ulp): every quotient and root
+// in the pair helpers is a first guess whose residual is formed exactly and
+// corrected, and the plain FP32 force terms carry error bounds (kTermErr,
+// kRotErr) well above that.
 __device__ __forceinline__ dfl df_div(dfl a, dfl b)
 {
-    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const float q1 = a.hi / b.hi;
     const dfl r = df_sub(a, df_mul(b, dfl{ q1, 0.f }));
     dfl q;
-    fast_two_sum(q1, __fdiv_rn(r.hi, b.hi), q.hi, q.lo);
+    fast_two_sum(q1, r.hi / b.hi, q.hi, q.lo);
     return q;
 }
 __device__ __forceinline__ dfl df_sqrt(dfl a)
 {
     if (!(a.hi > 0.f)) return dfl{ 0.f, 0.f };
-    const float s0 = __fsqrt_rn(a.hi);
+    const float s0 = sqrtf(a.hi);
     float p, pe;
     two_prod(s0, s0, p, pe);
     const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), pe), a.lo);
     dfl q;
-    fast_two_sum(s0, __fdiv_rn(r, __fmul_rn(2.f, s0)), q.hi, q.lo);
+    fast_two_sum(s0, r / __fmul_rn(2.f, s0), q.hi, q.lo);
     return q;
 }
 // an FP64 value as a float pair
@@ -892,7 +897,7 @@ __global__ void __launch_bounds__(256) k_lb_long(const uint4* __restrict__ gaps,
 
 // Reference FP64 contact decision (calculate_p2p_kernel, impl:449-452),
 // evaluated without multiply-add contraction like the oracle.
-__device__ __forceinline__ double fp64_cdist(const Master& M, unsigned i, unsigned j)
+__device__ __noinline__ double fp64_cdist(const Master& M, unsigned i, unsigned j)
 {
     double dx = __dsub_rn(__ldg(M.x + j), __ldg(M.x + i));
     double dy = __dsub_rn(__ldg(M.y + j), __ldg(M.y + i));
@@ -1824,8 +1829,11 @@ __device__ __forceinline__ WallRes wall_eval(const MixParams& P, const ContactAr
     const WallK k = wall_constants(P.pb_c43Eeq + b, P.pb_one_b2 + b, P.pb_sratio[b], P.pb_fric[b], rf, w.mf);
     const xd_polygon_mass_info* body = C.pmi + b;
     const d3 po2cp = cpt - tri_vertex(body->origin);
-    const d3 pvel = tri_vertex(body->vel);
-    const d3 dvd = P.rolling ? (pvel + cross(tri_vertex(body->omega), po2cp)) - w.iv : pvel - w.iv;
+    const d3 pvel = tri_vertex(body->vel), pom = tri_vertex(body->omega);
+    // a body at rest: the wall velocity is zero, and so is every term of it
+    const bool moving = pvel.x != 0.0 || pvel.y != 0.0 || pvel.z != 0.0 || pom.x != 0.0 || pom.y != 0.0 ||
+                        pom.z != 0.0;
+    const d3 dvd = !moving ? -w.iv : (P.rolling ? (pvel + cross(pom, po2cp)) - w.iv : pvel - w.iv);
     res.kind = 2;
     res.b = b;
     res.o = wall_force(P, k, cd, u, dvd, w.r, w.m, rf, w.wfloor, w.wh, w.wl, counters);
@@ -2197,6 +2205,24 @@ struct CoopBuf {
     float res[10][32];                // one contact per lane: Fn, Ft, Mm, slip
 };
 
+// A lane whose Verlet list overflowed: its cells searched from the start,
+// the partners before `done` skipped, up to kCoopSlots after them kept in
+// mine[]; returns whether more are left.  Out of line: rare, and the pass's
+// loop stays short.
+__device__ __noinline__ bool coop_cells(const MixParams& P, const ContactArgs& C, unsigned i, float4 pi,
+                                        longlong2 qai, longlong2 qbi, unsigned& done, unsigned* mine,
+                                        unsigned& cnt)
+{
+    unsigned seen = 0;
+    for_each_contact<true>(P, C.M, i, pi, qai, qbi, __ldg(C.keys + i), C.pf, C.qa, C.qb, C.lb, C.counters,
+                           [&](unsigned j, bool guard) {
+                               if (seen >= done && cnt < kCoopSlots) mine[cnt++] = j | (guard ? kGuardBit : 0u);
+                               ++seen;
+                           });
+    done += cnt;
+    return seen > done;
+}
+
 // Own data of slot i as contact_force reads it.
 __device__ __forceinline__ Own load_own(const MixParams& P, const ContactArgs& C, unsigned i)
 {
@@ -2277,17 +2303,7 @@ __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const Con
                 }
                 more = kpos < vc;
             } else {
-                // the cells: searched again from the start each round, the
-                // partners before `done` skipped
-                unsigned seen = 0;
-                for_each_contact<true>(P, C.M, i, pi, qai, qbi, __ldg(C.keys + i), C.pf, C.qa, C.qb, C.lb,
-                                       C.counters, [&](unsigned j, bool guard) {
-                                           if (seen >= done && cnt < kCoopSlots)
-                                               mine[cnt++] = j | (guard ? kGuardBit : 0u);
-                                           ++seen;
-                                       });
-                done += cnt;
-                more = seen > done;
+                more = coop_cells(P, C, i, pi, qai, qbi, done, mine, cnt);
             }
         }
         __syncwarp();

@@ -26,6 +26,12 @@ struct xd_scene {
     double *force = nullptr, *moment = nullptr, *mass = nullptr, *inertia = nullptr;
     // grid
     unsigned *hash = nullptr, *index = nullptr, *sorted = nullptr, *cstart = nullptr, *cend = nullptr;
+    // FP64 form with a grid of its own for the particles (xd_scene_set_particle_grid): the
+    // particles hashed, sorted and searched on Pp's cells, the triangles on the scene's grid
+    bool split = false;
+    Params Pp;
+    unsigned ncell_p = 0;
+    unsigned *pcstart = nullptr, *pcend = nullptr;
     // walls / mesh
     xd_plane_info* planes = nullptr;
     xd_contact_property* cp_planes = nullptr;
@@ -724,22 +730,38 @@ int fp64_steps(xd_scene* s, unsigned nsteps, cudaStream_t q)
     if (st != XD_OK) return st;
     // one step: grid, contacts, and the velocity update, fused with the next
     // step's position update unless `last`
+    Params Pp = s->Pp;
+    Pp.np = np;
+    // the particles' grid: the scene's, or their own (then the triangles'
+    // hashes, sorted order and cell ranges sit after the particles' in
+    // hash/index/sorted and in cstart/cend of the scene's grid)
+    const Params& PG = s->split ? Pp : P;
+    unsigned* const gcs = s->split ? s->pcstart : s->cstart;
+    unsigned* const gce = s->split ? s->pcend : s->cend;
     auto one_step = [&](bool last, cudaStream_t qq) {
         int r = XD_OK;
         {
             PhaseSpan ps(s, 1, qq);
-            r = launch_hash(P, s->hash, s->index, s->pos, np, 0, qq);
+            r = launch_hash(PG, s->hash, s->index, s->pos, np, 0, qq);
             if (r == XD_OK && s->ntri) r = launch_hash(P, s->hash, s->index, s->sphere, s->ntri, np, qq);
         }
         if (r == XD_OK) {
             PhaseSpan ps(s, 2, qq);
-            r = reorder_and_find_cell_start(s->hash, s->index, s->cstart, s->cend, s->sorted, ng, s->ncell,
-                                            s->scratch, qq, false);
+            if (!s->split) {
+                r = reorder_and_find_cell_start(s->hash, s->index, s->cstart, s->cend, s->sorted, ng, s->ncell,
+                                                s->scratch, qq, false);
+            } else {
+                r = reorder_and_find_cell_start(s->hash, s->index, s->pcstart, s->pcend, s->sorted, np,
+                                                s->ncell_p, s->scratch, qq, false);
+                if (r == XD_OK && s->ntri)
+                    r = reorder_and_find_cell_start(s->hash + np, s->index + np, s->cstart, s->cend,
+                                                    s->sorted + np, s->ntri, s->ncell, s->scratch, qq, false);
+            }
         }
         if (r == XD_OK) {
             PhaseSpan ps(s, 3, qq);
-            r = launch_p2p(P, s->pos, s->vel, s->omega, s->force, s->moment, s->mass, s->sorted, s->cstart,
-                           s->cend, s->cp_pp, np, qq, hp);
+            r = launch_p2p(PG, s->pos, s->vel, s->omega, s->force, s->moment, s->mass, s->sorted, gcs, gce,
+                           s->cp_pp, np, qq, hp);
         }
         if (r == XD_OK && s->nplanes) {
             PhaseSpan ps(s, 4, qq);
@@ -749,7 +771,8 @@ int fp64_steps(xd_scene* s, unsigned nsteps, cudaStream_t q)
         if (r == XD_OK && s->ntri) {
             PhaseSpan ps(s, 5, qq);
             r = launch_polygon(P, s->poly, s->pmi, s->pos, s->vel, s->omega, s->force, s->moment, s->mass,
-                               s->sorted, s->cstart, s->cend, s->cp_poly, s->nbodies, s->poly_scratch, qq, hp);
+                               s->split ? s->sorted + np : s->sorted, s->cstart, s->cend, s->cp_poly,
+                               s->nbodies, s->poly_scratch, qq, hp);
         }
         if (r == XD_OK) {
             PhaseSpan ps(s, 0, qq);
@@ -895,6 +918,40 @@ int xd_scene_active(xd_scene* s, unsigned* active)
 {
     if (!s || !active) return set_error(XD_ERR_INVALID, "scene_active: null argument");
     *active = s->active;
+    return XD_OK;
+}
+
+int xd_scene_set_particle_grid(xd_scene* s, const unsigned grid[3], double cell_size, const double origin[3])
+{
+    if (!s || !grid || !origin) return set_error(XD_ERR_INVALID, "scene_set_particle_grid: null argument");
+    if (s->mixed) return set_error(XD_ERR_STATE, "scene_set_particle_grid: FP64 scenes only");
+    for (int a = 0; a < 3; ++a)
+        if (grid[a] < 2 || grid[a] > 4096 || (grid[a] & (grid[a] - 1u)))
+            return set_error(XD_ERR_INVALID, "scene_set_particle_grid: dimension %u not a power of two in [2, 4096]",
+                             grid[a]);
+    const unsigned long long nc = (unsigned long long)grid[0] * grid[1] * grid[2];
+    if (nc > (1ull << 28)) return set_error(XD_ERR_INVALID, "scene_set_particle_grid: %llu cells", nc);
+    if (!(cell_size > 0.0)) return set_error(XD_ERR_INVALID, "scene_set_particle_grid: cell size %g", cell_size);
+    cudaDeviceSynchronize();   // the step graphs hold the grid arrays: replaced after what is queued
+    free_fp64_graphs(s);
+    s->graphs_np = ~0u;
+    if (nc > s->ncell_p) {
+        unsigned *a = nullptr, *b = nullptr;
+        int st = dalloc(s, &a, nc);
+        if (st == XD_OK) st = dalloc(s, &b, nc);
+        if (st != XD_OK) return st;
+        s->pcstart = a;
+        s->pcend = b;
+    }
+    s->ncell_p = (unsigned)nc;
+    s->Pp = s->P;
+    s->Pp.gx = grid[0];
+    s->Pp.gy = grid[1];
+    s->Pp.gz = grid[2];
+    s->Pp.ncell = (unsigned)nc;
+    s->Pp.cs = cell_size;
+    for (int a = 0; a < 3; ++a) s->Pp.wo[a] = origin[a];
+    s->split = true;
     return XD_OK;
 }
 

@@ -256,6 +256,24 @@ class DeviceScene:
         call("xd_scene_active", self.handle, out.ctypes.data)
         return int(out[0])
 
+    def set_particle_grid(self, grid=None, cell_size: float = None, origin=None):
+        """FP64 form: the particles on a grid of their own (xd_scene_set_particle_grid),
+        the triangles on the scene's.  With no arguments the grid is the one that
+        holds the current particles unwrapped: cells of the largest diameter (or
+        cell_size), the origin one cell below the lowest particle, power-of-two
+        dimensions.  Returns (grid, cell size, origin)."""
+        if grid is None:
+            pos = self.download()["pos"]
+            cell = float(2.0 * pos[:, 3].max()) if cell_size is None else float(cell_size)
+            lo = pos[:, :3].min(axis=0) - cell
+            hi = pos[:, :3].max(axis=0) + cell
+            grid = [1 << int(np.ceil(np.log2(max(2.0, (h - l) / cell)))) for l, h in zip(lo, hi)]
+            origin, cell_size = lo, cell
+        g = np.ascontiguousarray(grid, np.uint32)
+        o = np.ascontiguousarray(origin, np.float64)
+        call("xd_scene_set_particle_grid", self.handle, g.ctypes.data, float(cell_size), o.ctypes.data)
+        return [int(x) for x in g], float(cell_size), [float(x) for x in o]
+
     def set_tangential_history(self, slots: int = 12):
         """Tangential springs kept per contact (xd_scene_set_tangential_history);
         0 restores the reference's DHS model."""
