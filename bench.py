@@ -111,6 +111,8 @@ def _args():
     ap.add_argument("--prep-steps", type=int, default=5000,
                     help="settled beds: preparation steps (prepare.settle) before the timed run (0: none)")
     ap.add_argument("--prep-dt", type=float, default=4e-5, help="time step of the preparation")
+    ap.add_argument("--prep-cache", action="store_true",
+                    help="keep the settled batch in the temp directory and load it when present")
     ap.add_argument("--no-lattice", action="store_true", help="batched: skip the lattice-start timing")
     ap.add_argument("--count", type=int, default=256, help="scenes in the batch")
     ap.add_argument("--requests", type=int, default=32, help="requests of the served stream")
@@ -309,11 +311,40 @@ def _median_index(specs):
 def _settled_hoppers(specs, a, stream):
     """The batch's hoppers as settled beds with the orifice open: each scene
     generated with its gate closed, settled by prepare.settle (a.prep_steps
-    steps of a.prep_dt in one batch), the gates then opened."""
+    steps of a.prep_dt in one batch), the gates then opened.  With
+    a.prep_cache the settled states are kept in the temp directory (a
+    profiler's run of the same workload then loads them instead of
+    launching the preparation)."""
+    import tempfile
+
+    import numpy as np
+
     from metakonga_gb300 import prepare, scenes
     scs = [scenes.hopper(gate=True, **d) for d in specs]
-    if a.prep_steps:
+    keys = ("pos", "vel", "acc", "omega", "alpha")
+    path = os.path.join(tempfile.gettempdir(),
+                        f"xdem_hopper_batch_{len(specs)}_{a.prep_steps}_{a.prep_dt:g}.npz")
+    loaded = False
+    if a.prep_cache and a.prep_steps:
+        try:
+            z = np.load(path)
+            for k in keys:
+                flat = z[k]
+                off = 0
+                for sc in scs:
+                    arr = getattr(sc, k)
+                    arr[:] = flat[off:off + arr.shape[0]]
+                    off += arr.shape[0]
+            loaded = True
+        except (OSError, KeyError, ValueError):
+            loaded = False
+    if a.prep_steps and not loaded:
         prepare.settle(scs, a.prep_steps, dt=a.prep_dt, stream=stream)
+        if a.prep_cache:
+            try:
+                np.savez(path, **{k: np.concatenate([getattr(sc, k) for sc in scs]) for k in keys})
+            except OSError:
+                pass
     prepare.open_gates(scs)
     return scs
 

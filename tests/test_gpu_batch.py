@@ -23,9 +23,9 @@ def _scenes():
     return out
 
 
-def _run(split, batched, moved=None, timed=False):
+def _run(split, batched, moved=None, timed=False, tuning=None):
     scs = _scenes()
-    ds = [engine.DeviceScene(sc, mode=engine.MODE_MIXED) for sc in scs]
+    ds = [engine.DeviceScene(sc, mode=engine.MODE_MIXED, tuning=tuning) for sc in scs]
     b = engine.Batch(ds) if batched else None
     if timed:
         b.set_timing(True)
@@ -64,6 +64,20 @@ def test_batch_equals_each_scene_alone(cuda, moved, timed):
     alone = _run((5, 27, 16), False, moved)
     batch = _run((5, 27, 16), True, moved, timed)
     assert all(r > 1 for _, r, _ in alone), [r for _, r, _ in alone]
+    for (a, ra, ba), (b, rb, bb) in zip(alone, batch):
+        assert ra == rb
+        for k in ("pos", "vel", "omega", "acc"):
+            assert np.array_equal(a[k], b[k]), k
+        if ba is not None:
+            assert ba.tobytes() == bb.tobytes()
+
+
+@pytest.mark.parametrize("mode", [0, 2])
+def test_batch_equals_each_scene_alone_other_pair_passes(cuda, mode):
+    """The per-particle pass and the once-per-pair pass, batched and alone."""
+    t = {"contact_mode": mode}
+    alone = _run((5, 27, 16), False, tuning=t)
+    batch = _run((5, 27, 16), True, tuning=t)
     for (a, ra, ba), (b, rb, bb) in zip(alone, batch):
         assert ra == rb
         for k in ("pos", "vel", "omega", "acc"):
