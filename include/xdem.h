@@ -551,11 +551,7 @@ typedef struct xd_tuning {
     unsigned contact_threads;   /* 32, 64 or 128 */
     unsigned contact_mode;      /* pair pass: 0 a thread per listed particle, 1 warp-cooperative (the
                                    warp's contacts spread one per lane, summed per particle in list
-                                   order: the same bits as 0), 2 warp-cooperative with each pair of
-                                   particles whose lists are complete (at most 16 entries) computed
-                                   once and read by both, summed in list order (Newton's third law
-                                   exact for those pairs; within the mixed form's bounds of 0 and
-                                   1; 700 B more per particle) */
+                                   order: the same bits as 0) */
 } xd_tuning;
 int xd_scene_set_tuning(xd_scene* scene, const xd_tuning* tuning);
 int xd_scene_get_tuning(xd_scene* scene, xd_tuning* tuning);

@@ -71,8 +71,6 @@ constexpr float kSkinFactor = 0.1f;            // default: skin width over the l
 constexpr unsigned kContactThreads = 64;       // default block size of the contact pass
 constexpr unsigned kContactMaxThreads = 128;   // the largest block size a scene may choose
 constexpr unsigned kContactMode = 1;           // default pair pass: warp-cooperative
-constexpr unsigned kHalfCap = 16;              // contact_mode 2: list entries of a particle that shares its pairs
-constexpr unsigned kPartner = 0x80000000u;     // contact_mode 2 result index: the partner's slot
 constexpr unsigned kContactWarpsTotal = 152 * 16;   // warps of a full contact grid (every SM, 16 warps each)
 constexpr int kMaxBodies = 8;                  // polygon bodies of a mixed scene
 constexpr unsigned kGuardBit = 0x80000000u;    // list entry decided by the FP64 test
@@ -124,7 +122,6 @@ struct MixParams {
     float inv_gx, inv_gxy;   // 1 / gx, 1 / (gx gy) for the key decode
     float dtf, hf, half2dtf;
     float gf[3];
-    float gnorm;         // |g| in FP32: m g is a contact's smallest force scale
     float2 dt_df;        // dt as double-float
     float2 G1[3];        // dt * g, double-float (gravity's velocity increment)
     float2 G2[3];        // dt^2 / 2 * g, double-float
@@ -171,10 +168,7 @@ struct MixedScene {
     // tuning (xd_scene_set_tuning, before the first upload)
     float skin_factor = kSkinFactor;
     unsigned vcap = kVerletCap, tcap = kTriCap, cthreads = kContactThreads;
-    unsigned cmode = kContactMode;   // 0: a thread per listed particle; 1: warp-cooperative pairs;
-                                     // 2: warp-cooperative, each shared pair computed once
-    unsigned* vrid = nullptr;        // mode 2: per list entry, the slot of its pair's result
-    float4* hres = nullptr;          // mode 2: pair results, three float4 per slot
+    unsigned cmode = kContactMode;   // 0: a thread per listed particle; 1: warp-cooperative pairs
     unsigned active_req = ~0u;    // active count set before the first upload
     bool emitted = false;         // the particle count has changed since the graphs were made
     unsigned version = 0;         // raised whenever the step graphs are dropped (parameters changed)
@@ -1341,7 +1335,7 @@ struct PairAcc {
 // One pair contact's terms: the normal force, and -- when its slip is not
 // zero -- the tangential force and moment that replace the carried ones.
 struct PairOut {
-    f3 Fn, Ft, Mm, u;
+    f3 Fn, Ft, Mm;
     bool slip;
 };
 
@@ -1430,9 +1424,6 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     const f3 wj = fk(wj4.x, wj4.y, wj4.z);
     const float jr = __ldg(pf + j).w, jim = vj4.w;
     const float ir = I.r;
-    // the force scale floor of the pair: the lighter particle's weight (the
-    // contact's force goes to both when contact_mode 2 computes it once)
-    const float wfl = fminf(I.wfloor, P.gnorm / jim);
     // vj - vi formed exactly from the double-float velocities
     float dvs[3], dvt[3];
     df_diff(vj4.x, I.vh.x, __fsub_rn(vjl.x, I.vl.x), dvs[0], dvt[0]);
@@ -1470,7 +1461,7 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
         fca = P.coh * (3.14159265358979f * rc * rc);
     }
     float fn = fsn + fca + fdn;
-    if (normal_needs_fp64(fmaxf(fmaxf(fabsf(fsn), fabsf(fdn)), fca), fabsf(fn), wfl)) {
+    if (normal_needs_fp64(fmaxf(fmaxf(fabsf(fsn), fabsf(fdn)), fca), fabsf(fn), I.wfloor)) {
         // The elastic, (cohesive) and damping terms nearly cancel (the
         // normal force of an unloading contact crossing zero): FP32 rounding
         // of each term would dominate the small sum, so it is formed again
@@ -1499,7 +1490,7 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     // kForceTol of the contact's force scale max(|Fn|, m_i g): a sliding
     // contact (Coulomb cap) whose slip nearly cancels, or a fast spin.
     if (P.rolling && slip_needs_fp64(sqrtf(fdot(I.w, I.w)) * ir + sqrtf(fdot(wj, wj)) * jr, ee, ks * dt + vs, P.fric,
-                                     fabsf(fn), wfl)) {
+                                     fabsf(fn), I.wfloor)) {
         count_one(counters + CN_SLIPS);
         ev = slip_pair(dvs, dvt, dqi, dn, rqc, rq0, rq1, I.qb.y, qbj.y, make_float4(I.w.x, I.w.y, I.w.z, 0.f),
                        __ldg(M.wl + i), wj4, __ldg(M.wl + j));
@@ -1532,7 +1523,6 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
         const float mag_e = sqrtf(ee);
         if (OUT) {
             o->Fn = Fn;
-            o->u = u;
             o->slip = mag_e != 0.f;
         }
         if (mag_e != 0.f) {
@@ -1618,8 +1608,6 @@ struct ContactArgs {
     unsigned rec_cap;
     HistTable ht;
     int rxn_on;
-    const unsigned* vrid;   // contact_mode 2 (see k_half_rid)
-    float4* hres;
 };
 
 // ---- wall contacts in FP32 ------------------------------------------------
@@ -2213,9 +2201,8 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
 constexpr unsigned kCoopSlots = 16;
 
 struct CoopBuf {
-    unsigned cand[32 * kCoopSlots];         // lane L's partners at [L * kCoopSlots, ...)
-    unsigned char candk[32 * kCoopSlots];   // contact_mode 2: their list positions
-    float res[10][32];                      // one contact per lane: Fn, Ft, Mm, slip
+    unsigned cand[32 * kCoopSlots];   // lane L's partners at [L * kCoopSlots, ...)
+    float res[10][32];                // one contact per lane: Fn, Ft, Mm, slip
 };
 
 // A lane whose Verlet list overflowed: its cells searched from the start,
@@ -2497,230 +2484,6 @@ __global__ void __launch_bounds__(kContactMaxThreads) k_mx_walls(MixParams P, Co
         const bool valid = t < front;
         walls_entry_coop(P, C, valid, valid ? __ldg(C.hlist + t) : 0u, B);
     }
-}
-
-// ---- contact_mode 2: each shared pair computed once ---------------------------
-//
-// The reference computes every contact twice, once for each particle.  Here a
-// particle shares its pairs when its Verlet list is complete and holds at
-// most kHalfCap entries.  For a pair of two sharing particles that list each
-// other, the lower index computes the contact once (pass A, cooperative as
-// above) into its own result slot, entry k of particle i at k * n + i; the
-// other reads it with the signs of the normal, the force and the tangential
-// force turned (the contact seen from the other side).  Every other pair is
-// computed by each particle for itself, into its own slot.  Pass B then adds
-// each particle's contacts in its list order from the slots (the moment
-// with its own radius), so the sums run in the order of the other modes; a
-// particle that does not share computes its pairs there itself.  The pair's
-// FP32 recheck criteria use the lighter particle's weight.  The walls follow
-// in the wall pass.
-
-__device__ __forceinline__ bool shares(unsigned vc) { return !(vc & kIncomplete) && vc <= kHalfCap; }
-
-// At a re-binning: the result slot of every list entry of a sharing particle.
-__global__ void __launch_bounds__(256) k_half_rid(MixParams P, const unsigned* __restrict__ vcount,
-                                                  const unsigned* __restrict__ vlist, unsigned* __restrict__ vrid)
-{
-    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned n = P.n;
-    if (i >= n) return;
-    const unsigned vc = __ldg(vcount + i);
-    if (!shares(vc)) return;
-    for (unsigned k = 0; k < vc; ++k) {
-        const unsigned j = __ldg(vlist + (size_t)k * n + i);
-        unsigned rid = k * n + i;
-        if (j < i) {
-            const unsigned vj = __ldg(vcount + j);
-            if (shares(vj)) {
-                for (unsigned kk = 0; kk < vj; ++kk)
-                    if (__ldg(vlist + (size_t)kk * n + j) == i) {
-                        rid = (kk * n + j) | kPartner;
-                        break;
-                    }
-            }
-        }
-        vrid[(size_t)k * n + i] = rid;
-    }
-}
-
-// The pairs of slot i computed and summed by its own thread, in search order
-// (pass B, for a particle that does not share).
-__device__ __noinline__ void pairs_serial(const MixParams& P, const ContactArgs& C, unsigned i, PairAcc& A)
-{
-    const float4 pi = __ldg(C.pf + i);
-    const Own I = load_own(P, C, i);
-    HistState hs;
-    auto add = [&](unsigned j, bool guard) {
-        contact_force<0>(P, C.M, I, j, guard, C.mass0, C.pf, C.qa, C.qb, C.pr, C.counters, A, C.ht, hs);
-    };
-    const unsigned vc = __ldg(C.vcount + i);
-    if (!(vc & kIncomplete)) {
-        const float rt0 = pi.w + P.tol;
-        for (unsigned k = 0; k < vc; ++k) {
-            const unsigned j = __ldg(C.vlist + (size_t)k * P.n + i);
-            const float4 pj = __ldg(C.pf + j);
-            const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-            const float Rt = rt0 + pj.w;
-            if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) >= Rt * Rt) continue;
-            const int c = exact_touch<true>(P, C.M, i, j, I.qa, I.qb, C.qa, C.qb, C.counters);
-            if (c) add(j, c == 2);
-        }
-    } else {
-        for_each_contact<true>(P, C.M, i, pi, I.qa, I.qb, __ldg(C.keys + i), C.pf, C.qa, C.qb, C.lb, C.counters,
-                               add);
-    }
-}
-
-// Pass A: the entries of sharing particles whose slot is their own, every
-// lane of the warp taking part.  A touching entry's contact goes to its slot
-// (Fn and flags, Ft and u.x, u.y u.z); an entry out of contact gets flags 0.
-__device__ __forceinline__ void half_pass_a(const MixParams& P, const ContactArgs& C, bool valid, unsigned i,
-                                            CoopBuf& B)
-{
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned n = P.n;
-    float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
-    unsigned vc = 0;
-    longlong2 qai = make_longlong2(0, 0), qbi = make_longlong2(0, 0);
-    if (valid) {
-        vc = __ldg(C.vcount + i);
-        if (!shares(vc)) vc = 0;
-        if (vc) {
-            pi = __ldg(C.pf + i);
-            qai = __ldg(C.qa + i);
-            qbi = __ldg(C.qb + i);
-        }
-    }
-    PairAcc A;   // unused: contact_force writes the terms out
-    HistState hs;
-    unsigned kpos = 0;
-    bool more = vc != 0;
-    unsigned* mine = B.cand + lane * kCoopSlots;
-    unsigned char* mink = B.candk + lane * kCoopSlots;
-    while (__any_sync(0xffffffffu, more)) {
-        unsigned cnt = 0;
-        if (more) {
-            const float rt0 = pi.w + P.tol;
-            for (; kpos < vc && cnt < kCoopSlots; ++kpos) {
-                const size_t e = (size_t)kpos * n + i;
-                if (__ldg(C.vrid + e) & kPartner) continue;   // the partner computes it
-                const unsigned j = __ldg(C.vlist + e);
-                const float4 pj = __ldg(C.pf + j);
-                const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                const float Rt = rt0 + pj.w;
-                int c = 0;
-                if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < Rt * Rt)
-                    c = exact_touch<true>(P, C.M, i, j, qai, qbi, C.qa, C.qb, C.counters);
-                if (c) {
-                    mine[cnt] = j | (c == 2 ? kGuardBit : 0u);
-                    mink[cnt] = (unsigned char)kpos;
-                    ++cnt;
-                } else {
-                    C.hres[3 * e] = make_float4(0.f, 0.f, 0.f, __uint_as_float(0u));
-                }
-            }
-            more = kpos < vc;
-        }
-        __syncwarp();
-        unsigned incl = cnt;
-#pragma unroll
-        for (unsigned o = 1; o < 32u; o <<= 1) {
-            const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        const unsigned off = incl - cnt;
-        const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
-        for (unsigned base = 0; base < total; base += 32u) {
-            const unsigned c = base + lane;
-            unsigned L = 0;
-#pragma unroll
-            for (unsigned b = 16; b; b >>= 1) {
-                const unsigned o = __shfl_sync(0xffffffffu, off, L + b);
-                if (o <= c) L += b;
-            }
-            const unsigned offL = __shfl_sync(0xffffffffu, off, L);
-            const unsigned iL = __shfl_sync(0xffffffffu, i, L);
-            if (c < total) {
-                const unsigned slot = L * kCoopSlots + (c - offL);
-                const unsigned e = B.cand[slot];
-                const unsigned k = B.candk[slot];
-                const Own I = load_own(P, C, iL);
-                PairOut o;
-                contact_force<0, true>(P, C.M, I, e & ~kGuardBit, (e & kGuardBit) != 0u, C.mass0, C.pf, C.qa,
-                                       C.qb, C.pr, C.counters, A, C.ht, hs, &o);
-                float4* r = C.hres + 3 * ((size_t)k * n + iL);
-                r[0] = make_float4(o.Fn.x, o.Fn.y, o.Fn.z, __uint_as_float(o.slip ? 3u : 1u));
-                r[1] = make_float4(o.slip ? o.Ft.x : 0.f, o.slip ? o.Ft.y : 0.f, o.slip ? o.Ft.z : 0.f, o.u.x);
-                r[2] = make_float4(o.u.y, o.u.z, 0.f, 0.f);
-            }
-            __syncwarp();
-        }
-    }
-}
-
-// Pass B: a listed particle's pair sums from the result slots in its list
-// order (or, when it does not share, computed here), written to Fc and Mc.
-__device__ __forceinline__ void half_pass_b(const MixParams& P, const ContactArgs& C, unsigned i)
-{
-    PairAcc A;
-    A.Ft = fk(0.f, 0.f, 0.f);
-    A.Mm = fk(0.f, 0.f, 0.f);
-    A.sumF = fk(0.f, 0.f, 0.f);
-    A.sumM = fk(0.f, 0.f, 0.f);
-    const unsigned n = P.n;
-    const unsigned vc = __ldg(C.vcount + i);
-    if (!shares(vc)) {
-        pairs_serial(P, C, i, A);
-    } else {
-        const float ir = __ldg(C.pf + i).w;
-        for (unsigned k = 0; k < vc; ++k) {
-            const unsigned rid = __ldg(C.vrid + (size_t)k * n + i);
-            const float4* r = C.hres + 3 * (size_t)(rid & ~kPartner);
-            const float4 a = r[0];
-            const unsigned fl = __float_as_uint(a.w);
-            if (!(fl & 1u)) continue;
-            const float4 b = r[1], c = r[2];
-            PairOut o;
-            o.slip = (fl & 2u) != 0u;
-            if (rid & kPartner) {
-                // the contact seen from the other side: normal, force and slip turned
-                o.Fn = fk(-a.x, -a.y, -a.z);
-                o.Ft = fk(-b.x, -b.y, -b.z);
-                o.u = fk(-b.w, -c.x, -c.y);
-            } else {
-                o.Fn = fk(a.x, a.y, a.z);
-                o.Ft = fk(b.x, b.y, b.z);
-                o.u = fk(b.w, c.x, c.y);
-            }
-            if (o.slip) o.Mm = fcross_rn(fk(__fmul_rn(ir, o.u.x), __fmul_rn(ir, o.u.y), __fmul_rn(ir, o.u.z)), o.Ft);
-            accumulate(A, o);
-        }
-    }
-    C.Fc[i] = make_float4(A.sumF.x, A.sumF.y, A.sumF.z, 0.f);
-    C.Mc[i] = make_float4(A.sumM.x, A.sumM.y, A.sumM.z, 0.f);
-}
-
-// Single-scene passes: PASS 0 is pass A (cooperative, dynamic shared
-// memory of one CoopBuf per warp), 1 pass B.
-template <int PASS>
-__global__ void __launch_bounds__(kContactMaxThreads) k_mx_half(MixParams P, ContactArgs C)
-{
-    const unsigned total = C.counters[CN_HEAVY], front = C.counters[CN_HTRI];
-    const unsigned warps = gridDim.x * (blockDim.x / 32u);
-    const unsigned gw = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u;
-    if (PASS == 0) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) C.counters[CN_REBUILD] = 0;
-        extern __shared__ CoopBuf coop_buf[];
-        CoopBuf& B = coop_buf[threadIdx.x / 32u];
-        for (unsigned t0 = gw * 32u; t0 < total; t0 += warps * 32u) {
-            const unsigned t = t0 + (threadIdx.x & 31u);
-            const bool valid = t < total;
-            half_pass_a(P, C, valid, valid ? __ldg(C.hlist + list_index(t, front, P.n)) : 0u, B);
-        }
-        return;
-    }
-    for (unsigned t = gw * 32u + (threadIdx.x & 31u); t < total; t += warps * 32u)
-        half_pass_b(P, C, __ldg(C.hlist + list_index(t, front, P.n)));
 }
 
 // COOP: the warp-cooperative pair pass (no history, no recording; dynamic
@@ -3029,7 +2792,6 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
         P.G1[a] = df_split(dt * P.g[a]);
         P.G2[a] = df_split(half2dt * P.g[a]);
     }
-    P.gnorm = sqrtf(P.gf[0] * P.gf[0] + P.gf[1] * P.gf[1] + P.gf[2] * P.gf[2]);
     P.dt = dt;
     P.csf = (float)s->cs;
     P.inv_csf = (float)(1.0 / s->cs);
@@ -3122,13 +2884,6 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     A(alloc(s, &s->wmask, n));
     A(alloc(s, &s->vcount, n));
     A(alloc(s, &s->vlist, n * s->vcap));
-    if (s->cmode == 2) {
-        if ((unsigned long long)kHalfCap * n >= (1ull << 31))
-            return set_error(XD_ERR_CAPACITY, "mixed mode: contact_mode 2 holds at most %u particles",
-                             (1u << 31) / kHalfCap - 1u);
-        A(alloc(s, &s->vrid, (size_t)kHalfCap * n));
-        A(alloc(s, &s->hres, (size_t)3 * kHalfCap * n));
-    }
     A(alloc(s, &s->pref, n));
     A(alloc(s, &s->keys, n));
     A(alloc(s, &s->vals, n));
@@ -3528,7 +3283,6 @@ static int rebuild(MixedScene* s, cudaStream_t q)
     k_mx_build<<<blocks(n, 256), 256, 0, q>>>(s->P, s->pf, s->prev_keys, s->lb, s->vcount, s->vlist, s->pref,
                                               s->wmask, s->tcount, s->rxn, s->hlist, s->Fc, s->Mc,
                                               s->counters);
-    if (s->cmode == 2) k_half_rid<<<blocks(n, 256), 256, 0, q>>>(s->P, s->vcount, s->vlist, s->vrid);
     return launch_status("mixed re-binning");
 }
 
@@ -3618,8 +3372,6 @@ static ContactArgs contact_args(MixedScene* s, unsigned* rc, unsigned* rp, unsig
     C.rec_cap = rec_cap;
     C.ht = ht;
     C.rxn_on = rxn_on;
-    C.vrid = s->vrid;
-    C.hres = s->hres;
     return C;
 }
 
@@ -3688,10 +3440,6 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
         else if (hist == 1) XD_MX_CONTACT(false, 1);
         else if (s->cmode == 1) {
             k_mx_contact<false, 0, true><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(s->P, C);
-            if (s->P.nplanes || s->P.ntri) k_mx_walls<<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(s->P, C);
-        } else if (s->cmode == 2) {
-            k_mx_half<0><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(s->P, C);
-            k_mx_half<1><<<grid, ct, 0, q>>>(s->P, C);
             if (s->P.nplanes || s->P.ntri) k_mx_walls<<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(s->P, C);
         } else XD_MX_CONTACT(false, 0);
     }
@@ -3828,8 +3576,7 @@ unsigned long long mixed_launches(MixedScene* s, unsigned nsteps)
     // re-bins adds mixed_rebuild_launches()
     // (and the wall pass after a cooperative pair pass)
     const unsigned long long per = 2 + (s->kinematic && s->ntri ? 3 : 0) +
-                                   (s->cmode >= 1 && (s->P.nplanes || s->P.ntri) ? 1 : 0) +
-                                   (s->cmode == 2 ? 1 : 0);
+                                   (s->cmode == 1 && (s->P.nplanes || s->P.ntri) ? 1 : 0);
     unsigned long long total = per * nsteps + 1 + (s->nbodies ? 1 : 0);
     if (!s->cells_clean) total += mixed_rebuild_launches(s);   // the first step re-bins
     return total;
@@ -4028,8 +3775,8 @@ int mixed_set_tuning(MixedScene* s, const xd_tuning* t)
     if (t->contact_threads != 32 && t->contact_threads != 64 && t->contact_threads != 128)
         return set_error(XD_ERR_INVALID, "scene_set_tuning: contact block of %u threads (32, 64 or 128)",
                          t->contact_threads);
-    if (t->contact_mode > 2)
-        return set_error(XD_ERR_INVALID, "scene_set_tuning: contact mode %u (0, 1 or 2)", t->contact_mode);
+    if (t->contact_mode > 1)
+        return set_error(XD_ERR_INVALID, "scene_set_tuning: contact mode %u (0 or 1)", t->contact_mode);
     s->cmode = t->contact_mode;
     s->skin_factor = t->skin_factor;
     s->vcap = t->verlet_cap;
@@ -4268,9 +4015,8 @@ __device__ void batch_runs(const BatchScene* __restrict__ D, unsigned ns, unsign
     __syncthreads();
 }
 
-// The runs of the contact launch (chunk_start), of the wall launch
-// (chunk_start + ns + 2) and of contact_mode 2's pass B (chunk_start +
-// 2 (ns + 2)).
+// The runs of the contact launch (chunk_start) and of the wall launch
+// (chunk_start + ns + 2).
 __global__ void __launch_bounds__(1024) k_batch_chunks(const BatchScene* __restrict__ D, unsigned ns,
                                                        unsigned* __restrict__ chunk_start)
 {
@@ -4278,7 +4024,6 @@ __global__ void __launch_bounds__(1024) k_batch_chunks(const BatchScene* __restr
     __shared__ unsigned carry;
     batch_runs(D, ns, CN_HEAVY, chunk_start, c, carry);
     batch_runs(D, ns, CN_HTRI, chunk_start + ns + 2, c, carry);
-    batch_runs(D, ns, CN_HEAVY, chunk_start + 2 * (ns + 2), c, carry);   // a second pass over the lists
 }
 
 // The contact pass of every scene: each warp takes the next kBatchGrab runs
@@ -4288,8 +4033,7 @@ __global__ void __launch_bounds__(1024) k_batch_chunks(const BatchScene* __restr
 // warp loads the scene of a run into its own shared-memory slot when the
 // scene changes.
 // KIND 0: the per-particle contact pass; 1: the cooperative pair pass; 2:
-// the wall pass (runs over the front of each scene's list); 3 and 4:
-// contact_mode 2's passes A and B.
+// the wall pass (runs over the front of each scene's list).
 template <int KIND>
 __global__ void __launch_bounds__(kContactMaxThreads) k_batch_contact(const BatchScene* __restrict__ D, unsigned ns,
                                                                    unsigned* __restrict__ chunk_start)
@@ -4334,12 +4078,6 @@ __global__ void __launch_bounds__(kContactMaxThreads) k_batch_contact(const Batc
             extern __shared__ CoopBuf coop_buf[];
             const bool valid = t < front;
             walls_entry_coop(W.P, W.C, valid, valid ? __ldg(W.C.hlist + t) : 0u, coop_buf[wb]);
-        } else if (KIND == 3) {
-            extern __shared__ CoopBuf coop_buf[];
-            const bool valid = t < heavy;
-            half_pass_a(W.P, W.C, valid, valid ? __ldg(W.C.hlist + list_index(t, front, W.P.n)) : 0u, coop_buf[wb]);
-        } else if (KIND == 4) {
-            if (t < heavy) half_pass_b(W.P, W.C, __ldg(W.C.hlist + list_index(t, front, W.P.n)));
         } else if (t < heavy) {
             contact_entry<false, 0>(W.P, W.C, __ldg(W.C.hlist + list_index(t, front, W.P.n)));
         }
@@ -4379,15 +4117,10 @@ struct MixedBatch {
 static void launch_batch_pairs(const MixedBatch* b, unsigned ns, cudaStream_t q)
 {
     const unsigned ct = b->cthreads, grid = kContactWarpsTotal * 32u / ct;
-    if (b->cmode == 1) {
+    if (b->cmode == 1)
         k_batch_contact<1><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(b->d_scenes, ns, b->d_chunks);
-    } else if (b->cmode == 2) {
-        // pass B takes the same runs again: its counter is the wall runs' (cleared)
-        k_batch_contact<3><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(b->d_scenes, ns, b->d_chunks);
-        k_batch_contact<4><<<grid, ct, 0, q>>>(b->d_scenes, ns, b->d_chunks + 2 * (ns + 2));
-    } else {
+    else
         k_batch_contact<0><<<grid, ct, 0, q>>>(b->d_scenes, ns, b->d_chunks);
-    }
 }
 
 // The wall pass after a cooperative pair pass (none otherwise: the
@@ -4395,7 +4128,7 @@ static void launch_batch_pairs(const MixedBatch* b, unsigned ns, cudaStream_t q)
 static void launch_batch_walls(const MixedBatch* b, unsigned ns, cudaStream_t q)
 {
     const unsigned ct = b->cthreads, grid = kContactWarpsTotal * 32u / ct;
-    if (b->cmode >= 1 && b->walls)
+    if (b->cmode == 1 && b->walls)
         k_batch_contact<2><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(b->d_scenes, ns, b->d_chunks + ns + 2);
 }
 
@@ -4619,7 +4352,7 @@ int prepare_batch(MixedBatch* b)
     M(&b->d_scenes, ns, "batch scenes");
     M(&b->d_block_scene, block_scene.size(), "batch blocks");
     M(&b->d_flags, ns, "batch flags");
-    M(&b->d_chunks, 3 * (ns + 2), "batch runs");
+    M(&b->d_chunks, 2 * (ns + 2), "batch runs");
     M(&b->d_handles[0], ng + ns, "batch handles");
     M(&b->d_handles[1], ng + ns, "batch handles");
     M(&b->d_handles[2], (size_t)(ng + ns) * kBatchGraphSteps, "batch handles");
@@ -4729,7 +4462,7 @@ int batch_step_direct(MixedBatch* b, unsigned nsteps, cudaStream_t q)
         if (st != XD_OK) break;
         k_batch_chunks<<<1, 1024, 0, q>>>(b->d_scenes, ns, b->d_chunks);
         span(1, [&] { launch_batch_pairs(b, ns, q); });
-        if (b->cmode >= 1 && b->walls) span(2, [&] { launch_batch_walls(b, ns, q); });
+        if (b->cmode == 1 && b->walls) span(2, [&] { launch_batch_walls(b, ns, q); });
         st = launch_status("batch contact");
     }
     if (st == XD_OK) {

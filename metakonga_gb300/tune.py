@@ -11,8 +11,8 @@ choices that trade against each other differently per scene:
   overflows has its contact pass search the cells instead (correct, slower);
 * the contact pass's block size (32, 64 or 128 threads);
 * its pair pass: a thread per listed particle (best when few particles touch
-  anything), warp-cooperative (the warp's contacts spread one per lane), or
-  warp-cooperative with each shared pair computed once (packed beds).
+  anything) or warp-cooperative (the warp's contacts spread one per lane:
+  best in packed beds).
 
 ``tune`` times candidate settings on a short window of the scene's own steps
 (CUDA events, the same step graphs a run replays) and keeps the fastest; the
@@ -20,9 +20,8 @@ list capacities are raised where the defaults' lists overflowed.  Results
 are cached in a JSON file keyed by the scene's shape -- particle count
 (octave), radius spread, walls and triangles, packing -- so that similar
 scenes reuse them (``tuned``).  Every setting gives the same contacts: the
-choices change only how the contact pass finds them (the first two pair
-passes give the same bits; the third computes each shared pair once, within
-the same error bounds).
+choices change only how the contact pass finds them (and the two pair
+passes give the same bits).
 """
 from __future__ import annotations
 
@@ -37,7 +36,7 @@ from . import engine
 
 SKINS = (0.05, 0.1, 0.2, 0.35)
 THREADS = (32, 64, 128)
-MODES = (0, 1, 2)
+MODES = (0, 1)
 
 
 def cache_path() -> str:

@@ -72,10 +72,9 @@ def test_batch_equals_each_scene_alone(cuda, moved, timed):
             assert ba.tobytes() == bb.tobytes()
 
 
-@pytest.mark.parametrize("mode", [0, 2])
-def test_batch_equals_each_scene_alone_other_pair_passes(cuda, mode):
-    """The per-particle pass and the once-per-pair pass, batched and alone."""
-    t = {"contact_mode": mode}
+def test_batch_equals_each_scene_alone_per_particle_pass(cuda):
+    """The per-particle pair pass (contact_mode 0), batched and alone."""
+    t = {"contact_mode": 0}
     alone = _run((5, 27, 16), False, tuning=t)
     batch = _run((5, 27, 16), True, tuning=t)
     for (a, ra, ba), (b, rb, bb) in zip(alone, batch):

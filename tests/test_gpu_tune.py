@@ -28,8 +28,6 @@ def _packed():
     {"skin_factor": 0.2, "verlet_cap": 96},
     {"contact_mode": 0},
     {"contact_mode": 0, "verlet_cap": 8},
-    {"contact_mode": 2},
-    {"contact_mode": 2, "verlet_cap": 12},   # some lists over capacity, some over the shared cap
 ])
 def test_tuned_settings_give_the_oracle_contacts(cuda, oracle, tuning):
     sc = _packed()
@@ -115,24 +113,3 @@ def test_contact_modes_give_the_same_bits(cuda, case):
     if case == "packed_cells":
         assert t1["verlet_overflows"] > 0
 
-
-def test_once_per_pair_mode_on_a_settled_bed(cuda, oracle):
-    """contact_mode 2 on a settled hopper bed (pairs, the cone, the floor):
-    the oracle's pair list and forces within the mixed form's gate."""
-    from metakonga_gb300 import prepare
-
-    from .test_gpu_configs import _oracle_view as _oracle_view_walls
-    sc = scenes.hopper(n=6000, seed=12, gate=True)
-    prepare.settle(sc, 3000, dt=4e-5)
-    prepare.open_gates(sc)
-    d = engine.DeviceScene(sc, mode=engine.MODE_MIXED, tuning={"contact_mode": 2})
-    d.step(3, check=True)
-    st = d.download()
-    pairs_ref, f_ref, m_ref, mag = _oracle_view_walls(oracle, sc, st)
-    pairs = d.pair_list(cap=48)
-    f, m = d.eval_contacts()
-    d.close()
-    assert _pairset(pairs) == _pairset(pairs_ref)
-    assert _norm_err(f, f_ref, mag, sc.mass) <= FORCE_TOL
-    r = sc.pos[:, 3:4]
-    assert _norm_err(m / r, m_ref / r, mag, sc.mass) <= FORCE_TOL
