@@ -117,6 +117,8 @@ struct MixParams {
     float csf, inv_csf;
     float half_skin;     // a particle keeps its cell while within half the skin of it
     float rmaxf;         // largest radius
+    int small_q;         // 2 r_max < 2^-6 m: a touching pair's fixed-point separation and radius sum fit
+                         // in 32 bits (their FP32 values then come from 32-bit conversions)
     float vcut;          // Verlet list: pairs within ri + rj + vcut are listed
     float disp2;         // squared displacement that forces re-binning
     float inv_gx, inv_gxy;   // 1 / gx, 1 / (gx gy) for the key decode
@@ -368,12 +370,12 @@ __device__ __forceinline__ void df_diff(float ah, float bh, float dlo, float& s,
 }
 
 // Normal speed (dv . dq) / |dq| in double-float: dv = s + t per component,
-// dq the exact integer separation (|dq| < 2^31), D2 = |dq|^2 exact, d0 its
-// FP32 square root.  The dot product of a fast tangential velocity with the
-// contact normal cancels; here it is carried with ~2^-44 relative error and
-// rounded once.
+// dq the exact integer separation (|dq| < 2^31), D2 = |dq|^2 exact, D2h its
+// FP32 rounding, d0 the FP32 square root of that.  The dot product of a fast
+// tangential velocity with the contact normal cancels; here it is carried
+// with ~2^-44 relative error and rounded once.
 __device__ __forceinline__ float normal_speed(const float s[3], const float t[3], const int dq[3],
-                                              float d0, long long D2, float& q0_out, float& q1_out,
+                                              float d0, long long D2, float D2h, float& q0_out, float& q1_out,
                                               float& c_out)
 {
     float hi = 0.f, lo = 0.f;
@@ -392,7 +394,7 @@ __device__ __forceinline__ float normal_speed(const float s[3], const float t[3]
     // |dq| = d0 + c with c = (D2 - d0^2) / (2 d0)
     float p, pe;
     two_prod(d0, d0, p, pe);
-    const float D2h = __ll2float_rn(D2);
+    // D2h: D2 rounded to FP32 (the caller's, for d0)
     const float D2l = __ll2float_rn(D2 - __float2ll_rn(D2h));
     const float c = __fadd_rn(__fsub_rn(__fsub_rn(D2h, p), pe), D2l) / __fmul_rn(2.f, d0);
     // (nv + nl) / (d0 + c)
@@ -1403,16 +1405,31 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     const longlong2 qaj = __ldg(qa + j), qbj = __ldg(qb + j);
     const long long ddx = qaj.x - I.qa.x, ddy = qaj.y - I.qa.y, ddz = qbj.x - I.qb.x;
     const long long D2 = ddx * ddx + ddy * ddy + ddz * ddz;
-    const float dn = sqrtf((float)D2);
+    const float D2f = (float)D2;
+    const float dn = sqrtf(D2f);
+    // 64-bit integer conversions issue on the FP64 pipe: values that fit in
+    // 32 bits (a touching pair's separation and radius sum when 2 r_max <
+    // 2^-6 m) take the 32-bit ones, which round the same
+    float fdx, fdy, fdz;
+    if (P.small_q) {
+        fdx = __int2float_rn((int)ddx);
+        fdy = __int2float_rn((int)ddy);
+        fdz = __int2float_rn((int)ddz);
+    } else {
+        fdx = (float)ddx;
+        fdy = (float)ddy;
+        fdz = (float)ddz;
+    }
     float delta;
     if (guard) {
         delta = (float)fp64_cdist(M, i, j);
     } else {
         const long long Rq = I.qb.y + qbj.y;
-        delta = ((float)(Rq * Rq - D2) / ((float)Rq + dn)) * kU;
+        const float fRq = P.small_q ? __int2float_rn((int)Rq) : (float)Rq;
+        delta = ((float)(Rq * Rq - D2) / (fRq + dn)) * kU;
     }
     const float inv = 1.0f / dn;
-    const f3 u = fk((float)ddx * inv, (float)ddy * inv, (float)ddz * inv);
+    const f3 u = fk(fdx * inv, fdy * inv, fdz * inv);
     // The fixed point's residuals restore the FP64 positions: the overlap
     // gains (e_ri + e_rj) - u . (e_j - e_i) (the 2^-36 m grid alone would move
     // a light contact's overlap by up to ~3e-11 m, a part in 1e5 of 3e-6 m)
@@ -1436,7 +1453,7 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     // rv . u = dv . u (the rotation term is perpendicular to u), in double-float
     const int dqi[3] = { (int)ddx, (int)ddy, (int)ddz };
     float rq0, rq1, rqc;
-    float rvu = normal_speed(dvs, dvt, dqi, dn, D2, rq0, rq1, rqc);
+    float rvu = normal_speed(dvs, dvt, dqi, dn, D2, D2f, rq0, rq1, rqc);
     {
         // and the normal's turn (de - (u . de) u) / |d| in the normal speed
         const float cr = (fdot(dv, de) - rvu * ude) * (inv * (1.0f / kU));
@@ -2797,6 +2814,7 @@ static int mixed_setup(MixedScene* s, const xd_scene_desc& d, const double* pos_
     P.inv_csf = (float)(1.0 / s->cs);
     P.half_skin = (float)(0.5 * skin);
     P.rmaxf = (float)rmax;
+    P.small_q = 2.0 * rmax < 0x1p-6 ? 1 : 0;
     P.inv_gx = 1.0f / (float)g[0];
     P.inv_gxy = 1.0f / (float)((double)g[0] * g[1]);
     P.dtf = (float)dt;
