@@ -981,17 +981,45 @@ def run_batched(a):
     # spheres are in larger scenes), its choice applied to every scene
     tuned = None
     tuning = dict(engine.DEFAULT_TUNING)
+    tunings = [tuning] * len(scs)
     if not a.no_tune:
+        # the autotuner per scene shape (particle-count octave, radius
+        # spread, walls, packing: tune.shape_key) on the shape's median
+        # scene, cached in a file of this run and applied to every scene of
+        # the shape; the batch's launch shape and pair pass (one launch
+        # serves all scenes) are those of the particle-weighted median scene
+        import tempfile
+
         from metakonga_gb300 import tune
+        cache = os.path.join(tempfile.gettempdir(), f"xdem_bench_tuning_{os.getpid()}.json")
+        os.environ["XDEM_TUNE_CACHE"] = cache
+        t_tune = time.perf_counter()
+        groups = {}
+        for k, sc in enumerate(scs):
+            groups.setdefault(tune.shape_key(sc), []).append(k)
+        per_shape = {}
+        for key, ks in sorted(groups.items()):
+            ks = sorted(ks, key=lambda k: scs[k].np_)
+            rep = ks[len(ks) // 2]
+            tr = tune.tune(scs[rep], steps=a.tune_steps, warm=5, store=True)
+            per_shape[key] = {"scenes": len(ks), "scene": rep, "particles": int(scs[rep].np_),
+                              "choice": tr["tuning"], "ms_per_step": tr["ms_per_step"],
+                              "default_ms_per_step": tr["default_ms_per_step"]}
         order = np.argsort([sc.np_ for sc in scs])
         cum = np.cumsum([scs[k].np_ for k in order])
         k_w = int(order[int(np.searchsorted(cum, cum[-1] / 2))])
-        tr = tune.tune(scs[k_w], steps=a.tune_steps, warm=5, store=False)
-        tuning = dict(tr["tuning"])
-        tuned = {"scene": k_w, "particles": int(scs[k_w].np_), "choice": tuning,
-                 "scene_ms_per_step": tr["ms_per_step"], "scene_default_ms_per_step": tr["default_ms_per_step"],
-                 "candidates": tr["candidates"], "window_steps": tr["window_steps"], "seconds": tr["seconds"]}
-    ds = [engine.DeviceScene(sc, mode=engine.MODE_MIXED, tuning=tuning) for sc in scs]
+        launch = tune.tuned(scs[k_w])
+        tunings = [dict(tune.tuned(sc), contact_threads=launch["contact_threads"],
+                        contact_mode=launch["contact_mode"]) for sc in scs]
+        tuning = tunings[k_w]
+        try:
+            os.remove(cache)
+        except OSError:
+            pass
+        tuned = {"per_shape": per_shape, "launch_shape_scene": k_w, "launch": {
+                     "contact_threads": launch["contact_threads"], "contact_mode": launch["contact_mode"]},
+                 "seconds": time.perf_counter() - t_tune, "window_steps": a.tune_steps}
+    ds = [engine.DeviceScene(sc, mode=engine.MODE_MIXED, tuning=t) for sc, t in zip(scs, tunings)]
     dev_bytes = sum(d.device_bytes() for d in ds)
     batch = engine.Batch(ds)
     batch.step(a.warmup, check=True, stream=sh)
@@ -1059,7 +1087,7 @@ def run_batched(a):
     # per step: advance, decision, run prefix and contact over all scenes; per
     # call the finish and each scene's body-reaction sum; per re-binning its
     # kernels and its group's decision kernel
-    walls_pass = 1 if tuning.get("contact_mode", 1) == 1 else 0   # the cooperative pass's wall launch
+    walls_pass = 1 if tunings[0].get("contact_mode", 1) == 1 else 0   # the cooperative pass's wall launch
     launches = ((4 + walls_pass) * a.steps + 1 + sum(1 for sc in scs if sc.ntri)
                 + sum((b[0] - r[0]) * (b[1] + 1) for r, b in zip(rb0, rb1)))
 
@@ -1135,7 +1163,7 @@ def run_batched(a):
     check["scene"] = k_med
     # the batch with the default tuning, for the autotuner's gain
     if tuned is not None:
-        if tuning != engine.DEFAULT_TUNING:
+        if any(t != engine.DEFAULT_TUNING for t in tunings):
             ds0 = [engine.DeviceScene(sc, mode=engine.MODE_MIXED) for sc in scs]
             b0 = engine.Batch(ds0)
             b0.step(a.warmup, check=True, stream=sh)

@@ -2393,9 +2393,17 @@ __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const Con
 // then its wall force to its pair force -- the additions the per-particle
 // pass makes after its pairs (F += walls).  A launch of its own: the wall
 // code's FP64 region tests and registers stay out of the pair pass.
+// The wall pass's shared memory per warp: the candidate buffer, and each
+// lane's particle data read once by its own lane for all its candidates.
+struct WallBuf {
+    CoopBuf c;
+    WallOwn own[32];
+};
+
 __device__ __forceinline__ void walls_entry_coop(const MixParams& P, const ContactArgs& C, bool valid, unsigned i,
-                                                 CoopBuf& B)
+                                                 WallBuf& WB)
 {
+    CoopBuf& B = WB.c;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned n = P.n;
     unsigned wm = 0, kb = 0, ke = 0;
@@ -2419,6 +2427,7 @@ __device__ __forceinline__ void walls_entry_coop(const MixParams& P, const Conta
         }
     }
     const bool any = wm || kb < ke;
+    if (any) WB.own[lane] = load_wall_own(P, C, i);
     f3 f = fk(0.f, 0.f, 0.f), Ftri = fk(0.f, 0.f, 0.f);
     RxnAcc ra;
     ra.b = 0xffffffffu;
@@ -2448,10 +2457,8 @@ __device__ __forceinline__ void walls_entry_coop(const MixParams& P, const Conta
                 if (o <= c) L += b;
             }
             const unsigned offL = __shfl_sync(0xffffffffu, off, L);
-            const unsigned iL = __shfl_sync(0xffffffffu, i, L);
             if (c < total) {
-                const WallOwn w = load_wall_own(P, C, iL);
-                const WallRes r = wall_eval(P, C, w, B.cand[L * kCoopSlots + (c - offL)]);
+                const WallRes r = wall_eval(P, C, WB.own[L], B.cand[L * kCoopSlots + (c - offL)]);
                 B.res[0][lane] = r.o.Fn.x;
                 B.res[1][lane] = r.o.Fn.y;
                 B.res[2][lane] = r.o.Fn.z;
@@ -2491,8 +2498,8 @@ __device__ __forceinline__ void walls_entry_coop(const MixParams& P, const Conta
 
 __global__ void __launch_bounds__(kContactMaxThreads) k_mx_walls(MixParams P, ContactArgs C)
 {
-    extern __shared__ CoopBuf coop_buf[];
-    CoopBuf& B = coop_buf[threadIdx.x / 32u];
+    extern __shared__ WallBuf wall_buf[];
+    WallBuf& B = wall_buf[threadIdx.x / 32u];
     const unsigned front = C.counters[CN_HTRI];
     const unsigned warps = gridDim.x * (blockDim.x / 32u);
     const unsigned gw = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u;
@@ -3458,7 +3465,7 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
         else if (hist == 1) XD_MX_CONTACT(false, 1);
         else if (s->cmode == 1) {
             k_mx_contact<false, 0, true><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(s->P, C);
-            if (s->P.nplanes || s->P.ntri) k_mx_walls<<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(s->P, C);
+            if (s->P.nplanes || s->P.ntri) k_mx_walls<<<grid, ct, (ct / 32u) * sizeof(WallBuf), q>>>(s->P, C);
         } else XD_MX_CONTACT(false, 0);
     }
 #undef XD_MX_CONTACT
@@ -4093,9 +4100,9 @@ __global__ void __launch_bounds__(kContactMaxThreads) k_batch_contact(const Batc
             contact_entry_coop(W.P, W.C, valid, valid ? __ldg(W.C.hlist + list_index(t, front, W.P.n)) : 0u,
                                coop_buf[wb]);
         } else if (KIND == 2) {
-            extern __shared__ CoopBuf coop_buf[];
+            extern __shared__ WallBuf wall_buf[];
             const bool valid = t < front;
-            walls_entry_coop(W.P, W.C, valid, valid ? __ldg(W.C.hlist + t) : 0u, coop_buf[wb]);
+            walls_entry_coop(W.P, W.C, valid, valid ? __ldg(W.C.hlist + t) : 0u, wall_buf[wb]);
         } else if (t < heavy) {
             contact_entry<false, 0>(W.P, W.C, __ldg(W.C.hlist + list_index(t, front, W.P.n)));
         }
@@ -4147,7 +4154,7 @@ static void launch_batch_walls(const MixedBatch* b, unsigned ns, cudaStream_t q)
 {
     const unsigned ct = b->cthreads, grid = kContactWarpsTotal * 32u / ct;
     if (b->cmode == 1 && b->walls)
-        k_batch_contact<2><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(b->d_scenes, ns, b->d_chunks + ns + 2);
+        k_batch_contact<2><<<grid, ct, (ct / 32u) * sizeof(WallBuf), q>>>(b->d_scenes, ns, b->d_chunks + ns + 2);
 }
 
 static void launch_batch_contact(const MixedBatch* b, unsigned ns, cudaStream_t q)

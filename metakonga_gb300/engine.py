@@ -43,8 +43,9 @@ def _addr(a):
 
 
 class Tuning(C.Structure):
-    """xd_tuning: skin width over r_max, Verlet/triangle list capacities, and
-    the contact pass's block size (mixed form; set before the first upload)."""
+    """xd_tuning: skin width over r_max, Verlet/triangle list capacities, the
+    contact pass's block size and its pair pass (0 a thread per listed
+    particle, 1 warp-cooperative; mixed form; set before the first upload)."""
     _fields_ = [("skin_factor", C.c_float), ("verlet_cap", C.c_uint), ("triangle_cap", C.c_uint),
                 ("contact_threads", C.c_uint), ("contact_mode", C.c_uint)]
 
