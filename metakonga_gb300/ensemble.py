@@ -3,7 +3,7 @@
 Granular trajectories are chaotic: two runs whose forces differ by rounding
 separate after a few thousand steps, so long runs of two precision forms are
 compared through statistics of the state rather than particle by particle.
-These are the three the contact step is judged by:
+The long-run comparisons use these three:
 
 * kinetic energy (translational + rotational) -- sampled over a run it gives
   the decay curve of a settling bed;
