@@ -214,6 +214,7 @@ struct MixedScene {
     double* rxn = nullptr;        // reaction on the bodies per particle [nbodies][6][n]
     double* rxn_part = nullptr;   // block partials of its fixed-order sum
     bool bodies_dirty = false;
+    bool tri_table_dirty = true;   // the triangles' cell table is to be built before the next step
     std::vector<xd_polygon_info> host_poly;
     std::vector<double> host_sphere, host_vlist;
     std::vector<xd_polygon_mass_info> host_pmi;
@@ -3260,6 +3261,26 @@ static int flush_reactions(MixedScene* s, cudaStream_t q)
     return launch_status("mixed body reaction");
 }
 
+// The triangles' cell table: every triangle registered in each cell its
+// box widened by the reach covers, as (cell, triangle) pairs sorted by cell,
+// and the vertices it was built with (the moved-vertex test's reference).
+static int build_tri_table(MixedScene* s, cudaStream_t q)
+{
+    const unsigned T = s->ntri, cap = s->tpair_cap;
+    k_tri_count<<<blocks(T + 1, 256), 256, 0, q>>>(s->P, s->poly, s->tcells, s->tri_ref, s->tbound);
+    k_scan1<<<1, 1024, 0, q>>>(s->tcells, T + 1);
+    k_tri_fill<<<blocks(T, 256), 256, 0, q>>>(s->P, s->poly, s->tcells, cap, s->tpk, s->tpt);
+    k_tri_pad<<<blocks(cap, 256), 256, 0, q>>>(s->tcells, T, cap, s->ncell, s->tpk, s->tpt);
+    int st = launch_status("mixed triangle cells");
+    unsigned *tk = nullptr, *tt = nullptr;
+    if (st == XD_OK)
+        st = radix_sort_pairs(s->tpk, s->tpt, cap, key_bits_for(s->ncell + 1), s->tsort_scratch, q, &tk, &tt);
+    if (st != XD_OK) return st;
+    s->tpk_sorted = tk;
+    s->tpt_sorted = tt;
+    return XD_OK;
+}
+
 static int rebuild(MixedScene* s, cudaStream_t q)
 {
     const unsigned n = s->n;
@@ -3287,21 +3308,14 @@ static int rebuild(MixedScene* s, cudaStream_t q)
     k_lb_long<<<152 * 4, 256, 0, q>>>(s->gaps, s->counters, s->lb);
     st = launch_status("mixed re-binning");
     if (st == XD_OK && s->ntri) {
-        // triangles: (cell, triangle) pairs sorted by cell, then each particle's list
-        const unsigned T = s->ntri, cap = s->tpair_cap;
-        k_tri_count<<<blocks(T + 1, 256), 256, 0, q>>>(s->P, s->poly, s->tcells, s->tri_ref, s->tbound);
-        k_scan1<<<1, 1024, 0, q>>>(s->tcells, T + 1);
-        k_tri_fill<<<blocks(T, 256), 256, 0, q>>>(s->P, s->poly, s->tcells, cap, s->tpk, s->tpt);
-        k_tri_pad<<<blocks(cap, 256), 256, 0, q>>>(s->tcells, T, cap, s->ncell, s->tpk, s->tpt);
-        st = launch_status("mixed triangle cells");
-        unsigned *tk = nullptr, *tt = nullptr;
-        if (st == XD_OK)
-            st = radix_sort_pairs(s->tpk, s->tpt, cap, key_bits_for(s->ncell + 1), s->tsort_scratch, q, &tk, &tt);
+        // triangles: the (cell, triangle) table -- here for meshes that move
+        // on the device; the host keeps a static mesh's table (update_mesh)
+        // -- then each particle's list
+        if (s->kinematic) st = build_tri_table(s, q);
         if (st != XD_OK) return st;
-        s->tpk_sorted = tk;
-        s->tpt_sorted = tt;
-        k_tri_build<<<blocks(n, 256), 256, 0, q>>>(s->P, s->pf, s->prev_keys, tk, tt, cap, s->tri_ref, s->tbound,
-                                                   s->tcount, s->tlist, s->counters);
+        k_tri_build<<<blocks(n, 256), 256, 0, q>>>(s->P, s->pf, s->prev_keys, s->tpk_sorted, s->tpt_sorted,
+                                                   s->tpair_cap, s->tri_ref, s->tbound, s->tcount, s->tlist,
+                                                   s->counters);
         st = launch_status("mixed triangle lists");
     }
     if (st != XD_OK) return st;
@@ -3316,11 +3330,26 @@ static int rebuild(MixedScene* s, cudaStream_t q)
 // last build.  Runs before a step's advance.
 static int update_mesh(MixedScene* s, cudaStream_t q)
 {
-    if (!s->ntri || !s->bodies_dirty) return XD_OK;
-    const int st = launch_mesh_move(s->pmi, s->vlist_body, s->sphere, s->poly, s->ntri, s->tri_ref, s->P.wo,
-                                    s->P.disp2, s->counters + CN_REBUILD, s->trec, q);
-    if (st == XD_OK) s->bodies_dirty = false;
-    return st;
+    if (!s->ntri) return XD_OK;
+    int st = XD_OK;
+    if (s->bodies_dirty) {
+        st = launch_mesh_move(s->pmi, s->vlist_body, s->sphere, s->poly, s->ntri, s->tri_ref, s->P.wo,
+                              s->P.disp2, s->counters + CN_REBUILD, s->trec, q);
+        if (st != XD_OK) return st;
+        s->bodies_dirty = false;
+        if (!s->kinematic) s->tri_table_dirty = true;
+    }
+    // A mesh that moves only between calls keeps its cell table out of the
+    // re-binning: built here when it has moved (and after an upload), with a
+    // re-binning of the lists forced, so that the moved-vertex reference and
+    // the lists stay those of one build.
+    if (!s->kinematic && s->tri_table_dirty) {
+        st = build_tri_table(s, q);
+        if (st != XD_OK) return st;
+        s->tri_table_dirty = false;
+        s->cells_clean = false;
+    }
+    return XD_OK;
 }
 
 // Inside a stream capture: a conditional node that runs body(s, stream) when
@@ -3611,9 +3640,10 @@ unsigned long long mixed_rebuild_launches(MixedScene* s)
 {
     if (!s || s->n == 0) return 0;
     // keys, sort, permute, copy back, cell bounds (2), list build; with
-    // triangles also count, scan, fill, pad, their sort and their lists
+    // triangles also their lists, and for a mesh that moves on the device
+    // its cell table (count, scan, fill, pad and their sort)
     unsigned long long k = (s->n > 1 ? 5ull * s->passes : 0ull) + 6;
-    if (s->ntri) k += 5 + 5ull * ((key_bits_for(s->ncell + 1) + 7) / 8);
+    if (s->ntri) k += 1 + (s->kinematic ? 4 + 5ull * ((key_bits_for(s->ncell + 1) + 7) / 8) : 0ull);
     if (s->nbodies) k += 1;   // the reactions flushed first
     return k;
 }
@@ -3823,6 +3853,7 @@ int mixed_set_kinematic(MixedScene* s, bool enable)
 {
     if (enable && !s->desc.ntri) return set_error(XD_ERR_STATE, "scene_set_kinematic_bodies: no polygon bodies");
     if (enable != s->kinematic) destroy_graphs(s);   // the step graphs hold the step's launches
+    if (!enable && s->kinematic) s->tri_table_dirty = true;
     s->kinematic = enable;
     return XD_OK;
 }
@@ -4530,9 +4561,15 @@ void mixed_batch_kernel_times(MixedBatch* b, double ms[3], unsigned long long la
 int mixed_batch_step(MixedBatch* b, unsigned nsteps, cudaStream_t q)
 {
     if (nsteps == 0) return XD_OK;
+    int st = XD_OK;
+    // meshes moved and cell tables built first: the batch's capture takes the tables' addresses
+    for (MixedScene* sc : b->scenes) {
+        if (!sc->ready) return set_error(XD_ERR_STATE, "batch: a scene has no state uploaded");
+        if (!sc->kinematic) st = update_mesh(sc, q);
+        if (st != XD_OK) return st;
+    }
     bool stale = !b->captured;
     for (size_t k = 0; k < b->scenes.size() && !stale; ++k) stale = b->versions[k] != b->scenes[k]->version;
-    int st = XD_OK;
     if (stale) {
         for (size_t k = 0; k < b->scenes.size(); ++k) {
             const MixedScene* sc = b->scenes[k];
@@ -4546,9 +4583,7 @@ int mixed_batch_step(MixedBatch* b, unsigned nsteps, cudaStream_t q)
         if (st != XD_OK) return st;
     }
     for (MixedScene* sc : b->scenes) {
-        if (!sc->ready) return set_error(XD_ERR_STATE, "batch: a scene has no state uploaded");
-        st = update_mesh(sc, q);
-        if (st == XD_OK && !sc->cells_clean)
+        if (!sc->cells_clean)
             st = cuda_status(cudaMemsetAsync(sc->counters + CN_REBUILD, 1, 1, q), "batch re-binning flag");
         if (st != XD_OK) return st;
     }
