@@ -121,7 +121,7 @@ def _args():
     ap.add_argument("--chunk", type=int, default=50, help="served steps per scene per tick")
     ap.add_argument("--rates", default="", help="served: comma-separated arrival rates to sweep")
     ap.add_argument("--no-tune", action="store_true", help="batched: default tuning, no autotuner run")
-    ap.add_argument("--tune-steps", type=int, default=50, help="batched: autotuner window (steps per candidate)")
+    ap.add_argument("--tune-steps", type=int, default=200, help="batched: autotuner window (steps per candidate)")
     return ap.parse_args()
 
 

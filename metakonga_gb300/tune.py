@@ -102,7 +102,7 @@ def _time(sc, tuning, warm, steps):
         d.close()
 
 
-def tune(sc, steps: int = 200, warm: int = 20, store: bool = True, min_gain: float = 0.03) -> dict:
+def tune(sc, steps: int = 200, warm: int = 20, store: bool = True, min_gain: float = 0.05) -> dict:
     """Times the candidates on `steps` steps of the scene (after `warm`
     steps) and returns {"tuning", "ms_per_step", "default_ms_per_step",
     "candidates", "key", "seconds"}; stores the choice in the cache.  A

@@ -31,7 +31,7 @@ def test_shape_key_groups_by_octave_and_walls():
 def test_choice_needs_the_margin(monkeypatch, tmp_path):
     monkeypatch.setenv("XDEM_TUNE_CACHE", str(tmp_path / "t.json"))
     sc = scenes.settle_box(n_side=6)
-    # skin 0.2 is 2 % faster (inside the margin), 128 threads 10 % faster
+    # skin 0.2 is 2 % faster (inside the 5 % margin), 128 threads 10 % faster
     def cost(t):
         c = 1.0
         if t["skin_factor"] == 0.2:
@@ -84,4 +84,4 @@ def test_candidates_cover_skins_threads_and_pair_passes(monkeypatch, tmp_path):
     modes = {t["contact_mode"] for t in seen}
     assert skins == set(tune.SKINS) and threads == set(tune.THREADS) and modes == set(tune.MODES)
     # the choice is within the margin of the fastest candidate
-    assert out["ms_per_step"] * (1 - 0.03) <= min(c["ms_per_step"] for c in out["candidates"]) + 1e-12
+    assert out["ms_per_step"] * (1 - 0.05) <= min(c["ms_per_step"] for c in out["candidates"]) + 1e-12

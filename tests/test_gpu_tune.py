@@ -69,7 +69,7 @@ def test_autotuner_times_and_caches(cuda, monkeypatch, tmp_path):
     out = tune.tune(sc, steps=30, warm=5)
     assert out["tuning"] in [c["tuning"] for c in out["candidates"]]
     # the choice is within the tuner's margin of the fastest candidate
-    assert out["ms_per_step"] * (1.0 - 0.03) <= min(c["ms_per_step"] for c in out["candidates"]) + 1e-12
+    assert out["ms_per_step"] * (1.0 - 0.05) <= min(c["ms_per_step"] for c in out["candidates"]) + 1e-12
     assert tune.tuned(sc) == out["tuning"]
     assert (tmp_path / "tuning.json").exists()
     # the chosen setting runs the scene
