@@ -370,37 +370,20 @@ __device__ __forceinline__ void df_diff(float ah, float bh, float dlo, float& s,
     t = __fadd_rn(e, dlo);
 }
 
-// Integer <-> float conversions issue on the FP64 pipe on this part; the
-// two below are exact in integer and FP32 instructions instead.
-// The integer an integral FP32 value holds (|f| < 2^31).
-__device__ __forceinline__ int f2i_exact(float f)
-{
-    const int b = __float_as_int(f);
-    if ((b & 0x7fffffff) == 0) return 0;
-    const int e = ((b >> 23) & 0xff) - 150;   // f = m 2^e, m the 24-bit significand
-    const int m = (b & 0x7fffff) | 0x800000;
-    const int v = e >= 0 ? (m << e) : (m >> -e);
-    return b < 0 ? -v : v;
-}
-// A small integer (|r| < 2^22) as FP32: 1.5 2^23 + r is exact, and its bits
-// are those of 1.5 2^23 plus r.
-__device__ __forceinline__ float small_i2f(int r) { return __int_as_float(0x4B400000 + r) - 12582912.0f; }
-
 // Normal speed (dv . dq) / |dq| in double-float: dv = s + t per component,
 // dq the exact integer separation (|dq| < 2^31), D2 = |dq|^2 exact, D2h its
 // FP32 rounding, d0 the FP32 square root of that.  The dot product of a fast
 // tangential velocity with the contact normal cancels; here it is carried
 // with ~2^-44 relative error and rounded once.
 __device__ __forceinline__ float normal_speed(const float s[3], const float t[3], const int dq[3],
-                                              const float fq[3], float d0, long long D2, float D2h, float& q0_out,
-                                              float& q1_out, float& c_out)
+                                              float d0, long long D2, float D2h, float& q0_out, float& q1_out,
+                                              float& c_out)
 {
     float hi = 0.f, lo = 0.f;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        // dq = qh + ql exactly: qh its FP32 rounding (the caller's), ql the remainder
-        const float qh = fq[k];
-        const float ql = small_i2f(dq[k] - f2i_exact(qh));
+        const float qh = __int2float_rn(dq[k]);
+        const float ql = __int2float_rn(dq[k] - __float2int_rn(qh));
         float p, pe, ns, e1;
         two_prod(s[k], qh, p, pe);
         two_sum(hi, p, ns, e1);
@@ -470,7 +453,7 @@ __device__ __noinline__ f3 slip_pair(const float s[3], const float t[3], const i
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const float qh = __int2float_rn(dq[k]);
-        const float ql = small_i2f(dq[k] - f2i_exact(qh));
+        const float ql = __int2float_rn(dq[k] - __float2int_rn(qh));
         u[k] = df_mul(df_make(qh, ql), inv);
     }
     const dfl ri = q_to_df(qri), rj = q_to_df(qrj);
@@ -1471,8 +1454,7 @@ __device__ __forceinline__ void contact_force(const MixParams& P, const Master& 
     // rv . u = dv . u (the rotation term is perpendicular to u), in double-float
     const int dqi[3] = { (int)ddx, (int)ddy, (int)ddz };
     float rq0, rq1, rqc;
-    const float fq[3] = { fdx, fdy, fdz };
-    float rvu = normal_speed(dvs, dvt, dqi, fq, dn, D2, D2f, rq0, rq1, rqc);
+    float rvu = normal_speed(dvs, dvt, dqi, dn, D2, D2f, rq0, rq1, rqc);
     {
         // and the normal's turn (de - (u . de) u) / |d| in the normal speed
         const float cr = (fdot(dv, de) - rvu * ude) * (inv * (1.0f / kU));
