@@ -4088,15 +4088,25 @@ __global__ void __launch_bounds__(1024) k_batch_chunks(const BatchScene* __restr
 // take more; a run's result does not depend on which warp computes it.  A
 // warp loads the scene of a run into its own shared-memory slot when the
 // scene changes.
+// Shared-memory bytes of a batch contact block's WarpScene slots (rounded to
+// 16 bytes: the per-warp buffers follow).
+__host__ __device__ constexpr unsigned batch_scene_bytes(unsigned nwarps)
+{
+    return (unsigned)((nwarps * sizeof(WarpScene) + 15u) / 16u * 16u);
+}
+
 // KIND 0: the per-particle contact pass; 1: the cooperative pair pass; 2:
 // the wall pass (runs over the front of each scene's list).
 template <int KIND>
 __global__ void __launch_bounds__(kContactMaxThreads) k_batch_contact(const BatchScene* __restrict__ D, unsigned ns,
                                                                    unsigned* __restrict__ chunk_start)
 {
-    __shared__ WarpScene ws[kContactMaxThreads / 32];
-    const unsigned lane = threadIdx.x & 31u, wb = threadIdx.x / 32u;
-    WarpScene& W = ws[wb];
+    // dynamic shared memory: one WarpScene per warp of the block, then (the
+    // cooperative kinds) one CoopBuf or WallBuf per warp
+    extern __shared__ __align__(16) unsigned char batch_smem[];
+    const unsigned lane = threadIdx.x & 31u, wb = threadIdx.x / 32u, nwarps = blockDim.x / 32u;
+    WarpScene& W = reinterpret_cast<WarpScene*>(batch_smem)[wb];
+    unsigned char* const bufs = batch_smem + batch_scene_bytes(nwarps);
     const unsigned total = __ldg(chunk_start + ns);
     unsigned* next = chunk_start + ns + 1;
     unsigned cur = 0xffffffffu, lo = 0, heavy = 0, front = 0;
@@ -4126,14 +4136,13 @@ __global__ void __launch_bounds__(kContactMaxThreads) k_batch_contact(const Batc
         }
         const unsigned t = (ch - lo) * 32u + lane;
         if (KIND == 1) {
-            extern __shared__ CoopBuf coop_buf[];
             const bool valid = t < heavy;
             contact_entry_coop(W.P, W.C, valid, valid ? __ldg(W.C.hlist + list_index(t, front, W.P.n)) : 0u,
-                               coop_buf[wb]);
+                               reinterpret_cast<CoopBuf*>(bufs)[wb]);
         } else if (KIND == 2) {
-            extern __shared__ WallBuf wall_buf[];
             const bool valid = t < front;
-            walls_entry_coop(W.P, W.C, valid, valid ? __ldg(W.C.hlist + t) : 0u, wall_buf[wb]);
+            walls_entry_coop(W.P, W.C, valid, valid ? __ldg(W.C.hlist + t) : 0u,
+                             reinterpret_cast<WallBuf*>(bufs)[wb]);
         } else if (t < heavy) {
             contact_entry<false, 0>(W.P, W.C, __ldg(W.C.hlist + list_index(t, front, W.P.n)));
         }
@@ -4172,20 +4181,22 @@ struct MixedBatch {
 // The batch's contact launch: every scene's listed particles.
 static void launch_batch_pairs(const MixedBatch* b, unsigned ns, cudaStream_t q)
 {
-    const unsigned ct = b->cthreads, grid = kContactWarpsTotal * 32u / ct;
+    const unsigned ct = b->cthreads, grid = kContactWarpsTotal * 32u / ct, w = ct / 32u;
     if (b->cmode == 1)
-        k_batch_contact<1><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(b->d_scenes, ns, b->d_chunks);
+        k_batch_contact<1><<<grid, ct, batch_scene_bytes(w) + w * sizeof(CoopBuf), q>>>(b->d_scenes, ns,
+                                                                                         b->d_chunks);
     else
-        k_batch_contact<0><<<grid, ct, 0, q>>>(b->d_scenes, ns, b->d_chunks);
+        k_batch_contact<0><<<grid, ct, batch_scene_bytes(w), q>>>(b->d_scenes, ns, b->d_chunks);
 }
 
 // The wall pass after a cooperative pair pass (none otherwise: the
 // per-particle pass does its walls itself).
 static void launch_batch_walls(const MixedBatch* b, unsigned ns, cudaStream_t q)
 {
-    const unsigned ct = b->cthreads, grid = kContactWarpsTotal * 32u / ct;
+    const unsigned ct = b->cthreads, grid = kContactWarpsTotal * 32u / ct, w = ct / 32u;
     if (b->cmode == 1 && b->walls)
-        k_batch_contact<2><<<grid, ct, (ct / 32u) * sizeof(WallBuf), q>>>(b->d_scenes, ns, b->d_chunks + ns + 2);
+        k_batch_contact<2><<<grid, ct, batch_scene_bytes(w) + w * sizeof(WallBuf), q>>>(b->d_scenes, ns,
+                                                                                         b->d_chunks + ns + 2);
 }
 
 static void launch_batch_contact(const MixedBatch* b, unsigned ns, cudaStream_t q)
