@@ -2210,23 +2210,36 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
 // Here the 32 particles of a warp are done together in rounds.  Each lane
 // first scans its own particle's Verlet list (or its cells) and keeps up to
 // kCoopSlots touching partners in shared memory; then the warp's partners,
-// in lane order, are spread over the lanes, one contact per lane, each
-// forming its contact's force with contact_force; and each particle's lane
-// adds its own contacts' terms in its list order (accumulate).  The sums are
+// level by level (every lane's first, then every lane's second, ...), are
+// spread over the lanes, one contact per lane, each forming its contact's
+// force with contact_force; and each particle's lane adds its own contacts'
+// terms in its list order (accumulate).  With the contacts by level, a group
+// of 32 holds one or two of most particles, so the adding is spread over
+// the lanes instead of running on a few of them.  The sums are
 // therefore the same bits as the per-particle pass's.  A lane with more
 // than kCoopSlots contacts goes on in the next round where it stopped.
 
 constexpr unsigned kCoopSlots = 16;
 
 struct CoopBuf {
-    unsigned cand[32 * kCoopSlots];   // lane L's partners at [L * kCoopSlots, ...)
+    unsigned cand[32 * kCoopSlots];   // the wall pass: lane L's candidates at [L * kCoopSlots, ...)
     float res[10][32];                // one contact per lane: Fn, Ft, Mm, slip
+};
+
+// The pair pass's buffer: the partners k-major (lane L's k-th partner at
+// c.cand[k * 32 + L], so that the lanes' writes and a level's reads fall in
+// distinct banks), and the round's order of contacts: slot[p] the
+// partner at position p, pos[k * 32 + L] the position of lane L's k-th.
+struct PairBuf {
+    CoopBuf c;
+    unsigned short slot[32 * kCoopSlots];
+    unsigned short pos[32 * kCoopSlots];
 };
 
 // A lane whose Verlet list overflowed: its cells searched from the start,
 // the partners before `done` skipped, up to kCoopSlots after them kept in
-// mine[]; returns whether more are left.  Out of line: rare, and the pass's
-// loop stays short.
+// mine[0], mine[32], ...; returns whether more are left.  Out of line:
+// rare, and the pass's loop stays short.
 __device__ __noinline__ bool coop_cells(const MixParams& P, const ContactArgs& C, unsigned i, float4 pi,
                                         longlong2 qai, longlong2 qbi, unsigned& done, unsigned* mine,
                                         unsigned& cnt)
@@ -2234,7 +2247,8 @@ __device__ __noinline__ bool coop_cells(const MixParams& P, const ContactArgs& C
     unsigned seen = 0;
     for_each_contact<true>(P, C.M, i, pi, qai, qbi, __ldg(C.keys + i), C.pf, C.qa, C.qb, C.lb, C.counters,
                            [&](unsigned j, bool guard) {
-                               if (seen >= done && cnt < kCoopSlots) mine[cnt++] = j | (guard ? kGuardBit : 0u);
+                               if (seen >= done && cnt < kCoopSlots)
+                                   mine[32u * cnt++] = j | (guard ? kGuardBit : 0u);
                                ++seen;
                            });
     done += cnt;
@@ -2263,8 +2277,9 @@ __device__ __forceinline__ Own load_own(const MixParams& P, const ContactArgs& C
 // history, every lane of the warp taking part: pairs cooperatively, then
 // each particle's planes and triangles (walls_fp32) by its own lane.
 __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const ContactArgs& C, bool valid, unsigned i,
-                                                   CoopBuf& B)
+                                                   PairBuf& PB)
 {
+    CoopBuf& B = PB.c;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned n = P.n;
     float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -2285,7 +2300,8 @@ __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const Con
     HistState hs;
     unsigned kpos = 0, done = 0;
     bool more = valid;
-    unsigned* mine = B.cand + lane * kCoopSlots;
+    unsigned* mine = B.cand + lane;
+    const unsigned lt = (1u << lane) - 1u;
     while (__any_sync(0xffffffffu, more)) {
         // this lane's next partners, in its search order
         unsigned cnt = 0;
@@ -2316,7 +2332,7 @@ __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const Con
                         const float Rt = rt0 + pp[q].w;
                         if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) >= Rt * Rt) continue;
                         const int c = exact_touch_q<true>(P, C.M, i, jj[q], qai, qbi, aa[q], bb[q], C.counters);
-                        if (c) mine[cnt++] = jj[q] | (c == 2 ? kGuardBit : 0u);
+                        if (c) mine[32u * cnt++] = jj[q] | (c == 2 ? kGuardBit : 0u);
                     }
                 }
                 more = kpos < vc;
@@ -2325,28 +2341,28 @@ __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const Con
             }
         }
         __syncwarp();
-        // the round's contacts in lane order: lane L owns [off, off + cnt)
-        unsigned incl = cnt;
-#pragma unroll
-        for (unsigned o = 1; o < 32u; o <<= 1) {
-            const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
+        // the round's contacts by level: every lane's first partner (in lane
+        // order), then every lane's second, ...; a group of 32 positions then
+        // holds few contacts of any one particle
+        const unsigned maxc = __reduce_max_sync(0xffffffffu, cnt);
+        unsigned total = 0;
+        for (unsigned k = 0; k < maxc; ++k) {
+            const unsigned b = __ballot_sync(0xffffffffu, cnt > k);
+            if (cnt > k) {
+                const unsigned p = total + __popc(b & lt);
+                PB.slot[p] = (unsigned short)(k * 32u + lane);
+                PB.pos[k * 32u + lane] = (unsigned short)p;
+            }
+            total += __popc(b);
         }
-        const unsigned off = incl - cnt;
-        const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();
+        unsigned kacc = 0;   // this lane's partners added so far this round
         for (unsigned base = 0; base < total; base += 32u) {
             const unsigned c = base + lane;
-            // the owner of contact c: the last lane whose range starts at or before c
-            unsigned L = 0;
-#pragma unroll
-            for (unsigned b = 16; b; b >>= 1) {
-                const unsigned o = __shfl_sync(0xffffffffu, off, L + b);
-                if (o <= c) L += b;
-            }
-            const unsigned offL = __shfl_sync(0xffffffffu, off, L);
-            const unsigned iL = __shfl_sync(0xffffffffu, i, L);
+            const unsigned sc = c < total ? PB.slot[c] : 0u;
+            const unsigned iL = __shfl_sync(0xffffffffu, i, sc & 31u);
             if (c < total) {
-                const unsigned e = B.cand[L * kCoopSlots + (c - offL)];
+                const unsigned e = B.cand[sc];
                 const Own I = load_own(P, C, iL);
                 PairOut o;
                 contact_force<0, true>(P, C.M, I, e & ~kGuardBit, (e & kGuardBit) != 0u, C.mass0, C.pf, C.qa,
@@ -2365,9 +2381,11 @@ __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const Con
                 }
             }
             __syncwarp();
-            const unsigned q1 = min(off + cnt, base + 32u);
-            for (unsigned q = max(off, base); q < q1; ++q) {
-                const unsigned k = q - base;
+            // this lane's contacts in the group, in its list order
+            for (; kacc < cnt; ++kacc) {
+                const unsigned p = PB.pos[kacc * 32u + lane];
+                if (p >= base + 32u) break;
+                const unsigned k = p - base;
                 PairOut o;
                 o.Fn = fk(B.res[0][k], B.res[1][k], B.res[2][k]);
                 o.slip = B.res[9][k] != 0.f;
@@ -2512,7 +2530,7 @@ __global__ void __launch_bounds__(kContactMaxThreads) k_mx_walls(MixParams P, Co
 }
 
 // COOP: the warp-cooperative pair pass (no history, no recording; dynamic
-// shared memory of one CoopBuf per warp).
+// shared memory of one PairBuf per warp).
 template <bool RECORD, int HIST, bool COOP>
 __global__ void __launch_bounds__(kContactMaxThreads) k_mx_contact(MixParams P, ContactArgs C)
 {
@@ -2523,8 +2541,8 @@ __global__ void __launch_bounds__(kContactMaxThreads) k_mx_contact(MixParams P, 
     const unsigned warps = gridDim.x * (blockDim.x / 32u);
     const unsigned gw = blockIdx.x * (blockDim.x / 32u) + threadIdx.x / 32u;
     if (COOP) {
-        extern __shared__ CoopBuf coop_buf[];
-        CoopBuf& B = coop_buf[threadIdx.x / 32u];
+        extern __shared__ PairBuf pair_buf[];
+        PairBuf& B = pair_buf[threadIdx.x / 32u];
         for (unsigned t0 = gw * 32u; t0 < total; t0 += warps * 32u) {
             const unsigned t = t0 + (threadIdx.x & 31u);
             const bool valid = t < total;
@@ -3493,7 +3511,7 @@ static int step_once(MixedScene* s, cudaStream_t q, const Phases& ph, bool recor
         if (hist == 2) XD_MX_CONTACT(false, 2);
         else if (hist == 1) XD_MX_CONTACT(false, 1);
         else if (s->cmode == 1) {
-            k_mx_contact<false, 0, true><<<grid, ct, (ct / 32u) * sizeof(CoopBuf), q>>>(s->P, C);
+            k_mx_contact<false, 0, true><<<grid, ct, (ct / 32u) * sizeof(PairBuf), q>>>(s->P, C);
             if (s->P.nplanes || s->P.ntri) k_mx_walls<<<grid, ct, (ct / 32u) * sizeof(WallBuf), q>>>(s->P, C);
         } else XD_MX_CONTACT(false, 0);
     }
@@ -4102,7 +4120,7 @@ __global__ void __launch_bounds__(kContactMaxThreads) k_batch_contact(const Batc
                                                                    unsigned* __restrict__ chunk_start)
 {
     // dynamic shared memory: one WarpScene per warp of the block, then (the
-    // cooperative kinds) one CoopBuf or WallBuf per warp
+    // cooperative kinds) one PairBuf or WallBuf per warp
     extern __shared__ __align__(16) unsigned char batch_smem[];
     const unsigned lane = threadIdx.x & 31u, wb = threadIdx.x / 32u, nwarps = blockDim.x / 32u;
     WarpScene& W = reinterpret_cast<WarpScene*>(batch_smem)[wb];
@@ -4138,7 +4156,7 @@ __global__ void __launch_bounds__(kContactMaxThreads) k_batch_contact(const Batc
         if (KIND == 1) {
             const bool valid = t < heavy;
             contact_entry_coop(W.P, W.C, valid, valid ? __ldg(W.C.hlist + list_index(t, front, W.P.n)) : 0u,
-                               reinterpret_cast<CoopBuf*>(bufs)[wb]);
+                               reinterpret_cast<PairBuf*>(bufs)[wb]);
         } else if (KIND == 2) {
             const bool valid = t < front;
             walls_entry_coop(W.P, W.C, valid, valid ? __ldg(W.C.hlist + t) : 0u,
@@ -4183,7 +4201,7 @@ static void launch_batch_pairs(const MixedBatch* b, unsigned ns, cudaStream_t q)
 {
     const unsigned ct = b->cthreads, grid = kContactWarpsTotal * 32u / ct, w = ct / 32u;
     if (b->cmode == 1)
-        k_batch_contact<1><<<grid, ct, batch_scene_bytes(w) + w * sizeof(CoopBuf), q>>>(b->d_scenes, ns,
+        k_batch_contact<1><<<grid, ct, batch_scene_bytes(w) + w * sizeof(PairBuf), q>>>(b->d_scenes, ns,
                                                                                          b->d_chunks);
     else
         k_batch_contact<0><<<grid, ct, batch_scene_bytes(w), q>>>(b->d_scenes, ns, b->d_chunks);
