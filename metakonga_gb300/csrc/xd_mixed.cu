@@ -2222,19 +2222,41 @@ __device__ __forceinline__ void contact_entry(const MixParams& P, const ContactA
 constexpr unsigned kCoopSlots = 16;
 
 struct CoopBuf {
-    unsigned cand[32 * kCoopSlots];   // the wall pass: lane L's candidates at [L * kCoopSlots, ...)
+    unsigned cand[32 * kCoopSlots];   // k-major: lane L's k-th candidate at [k * 32 + L]
     float res[10][32];                // one contact per lane: Fn, Ft, Mm, slip
 };
 
-// The pair pass's buffer: the partners k-major (lane L's k-th partner at
-// c.cand[k * 32 + L], so that the lanes' writes and a level's reads fall in
-// distinct banks), and the round's order of contacts: slot[p] the
-// partner at position p, pos[k * 32 + L] the position of lane L's k-th.
+// A cooperative pass's buffer: the candidates k-major (so that the lanes'
+// writes and a level's reads fall in distinct banks), and the round's order
+// of contacts: slot[p] the candidate at position p, pos[k * 32 + L] the
+// position of lane L's k-th.
 struct PairBuf {
     CoopBuf c;
     unsigned short slot[32 * kCoopSlots];
     unsigned short pos[32 * kCoopSlots];
 };
+
+// Orders a round's candidates (cnt of this lane's) by level: every lane's
+// first in lane order, then every lane's second, ...  A group of 32
+// positions then holds one or two candidates of most particles, and each
+// lane's own stay in its order.  Returns the round's count.
+__device__ __forceinline__ unsigned level_order(PairBuf& PB, unsigned cnt, unsigned lane)
+{
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned maxc = __reduce_max_sync(0xffffffffu, cnt);
+    unsigned total = 0;
+    for (unsigned k = 0; k < maxc; ++k) {
+        const unsigned b = __ballot_sync(0xffffffffu, cnt > k);
+        if (cnt > k) {
+            const unsigned p = total + __popc(b & lt);
+            PB.slot[p] = (unsigned short)(k * 32u + lane);
+            PB.pos[k * 32u + lane] = (unsigned short)p;
+        }
+        total += __popc(b);
+    }
+    __syncwarp();
+    return total;
+}
 
 // A lane whose Verlet list overflowed: its cells searched from the start,
 // the partners before `done` skipped, up to kCoopSlots after them kept in
@@ -2301,7 +2323,6 @@ __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const Con
     unsigned kpos = 0, done = 0;
     bool more = valid;
     unsigned* mine = B.cand + lane;
-    const unsigned lt = (1u << lane) - 1u;
     while (__any_sync(0xffffffffu, more)) {
         // this lane's next partners, in its search order
         unsigned cnt = 0;
@@ -2341,21 +2362,7 @@ __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const Con
             }
         }
         __syncwarp();
-        // the round's contacts by level: every lane's first partner (in lane
-        // order), then every lane's second, ...; a group of 32 positions then
-        // holds few contacts of any one particle
-        const unsigned maxc = __reduce_max_sync(0xffffffffu, cnt);
-        unsigned total = 0;
-        for (unsigned k = 0; k < maxc; ++k) {
-            const unsigned b = __ballot_sync(0xffffffffu, cnt > k);
-            if (cnt > k) {
-                const unsigned p = total + __popc(b & lt);
-                PB.slot[p] = (unsigned short)(k * 32u + lane);
-                PB.pos[k * 32u + lane] = (unsigned short)p;
-            }
-            total += __popc(b);
-        }
-        __syncwarp();
+        const unsigned total = level_order(PB, cnt, lane);
         unsigned kacc = 0;   // this lane's partners added so far this round
         for (unsigned base = 0; base < total; base += 32u) {
             const unsigned c = base + lane;
@@ -2415,14 +2422,14 @@ __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const Con
 // The wall pass's shared memory per warp: the candidate buffer, and each
 // lane's particle data read once by its own lane for all its candidates.
 struct WallBuf {
-    CoopBuf c;
+    PairBuf c;
     WallOwn own[32];
 };
 
 __device__ __forceinline__ void walls_entry_coop(const MixParams& P, const ContactArgs& C, bool valid, unsigned i,
                                                  WallBuf& WB)
 {
-    CoopBuf& B = WB.c;
+    CoopBuf& B = WB.c.c;
     const unsigned lane = threadIdx.x & 31u;
     const unsigned n = P.n;
     unsigned wm = 0, kb = 0, ke = 0;
@@ -2450,34 +2457,23 @@ __device__ __forceinline__ void walls_entry_coop(const MixParams& P, const Conta
     f3 f = fk(0.f, 0.f, 0.f), Ftri = fk(0.f, 0.f, 0.f);
     RxnAcc ra;
     ra.b = 0xffffffffu;
-    unsigned* mine = B.cand + lane * kCoopSlots;
+    unsigned* mine = B.cand + lane;
     bool more = any;
     while (__any_sync(0xffffffffu, more)) {
         unsigned cnt = 0;
-        for (; more && wm && cnt < kCoopSlots; wm &= wm - 1u) mine[cnt++] = kWallPlane | (unsigned)(__ffs(wm) - 1);
+        for (; more && wm && cnt < kCoopSlots; wm &= wm - 1u)
+            mine[32u * cnt++] = kWallPlane | (unsigned)(__ffs(wm) - 1);
         for (; more && kb < ke && cnt < kCoopSlots; ++kb)
-            mine[cnt++] = listed ? __ldg(C.tlist + (size_t)kb * n + i) : __ldg(C.tpt + kb);
+            mine[32u * cnt++] = listed ? __ldg(C.tlist + (size_t)kb * n + i) : __ldg(C.tpt + kb);
         more = more && (wm || kb < ke);
         __syncwarp();
-        unsigned incl = cnt;
-#pragma unroll
-        for (unsigned o = 1; o < 32u; o <<= 1) {
-            const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        const unsigned off = incl - cnt;
-        const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+        const unsigned total = level_order(WB.c, cnt, lane);
+        unsigned kacc = 0;
         for (unsigned base = 0; base < total; base += 32u) {
             const unsigned c = base + lane;
-            unsigned L = 0;
-#pragma unroll
-            for (unsigned b = 16; b; b >>= 1) {
-                const unsigned o = __shfl_sync(0xffffffffu, off, L + b);
-                if (o <= c) L += b;
-            }
-            const unsigned offL = __shfl_sync(0xffffffffu, off, L);
             if (c < total) {
-                const WallRes r = wall_eval(P, C, WB.own[L], B.cand[L * kCoopSlots + (c - offL)]);
+                const unsigned sc = WB.c.slot[c];
+                const WallRes r = wall_eval(P, C, WB.own[sc & 31u], B.cand[sc]);
                 B.res[0][lane] = r.o.Fn.x;
                 B.res[1][lane] = r.o.Fn.y;
                 B.res[2][lane] = r.o.Fn.z;
@@ -2490,9 +2486,10 @@ __device__ __forceinline__ void walls_entry_coop(const MixParams& P, const Conta
                 B.res[9][lane] = __uint_as_float(r.kind | (r.kind && r.o.slip ? 4u : 0u) | (r.b << 3));
             }
             __syncwarp();
-            const unsigned q1 = min(off + cnt, base + 32u);
-            for (unsigned q = max(off, base); q < q1; ++q) {
-                const unsigned k = q - base;
+            for (; kacc < cnt; ++kacc) {
+                const unsigned p = WB.c.pos[kacc * 32u + lane];
+                if (p >= base + 32u) break;
+                const unsigned k = p - base;
                 const unsigned code = __float_as_uint(B.res[9][k]);
                 WallRes r;
                 r.kind = code & 3u;
@@ -4480,6 +4477,19 @@ int mixed_batch_create(MixedScene* const* scenes, unsigned count, MixedBatch** o
         if (sc->kinematic) return set_error(XD_ERR_STATE, "batch: scene %u has kinematic bodies", k);
         for (unsigned j = 0; j < k; ++j)
             if (scenes[j] == sc) return set_error(XD_ERR_INVALID, "batch: scene %u given twice", k);
+    }
+    // the cooperative kinds' shared memory at the largest block: the wall
+    // pass's is above the 48 KB a launch may take without asking
+    {
+        const unsigned w = kContactMaxThreads / 32u;
+        int st = cuda_status(cudaFuncSetAttribute(k_batch_contact<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)(batch_scene_bytes(w) + w * sizeof(PairBuf))),
+                             "batch pair pass shared memory");
+        if (st == XD_OK)
+            st = cuda_status(cudaFuncSetAttribute(k_batch_contact<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)(batch_scene_bytes(w) + w * sizeof(WallBuf))),
+                             "batch wall pass shared memory");
+        if (st != XD_OK) return st;
     }
     MixedBatch* b = new (std::nothrow) MixedBatch();
     if (!b) return set_error(XD_ERR_NOMEM, "batch: host allocation");
