@@ -607,12 +607,13 @@ def _torch_setup():
     return world, rank, local, barrier
 
 
-def _max_over_ranks(x, world):
+def _max_over_ranks(x, world, device="cuda"):
+    """The largest of the ranks' x (a time): the job ends with its slowest rank."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    t = torch.tensor([x], device=device, dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
