@@ -1,6 +1,7 @@
-"""Known answers worked by hand for the oracle's contact laws (no GPU): two
-equal spheres of the 8,000-sphere settle's material meeting head on, and one
-sphere against one triangle in its face, edge and vertex regions.
+"""Known answers worked by hand for the oracle (no GPU): two equal spheres of
+the 8,000-sphere settle's material meeting head on, one sphere against one
+triangle in its face, edge and vertex regions, and the grid hash on cell
+faces, below the grid's origin and beyond its end.
 
 getConstant with TCM = 1 (mphysics_cuda_impl.cuh:238-246): Eeq = Ei Ej /
 (Ei (1 - nuj^2) + Ej (1 - nui^2)), kn = 4/3 Eeq sqrt(Req), beta = pi / ln e,
@@ -84,3 +85,26 @@ def test_sphere_on_a_triangle_face_edge_and_vertex(oracle):
         np.testing.assert_allclose(force[i], (0.0, 0.0, fz), rtol=1e-9, atol=1e-9 * fz)
     assert np.all(moment == 0.0)
     np.testing.assert_allclose(pmi["force"][0], (0.0, 0.0, -n * fz), rtol=1e-9, atol=1e-9 * fz)
+
+
+def test_grid_hash_on_cell_faces_below_and_beyond_the_grid(oracle):
+    """calcGridPos / calcGridHash (impl:65-83): c = floor((p - wo) / cs),
+    hash = (cz & (gz-1)) gy gx + (cy & (gy-1)) gx + (cx & (gx-1)).  Cells of
+    0.25 m from wo = -1 m on a 128^3 grid: a coordinate on a cell face falls
+    in the cell above it, one below the origin wraps to cell 127, and one
+    128 cells up wraps to cell 0."""
+    g = 128
+    prm = make_params(np_=5, ncell=g ** 3, grid=(g, g, g), dt=1e-5, cell_size=0.25,
+                      world_origin=(-1, -1, -1), gravity=(0, 0, -9.81))
+    pos = np.array([[-1.0, -1.0, -1.0, 0.01],      # the origin: cell (0, 0, 0)
+                    [-0.75, -0.5, 0.0, 0.01],      # faces: cells (1, 2, 4)
+                    [-1.25, -1.0, -1.0, 0.01],     # below the origin: cx = -1 -> 127
+                    [31.0, -0.875, -1.0, 0.01],    # 128 cells up: cx = 128 -> 0; cy = 0
+                    [-1.0, -1.0, -1.0 - 1e-12, 0.01]])   # just below a face: cz = -1 -> 127
+    cells = [(0, 0, 0), (1, 2, 4), (127, 0, 0), (0, 0, 0), (0, 0, 127)]
+    want = np.array([cz * g * g + cy * g + cx for cx, cy, cz in cells], dtype=np.uint32)
+    h = np.zeros(5, np.uint32)
+    ix = np.zeros(5, np.uint32)
+    oracle.hash_and_index(prm, pos, h, ix)
+    assert np.array_equal(h, want)
+    assert np.array_equal(ix, np.arange(5, dtype=np.uint32))
