@@ -2365,6 +2365,7 @@ __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const Con
         const unsigned total = level_order(PB, cnt, lane);
         unsigned kacc = 0;   // this lane's partners added so far this round
         for (unsigned base = 0; base < total; base += 32u) {
+            // position c: the partner in slot sc, of lane sc % 32's particle
             const unsigned c = base + lane;
             const unsigned sc = c < total ? PB.slot[c] : 0u;
             const unsigned iL = __shfl_sync(0xffffffffu, i, sc & 31u);
@@ -2414,7 +2415,8 @@ __device__ __forceinline__ void contact_entry_coop(const MixParams& P, const Con
 // The wall pass after the cooperative pair pass, warp-cooperative as well:
 // the listed particles with walls in reach (the front of the list) list
 // their wall candidates (planes in reach, then their triangles) into the
-// warp's buffer, the candidates are spread one per lane (wall_eval), and
+// warp's buffer, the candidates are spread one per lane in level order
+// (level_order, wall_eval), and
 // each particle's lane adds its results in candidate order (wall_add) and
 // then its wall force to its pair force -- the additions the per-particle
 // pass makes after its pairs (F += walls).  A launch of its own: the wall
