@@ -135,15 +135,31 @@ def _ref():
     return RefKernels()
 
 
-@pytest.mark.parametrize("case", ["packed", "drum", "wrapped"])
+@pytest.mark.parametrize("case", ["packed", "drum", "wrapped", "cohesion", "no_rolling", "polydisperse"])
 def test_oracle_matches_reference_kernels(oracle, case):
     """Pin: the restatement equals the reference's own kernels (host build)
-    on fresh seeded inputs, step by step."""
+    on fresh seeded inputs, step by step: packed overlaps with the box's
+    planes, triangle contacts in a drum, the grid's wrap, cohesion
+    (cohesionForce, impl:259-279), the relative velocity without rolling
+    (impl:455-457), and radii of a spread (getConstant's Req and Meq)."""
     ref = _ref()
     if case == "packed":
         sc = packed_scene(n_side=9)
     elif case == "drum":
         sc = small_drum(n=300)
+    elif case == "cohesion":
+        sc = packed_scene(n_side=7)        # the planes keep their property without cohesion
+        sc.cp_pp["coh"] = 1e5
+    elif case == "no_rolling":
+        sc = packed_scene(n_side=7)
+        sc.params["rolling"] = 0
+    elif case == "polydisperse":
+        sc = packed_scene(n_side=8)
+        rng = np.random.Generator(np.random.MT19937(17))
+        sc.pos[:, 3] = rng.uniform(0.0048, 0.0062, sc.np_)
+        sc.mass[:], sc.inertia[:] = scenes.mass_inertia(sc.pos[:, 3])
+        sc.force[:] = sc.mass[:, None] * np.array(scenes.GRAVITY)
+        sc.params["cell_size"] = 2.0 * sc.pos[:, 3].max()
     else:
         sc = packed_scene(n_side=7)
         sc.pos[:, :3] += np.array([1.7, -1.3, 0.9])      # beyond 128 cells: exercises the wrap
