@@ -177,6 +177,25 @@ def test_oracle_matches_reference_kernels(oracle, case):
         assert struct_equal(a.pmi, b.pmi)
 
 
+def test_oracle_cube_matches_reference(oracle):
+    """Pin: cu_cube_contact_force (six plane launches, mphysics_cuda_def.cu:158-179)
+    against the reference's kernels on a packed lattice whose outer spheres
+    overlap the walls: the same bits."""
+    ref = _ref()
+    sc = packed_scene(n_side=8)
+    p = sc.params.copy()
+    p["np"] = sc.np_
+    assert sc.planes.shape[0] == 6
+    planes6 = np.ascontiguousarray(sc.planes)
+    out = []
+    for fn in (oracle.cube, ref.cube):
+        f, m = sc.force.copy(), sc.moment.copy()
+        fn(p, planes6, sc.pos, sc.vel, sc.omega, f, m, sc.mass, sc.cp_pp)
+        out.append((f, m))
+    assert np.abs(out[0][0] - sc.force).max() > 1e-3, "no wall contacts"
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
 def test_oracle_update_polygon_matches_reference(oracle):
     ref = _ref()
     sc = small_drum(n=20)
